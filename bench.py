@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""bench.py -- particle-steps/s of the Stress-Particle SPH step on GB300.
+
+Workload (the configuration the headline metric is quoted on): a 10 m vertical slope
+(block 4.4 m x 10 m) on a 20 m x 5 m foundation, spacing 1.2 cm -> about 1.00M velocity
+particles + 1.00M stress-points, Drucker-Prager soil (rho 1850, E 20 MPa, nu 0.3,
+phi 30 deg, c 10 kPa), K0 stress, gravity ramped in over 0.05 s, dt = 0.1 h / sqrt(E/rho).
+A "step" is one call of the reference's time_integration (neighbour search + RK4 +
+position update) over the whole particle set.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value  = (N_v + N_s) * K * ranks / max-over-ranks device time of K graph-launched steps
+         (CUDA events on the context's own stream; state resident in HBM, working set
+         larger than L2).
+e2e    = the same metric through the C-ABI with host buffers: every step uploads the
+         state from pinned host memory (sps_upload), advances one step (sps_step) and
+         downloads the fields (sps_download).
+--impl reference times the CPU restatement of the reference's step (the oracle; the
+         Fortran reference cannot be compiled on either machine) on a bounded sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "stress-particle-sph_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-steps/s at 1M particles: FP64 plain vs FP32+surrogate at stated error"
+SLOPE = dict(Lf=20.0, Hf=5.0, Ls=4.4, Hs=10.0, young=20e6, poiss=0.3, rho=1850.0, phi_deg=30.0,
+             cohesion=10e3, k0=0.5, t_ramp=0.05)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="plain", choices=["plain"])
+    ap.add_argument("--dx", type=float, default=0.012)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist.get_rank(), dist.get_world_size(), dist
+
+
+def reduce_max(dist, v, device=None):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = max(smax, float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp64_peak_tflops():
+    """FP64 throughput of cuBLAS DGEMM on this GPU (the FP64 pipe's practical ceiling)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for _ in range(3):
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def workload(dx):
+    import sps_gb300
+    return sps_gb300.Problem.slope(dx=dx, **SLOPE)
+
+
+def workload_name(prob, dx):
+    return ("vertical slope 10 m (block 4.4 x 10 m) on a 20 x 5 m foundation, dx %.4g m, "
+            "%d velocity + %d stress particles + %d wall dummies" % (dx, prob.nnode, prob.nstress,
+                                                                     prob.ntotal2 - prob.ntotal))
+
+
+# algorithmic bytes per target entry / particle for the roofline of each kernel class
+# (FP64 plain layout): a neighbour entry is 16 B; per-particle state is counted once.
+def kernel_bytes(name, prob, deg):
+    nn, ns, n2 = prob.nnode, prob.nstress, prob.ntotal2
+    ent = 16.0
+    if name == "derivs":
+        # entries + SP (v,s,m,rho,grad_u w, RHS1 w, RKs rw, fdp rw, RKd rw) + node terms
+        return ent * deg["cross"] + ns * (16 + 32 + 16 + 32 + 32 + 64 + 16 + 16) + \
+            nn * (16 + 32 + 16 + 16 + 32 + 16) + ent * deg["same_nodes"]
+    if name == "interp":
+        return ent * deg["cross"] + ns * (16 + 16) + nn * (40 + 16 + 16)
+    if name == "half":
+        return n2 * (4 * 8 + 8) + ent * deg["pairs"]
+    if name == "lists":
+        return ent * (deg["cross"] + deg["same"]) * 1.5
+    return None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import sps_gb300
+    from sps_gb300 import _abi
+
+    rank, world, dist = dist_init("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sps_gb300.build_all()
+    prob = workload(args.dx)
+    prec = _abi.SPS_PREC_FP64_PLAIN
+    params = prob.params_copy(precision=prec)
+    ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", params)
+    ctx.upload_problem(prob)
+    nparticles = prob.nnode + prob.nstress
+    t = 0.0
+    t = ctx.step(max(args.warmup, 1), t)  # warm-up (also instantiates the step graph)
+    kps = sps_gb300.kernels_per_step(ctx)
+    stream = torch.cuda.ExternalStream(sps_gb300.stream_of(ctx))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0.record(stream)
+    t = ctx.step(args.steps, t)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms = e0.elapsed_time(e1)
+    ms_max = reduce_max(dist, ms, device="cuda")
+    value = nparticles * args.steps * world / (ms_max * 1e-3)
+
+    # per-kernel profile of two steps (events around every kernel, no graph)
+    t, prof = sps_gb300.profile_steps(ctx, 2, t)
+    # neighbour-list statistics for the algorithmic byte counts
+    pairs = ctx.dump_pairs()
+    pt = np.bincount(pairs["pint_type"], minlength=10)
+    deg = {"cross": 2 * (pt[1]) + pt[6] + pt[9], "same": 2 * (pt[2] + pt[3]),
+           "same_nodes": 2 * pt[3], "pairs": len(pairs["pair_i"])}
+    top = max((k for k in prof if k not in ("end",)), key=lambda k: prof[k][0])
+    top_ms, top_n = prof[top]
+    per_launch_ms = top_ms / top_n
+    peaks, peak_kind = measured_peaks()
+    b = kernel_bytes(top, prob, deg)
+    roof = None
+    if b is not None:
+        ach = b / (per_launch_ms * 1e-3) / 1e9
+        roof = {"kernel": "k_" + top, "bound": "hbm", "achieved": round(ach, 1),
+                "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": round(ach / peaks.get("hbm_gbs"), 4), "traffic": None,
+                "peak_kind": peak_kind, "per_launch_ms": round(per_launch_ms, 4),
+                "launches_per_step": top_n / 2,
+                "share_of_step": round(top_ms / sum(v[0] for v in prof.values()), 3)}
+    try:
+        f64 = fp64_peak_tflops()
+    except Exception:
+        f64 = None
+
+    # end to end through the C-ABI with pinned host buffers
+    st = prob.state()
+    pinned = {}
+    for k, v in st.items():
+        tt = torch.empty(v.size, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
+                         pin_memory=True)
+        a = tt.numpy()
+        a[:] = v
+        pinned[k] = (tt, a)
+    h2d = sum(a.nbytes for _, a in pinned.values())
+    down = ctx.download()
+    d2h = sum(v.nbytes for v in down.values())
+    ctx.upload(**{k: a for k, (_, a) in pinned.items()})
+    torch.cuda.synchronize()
+    barrier(dist)
+    w0 = time.perf_counter()
+    te = 0.0
+    for _ in range(args.e2e_steps):
+        ctx.upload(**{k: a for k, (_, a) in pinned.items()})
+        te = ctx.step(1, te)
+        down = ctx.download()
+    w1 = time.perf_counter()
+    e2e_s = reduce_max(dist, w1 - w0, device="cuda")
+    e2e = {"value": round(nparticles * args.e2e_steps * world / e2e_s, 1),
+           "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (generated slope geometry, no dataset)",
+            "config": {"workload": workload_name(prob, args.dx), "precision": "fp64_plain",
+                       "particles": nparticles, "pairs": deg["pairs"],
+                       "l2": "state and pair tables (%.1f GB) larger than L2; no flush" % (
+                           (prob.ntotal2 * (3 * 48 * 16 + 400)) / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
+            "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
+            "kernel_ms_per_step": {k: round(v[0] / 2, 4) for k, v in sorted(
+                prof.items(), key=lambda kv: -kv[1][0])},
+            "cpu_baseline": cpu, "clocks": clk,
+        }
+        print(json.dumps(line))
+
+
+def cpu_sample(seconds_target=20.0):
+    """The oracle (single-threaded restatement of the reference step) on a coarser slope of
+    the same geometry and material, timed for a bounded number of steps."""
+    import orc
+    import sps_gb300
+    dx = 0.06
+    prob = sps_gb300.Problem.slope(dx=dx, **SLOPE)
+    ctx = orc.context(prob.params_copy())
+    ctx.upload_problem(prob)
+    t = ctx.step(1, 0.0)
+    steps, el = 0, 0.0
+    while el < seconds_target and steps < 200:
+        w0 = time.perf_counter()
+        t = ctx.step(1, t)
+        el += time.perf_counter() - w0
+        steps += 1
+    n = prob.nnode + prob.nstress
+    return n * steps / el, "oracle (C restatement, 1 thread) on the same slope at dx %.3g m: " \
+        "%d velocity + %d stress particles, %d steps in %.1f s" % (dx, prob.nnode, prob.nstress,
+                                                                   steps, el), steps
+
+
+def cpu_baseline(args):
+    v, sample, _ = cpu_sample()
+    return {"value": round(v, 1), "unit": "particle-steps/s", "cores": 1, "kind": "port",
+            "sample": sample}
+
+
+def run_reference(args):
+    rank, world, dist = dist_init("gloo")
+    if rank != 0:
+        return
+    import orc
+    orc.build()
+    import sps_gb300
+    sps_gb300.build_host()
+    per_step = max(2.0, 60.0 / max(args.steps + args.warmup, 1))
+    v, sample, steps = cpu_sample(seconds_target=per_step * args.steps)
+    line = {
+        "metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world,
+        "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": "vertical slope (same geometry and material), coarser sample",
+                   "precision": "fp64 (reference mixed precision)"},
+        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": 1,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(v, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/*
+ * sps.h -- C-ABI of the GB300 stress-particle SPH step library (libsps_gb300.so).
+ *
+ * The reference (CaitlinChalk/Stress-Particle-SPH, Fortran 90) advances one time
+ * step with `time_integration` (code/2_SPH_main_2018.f90:78, public at :22), called
+ * once per step by the driver (code/1_SPH_2018.f90:82).  All state lives in module
+ * globals (code/5_SPH_global_vars_2018.f90, code/6_SPH_time_vars_2018.f90,
+ * code/4_SPH_material_vars_2018.f90).  This header is the drop-in seam for that call:
+ * the caller keeps its arrays, copies them in once (`sps_upload`), replaces every
+ * `call time_integration` + `time_sph = time_sph + dt_sph` pair with `sps_step`, and
+ * copies fields back (`sps_download`) before it writes output.
+ *
+ * Conventions
+ *   - plain C types only: int32 counts, double / float / int32 arrays;
+ *   - arrays use the reference's Fortran layout: x(2,N) is interleaved (x1,y1,x2,y2,..),
+ *     stress(4,N) is (sxx,syy,sxy,szz) per particle, bc_info(8,N) column-major;
+ *   - particle order is the reference's: nodes 1..nnode, stress-points
+ *     nnode+1..ntotal, dummy wall particles ntotal+1..ntotal2 (0-based here);
+ *   - every function returns an int status: SPS_OK (0) or a negative SPS_ERR_*;
+ *     no C++ exception crosses the boundary; the message of the last failure on a
+ *     context is available from sps_last_error;
+ *   - a context owns one CUDA stream and its device buffers; it is used from one
+ *     host thread at a time and is not re-entrant.
+ */
+#ifndef SPS_GB300_H
+#define SPS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPS_OK 0
+#define SPS_ERR_ARG (-1)         /* bad argument / inconsistent sizes              */
+#define SPS_ERR_UNSUPPORTED (-2) /* option outside the implemented hot path        */
+#define SPS_ERR_CUDA (-3)        /* CUDA runtime failure (no device, launch error) */
+#define SPS_ERR_CAPACITY (-4)    /* neighbour / pair capacity exceeded             */
+#define SPS_ERR_NONFINITE (-5)   /* NaN/Inf found in the state after a step        */
+#define SPS_ERR_STATE (-6)       /* call out of order (e.g. step before upload)    */
+
+/* arithmetic of the step */
+#define SPS_PREC_FP64_PLAIN 0 /* FP64 with the reference's FP32 roundings (oracle-exact) */
+#define SPS_PREC_FP32_FAST 1  /* FP32 pair arithmetic, compensated neighbour sums       */
+
+/*
+ * Problem description: the module variables that `time_integration` reads but never
+ * writes.  Field names follow the reference's variable names.  Pointers are only read
+ * during sps_create (the context keeps its own copies).
+ */
+typedef struct sps_params {
+  /* counts (code/3_SPH_material_2018.f90 Read_2DMesh / set_up_dummy_nodes) */
+  int32_t nnode;   /* velocity particles ("nodes")                            */
+  int32_t nstress; /* stress-points                                           */
+  int32_t ndummy;  /* all dummy wall particles (nrow * ndummy2)               */
+  int32_t ndummy2; /* dummies of the innermost layer (ids ntotal+1..+ndummy2) */
+  int32_t ndimn;   /* must be 2                                               */
+  int32_t nstre;   /* must be 4                                               */
+  int32_t ntype_solid; /* 1 plane stress (szz = nu (sxx+syy) in the return), 2 plane strain */
+
+  /* solver flags (.dat `pa_sph nnps sle skf CSPM update_x XSPH`, input.txt) */
+  int32_t sp_sph, inside_approach, cspm, xsph, update_x, cont_density, sle, skf;
+  int32_t art_stress; /* must be 0 (artificial stress is not in the hot path) */
+
+  /* material props(1,1..20): 1 ntype_eco, 2 ncrit, 3 E, 4 nu, 6 rho, 13 tan(phi), 14 c */
+  double props[20];
+  /* elastic constants exactly as the caller's module holds them
+     (code/3_SPH_material_2018.f90:738-749: D11 = (4./3.)G + K with FP32 literals) */
+  double D11, D12, D22, D33, D41, D42;
+  double pi; /* module `pi` = 4*atan(1.0) evaluated in FP32 (:163) */
+  double dx, dy;
+  double dt_sph;
+  double alpha, beta; /* artificial viscosity                        */
+  double damping;     /* DampingTG                                   */
+
+  /* gravity: cgrav * ft_grav * timecurve(tcurve_grav)(time_sph) */
+  int32_t ic_grav, tcurve_grav;
+  double cgrav[2];
+  double ft_grav;
+
+  /* time curves ttcurves(ntcurves,mptstcurves) (FP64), ftcurves(...) (FP32),
+     column-major exactly as allocated by the reference */
+  int32_t ntcurves, mptstcurves;
+  const int32_t* nptstcurves;
+  const double* ttcurves;
+  const float* ftcurves;
+
+  /* boundary conditions: bc_list(8,no_bcs) as read (column 7 already x twopi) */
+  int32_t no_bcs, ifsigman;
+  const double* bc_list;
+
+  double xmin_domain[2], xmax_domain[2];
+
+  /* dummy wall tables, length ntotal2 (entries below ntotal unused), FP32 like the reference */
+  const float* wall_position;
+  const float* horizontal_or_not;
+
+  int32_t precision;      /* SPS_PREC_*                                      */
+  int32_t max_neighbours; /* neighbour capacity per particle (two lists of half this size);
+                             0 = sized from the kernel support at upload */
+} sps_params;
+
+typedef struct sps_ctx sps_ctx;
+
+/* Allocate a context on the current CUDA device.  Replaces the allocation part of
+   Setup_Global_Arrays (code/3_SPH_material_2018.f90:883) for the hot-path arrays. */
+int sps_create(const sps_params* p, sps_ctx** out);
+
+/* Copy the dynamic state in (all arrays length ntotal2 unless noted):
+   x(2,.), vel(2,.), stress(4,.), mass, rho, hsml, itype (1 SP, 2 node, 25 dummy),
+   intvars1 = Internal_Vars(1,.) (length ntotal), f_drucker (length ntotal),
+   x00(2,.) initial positions (displacement origin). */
+int sps_upload(sps_ctx* ctx, const double* x, const double* vel, const double* stress,
+               const double* mass, const double* rho, const double* hsml, const int32_t* itype,
+               const double* intvars1, const double* f_drucker, const double* x00);
+
+/* Boundary-condition bookkeeping of Get_BCs_on_node (code/3_SPH_material_2018.f90:1049):
+   bc_or_not(ntotal), bc_info(8,ntotal). Optional when no_bcs == 0. */
+int sps_upload_bcs(sps_ctx* ctx, const int32_t* bc_or_not, const int32_t* bc_info);
+
+/* Advance nsteps steps.  Each step is `call time_integration` followed by
+   `time_sph = time_sph + dt_sph` (code/1_SPH_2018.f90:82-83); *time_sph is read on entry
+   and holds the advanced time on return.  Itimestep bookkeeping of the pair list
+   (grid_find_NEW's linked-list reuse) is carried by the context across calls. */
+int sps_step(sps_ctx* ctx, int32_t nsteps, double* time_sph);
+
+/* Copy fields back; any pointer may be NULL to skip that field.
+   x, vel: (2,ntotal2); stress: (4,ntotal2); rho: ntotal2; intvars1: ntotal;
+   displ: (2,nnode); bc_or_not: ntotal; f_drucker: ntotal.  The stress of dummy particles
+   is returned as 0: the reference only writes it as pair-local scratch inside
+   get_derivatives (node--dummy pairs, 2_SPH_main_2018.f90:577-588) and never reads it
+   outside that pair. */
+int sps_download(sps_ctx* ctx, double* x, double* vel, double* stress, double* rho,
+                 double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker);
+
+/* Test hook: the pair list of the last step in the reference's traversal order (the
+   order its linked list `last -> next` is walked), after Pint_Update
+   (code/3_SPH_material_2018.f90:1574): 1-based pair_i, pair_j, pint_type, and the FP32
+   w, dwdx, dwdy.  Call with NULL arrays to get the count in *npairs; otherwise *npairs
+   holds the capacity on entry and the count on return. */
+int sps_dump_pairs(sps_ctx* ctx, int32_t* pair_i, int32_t* pair_j, int32_t* pint_type,
+                   float* w, float* dwdx, float* dwdy, int64_t* npairs);
+
+/* The CUDA stream (a cudaStream_t) every launch of this context is issued on, so that a
+   caller can order its own work or record CUDA events against it.  No reference
+   counterpart (the reference has no device). */
+int sps_get_stream(sps_ctx* ctx, void** stream);
+
+/* Number of this library's kernels one step launches (no reference counterpart). */
+int sps_kernels_per_step(sps_ctx* ctx, int32_t* n);
+
+/* Profiling hook (no reference counterpart): run nsteps steps launching each kernel with
+   CUDA events around it on the context stream, and return the per-kernel totals.  names
+   receives up to cap NUL-separated kernel names (names_len bytes), ms[k] the summed
+   milliseconds and launches[k] the launch count of kernel k; *nkernels the number of
+   distinct kernels.  The state advances exactly as with sps_step. */
+int sps_profile_step(sps_ctx* ctx, int32_t nsteps, double* time_sph, char* names,
+                     int32_t names_len, double* ms, int32_t* launches, int32_t cap,
+                     int32_t* nkernels);
+
+/* Copy the last error message of this context (or of the last failed sps_create when
+   ctx is NULL) into buf (NUL-terminated, truncated to len). Returns its length. */
+int sps_last_error(sps_ctx* ctx, char* buf, int32_t len);
+
+void sps_destroy(sps_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPS_GB300_H */

@@ -1,0 +1,1131 @@
+/*
+ * sps_oracle.c -- CPU oracle of the stress-particle SPH step.  TEST INFRASTRUCTURE ONLY:
+ * loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, never by the
+ * product path.
+ *
+ * PARITY UNPINNED: the reference is Fortran 90; no Fortran compiler exists on either
+ * machine of this build and the reference ships no golden outputs, so this restatement is
+ * pinned only by its own known-answer and invariant tests (tests/test_oracle_*.py).
+ *
+ * It restates, routine by routine and in the same floating-point operation order, the
+ * Drucker-Prager example's copy of the reference (paths below are relative to
+ * example_problems/soil_failure_bui_et_al_2008/):
+ *   2_SPH_main_2018.f90   time_integration :78, XSPH_update :189, stress_point_update :403,
+ *                         get_derivatives :487, RK4 :653, density_update :807,
+ *                         artificial_viscosity :826, get_spin_rate_tensor :1021,
+ *                         boundary_forces :1039, Check_Out_Domain :1170,
+ *                         grid_find_NEW :1199, kernel :1440
+ *   3_SPH_material_2018.f90  Pint_Update :1574, BCs/Normal_BCs :1641/:1665,
+ *                         update_strain :1864, plastic_terms :1884, drucker_prager :1958,
+ *                         adapt_stress2 :2087, Get_derivative_intvars :2697,
+ *                         gravity_force :2809
+ * Mixed precision is reproduced: FP32 `real` locals become `float`, FP32 literals such as
+ * 2./3. stay float, pair kernel values are stored as float (5_SPH_global_vars_2018.f90:19-21).
+ * Build with -ffp-contract=off so no multiply-add is fused (gfortran -O3 on x86-64 has no
+ * FMA instructions available).
+ *
+ * Pair order: grid_find_NEW keeps its pairs in a linked list that is walked from `last`;
+ * new nodes are prepended and old nodes are refilled in list order
+ * (2_SPH_main_2018.f90:1309-1401).  Every scatter loop of the reference accumulates in
+ * that walk order, so the oracle keeps the pairs in creation order and walks them through
+ * the permutation `order[]` that the linked list produces (see build_walk_order).
+ */
+#include "sps_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct orc_ctx {
+  sps_params p;
+  int NN, NT, N2; /* nnode, ntotal, ntotal2 */
+  int32_t *nptstcurves;
+  double *ttcurves;
+  float *ftcurves;
+  double *bc_list;
+  float *wall_position, *horizontal_or_not;
+  /* state (Fortran layouts) */
+  double *x, *vel, *stress, *mass, *rho, *hsml, *x00, *x0, *vx0, *displ;
+  int32_t *itype, *out_domain, *bc_or_not, *bc_info, *bc_int;
+  double *intvars1, *f_drucker, *grad_u, *Ddev;
+  double *f_bound, *art_visc;
+  /* pair list, creation order */
+  int64_t npairs, cap, m_pairs;
+  int32_t *pi, *pj, *ptype;
+  float *pw, *pdx, *pdy;
+  int64_t *order; /* walk position -> creation index */
+  /* scratch */
+  int32_t *which_cell, *cell_cnt, *cell_start, *cell_list;
+  int64_t cell_cap;
+  double time_sph;
+  int uploaded;
+  int step_count;
+};
+
+#define X(c, d, i) ((c)->x[(d) + 2 * (size_t)(i)])
+#define V(c, d, i) ((c)->vel[(d) + 2 * (size_t)(i)])
+#define S(c, k, i) ((c)->stress[(k) + 4 * (size_t)(i)])
+
+static void* xcalloc(size_t n, size_t sz) {
+  void* p = calloc(n ? n : 1, sz);
+  return p;
+}
+
+/* ------------------------------------------------------------------------------------
+ * kernel (2_SPH_main_2018.f90:1440-1538).  FP64 except the FP32 literal 2./3. (:1480).
+ * x**n with a constant n is expanded by gfortran into multiplications: x**2 = x*x,
+ * x**3 = (x*x)*x, x**4 = (x*x)*(x*x), x**5 = ((x*x)*x)*(x*x).
+ * ---------------------------------------------------------------------------------- */
+void orc_kernel(int32_t skf, double pi, double r, const double* dx2, double hsml, double* w,
+                double* dwdx) {
+  double q = r / hsml;
+  double factor;
+  *w = 0.0;
+  dwdx[0] = 0.0;
+  dwdx[1] = 0.0;
+  if (skf == 1) {
+    factor = 15.0 / (7.0 * pi * hsml * hsml);
+    if (q >= 0 && q <= 1.0) {
+      const double two_thirds = (double)(2.0f / 3.0f);
+      *w = factor * ((two_thirds - q * q) + (q * q * q) / 2.0);
+      for (int d = 0; d < 2; d++) dwdx[d] = ((factor * (-2.0 + 1.5 * q)) / (hsml * hsml)) * dx2[d];
+    } else if (q > 1.0 && q <= 2.0) {
+      double t = 2.0 - q;
+      *w = (factor / 6.0) * ((t * t) * t);
+      for (int d = 0; d < 2; d++)
+        dwdx[d] = -(((((factor / 6.0) * 3.0) * (t * t)) / hsml) * (dx2[d] / r));
+    }
+  } else if (skf == 2) {
+    factor = 1.0 / ((hsml * hsml) * pi);
+    if (q >= 0 && q <= 3.0) {
+      *w = factor * exp(-(q * q));
+      for (int d = 0; d < 2; d++) dwdx[d] = *w * (((-2.0 * dx2[d]) / hsml) / hsml);
+    }
+  } else if (skf == 3) {
+    factor = 7.0 / (478.0 * pi * hsml * hsml);
+    double a = 3.0 - q, b = 2.0 - q, c1 = 1.0 - q;
+    double a2 = a * a, b2 = b * b, c2 = c1 * c1;
+    double a4 = a2 * a2, b4 = b2 * b2;
+    double a5 = (a2 * a) * a2, b5 = (b2 * b) * b2, c5 = (c2 * c1) * c2;
+    if (q >= 0 && q <= 1.0) {
+      *w = factor * ((a5 - 6.0 * b5) + 15.0 * c5);
+      for (int d = 0; d < 2; d++)
+        dwdx[d] = factor * ((((-120.0 + 120.0 * q) - 50.0 * (q * q)) / (hsml * hsml)) * dx2[d]);
+    } else if (q > 1.0 && q <= 2.0) {
+      *w = factor * (a5 - 6.0 * b5);
+      for (int d = 0; d < 2; d++)
+        dwdx[d] = ((factor * (-5.0 * a4 + 30.0 * b4)) / hsml) * (dx2[d] / r);
+    } else if (q > 2.0 && q <= 3.0) {
+      *w = factor * a5;
+      for (int d = 0; d < 2; d++) dwdx[d] = ((factor * (-5.0 * a4)) / hsml) * (dx2[d] / r);
+    }
+  }
+}
+
+/* adapt_stress2 body for one particle (3_SPH_material_2018.f90:2087-2161), FP64 */
+static void adapt_one(double alpha2, double kc, double* s) {
+  double smean = ((s[0] + s[1]) + s[3]) / 3.0;
+  double d0 = s[0] - smean, d1 = s[1] - smean, d2 = s[2], d3 = s[3] - smean;
+  double varj2 = d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3);
+  double yield = -((alpha2 * 3.0) * smean) + kc;
+  if (yield < 0) {
+    double shift = kc / (3.0 * alpha2);
+    s[0] = (s[0] - smean) + shift;
+    s[1] = (s[1] - smean) + shift;
+    s[3] = (s[3] - smean) + shift;
+    smean = ((s[0] + s[1]) + s[3]) / 3.0;
+    d0 = s[0] - smean;
+    d1 = s[1] - smean;
+    d2 = s[2];
+    d3 = s[3] - smean;
+    varj2 = d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3);
+    yield = -((alpha2 * 3.0) * smean) + kc;
+  }
+  double sj = sqrt(varj2);
+  if (yield < sj) {
+    double rn = (-((3.0 * alpha2) * smean) + kc) / sj;
+    if (sj <= (double)1e-5f) rn = 0.0;
+    s[0] = rn * d0 + smean;
+    s[1] = rn * d1 + smean;
+    s[3] = rn * d3 + smean;
+    s[2] = rn * d2;
+  }
+}
+
+static void dp_constants(double tanfi, double coh, double* alpha2, double* kc) {
+  double den = sqrt(9.0 + 12.0 * (tanfi * tanfi));
+  *alpha2 = tanfi / den;
+  *kc = (3.0 * coh) / den;
+}
+
+void orc_adapt_stress(double tanfi, double coh, double* stress4) {
+  double a2, kc;
+  dp_constants(tanfi, coh, &a2, &kc);
+  adapt_one(a2, kc, stress4);
+}
+
+/* drucker_prager (3_SPH_material_2018.f90:1958-2083): FP32 body, FP64 interface */
+static void drucker_prager(const double* props, double time_sph, const double* s,
+                           const double* gu /* grad_u(2,2) of this SP */, double* f_dp,
+                           double* G, double* vivel) {
+  double f0 = *f_dp;
+  float tanfi = (float)props[12], coh = (float)props[13];
+  float young = (float)props[2], poiss = (float)props[3];
+  float smean = (float)(((s[0] + s[1]) + s[3]) / 3.0);
+  float devia[4];
+  devia[0] = (float)(s[0] - (double)smean);
+  devia[1] = (float)(s[1] - (double)smean);
+  devia[2] = (float)s[2];
+  devia[3] = (float)(s[3] - (double)smean);
+  float varj2 = devia[2] * devia[2] +
+                0.5f * ((devia[0] * devia[0] + devia[1] * devia[1]) + devia[3] * devia[3]);
+  float vari1 = 3.0f * smean;
+  float eps11 = (float)gu[0];                      /* grad_u(1,1) */
+  float eps12 = (float)(0.5 * (gu[2] + gu[1]));    /* 0.5*(grad_u(1,2)+grad_u(2,1)) */
+  float eps22 = (float)gu[3];                      /* grad_u(2,2) */
+  float emean = eps11 + eps22;
+  float alpha2 = tanfi / sqrtf(9.0f + 12.0f * (tanfi * tanfi));
+  float kc = (3.0f * coh) / sqrtf(9.0f + 12.0f * (tanfi * tanfi));
+  float yield = -(alpha2 * vari1) + kc;
+  float sj = sqrtf(varj2);
+  *f_dp = (double)(sj - yield);
+  float f1 = (float)(*f_dp);
+  double df = (double)f1 - f0;
+  float G_mod = young / (2.0f * (1.0f + poiss));
+  float K_mod = young / (3.0f * (1.0f - 2.0f * poiss));
+  float s_eps = (devia[0] * eps11 + (2.0f * devia[2]) * eps12) + devia[1] * eps22;
+  if (time_sph > 0 && f1 >= 0 && df >= 0 && sj >= 1e-5f) {
+    float G1[4];
+    for (int i = 0; i < 4; i++) G1[i] = (G_mod / sj) * devia[i];
+    float lambda_1 = ((3.0f * alpha2) * K_mod) * emean;
+    float lambda_2 = (G_mod / sj) * s_eps;
+    float lambda_3 = G_mod;
+    float G2 = (lambda_1 + lambda_2) / lambda_3;
+    for (int i = 0; i < 4; i++) G[i] = (double)(G1[i] * G2);
+    const float sixth = 1.0f / 6.0f;
+    float rs = 1.0f / sj;
+    vivel[0] = (double)((sixth * rs) * ((2.0f * devia[0] - devia[1]) - devia[3]));
+    vivel[1] = (double)((sixth * rs) * ((2.0f * devia[1] - devia[0]) - devia[3]));
+    vivel[2] = (double)(rs * devia[2]);
+    vivel[3] = (double)((sixth * rs) * ((2.0f * devia[3] - devia[0]) - devia[1]));
+    for (int i = 0; i < 4; i++) vivel[i] = vivel[i] * (double)G2;
+  } else {
+    for (int i = 0; i < 4; i++) {
+      G[i] = 0.0;
+      vivel[i] = 0.0;
+    }
+  }
+}
+
+void orc_drucker_prager(const double* props, double time_sph, const double* stress4,
+                        const double* grad_u4, double* f_drucker, double* G, double* vivel) {
+  drucker_prager(props, time_sph, stress4, grad_u4, f_drucker, G, vivel);
+}
+
+/* plastic_terms (3_SPH_material_2018.f90:1884-1954) + Get_derivative_intvars 2D branch
+   (:2767-2775).  Returns Gs (= -G) and der_intvars(1). */
+static void plastic_terms(orc_ctx* c, int ie, const double* fi, double* Gs, double* der1) {
+  const double* props = c->p.props;
+  int ntype_eco = (int)props[0];
+  int ncrit = (int)props[1];
+  double vivel[4] = {0, 0, 0, 0}, G2[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; k++) Gs[k] = 0.0;
+  if (ntype_eco > 1) {
+    double poiss = props[3];
+    double s2[4] = {fi[0], fi[1], fi[2], fi[3]};
+    if (c->p.ntype_solid == 1) s2[3] = poiss * (s2[0] + s2[1]);
+    if (ncrit == 12) {
+      drucker_prager(props, c->time_sph, s2, &c->grad_u[4 * (size_t)ie], &c->f_drucker[ie], G2,
+                     vivel);
+      for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
+    }
+    *der1 = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
+                  vivel[2] * vivel[2]) /
+                 3.0);
+  } else {
+    *der1 = 0.0;
+  }
+}
+
+/* Check_Out_Domain (2_SPH_main_2018.f90:1170-1194) */
+static void check_out_domain(orc_ctx* c) {
+  for (int i = 0; i < c->N2; i++)
+    for (int d = 0; d < 2; d++) {
+      double dxx = (X(c, d, i) - c->p.xmin_domain[d]) * (X(c, d, i) - c->p.xmax_domain[d]);
+      if (dxx > 0.0) c->out_domain[i] = 1;
+    }
+}
+
+static int ensure_pair_cap(orc_ctx* c, int64_t need) {
+  if (need <= c->cap) return 0;
+  int64_t nc = c->cap ? c->cap : 1024;
+  while (nc < need) nc *= 2;
+  int32_t* a = realloc(c->pi, nc * sizeof(int32_t));
+  if (!a) return -1;
+  c->pi = a;
+  a = realloc(c->pj, nc * sizeof(int32_t));
+  if (!a) return -1;
+  c->pj = a;
+  a = realloc(c->ptype, nc * sizeof(int32_t));
+  if (!a) return -1;
+  c->ptype = a;
+  float* f = realloc(c->pw, nc * sizeof(float));
+  if (!f) return -1;
+  c->pw = f;
+  f = realloc(c->pdx, nc * sizeof(float));
+  if (!f) return -1;
+  c->pdx = f;
+  f = realloc(c->pdy, nc * sizeof(float));
+  if (!f) return -1;
+  c->pdy = f;
+  int64_t* o = realloc(c->order, nc * sizeof(int64_t));
+  if (!o) return -1;
+  c->order = o;
+  c->cap = nc;
+  return 0;
+}
+
+/* Walk order of grid_find_NEW's linked list (2_SPH_main_2018.f90:1309-1401).  With m the
+   number of list nodes before this step and n the pairs found now, pair k (creation order)
+   refills the k-th node from `last` when k < m; pairs k >= m get new nodes prepended, so the
+   walk is pairs n-1, n-2, ..., m followed by 0, 1, ..., min(n,m)-1. */
+static void build_walk_order(orc_ctx* c) {
+  int64_t n = c->npairs, m = c->m_pairs, k = 0;
+  for (int64_t a = n - 1; a >= m; a--) c->order[k++] = a;
+  for (int64_t a = 0; a < (n < m ? n : m); a++) c->order[k++] = a;
+  if (n > c->m_pairs) c->m_pairs = n;
+}
+
+/* grid_find_NEW (2_SPH_main_2018.f90:1199-1435) with kernel() and the FP32 store */
+static int grid_find_new(orc_ctx* c) {
+  double xmin[2], xmax[2], deltx[2];
+  int ndivx[2];
+  int scale_k = (c->p.skf == 1) ? 2 : 3;
+  for (int d = 0; d < 2; d++) {
+    xmin[d] = (double)1.e10f;
+    xmax[d] = -xmin[d];
+    deltx[d] = 0.0;
+  }
+  for (int d = 0; d < 2; d++) {
+    for (int i = 0; i < c->N2; i++) {
+      if (c->out_domain[i] == 1) continue;
+      if (X(c, d, i) < xmin[d]) xmin[d] = X(c, d, i);
+      if (X(c, d, i) > xmax[d]) xmax[d] = X(c, d, i);
+      if (deltx[d] < c->hsml[i]) deltx[d] = c->hsml[i];
+    }
+    deltx[d] = deltx[d] * 2.0;
+    double length = xmax[d] - xmin[d];
+    ndivx[d] = (int)(length / deltx[d] + 1.0);
+    double length_new = (double)ndivx[d] * deltx[d];
+    xmin[d] = (xmin[d] - (length_new - length) / 2.0) - (double)0.001f * length;
+    xmax[d] = (xmax[d] + (length_new - length) / 2.0) + (double)0.001f * length;
+  }
+  int64_t ndivt = (int64_t)ndivx[0] * ndivx[1];
+  if (ndivt > c->cell_cap) {
+    free(c->cell_cnt);
+    free(c->cell_start);
+    c->cell_cnt = xcalloc(ndivt, sizeof(int32_t));
+    c->cell_start = xcalloc(ndivt, sizeof(int32_t));
+    if (!c->cell_cnt || !c->cell_start) return -1;
+    c->cell_cap = ndivt;
+  }
+  memset(c->cell_cnt, 0, ndivt * sizeof(int32_t));
+  for (int i = 0; i < c->N2; i++) {
+    c->which_cell[i] = -1;
+    if (c->out_domain[i] == 1) continue;
+    int idv[2];
+    for (int d = 0; d < 2; d++) {
+      idv[d] = (int)((X(c, d, i) - xmin[d]) / deltx[d] + 1.0);
+      if (idv[d] > ndivx[d]) idv[d] = ndivx[d];
+    }
+    int64_t idivt = (int64_t)ndivx[0] * (idv[1] - 1) + idv[0]; /* 1-based */
+    c->which_cell[i] = (int32_t)(idivt - 1);
+    c->cell_cnt[idivt - 1]++;
+  }
+  int32_t pos = 0;
+  for (int64_t t = 0; t < ndivt; t++) {
+    c->cell_start[t] = pos;
+    pos += c->cell_cnt[t];
+  }
+  {
+    /* fill in ascending particle id within each cell (:1297-1305) */
+    int32_t* cur = xcalloc(ndivt, sizeof(int32_t));
+    if (!cur) return -1;
+    for (int i = 0; i < c->N2; i++) {
+      int32_t t = c->which_cell[i];
+      if (t < 0) continue;
+      c->cell_list[c->cell_start[t] + cur[t]++] = i;
+    }
+    free(cur);
+  }
+  c->npairs = 0;
+  for (int idy = 1; idy <= ndivx[1]; idy++)
+    for (int idx = 1; idx <= ndivx[0]; idx++) {
+      int64_t idivt = (int64_t)ndivx[0] * (idy - 1) + idx;
+      int npicsi = c->cell_cnt[idivt - 1];
+      for (int ii = 1; ii <= npicsi; ii++) {
+        int it = c->cell_list[c->cell_start[idivt - 1] + ii - 1];
+        int idx0 = idx - 1 > 1 ? idx - 1 : 1;
+        int idx1 = idx + 1 < ndivx[0] ? idx + 1 : ndivx[0];
+        int idy1 = idy + 1 < ndivx[1] ? idy + 1 : ndivx[1];
+        for (int jdy = idy; jdy <= idy1; jdy++)
+          for (int jdx = idx0; jdx <= idx1; jdx++) {
+            int64_t jdivt = (int64_t)ndivx[0] * (jdy - 1) + jdx;
+            if (jdivt < idivt) continue;
+            int jj = (idivt == jdivt) ? ii + 1 : 1;
+            int npicsj = c->cell_cnt[jdivt - 1];
+            for (int j = jj; j <= npicsj; j++) {
+              int jt = c->cell_list[c->cell_start[jdivt - 1] + j - 1];
+              double dxiac[2];
+              dxiac[0] = X(c, 0, it) - X(c, 0, jt);
+              double driac = dxiac[0] * dxiac[0];
+              dxiac[1] = X(c, 1, it) - X(c, 1, jt);
+              driac = driac + dxiac[1] * dxiac[1];
+              double mhsml = (c->hsml[it] + c->hsml[jt]) / 2.0;
+              double r = sqrt(driac);
+              if (r < (double)scale_k * mhsml) {
+                if (ensure_pair_cap(c, c->npairs + 1)) return -1;
+                double w, dw[2];
+                orc_kernel(c->p.skf, c->p.pi, r, dxiac, mhsml, &w, dw);
+                int64_t k = c->npairs++;
+                c->pi[k] = it;
+                c->pj[k] = jt;
+                c->ptype[k] = 0;
+                c->pw[k] = (float)w;
+                c->pdx[k] = (float)dw[0];
+                c->pdy[k] = (float)dw[1];
+              }
+            }
+          }
+      }
+    }
+  build_walk_order(c);
+  return 0;
+}
+
+/* Pint_Update (3_SPH_material_2018.f90:1574-1634): orientation and pair type */
+static void pint_update(orc_ctx* c) {
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int i = c->pi[k], j = c->pj[k];
+    int ti = c->itype[i], tj = c->itype[j];
+    int ii = abs(ti), jj = abs(tj), isumm = ti + tj;
+    if ((ii == 2 && jj == 1) || (ii == 2 && jj == 25) || (ii == 1 && jj == 25)) {
+      c->pi[k] = j;
+      c->pj[k] = i;
+      c->pdx[k] = -c->pdx[k];
+      c->pdy[k] = -c->pdy[k];
+    }
+    int t = 0;
+    if (isumm == 3) t = 1;
+    else if (isumm == 2) t = 2;
+    else if (isumm == 4) t = 3;
+    else if (isumm == 27) t = 6;
+    else if (isumm == 26) t = 9;
+    c->ptype[k] = t;
+  }
+}
+
+/* stress_point_update (2_SPH_main_2018.f90:403-482) */
+static void stress_point_update(orc_ctx* c) {
+  const int NN = c->NN, NT = c->NT;
+  if (!c->p.sp_sph) {
+    for (int i = 0; i < NN; i++) {
+      for (int d = 0; d < 2; d++) V(c, d, NN + i) = V(c, d, i);
+      for (int k = 0; k < 4; k++) S(c, k, i) = S(c, k, NN + i);
+      c->intvars1[i] = c->intvars1[NN + i];
+      if (c->p.cont_density) c->rho[i] = c->rho[NN + i];
+    }
+    return;
+  }
+  double* vel_t = xcalloc(2 * (size_t)NT, sizeof(double));
+  double* st_t = xcalloc(4 * (size_t)NT, sizeof(double));
+  double* iv_t = xcalloc(NT, sizeof(double));
+  double* rho_t = xcalloc(NT, sizeof(double));
+  double* norm = xcalloc(NT, sizeof(double));
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    if (c->ptype[q] != 1) continue;
+    int j = c->pi[q]; /* stress point */
+    int i = c->pj[q]; /* node */
+    double w = (double)c->pw[q];
+    double h1 = (c->mass[j] / c->rho[j]) * w;
+    double h2 = (c->mass[i] / c->rho[i]) * w;
+    for (int d = 0; d < 2; d++) vel_t[d + 2 * (size_t)j] = vel_t[d + 2 * (size_t)j] + V(c, d, i) * h2;
+    for (int s = 0; s < 4; s++)
+      st_t[s + 4 * (size_t)i] = st_t[s + 4 * (size_t)i] + S(c, s, j) * h1;
+    iv_t[i] = iv_t[i] + c->intvars1[j] * h1;
+    if (c->p.cont_density) rho_t[i] = rho_t[i] + c->rho[j] * h1;
+    norm[j] = norm[j] + (w * c->mass[i]) / c->rho[i];
+    norm[i] = norm[i] + (w * c->mass[j]) / c->rho[j];
+  }
+  for (int i = NN; i < NT; i++) {
+    if (norm[i] == 0) continue;
+    V(c, 0, i) = vel_t[0 + 2 * (size_t)i] / norm[i];
+    V(c, 1, i) = vel_t[1 + 2 * (size_t)i] / norm[i];
+  }
+  for (int i = 0; i < NN; i++) {
+    if (norm[i] != 0) {
+      for (int s = 0; s < 4; s++) S(c, s, i) = st_t[s + 4 * (size_t)i] / norm[i];
+      c->intvars1[i] = iv_t[i] / norm[i];
+    } else {
+      V(c, 0, i) = 0.0;
+      V(c, 1, i) = 0.0;
+    }
+  }
+  if (c->p.cont_density)
+    for (int i = 0; i < NN; i++) c->rho[i] = rho_t[i] / norm[i];
+  free(vel_t);
+  free(st_t);
+  free(iv_t);
+  free(rho_t);
+  free(norm);
+}
+
+/* get_derivatives (2_SPH_main_2018.f90:487-648); div1(4,NT), div2(2,NT) */
+static void get_derivatives(orc_ctx* c, double* div1, double* div2) {
+  const int NN = c->NN, NT = c->NT;
+  double* g1 = xcalloc(4 * (size_t)NT, sizeof(double)); /* grad1(a,b,i) -> a + 2b + 4i */
+  double* g2 = xcalloc(6 * (size_t)NT, sizeof(double)); /* grad2(s,b,i) -> s + 3b + 6i */
+  double* AE = xcalloc(5 * (size_t)NT, sizeof(double));
+  memset(div1, 0, 4 * (size_t)NT * sizeof(double));
+  memset(div2, 0, 2 * (size_t)NT * sizeof(double));
+  for (int i = 0; i < NN; i++) c->bc_int[i] = 0;
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    int j = c->pi[q];
+    int i = c->pj[q];
+    double dwx = (double)c->pdx[q], dwy = (double)c->pdy[q];
+    double h1 = (dwx * c->mass[i]) / c->rho[i];
+    int t = c->ptype[q];
+    if (t == 1) {
+      double h2 = 0.0;
+      for (int d = 0; d < 2; d++) {
+        g1[d + 0 + 4 * (size_t)j] = g1[d + 0 + 4 * (size_t)j] + (V(c, d, i) - V(c, d, j)) * h1;
+        h2 = (dwy * c->mass[i]) / c->rho[i];
+        g1[d + 2 + 4 * (size_t)j] = g1[d + 2 + 4 * (size_t)j] + (V(c, d, i) - V(c, d, j)) * h2;
+      }
+      for (int s = 0; s < 3; s++) {
+        double ai = S(c, s, i) / (c->rho[i] * c->rho[i]);
+        double aj = S(c, s, j) / (c->rho[j] * c->rho[j]);
+        double gg1 = dwx * (ai + aj);
+        g2[s + 0 + 6 * (size_t)i] = g2[s + 0 + 6 * (size_t)i] - c->mass[j] * gg1;
+        double gg2 = dwy * (ai + aj);
+        g2[s + 3 + 6 * (size_t)i] = g2[s + 3 + 6 * (size_t)i] - c->mass[j] * gg2;
+      }
+      if (c->p.cspm) {
+        double h1b = -((dwx * c->mass[j]) / c->rho[j]);
+        double h2b = -((dwy * c->mass[j]) / c->rho[j]);
+        double* Aj = &AE[5 * (size_t)j];
+        double* Ai = &AE[5 * (size_t)i];
+        Aj[0] = Aj[0] + (X(c, 0, i) - X(c, 0, j)) * h1;
+        Aj[1] = Aj[1] + (X(c, 1, i) - X(c, 1, j)) * h1;
+        Aj[2] = Aj[2] + (X(c, 0, i) - X(c, 0, j)) * h2;
+        Aj[3] = Aj[3] + (X(c, 1, i) - X(c, 1, j)) * h2;
+        Ai[0] = Ai[0] + (X(c, 0, j) - X(c, 0, i)) * h1b;
+        Ai[1] = Ai[1] + (X(c, 1, j) - X(c, 1, i)) * h1b;
+        Ai[2] = Ai[2] + (X(c, 0, j) - X(c, 0, i)) * h2b;
+        Ai[3] = Ai[3] + (X(c, 1, j) - X(c, 1, i)) * h2b;
+      }
+    } else if (t == 9) {
+      /* i is the stress point, j the dummy */
+      const double beta_max = 1.5, vel_wall = 0.0;
+      double wall = (double)c->wall_position[j];
+      double da, db;
+      if (c->horizontal_or_not[j] == 1.0f) {
+        da = fabs(X(c, 1, i) - wall);
+        db = fabs(X(c, 1, j) - wall);
+      } else {
+        da = fabs(X(c, 0, i) - wall);
+        db = fabs(X(c, 0, j) - wall);
+      }
+      double bq = 1.0 + db / da;
+      double beta = beta_max < bq ? beta_max : bq;
+      double dv[2];
+      for (int d = 0; d < 2; d++) dv[d] = V(c, d, i) * (1.0 - beta) + beta * vel_wall;
+      double hh1 = (dwx * c->mass[j]) / c->rho[j];
+      for (int d = 0; d < 2; d++) {
+        g1[d + 0 + 4 * (size_t)i] = g1[d + 0 + 4 * (size_t)i] + (V(c, d, i) - dv[d]) * hh1;
+        double hh2 = (dwy * c->mass[j]) / c->rho[j];
+        g1[d + 2 + 4 * (size_t)i] = g1[d + 2 + 4 * (size_t)i] + (V(c, d, i) - dv[d]) * hh2;
+      }
+    } else if (t == 6) {
+      /* i is the node, j the dummy: stress(:,j) = stress(:,i) (pair-local) */
+      c->bc_int[i] = 1;
+      for (int s = 0; s < 4; s++) S(c, s, j) = S(c, s, i);
+      for (int s = 0; s < 3; s++) {
+        double ai = S(c, s, i) / (c->rho[i] * c->rho[i]);
+        double aj = S(c, s, j) / (c->rho[j] * c->rho[j]);
+        double hh1 = dwx * (ai + aj);
+        g2[s + 0 + 6 * (size_t)i] = g2[s + 0 + 6 * (size_t)i] - c->mass[j] * hh1;
+        double hh2 = dwy * (ai + aj);
+        g2[s + 3 + 6 * (size_t)i] = g2[s + 3 + 6 * (size_t)i] - c->mass[j] * hh2;
+      }
+    }
+  }
+  if (c->p.cspm) {
+    for (int i = 0; i < NT; i++) {
+      double* A = &AE[5 * (size_t)i];
+      A[4] = A[0] * A[3] - A[1] * A[2];
+      if (fabs(A[4]) < (double)1e-07f) {
+        A[4] = 1;
+        A[0] = 1;
+        A[1] = 0;
+        A[2] = 0;
+        A[3] = 1;
+      } else {
+        A[4] = 1.0 / A[4];
+      }
+    }
+    for (int d = 0; d < 2; d++) {
+      for (int i = NN; i < NT; i++) {
+        double* A = &AE[5 * (size_t)i];
+        double* g = &g1[4 * (size_t)i];
+        g[d + 0] = A[4] * (A[0] * g[d + 0] + A[1] * g[d + 2]);
+      }
+      for (int i = NN; i < NT; i++) {
+        double* A = &AE[5 * (size_t)i];
+        double* g = &g1[4 * (size_t)i];
+        g[d + 2] = A[4] * (A[2] * g[d + 0] + A[3] * g[d + 2]);
+      }
+      for (int i = 0; i < NN; i++) {
+        double* A = &AE[5 * (size_t)i];
+        double* g = &g2[6 * (size_t)i];
+        g[d + 0] = A[4] * (A[0] * g[d + 0] + A[1] * g[d + 3]);
+      }
+      for (int i = 0; i < NN; i++) {
+        double* A = &AE[5 * (size_t)i];
+        double* g = &g2[6 * (size_t)i];
+        g[d + 3] = A[4] * (A[2] * g[d + 0] + A[3] * g[d + 3]);
+      }
+    }
+  }
+  const double D11 = c->p.D11, D12 = c->p.D12, D22 = c->p.D22, D33 = c->p.D33, D41 = c->p.D41,
+               D42 = c->p.D42;
+  for (int i = NN; i < NT; i++) {
+    double* g = &g1[4 * (size_t)i];
+    double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
+    div1[0 + 4 * (size_t)i] = -(D11 * g11 + D12 * g22);
+    div1[1 + 4 * (size_t)i] = -(D12 * g11 + D22 * g22);
+    div1[2 + 4 * (size_t)i] = -(D33 * g21 + D33 * g12);
+    div1[3 + 4 * (size_t)i] = -(D41 * g11 + D42 * g22);
+  }
+  for (int i = 0; i < NN; i++) {
+    double* g = &g2[6 * (size_t)i];
+    div2[0 + 2 * (size_t)i] = -(g[0] + g[2 + 3]);
+    div2[1 + 2 * (size_t)i] = -(g[2] + g[1 + 3]);
+  }
+  memcpy(c->grad_u, g1, 4 * (size_t)NT * sizeof(double));
+  free(g1);
+  free(g2);
+  free(AE);
+}
+
+/* time-curve factor used by gravity_force (3_SPH_material_2018.f90:2830-2848) and the
+   time-curve BC branch of Normal_BCs (:1707-1722) */
+static double tcurve_value(const orc_ctx* c, int it, double t) {
+  int nc = c->p.ntcurves;
+  int npts = c->nptstcurves[it - 1];
+  double tt0 = 0, tt1 = 0;
+  int ip;
+  for (ip = 1; ip <= npts - 1; ip++) {
+    tt0 = c->ttcurves[(it - 1) + (size_t)(ip - 1) * nc];
+    tt1 = c->ttcurves[(it - 1) + (size_t)ip * nc];
+    if (t >= tt0 && t <= tt1) break;
+    tt0 = -1000.0;
+  }
+  if (tt0 >= 0.0) {
+    double xi = (t - tt0) / (tt1 - tt0);
+    return (1.0 - xi) * (double)c->ftcurves[(it - 1) + (size_t)(ip - 1) * nc] +
+           xi * (double)c->ftcurves[(it - 1) + (size_t)ip * nc];
+  }
+  return 0.0;
+}
+
+/* gravity_force (3_SPH_material_2018.f90:2809-2871) over the nodes */
+static void gravity_force(const orc_ctx* c, double* Gs /* (2,NN) */) {
+  double factg = 0.0;
+  for (size_t k = 0; k < 2 * (size_t)c->NN; k++) Gs[k] = 0.0;
+  if (c->p.ic_grav != 0) {
+    factg = tcurve_value(c, c->p.tcurve_grav, c->time_sph);
+    factg = factg * c->p.ft_grav;
+    if (c->p.ic_grav == 1)
+      for (int i = 0; i < c->NN; i++)
+        for (int d = 0; d < 2; d++) Gs[d + 2 * (size_t)i] = factg * c->p.cgrav[d];
+  }
+  for (int i = 0; i < c->NN; i++)
+    for (int d = 0; d < 2; d++)
+      Gs[d + 2 * (size_t)i] = Gs[d + 2 * (size_t)i] - c->p.damping * V(c, d, i);
+}
+
+/* boundary_forces, test == 2 branch (2_SPH_main_2018.f90:1117-1161): FP32 locals */
+static void boundary_forces(orc_ctx* c) {
+  const int NN = c->NN;
+  for (size_t k = 0; k < 2 * (size_t)NN; k++) c->f_bound[k] = 0.0;
+  const float cc = 20.0f;
+  const float d0 = (float)(c->p.dx / 2.0);
+  for (int j = c->NT; j < c->NT + c->p.ndummy2; j++) {
+    for (int i = 0; i < NN; i++) {
+      float r[2];
+      r[0] = (float)(X(c, 0, i) - X(c, 0, j));
+      r[1] = (float)(X(c, 1, i) - X(c, 1, j));
+      float r2 = sqrtf(r[0] * r[0] + r[1] * r[1]);
+      float f2;
+      float h = (float)(0.5 * (c->hsml[i] + c->hsml[j]));
+      float r_bound = r2 / (0.75f * h);
+      if (r2 > 0 && r2 < 1.5f * d0) f2 = 1.0f - (r2 / (1.5f * d0));
+      else f2 = 0.0f;
+      float f;
+      if (0 < r_bound && r_bound <= 2.0f / 3.0f) f = 2.0f / 3.0f;
+      else if (2.0f / 3.0f < r_bound && r_bound <= 1) f = 2.0f * r_bound - 1.5f * (r_bound * r_bound);
+      else if (1 < r_bound && r_bound < 2) f = 0.5f * ((2.0f - r_bound) * (2.0f - r_bound));
+      else f = 0.0f;
+      for (int d = 0; d < 2; d++)
+        c->f_bound[d + 2 * (size_t)i] =
+            c->f_bound[d + 2 * (size_t)i] +
+            (double)((((0.01f * (cc * cc)) * f2) * f) * (r[d] / (r2 * r2)));
+    }
+  }
+}
+
+/* artificial_viscosity (2_SPH_main_2018.f90:826-904): FP32 accumulators */
+static void artificial_viscosity(orc_ctx* c) {
+  const int NN = c->NN;
+  float* avt = xcalloc(2 * (size_t)NN, sizeof(float));
+  float visc = 0.0f;
+  const float cs = 600.0f;
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    if (c->ptype[q] != 3) continue;
+    int i = c->pi[q], j = c->pj[q];
+    float xij = (float)(X(c, 0, i) - X(c, 0, j));
+    float yij = (float)(X(c, 1, i) - X(c, 1, j));
+    float h = (float)(0.5 * (c->hsml[i] + c->hsml[j]));
+    float rho2 = (float)(0.5 * (c->rho[i] + c->rho[j]));
+    float div_u = (float)((double)xij * (V(c, 0, i) - V(c, 0, j)));
+    div_u = (float)((double)div_u + (double)yij * (V(c, 1, i) - V(c, 1, j)));
+    float sq = sqrtf(xij * xij + yij * yij);
+    float theta = (h * div_u) / (sq * sq + 0.01f * (h * h));
+    if (div_u < 0)
+      visc = (float)((-((c->p.alpha * (double)cs) * (double)theta) +
+                      c->p.beta * (double)(theta * theta)) /
+                     (double)rho2);
+    else if (div_u >= 0)
+      visc = 0.0f;
+    float px = visc * c->pdx[q], py = visc * c->pdy[q];
+    avt[0 + 2 * (size_t)i] = (float)((double)avt[0 + 2 * (size_t)i] + (double)px * c->mass[j]);
+    avt[0 + 2 * (size_t)j] = (float)((double)avt[0 + 2 * (size_t)j] - (double)px * c->mass[i]);
+    avt[1 + 2 * (size_t)i] = (float)((double)avt[1 + 2 * (size_t)i] + (double)py * c->mass[j]);
+    avt[1 + 2 * (size_t)j] = (float)((double)avt[1 + 2 * (size_t)j] - (double)py * c->mass[i]);
+  }
+  for (size_t k = 0; k < 2 * (size_t)NN; k++) c->art_visc[k] = -(double)avt[k];
+  free(avt);
+}
+
+/* Normal_BCs (3_SPH_material_2018.f90:1665-1770); ic_time is an uninitialised local in the
+   reference and is taken as 0, so t_actual = time_sph. */
+static void normal_bcs(orc_ctx* c) {
+  if (c->p.no_bcs <= 0) return;
+  double t = c->time_sph;
+  for (int ip = 0; ip < c->NT; ip++) {
+    int nber = c->bc_info[1 + 8 * (size_t)ip];
+    if (c->bc_or_not[ip] != 1) continue;
+    if (nber == 0) continue;
+    for (int r = 0; r < 5; r++) {
+      int bt = c->bc_info[r + 2 + 8 * (size_t)ip];
+      if (bt == 0) continue;
+      const double* b = &c->bc_list[8 * (size_t)(bt - 1)];
+      int itc = (int)b[2];
+      double val = 0.0;
+      if (itc == 0) {
+        double a0 = b[4], a1 = b[3], w = b[5], phi = b[6], tt = b[7];
+        double fact = 1.0 - exp(-t / tt);
+        double argum = w * t - phi;
+        val = (a0 + a1 * sin(argum)) * fact;
+      } else if (itc > 0) {
+        val = tcurve_value(c, itc, t) * b[3];
+      }
+      int var = (int)b[1];
+      if (var == 5) V(c, 0, ip) = val;
+      else if (var == 6) V(c, 1, ip) = val;
+      else if (var == 1) S(c, 0, ip) = val;
+      else if (var == 3) S(c, 2, ip) = val;
+      else if (var == 2) S(c, 1, ip) = val;
+    }
+  }
+}
+
+static void adapt_all(orc_ctx* c) {
+  double a2, kc;
+  dp_constants(c->p.props[12], c->p.props[13], &a2, &kc);
+  for (int i = 0; i < c->NT; i++) adapt_one(a2, kc, &c->stress[4 * (size_t)i]);
+}
+
+/* RK4 (2_SPH_main_2018.f90:653-802) */
+static void rk4(orc_ctx* c) {
+  const int NN = c->NN, NT = c->NT;
+  const double f1rk[4] = {0.0, 0.5, 0.5, 1.0}, f2rk[4] = {1.0, 2.0, 2.0, 1.0};
+  const int ncrit = (int)c->p.props[1];
+  const double dt = c->p.dt_sph;
+  size_t n2 = 2 * (size_t)NT, n4 = 4 * (size_t)NT;
+  double* vel0 = xcalloc(n2, sizeof(double));
+  double* st0 = xcalloc(n4, sizeof(double));
+  double* rho0 = xcalloc(NT, sizeof(double));
+  double* hsml0 = xcalloc(NT, sizeof(double));
+  double* RKv = xcalloc(n2, sizeof(double));
+  double* RKs = xcalloc(n4, sizeof(double));
+  double* RKr = xcalloc(NT, sizeof(double));
+  double* RKh = xcalloc(NT, sizeof(double));
+  double* RKd = xcalloc(NT, sizeof(double));
+  double* RHS1 = xcalloc(n4, sizeof(double));
+  double* RHS2 = xcalloc(n2, sizeof(double));
+  double* RHSr = xcalloc(NT, sizeof(double));
+  double* RHSh = xcalloc(NT, sizeof(double));
+  double* div1 = xcalloc(n4, sizeof(double));
+  double* div2 = xcalloc(n2, sizeof(double));
+  double* src = xcalloc(n4, sizeof(double));
+  double* spin = xcalloc(n4, sizeof(double));
+  double* grav = xcalloc(2 * (size_t)NN, sizeof(double));
+  memcpy(vel0, c->vel, n2 * sizeof(double));
+  memcpy(st0, c->stress, n4 * sizeof(double));
+  memcpy(rho0, c->rho, NT * sizeof(double));
+  memcpy(hsml0, c->hsml, NT * sizeof(double));
+  for (size_t k = 0; k < 2 * (size_t)NN; k++) c->art_visc[k] = 0.0;
+  memset(c->vel, 0, 2 * (size_t)c->N2 * sizeof(double));
+  memset(c->stress, 0, 4 * (size_t)c->N2 * sizeof(double));
+  for (int st = 0; st < 4; st++) {
+    for (int i = 0; i < NN; i++)
+      for (int d = 0; d < 2; d++)
+        V(c, d, i) = vel0[d + 2 * (size_t)i] + (f1rk[st] * dt) * RHS2[d + 2 * (size_t)i];
+    for (int i = NN; i < NT; i++)
+      for (int s = 0; s < 4; s++)
+        S(c, s, i) = st0[s + 4 * (size_t)i] + (f1rk[st] * dt) * RHS1[s + 4 * (size_t)i];
+    if (c->p.cont_density) {
+      for (int i = NN; i < NT; i++)
+        RHSr[i] = -c->rho[i] * (c->grad_u[0 + 4 * (size_t)i] + c->grad_u[3 + 4 * (size_t)i]);
+      for (int i = NN; i < NT; i++) c->rho[i] = rho0[i] + (f1rk[st] * dt) * RHSr[i];
+      if (c->p.sle == 2) {
+        for (int i = NN; i < NT; i++) RHSh[i] = -(hsml0[i] / (c->rho[i] * 2.0)) * RHSr[i];
+        for (int i = NN; i < NT; i++) c->hsml[i] = hsml0[i] + (f1rk[st] * dt) * RHSh[i];
+      }
+    }
+    if (ncrit == 12) adapt_all(c);
+    if (c->p.no_bcs > 0) normal_bcs(c);
+    stress_point_update(c);
+    if (c->p.sp_sph) {
+      if (ncrit == 12) adapt_all(c);
+      if (c->p.no_bcs > 0) normal_bcs(c);
+    }
+    get_derivatives(c, div1, div2);
+    for (int j = NN; j < NT; j++) {
+      double G[4], der1;
+      plastic_terms(c, j, &c->stress[4 * (size_t)j], G, &der1);
+      for (int s = 0; s < 4; s++) src[s + 4 * (size_t)j] = G[s];
+      RKd[j] = RKd[j] + der1 * f2rk[st];
+    }
+    gravity_force(c, grav);
+    if (c->p.inside_approach) boundary_forces(c);
+    if (c->p.alpha > 0 || c->p.beta > 0) artificial_viscosity(c);
+    if (c->p.update_x) {
+      for (int i = NN; i < NT; i++) {
+        const double* g = &c->grad_u[4 * (size_t)i];
+        double om1 = 0.5 * (g[2] - g[1]);
+        double om2 = -0.5 * (g[2] - g[1]);
+        spin[0 + 4 * (size_t)i] = 2.0 * om1 * S(c, 2, i);
+        spin[1 + 4 * (size_t)i] = 2.0 * om2 * S(c, 2, i);
+        spin[2 + 4 * (size_t)i] = om2 * S(c, 0, i) + om1 * S(c, 1, i);
+      }
+    }
+    for (int i = NN; i < NT; i++)
+      for (int s = 0; s < 4; s++) {
+        size_t o = s + 4 * (size_t)i;
+        RHS1[o] = (-div1[o] + spin[o]) + src[o];
+      }
+    for (int i = 0; i < NN; i++)
+      for (int d = 0; d < 2; d++) {
+        size_t o = d + 2 * (size_t)i;
+        RHS2[o] = (((-div2[o] + grav[o]) + c->art_visc[o]) + c->f_bound[o]) + 0.0;
+      }
+    for (int i = 0; i < NN; i++)
+      for (int d = 0; d < 2; d++) RKv[d + 2 * (size_t)i] += f2rk[st] * RHS2[d + 2 * (size_t)i];
+    for (int i = NN; i < NT; i++)
+      for (int s = 0; s < 4; s++) RKs[s + 4 * (size_t)i] += f2rk[st] * RHS1[s + 4 * (size_t)i];
+    if (c->p.cont_density) {
+      for (int i = 0; i < NT; i++) RKr[i] = RKr[i] + f2rk[st] * RHSr[i];
+      if (c->p.sle == 2)
+        for (int i = 0; i < NT; i++) RKh[i] = RKh[i] + f2rk[st] * RHSh[i];
+    }
+  }
+  for (int i = 0; i < NN; i++)
+    for (int d = 0; d < 2; d++)
+      V(c, d, i) = vel0[d + 2 * (size_t)i] + (dt / 6.0) * RKv[d + 2 * (size_t)i];
+  for (int i = NN; i < NT; i++)
+    for (int s = 0; s < 4; s++)
+      S(c, s, i) = st0[s + 4 * (size_t)i] + (dt / 6.0) * RKs[s + 4 * (size_t)i];
+  if (ncrit == 12) adapt_all(c);
+  if (c->p.no_bcs > 0) normal_bcs(c);
+  if (c->p.cont_density) {
+    for (int i = NN; i < NT; i++) c->rho[i] = rho0[i] + (dt / 6.0) * RKr[i];
+    if (c->p.sle == 2)
+      for (int i = NN; i < NT; i++) c->hsml[i] = hsml0[i] + (dt / 6.0) * RKh[i];
+  }
+  for (int i = 0; i < NT; i++) c->Ddev[i] = RKd[i] / 6.0;
+  free(vel0);
+  free(st0);
+  free(rho0);
+  free(hsml0);
+  free(RKv);
+  free(RKs);
+  free(RKr);
+  free(RKh);
+  free(RKd);
+  free(RHS1);
+  free(RHS2);
+  free(RHSr);
+  free(RHSh);
+  free(div1);
+  free(div2);
+  free(src);
+  free(spin);
+  free(grav);
+}
+
+/* XSPH_update (2_SPH_main_2018.f90:189-239) */
+static void xsph_update(orc_ctx* c) {
+  const int NT = c->NT;
+  double* vs = xcalloc(2 * (size_t)NT, sizeof(double));
+  double* xl = xcalloc(2 * (size_t)NT, sizeof(double));
+  memcpy(xl, c->x, 2 * (size_t)NT * sizeof(double));
+  const double eps = 0.5;
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    int t = c->ptype[q];
+    if (t != 2 && t != 3) continue;
+    int i = c->pi[q], j = c->pj[q];
+    double w = (double)c->pw[q];
+    if (t == 2) {
+      for (int d = 0; d < 2; d++)
+        vs[d + 2 * (size_t)i] += ((c->mass[j] / c->rho[j]) * (V(c, d, j) - V(c, d, i))) * w;
+      for (int d = 0; d < 2; d++)
+        vs[d + 2 * (size_t)j] += ((c->mass[i] / c->rho[i]) * (V(c, d, i) - V(c, d, j))) * w;
+    } else {
+      for (int d = 0; d < 2; d++)
+        vs[d + 2 * (size_t)j] += ((c->mass[i] / c->rho[i]) * (V(c, d, i) - V(c, d, j))) * w;
+      for (int d = 0; d < 2; d++)
+        vs[d + 2 * (size_t)i] += ((c->mass[j] / c->rho[j]) * (V(c, d, j) - V(c, d, i))) * w;
+      if (c->bc_or_not[i] == 2 && c->bc_or_not[j] != 2) c->bc_or_not[j] = 3;
+      if (c->bc_or_not[j] == 2 && c->bc_or_not[i] != 2) c->bc_or_not[i] = 3;
+    }
+  }
+  const double dt = c->p.dt_sph;
+  for (int i = 0; i < NT; i++)
+    for (int d = 0; d < 2; d++)
+      X(c, d, i) = xl[d + 2 * (size_t)i] + dt * (V(c, d, i) + eps * vs[d + 2 * (size_t)i]);
+  free(vs);
+  free(xl);
+}
+
+/* time_integration (2_SPH_main_2018.f90:78-184) */
+static int time_integration(orc_ctx* c) {
+  const int NN = c->NN, NT = c->NT;
+  const int ncrit = (int)c->p.props[1];
+  check_out_domain(c);
+  if (grid_find_new(c)) return SPS_ERR_CAPACITY;
+  pint_update(c);
+  memcpy(c->vx0, c->vel, 2 * (size_t)NT * sizeof(double));
+  memcpy(c->x0, c->x, 2 * (size_t)NT * sizeof(double));
+  rk4(c);
+  for (int i = NN; i < NT; i++) c->intvars1[i] = c->intvars1[i] + c->p.dt_sph * c->Ddev[i];
+  stress_point_update(c);
+  if (c->p.sp_sph) {
+    if (ncrit == 12) adapt_all(c);
+    if (c->p.no_bcs > 0) normal_bcs(c);
+  }
+  if (c->p.update_x) {
+    if (c->p.xsph) {
+      xsph_update(c);
+    } else {
+      for (int i = 0; i < NT; i++)
+        for (int d = 0; d < 2; d++) {
+          float vh = (float)(0.5 * (c->vx0[d + 2 * (size_t)i] + V(c, d, i)));
+          X(c, d, i) = c->x0[d + 2 * (size_t)i] + (double)vh * c->p.dt_sph;
+        }
+    }
+    if (!c->p.sp_sph)
+      for (int i = 0; i < NN; i++)
+        for (int d = 0; d < 2; d++) X(c, d, NN + i) = X(c, d, i);
+    for (int i = 0; i < NN; i++)
+      for (int d = 0; d < 2; d++)
+        c->displ[d + 2 * (size_t)i] = X(c, d, i) - c->x00[d + 2 * (size_t)i];
+  } else {
+    for (int i = 0; i < NN; i++)
+      for (int d = 0; d < 2; d++)
+        c->displ[d + 2 * (size_t)i] =
+            c->displ[d + 2 * (size_t)i] +
+            (0.5 * (c->vx0[d + 2 * (size_t)i] + V(c, d, i))) * c->p.dt_sph;
+  }
+  return SPS_OK;
+}
+
+/* ------------------------------------------------------------------------------------ */
+
+int orc_create(const sps_params* p, orc_ctx** out) {
+  if (!p || !out) return SPS_ERR_ARG;
+  *out = NULL;
+  if (p->ndimn != 2 || p->nstre != 4) return SPS_ERR_UNSUPPORTED;
+  if (p->art_stress) return SPS_ERR_UNSUPPORTED;
+  if (p->nnode <= 0 || p->nstress < 0 || p->ndummy < 0 || p->ndummy2 < 0 ||
+      p->ndummy2 > p->ndummy)
+    return SPS_ERR_ARG;
+  int ntype_eco = (int)p->props[0], ncrit = (int)p->props[1];
+  if (ntype_eco > 1 && ncrit != 12) return SPS_ERR_UNSUPPORTED;
+  if (p->skf < 1 || p->skf > 3) return SPS_ERR_ARG;
+  if (p->ifsigman) return SPS_ERR_UNSUPPORTED;
+  if (!p->sp_sph && p->nstress != p->nnode) return SPS_ERR_ARG;
+  orc_ctx* c = xcalloc(1, sizeof(orc_ctx));
+  if (!c) return SPS_ERR_ARG;
+  c->p = *p;
+  c->NN = p->nnode;
+  c->NT = p->nnode + p->nstress;
+  c->N2 = c->NT + p->ndummy;
+  size_t N2 = c->N2, NT = c->NT, NN = c->NN;
+  if (p->ntcurves > 0) {
+    size_t nt = (size_t)p->ntcurves * p->mptstcurves;
+    c->nptstcurves = xcalloc(p->ntcurves, sizeof(int32_t));
+    c->ttcurves = xcalloc(nt, sizeof(double));
+    c->ftcurves = xcalloc(nt, sizeof(float));
+    memcpy(c->nptstcurves, p->nptstcurves, p->ntcurves * sizeof(int32_t));
+    memcpy(c->ttcurves, p->ttcurves, nt * sizeof(double));
+    memcpy(c->ftcurves, p->ftcurves, nt * sizeof(float));
+  }
+  if (p->no_bcs > 0) {
+    c->bc_list = xcalloc(8 * (size_t)p->no_bcs, sizeof(double));
+    memcpy(c->bc_list, p->bc_list, 8 * (size_t)p->no_bcs * sizeof(double));
+  }
+  c->wall_position = xcalloc(N2, sizeof(float));
+  c->horizontal_or_not = xcalloc(N2, sizeof(float));
+  if (p->wall_position) memcpy(c->wall_position, p->wall_position, N2 * sizeof(float));
+  if (p->horizontal_or_not)
+    memcpy(c->horizontal_or_not, p->horizontal_or_not, N2 * sizeof(float));
+  c->p.nptstcurves = c->nptstcurves;
+  c->p.ttcurves = c->ttcurves;
+  c->p.ftcurves = c->ftcurves;
+  c->p.bc_list = c->bc_list;
+  c->p.wall_position = c->wall_position;
+  c->p.horizontal_or_not = c->horizontal_or_not;
+  c->x = xcalloc(2 * N2, sizeof(double));
+  c->vel = xcalloc(2 * N2, sizeof(double));
+  c->stress = xcalloc(4 * N2, sizeof(double));
+  c->mass = xcalloc(N2, sizeof(double));
+  c->rho = xcalloc(N2, sizeof(double));
+  c->hsml = xcalloc(N2, sizeof(double));
+  c->x00 = xcalloc(2 * N2, sizeof(double));
+  c->x0 = xcalloc(2 * N2, sizeof(double));
+  c->vx0 = xcalloc(2 * N2, sizeof(double));
+  c->displ = xcalloc(2 * NN, sizeof(double));
+  c->itype = xcalloc(N2, sizeof(int32_t));
+  c->out_domain = xcalloc(N2, sizeof(int32_t));
+  c->bc_or_not = xcalloc(NT, sizeof(int32_t));
+  c->bc_info = xcalloc(8 * NT, sizeof(int32_t));
+  c->bc_int = xcalloc(NN, sizeof(int32_t));
+  c->intvars1 = xcalloc(NT, sizeof(double));
+  c->f_drucker = xcalloc(NT, sizeof(double));
+  c->grad_u = xcalloc(4 * NT, sizeof(double));
+  c->Ddev = xcalloc(NT, sizeof(double));
+  c->f_bound = xcalloc(2 * NN, sizeof(double));
+  c->art_visc = xcalloc(2 * NN, sizeof(double));
+  c->which_cell = xcalloc(N2, sizeof(int32_t));
+  c->cell_list = xcalloc(N2, sizeof(int32_t));
+  for (size_t i = 0; i < NT; i++) c->bc_info[8 * i] = (int32_t)(i + 1);
+  *out = c;
+  return SPS_OK;
+}
+
+int orc_upload(orc_ctx* c, const double* x, const double* vel, const double* stress,
+               const double* mass, const double* rho, const double* hsml, const int32_t* itype,
+               const double* intvars1, const double* f_drucker, const double* x00) {
+  if (!c || !x || !vel || !stress || !mass || !rho || !hsml || !itype) return SPS_ERR_ARG;
+  size_t N2 = c->N2, NT = c->NT;
+  memcpy(c->x, x, 2 * N2 * sizeof(double));
+  memcpy(c->vel, vel, 2 * N2 * sizeof(double));
+  memcpy(c->stress, stress, 4 * N2 * sizeof(double));
+  memcpy(c->mass, mass, N2 * sizeof(double));
+  memcpy(c->rho, rho, N2 * sizeof(double));
+  memcpy(c->hsml, hsml, N2 * sizeof(double));
+  memcpy(c->itype, itype, N2 * sizeof(int32_t));
+  if (intvars1) memcpy(c->intvars1, intvars1, NT * sizeof(double));
+  if (f_drucker) memcpy(c->f_drucker, f_drucker, NT * sizeof(double));
+  memcpy(c->x00, x00 ? x00 : x, 2 * N2 * sizeof(double));
+  memset(c->out_domain, 0, N2 * sizeof(int32_t));
+  memset(c->displ, 0, 2 * (size_t)c->NN * sizeof(double));
+  c->uploaded = 1;
+  return SPS_OK;
+}
+
+int orc_upload_bcs(orc_ctx* c, const int32_t* bc_or_not, const int32_t* bc_info) {
+  if (!c) return SPS_ERR_ARG;
+  if (bc_or_not) memcpy(c->bc_or_not, bc_or_not, (size_t)c->NT * sizeof(int32_t));
+  if (bc_info) memcpy(c->bc_info, bc_info, 8 * (size_t)c->NT * sizeof(int32_t));
+  return SPS_OK;
+}
+
+int orc_step(orc_ctx* c, int32_t nsteps, double* time_sph) {
+  if (!c || !time_sph || nsteps < 0) return SPS_ERR_ARG;
+  if (!c->uploaded) return SPS_ERR_STATE;
+  c->time_sph = *time_sph;
+  for (int s = 0; s < nsteps; s++) {
+    int rc = time_integration(c);
+    if (rc) return rc;
+    c->time_sph = c->time_sph + c->p.dt_sph;
+    c->step_count++;
+  }
+  *time_sph = c->time_sph;
+  return SPS_OK;
+}
+
+int orc_download(orc_ctx* c, double* x, double* vel, double* stress, double* rho,
+                 double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker) {
+  if (!c) return SPS_ERR_ARG;
+  size_t N2 = c->N2, NT = c->NT;
+  if (x) memcpy(x, c->x, 2 * N2 * sizeof(double));
+  if (vel) memcpy(vel, c->vel, 2 * N2 * sizeof(double));
+  if (stress) memcpy(stress, c->stress, 4 * N2 * sizeof(double));
+  if (rho) memcpy(rho, c->rho, N2 * sizeof(double));
+  if (intvars1) memcpy(intvars1, c->intvars1, NT * sizeof(double));
+  if (displ) memcpy(displ, c->displ, 2 * (size_t)c->NN * sizeof(double));
+  if (bc_or_not) memcpy(bc_or_not, c->bc_or_not, NT * sizeof(int32_t));
+  if (f_drucker) memcpy(f_drucker, c->f_drucker, NT * sizeof(double));
+  return SPS_OK;
+}
+
+int orc_dump_pairs(orc_ctx* c, int32_t* pair_i, int32_t* pair_j, int32_t* pint_type, float* w,
+                   float* dwdx, float* dwdy, int64_t* npairs) {
+  if (!c || !npairs) return SPS_ERR_ARG;
+  if (!pair_i) {
+    *npairs = c->npairs;
+    return SPS_OK;
+  }
+  if (*npairs < c->npairs) return SPS_ERR_CAPACITY;
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    pair_i[k] = c->pi[q] + 1;
+    pair_j[k] = c->pj[q] + 1;
+    if (pint_type) pint_type[k] = c->ptype[q];
+    if (w) w[k] = c->pw[q];
+    if (dwdx) dwdx[k] = c->pdx[q];
+    if (dwdy) dwdy[k] = c->pdy[q];
+  }
+  *npairs = c->npairs;
+  return SPS_OK;
+}
+
+void orc_destroy(orc_ctx* c) {
+  if (!c) return;
+  void* ptrs[] = {c->nptstcurves, c->ttcurves, c->ftcurves, c->bc_list, c->wall_position,
+                  c->horizontal_or_not, c->x, c->vel, c->stress, c->mass, c->rho, c->hsml,
+                  c->x00, c->x0, c->vx0, c->displ, c->itype, c->out_domain, c->bc_or_not,
+                  c->bc_info, c->bc_int, c->intvars1, c->f_drucker, c->grad_u, c->Ddev,
+                  c->f_bound, c->art_visc, c->pi, c->pj, c->ptype, c->pw, c->pdx, c->pdy,
+                  c->order, c->which_cell, c->cell_cnt, c->cell_start, c->cell_list};
+  for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
+  free(c);
+}

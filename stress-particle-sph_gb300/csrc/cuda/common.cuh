@@ -1,0 +1,268 @@
+// common.cuh -- device-side layout and shared device functions of the SPS step.
+//
+// Data layout in HBM (one context):
+//   particle state, reference id order (0-based), structure of arrays:
+//     px,py  vx,vy  s0..s3 (sxx,syy,sxy,szz)  mass rho hsml itype  iv1 fdp  x00x,x00y ...
+//   per-step cell sort: cell_of[id], cell_start[c], sorted[s] (id at sorted position s),
+//     spos[id]; sorted order = cells ascending, particle id ascending within a cell,
+//     out-of-domain particles last.
+//   pair tables per step:
+//     half[s*capH + k]  pairs created by the particle at sorted position s (the reference's
+//                       grid_find_NEW creation order), 16 B {b sorted pos, w, dwdx, dwdy}
+//     cross/same lists  ELL layout entry[k*N2 + s]: per target, the neighbours it meets in
+//                       the reference's linked-list walk order, 16 B {u id, w, Gx, Gy} with
+//                       G the kernel gradient with respect to the target.
+// The FP64 plain kernels reproduce the reference's arithmetic operation by operation
+// (compiled with -fmad=false: no multiply-add contraction).
+#pragma once
+#include <cstdint>
+
+#include "sps.h"
+
+namespace sps {
+
+constexpr int kMaxBC = 16;
+
+struct StepScalars {
+  double time_sph;
+  double factg;
+  double bcval[kMaxBC];
+};
+
+struct Grid {
+  double xmin[2];
+  double deltx[2];
+  int ndiv[2];
+  int ncells;
+  int nactive;   // particles in cells (sorted positions below nactive)
+  int overflow;  // cells exceeded capacity
+  float xr0[2];  // origin of the FP32 prefilter coordinates (= xmin)
+};
+
+// pair bookkeeping of grid_find_NEW's linked list
+struct PairMeta {
+  int64_t n;       // pairs found this step
+  int64_t m_prev;  // list nodes before this step (m_pairs)
+  int64_t m;       // list nodes after this step
+};
+
+enum ErrBits : int {
+  ERR_HALF_CAP = 1,
+  ERR_LIST_CAP = 2,
+  ERR_CELLS = 4,
+  ERR_NPAIRS = 8,
+  ERR_BOUND = 16,
+};
+
+struct Dev {
+  // sizes
+  int NN, NT, N2, ndummy2;
+  int capH, capC, capS;
+  int cell_cap;
+  // flags and constants
+  int skf, scale_k, cspm, xsph, update_x, cont_density, sle, sp_sph, inside, no_bcs;
+  int ntype_eco, ncrit, ntype_solid, ic_grav;
+  int bound_from_lists;
+  double pi, dt, alpha, beta, damping, dx;
+  double D11, D12, D22, D33, D41, D42;
+  double tanfi, coh, young, poiss;
+  double alpha2, kc;  // adapt_stress2 constants (FP64)
+  double xmin_dom[2], xmax_dom[2];
+  double cgrav[2];
+  int bcvar[kMaxBC];
+  // particle state (id order)
+  double *px, *py, *vx, *vy, *s0, *s1, *s2, *s3;
+  double *mass, *rho, *hsml, *iv1, *fdp, *x00x, *x00y, *dispx, *dispy;
+  int32_t* itype;
+  uint8_t* out;
+  int32_t *bc_or_not, *bc_info;
+  int32_t* bc_int;
+  float *wallpos, *horiz;
+  double* grad_u;  // (4, NT): grad_u(a,b) at a + 2b
+  // step temporaries
+  double *x0x, *x0y, *vx0, *vy0;  // positions and velocities at the start of the step
+  double *st0[4], *rho0, *hsml0;  // RK4 initial stress / rho / hsml (stress-points)
+  double *RKv[2], *RKs[4], *RKr, *RKh, *RKd;
+  double *RHS1[4], *RHS2[2], *RHSr, *RHSh;
+  double *fbx, *fby;  // boundary force (nodes), once per step
+  double* Ddev;
+  // cells
+  int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
+  float *xr, *yr, *hr;
+  Grid* grid;
+  double* bbox_part;  // per-block partial (minx, miny, -maxx, -maxy, -maxh)
+  int nbbox_blocks;
+  // pairs
+  int4* half;
+  int32_t* half_cnt;
+  int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
+  int4 *cross, *same;
+  int32_t *degC, *degS;
+  PairMeta* meta;
+  // scalars of the current step
+  const StepScalars* scal_table;
+  int* step_idx;
+  StepScalars* cur;
+  int* err;
+  // scan scratch
+  int64_t* scan_tmp;
+};
+
+// ----------------------------------------------------------------------------------------
+// kernel (example_problems/soil_failure_bui_et_al_2008/2_SPH_main_2018.f90:1440-1538).
+// FP64 with the FP32 literal 2./3. (:1480); x**n expanded into multiplications.
+__device__ __forceinline__ void sph_kernel(int skf, double pi, double r, double dx0, double dx1,
+                                           double hsml, double* w, double* dw0, double* dw1) {
+  double q = r / hsml;
+  *w = 0.0;
+  *dw0 = 0.0;
+  *dw1 = 0.0;
+  if (skf == 1) {
+    double factor = 15.0 / (7.0 * pi * hsml * hsml);
+    if (q >= 0 && q <= 1.0) {
+      const double two_thirds = (double)(2.0f / 3.0f);
+      *w = factor * ((two_thirds - q * q) + (q * q * q) / 2.0);
+      double a = (factor * (-2.0 + 1.5 * q)) / (hsml * hsml);
+      *dw0 = a * dx0;
+      *dw1 = a * dx1;
+    } else if (q > 1.0 && q <= 2.0) {
+      double t = 2.0 - q;
+      *w = (factor / 6.0) * ((t * t) * t);
+      double a = (((factor / 6.0) * 3.0) * (t * t)) / hsml;
+      *dw0 = -(a * (dx0 / r));
+      *dw1 = -(a * (dx1 / r));
+    }
+  } else if (skf == 2) {
+    double factor = 1.0 / ((hsml * hsml) * pi);
+    if (q >= 0 && q <= 3.0) {
+      *w = factor * exp(-(q * q));
+      *dw0 = *w * (((-2.0 * dx0) / hsml) / hsml);
+      *dw1 = *w * (((-2.0 * dx1) / hsml) / hsml);
+    }
+  } else if (skf == 3) {
+    double factor = 7.0 / (478.0 * pi * hsml * hsml);
+    double a = 3.0 - q, b = 2.0 - q, c1 = 1.0 - q;
+    double a2 = a * a, b2 = b * b, c2 = c1 * c1;
+    double a4 = a2 * a2, b4 = b2 * b2;
+    double a5 = (a2 * a) * a2, b5 = (b2 * b) * b2, c5 = (c2 * c1) * c2;
+    if (q >= 0 && q <= 1.0) {
+      *w = factor * ((a5 - 6.0 * b5) + 15.0 * c5);
+      double g = ((-120.0 + 120.0 * q) - 50.0 * (q * q)) / (hsml * hsml);
+      *dw0 = factor * (g * dx0);
+      *dw1 = factor * (g * dx1);
+    } else if (q > 1.0 && q <= 2.0) {
+      *w = factor * (a5 - 6.0 * b5);
+      double g = (factor * (-5.0 * a4 + 30.0 * b4)) / hsml;
+      *dw0 = g * (dx0 / r);
+      *dw1 = g * (dx1 / r);
+    } else if (q > 2.0 && q <= 3.0) {
+      *w = factor * a5;
+      double g = (factor * (-5.0 * a4)) / hsml;
+      *dw0 = g * (dx0 / r);
+      *dw1 = g * (dx1 / r);
+    }
+  }
+}
+
+// adapt_stress2 body (3_SPH_material_2018.f90:2087-2161), FP64
+__device__ __forceinline__ void adapt_stress(double alpha2, double kc, double& a, double& b,
+                                             double& c, double& d) {
+  double smean = ((a + b) + d) / 3.0;
+  double d0 = a - smean, d1 = b - smean, d2 = c, d3 = d - smean;
+  double varj2 = d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3);
+  double yield = -((alpha2 * 3.0) * smean) + kc;
+  if (yield < 0) {
+    double shift = kc / (3.0 * alpha2);
+    a = (a - smean) + shift;
+    b = (b - smean) + shift;
+    d = (d - smean) + shift;
+    smean = ((a + b) + d) / 3.0;
+    d0 = a - smean;
+    d1 = b - smean;
+    d2 = c;
+    d3 = d - smean;
+    varj2 = d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3);
+    yield = -((alpha2 * 3.0) * smean) + kc;
+  }
+  double sj = sqrt(varj2);
+  if (yield < sj) {
+    double rn = (-((3.0 * alpha2) * smean) + kc) / sj;
+    if (sj <= (double)1e-5f) rn = 0.0;
+    a = rn * d0 + smean;
+    b = rn * d1 + smean;
+    d = rn * d3 + smean;
+    c = rn * d2;
+  }
+}
+
+// drucker_prager (3_SPH_material_2018.f90:1958-2083): FP32 body.  s: stress (plane-stress
+// szz already substituted), gu: grad_u(2,2).  Updates *fdp, returns G and vivel.
+__device__ __forceinline__ void drucker_prager(const Dev& D, double time_sph, const double* s,
+                                               const double* gu, double* fdp, double* G,
+                                               double* vivel) {
+  double f0 = *fdp;
+  float tanfi = (float)D.tanfi, coh = (float)D.coh, young = (float)D.young,
+        poiss = (float)D.poiss;
+  float smean = (float)(((s[0] + s[1]) + s[3]) / 3.0);
+  float dv0 = (float)(s[0] - (double)smean);
+  float dv1 = (float)(s[1] - (double)smean);
+  float dv2 = (float)s[2];
+  float dv3 = (float)(s[3] - (double)smean);
+  float varj2 = dv2 * dv2 + 0.5f * ((dv0 * dv0 + dv1 * dv1) + dv3 * dv3);
+  float vari1 = 3.0f * smean;
+  float eps11 = (float)gu[0];
+  float eps12 = (float)(0.5 * (gu[2] + gu[1]));
+  float eps22 = (float)gu[3];
+  float emean = eps11 + eps22;
+  float den = sqrtf(9.0f + 12.0f * (tanfi * tanfi));
+  float alpha2 = tanfi / den;
+  float kc = (3.0f * coh) / den;
+  float yield = -(alpha2 * vari1) + kc;
+  float sj = sqrtf(varj2);
+  *fdp = (double)(sj - yield);
+  float f1 = (float)(*fdp);
+  double df = (double)f1 - f0;
+  float G_mod = young / (2.0f * (1.0f + poiss));
+  float K_mod = young / (3.0f * (1.0f - 2.0f * poiss));
+  float s_eps = (dv0 * eps11 + (2.0f * dv2) * eps12) + dv1 * eps22;
+  if (time_sph > 0 && f1 >= 0 && df >= 0 && sj >= 1e-5f) {
+    float gs = G_mod / sj;
+    float lambda_1 = ((3.0f * alpha2) * K_mod) * emean;
+    float lambda_2 = gs * s_eps;
+    float G2 = (lambda_1 + lambda_2) / G_mod;
+    G[0] = (double)((gs * dv0) * G2);
+    G[1] = (double)((gs * dv1) * G2);
+    G[2] = (double)((gs * dv2) * G2);
+    G[3] = (double)((gs * dv3) * G2);
+    const float sixth = 1.0f / 6.0f;
+    float rs = 1.0f / sj;
+    double g2 = (double)G2;
+    vivel[0] = (double)((sixth * rs) * ((2.0f * dv0 - dv1) - dv3)) * g2;
+    vivel[1] = (double)((sixth * rs) * ((2.0f * dv1 - dv0) - dv3)) * g2;
+    vivel[2] = (double)(rs * dv2) * g2;
+    vivel[3] = (double)((sixth * rs) * ((2.0f * dv3 - dv0) - dv1)) * g2;
+  } else {
+    G[0] = G[1] = G[2] = G[3] = 0.0;
+    vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0;
+  }
+}
+
+__device__ __forceinline__ bool is_sp(int t) { return t == 1; }
+__device__ __forceinline__ bool is_node(int t) { return t == 2; }
+__device__ __forceinline__ bool is_dummy(int t) { return t == 25; }
+
+// pair type of Pint_Update (3_SPH_material_2018.f90:1617-1627) from the itype sum
+__device__ __forceinline__ int pint_type(int ti, int tj) {
+  int s = ti + tj;
+  return s == 3 ? 1 : s == 2 ? 2 : s == 4 ? 3 : s == 27 ? 6 : s == 26 ? 9 : 0;
+}
+
+}  // namespace sps
+
+// launchers implemented in the .cu units
+namespace sps {
+struct Ctx;
+int launch_pair_build(Ctx& c);
+int launch_plain_step(Ctx& c);
+int launch_fast_step(Ctx& c);
+}  // namespace sps

@@ -1,0 +1,67 @@
+// ctx.cuh -- host-side context of one sps_ctx (device buffers, stream, graph).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "common.cuh"
+
+namespace sps {
+
+struct Ctx {
+  sps_params p{};
+  Dev d{};       // device pointers + constants, passed by value to kernels
+  Dev* d_dev = nullptr;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::vector<void*> allocs;
+  // host copies of tables
+  std::vector<int32_t> nptstcurves;
+  std::vector<double> ttcurves, bc_list;
+  std::vector<float> ftcurves;
+  StepScalars* d_scal_table = nullptr;
+  int scal_cap = 0;
+  std::vector<StepScalars> h_scal;
+  int* h_err = nullptr;  // pinned
+  double* stage = nullptr;  // device staging for interleaved host arrays (4 x ntotal2)
+  bool uploaded = false;
+  int64_t steps_done = 0;
+  int precision = SPS_PREC_FP64_PLAIN;
+  std::string last_error;
+  // graph of one step
+  cudaGraphExec_t graph = nullptr;
+  bool use_graph = true;
+  // scratch for scans
+  int scan_blocks = 0;
+  // per-kernel event timing (sps_profile_step)
+  bool profiling = false;
+  std::vector<std::pair<const char*, cudaEvent_t>> prof_events;
+  int64_t kernels_launched = 0;  // kernels enqueued by the launch functions
+  int kernels_per_step = 0;
+  // called before each kernel group: counts its kernels and, when profiling, records an
+  // event that opens the group's timing interval
+  void mark(const char* name, int nkernels = 1) {
+    kernels_launched += nkernels;
+    if (!profiling) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream);
+    prof_events.push_back({name, e});
+  }
+};
+
+// generic exclusive scans on the context stream
+void scan_i32_to_i32(Ctx& c, const int32_t* in, int32_t* out, int n);
+void scan_i32_to_i64(Ctx& c, const int32_t* in, int64_t* out, int n);
+
+}  // namespace sps
+
+#define SPS_CUDA_CHECK(expr)                                                         \
+  do {                                                                               \
+    cudaError_t e_ = (expr);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      throw std::runtime_error(std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    }                                                                                \
+  } while (0)

@@ -1,0 +1,482 @@
+// neighbours.cu -- cell-linked neighbour search of the SPS step (compiled with -fmad=false).
+//
+// Restates grid_find_NEW (example_problems/soil_failure_bui_et_al_2008/
+// 2_SPH_main_2018.f90:1199-1435), kernel (:1440) and Pint_Update
+// (3_SPH_material_2018.f90:1574) as a GB300 pipeline:
+//   k_bbox      Check_Out_Domain (:1170) + bounding box / max h over active particles
+//   k_grid      grid parameters with the reference's arithmetic (:1245-1258)
+//   k_cell_*    counting sort by cell, stable in particle id (the order list_picell holds)
+//   k_half      pairs created by each particle over the half stencil (self, +x, row
+//               above), in the reference's creation order, with FP32-stored W and dW
+//   k_lists     per-target neighbour lists in the reference's linked-list walk order
+// The distance test r < scale_k*(h_i+h_j)/2 is decided on FP32 cell-frame coordinates
+// with a guard band; candidates inside the band are re-tested with the exact FP64
+// expression, so the pair set equals the reference's.
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+
+#include "ctx.cuh"
+
+namespace sps {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ double warp_min(double v) {
+  for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Check_Out_Domain + per-block partial bounding box (minx, miny, -maxx, -maxy, -maxh, minh)
+__global__ void k_bbox(Dev D) {
+  __shared__ double sh[6][kBlock / 32];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
+  if (i < D.N2) {
+    double x = D.px[i], y = D.py[i];
+    double dxx = (x - D.xmin_dom[0]) * (x - D.xmax_dom[0]);
+    double dyy = (y - D.xmin_dom[1]) * (y - D.xmax_dom[1]);
+    uint8_t o = D.out[i];
+    if (dxx > 0.0 || dyy > 0.0) o = 1;
+    D.out[i] = o;
+    if (!o) {
+      double h = D.hsml[i];
+      v[0] = x;
+      v[1] = y;
+      v[2] = -x;
+      v[3] = -y;
+      v[4] = -h;
+      v[5] = h;
+    }
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = 0; k < 6; k++) {
+    double r = warp_min(v[k]);
+    if (lane == 0) sh[k][wid] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    for (int k = 0; k < 6; k++) {
+      double r = threadIdx.x < kBlock / 32 ? sh[k][threadIdx.x] : 1e300;
+      r = warp_min(r);
+      if (threadIdx.x == 0) D.bbox_part[6 * (size_t)blockIdx.x + k] = r;
+    }
+  }
+}
+
+// grid parameters (2_SPH_main_2018.f90:1230-1260)
+__global__ void k_grid(Dev D) {
+  __shared__ double sh[6][kBlock / 32];
+  double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
+  for (int b = threadIdx.x; b < D.nbbox_blocks; b += blockDim.x)
+    for (int k = 0; k < 6; k++) v[k] = fmin(v[k], D.bbox_part[6 * (size_t)b + k]);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = 0; k < 6; k++) {
+    double r = warp_min(v[k]);
+    if (lane == 0) sh[k][wid] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double red[6];
+  for (int k = 0; k < 6; k++) {
+    double r = 1e300;
+    for (int w = 0; w < kBlock / 32; w++) r = fmin(r, sh[k][w]);
+    red[k] = r;
+  }
+  Grid g;
+  double hmax = -red[4];
+  if (red[0] > 1e299) {  // no active particle
+    hmax = 0.0;
+  }
+  double cellsz = hmax * 2.0;
+  double nc = 1.0;
+  for (int d = 0; d < 2; d++) {
+    double xmin = red[d] > 1e299 ? (double)1.e10f : red[d];
+    double xmax = red[d] > 1e299 ? -(double)1.e10f : -red[2 + d];
+    double length = xmax - xmin;
+    double qd = length / cellsz + 1.0;
+    int ndiv = (qd >= 1.0 && qd < 1.0e9) ? (int)qd : 1;
+    double length_new = (double)ndiv * cellsz;
+    g.xmin[d] = (xmin - (length_new - length) / 2.0) - (double)0.001f * length;
+    g.deltx[d] = cellsz;
+    g.ndiv[d] = ndiv;
+    g.xr0[d] = 0.0f;
+    nc *= ndiv;
+  }
+  g.overflow = (nc > (double)D.cell_cap || !(cellsz > 0.0)) ? 1 : 0;
+  g.ncells = g.overflow ? 0 : (int)nc;
+  g.nactive = 0;
+  if (g.overflow) atomicOr(D.err, ERR_CELLS);
+  *D.grid = g;
+  // FP32 prefilter band: coordinates relative to xmin carry |err| <= 2^-24 * extent
+  double ext = fmax(g.deltx[0] * g.ndiv[0], g.deltx[1] * g.ndiv[1]);
+  double smin = (double)D.scale_k * red[5];
+  double tau = (smin > 0) ? 8.0 * ext * 1.1920929e-07 / smin + 4e-6 : 1.0;
+  D.bbox_part[0] = tau;  // reused as the band width of this step
+}
+
+__device__ __forceinline__ int cell_index(const Grid& g, double x, double y) {
+  double qx = (x - g.xmin[0]) / g.deltx[0] + 1.0;
+  double qy = (y - g.xmin[1]) / g.deltx[1] + 1.0;
+  // particles inside the bounding box give 1 <= q < ndiv + 1; the clamps only guard
+  // against non-finite coordinates
+  int ix = (qx >= 1.0) ? (qx < (double)g.ndiv[0] ? (int)qx : g.ndiv[0]) : 1;
+  int iy = (qy >= 1.0) ? (qy < (double)g.ndiv[1] ? (int)qy : g.ndiv[1]) : 1;
+  return g.ndiv[0] * (iy - 1) + (ix - 1);
+}
+
+__global__ void k_cell_count(Dev D) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.N2) return;
+  const Grid g = *D.grid;
+  int c;
+  if (D.out[i] || g.overflow) {
+    c = g.ncells;  // out-of-domain bucket, after every real cell
+  } else {
+    double x = D.px[i], y = D.py[i];
+    c = cell_index(g, x, y);
+    D.xr[i] = (float)(x - g.xmin[0]);
+    D.yr[i] = (float)(y - g.xmin[1]);
+    D.hr[i] = (float)D.hsml[i];
+  }
+  D.cell_of[i] = c;
+  atomicAdd(&D.cell_cnt[c], 1);
+}
+
+__global__ void k_cell_fill(Dev D) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.N2) return;
+  int c = D.cell_of[i];
+  int slot = atomicAdd(&D.cell_cursor[c], 1);
+  D.spos[D.cell_start[c] + slot] = i;  // spos used as scratch here
+}
+
+// per cell: sort the ids ascending (list_picell order), write sorted[] and spos[]
+__global__ void k_cell_sort(Dev D) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const Grid g = *D.grid;
+  if (c > g.ncells) return;
+  int st = D.cell_start[c], n = D.cell_cnt[c];
+  for (int a = 0; a < n; a++) {
+    int v = D.spos[st + a];
+    int b = a - 1;
+    while (b >= 0 && D.sorted[st + b] > v) {
+      D.sorted[st + b + 1] = D.sorted[st + b];
+      b--;
+    }
+    D.sorted[st + b + 1] = v;
+  }
+  if (c == g.ncells) D.grid->nactive = st;
+}
+
+__global__ void k_spos(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  D.spos[D.sorted[s]] = s;
+}
+
+// exact distance test of the reference (2_SPH_main_2018.f90:1345-1353) on the pair
+// (a = creator, b); returns true and r, dx, dy, mhsml when the pair is accepted
+__device__ __forceinline__ bool exact_test(const Dev& D, int a, int b, double& r, double& dx,
+                                           double& dy, double& mh) {
+  dx = D.px[a] - D.px[b];
+  double driac = dx * dx;
+  dy = D.py[a] - D.py[b];
+  driac = driac + dy * dy;
+  mh = (D.hsml[a] + D.hsml[b]) / 2.0;
+  r = sqrt(driac);
+  return r < (double)D.scale_k * mh;
+}
+
+// 0 = reject, 1 = accept, 2 = undecided (inside the guard band)
+__device__ __forceinline__ int prefilter(const Dev& D, float xa, float ya, float ha, int b,
+                                         float tau) {
+  float fx = xa - D.xr[b], fy = ya - D.yr[b];
+  float d2 = fx * fx + fy * fy;
+  float s = (float)D.scale_k * ((ha + D.hr[b]) * 0.5f);
+  float s2 = s * s;
+  if (d2 < s2 * (1.0f - tau)) return 1;
+  if (d2 > s2 * (1.0f + tau)) return 0;
+  return 2;
+}
+
+// pairs created by the particle at sorted position s (its half stencil), creation order
+__global__ void k_half(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const Grid g = *D.grid;
+  if (s >= g.nactive) {
+    D.half_cnt[s] = 0;
+    return;
+  }
+  const float tau = (float)D.bbox_part[0];
+  int a = D.sorted[s];
+  int c = D.cell_of[a];
+  int nx = g.ndiv[0], ny = g.ndiv[1];
+  int ix = c % nx, iy = c / nx;
+  float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
+  // R1: rest of own cell and the cell to the right; R2: the three cells of the row above
+  int r1_end_cell = (ix + 1 < nx) ? c + 1 : c;
+  int lo[2], hi[2];
+  lo[0] = s + 1;
+  hi[0] = D.cell_start[r1_end_cell] + D.cell_cnt[r1_end_cell];
+  if (iy + 1 < ny) {
+    int c0 = (iy + 1) * nx + (ix > 0 ? ix - 1 : 0);
+    int c1 = (iy + 1) * nx + (ix + 1 < nx ? ix + 1 : ix);
+    lo[1] = D.cell_start[c0];
+    hi[1] = D.cell_start[c1] + D.cell_cnt[c1];
+  } else {
+    lo[1] = hi[1] = 0;
+  }
+  int k = 0;
+  int4* out = D.half + (size_t)s * D.capH;
+  for (int rgn = 0; rgn < 2; rgn++)
+    for (int bs = lo[rgn]; bs < hi[rgn]; bs++) {
+      int b = D.sorted[bs];
+      int pf = prefilter(D, xa, ya, ha, b, tau);
+      if (pf == 0) continue;
+      double r, dx, dy, mh;
+      bool acc = exact_test(D, a, b, r, dx, dy, mh);
+      if (!acc) continue;
+      double w, dw0, dw1;
+      sph_kernel(D.skf, D.pi, r, dx, dy, mh, &w, &dw0, &dw1);
+      if (k < D.capH) {
+        out[k] = make_int4(bs, __float_as_int((float)w), __float_as_int((float)dw0),
+                           __float_as_int((float)dw1));
+      }
+      k++;
+    }
+  if (k > D.capH) {
+    atomicOr(D.err, ERR_HALF_CAP);
+    k = D.capH;
+  }
+  D.half_cnt[s] = k;
+}
+
+__global__ void k_pair_meta(Dev D) {
+  PairMeta m = *D.meta;
+  int64_t n = D.half_off[D.N2];
+  m.m_prev = m.m;
+  m.n = n;
+  if (n > m.m) m.m = n;
+  *D.meta = m;
+  if (n > 2147483647LL) atomicOr(D.err, ERR_NPAIRS);
+}
+
+__device__ __forceinline__ void reverse_ell(int4* base, int N2, int s, int lo, int hi) {
+  // reverse entries [lo, hi) of column s
+  hi--;
+  while (lo < hi) {
+    int4 t = base[(size_t)lo * N2 + s];
+    base[(size_t)lo * N2 + s] = base[(size_t)hi * N2 + s];
+    base[(size_t)hi * N2 + s] = t;
+    lo++;
+    hi--;
+  }
+}
+
+// Per-target lists.  The pairs a target t meets, in creation order, are: first the pairs
+// created by particles before t in sorted order (each holds t in its half list), then
+// t's own half list.  The linked list of the reference is walked as: pairs created this
+// step beyond the previous list length m (newest first), then pairs 0..m-1 in creation
+// order; the lists are written in that walk order.
+__global__ void k_lists(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const Grid g = *D.grid;
+  int nC = 0, nS = 0, newC = 0, newS = 0;
+  if (s < g.nactive) {
+    int t = D.sorted[s];
+    int tt = D.itype[t];
+    if (!is_dummy(tt)) {
+      const PairMeta meta = *D.meta;
+      const bool reorder = meta.n > meta.m_prev;
+      int c = D.cell_of[t];
+      int nx = g.ndiv[0];
+      int ix = c % nx, iy = c / nx;
+      int lo[2], hi[2];
+      if (iy > 0) {
+        int c0 = (iy - 1) * nx + (ix > 0 ? ix - 1 : 0);
+        int c1 = (iy - 1) * nx + (ix + 1 < nx ? ix + 1 : ix);
+        lo[0] = D.cell_start[c0];
+        hi[0] = D.cell_start[c1] + D.cell_cnt[c1];
+      } else {
+        lo[0] = hi[0] = 0;
+      }
+      lo[1] = D.cell_start[ix > 0 ? c - 1 : c];
+      hi[1] = s;
+      auto push = [&](int u, int w, float gx, float gy, int64_t cidx) {
+        int ut = D.itype[u];
+        int pt = pint_type(tt, ut);
+        bool same = (pt == 2 || pt == 3);
+        int4 e = make_int4(u, w, __float_as_int(gx), __float_as_int(gy));
+        bool isnew = reorder && cidx >= meta.m_prev;
+        if (same) {
+          if (nS < D.capS) D.same[(size_t)nS * D.N2 + s] = e;
+          nS++;
+          newS += isnew;
+        } else if (pt != 0) {
+          if (nC < D.capC) D.cross[(size_t)nC * D.N2 + s] = e;
+          nC++;
+          newC += isnew;
+        }
+      };
+      for (int rgn = 0; rgn < 2; rgn++)
+        for (int as = lo[rgn]; as < hi[rgn]; as++) {
+          int n = D.half_cnt[as];
+          const int4* h = D.half + (size_t)as * D.capH;
+          // binary search for s among the (ascending) partner positions of as
+          int l = 0, r = n;
+          while (l < r) {
+            int m = (l + r) >> 1;
+            if (h[m].x < s) l = m + 1;
+            else r = m;
+          }
+          if (l < n && h[l].x == s) {
+            int4 e = h[l];
+            push(D.sorted[as], e.y, -__int_as_float(e.z), -__int_as_float(e.w),
+                 D.half_off[as] + l);
+          }
+        }
+      {
+        int n = D.half_cnt[s];
+        const int4* h = D.half + (size_t)s * D.capH;
+        for (int k = 0; k < n; k++) {
+          int4 e = h[k];
+          push(D.sorted[e.x], e.y, __int_as_float(e.z), __int_as_float(e.w), D.half_off[s] + k);
+        }
+      }
+      if (nC > D.capC || nS > D.capS) {
+        atomicOr(D.err, ERR_LIST_CAP);
+        nC = min(nC, D.capC);
+        nS = min(nS, D.capS);
+        newC = newS = 0;
+      }
+      // walk order: [new entries, descending creation] + [old entries, ascending]
+      if (newC > 0) {
+        reverse_ell(D.cross, D.N2, s, 0, nC);
+        reverse_ell(D.cross, D.N2, s, newC, nC);
+      }
+      if (newS > 0) {
+        reverse_ell(D.same, D.N2, s, 0, nS);
+        reverse_ell(D.same, D.N2, s, newS, nS);
+      }
+    }
+  }
+  D.degC[s] = nC;
+  D.degS[s] = nS;
+}
+
+// ------------------------------------------------------------------------ scans
+template <typename TI, typename TO>
+__global__ void k_scan_blocks(const TI* in, TO* out, TO* bsum, int n, int per_block) {
+  // each block scans per_block elements (per_block = blockDim.x * items)
+  __shared__ TO sh[kBlock];
+  int base = blockIdx.x * per_block;
+  int items = per_block / blockDim.x;
+  int i0 = base + threadIdx.x * items;
+  TO local = 0;
+  for (int k = 0; k < items; k++) {
+    int i = i0 + k;
+    if (i < n) local += (TO)in[i];
+  }
+  sh[threadIdx.x] = local;
+  __syncthreads();
+  for (int o = 1; o < blockDim.x; o <<= 1) {
+    TO v = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  TO run = sh[threadIdx.x] - local;  // exclusive prefix of this thread
+  for (int k = 0; k < items; k++) {
+    int i = i0 + k;
+    if (i < n) {
+      out[i] = run;
+      run += (TO)in[i];
+    }
+  }
+  if (threadIdx.x == blockDim.x - 1) bsum[blockIdx.x] = sh[threadIdx.x];
+}
+
+template <typename TO>
+__global__ void k_scan_top(TO* bsum, int nb, TO* total) {
+  // single block: exclusive scan of block sums (sequential chunks of blockDim)
+  __shared__ TO sh[kBlock];
+  __shared__ TO carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    TO v = i < nb ? bsum[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < blockDim.x; o <<= 1) {
+      TO u = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += u;
+      __syncthreads();
+    }
+    if (i < nb) bsum[i] = sh[threadIdx.x] - v + carry;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += sh[threadIdx.x];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+template <typename TO>
+__global__ void k_scan_add(TO* out, const TO* bsum, int n, int per_block) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += bsum[i / per_block];
+}
+
+template <typename TI, typename TO>
+void scan_impl(Ctx& c, const TI* in, TO* out, int n) {
+  const int per_block = kBlock * 16;
+  int nb = (n + per_block - 1) / per_block;
+  TO* bsum = reinterpret_cast<TO*>(c.d.scan_tmp);
+  k_scan_blocks<TI, TO><<<nb, kBlock, 0, c.stream>>>(in, out, bsum, n, per_block);
+  k_scan_top<TO><<<1, kBlock, 0, c.stream>>>(bsum, nb, out + n);
+  k_scan_add<TO><<<(n + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(out, bsum, n, per_block);
+}
+
+}  // namespace
+
+void scan_i32_to_i32(Ctx& c, const int32_t* in, int32_t* out, int n) { scan_impl(c, in, out, n); }
+void scan_i32_to_i64(Ctx& c, const int32_t* in, int64_t* out, int n) { scan_impl(c, in, out, n); }
+
+int launch_pair_build(Ctx& c) {
+  Dev& D = c.d;
+  cudaStream_t st = c.stream;
+  int nb = (D.N2 + kBlock - 1) / kBlock;
+  c.mark("bbox");
+  k_bbox<<<nb, kBlock, 0, st>>>(D);
+  c.mark("grid");
+  k_grid<<<1, kBlock, 0, st>>>(D);
+  c.mark("cell_count");
+  cudaMemsetAsync(D.cell_cnt, 0, sizeof(int32_t) * (D.cell_cap + 2), st);
+  cudaMemsetAsync(D.cell_cursor, 0, sizeof(int32_t) * (D.cell_cap + 2), st);
+  k_cell_count<<<nb, kBlock, 0, st>>>(D);
+  c.mark("scan_cells", 3);
+  scan_i32_to_i32(c, D.cell_cnt, D.cell_start, D.cell_cap + 1);
+  c.mark("cell_fill");
+  k_cell_fill<<<nb, kBlock, 0, st>>>(D);
+  c.mark("cell_sort");
+  k_cell_sort<<<(D.cell_cap + 1 + kBlock - 1) / kBlock, kBlock, 0, st>>>(D);
+  c.mark("spos");
+  k_spos<<<nb, kBlock, 0, st>>>(D);
+  c.mark("half");
+  k_half<<<nb, kBlock, 0, st>>>(D);
+  c.mark("scan_half", 3);
+  scan_i32_to_i64(c, D.half_cnt, D.half_off, D.N2);
+  c.mark("pair_meta");
+  k_pair_meta<<<1, 1, 0, st>>>(D);
+  c.mark("lists");
+  k_lists<<<nb, kBlock, 0, st>>>(D);
+  return 0;
+}
+
+}  // namespace sps

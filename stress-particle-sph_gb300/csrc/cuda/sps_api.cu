@@ -1,0 +1,764 @@
+// sps_api.cu -- the C-ABI of include/sps.h on top of the CUDA step.
+//
+// sps_step(ctx, n, &time_sph) replaces n iterations of the reference driver's
+//   call time_integration ; time_sph = time_sph + dt_sph      (code/1_SPH_2018.f90:82-83)
+// The per-step scalars that depend only on time (gravity time-curve factor of
+// gravity_force, 3_SPH_material_2018.f90:2830-2848, and the boundary-condition values of
+// Normal_BCs, :1693-1724) are evaluated on the host with the reference's arithmetic and
+// uploaded as a table; the device replays one captured CUDA graph per step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ctx.cuh"
+
+struct sps_ctx {
+  sps::Ctx c;
+};
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_error;
+
+constexpr int kBlock = 256;
+
+template <typename T>
+T* dalloc(sps::Ctx& c, size_t n) {
+  void* p = nullptr;
+  SPS_CUDA_CHECK(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)));
+  c.allocs.push_back(p);
+  return static_cast<T*>(p);
+}
+
+double tcurve_value(const sps::Ctx& c, int it, double t) {
+  int nc = c.p.ntcurves;
+  if (it < 1 || it > nc) return 0.0;
+  int npts = c.nptstcurves[it - 1];
+  double tt0 = 0, tt1 = 0;
+  int ip;
+  for (ip = 1; ip <= npts - 1; ip++) {
+    tt0 = c.ttcurves[(it - 1) + (size_t)(ip - 1) * nc];
+    tt1 = c.ttcurves[(it - 1) + (size_t)ip * nc];
+    if (t >= tt0 && t <= tt1) break;
+    tt0 = -1000.0;
+  }
+  if (tt0 >= 0.0) {
+    double xi = (t - tt0) / (tt1 - tt0);
+    return (1.0 - xi) * (double)c.ftcurves[(it - 1) + (size_t)(ip - 1) * nc] +
+           xi * (double)c.ftcurves[(it - 1) + (size_t)ip * nc];
+  }
+  return 0.0;
+}
+
+void fill_scalars(sps::Ctx& c, double t, sps::StepScalars& s) {
+  std::memset(&s, 0, sizeof(s));
+  s.time_sph = t;
+  if (c.p.ic_grav != 0) s.factg = tcurve_value(c, c.p.tcurve_grav, t) * c.p.ft_grav;
+  for (int b = 0; b < c.p.no_bcs; b++) {
+    const double* q = &c.bc_list[8 * (size_t)b];
+    int itc = (int)q[2];
+    double val = 0.0;
+    if (itc == 0) {
+      double a0 = q[4], a1 = q[3], w = q[5], phi = q[6], tt = q[7];
+      double fact = 1.0 - std::exp(-t / tt);
+      double argum = w * t - phi;
+      val = (a0 + a1 * std::sin(argum)) * fact;
+    } else if (itc > 0) {
+      val = tcurve_value(c, itc, t) * q[3];
+    }
+    s.bcval[b] = val;
+  }
+}
+
+__global__ void k_aos_to_soa2(const double* in, double* a, double* b, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    a[i] = in[2 * (size_t)i];
+    b[i] = in[2 * (size_t)i + 1];
+  }
+}
+__global__ void k_soa_to_aos2(double* out, const double* a, const double* b, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    out[2 * (size_t)i] = a[i];
+    out[2 * (size_t)i + 1] = b[i];
+  }
+}
+__global__ void k_aos_to_soa4(const double* in, double* a, double* b, double* c, double* d, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    a[i] = in[4 * (size_t)i];
+    b[i] = in[4 * (size_t)i + 1];
+    c[i] = in[4 * (size_t)i + 2];
+    d[i] = in[4 * (size_t)i + 3];
+  }
+}
+__global__ void k_soa_to_aos4(double* out, const double* a, const double* b, const double* c,
+                              const double* d, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    out[4 * (size_t)i] = a[i];
+    out[4 * (size_t)i + 1] = b[i];
+    out[4 * (size_t)i + 2] = c[i];
+    out[4 * (size_t)i + 3] = d[i];
+  }
+}
+__global__ void k_check_finite(sps::Dev D) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.NT) return;
+  double v = D.px[i] + D.py[i] + D.vx[i] + D.vy[i] + D.s0[i] + D.s1[i] + D.s2[i] + D.s3[i];
+  if (!isfinite(v)) atomicOr(D.err, 1 << 20);
+}
+
+int fail(sps::Ctx* c, int rc, const std::string& msg) {
+  if (c) c->last_error = msg;
+  else {
+    std::lock_guard<std::mutex> g(g_err_mu);
+    g_create_error = msg;
+  }
+  return rc;
+}
+
+void build_graph(sps::Ctx& c) {
+  if (c.graph) {
+    cudaGraphExecDestroy(c.graph);
+    c.graph = nullptr;
+  }
+  cudaGraph_t g;
+  SPS_CUDA_CHECK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  int64_t k0 = c.kernels_launched;
+  if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
+  else sps::launch_fast_step(c);
+  c.kernels_per_step = (int)(c.kernels_launched - k0);
+  SPS_CUDA_CHECK(cudaStreamEndCapture(c.stream, &g));
+  SPS_CUDA_CHECK(cudaGraphInstantiate(&c.graph, g, 0));
+  cudaGraphDestroy(g);
+}
+
+void ensure_scal(sps::Ctx& c, int n) {
+  if (n <= c.scal_cap) return;
+  int cap = std::max(n, 256);
+  void* p = nullptr;
+  SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(sps::StepScalars) * cap));
+  c.allocs.push_back(p);
+  c.d_scal_table = static_cast<sps::StepScalars*>(p);
+  c.scal_cap = cap;
+  c.d.scal_table = c.d_scal_table;
+  if (c.graph) {
+    cudaGraphExecDestroy(c.graph);
+    c.graph = nullptr;
+  }
+}
+
+std::string err_text(int e) {
+  std::string m;
+  if (e & sps::ERR_HALF_CAP) m += "half-stencil pair capacity exceeded; ";
+  if (e & sps::ERR_LIST_CAP) m += "neighbour list capacity exceeded (raise max_neighbours); ";
+  if (e & sps::ERR_CELLS) m += "cell grid capacity exceeded; ";
+  if (e & sps::ERR_NPAIRS) m += "more than 2^31 pairs; ";
+  if (e & sps::ERR_BOUND) m += "more than 8 wall particles within 0.75 dx of a node; ";
+  if (e & (1 << 20)) m += "non-finite value in the particle state; ";
+  return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sps_create(const sps_params* p, sps_ctx** out) {
+  if (!p || !out) return fail(nullptr, SPS_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (p->ndimn != 2 || p->nstre != 4)
+    return fail(nullptr, SPS_ERR_UNSUPPORTED, "only ndimn = 2, nstre = 4 are implemented");
+  if (p->art_stress)
+    return fail(nullptr, SPS_ERR_UNSUPPORTED, "artificial stress is outside the hot path");
+  if (p->nnode <= 0 || p->nstress < 0 || p->ndummy < 0 || p->ndummy2 < 0 || p->ndummy2 > p->ndummy)
+    return fail(nullptr, SPS_ERR_ARG, "inconsistent particle counts");
+  int ntype_eco = (int)p->props[0], ncrit = (int)p->props[1];
+  if (ntype_eco > 1 && ncrit != 12)
+    return fail(nullptr, SPS_ERR_UNSUPPORTED,
+                "only the Drucker-Prager law (ncrit = 12) or elastic (ntype_eco = 1) is implemented");
+  if (p->skf < 1 || p->skf > 3) return fail(nullptr, SPS_ERR_ARG, "skf must be 1, 2 or 3");
+  if (p->ifsigman)
+    return fail(nullptr, SPS_ERR_UNSUPPORTED, "stress-free surface BC (ifsigman = 1) not implemented");
+  if (p->no_bcs > sps::kMaxBC) return fail(nullptr, SPS_ERR_UNSUPPORTED, "more than 16 BCs");
+  if (p->no_bcs > 0 && !p->bc_list) return fail(nullptr, SPS_ERR_ARG, "bc_list missing");
+  if (!p->sp_sph && p->nstress != p->nnode)
+    return fail(nullptr, SPS_ERR_ARG, "standard SPH needs nstress == nnode");
+  if (!p->sp_sph && p->inside_approach)
+    return fail(nullptr, SPS_ERR_ARG, "standard SPH has no inside approach");
+  if (p->sp_sph && !p->inside_approach)
+    return fail(nullptr, SPS_ERR_UNSUPPORTED, "outside approach (stress-point shifting) not implemented");
+  if (p->precision != SPS_PREC_FP64_PLAIN && p->precision != SPS_PREC_FP32_FAST)
+    return fail(nullptr, SPS_ERR_ARG, "unknown precision");
+  for (int b = 0; b < p->no_bcs; b++)
+    if ((int)p->bc_list[8 * (size_t)b + 2] < 0)
+      return fail(nullptr, SPS_ERR_UNSUPPORTED, "negative time-curve index in bc_list");
+  if (p->ic_grav != 0 && (p->tcurve_grav < 1 || p->tcurve_grav > p->ntcurves))
+    return fail(nullptr, SPS_ERR_ARG, "gravity time curve out of range");
+  sps_ctx* h = nullptr;
+  try {
+    h = new sps_ctx();
+    sps::Ctx& c = h->c;
+    c.p = *p;
+    c.precision = p->precision;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
+    c.device = dev;
+    SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    if (p->ntcurves > 0) {
+      size_t nt = (size_t)p->ntcurves * p->mptstcurves;
+      c.nptstcurves.assign(p->nptstcurves, p->nptstcurves + p->ntcurves);
+      c.ttcurves.assign(p->ttcurves, p->ttcurves + nt);
+      c.ftcurves.assign(p->ftcurves, p->ftcurves + nt);
+    }
+    if (p->no_bcs > 0) c.bc_list.assign(p->bc_list, p->bc_list + 8 * (size_t)p->no_bcs);
+    sps::Dev& D = c.d;
+    D.NN = p->nnode;
+    D.NT = p->nnode + p->nstress;
+    D.N2 = D.NT + p->ndummy;
+    D.ndummy2 = p->ndummy2;
+    D.capC = D.capS = D.capH = 0;  // sized at upload from the kernel support
+    D.skf = p->skf;
+    D.scale_k = p->skf == 1 ? 2 : 3;
+    D.cspm = p->cspm;
+    D.xsph = p->xsph;
+    D.update_x = p->update_x;
+    D.cont_density = p->cont_density;
+    D.sle = p->sle;
+    D.sp_sph = p->sp_sph;
+    D.inside = p->inside_approach;
+    D.no_bcs = p->no_bcs;
+    D.ntype_eco = ntype_eco;
+    D.ncrit = ncrit;
+    D.ntype_solid = p->ntype_solid;
+    D.ic_grav = p->ic_grav;
+    D.pi = p->pi;
+    D.dt = p->dt_sph;
+    D.alpha = p->alpha;
+    D.beta = p->beta;
+    D.damping = p->damping;
+    D.dx = p->dx;
+    D.D11 = p->D11;
+    D.D12 = p->D12;
+    D.D22 = p->D22;
+    D.D33 = p->D33;
+    D.D41 = p->D41;
+    D.D42 = p->D42;
+    D.tanfi = p->props[12];
+    D.coh = p->props[13];
+    D.young = p->props[2];
+    D.poiss = p->props[3];
+    {
+      double den = std::sqrt(9.0 + 12.0 * (D.tanfi * D.tanfi));
+      D.alpha2 = D.tanfi / den;
+      D.kc = (3.0 * D.coh) / den;
+    }
+    for (int d = 0; d < 2; d++) {
+      D.xmin_dom[d] = p->xmin_domain[d];
+      D.xmax_dom[d] = p->xmax_domain[d];
+      D.cgrav[d] = p->cgrav[d];
+    }
+    for (int b = 0; b < p->no_bcs; b++) D.bcvar[b] = (int)p->bc_list[8 * (size_t)b + 1];
+    const size_t N2 = D.N2, NT = D.NT, NN = D.NN;
+    D.px = dalloc<double>(c, N2);
+    D.py = dalloc<double>(c, N2);
+    D.vx = dalloc<double>(c, N2);
+    D.vy = dalloc<double>(c, N2);
+    D.s0 = dalloc<double>(c, N2);
+    D.s1 = dalloc<double>(c, N2);
+    D.s2 = dalloc<double>(c, N2);
+    D.s3 = dalloc<double>(c, N2);
+    D.mass = dalloc<double>(c, N2);
+    D.rho = dalloc<double>(c, N2);
+    D.hsml = dalloc<double>(c, N2);
+    D.iv1 = dalloc<double>(c, NT);
+    D.fdp = dalloc<double>(c, NT);
+    D.x00x = dalloc<double>(c, N2);
+    D.x00y = dalloc<double>(c, N2);
+    D.dispx = dalloc<double>(c, NN);
+    D.dispy = dalloc<double>(c, NN);
+    D.itype = dalloc<int32_t>(c, N2);
+    D.out = dalloc<uint8_t>(c, N2);
+    D.bc_or_not = dalloc<int32_t>(c, NT);
+    D.bc_info = dalloc<int32_t>(c, 8 * NT);
+    D.bc_int = dalloc<int32_t>(c, NN);
+    D.wallpos = dalloc<float>(c, N2);
+    D.horiz = dalloc<float>(c, N2);
+    D.grad_u = dalloc<double>(c, 4 * NT);
+    D.x0x = dalloc<double>(c, NT);
+    D.x0y = dalloc<double>(c, NT);
+    D.vx0 = dalloc<double>(c, NT);
+    D.vy0 = dalloc<double>(c, NT);
+    for (int k = 0; k < 4; k++) {
+      D.st0[k] = dalloc<double>(c, NT);
+      D.RKs[k] = dalloc<double>(c, NT);
+      D.RHS1[k] = dalloc<double>(c, NT);
+    }
+    for (int k = 0; k < 2; k++) {
+      D.RKv[k] = dalloc<double>(c, NT);
+      D.RHS2[k] = dalloc<double>(c, NT);
+    }
+    D.rho0 = dalloc<double>(c, NT);
+    D.hsml0 = dalloc<double>(c, NT);
+    D.RKr = dalloc<double>(c, NT);
+    D.RKh = dalloc<double>(c, NT);
+    D.RKd = dalloc<double>(c, NT);
+    D.RHSr = dalloc<double>(c, NT);
+    D.RHSh = dalloc<double>(c, NT);
+    D.fbx = dalloc<double>(c, NN);
+    D.fby = dalloc<double>(c, NN);
+    D.Ddev = dalloc<double>(c, NT);
+    D.cell_of = dalloc<int32_t>(c, N2);
+    D.sorted = dalloc<int32_t>(c, N2);
+    D.spos = dalloc<int32_t>(c, N2);
+    D.xr = dalloc<float>(c, N2);
+    D.yr = dalloc<float>(c, N2);
+    D.hr = dalloc<float>(c, N2);
+    D.grid = dalloc<sps::Grid>(c, 1);
+    D.nbbox_blocks = (int)((N2 + kBlock - 1) / kBlock);
+    D.bbox_part = dalloc<double>(c, 6 * (size_t)D.nbbox_blocks + 8);
+    D.half_cnt = dalloc<int32_t>(c, N2);
+    D.half_off = dalloc<int64_t>(c, N2 + 1);
+    D.degC = dalloc<int32_t>(c, N2);
+    D.degS = dalloc<int32_t>(c, N2);
+    D.meta = dalloc<sps::PairMeta>(c, 1);
+    D.step_idx = dalloc<int>(c, 1);
+    D.cur = dalloc<sps::StepScalars>(c, 1);
+    D.err = dalloc<int>(c, 1);
+    D.scan_tmp = dalloc<int64_t>(c, (N2 + 4096) / 4096 + 64);
+    c.stage = dalloc<double>(c, 4 * N2);
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.meta, 0, sizeof(sps::PairMeta), c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.err, 0, sizeof(int), c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.grad_u, 0, sizeof(double) * 4 * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_or_not, 0, sizeof(int32_t) * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_info, 0, sizeof(int32_t) * 8 * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_int, 0, sizeof(int32_t) * NN, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.fbx, 0, sizeof(double) * NN, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.fby, 0, sizeof(double) * NN, c.stream));
+    {
+      std::vector<float> wp(N2, 0.0f), ho(N2, 0.0f);
+      if (p->wall_position) std::copy(p->wall_position, p->wall_position + N2, wp.begin());
+      if (p->horizontal_or_not) std::copy(p->horizontal_or_not, p->horizontal_or_not + N2, ho.begin());
+      SPS_CUDA_CHECK(cudaMemcpyAsync(D.wallpos, wp.data(), sizeof(float) * N2, cudaMemcpyHostToDevice, c.stream));
+      SPS_CUDA_CHECK(cudaMemcpyAsync(D.horiz, ho.data(), sizeof(float) * N2, cudaMemcpyHostToDevice, c.stream));
+      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    }
+    SPS_CUDA_CHECK(cudaMallocHost(&c.h_err, sizeof(int)));
+    ensure_scal(c, 256);
+    D.cell_cap = 0;  // sized at upload
+    c.d_dev = nullptr;
+  } catch (const std::bad_alloc&) {
+    sps_destroy(h);
+    return fail(nullptr, SPS_ERR_CUDA, "host allocation failed");
+  } catch (const std::exception& e) {
+    sps_destroy(h);
+    return fail(nullptr, SPS_ERR_CUDA, e.what());
+  }
+  *out = h;
+  return SPS_OK;
+}
+
+int sps_upload(sps_ctx* h, const double* x, const double* vel, const double* stress,
+               const double* mass, const double* rho, const double* hsml, const int32_t* itype,
+               const double* intvars1, const double* f_drucker, const double* x00) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!x || !vel || !stress || !mass || !rho || !hsml || !itype)
+    return fail(&c, SPS_ERR_ARG, "sps_upload: null array");
+  sps::Dev& D = c.d;
+  const size_t N2 = D.N2, NT = D.NT;
+  for (size_t i = 0; i < N2; i++)
+    if (itype[i] != 1 && itype[i] != 2 && itype[i] != 25)
+      return fail(&c, SPS_ERR_ARG, "sps_upload: itype must be 1, 2 or 25");
+  for (size_t i = 0; i < N2; i++) {
+    int want = i < (size_t)D.NN ? 2 : i < NT ? 1 : 25;
+    if (itype[i] != want)
+      return fail(&c, SPS_ERR_ARG, "sps_upload: particles must be ordered nodes, stress-points, dummies");
+  }
+  try {
+    // staging buffers: interleaved arrays are transposed on the device
+    double* stage = c.stage;
+    int nb = (int)((N2 + kBlock - 1) / kBlock);
+    auto up2 = [&](const double* src, double* a, double* b) {
+      SPS_CUDA_CHECK(cudaMemcpyAsync(stage, src, sizeof(double) * 2 * N2, cudaMemcpyHostToDevice, c.stream));
+      k_aos_to_soa2<<<nb, kBlock, 0, c.stream>>>(stage, a, b, (int)N2);
+      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    };
+    up2(x, D.px, D.py);
+    up2(vel, D.vx, D.vy);
+    up2(x00 ? x00 : x, D.x00x, D.x00y);
+    SPS_CUDA_CHECK(cudaMemcpyAsync(stage, stress, sizeof(double) * 4 * N2, cudaMemcpyHostToDevice, c.stream));
+    k_aos_to_soa4<<<nb, kBlock, 0, c.stream>>>(stage, D.s0, D.s1, D.s2, D.s3, (int)N2);
+    SPS_CUDA_CHECK(cudaMemcpyAsync(D.mass, mass, sizeof(double) * N2, cudaMemcpyHostToDevice, c.stream));
+    SPS_CUDA_CHECK(cudaMemcpyAsync(D.rho, rho, sizeof(double) * N2, cudaMemcpyHostToDevice, c.stream));
+    SPS_CUDA_CHECK(cudaMemcpyAsync(D.hsml, hsml, sizeof(double) * N2, cudaMemcpyHostToDevice, c.stream));
+    SPS_CUDA_CHECK(cudaMemcpyAsync(D.itype, itype, sizeof(int32_t) * N2, cudaMemcpyHostToDevice, c.stream));
+    if (intvars1)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(D.iv1, intvars1, sizeof(double) * NT, cudaMemcpyHostToDevice, c.stream));
+    else
+      SPS_CUDA_CHECK(cudaMemsetAsync(D.iv1, 0, sizeof(double) * NT, c.stream));
+    if (f_drucker)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(D.fdp, f_drucker, sizeof(double) * NT, cudaMemcpyHostToDevice, c.stream));
+    else
+      SPS_CUDA_CHECK(cudaMemsetAsync(D.fdp, 0, sizeof(double) * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.out, 0, N2, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.dispx, 0, sizeof(double) * D.NN, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.dispy, 0, sizeof(double) * D.NN, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    // cell grid capacity from the uploaded extent (4x margin for spreading)
+    double xmn[2] = {1e300, 1e300}, xmx[2] = {-1e300, -1e300}, hmax = 0, hmin_nd = 1e300;
+    for (size_t i = 0; i < N2; i++) {
+      for (int d = 0; d < 2; d++) {
+        xmn[d] = std::min(xmn[d], x[2 * i + d]);
+        xmx[d] = std::max(xmx[d], x[2 * i + d]);
+      }
+      hmax = std::max(hmax, hsml[i]);
+      if (i < (size_t)D.NN || i >= NT) hmin_nd = std::min(hmin_nd, hsml[i]);
+    }
+    double cell = 2.0 * hmax;
+    double nc = 1.0;
+    for (int d = 0; d < 2; d++) nc *= std::floor((xmx[d] - xmn[d]) / cell + 1.0) + 2.0;
+    int cap = (int)std::min(4.0 * nc + 1024.0, 2.0e9 / 4.0);
+    if (cap > D.cell_cap) {
+      D.cell_cnt = dalloc<int32_t>(c, (size_t)cap + 2);
+      D.cell_start = dalloc<int32_t>(c, (size_t)cap + 2);
+      D.cell_cursor = dalloc<int32_t>(c, (size_t)cap + 2);
+      D.cell_cap = cap;
+      size_t nscan = std::max<size_t>(N2, (size_t)cap + 2);
+      D.scan_tmp = dalloc<int64_t>(c, nscan / 4096 + 64);
+      if (c.graph) {
+        cudaGraphExecDestroy(c.graph);
+        c.graph = nullptr;
+      }
+    }
+    // neighbour capacities: one species holds about pi (scale_k h / dx)^2 partners in the
+    // support; 2x headroom plus the wall rows.  max_neighbours (total per particle) raises
+    // or lowers the per-list capacity explicitly.
+    {
+      double rs = (double)D.scale_k * hmax / c.p.dx;
+      int est = (int)std::ceil(2.0 * M_PI * rs * rs) + 8;
+      int cap = c.p.max_neighbours > 0 ? std::max(4, c.p.max_neighbours / 2) : std::max(48, est);
+      if (cap != D.capH) {
+        D.half = dalloc<int4>(c, N2 * (size_t)cap);
+        D.cross = dalloc<int4>(c, N2 * (size_t)cap);
+        D.same = dalloc<int4>(c, N2 * (size_t)cap);
+        D.capH = D.capC = D.capS = cap;
+        if (c.graph) {
+          cudaGraphExecDestroy(c.graph);
+          c.graph = nullptr;
+        }
+      }
+    }
+    // node-wall boundary force can use the pair lists when every node-dummy pair closer
+    // than 0.75 dx is inside the kernel support
+    D.bound_from_lists = ((double)D.scale_k * hmin_nd > 0.76 * D.dx) ? 1 : 0;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  c.uploaded = true;
+  return SPS_OK;
+}
+
+int sps_upload_bcs(sps_ctx* h, const int32_t* bc_or_not, const int32_t* bc_info) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  try {
+    const size_t NT = c.d.NT;
+    if (bc_or_not)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(c.d.bc_or_not, bc_or_not, sizeof(int32_t) * NT, cudaMemcpyHostToDevice, c.stream));
+    if (bc_info) {
+      for (size_t i = 0; i < NT; i++)
+        for (int r = 2; r < 7; r++) {
+          int b = bc_info[8 * i + r];
+          if (b < 0 || b > c.p.no_bcs)
+            return fail(&c, SPS_ERR_ARG, "sps_upload_bcs: bc_info refers to a missing BC");
+        }
+      SPS_CUDA_CHECK(cudaMemcpyAsync(c.d.bc_info, bc_info, sizeof(int32_t) * 8 * NT, cudaMemcpyHostToDevice, c.stream));
+    }
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
+  if (!h || !time_sph || nsteps < 0) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!c.uploaded) return fail(&c, SPS_ERR_STATE, "sps_step before sps_upload");
+  if (nsteps == 0) return SPS_OK;
+  try {
+    double t = *time_sph;
+    int done = 0;
+    while (done < nsteps) {
+      int chunk = std::min(nsteps - done, 4096);
+      ensure_scal(c, chunk);
+      c.h_scal.resize(chunk);
+      for (int k = 0; k < chunk; k++) {
+        fill_scalars(c, t, c.h_scal[k]);
+        t = t + c.p.dt_sph;
+      }
+      SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(), sizeof(sps::StepScalars) * chunk,
+                                     cudaMemcpyHostToDevice, c.stream));
+      SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
+      if (c.use_graph) {
+        if (!c.graph) build_graph(c);
+        for (int k = 0; k < chunk; k++) SPS_CUDA_CHECK(cudaGraphLaunch(c.graph, c.stream));
+      } else {
+        for (int k = 0; k < chunk; k++) {
+          if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
+          else sps::launch_fast_step(c);
+        }
+      }
+      done += chunk;
+    }
+    int nb = (c.d.NT + kBlock - 1) / kBlock;
+    k_check_finite<<<nb, kBlock, 0, c.stream>>>(c.d);
+    SPS_CUDA_CHECK(cudaGetLastError());
+    SPS_CUDA_CHECK(cudaMemcpyAsync(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    c.steps_done += nsteps;
+    *time_sph = t;
+    int e = *c.h_err;
+    if (e) {
+      SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
+      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+      if (e & (1 << 20)) return fail(&c, SPS_ERR_NONFINITE, err_text(e));
+      return fail(&c, SPS_ERR_CAPACITY, err_text(e));
+    }
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_download(sps_ctx* h, double* x, double* vel, double* stress, double* rho,
+                 double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  sps::Dev& D = c.d;
+  const size_t N2 = D.N2, NT = D.NT, NN = D.NN;
+  try {
+    double* stage = c.stage;
+    int nb = (int)((N2 + kBlock - 1) / kBlock);
+    auto down2 = [&](double* dst, const double* a, const double* b, size_t n) {
+      k_soa_to_aos2<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, c.stream>>>(stage, a, b, (int)n);
+      SPS_CUDA_CHECK(cudaMemcpyAsync(dst, stage, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c.stream));
+      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    };
+    if (x) down2(x, D.px, D.py, N2);
+    if (vel) down2(vel, D.vx, D.vy, N2);
+    if (displ) down2(displ, D.dispx, D.dispy, NN);
+    if (stress) {
+      k_soa_to_aos4<<<nb, kBlock, 0, c.stream>>>(stage, D.s0, D.s1, D.s2, D.s3, (int)N2);
+      SPS_CUDA_CHECK(cudaMemcpyAsync(stress, stage, sizeof(double) * 4 * N2, cudaMemcpyDeviceToHost, c.stream));
+    }
+    if (rho) SPS_CUDA_CHECK(cudaMemcpyAsync(rho, D.rho, sizeof(double) * N2, cudaMemcpyDeviceToHost, c.stream));
+    if (intvars1)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(intvars1, D.iv1, sizeof(double) * NT, cudaMemcpyDeviceToHost, c.stream));
+    if (bc_or_not)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(bc_or_not, D.bc_or_not, sizeof(int32_t) * NT, cudaMemcpyDeviceToHost, c.stream));
+    if (f_drucker)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(f_drucker, D.fdp, sizeof(double) * NT, cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    if (stress) {
+      // dummy stress is pair-local in the reference; report zero like its RK4 clear (:690)
+      for (size_t i = NT; i < N2; i++)
+        for (int k = 0; k < 4; k++) stress[4 * i + k] = 0.0;
+    }
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_dump_pairs(sps_ctx* h, int32_t* pair_i, int32_t* pair_j, int32_t* pint_type, float* w,
+                   float* dwdx, float* dwdy, int64_t* npairs) {
+  if (!h || !npairs) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  sps::Dev& D = c.d;
+  try {
+    sps::PairMeta meta;
+    SPS_CUDA_CHECK(cudaMemcpy(&meta, D.meta, sizeof(meta), cudaMemcpyDeviceToHost));
+    if (!pair_i) {
+      *npairs = meta.n;
+      return SPS_OK;
+    }
+    if (*npairs < meta.n) return fail(&c, SPS_ERR_CAPACITY, "sps_dump_pairs: buffer too small");
+    const size_t N2 = D.N2;
+    std::vector<int32_t> cnt(N2), sorted(N2), itype(N2);
+    std::vector<int4> half(N2 * D.capH);
+    SPS_CUDA_CHECK(cudaMemcpy(cnt.data(), D.half_cnt, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost));
+    SPS_CUDA_CHECK(cudaMemcpy(sorted.data(), D.sorted, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost));
+    SPS_CUDA_CHECK(cudaMemcpy(itype.data(), D.itype, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost));
+    SPS_CUDA_CHECK(cudaMemcpy(half.data(), D.half, sizeof(int4) * N2 * D.capH, cudaMemcpyDeviceToHost));
+    // creation order
+    std::vector<int32_t> ci, cj, ct;
+    std::vector<float> cw, cx, cy;
+    ci.reserve(meta.n);
+    for (size_t s = 0; s < N2; s++)
+      for (int k = 0; k < cnt[s]; k++) {
+        const int4 e = half[s * D.capH + k];
+        int a = sorted[s], b = sorted[e.x];
+        float ww, gx, gy;
+        std::memcpy(&ww, &e.y, 4);
+        std::memcpy(&gx, &e.z, 4);
+        std::memcpy(&gy, &e.w, 4);
+        int ta = itype[a], tb = itype[b];
+        int ia = std::abs(ta), ib = std::abs(tb);
+        // Pint_Update orientation (3_SPH_material_2018.f90:1599-1614)
+        if ((ia == 2 && ib == 1) || (ia == 2 && ib == 25) || (ia == 1 && ib == 25)) {
+          std::swap(a, b);
+          gx = -gx;
+          gy = -gy;
+        }
+        int sum = ta + tb;
+        int t = sum == 3 ? 1 : sum == 2 ? 2 : sum == 4 ? 3 : sum == 27 ? 6 : sum == 26 ? 9 : 0;
+        ci.push_back(a + 1);
+        cj.push_back(b + 1);
+        ct.push_back(t);
+        cw.push_back(ww);
+        cx.push_back(gx);
+        cy.push_back(gy);
+      }
+    int64_t n = (int64_t)ci.size(), m = meta.m_prev, k = 0;
+    auto put = [&](int64_t q) {
+      pair_i[k] = ci[q];
+      pair_j[k] = cj[q];
+      if (pint_type) pint_type[k] = ct[q];
+      if (w) w[k] = cw[q];
+      if (dwdx) dwdx[k] = cx[q];
+      if (dwdy) dwdy[k] = cy[q];
+      k++;
+    };
+    for (int64_t a = n - 1; a >= m; a--) put(a);
+    for (int64_t a = 0; a < std::min(n, m); a++) put(a);
+    *npairs = n;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_kernels_per_step(sps_ctx* h, int32_t* n) {
+  if (!h || !n) return SPS_ERR_ARG;
+  try {
+    if (!h->c.graph) build_graph(h->c);
+  } catch (const std::exception& e) {
+    return fail(&h->c, SPS_ERR_CUDA, e.what());
+  }
+  *n = h->c.kernels_per_step;
+  return SPS_OK;
+}
+
+int sps_get_stream(sps_ctx* h, void** stream) {
+  if (!h || !stream) return SPS_ERR_ARG;
+  *stream = (void*)h->c.stream;
+  return SPS_OK;
+}
+
+int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, int32_t names_len,
+                     double* ms, int32_t* launches, int32_t cap, int32_t* nkernels) {
+  if (!h || !time_sph || nsteps <= 0 || !names || !ms || !launches || !nkernels)
+    return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!c.uploaded) return fail(&c, SPS_ERR_STATE, "sps_profile_step before sps_upload");
+  std::vector<std::string> kn;
+  std::vector<double> kms;
+  std::vector<int> kl;
+  try {
+    double t = *time_sph;
+    ensure_scal(c, nsteps);
+    c.h_scal.resize(nsteps);
+    for (int k = 0; k < nsteps; k++) {
+      fill_scalars(c, t, c.h_scal[k]);
+      t = t + c.p.dt_sph;
+    }
+    SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(), sizeof(sps::StepScalars) * nsteps,
+                                   cudaMemcpyHostToDevice, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
+    c.profiling = true;
+    for (int k = 0; k < nsteps; k++) {
+      if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
+      else sps::launch_fast_step(c);
+      c.mark("end");
+    }
+    c.profiling = false;
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    SPS_CUDA_CHECK(cudaGetLastError());
+    for (size_t k = 0; k + 1 < c.prof_events.size(); k++) {
+      const char* nm = c.prof_events[k].first;
+      if (std::strcmp(nm, "end") == 0) continue;
+      float e = 0.0f;
+      cudaEventElapsedTime(&e, c.prof_events[k].second, c.prof_events[k + 1].second);
+      size_t q = 0;
+      while (q < kn.size() && kn[q] != nm) q++;
+      if (q == kn.size()) {
+        kn.push_back(nm);
+        kms.push_back(0.0);
+        kl.push_back(0);
+      }
+      kms[q] += e;
+      kl[q] += 1;
+    }
+    for (auto& pe : c.prof_events) cudaEventDestroy(pe.second);
+    c.prof_events.clear();
+    SPS_CUDA_CHECK(cudaMemcpy(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost));
+    *time_sph = t;
+    c.steps_done += nsteps;
+  } catch (const std::exception& e) {
+    c.profiling = false;
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  int n = (int)std::min<size_t>(kn.size(), (size_t)cap);
+  size_t off = 0;
+  for (int k = 0; k < n; k++) {
+    size_t L = kn[k].size() + 1;
+    if (off + L <= (size_t)names_len) {
+      std::memcpy(names + off, kn[k].c_str(), L);
+      off += L;
+    }
+    ms[k] = kms[k];
+    launches[k] = kl[k];
+  }
+  *nkernels = n;
+  if (*c.h_err) {
+    int e = *c.h_err;
+    cudaMemset(c.d.err, 0, sizeof(int));
+    return fail(&c, SPS_ERR_CAPACITY, err_text(e));
+  }
+  return SPS_OK;
+}
+
+int sps_last_error(sps_ctx* h, char* buf, int32_t len) {
+  std::string m;
+  if (h) m = h->c.last_error;
+  else {
+    std::lock_guard<std::mutex> g(g_err_mu);
+    m = g_create_error;
+  }
+  if (buf && len > 0) std::snprintf(buf, (size_t)len, "%s", m.c_str());
+  return (int)m.size();
+}
+
+void sps_destroy(sps_ctx* h) {
+  if (!h) return;
+  sps::Ctx& c = h->c;
+  if (c.graph) cudaGraphExecDestroy(c.graph);
+  for (void* p : c.allocs) cudaFree(p);
+  if (c.h_err) cudaFreeHost(c.h_err);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  delete h;
+}
+
+}  // extern "C"

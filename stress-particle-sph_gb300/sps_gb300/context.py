@@ -1,0 +1,184 @@
+"""Python binding of the step C-ABI (include/sps.h).
+
+`StepContext` is generic over the library prefix so that the same class drives the GPU
+library (libsps_gb300.so, prefix "sps") and, in the tests, the CPU oracle (prefix "orc").
+`Solver` is the GPU entry point a user calls: it mirrors the reference's
+`time_integration` (code/2_SPH_main_2018.f90:78) -- one call advances one step.
+"""
+import ctypes as C
+import numpy as np
+
+from . import _abi
+from . import build as _build
+
+_GPU = None
+
+
+def gpu_lib():
+    """Load libsps_gb300.so; raises if it has not been built (no silent fallback)."""
+    global _GPU
+    if _GPU is None:
+        lib = C.CDLL(_build.lib_path("libsps_gb300.so"))
+        _abi.declare_step_api(lib, "sps")
+        lib.sps_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_int32]
+        lib.sps_last_error.restype = C.c_int
+        lib.sps_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        lib.sps_kernels_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        lib.sps_profile_step.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
+                                         C.c_char_p, C.c_int32, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]
+        _GPU = lib
+    return _GPU
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32)) if a is not None else None
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+class SpsError(RuntimeError):
+    def __init__(self, where, rc, msg=""):
+        super().__init__("%s failed: %s (%d) %s" % (where, _abi.ERR_NAMES.get(rc, "?"), rc, msg))
+        self.rc = rc
+
+
+class StepContext:
+    def __init__(self, lib, prefix, params):
+        self._lib = lib
+        self._pre = prefix
+        self._h = C.c_void_p()
+        self.params = params
+        rc = self._call("create", C.byref(params), C.byref(self._h))
+        self.nnode = params.nnode
+        self.ntotal = params.nnode + params.nstress
+        self.ntotal2 = self.ntotal + params.ndummy
+
+    def _fn(self, name):
+        return getattr(self._lib, self._pre + "_" + name)
+
+    def _err(self):
+        if self._pre != "sps":
+            return ""
+        buf = C.create_string_buffer(1024)
+        self._lib.sps_last_error(self._h if self._h else None, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def _call(self, name, *args):
+        rc = self._fn(name)(*args)
+        if rc != _abi.SPS_OK:
+            raise SpsError(self._pre + "_" + name, rc, self._err())
+        return rc
+
+    def upload(self, x, vel, stress, mass, rho, hsml, itype, intvars1=None, f_drucker=None,
+               x00=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, vel, stress, mass, rho, hsml)]
+        it = np.ascontiguousarray(itype, dtype=np.int32)
+        iv = None if intvars1 is None else np.ascontiguousarray(intvars1, dtype=np.float64)
+        fd = None if f_drucker is None else np.ascontiguousarray(f_drucker, dtype=np.float64)
+        x0 = None if x00 is None else np.ascontiguousarray(x00, dtype=np.float64)
+        self._call("upload", self._h, *[_dp(a) for a in arrs], _ip(it), _dp(iv), _dp(fd), _dp(x0))
+
+    def upload_bcs(self, bc_or_not, bc_info):
+        b = np.ascontiguousarray(bc_or_not, dtype=np.int32)
+        i = np.ascontiguousarray(bc_info, dtype=np.int32)
+        self._call("upload_bcs", self._h, _ip(b), _ip(i))
+
+    def upload_problem(self, prob):
+        s = prob.state()
+        self.upload(**s)
+        self.upload_bcs(prob.bc_or_not, prob.bc_info)
+
+    def step(self, nsteps, time_sph):
+        t = C.c_double(time_sph)
+        self._call("step", self._h, int(nsteps), C.byref(t))
+        return t.value
+
+    def download(self):
+        n2, nt, nn = self.ntotal2, self.ntotal, self.nnode
+        out = dict(x=np.empty(2 * n2), vel=np.empty(2 * n2), stress=np.empty(4 * n2),
+                   rho=np.empty(n2), intvars1=np.empty(nt), displ=np.empty(2 * nn),
+                   bc_or_not=np.empty(nt, np.int32), f_drucker=np.empty(nt))
+        self._call("download", self._h, _dp(out["x"]), _dp(out["vel"]), _dp(out["stress"]),
+                   _dp(out["rho"]), _dp(out["intvars1"]), _dp(out["displ"]),
+                   _ip(out["bc_or_not"]), _dp(out["f_drucker"]))
+        return out
+
+    def dump_pairs(self):
+        n = C.c_int64(0)
+        N = None
+        self._call("dump_pairs", self._h, N, N, N, N, N, N, C.byref(n))
+        k = n.value
+        pi = np.empty(k, np.int32)
+        pj = np.empty(k, np.int32)
+        pt = np.empty(k, np.int32)
+        w = np.empty(k, np.float32)
+        dx = np.empty(k, np.float32)
+        dy = np.empty(k, np.float32)
+        self._call("dump_pairs", self._h, _ip(pi), _ip(pj), _ip(pt), _fp(w), _fp(dx), _fp(dy),
+                   C.byref(n))
+        return dict(pair_i=pi, pair_j=pj, pint_type=pt, w=w, dwdx=dx, dwdy=dy)
+
+    def close(self):
+        if self._h and self._h.value:
+            self._fn("destroy")(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def stream_of(ctx):
+    """cudaStream_t (as int) of a GPU context."""
+    p = C.c_void_p()
+    ctx._call("get_stream", ctx._h, C.byref(p))
+    return p.value or 0
+
+
+def kernels_per_step(ctx):
+    n = C.c_int32(0)
+    ctx._call("kernels_per_step", ctx._h, C.byref(n))
+    return n.value
+
+
+def profile_steps(ctx, nsteps, time_sph):
+    """Run nsteps with per-kernel CUDA events; returns (time_sph, {kernel: (ms, launches)})."""
+    cap = 64
+    names = C.create_string_buffer(4096)
+    ms = (C.c_double * cap)()
+    nl = (C.c_int32 * cap)()
+    nk = C.c_int32(0)
+    t = C.c_double(time_sph)
+    ctx._call("profile_step", ctx._h, int(nsteps), C.byref(t), names, 4096, ms, nl, cap,
+              C.byref(nk))
+    raw = names.raw.split(b"\0")
+    out = {}
+    for k in range(nk.value):
+        out[raw[k].decode()] = (ms[k], nl[k])
+    return t.value, out
+
+
+class Solver(StepContext):
+    """GPU step context.  `time_integration()` advances one step like the reference."""
+
+    def __init__(self, problem, precision=_abi.SPS_PREC_FP64_PLAIN, **param_overrides):
+        self.problem = problem
+        p = problem.params_copy(precision=precision, **param_overrides)
+        super().__init__(gpu_lib(), "sps", p)
+        self.upload_problem(problem)
+        self.time_sph = 0.0
+        self.itimestep_sph = 0
+
+    def time_integration(self, nsteps=1):
+        self.time_sph = self.step(nsteps, self.time_sph)
+        self.itimestep_sph += nsteps
+        return self.time_sph

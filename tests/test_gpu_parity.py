@@ -1,0 +1,126 @@
+"""GPU parity: the CUDA FP64 plain path against the CPU oracle, through the C-ABI.
+
+The plain path sums every neighbour term in the reference's linked-list walk order and
+repeats its FP32 roundings, so it must equal the oracle bit for bit (tolerance 0) on every
+downloaded field, step after step.
+"""
+import numpy as np
+import pytest
+
+import cases
+import orc
+import sps_gb300
+from sps_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_ctx(problem, **over):
+    p = problem.params_copy(precision=_abi.SPS_PREC_FP64_PLAIN, **over)
+    return sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", p)
+
+
+def _orc_ctx(problem, **over):
+    return orc.context(problem.params_copy(**over))
+
+
+def _compare(problem, nsteps, chunks=None, pairs=True, **over):
+    g = _gpu_ctx(problem, **over)
+    o = _orc_ctx(problem, **over)
+    tg, to = cases.run_pair(problem, nsteps, [g, o], chunks)
+    assert tg == to
+    if pairs:
+        pg, po = g.dump_pairs(), o.dump_pairs()
+        for k in ("pair_i", "pair_j", "pint_type"):
+            np.testing.assert_array_equal(pg[k], po[k], err_msg=k)
+        for k in ("w", "dwdx", "dwdy"):
+            np.testing.assert_array_equal(pg[k].view(np.int32), po[k].view(np.int32), err_msg=k)
+    fg, fo = g.download(), o.download()
+    cases.assert_bitwise(fg, fo, problem.ntotal)
+    np.testing.assert_array_equal(fg["bc_or_not"], fo["bc_or_not"])
+    return fg
+
+
+def test_pairs_first_step(built_gpu):
+    p = cases.bui_like()
+    _compare(p, 1)
+
+
+def test_bui_like_steps(built_gpu):
+    # cohesive Drucker-Prager block, XSPH, artificial viscosity, wall dummies
+    p = cases.bui_like()
+    f = _compare(p, 10, chunks=[1, 2, 7])
+    assert np.isfinite(f["stress"]).all()
+
+
+def test_bui_like_finer_trapezoid(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.02, xsph=False, alpha=0.0, beta=0.0,
+                       dt=4e-5)
+    _compare(p, 25, chunks=[5, 20])
+
+
+def test_column_k0(built_gpu):
+    # granular column with a K0 stress state (plastic from the first return on)
+    p = cases.column(dx=0.004)
+    _compare(p, 30, chunks=[10, 20])
+
+
+def test_cspm_cont_density(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05, cspm=True, cont_density=True, sle=2,
+                       dt=5e-5)
+    _compare(p, 12, chunks=[4, 8])
+
+
+def test_plane_stress_quintic(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.6, dx=0.05, skf=3, ntype_solid=1, dt=5e-5)
+    _compare(p, 8)
+
+
+def test_boundary_conditions(built_gpu):
+    p = cases.bc_case()
+    _compare(p, 20, chunks=[7, 13])
+    p = cases.bc_case(plastic=True, cspm=False, xsph=True)
+    _compare(p, 20, chunks=[20])
+
+
+def test_standard_sph(built_gpu):
+    p = cases.standard_sph()
+    _compare(p, 6)
+
+
+def test_gauss_kernel_close(built_gpu):
+    # skf = 2 calls exp(): CUDA's and the host libm's may differ in the last bit, so this
+    # case is compared with a relative tolerance of 1e-10 instead of bitwise
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05, skf=2, dt=5e-5)
+    g = _gpu_ctx(p)
+    o = _orc_ctx(p)
+    cases.run_pair(p, 5, [g, o])
+    fg, fo = g.download(), o.download()
+    for k in ("x", "vel", "stress"):
+        a, b = fg[k], fo[k]
+        scale = np.abs(b).max() + 1e-300
+        assert np.abs(a - b).max() <= 1e-10 * scale, k
+
+
+def test_capacity_error(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
+    g = _gpu_ctx(p, max_neighbours=16)
+    g.upload_problem(p)
+    with pytest.raises(sps_gb300.SpsError) as e:
+        g.step(1, 0.0)
+    assert e.value.rc == _abi.SPS_ERR_CAPACITY
+
+
+def test_unsupported_options(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
+    for over in (dict(art_stress=1), dict(ifsigman=1), dict(inside_approach=0), dict(skf=7)):
+        with pytest.raises(sps_gb300.SpsError):
+            _gpu_ctx(p, **over)
+
+
+def test_step_before_upload(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
+    g = _gpu_ctx(p)
+    with pytest.raises(sps_gb300.SpsError) as e:
+        g.step(1, 0.0)
+    assert e.value.rc == _abi.SPS_ERR_STATE

@@ -1,0 +1,145 @@
+"""The host-side reader / particle generator (CPU only).
+
+Every input set of the reference's examples must parse, and the generated counts, masses
+and dummy layout must follow the reference's formulas
+(example_problems/soil_failure_bui_et_al_2008/3_SPH_material_2018.f90:431-461, :682-733,
+:795-879).  The example inputs are read from the reference checkout when it is present.
+"""
+import glob
+import math
+import os
+
+import numpy as np
+import pytest
+
+import cases
+import sps_gb300
+
+REF = "/root/reference/example_problems"
+
+
+def example_dirs():
+    if not os.path.isdir(REF):
+        return []
+    # input sets are the directories holding input.txt next to a .dat and a .pts file
+    return sorted(os.path.dirname(p) for p in glob.glob(REF + "/**/input.txt", recursive=True)
+                  if glob.glob(os.path.join(os.path.dirname(p), "*.dat")))
+
+
+@pytest.mark.parametrize("d", example_dirs() or [None])
+def test_reference_inputs_parse(built, d):
+    if d is None:
+        pytest.skip("reference example inputs not present on this machine")
+    p = sps_gb300.Problem.from_dir(d)
+    par = p.params
+    assert par.nnode > 0 and p.ntotal2 >= p.ntotal
+    assert len(p.blocks) >= 1 and p.blocks[0]["dt"] > 0
+
+
+def test_bui_counts_and_masses(built):
+    # the Drucker-Prager example's layout: 4 x 2 m block at dx 0.1, inside approach
+    p = cases.bui_like()
+    ndivx, ndivy = int(4.0 / 0.1 + 1.0), int(2.0 / 0.1 + 1.0)
+    assert p.nnode == ndivx * ndivy == 861
+    assert p.nstress == (ndivx - 1) * (ndivy - 1) == 800
+    # walls: LHS (-0.1 .. 2.1) and floor (-0.3 .. 9) at FP32 spacing, three rows each
+    f = np.float32
+    nd = int((f(2.1) - f(-0.1)) / f(0.1) + f(1.0)) + int((f(9.0) - f(-0.3)) / f(0.1) + f(1.0))
+    assert p.params.ndummy2 == nd and p.params.ndummy == 3 * nd
+    rho, dx = 1850.0, 0.1
+    area = ((rho * dx) * dx) / 8.0
+    m = p.mass
+    X = p.x.reshape(-1, 2)
+    nn = p.nnode
+    corner = [k for k in range(nn) if X[k, 0] in (0.0, 4.0) and X[k, 1] in (0.0, 2.0)]
+    assert all(m[k] == 2 * area for k in corner)
+    interior = (X[:nn, 0] > 0) & (X[:nn, 0] < 4.0) & (X[:nn, 1] < 2.0)
+    assert np.all(m[:nn][interior] == 8 * area)  # bottom row counts as interior (:522-526)
+    assert np.all(m[nn:p.ntotal] == 8 * area)
+    # stress-points at the cell centres, offset by dx/2 in both directions (:567-568)
+    Xs = X[nn:p.ntotal]
+    assert np.allclose(Xs[:, 0] % dx, dx / 2) and np.allclose(Xs[:, 1] % dx, dx / 2)
+    # dummy coordinates are FP32 values and masses FP32 dx^2 * rho
+    Xd = X[p.ntotal:]
+    assert np.all(Xd == Xd.astype(np.float32).astype(np.float64))
+    assert np.all(m[p.ntotal:] == float(np.float32(dx) * np.float32(dx)) * rho)
+    # the innermost layer comes first and carries its wall's position
+    wp = p.wall_position[p.ntotal:p.ntotal + p.params.ndummy2]
+    assert np.all(wp == np.float32(-0.1))
+
+
+def test_elastic_constants(built):
+    p = cases.bui_like()
+    E, nu = 1.8e6, 0.3
+    K = E / (3 * (1 - 2 * nu))
+    G = E / (2 * (1 + nu))
+    assert p.params.D11 == float(np.float32(4.0) / np.float32(3.0)) * G + K
+    assert p.params.D12 == -(float(np.float32(2.0) / np.float32(3.0)) * G) + K
+    assert p.params.D33 == G
+    assert p.params.pi == float(np.float32(math.pi))
+
+
+def test_boundary_condition_tables(built):
+    p = cases.bc_case()
+    par = p.params
+    assert par.no_bcs == 6
+    bl = np.ctypeslib.as_array(par.bc_list, shape=(8 * par.no_bcs,)).reshape(-1, 8)
+    twopi = np.float32(np.float32(math.acos(0.0)) * np.float32(4.0)) / np.float32(360.0)
+    assert bl[2, 6] == 30.0 * float(twopi)
+    info = p.bc_info.reshape(-1, 8)
+    X = p.x.reshape(-1, 2)
+    left = np.nonzero(X[:p.ntotal, 0] == 0.0)[0]
+    assert np.all(p.bc_or_not[left] == 1)
+    assert np.all(info[left, 1] >= 2)
+    # the nodal BC lands in the row of its variable (bc_var + 2)
+    node = 2 * (int(round(1.0 / 0.05)) + 1) + 5 - 1
+    assert info[node, 3] == 6 and p.bc_or_not[node] == 1
+
+
+def test_conflicting_nodal_bc_is_an_error(built):
+    inp, dat, pts = _bc_texts()
+    bad = dat.replace("nber of nodes with BCs\n0", "nber of nodes with BCs\n2\nnode bc\n1 1\n1 4")
+    with pytest.raises(ValueError):
+        sps_gb300.Problem.from_text(inp, bad, pts)
+
+
+def _bc_texts():
+    pts = "geom_type\n1\nx\n0 0.2 0 0.2 0.05\ny\n0 0 0.2 0.2 0.05\ndummy\nF\n"
+    dat = ("1\nt\nndimn\n2\nh\n2 4 1\nm\n1 1 12 1e7 0.3 1. 2000 1 0 0 1 1 1\nt\n0.5 0 0 0 0 0 0 0\n"
+           "ic\n0\nBC\n4 0\nbc\n1 5 1 0 0 0 0 0\n2 6 1 0 0 0 0 0\n3 1 1 0 0 0 0 0\n4 5 1 1 0 0 0 0\n"
+           "seg\n0\nnber of nodes with BCs\n0\nic_tcurve\n1\nn\n1 10\np\n2\nt\n0 1\n1 1\n"
+           "dom\n-1 -1 1 1\nIC\n2\na\n0\nb\n0\nc\n0\nd\n0\ne\n0\nf\n0\nflags\n2 2 1 1 F T F\n"
+           "d\nF F\ndamp\n0\nab\n0 0\ng\n0\no\nx\n1 1 1 1 1 1 1 0 0 0\n")
+    inp = ("p\nt\nf\nT F F\ni\nT\nn\n1\ns\n1.2\nt\n1e-5,1,10\np\n1,1,1\ne\n-1,1,1\n")
+    return inp, dat, pts
+
+
+def test_reader_errors(built):
+    inp, dat, pts = _bc_texts()
+    with pytest.raises(ValueError):
+        sps_gb300.Problem.from_text(inp, dat[:200], pts)  # truncated .dat
+    with pytest.raises(ValueError):
+        sps_gb300.Problem.from_text(inp, dat.replace("2 2 1 1 F T F", "2 2 1 x F T F"), pts)
+
+
+def test_column_k0(built):
+    p = cases.column(dx=0.004)
+    st = p.stress.reshape(-1, 4)[:p.ntotal]
+    X = p.x.reshape(-1, 2)[:p.ntotal]
+    depth = np.maximum(0.10 - X[:, 1], 0)
+    assert np.allclose(st[:, 1], -2650 * 9.81 * depth)
+    assert np.allclose(st[:, 0], 0.5 * st[:, 1]) and np.all(st[:, 2] == 0)
+
+
+def test_slope_generator(built):
+    # extents are snapped to the lattice; these are multiples of dx
+    p = sps_gb300.Problem.slope(Lf=2.0, Hf=0.5, Ls=0.45, Hs=1.0, dx=0.05)
+    X = p.x.reshape(-1, 2)
+    nn = p.nnode
+    # the slope block sits on the foundation with a vertical face at x = Ls
+    above = X[:nn, 1] > 0.5 + 1e-9
+    assert np.all(X[:nn][above, 0] <= 0.45 + 1e-9) and above.any()
+    # total mass equals rho * area (each node a quarter cell per adjacent cell)
+    area = 2.0 * 0.5 + 0.45 * 1.0
+    assert abs(p.mass[:nn].sum() - 1850.0 * area) < 1e-6 * 1850 * area
+    assert abs(p.mass[nn:p.ntotal].sum() - 1850.0 * area) < 1e-6 * 1850 * area
