@@ -98,6 +98,8 @@ def test_gauss_kernel_close(built_gpu):
     fg, fo = g.download(), o.download()
     for k in ("x", "vel", "stress"):
         a, b = fg[k], fo[k]
+        if k == "stress":
+            a, b = a[:4 * p.ntotal], b[:4 * p.ntotal]
         scale = np.abs(b).max() + 1e-300
         assert np.abs(a - b).max() <= 1e-10 * scale, k
 
