@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="plain", choices=["plain"])
+    ap.add_argument("--precision", default="fast", choices=["plain", "fast"])
     ap.add_argument("--dx", type=float, default=0.012)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -166,9 +166,16 @@ def workload_name(prob, dx):
 
 # algorithmic bytes per target entry / particle for the roofline of each kernel class
 # (FP64 plain layout): a neighbour entry is 16 B; per-particle state is counted once.
-def kernel_bytes(name, prob, deg):
+def kernel_bytes(name, prob, deg, fast=False):
     nn, ns, n2 = prob.nnode, prob.nstress, prob.ntotal2
     ent = 16.0
+    if fast and name == "derivs":
+        # entries + one 16 B record per neighbour-visible particle + per-particle FP64
+        # state read/written once (SP: v, s, grad_u, RHS1, RKs, fdp, RKd; node: v, RHS2, RKv)
+        return ent * deg["cross"] + ent * deg["same_nodes"] + 16 * (nn + ns) + \
+            ns * (16 + 32 + 32 + 32 + 64 + 16 + 16) + nn * (16 + 16 + 32 + 16)
+    if fast and name == "interp":
+        return ent * deg["cross"] + 16 * nn + 32 * ns + ns * 16 + nn * 40
     if name == "derivs":
         # entries + SP (v,s,m,rho,grad_u w, RHS1 w, RKs rw, fdp rw, RKd rw) + node terms
         return ent * deg["cross"] + ns * (16 + 32 + 16 + 32 + 32 + 64 + 16 + 16) + \
@@ -182,6 +189,35 @@ def kernel_bytes(name, prob, deg):
     return None
 
 
+def timed_steps(ctx, nsteps, t, dist, local):
+    """Device time (ms, max over ranks) of nsteps graph-launched steps on the context's
+    own stream; clocks sampled meanwhile."""
+    import torch
+    import sps_gb300
+    stream = torch.cuda.ExternalStream(sps_gb300.stream_of(ctx))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0.record(stream)
+    t = ctx.step(nsteps, t)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms = reduce_max(dist, e0.elapsed_time(e1), device="cuda")
+    return t, ms, clk
+
+
+def rel_errors(a, b):
+    import numpy as np
+    d = a - b
+    return (float(np.linalg.norm(d) / max(np.linalg.norm(b), 1e-300)),
+            float(np.abs(d).max() / max(np.abs(b).max(), 1e-300)))
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -193,51 +229,61 @@ def run_ours(args):
     torch.cuda.set_device(local)
     sps_gb300.build_all()
     prob = workload(args.dx)
-    prec = _abi.SPS_PREC_FP64_PLAIN
-    params = prob.params_copy(precision=prec)
-    ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", params)
-    ctx.upload_problem(prob)
     nparticles = prob.nnode + prob.nstress
-    t = 0.0
-    t = ctx.step(max(args.warmup, 1), t)  # warm-up (also instantiates the step graph)
+    fast = args.precision == "fast"
+    prec = _abi.SPS_PREC_FP32_FAST if fast else _abi.SPS_PREC_FP64_PLAIN
+    ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", prob.params_copy(precision=prec))
+    ctx.upload_problem(prob)
+    t = ctx.step(max(args.warmup, 1), 0.0)  # warm-up (also instantiates the step graph)
     kps = sps_gb300.kernels_per_step(ctx)
-    stream = torch.cuda.ExternalStream(sps_gb300.stream_of(ctx))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = Clocks(local)
-    barrier(dist)
-    torch.cuda.synchronize()
-    clocks.start()
-    e0.record(stream)
-    t = ctx.step(args.steps, t)
-    e1.record(stream)
-    e1.synchronize()
-    clk = clocks.stop()
-    torch.cuda.synchronize()
-    barrier(dist)
-    ms = e0.elapsed_time(e1)
-    ms_max = reduce_max(dist, ms, device="cuda")
+    t, ms_max, clk = timed_steps(ctx, args.steps, t, dist, local)
     value = nparticles * args.steps * world / (ms_max * 1e-3)
+    nsteps_done = max(args.warmup, 1) + args.steps
+
+    plain = None
+    errors = None
+    if fast:
+        # the FP64 plain form on the same workload, advanced by the same number of steps
+        cp = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                   prob.params_copy(precision=_abi.SPS_PREC_FP64_PLAIN))
+        cp.upload_problem(prob)
+        tp = cp.step(max(args.warmup, 1), 0.0)
+        tp, ms_p, _ = timed_steps(cp, args.steps, tp, dist, local)
+        plain = {"value": round(nparticles * args.steps * world / (ms_p * 1e-3), 1),
+                 "ms_per_step": round(ms_p / args.steps, 4), "dtype": "f64"}
+        ff, fp = ctx.download(), cp.download()
+        nt = prob.ntotal
+        sl2, sli = rel_errors(ff["stress"][:4 * nt], fp["stress"][:4 * nt])
+        vl2, vli = rel_errors(ff["vel"][:2 * nt], fp["vel"][:2 * nt])
+        dl2, dli = rel_errors(ff["displ"], fp["displ"])
+        errors = {"after_steps": nsteps_done, "time_s": t,
+                  "stress_rel_l2": sl2, "stress_rel_linf": sli, "vel_rel_l2": vl2,
+                  "vel_rel_linf": vli, "displ_rel_l2": dl2, "displ_rel_linf": dli,
+                  "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
+        _, prof_p = sps_gb300.profile_steps(cp, 1, tp)
+        plain["kernel_ms_per_step"] = {k: round(v[0], 4) for k, v in sorted(
+            prof_p.items(), key=lambda kv: -kv[1][0])[:6]}
+        cp.close()
 
     # per-kernel profile of two steps (events around every kernel, no graph)
     t, prof = sps_gb300.profile_steps(ctx, 2, t)
-    # neighbour-list statistics for the algorithmic byte counts
     pairs = ctx.dump_pairs()
     pt = np.bincount(pairs["pint_type"], minlength=10)
-    deg = {"cross": 2 * (pt[1]) + pt[6] + pt[9], "same": 2 * (pt[2] + pt[3]),
-           "same_nodes": 2 * pt[3], "pairs": len(pairs["pair_i"])}
-    top = max((k for k in prof if k not in ("end",)), key=lambda k: prof[k][0])
+    deg = {"cross": 2 * int(pt[1]) + int(pt[6] + pt[9]), "same": 2 * int(pt[2] + pt[3]),
+           "same_nodes": 2 * int(pt[3]), "pairs": len(pairs["pair_i"])}
+    top = max(prof, key=lambda k: prof[k][0])
     top_ms, top_n = prof[top]
     per_launch_ms = top_ms / top_n
     peaks, peak_kind = measured_peaks()
-    b = kernel_bytes(top, prob, deg)
+    b = kernel_bytes(top, prob, deg, fast)
     roof = None
     if b is not None:
         ach = b / (per_launch_ms * 1e-3) / 1e9
         roof = {"kernel": "k_" + top, "bound": "hbm", "achieved": round(ach, 1),
                 "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": round(ach / peaks.get("hbm_gbs"), 4), "traffic": None,
-                "peak_kind": peak_kind, "per_launch_ms": round(per_launch_ms, 4),
-                "launches_per_step": top_n / 2,
+                "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(b),
+                "per_launch_ms": round(per_launch_ms, 4), "launches_per_step": top_n / 2,
                 "share_of_step": round(top_ms / sum(v[0] for v in prof.values()), 3)}
     try:
         f64 = fp64_peak_tflops()
@@ -269,7 +315,8 @@ def run_ours(args):
     e2e_s = reduce_max(dist, w1 - w0, device="cuda")
     e2e = {"value": round(nparticles * args.e2e_steps * world / e2e_s, 1),
            "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps}
+           "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+           "path": "sps_upload (pinned host) + sps_step(1) + sps_download, every step"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -280,13 +327,17 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 1), "unit": "particle-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if fast else "f64",
             "data": "synthetic (generated slope geometry, no dataset)",
-            "config": {"workload": workload_name(prob, args.dx), "precision": "fp64_plain",
+            "config": {"workload": workload_name(prob, args.dx),
+                       "precision": ("fp32 neighbour sums (Kahan), fp64 state and stress return"
+                                     if fast else "fp64 plain (reference rounding)"),
                        "particles": nparticles, "pairs": deg["pairs"],
                        "l2": "state and pair tables (%.1f GB) larger than L2; no flush" % (
                            (prob.ntotal2 * (3 * 48 * 16 + 400)) / 1e9),
+                       "surrogate": "not built (exact Drucker-Prager return on every particle)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plain": plain, "error_vs_plain": errors,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
             "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
             "kernel_ms_per_step": {k: round(v[0] / 2, 4) for k, v in sorted(

@@ -146,6 +146,12 @@ int sps_dump_pairs(sps_ctx* ctx, int32_t* pair_i, int32_t* pair_j, int32_t* pint
    counterpart (the reference has no device). */
 int sps_get_stream(sps_ctx* ctx, void** stream);
 
+/* Self-test (no reference counterpart): compare, on the device, the reciprocal-corrected
+   division the step uses for quotients by a particle's density or smoothing length with
+   the IEEE division, on n pseudo-random operand pairs; *mismatches counts results that
+   differ in any bit. */
+int sps_selftest_division(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
+
 /* Number of this library's kernels one step launches (no reference counterpart). */
 int sps_kernels_per_step(sps_ctx* ctx, int32_t* n);
 

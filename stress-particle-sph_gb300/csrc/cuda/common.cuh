@@ -37,6 +37,10 @@ struct Grid {
   int nactive;   // particles in cells (sorted positions below nactive)
   int overflow;  // cells exceeded capacity
   float xr0[2];  // origin of the FP32 prefilter coordinates (= xmin)
+  // every active particle has the same smoothing length h this step: the kernel's
+  // h-only subexpressions are formed once (same operations, same values)
+  int uniform_h;
+  double h, yh, hh, yhh, factor, factor6, c3;
 };
 
 // pair bookkeeping of grid_find_NEW's linked list
@@ -85,6 +89,17 @@ struct Dev {
   double *RKv[2], *RKs[4], *RKr, *RKh, *RKd;
   double *RHS1[4], *RHS2[2], *RHSr, *RHSh;
   double *fbx, *fby;  // boundary force (nodes), once per step
+  double *vol, *rinv;  // m / rho and 1 / rho per particle (refreshed when rho changes)
+  double* A[3];        // sigma_k / (rho * rho) of the stage, per particle
+  // FP32 form: packed neighbour records (written by the per-particle kernels)
+  int fast;
+  // velocities and sigma/rho^2 are double-float pairs (hi = RN32(x), lo = RN32(x - hi)) so
+  // that neighbour differences keep FP64-level accuracy
+  float4* recV;   // {vx_hi, vy_hi, vx_lo, vy_lo}               all particles
+  float4* recS;   // {sxx, syy, sxy, szz}                        nodes + stress-points
+  float4* recI;   // {intvar1, m/rho, rho, m}                    all particles
+  float4* recA;   // {sxx, syy, sxy}/rho^2 (hi), m               nodes + stress-points
+  float4* recAl;  // {sxx, syy, sxy}/rho^2 (lo), 0               nodes + stress-points
   double* Ddev;
   // cells
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
@@ -107,6 +122,24 @@ struct Dev {
   // scan scratch
   int64_t* scan_tmp;
 };
+
+// Correctly rounded a / b given y = RN(1/b), by Markstein's theorem (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990; see also Muller et al., Handbook of Floating-Point Arithmetic, the theorem on
+// FMA-based division): when y is within 1/2 ulp of 1/b and q within 1 ulp of a/b, the
+// corrected q' = RN(q + y * (a - b q)) equals RN(a/b).  q = RN(a y) can be up to 1.5 ulp
+// off, so one correction step brings it within 1 ulp and a second one rounds correctly.
+// Valid for normal operands without overflow or underflow (masses, densities and kernel
+// values here); a zero numerator returns a signed zero.  Bit-for-bit agreement with the
+// IEEE division is checked on the GPU by sps_selftest.
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  if (a == 0.0) return a * y;
+  double q = a * y;
+  double r = fma(-b, q, a);
+  q = fma(r, y, q);
+  r = fma(-b, q, a);
+  return fma(r, y, q);
+}
 
 // ----------------------------------------------------------------------------------------
 // kernel (example_problems/soil_failure_bui_et_al_2008/2_SPH_main_2018.f90:1440-1538).
@@ -161,6 +194,31 @@ __device__ __forceinline__ void sph_kernel(int skf, double pi, double r, double 
       *dw0 = g * (dx0 / r);
       *dw1 = g * (dx1 / r);
     }
+  }
+}
+
+// cubic kernel for a uniform smoothing length: identical results to sph_kernel(1, ...)
+// with the h-only subexpressions taken from g and the divisions by h, h*h and r done by
+// div_rcp with their exact reciprocals
+__device__ __forceinline__ void cubic_uniform(const Grid& g, double r, double dx0, double dx1,
+                                              double* w, double* dw0, double* dw1) {
+  double q = div_rcp(r, g.h, g.yh);
+  *w = 0.0;
+  *dw0 = 0.0;
+  *dw1 = 0.0;
+  if (q >= 0 && q <= 1.0) {
+    const double two_thirds = (double)(2.0f / 3.0f);
+    *w = g.factor * ((two_thirds - q * q) + (q * q * q) / 2.0);
+    double a = div_rcp(g.factor * (-2.0 + 1.5 * q), g.hh, g.yhh);
+    *dw0 = a * dx0;
+    *dw1 = a * dx1;
+  } else if (q > 1.0 && q <= 2.0) {
+    double t = 2.0 - q;
+    *w = g.factor6 * ((t * t) * t);
+    double a = div_rcp(g.c3 * (t * t), g.h, g.yh);
+    double yr = 1.0 / r;
+    *dw0 = -(a * div_rcp(dx0, r, yr));
+    *dw1 = -(a * div_rcp(dx1, r, yr));
   }
 }
 
@@ -265,4 +323,9 @@ struct Ctx;
 int launch_pair_build(Ctx& c);
 int launch_plain_step(Ctx& c);
 int launch_fast_step(Ctx& c);
+void launch_vol(Ctx& c, int lo, int hi);
+void launch_finterp(Ctx& c);
+void launch_fderivs(Ctx& c, int stage);
+void launch_fxsph(Ctx& c);
+void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 }  // namespace sps

@@ -1,15 +1,341 @@
-// fast_step.cu -- FP32 compensated form of the SPS step (placeholder until implemented).
+// fast_step.cu -- neighbour sums of the FP32 form of the SPS step.
+//
+// The FP32 form keeps the particle state, the RK4 update and the stress return in FP64
+// (per-particle work, shared with the plain form through stage_tail.cuh) and moves the
+// neighbour sums -- the O(N x neighbours) part -- to FP32:
+//   * neighbours are read from packed FP32 records written by the per-particle kernels
+//     (recV: velocity as double-float hi/lo pairs, recS: stress, recI {intvar1, m/rho, rho,
+//     m}, recA / recAl: sigma/rho^2 as double-float pairs and m), 16 bytes per field set;
+//   * every sum is Kahan-compensated (Kahan, "Further remarks on reducing truncation
+//     errors", CACM 8(1), 1965), so its error stays at a few FP32 ulps of the result
+//     regardless of the neighbour count;
+//   * differences of nearly equal neighbour values (velocities, sigma/rho^2) are taken in
+//     double-float, and the near-cancelling sums are rearranged so that their terms are
+//     small (see k_finterp and k_fderivs);
+//   * the quotients (G m)/rho and (w m)/rho of the reference are formed as G (m/rho).
+// The pair set is the same exact set as the plain form's; kernel values are evaluated in
+// FP32 (k_half<true>).
 #include <cuda_runtime.h>
 
-#include <stdexcept>
-
 #include "ctx.cuh"
+#include "stage_tail.cuh"
 
 namespace sps {
 
-int launch_fast_step(Ctx& c) {
-  (void)c;
-  throw std::runtime_error("the FP32 fast form is not implemented yet");
+namespace {
+
+constexpr int kBlock = 256;
+
+struct Kahan {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double val() const { return (double)s - (double)c; }
+};
+
+// sum of exact FP32 products: p = RN(a b) and e = a b - p (exact, by one FMA: the
+// error-free product transformation of Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26(6), 2005); p is Kahan-summed, e summed plainly
+struct ProdSum {
+  Kahan hi;
+  float lo = 0.0f;
+  __device__ __forceinline__ void add(float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    hi.add(p);
+    lo += e;
+  }
+  __device__ __forceinline__ double val() const { return hi.val() + (double)lo; }
+};
+
+// difference of two double-float values (hi + lo) in FP32
+__device__ __forceinline__ float dfdiff(float ah, float al, float bh, float bl) {
+  return (ah - bh) + (al - bl);
 }
+
+// stress_point_update (2_SPH_main_2018.f90:403-482), FP32 sums.  A stress-point's velocity
+// is the weighted mean of its nodes' velocities; it is formed as the first node's velocity
+// plus the weighted mean of the deviations, which are small and exact in double-float.
+__global__ void k_finterp(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  int t = D.sorted[s];
+  if (t >= D.NT) return;
+  int tt = D.itype[t];
+  if (!D.sp_sph) {
+    if (t >= D.NN) {
+      D.vx[t] = D.vx[t - D.NN];
+      D.vy[t] = D.vy[t - D.NN];
+    } else {
+      int sp = t + D.NN;
+      D.s0[t] = D.s0[sp];
+      D.s1[t] = D.s1[sp];
+      D.s2[t] = D.s2[sp];
+      D.s3[t] = D.s3[sp];
+      D.iv1[t] = D.iv1[sp];
+      if (D.cont_density) D.rho0[t] = D.rho[sp];
+    }
+    return;
+  }
+  int deg = D.degC[s];
+  if (is_sp(tt)) {
+    Kahan v0, v1, nm;
+    bool have = false;
+    float4 ref = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = 0; k < deg; k++) {
+      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int u = e.x;
+      if (D.itype[u] != 2) continue;
+      float w = __int_as_float(e.y);
+      float4 r = D.recV[u];
+      if (!have) {
+        ref = r;
+        have = true;
+      }
+      float h2 = D.recI[u].y * w;
+      v0.add(dfdiff(r.x, r.z, ref.x, ref.z) * h2);
+      v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
+      nm.add(h2);
+    }
+    double norm = nm.val();
+    if (norm != 0) {
+      D.vx[t] = ((double)ref.x + (double)ref.z) + v0.val() / norm;
+      D.vy[t] = ((double)ref.y + (double)ref.w) + v1.val() / norm;
+    }
+  } else {
+    Kahan a, b, c, d, iv, rt, nm;
+    for (int k = 0; k < deg; k++) {
+      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int u = e.x;
+      if (D.itype[u] != 1) continue;
+      float w = __int_as_float(e.y);
+      float4 rs = D.recS[u];
+      float4 ri = D.recI[u];
+      float h1 = ri.y * w;
+      a.add(rs.x * h1);
+      b.add(rs.y * h1);
+      c.add(rs.z * h1);
+      d.add(rs.w * h1);
+      iv.add(ri.x * h1);
+      if (D.cont_density) rt.add(ri.z * h1);
+      nm.add(h1);
+    }
+    double norm = nm.val();
+    if (norm != 0) {
+      D.s0[t] = a.val() / norm;
+      D.s1[t] = b.val() / norm;
+      D.s2[t] = c.val() / norm;
+      D.s3[t] = d.val() / norm;
+      D.iv1[t] = iv.val() / norm;
+    } else {
+      D.vx[t] = 0.0;
+      D.vy[t] = 0.0;
+    }
+    if (D.cont_density) D.rho0[t] = rt.val() / norm;
+  }
+}
+
+// get_derivatives (2_SPH_main_2018.f90:487-648) with FP32 sums, then the FP64 tails.
+// Node side: sum_u m (A_t + A_u) dW = sum_u m (A_u - A_t) dW + 2 A_t sum_u m dW, with
+// A = sigma / rho^2.  The first sum has small terms (double-float differences); the second
+// is a sum of exact products.  This keeps the near-cancelling stress divergence accurate.
+__global__ void k_fderivs(Dev D, int stage) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  int t = D.sorted[s];
+  if (t >= D.NT) return;
+  const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
+  const double f2 = f2rk[stage];
+  const StepScalars& sc = *D.cur;
+  int tt = D.itype[t];
+  int deg = D.degC[s];
+  const double xt = D.px[t], yt = D.py[t];
+  if (is_sp(tt)) {
+    Kahan g0, g1, g2, g3, e0, e1, e2, e3;
+    const double vtx = D.vx[t], vty = D.vy[t];
+    const float vh0 = (float)vtx, vh1 = (float)vty;
+    const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
+    for (int k = 0; k < deg; k++) {
+      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int u = e.x;
+      int ut = D.itype[u];
+      float Gx = __int_as_float(e.z), Gy = __int_as_float(e.w);
+      float vol = D.recI[u].y;
+      if (ut == 2) {
+        float4 r = D.recV[u];
+        float h1 = Gx * vol, h2 = Gy * vol;
+        float du0 = dfdiff(r.x, r.z, vh0, vl0), du1 = dfdiff(r.y, r.w, vh1, vl1);
+        g0.add(du0 * h1);
+        g2.add(du0 * h2);
+        g1.add(du1 * h1);
+        g3.add(du1 * h2);
+        if (D.cspm) {
+          float xu = (float)(D.px[u] - xt), yu = (float)(D.py[u] - yt);
+          e0.add(xu * h1);
+          e1.add(yu * h1);
+          e2.add(xu * h2);
+          e3.add(yu * h2);
+        }
+      } else if (ut == 25) {
+        double wall = (double)D.wallpos[u];
+        double da, db;
+        if (D.horiz[u] == 1.0f) {
+          da = fabs(yt - wall);
+          db = fabs(D.py[u] - wall);
+        } else {
+          da = fabs(xt - wall);
+          db = fabs(D.px[u] - wall);
+        }
+        double bq = 1.0 + db / da;
+        double beta = 1.5 < bq ? 1.5 : bq;
+        float du0 = (float)(vtx - vtx * (1.0 - beta)), du1 = (float)(vty - vty * (1.0 - beta));
+        float hh1 = -Gx * vol, hh2 = -Gy * vol;
+        g0.add(du0 * hh1);
+        g2.add(du0 * hh2);
+        g1.add(du1 * hh1);
+        g3.add(du1 * hh2);
+      }
+    }
+    double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
+    double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
+    tail_sp(D, sc, t, g, AE, f2);
+  } else if (is_node(tt)) {
+    Kahan q0, q1, q2, q3, q4, q5, e0, e1, e2, e3;
+    ProdSum sx, sy;
+    const float4 ah = D.recA[t], al = D.recAl[t];
+    const double At[3] = {D.A[0][t], D.A[1][t], D.A[2][t]};
+    int bc_int = 0;
+    for (int k = 0; k < deg; k++) {
+      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int u = e.x;
+      int ut = D.itype[u];
+      float dwx = -__int_as_float(e.z), dwy = -__int_as_float(e.w);
+      float m, d0, d1, d2;
+      if (ut == 1) {
+        float4 ra = D.recA[u], rl = D.recAl[u];
+        m = ra.w;
+        d0 = dfdiff(ra.x, rl.x, ah.x, al.x);
+        d1 = dfdiff(ra.y, rl.y, ah.y, al.y);
+        d2 = dfdiff(ra.z, rl.z, ah.z, al.z);
+        if (D.cspm) {
+          float vol = D.recI[u].y;
+          float h1b = -(dwx * vol), h2b = -(dwy * vol);
+          float xu = (float)(D.px[u] - xt), yu = (float)(D.py[u] - yt);
+          e0.add(xu * h1b);
+          e1.add(yu * h1b);
+          e2.add(xu * h2b);
+          e3.add(yu * h2b);
+        }
+      } else if (ut == 25) {
+        // the dummy carries the node's stress: A_u = sigma_t / rho_d^2
+        bc_int = 1;
+        double rd = D.rho[u];
+        double rd2 = rd * rd;
+        m = (float)D.mass[u];
+        d0 = (float)(D.s0[t] / rd2 - At[0]);
+        d1 = (float)(D.s1[t] / rd2 - At[1]);
+        d2 = (float)(D.s2[t] / rd2 - At[2]);
+      } else {
+        continue;
+      }
+      float mx = m * dwx, my = m * dwy;
+      q0.add(mx * d0);
+      q1.add(mx * d1);
+      q2.add(mx * d2);
+      q3.add(my * d0);
+      q4.add(my * d1);
+      q5.add(my * d2);
+      sx.add(m, dwx);
+      sy.add(m, dwy);
+    }
+    double avx = 0.0, avy = 0.0;
+    if (D.alpha > 0 || D.beta > 0) {
+      // artificial_viscosity (2_SPH_main_2018.f90:826-904) in FP32
+      Kahan ax, ay;
+      int degs = D.degS[s];
+      const double vtx = D.vx[t], vty = D.vy[t];
+      const float vh0 = (float)vtx, vh1 = (float)vty;
+      const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
+      const float ht = (float)D.hsml[t], rt = (float)D.rho[t];
+      for (int k = 0; k < degs; k++) {
+        int4 e = D.same[(size_t)k * D.N2 + s];
+        int u = e.x;
+        float4 r = D.recV[u];
+        float4 ri = D.recI[u];
+        float xij = (float)(xt - D.px[u]);
+        float yij = (float)(yt - D.py[u]);
+        float h = 0.5f * (ht + (float)D.hsml[u]);
+        float rho2 = 0.5f * (rt + ri.z);
+        float div_u = xij * dfdiff(vh0, vl0, r.x, r.z) + yij * dfdiff(vh1, vl1, r.y, r.w);
+        float sq2 = xij * xij + yij * yij;
+        float theta = (h * div_u) / (sq2 + 0.01f * (h * h));
+        float visc = 0.0f;
+        if (div_u < 0)
+          visc = (-((float)D.alpha * 600.0f) * theta + (float)D.beta * (theta * theta)) / rho2;
+        ax.add(visc * __int_as_float(e.z) * ri.w);
+        ay.add(visc * __int_as_float(e.w) * ri.w);
+      }
+      avx = -ax.val();
+      avy = -ay.val();
+    }
+    const double Sx = sx.val(), Sy = sy.val();
+    double g2v[6];
+    g2v[0] = -(q0.val() + 2.0 * At[0] * Sx);
+    g2v[1] = -(q1.val() + 2.0 * At[1] * Sx);
+    g2v[2] = -(q2.val() + 2.0 * At[2] * Sx);
+    g2v[3] = -(q3.val() + 2.0 * At[0] * Sy);
+    g2v[4] = -(q4.val() + 2.0 * At[1] * Sy);
+    g2v[5] = -(q5.val() + 2.0 * At[2] * Sy);
+    double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
+    tail_node(D, sc, t, g2v, AE, bc_int, avx, avy, f2);
+  }
+}
+
+// XSPH_update (2_SPH_main_2018.f90:189-239), FP32 sums of double-float velocity differences
+__global__ void k_fxsph(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  int t = D.sorted[s];
+  if (t >= D.NT) return;
+  int deg = D.degS[s];
+  const double vt0 = D.vx[t], vt1 = D.vy[t];
+  const float vh0 = (float)vt0, vh1 = (float)vt1;
+  const float vl0 = (float)(vt0 - (double)vh0), vl1 = (float)(vt1 - (double)vh1);
+  Kahan s0, s1;
+  int flag = D.bc_or_not[t];
+  bool mark = false;
+  for (int k = 0; k < deg; k++) {
+    int4 e = D.same[(size_t)k * D.N2 + s];
+    int u = e.x;
+    float w = __int_as_float(e.y);
+    float4 r = D.recV[u];
+    float vw = D.recI[u].y * w;
+    s0.add(dfdiff(r.x, r.z, vh0, vl0) * vw);
+    s1.add(dfdiff(r.y, r.w, vh1, vl1) * vw);
+    if (t < D.NN && D.bc_or_not[u] == 2 && flag != 2) mark = true;
+  }
+  const double eps = 0.5;
+  D.px[t] = D.x0x[t] + D.dt * (vt0 + eps * s0.val());
+  D.py[t] = D.x0y[t] + D.dt * (vt1 + eps * s1.val());
+  if (mark) D.bc_or_not[t] = 3;
+}
+
+}  // namespace
+
+void launch_finterp(Ctx& c) {
+  k_finterp<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);
+}
+void launch_fderivs(Ctx& c, int stage) {
+  k_fderivs<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d, stage);
+}
+void launch_fxsph(Ctx& c) {
+  k_fxsph<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);
+}
+
+int launch_fast_step(Ctx& c) { return launch_plain_step(c); }
 
 }  // namespace sps

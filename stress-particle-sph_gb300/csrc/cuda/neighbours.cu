@@ -108,10 +108,23 @@ __global__ void k_grid(Dev D) {
   g.overflow = (nc > (double)D.cell_cap || !(cellsz > 0.0)) ? 1 : 0;
   g.ncells = g.overflow ? 0 : (int)nc;
   g.nactive = 0;
+  // uniform smoothing length: (h + h) / 2 == h, so every pair's kernel shares these values
+  g.uniform_h = (D.skf == 1 && red[5] == hmax && hmax > 0.0) ? 1 : 0;
+  {
+    double h = hmax;
+    g.h = h;
+    g.yh = 1.0 / h;
+    g.hh = h * h;
+    g.yhh = 1.0 / g.hh;
+    g.factor = 15.0 / (7.0 * D.pi * h * h);
+    g.factor6 = g.factor / 6.0;
+    g.c3 = g.factor6 * 3.0;
+  }
   if (g.overflow) atomicOr(D.err, ERR_CELLS);
   *D.grid = g;
-  // FP32 prefilter band: coordinates relative to xmin carry |err| <= 2^-24 * extent
-  double ext = fmax(g.deltx[0] * g.ndiv[0], g.deltx[1] * g.ndiv[1]);
+  // FP32 prefilter band: cell-relative offsets and the cell-corner shift each carry
+  // |err| <= 2^-24 * 2 cells; the band covers eight times that relative to the support
+  double ext = 2.0 * fmax(g.deltx[0], g.deltx[1]);
   double smin = (double)D.scale_k * red[5];
   double tau = (smin > 0) ? 8.0 * ext * 1.1920929e-07 / smin + 4e-6 : 1.0;
   D.bbox_part[0] = tau;  // reused as the band width of this step
@@ -137,8 +150,10 @@ __global__ void k_cell_count(Dev D) {
   } else {
     double x = D.px[i], y = D.py[i];
     c = cell_index(g, x, y);
-    D.xr[i] = (float)(x - g.xmin[0]);
-    D.yr[i] = (float)(y - g.xmin[1]);
+    // FP32 offsets from the particle's own cell corner (|offset| <= one cell)
+    int ix = c % g.ndiv[0], iy = c / g.ndiv[0];
+    D.xr[i] = (float)(x - (g.xmin[0] + (double)ix * g.deltx[0]));
+    D.yr[i] = (float)(y - (g.xmin[1] + (double)iy * g.deltx[1]));
     D.hr[i] = (float)D.hsml[i];
   }
   D.cell_of[i] = c;
@@ -190,10 +205,13 @@ __device__ __forceinline__ bool exact_test(const Dev& D, int a, int b, double& r
   return r < (double)D.scale_k * mh;
 }
 
-// 0 = reject, 1 = accept, 2 = undecided (inside the guard band)
+// 0 = reject, 1 = accept, 2 = undecided (inside the guard band).  (cx, cy) is the corner
+// of b's cell relative to a's in FP32 (multiples of the cell size); fx, fy return the
+// FP32 separation x_a - x_b.
 __device__ __forceinline__ int prefilter(const Dev& D, float xa, float ya, float ha, int b,
-                                         float tau) {
-  float fx = xa - D.xr[b], fy = ya - D.yr[b];
+                                         float cx, float cy, float tau, float& fx, float& fy) {
+  fx = (xa - D.xr[b]) - cx;
+  fy = (ya - D.yr[b]) - cy;
   float d2 = fx * fx + fy * fy;
   float s = (float)D.scale_k * ((ha + D.hr[b]) * 0.5f);
   float s2 = s * s;
@@ -202,7 +220,65 @@ __device__ __forceinline__ int prefilter(const Dev& D, float xa, float ya, float
   return 2;
 }
 
-// pairs created by the particle at sorted position s (its half stencil), creation order
+// FP32 cubic / Gaussian / quintic kernel of the FP32 form (same formulas as the reference's
+// kernel routine, evaluated in single precision)
+__device__ __forceinline__ void sph_kernel_f32(int skf, float pi, float r, float dx0, float dx1,
+                                               float h, float* w, float* dw0, float* dw1) {
+  float q = r / h;
+  *w = 0.0f;
+  *dw0 = 0.0f;
+  *dw1 = 0.0f;
+  if (skf == 1) {
+    float factor = 15.0f / (7.0f * pi * h * h);
+    if (q <= 1.0f) {
+      *w = factor * ((2.0f / 3.0f - q * q) + (q * q * q) * 0.5f);
+      float a = (factor * (-2.0f + 1.5f * q)) / (h * h);
+      *dw0 = a * dx0;
+      *dw1 = a * dx1;
+    } else if (q <= 2.0f) {
+      float t = 2.0f - q;
+      *w = (factor / 6.0f) * (t * t * t);
+      float a = -(factor * 0.5f) * (t * t) / (h * r);
+      *dw0 = a * dx0;
+      *dw1 = a * dx1;
+    }
+  } else if (skf == 2) {
+    float factor = 1.0f / (h * h * pi);
+    if (q <= 3.0f) {
+      *w = factor * expf(-(q * q));
+      *dw0 = *w * (-2.0f * dx0 / (h * h));
+      *dw1 = *w * (-2.0f * dx1 / (h * h));
+    }
+  } else {
+    float factor = 7.0f / (478.0f * pi * h * h);
+    float a = 3.0f - q, b = 2.0f - q, c1 = 1.0f - q;
+    float a2 = a * a, b2 = b * b, c2 = c1 * c1;
+    float a4 = a2 * a2, b4 = b2 * b2;
+    float a5 = a4 * a, b5 = b4 * b, c5 = c2 * c2 * c1;
+    if (q <= 1.0f) {
+      *w = factor * ((a5 - 6.0f * b5) + 15.0f * c5);
+      float g = factor * ((-120.0f + 120.0f * q) - 50.0f * (q * q)) / (h * h);
+      *dw0 = g * dx0;
+      *dw1 = g * dx1;
+    } else if (q <= 2.0f) {
+      *w = factor * (a5 - 6.0f * b5);
+      float g = factor * (-5.0f * a4 + 30.0f * b4) / (h * r);
+      *dw0 = g * dx0;
+      *dw1 = g * dx1;
+    } else if (q <= 3.0f) {
+      *w = factor * a5;
+      float g = factor * (-5.0f * a4) / (h * r);
+      *dw0 = g * dx0;
+      *dw1 = g * dx1;
+    }
+  }
+}
+
+// Pairs created by the particle at sorted position s, in the reference's creation order:
+// the rest of its own cell, the cell to its right, then the three cells of the row above.
+// FAST = false: W and dW from the reference's FP64 kernel, stored in FP32 (the plain
+// form); FAST = true: kernel evaluated in FP32 (the FP32 form).  The pair set is the same.
+template <bool FAST>
 __global__ void k_half(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
@@ -217,37 +293,46 @@ __global__ void k_half(Dev D) {
   int nx = g.ndiv[0], ny = g.ndiv[1];
   int ix = c % nx, iy = c / nx;
   float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
-  // R1: rest of own cell and the cell to the right; R2: the three cells of the row above
-  int r1_end_cell = (ix + 1 < nx) ? c + 1 : c;
-  int lo[2], hi[2];
-  lo[0] = s + 1;
-  hi[0] = D.cell_start[r1_end_cell] + D.cell_cnt[r1_end_cell];
-  if (iy + 1 < ny) {
-    int c0 = (iy + 1) * nx + (ix > 0 ? ix - 1 : 0);
-    int c1 = (iy + 1) * nx + (ix + 1 < nx ? ix + 1 : ix);
-    lo[1] = D.cell_start[c0];
-    hi[1] = D.cell_start[c1] + D.cell_cnt[c1];
-  } else {
-    lo[1] = hi[1] = 0;
-  }
+  const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
   int k = 0;
   int4* out = D.half + (size_t)s * D.capH;
-  for (int rgn = 0; rgn < 2; rgn++)
-    for (int bs = lo[rgn]; bs < hi[rgn]; bs++) {
+  // stencil cells in creation order: (dix, diy) and the first sorted position to scan
+  int cells[5][2] = {{0, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+  for (int q = 0; q < 5; q++) {
+    int jx = ix + cells[q][0], jy = iy + cells[q][1];
+    if (jx < 0 || jx >= nx || jy >= ny) continue;
+    int cc = jy * nx + jx;
+    int lo = (q == 0) ? s + 1 : D.cell_start[cc];
+    int hi = D.cell_start[cc] + D.cell_cnt[cc];
+    float cx = (float)cells[q][0] * cw, cy = (float)cells[q][1] * ch;
+    for (int bs = lo; bs < hi; bs++) {
       int b = D.sorted[bs];
-      int pf = prefilter(D, xa, ya, ha, b, tau);
+      float fx, fy;
+      int pf = prefilter(D, xa, ya, ha, b, cx, cy, tau, fx, fy);
       if (pf == 0) continue;
       double r, dx, dy, mh;
-      bool acc = exact_test(D, a, b, r, dx, dy, mh);
-      if (!acc) continue;
-      double w, dw0, dw1;
-      sph_kernel(D.skf, D.pi, r, dx, dy, mh, &w, &dw0, &dw1);
-      if (k < D.capH) {
-        out[k] = make_int4(bs, __float_as_int((float)w), __float_as_int((float)dw0),
-                           __float_as_int((float)dw1));
+      if (pf == 2 || !FAST) {
+        bool acc = exact_test(D, a, b, r, dx, dy, mh);
+        if (!acc) continue;
       }
+      float wf, d0f, d1f;
+      if (!FAST) {
+        double w, dw0, dw1;
+        if (g.uniform_h) cubic_uniform(g, r, dx, dy, &w, &dw0, &dw1);
+        else sph_kernel(D.skf, D.pi, r, dx, dy, mh, &w, &dw0, &dw1);
+        wf = (float)w;
+        d0f = (float)dw0;
+        d1f = (float)dw1;
+      } else {
+        float hm = (ha + D.hr[b]) * 0.5f;
+        float rf = sqrtf(fx * fx + fy * fy);
+        sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
+      }
+      if (k < D.capH)
+        out[k] = make_int4(bs, __float_as_int(wf), __float_as_int(d0f), __float_as_int(d1f));
       k++;
     }
+  }
   if (k > D.capH) {
     atomicOr(D.err, ERR_HALF_CAP);
     k = D.capH;
@@ -469,7 +554,8 @@ int launch_pair_build(Ctx& c) {
   c.mark("spos");
   k_spos<<<nb, kBlock, 0, st>>>(D);
   c.mark("half");
-  k_half<<<nb, kBlock, 0, st>>>(D);
+  if (c.precision == SPS_PREC_FP32_FAST) k_half<true><<<nb, kBlock, 0, st>>>(D);
+  else k_half<false><<<nb, kBlock, 0, st>>>(D);
   c.mark("scan_half", 3);
   scan_i32_to_i64(c, D.half_cnt, D.half_off, D.N2);
   c.mark("pair_meta");

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "ctx.cuh"
+#include "stage_tail.cuh"
 
 namespace sps {
 
@@ -28,24 +29,17 @@ namespace {
 
 constexpr int kBlock = 256;
 
-// Normal_BCs (3_SPH_material_2018.f90:1665-1770) for one particle
-__device__ __forceinline__ void apply_bcs(const Dev& D, const StepScalars& sc, int ip, double& vx,
-                                          double& vy, double& s0, double& s1, double& s2) {
-  if (D.no_bcs <= 0) return;
-  if (D.bc_or_not[ip] != 1) return;
-  const int32_t* bi = D.bc_info + 8 * (size_t)ip;
-  if (bi[1] == 0) return;
-  for (int r = 0; r < 5; r++) {
-    int bt = bi[r + 2];
-    if (bt == 0) continue;
-    double val = sc.bcval[bt - 1];
-    int var = D.bcvar[bt - 1];
-    if (var == 5) vx = val;
-    else if (var == 6) vy = val;
-    else if (var == 1) s0 = val;
-    else if (var == 3) s2 = val;
-    else if (var == 2) s1 = val;
-  }
+// FP32-form neighbour records of particle i (velocity, volume, stress, internal variable)
+__device__ __forceinline__ float4 split2(double x, double y) {
+  float xh = (float)x, yh = (float)y;
+  return make_float4(xh, yh, (float)(x - (double)xh), (float)(y - (double)yh));
+}
+
+__device__ __forceinline__ void write_records(const Dev& D, int i, double vx, double vy, double a,
+                                              double b, double c, double d) {
+  D.recV[i] = split2(vx, vy);
+  D.recS[i] = make_float4((float)a, (float)b, (float)c, (float)d);
+  D.recI[i] = make_float4((float)D.iv1[i], (float)D.vol[i], (float)D.rho[i], (float)D.mass[i]);
 }
 
 __global__ void k_load_scalars(Dev D) {
@@ -192,6 +186,8 @@ __global__ void k_stage_begin(Dev D, int stage) {
       D.RHSr[i] = rr;
       double rho = D.rho0[i] + f1dt * rr;
       D.rho[i] = rho;
+      D.vol[i] = D.mass[i] / rho;
+      D.rinv[i] = 1.0 / rho;
       if (D.sle == 2) {
         double rh = -(D.hsml0[i] / (rho * 2.0)) * rr;
         D.RHSh[i] = rh;
@@ -207,6 +203,7 @@ __global__ void k_stage_begin(Dev D, int stage) {
   D.s1[i] = b;
   D.s2[i] = c;
   D.s3[i] = d;
+  if (D.fast) write_records(D, i, vx, vy, a, b, c, d);
 }
 
 // stress_point_update (2_SPH_main_2018.f90:403-482) as a gather per target
@@ -240,11 +237,10 @@ __global__ void k_interp(Dev D) {
       int u = e.x;
       if (D.itype[u] != 2) continue;
       double w = (double)__int_as_float(e.y);
-      double mu = D.mass[u], ru = D.rho[u];
-      double h2 = (mu / ru) * w;
+      double h2 = D.vol[u] * w;  // (mass/rho)*w with mass/rho formed once per particle
       v0 = v0 + D.vx[u] * h2;
       v1 = v1 + D.vy[u] * h2;
-      norm = norm + (w * mu) / ru;
+      norm = norm + div_rcp(w * D.mass[u], D.rho[u], D.rinv[u]);
     }
     if (norm != 0) {
       D.vx[t] = v0 / norm;
@@ -257,15 +253,15 @@ __global__ void k_interp(Dev D) {
       int u = e.x;
       if (D.itype[u] != 1) continue;
       double w = (double)__int_as_float(e.y);
-      double mu = D.mass[u], ru = D.rho[u];
-      double h1 = (mu / ru) * w;
+      double ru = D.rho[u];
+      double h1 = D.vol[u] * w;
       a = a + D.s0[u] * h1;
       b = b + D.s1[u] * h1;
       c = c + D.s2[u] * h1;
       d = d + D.s3[u] * h1;
       iv = iv + D.iv1[u] * h1;
       if (D.cont_density) rt = rt + ru * h1;
-      norm = norm + (w * mu) / ru;
+      norm = norm + div_rcp(w * D.mass[u], ru, D.rinv[u]);
     }
     if (norm != 0) {
       D.s0[t] = a / norm;
@@ -283,23 +279,63 @@ __global__ void k_interp(Dev D) {
 
 __global__ void k_node_rho(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < D.NN) D.rho[i] = D.rho0[i];
+  if (i < D.NN) {
+    double r = D.rho0[i];
+    D.rho[i] = r;
+    D.vol[i] = D.mass[i] / r;
+    D.rinv[i] = 1.0 / r;
+  }
 }
 
-__global__ void k_adapt_bc(Dev D) {
+// adapt_stress2 + BCs after the interpolation (SP-SPH only), then sigma / rho^2 of the
+// stage for get_derivatives (the same quotient the reference forms per pair)
+__global__ void k_adapt_bc(Dev D, int with_A) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
   const StepScalars& sc = *D.cur;
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
-  if (D.ncrit == 12) adapt_stress(D.alpha2, D.kc, a, b, c, d);
-  apply_bcs(D, sc, i, vx, vy, a, b, c);
-  D.vx[i] = vx;
-  D.vy[i] = vy;
-  D.s0[i] = a;
-  D.s1[i] = b;
-  D.s2[i] = c;
-  D.s3[i] = d;
+  if (D.sp_sph) {
+    if (D.ncrit == 12) adapt_stress(D.alpha2, D.kc, a, b, c, d);
+    apply_bcs(D, sc, i, vx, vy, a, b, c);
+    D.vx[i] = vx;
+    D.vy[i] = vy;
+    D.s0[i] = a;
+    D.s1[i] = b;
+    D.s2[i] = c;
+    D.s3[i] = d;
+  }
+  if (with_A) {
+    double r = D.rho[i];
+    double r2 = r * r;
+    D.A[0][i] = a / r2;
+    D.A[1][i] = b / r2;
+    D.A[2][i] = c / r2;
+    if (D.fast) {
+      float h0 = (float)D.A[0][i], h1 = (float)D.A[1][i], h2 = (float)D.A[2][i];
+      D.recA[i] = make_float4(h0, h1, h2, (float)D.mass[i]);
+      D.recAl[i] = make_float4((float)(D.A[0][i] - (double)h0), (float)(D.A[1][i] - (double)h1),
+                               (float)(D.A[2][i] - (double)h2), 0.0f);
+    }
+  }
+  if (D.fast) {
+    D.recV[i] = split2(vx, vy);
+    D.recI[i] = make_float4((float)D.iv1[i], (float)D.vol[i], (float)D.rho[i], (float)D.mass[i]);
+  }
+}
+
+// m / rho and 1 / rho of particles [lo, hi)
+__global__ void k_vol(Dev D, int lo, int hi) {
+  int i = lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  double r = D.rho[i];
+  D.vol[i] = D.mass[i] / r;
+  D.rinv[i] = 1.0 / r;
+  if (D.fast) {
+    D.recV[i] = split2(D.vx[i], D.vy[i]);
+    D.recI[i] = make_float4(i < D.NT ? (float)D.iv1[i] : 0.0f, (float)D.vol[i], (float)r,
+                            (float)D.mass[i]);
+  }
 }
 
 // get_derivatives (2_SPH_main_2018.f90:487-648) + the per-particle stage work of RK4
@@ -323,10 +359,10 @@ __global__ void k_derivs(Dev D, int stage) {
       int u = e.x;
       int ut = D.itype[u];
       double Gx = (double)__int_as_float(e.z), Gy = (double)__int_as_float(e.w);
-      double mu = D.mass[u], ru = D.rho[u];
+      double mu = D.mass[u], ru = D.rho[u], iu = D.rinv[u];
       if (ut == 2) {  // node -- stress-point (target is pair_i)
-        double h1 = (Gx * mu) / ru;
-        double h2 = (Gy * mu) / ru;
+        double h1 = div_rcp(Gx * mu, ru, iu);
+        double h2 = div_rcp(Gy * mu, ru, iu);
         double du0 = D.vx[u] - vt[0], du1 = D.vy[u] - vt[1];
         g[0] = g[0] + du0 * h1;
         g[2] = g[2] + du0 * h2;
@@ -353,82 +389,19 @@ __global__ void k_derivs(Dev D, int stage) {
         double beta = 1.5 < bq ? 1.5 : bq;
         double dv0 = vt[0] * (1.0 - beta) + beta * 0.0;
         double dv1 = vt[1] * (1.0 - beta) + beta * 0.0;
-        double hh1 = (-Gx * mu) / ru;
-        double hh2 = (-Gy * mu) / ru;
+        double hh1 = div_rcp(-Gx * mu, ru, iu);
+        double hh2 = div_rcp(-Gy * mu, ru, iu);
         g[0] = g[0] + (vt[0] - dv0) * hh1;
         g[2] = g[2] + (vt[0] - dv0) * hh2;
         g[1] = g[1] + (vt[1] - dv1) * hh1;
         g[3] = g[3] + (vt[1] - dv1) * hh2;
       }
     }
-    if (D.cspm) {
-      double A4 = AE[0] * AE[3] - AE[1] * AE[2];
-      double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
-      if (fabs(A4) < (double)1e-07f) {
-        A4 = 1;
-        A0 = 1;
-        A1 = 0;
-        A2 = 0;
-        A3 = 1;
-      } else {
-        A4 = 1.0 / A4;
-      }
-      for (int d = 0; d < 2; d++) {
-        g[d] = A4 * (A0 * g[d] + A1 * g[d + 2]);
-        g[d + 2] = A4 * (A2 * g[d] + A3 * g[d + 2]);
-      }
-    }
-    double* gu = D.grad_u + 4 * (size_t)t;
-    gu[0] = g[0];
-    gu[1] = g[1];
-    gu[2] = g[2];
-    gu[3] = g[3];
-    const double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
-    double div1[4];
-    div1[0] = -(D.D11 * g11 + D.D12 * g22);
-    div1[1] = -(D.D12 * g11 + D.D22 * g22);
-    div1[2] = -(D.D33 * g21 + D.D33 * g12);
-    div1[3] = -(D.D41 * g11 + D.D42 * g22);
-    // plastic_terms (3_SPH_material_2018.f90:1884-1954)
-    double st[4] = {D.s0[t], D.s1[t], D.s2[t], D.s3[t]};
-    double Gs[4] = {0.0, 0.0, 0.0, 0.0}, der = 0.0;
-    if (D.ntype_eco > 1) {
-      double s2v[4] = {st[0], st[1], st[2], st[3]};
-      if (D.ntype_solid == 1) s2v[3] = D.poiss * (s2v[0] + s2v[1]);
-      double vivel[4] = {0.0, 0.0, 0.0, 0.0}, G2[4];
-      if (D.ncrit == 12) {
-        double f = D.fdp[t];
-        drucker_prager(D, sc.time_sph, s2v, g, &f, G2, vivel);
-        D.fdp[t] = f;
-        for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
-      }
-      der = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
-                  vivel[2] * vivel[2]) /
-                 3.0);
-    }
-    double spin[4] = {0.0, 0.0, 0.0, 0.0};
-    if (D.update_x) {
-      double om1 = 0.5 * (g12 - g21);
-      double om2 = -0.5 * (g12 - g21);
-      spin[0] = 2.0 * om1 * st[2];
-      spin[1] = 2.0 * om2 * st[2];
-      spin[2] = om2 * st[0] + om1 * st[1];
-    }
-    for (int k = 0; k < 4; k++) {
-      double rhs = (-div1[k] + spin[k]) + Gs[k];
-      D.RHS1[k][t] = rhs;
-      D.RKs[k][t] = D.RKs[k][t] + f2 * rhs;
-    }
-    D.RKd[t] = D.RKd[t] + der * f2;
-    if (D.cont_density) {
-      D.RKr[t] = D.RKr[t] + f2 * D.RHSr[t];
-      if (D.sle == 2) D.RKh[t] = D.RKh[t] + f2 * D.RHSh[t];
-    }
+    tail_sp(D, sc, t, g, AE, f2);
   } else if (is_node(tt)) {
     double g2[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // grad2(s,b) at s + 3b
     const double rt = D.rho[t];
-    const double rt2 = rt * rt;
-    const double at[3] = {D.s0[t] / rt2, D.s1[t] / rt2, D.s2[t] / rt2};
+    const double at[3] = {D.A[0][t], D.A[1][t], D.A[2][t]};  // sigma / rho^2 of the target
     const double stt[3] = {D.s0[t], D.s1[t], D.s2[t]};
     int bc_int = 0;
     for (int k = 0; k < deg; k++) {
@@ -436,18 +409,18 @@ __global__ void k_derivs(Dev D, int stage) {
       int u = e.x;
       int ut = D.itype[u];
       double dwx = -(double)__int_as_float(e.z), dwy = -(double)__int_as_float(e.w);
-      double mu = D.mass[u], ru = D.rho[u];
-      double ru2 = ru * ru;
+      double mu = D.mass[u];
       if (ut == 1) {  // node -- stress-point (stress-point is pair_i)
-        const double su[3] = {D.s0[u], D.s1[u], D.s2[u]};
+        const double au[3] = {D.A[0][u], D.A[1][u], D.A[2][u]};
         for (int q = 0; q < 3; q++) {
-          double sum = at[q] + su[q] / ru2;
+          double sum = at[q] + au[q];
           g2[q] = g2[q] - mu * (dwx * sum);
           g2[q + 3] = g2[q + 3] - mu * (dwy * sum);
         }
         if (D.cspm) {
-          double h1b = -((dwx * mu) / ru);
-          double h2b = -((dwy * mu) / ru);
+          double ru = D.rho[u], iu = D.rinv[u];
+          double h1b = -div_rcp(dwx * mu, ru, iu);
+          double h2b = -div_rcp(dwy * mu, ru, iu);
           double xu = D.px[u] - xt, yu = D.py[u] - yt;
           AE[0] = AE[0] + xu * h1b;
           AE[1] = AE[1] + yu * h1b;
@@ -456,6 +429,8 @@ __global__ void k_derivs(Dev D, int stage) {
         }
       } else if (ut == 25) {  // node -- dummy: the dummy carries the node's stress
         bc_int = 1;
+        double ru = D.rho[u];
+        double ru2 = ru * ru;
         for (int q = 0; q < 3; q++) {
           double sum = at[q] + stt[q] / ru2;
           g2[q] = g2[q] - mu * (dwx * sum);
@@ -463,38 +438,12 @@ __global__ void k_derivs(Dev D, int stage) {
         }
       }
     }
-    D.bc_int[t] = bc_int;
-    if (D.cspm) {
-      double A4 = AE[0] * AE[3] - AE[1] * AE[2];
-      double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
-      if (fabs(A4) < (double)1e-07f) {
-        A4 = 1;
-        A0 = 1;
-        A1 = 0;
-        A2 = 0;
-        A3 = 1;
-      } else {
-        A4 = 1.0 / A4;
-      }
-      for (int d = 0; d < 2; d++) {
-        g2[d] = A4 * (A0 * g2[d] + A1 * g2[d + 3]);
-        g2[d + 3] = A4 * (A2 * g2[d] + A3 * g2[d + 3]);
-      }
-    }
-    double div2x = -(g2[0] + g2[2 + 3]);
-    double div2y = -(g2[2] + g2[1 + 3]);
     const double vtx = D.vx[t], vty = D.vy[t];
-    double gx = (D.ic_grav == 1) ? sc.factg * D.cgrav[0] : 0.0;
-    double gy = (D.ic_grav == 1) ? sc.factg * D.cgrav[1] : 0.0;
-    gx = gx - D.damping * vtx;
-    gy = gy - D.damping * vty;
     double avx = 0.0, avy = 0.0;
     if (D.alpha > 0 || D.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904): FP32 accumulators
       float ax = 0.0f, ay = 0.0f;
       int degs = D.degS[s];
-      const float ht = (float)0.0;  // unused placeholder to keep types explicit
-      (void)ht;
       for (int k = 0; k < degs; k++) {
         int4 e = D.same[(size_t)k * D.N2 + s];
         int u = e.x;
@@ -518,12 +467,7 @@ __global__ void k_derivs(Dev D, int stage) {
       avx = -(double)ax;
       avy = -(double)ay;
     }
-    double rhsx = (((-div2x + gx) + avx) + D.fbx[t]) + 0.0;
-    double rhsy = (((-div2y + gy) + avy) + D.fby[t]) + 0.0;
-    D.RHS2[0][t] = rhsx;
-    D.RHS2[1][t] = rhsy;
-    D.RKv[0][t] = D.RKv[0][t] + f2 * rhsx;
-    D.RKv[1][t] = D.RKv[1][t] + f2 * rhsy;
+    tail_node(D, sc, t, g2, AE, bc_int, avx, avy, f2);
   }
 }
 
@@ -553,13 +497,17 @@ __global__ void k_rk_final(Dev D) {
   D.s3[i] = d;
   if (i >= D.NN) {
     if (D.cont_density) {
-      D.rho[i] = D.rho0[i] + dt6 * D.RKr[i];
+      double r = D.rho0[i] + dt6 * D.RKr[i];
+      D.rho[i] = r;
+      D.vol[i] = D.mass[i] / r;
+      D.rinv[i] = 1.0 / r;
       if (D.sle == 2) D.hsml[i] = D.hsml0[i] + dt6 * D.RKh[i];
     }
     double dd = D.RKd[i] / 6.0;
     D.Ddev[i] = dd;
     D.iv1[i] = D.iv1[i] + D.dt * dd;  // update_strain (3_SPH_material_2018.f90:1864)
   }
+  if (D.fast) write_records(D, i, vx, vy, a, b, c, d);
 }
 
 __global__ void k_trapezoid(Dev D) {
@@ -590,7 +538,7 @@ __global__ void k_xsph(Dev D) {
     int4 e = D.same[(size_t)k * D.N2 + s];
     int u = e.x;
     double w = (double)__int_as_float(e.y);
-    double vol = D.mass[u] / D.rho[u];
+    double vol = D.vol[u];
     s0 = s0 + (vol * (D.vx[u] - vt0)) * w;
     s1 = s1 + (vol * (D.vy[u] - vt1)) * w;
     if (t < D.NN && D.bc_or_not[u] == 2 && flag != 2) mark = true;
@@ -619,6 +567,39 @@ __global__ void k_displ(Dev D) {
 
 }  // namespace
 
+// self-test of div_rcp against the IEEE division on n pseudo-random operands
+// (log-uniform magnitudes over the ranges the step meets, random signs)
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__global__ void k_selftest_div(int64_t n, uint64_t seed, unsigned long long* bad) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long nb = 0;
+  for (; i < n; i += stride) {
+    uint64_t r1 = mix64(seed ^ (uint64_t)i), r2 = mix64(r1), r3 = mix64(r2);
+    double ea = -40.0 + 52.0 * ((r1 >> 11) * 0x1.0p-53);  // |a| in [1e-40, 1e12]
+    double eb = -6.0 + 14.0 * ((r2 >> 11) * 0x1.0p-53);   // |b| in [1e-6, 1e8]
+    double a = exp2(ea * 3.3219280948873622) * ((r3 & 1) ? -1.0 : 1.0);
+    double b = exp2(eb * 3.3219280948873622) * ((r3 & 2) ? -1.0 : 1.0);
+    double y = 1.0 / b;
+    double q1 = div_rcp(a, b, y), q2 = a / b;
+    if (__double_as_longlong(q1) != __double_as_longlong(q2)) nb++;
+  }
+  if (nb) atomicAdd(bad, nb);
+}
+
+void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad) {
+  k_selftest_div<<<152 * 8, 256, 0, c.stream>>>(n, seed, d_bad);
+}
+
+void launch_vol(Ctx& c, int lo, int hi) {
+  if (hi > lo) k_vol<<<(hi - lo + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d, lo, hi);
+}
+
 int launch_plain_step(Ctx& c) {
   Dev& D = c.d;
   cudaStream_t st = c.stream;
@@ -638,33 +619,35 @@ int launch_plain_step(Ctx& c) {
     c.mark("stage_begin");
     k_stage_begin<<<nbT, kBlock, 0, st>>>(D, stage);
     c.mark("interp");
-    k_interp<<<nb2, kBlock, 0, st>>>(D);
+    if (D.fast) launch_finterp(c);
+    else k_interp<<<nb2, kBlock, 0, st>>>(D);
     if (D.cont_density && D.sp_sph) {
       c.mark("node_rho");
       k_node_rho<<<nbN, kBlock, 0, st>>>(D);
     }
-    if (D.sp_sph) {
-      c.mark("adapt_bc");
-      k_adapt_bc<<<nbT, kBlock, 0, st>>>(D);
-    }
+    c.mark("adapt_bc");
+    k_adapt_bc<<<nbT, kBlock, 0, st>>>(D, 1);
     c.mark("derivs");
-    k_derivs<<<nb2, kBlock, 0, st>>>(D, stage);
+    if (D.fast) launch_fderivs(c, stage);
+    else k_derivs<<<nb2, kBlock, 0, st>>>(D, stage);
   }
   c.mark("rk_final");
   k_rk_final<<<nbT, kBlock, 0, st>>>(D);
   c.mark("interp");
-  k_interp<<<nb2, kBlock, 0, st>>>(D);
+  if (D.fast) launch_finterp(c);
+  else k_interp<<<nb2, kBlock, 0, st>>>(D);
   if (D.cont_density && D.sp_sph) {
     c.mark("node_rho");
     k_node_rho<<<nbN, kBlock, 0, st>>>(D);
   }
-  if (D.sp_sph) {
+  if (D.sp_sph || D.fast) {
     c.mark("adapt_bc");
-    k_adapt_bc<<<nbT, kBlock, 0, st>>>(D);
+    k_adapt_bc<<<nbT, kBlock, 0, st>>>(D, 0);
   }
   if (D.update_x && D.xsph) {
     c.mark("xsph");
-    k_xsph<<<nb2, kBlock, 0, st>>>(D);
+    if (D.fast) launch_fxsph(c);
+    else k_xsph<<<nb2, kBlock, 0, st>>>(D);
   } else {
     c.mark("trapezoid");
     k_trapezoid<<<nbT, kBlock, 0, st>>>(D);

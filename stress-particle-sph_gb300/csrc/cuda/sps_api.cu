@@ -318,6 +318,17 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     D.fbx = dalloc<double>(c, NN);
     D.fby = dalloc<double>(c, NN);
     D.Ddev = dalloc<double>(c, NT);
+    D.vol = dalloc<double>(c, N2);
+    D.rinv = dalloc<double>(c, N2);
+    for (int k = 0; k < 3; k++) D.A[k] = dalloc<double>(c, NT);
+    D.fast = (p->precision == SPS_PREC_FP32_FAST) ? 1 : 0;
+    if (D.fast) {
+      D.recV = dalloc<float4>(c, N2);
+      D.recS = dalloc<float4>(c, NT);
+      D.recI = dalloc<float4>(c, N2);
+      D.recA = dalloc<float4>(c, NT);
+      D.recAl = dalloc<float4>(c, NT);
+    }
     D.cell_of = dalloc<int32_t>(c, N2);
     D.sorted = dalloc<int32_t>(c, N2);
     D.spos = dalloc<int32_t>(c, N2);
@@ -414,6 +425,7 @@ int sps_upload(sps_ctx* h, const double* x, const double* vel, const double* str
     SPS_CUDA_CHECK(cudaMemsetAsync(D.out, 0, N2, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.dispx, 0, sizeof(double) * D.NN, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.dispy, 0, sizeof(double) * D.NN, c.stream));
+    sps::launch_vol(c, 0, (int)N2);
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     // cell grid capacity from the uploaded extent (4x margin for spreading)
     double xmn[2] = {1e300, 1e300}, xmx[2] = {-1e300, -1e300}, hmax = 0, hmin_nd = 1e300;
@@ -658,6 +670,25 @@ int sps_kernels_per_step(sps_ctx* h, int32_t* n) {
     return fail(&h->c, SPS_ERR_CUDA, e.what());
   }
   *n = h->c.kernels_per_step;
+  return SPS_OK;
+}
+
+int sps_selftest_division(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatches) {
+  if (!h || !mismatches || n < 0) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  try {
+    unsigned long long* d = nullptr;
+    SPS_CUDA_CHECK(cudaMalloc(&d, sizeof(unsigned long long)));
+    SPS_CUDA_CHECK(cudaMemsetAsync(d, 0, sizeof(unsigned long long), c.stream));
+    sps::launch_selftest_div(c, n, seed, d);
+    unsigned long long v = 0;
+    SPS_CUDA_CHECK(cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    cudaFree(d);
+    *mismatches = (int64_t)v;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
   return SPS_OK;
 }
 

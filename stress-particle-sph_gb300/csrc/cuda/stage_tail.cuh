@@ -1,0 +1,139 @@
+// stage_tail.cuh -- per-particle FP64 work shared by the plain and the FP32 forms.
+//
+// Normal_BCs for one particle, and the tails of get_derivatives / RK4 that follow the
+// neighbour sums (2_SPH_main_2018.f90:596-648 and :727-777 of the Drucker-Prager example):
+// CSPM correction, D : grad(v), plastic_terms / drucker_prager, Jaumann spin, gravity with
+// damping, right-hand sides and RK4 accumulation.  In the plain form (compiled with
+// -fmad=false) these reproduce the reference's rounding exactly.
+#pragma once
+#include "common.cuh"
+
+namespace sps {
+
+// Normal_BCs (3_SPH_material_2018.f90:1665-1770) for one particle
+__device__ __forceinline__ void apply_bcs(const Dev& D, const StepScalars& sc, int ip, double& vx,
+                                          double& vy, double& s0, double& s1, double& s2) {
+  if (D.no_bcs <= 0) return;
+  if (D.bc_or_not[ip] != 1) return;
+  const int32_t* bi = D.bc_info + 8 * (size_t)ip;
+  if (bi[1] == 0) return;
+  for (int r = 0; r < 5; r++) {
+    int bt = bi[r + 2];
+    if (bt == 0) continue;
+    double val = sc.bcval[bt - 1];
+    int var = D.bcvar[bt - 1];
+    if (var == 5) vx = val;
+    else if (var == 6) vy = val;
+    else if (var == 1) s0 = val;
+    else if (var == 3) s2 = val;
+    else if (var == 2) s1 = val;
+  }
+}
+
+
+// stress-point tail: g = grad1(a,b) at a + 2b, AE = CSPM moments (used when cspm)
+__device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int t, double* g,
+                                        double* AE, double f2) {
+    if (D.cspm) {
+      double A4 = AE[0] * AE[3] - AE[1] * AE[2];
+      double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
+      if (fabs(A4) < (double)1e-07f) {
+        A4 = 1;
+        A0 = 1;
+        A1 = 0;
+        A2 = 0;
+        A3 = 1;
+      } else {
+        A4 = 1.0 / A4;
+      }
+      for (int d = 0; d < 2; d++) {
+        g[d] = A4 * (A0 * g[d] + A1 * g[d + 2]);
+        g[d + 2] = A4 * (A2 * g[d] + A3 * g[d + 2]);
+      }
+    }
+    double* gu = D.grad_u + 4 * (size_t)t;
+    gu[0] = g[0];
+    gu[1] = g[1];
+    gu[2] = g[2];
+    gu[3] = g[3];
+    const double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
+    double div1[4];
+    div1[0] = -(D.D11 * g11 + D.D12 * g22);
+    div1[1] = -(D.D12 * g11 + D.D22 * g22);
+    div1[2] = -(D.D33 * g21 + D.D33 * g12);
+    div1[3] = -(D.D41 * g11 + D.D42 * g22);
+    // plastic_terms (3_SPH_material_2018.f90:1884-1954)
+    double st[4] = {D.s0[t], D.s1[t], D.s2[t], D.s3[t]};
+    double Gs[4] = {0.0, 0.0, 0.0, 0.0}, der = 0.0;
+    if (D.ntype_eco > 1) {
+      double s2v[4] = {st[0], st[1], st[2], st[3]};
+      if (D.ntype_solid == 1) s2v[3] = D.poiss * (s2v[0] + s2v[1]);
+      double vivel[4] = {0.0, 0.0, 0.0, 0.0}, G2[4];
+      if (D.ncrit == 12) {
+        double f = D.fdp[t];
+        drucker_prager(D, sc.time_sph, s2v, g, &f, G2, vivel);
+        D.fdp[t] = f;
+        for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
+      }
+      der = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
+                  vivel[2] * vivel[2]) /
+                 3.0);
+    }
+    double spin[4] = {0.0, 0.0, 0.0, 0.0};
+    if (D.update_x) {
+      double om1 = 0.5 * (g12 - g21);
+      double om2 = -0.5 * (g12 - g21);
+      spin[0] = 2.0 * om1 * st[2];
+      spin[1] = 2.0 * om2 * st[2];
+      spin[2] = om2 * st[0] + om1 * st[1];
+    }
+    for (int k = 0; k < 4; k++) {
+      double rhs = (-div1[k] + spin[k]) + Gs[k];
+      D.RHS1[k][t] = rhs;
+      D.RKs[k][t] = D.RKs[k][t] + f2 * rhs;
+    }
+    D.RKd[t] = D.RKd[t] + der * f2;
+    if (D.cont_density) {
+      D.RKr[t] = D.RKr[t] + f2 * D.RHSr[t];
+      if (D.sle == 2) D.RKh[t] = D.RKh[t] + f2 * D.RHSh[t];
+    }
+}
+
+// node tail: g2 = grad2(s,b) at s + 3b, AE = CSPM moments, av = artificial viscosity
+__device__ __forceinline__ void tail_node(const Dev& D, const StepScalars& sc, int t, double* g2,
+                                          double* AE, int bc_int, double avx, double avy,
+                                          double f2) {
+  D.bc_int[t] = bc_int;
+  if (D.cspm) {
+    double A4 = AE[0] * AE[3] - AE[1] * AE[2];
+    double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
+    if (fabs(A4) < (double)1e-07f) {
+      A4 = 1;
+      A0 = 1;
+      A1 = 0;
+      A2 = 0;
+      A3 = 1;
+    } else {
+      A4 = 1.0 / A4;
+    }
+    for (int d = 0; d < 2; d++) {
+      g2[d] = A4 * (A0 * g2[d] + A1 * g2[d + 3]);
+      g2[d + 3] = A4 * (A2 * g2[d] + A3 * g2[d + 3]);
+    }
+  }
+  double div2x = -(g2[0] + g2[2 + 3]);
+  double div2y = -(g2[2] + g2[1 + 3]);
+  const double vtx = D.vx[t], vty = D.vy[t];
+  double gx = (D.ic_grav == 1) ? sc.factg * D.cgrav[0] : 0.0;
+  double gy = (D.ic_grav == 1) ? sc.factg * D.cgrav[1] : 0.0;
+  gx = gx - D.damping * vtx;
+  gy = gy - D.damping * vty;
+  double rhsx = (((-div2x + gx) + avx) + D.fbx[t]) + 0.0;
+  double rhsy = (((-div2y + gy) + avy) + D.fby[t]) + 0.0;
+  D.RHS2[0][t] = rhsx;
+  D.RHS2[1][t] = rhsy;
+  D.RKv[0][t] = D.RKv[0][t] + f2 * rhsx;
+  D.RKv[1][t] = D.RKv[1][t] + f2 * rhsy;
+}
+
+}  // namespace sps

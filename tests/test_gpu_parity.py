@@ -126,3 +126,11 @@ def test_step_before_upload(built_gpu):
     with pytest.raises(sps_gb300.SpsError) as e:
         g.step(1, 0.0)
     assert e.value.rc == _abi.SPS_ERR_STATE
+
+
+def test_corrected_division_matches_ieee(built_gpu):
+    # the plain path divides by densities and smoothing lengths through exact reciprocals
+    # (Markstein correction); it must reproduce the IEEE quotient bit for bit
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
+    g = _gpu_ctx(p)
+    assert sps_gb300.selftest_division(g, 200_000_000, seed=12345) == 0
