@@ -29,6 +29,11 @@ struct StepScalars {
   double bcval[kMaxBC];
 };
 
+// unevaluated sum hi + lo of two FP32 numbers (double-float)
+struct dfl {
+  float hi, lo;
+};
+
 struct Grid {
   double xmin[2];
   double deltx[2];
@@ -41,6 +46,8 @@ struct Grid {
   // h-only subexpressions are formed once (same operations, same values)
   int uniform_h;
   double h, yh, hh, yhh, factor, factor6, c3;
+  // the same constants, and the cell size, as double-float pairs (FP32 form)
+  dfl df_h, df_yh, df_yhh, df_factor, df_factor6, df_c3, df_cell[2];
 };
 
 // pair bookkeeping of grid_find_NEW's linked list
@@ -104,6 +111,7 @@ struct Dev {
   // cells
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
   float *xr, *yr, *hr;
+  float *xrl, *yrl;  // FP32 form: low parts of the cell-relative offsets
   Grid* grid;
   double* bbox_part;  // per-block partial (minx, miny, -maxx, -maxy, -maxh)
   int nbbox_blocks;

@@ -143,7 +143,7 @@ __global__ void k_finterp(Dev D) {
 // Node side: sum_u m (A_t + A_u) dW = sum_u m (A_u - A_t) dW + 2 A_t sum_u m dW, with
 // A = sigma / rho^2.  The first sum has small terms (double-float differences); the second
 // is a sum of exact products.  This keeps the near-cancelling stress divergence accurate.
-__global__ void k_fderivs(Dev D, int stage) {
+__global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
   int t = D.sorted[s];

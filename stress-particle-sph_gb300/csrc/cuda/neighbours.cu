@@ -29,6 +29,59 @@ __device__ __forceinline__ double warp_min(double v) {
   return v;
 }
 
+// ---- double-float (unevaluated sum of two FP32 numbers) arithmetic: Dekker, "A floating-
+// point technique for extending the available precision", Numer. Math. 18, 1971, with the
+// FMA-based exact product.  Used by the FP32 form to produce the FP32 kernel values the
+// reference stores (FP64 evaluation rounded to FP32): a double-float result (~44 bits)
+// rounds the same way except within ~1e-12 of an FP32 rounding boundary.
+__device__ __forceinline__ dfl df_fast2sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ dfl df_2sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ dfl df_add(dfl x, dfl y) {
+  dfl s = df_2sum(x.hi, y.hi);
+  dfl t = df_2sum(x.lo, y.lo);
+  s.lo += t.hi;
+  s = df_fast2sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return df_fast2sum(s.hi, s.lo);
+}
+__device__ __forceinline__ dfl df_neg(dfl x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
+  float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e += x.hi * y.lo + x.lo * y.hi;
+  return df_fast2sum(p, e);
+}
+// quotient seeds may be approximate: each residual step corrects them
+__device__ __forceinline__ dfl df_div(dfl x, dfl y) {
+  float yi = __frcp_rn(y.hi);
+  float q1 = x.hi * yi;
+  dfl r = df_add(x, df_neg(df_mul(y, {q1, 0.0f})));
+  float q2 = r.hi * yi;
+  r = df_add(r, df_neg(df_mul(y, {q2, 0.0f})));
+  float q3 = r.hi * yi;
+  dfl q = df_fast2sum(q1, q2);
+  return df_add(q, {q3, 0.0f});
+}
+__device__ __forceinline__ dfl df_sqrt(dfl x) {
+  if (x.hi <= 0.0f) return {0.0f, 0.0f};
+  float s = x.hi * rsqrtf(x.hi);  // approximate seed, corrected below
+  float p = s * s;
+  float e = fmaf(s, s, -p);
+  float r = ((x.hi - p) - e) + x.lo;
+  return df_fast2sum(s, r * (0.5f * __frcp_rn(s)));
+}
+__device__ __forceinline__ dfl df_from(double v) {
+  float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+
 // Check_Out_Domain + per-block partial bounding box (minx, miny, -maxx, -maxy, -maxh, minh)
 __global__ void k_bbox(Dev D) {
   __shared__ double sh[6][kBlock / 32];
@@ -119,6 +172,14 @@ __global__ void k_grid(Dev D) {
     g.factor = 15.0 / (7.0 * D.pi * h * h);
     g.factor6 = g.factor / 6.0;
     g.c3 = g.factor6 * 3.0;
+    g.df_h = df_from(g.h);
+    g.df_yh = df_from(g.yh);
+    g.df_yhh = df_from(g.yhh);
+    g.df_factor = df_from(g.factor);
+    g.df_factor6 = df_from(g.factor6);
+    g.df_c3 = df_from(g.c3);
+    g.df_cell[0] = df_from(g.deltx[0]);
+    g.df_cell[1] = df_from(g.deltx[1]);
   }
   if (g.overflow) atomicOr(D.err, ERR_CELLS);
   *D.grid = g;
@@ -152,8 +213,15 @@ __global__ void k_cell_count(Dev D) {
     c = cell_index(g, x, y);
     // FP32 offsets from the particle's own cell corner (|offset| <= one cell)
     int ix = c % g.ndiv[0], iy = c / g.ndiv[0];
-    D.xr[i] = (float)(x - (g.xmin[0] + (double)ix * g.deltx[0]));
-    D.yr[i] = (float)(y - (g.xmin[1] + (double)iy * g.deltx[1]));
+    double ox = x - (g.xmin[0] + (double)ix * g.deltx[0]);
+    double oy = y - (g.xmin[1] + (double)iy * g.deltx[1]);
+    float oxh = (float)ox, oyh = (float)oy;
+    D.xr[i] = oxh;
+    D.yr[i] = oyh;
+    if (D.fast) {
+      D.xrl[i] = (float)(ox - (double)oxh);
+      D.yrl[i] = (float)(oy - (double)oyh);
+    }
     D.hr[i] = (float)D.hsml[i];
   }
   D.cell_of[i] = c;
@@ -274,6 +342,35 @@ __device__ __forceinline__ void sph_kernel_f32(int skf, float pi, float r, float
   }
 }
 
+// the reference's cubic kernel for a uniform h (2_SPH_main_2018.f90:1468-1492) in
+// double-float, returning the FP32-rounded W and dW (the hi parts)
+__device__ __forceinline__ void cubic_df(const Grid& g, dfl dx, dfl dy, float* w, float* dw0,
+                                         float* dw1) {
+  dfl r = df_sqrt(df_add(df_mul(dx, dx), df_mul(dy, dy)));
+  dfl q = df_mul(r, g.df_yh);
+  q = df_add(q, df_neg(df_mul(df_add(df_mul(q, g.df_h), df_neg(r)), g.df_yh)));  // refine r/h
+  *w = 0.0f;
+  *dw0 = 0.0f;
+  *dw1 = 0.0f;
+  if (q.hi < 1.0f || (q.hi == 1.0f && q.lo <= 0.0f)) {
+    dfl q2 = df_mul(q, q);
+    dfl q3 = df_mul(q2, q);
+    dfl in = df_add(df_add({2.0f / 3.0f, 0.0f}, df_neg(q2)), {0.5f * q3.hi, 0.5f * q3.lo});
+    *w = df_mul(g.df_factor, in).hi;
+    dfl a = df_mul(df_mul(g.df_factor, df_add({-2.0f, 0.0f}, df_mul({1.5f, 0.0f}, q))), g.df_yhh);
+    *dw0 = (dx.hi == 0.0f) ? -0.0f : df_mul(a, dx).hi;  // a < 0: a * (+0) = -0
+    *dw1 = (dy.hi == 0.0f) ? -0.0f : df_mul(a, dy).hi;
+  } else if (q.hi < 2.0f || (q.hi == 2.0f && q.lo <= 0.0f)) {
+    dfl t = df_add({2.0f, 0.0f}, df_neg(q));
+    dfl t2 = df_mul(t, t);
+    *w = df_mul(g.df_factor6, df_mul(t2, t)).hi;
+    dfl a = df_mul(df_mul(g.df_c3, t2), g.df_yh);
+    dfl ar = df_div(a, r);
+    *dw0 = (dx.hi == 0.0f) ? -0.0f : -df_mul(ar, dx).hi;  // -(a * (+0)) = -0
+    *dw1 = (dy.hi == 0.0f) ? -0.0f : -df_mul(ar, dy).hi;
+  }
+}
+
 // Pairs created by the particle at sorted position s, in the reference's creation order:
 // the rest of its own cell, the cell to its right, then the three cells of the row above.
 // FAST = false: W and dW from the reference's FP64 kernel, stored in FP32 (the plain
@@ -293,6 +390,7 @@ __global__ void k_half(Dev D) {
   int nx = g.ndiv[0], ny = g.ndiv[1];
   int ix = c % nx, iy = c / nx;
   float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
+  float xal = FAST ? D.xrl[a] : 0.0f, yal = FAST ? D.yrl[a] : 0.0f;
   const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
   int k = 0;
   int4* out = D.half + (size_t)s * D.capH;
@@ -323,6 +421,14 @@ __global__ void k_half(Dev D) {
         wf = (float)w;
         d0f = (float)dw0;
         d1f = (float)dw1;
+      } else if (g.uniform_h) {
+        // separation as double-float from the cell-relative hi/lo offsets
+        // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float
+        dfl ddx = df_add(df_add({xa, xal}, {-D.xr[b], -D.xrl[b]}),
+                         {-(float)cells[q][0] * g.df_cell[0].hi, -(float)cells[q][0] * g.df_cell[0].lo});
+        dfl ddy = df_add(df_add({ya, yal}, {-D.yr[b], -D.yrl[b]}),
+                         {-(float)cells[q][1] * g.df_cell[1].hi, -(float)cells[q][1] * g.df_cell[1].lo});
+        cubic_df(g, ddx, ddy, &wf, &d0f, &d1f);
       } else {
         float hm = (ha + D.hr[b]) * 0.5f;
         float rf = sqrtf(fx * fx + fy * fy);

@@ -335,6 +335,8 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     D.xr = dalloc<float>(c, N2);
     D.yr = dalloc<float>(c, N2);
     D.hr = dalloc<float>(c, N2);
+    D.xrl = dalloc<float>(c, N2);
+    D.yrl = dalloc<float>(c, N2);
     D.grid = dalloc<sps::Grid>(c, 1);
     D.nbbox_blocks = (int)((N2 + kBlock - 1) / kBlock);
     D.bbox_part = dalloc<double>(c, 6 * (size_t)D.nbbox_blocks + 8);

@@ -75,14 +75,24 @@ def compare(problem, nsteps, tol_s=1e-4, tol_v=1e-4, tol_d=1e-4, tol_linf=1e-3):
 
 def test_fast_pairs_identical(built_gpu):
     p = cases.bui_like()
+    # after three steps the positions of the two forms differ slightly; the pair set
+    # must still be the same (the lattice is far from the support radius)
     cf, _ = run(p, _abi.SPS_PREC_FP32_FAST, 3)
     cp, _ = run(p, _abi.SPS_PREC_FP64_PLAIN, 3)
     a, b = cf.dump_pairs(), cp.dump_pairs()
     np.testing.assert_array_equal(a["pair_i"], b["pair_i"])
     np.testing.assert_array_equal(a["pair_j"], b["pair_j"])
     np.testing.assert_array_equal(a["pint_type"], b["pint_type"])
-    # FP32-evaluated kernel values agree with the FP64-evaluated, FP32-stored ones
-    np.testing.assert_allclose(a["w"], b["w"], rtol=2e-6, atol=1e-6 * np.abs(b["w"]).max())
+    # kernel values are compared on the first step, where the positions are identical
+    cf, _ = run(p, _abi.SPS_PREC_FP32_FAST, 1)
+    cp, _ = run(p, _abi.SPS_PREC_FP64_PLAIN, 1)
+    a, b = cf.dump_pairs(), cp.dump_pairs()
+    # the FP32 form evaluates the kernel in double-float and must reproduce the FP32-stored
+    # values of the FP64 evaluation except within ~1e-12 of a rounding boundary
+    for k in ("w", "dwdx", "dwdy"):
+        same = a[k].view(np.int32) == b[k].view(np.int32)
+        assert same.mean() >= 0.99999, (k, same.mean())
+        np.testing.assert_allclose(a[k], b[k], rtol=3e-7, atol=1e-30)
 
 
 def test_fast_column(built_gpu):
