@@ -170,6 +170,44 @@ int sps_last_error(sps_ctx* ctx, char* buf, int32_t len);
 
 void sps_destroy(sps_ctx* ctx);
 
+/* ---- allocation-free neighbour statistics (no counterpart in the reference) -----------
+   For callers that cannot call cudaMalloc -- hosts whose device memory is all reserved by
+   their own pool allocator, so that a further cudaMalloc fails although the pool has room,
+   and loops with a latency bound that may not take the device-wide synchronisation that
+   cudaMalloc and cudaFree can imply.  No context is needed and no device memory is
+   allocated: all device scratch is one fixed array of SPS_STATIC_SCRATCH_BYTES inside
+   this library's device code, which limits a call to SPS_STATIC_MAX_PARTICLES particles.
+
+   For the n particles x(2,n), hsml(n), on the current device: degree[a] = the number of
+   particles b != a the step's pair test accepts (r < scale_k (h_a + h_b) / 2, scale_k = 2
+   for skf 1 and 3 otherwise, the test of grid_find_NEW, code/2_SPH_main_2018.f90:1345-1353),
+   wsum[a] = the sum over those b of the kernel value W_ab rounded to FP32 as the step
+   stores it (kernel of code/2_SPH_main_2018.f90:1458-1560 with the caller's pi), and
+   *npairs = the number of accepted pairs.  As in the step, b is looked for only in the
+   3 x 3 cells (2 hmax wide) of the step's grid around a, so with skf 2 or 3 partners more
+   than one cell away are not counted; the pair set is the one the step builds when every
+   particle lies inside the domain.  The sums run in an unspecified order (rounding at the
+   1e-16 relative level may differ between calls).
+   stream: a cudaStream_t to run on, or NULL for the default stream; the call
+   synchronises it before returning.  msg (msg_len bytes, may be NULL) receives a
+   NUL-terminated message when the call fails.
+   Returns SPS_ERR_CAPACITY when n > SPS_STATIC_MAX_PARTICLES or the particles span more
+   than SPS_STATIC_MAX_CELLS cells of the grid, SPS_ERR_ARG for bad
+   arguments (NULL pointers, skf outside 1..3, a non-finite position or a non-positive
+   smoothing length), SPS_ERR_CUDA for a runtime failure.
+   The first call on each device looks the scratch array's address up
+   (cudaGetSymbolAddress), which may load this library's device code onto that device;
+   make that first call before any stream capture begins.  Every call on a device shares
+   the one scratch array, so calls that overlapped would race on it: each call holds a
+   process-wide lock and synchronises its stream before it returns, so calls from several
+   host threads run one after another. */
+#define SPS_STATIC_MAX_PARTICLES 65536
+#define SPS_STATIC_MAX_CELLS 65536
+#define SPS_STATIC_SCRATCH_BYTES 3670016 /* 3.5 MiB */
+int sps_neighbour_stats_static(int32_t n, const double* x, const double* hsml, int32_t skf,
+                               double pi, void* stream, int32_t* degree, double* wsum,
+                               int64_t* npairs, char* msg, int32_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif
