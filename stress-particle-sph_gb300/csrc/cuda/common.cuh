@@ -108,6 +108,17 @@ struct Dev {
   float4* recA;   // {sxx, syy, sxy}/rho^2 (hi), m               nodes + stress-points
   float4* recAl;  // {sxx, syy, sxy}/rho^2 (lo), 0               nodes + stress-points
   double* Ddev;
+  // training capture (sps_capture): one tuple per loading stress-point evaluation
+  float* cap_buf;               // (cap_max, 18) floats, or null when not capturing
+  unsigned long long* cap_cnt;  // tuples offered since the capture started
+  long long cap_max;
+  // learned surrogate (sps_surrogate_install), FP32 form only
+  int surr;
+  const uint2* mlp_frag;  // packed BF16 B fragments of the four layers
+  const float* mlp_bias;  // FP32 biases of the four layers
+  float env_lo[14], env_hi[14], out_max;
+  double surr_tol;
+  unsigned long long* surr_cnt;  // loading, answered, outside envelope, drift-rejected
   // cells
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
   float *xr, *yr, *hr;
@@ -334,6 +345,7 @@ int launch_fast_step(Ctx& c);
 void launch_vol(Ctx& c, int lo, int hi);
 void launch_finterp(Ctx& c);
 void launch_fderivs(Ctx& c, int stage);
+void launch_fsp_tail(Ctx& c, int stage);
 void launch_fxsph(Ctx& c);
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 }  // namespace sps

@@ -38,6 +38,12 @@ struct Ctx {
   // per-kernel event timing (sps_profile_step)
   bool profiling = false;
   std::vector<std::pair<const char*, cudaEvent_t>> prof_events;
+  // training capture and learned surrogate (device buffers freed at destroy)
+  float* cap_buf = nullptr;
+  unsigned long long* cap_cnt = nullptr;
+  uint2* mlp_frag = nullptr;
+  float* mlp_bias = nullptr;
+  unsigned long long* surr_cnt = nullptr;
   int64_t kernels_launched = 0;  // kernels enqueued by the launch functions
   int kernels_per_step = 0;
   // called before each kernel group: counts its kernels and, when profiling, records an

@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
     }
     double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
     double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
-    tail_sp(D, sc, t, g, AE, f2);
+    if (D.surr) tail_sp_grad(D, t, g, AE);  // the rates follow in k_fsp_tail
+    else tail_sp(D, sc, t, g, AE, f2);
   } else if (is_node(tt)) {
     Kahan q0, q1, q2, q3, q4, q5, e0, e1, e2, e3;
     ProdSum sx, sy;
@@ -295,6 +296,109 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
   }
 }
 
+// Stress-point rates with the learned surrogate (FP32 form): one thread per stress-point,
+// one warp per 32 consecutive stress-points.  Loading stress-points whose inputs lie in the
+// training envelope are packed into 16-row tiles of the warp and sent through the network
+// together on the tensor cores (mma.m16n8k16, BF16 in, FP32 accumulate); a prediction is
+// kept when the yield-function drift it causes over one step,
+//   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
+// is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
+// Every other stress-point takes the exact flow rule through the same tail as k_fderivs.
+__global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
+  __shared__ float xs[4][32][16];
+  __shared__ float ys[4][32][8];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = i < D.NT - D.NN;
+  const int t = D.NN + (act ? i : 0);
+  const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
+  const double f2 = f2rk[stage];
+  const StepScalars& sc = *D.cur;
+  double g[4] = {0.0, 0.0, 0.0, 0.0}, s2v[4] = {0.0, 0.0, 0.0, 0.0};
+  float x[16];
+  double scale = 0.0;
+  bool loading = false, cand = false;
+  if (act && D.ntype_eco > 1 && D.ncrit == 12) {
+    const double* gu = D.grad_u + 4 * (size_t)t;
+    for (int k = 0; k < 4; k++) g[k] = gu[k];
+    s2v[0] = D.s0[t];
+    s2v[1] = D.s1[t];
+    s2v[2] = D.s2[t];
+    s2v[3] = D.s3[t];
+    if (D.ntype_solid == 1) s2v[3] = D.poiss * (s2v[0] + s2v[1]);
+    double f = D.fdp[t], G2[4], vivel[4];
+    drucker_prager(D, sc.time_sph, s2v, g, &f, G2, vivel);  // loading test only
+    loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
+    if (loading) {
+      scale = mlp_features(s2v, g, D.tanfi, D.coh, D.young, D.poiss, D.rho[t], x);
+      cand = scale > 0.0;
+      for (int k = 0; k < MLP_NIN && cand; k++)
+        cand = x[k] >= D.env_lo[k] && x[k] <= D.env_hi[k];
+    }
+  }
+  const unsigned mask = __ballot_sync(0xffffffffu, cand);
+  const int nrows = __popc(mask);
+  double Gnet[4];
+  bool accept = false;
+  if (nrows) {  // warp-uniform
+    const int row = __popc(mask & ((1u << lane) - 1u));
+    const int ntile = (nrows + 15) >> 4;
+    if (cand)
+      for (int k = 0; k < 16; k++) xs[w][row][k] = x[k];
+    for (int r = nrows + lane; r < ntile * 16; r += 32)
+      for (int k = 0; k < 16; k++) xs[w][r][k] = 0.0f;
+    __syncwarp();
+    mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[w][0][0], &ys[w][0][0], lane);
+    if (ntile > 1) mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[w][16][0], &ys[w][16][0], lane);
+    __syncwarp();
+    if (cand) {
+      bool inside = true;
+      for (int k = 0; k < MLP_NOUT; k++) {
+        float yk = ys[w][row][k];
+        inside = inside && fabsf(yk) <= 1.5f * D.out_max;
+        Gnet[k] = (double)yk * scale;
+      }
+      if (inside) {
+        // drift test in FP64
+        double sm = ((s2v[0] + s2v[1]) + s2v[3]) / 3.0;
+        double d0 = s2v[0] - sm, d1 = s2v[1] - sm, d2 = s2v[2], d3 = s2v[3] - sm;
+        double sj = sqrt(d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3));
+        double e0 = D.D11 * g[0] + D.D12 * g[3] + Gnet[0];
+        double e1 = D.D12 * g[0] + D.D22 * g[3] + Gnet[1];
+        double e2 = D.D33 * g[1] + D.D33 * g[2] + Gnet[2];
+        double e3 = D.D41 * g[0] + D.D42 * g[3] + Gnet[3];
+        double df = (d0 * e0 + d1 * e1 + d3 * e3 + 2.0 * d2 * e2) / (2.0 * sj) +
+                    D.alpha2 * (e0 + e1 + e3);
+        accept = sj > 0.0 && D.dt * fabs(df) <= D.surr_tol * sj;
+      } else {
+        cand = false;  // counted as outside the envelope
+      }
+    }
+  }
+  // counters: loading, answered, outside the envelope, drift-rejected
+  {
+    unsigned ml = __ballot_sync(0xffffffffu, loading), ma = __ballot_sync(0xffffffffu, accept),
+             mc = __ballot_sync(0xffffffffu, cand);
+    if (lane == 0 && ml) {
+      atomicAdd(&D.surr_cnt[0], (unsigned long long)__popc(ml));
+      atomicAdd(&D.surr_cnt[1], (unsigned long long)__popc(ma));
+      atomicAdd(&D.surr_cnt[2], (unsigned long long)(__popc(ml) - __popc(mc)));
+      atomicAdd(&D.surr_cnt[3], (unsigned long long)(__popc(mc) - __popc(ma)));
+    }
+  }
+  if (!act) return;
+  if (accept) {
+    // plastic strain rate of the predicted source: e_p = G / (2 G_mod), shear G / G_mod
+    const double gm = D.young / (2.0 * (1.0 + D.poiss));
+    double v0 = -Gnet[0] / (2.0 * gm), v1 = -Gnet[1] / (2.0 * gm), v2 = -Gnet[2] / gm,
+           v3 = -Gnet[3] / (2.0 * gm);
+    double der = sqrt((2.0 * ((v0 * v0 + v1 * v1) + v3 * v3) + v2 * v2) / 3.0);
+    tail_sp_rates(D, sc, t, D.grad_u + 4 * (size_t)t, f2, Gnet, der);
+  } else {
+    tail_sp_rates(D, sc, t, D.grad_u + 4 * (size_t)t, f2);
+  }
+}
+
 // XSPH_update (2_SPH_main_2018.f90:189-239), FP32 sums of double-float velocity differences
 __global__ void k_fxsph(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -331,6 +435,10 @@ void launch_finterp(Ctx& c) {
 }
 void launch_fderivs(Ctx& c, int stage) {
   k_fderivs<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d, stage);
+}
+void launch_fsp_tail(Ctx& c, int stage) {
+  int ns = c.d.NT - c.d.NN;
+  if (ns > 0) k_fsp_tail<<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
   k_fxsph<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);

@@ -630,6 +630,10 @@ int launch_plain_step(Ctx& c) {
     c.mark("derivs");
     if (D.fast) launch_fderivs(c, stage);
     else k_derivs<<<nb2, kBlock, 0, st>>>(D, stage);
+    if (D.surr) {
+      c.mark("sp_tail");
+      launch_fsp_tail(c, stage);
+    }
   }
   c.mark("rk_final");
   k_rk_final<<<nbT, kBlock, 0, st>>>(D);

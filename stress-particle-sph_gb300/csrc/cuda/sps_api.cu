@@ -19,6 +19,8 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "mlp.cuh"
+#include "sps_surrogate.h"
 
 struct sps_ctx {
   sps::Ctx c;
@@ -788,10 +790,138 @@ void sps_destroy(sps_ctx* h) {
   if (!h) return;
   sps::Ctx& c = h->c;
   if (c.graph) cudaGraphExecDestroy(c.graph);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  for (void* p : {(void*)c.cap_buf, (void*)c.cap_cnt, (void*)c.mlp_frag, (void*)c.mlp_bias,
+                  (void*)c.surr_cnt})
+    if (p) cudaFree(p);
   for (void* p : c.allocs) cudaFree(p);
   if (c.h_err) cudaFreeHost(c.h_err);
   if (c.stream) cudaStreamDestroy(c.stream);
   delete h;
+}
+
+// ---- learned surrogate: capture and installation (include/sps_surrogate.h) ----------------
+
+int sps_capture(sps_ctx* h, int64_t cap) {
+  if (!h || cap < 0) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    if (c.cap_buf) cudaFree(c.cap_buf);
+    c.cap_buf = nullptr;
+    c.d.cap_buf = nullptr;
+    c.d.cap_max = 0;
+    if (cap > 0) {
+      if (!c.cap_cnt) {
+        void* p = nullptr;
+        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(unsigned long long)));
+        c.cap_cnt = static_cast<unsigned long long*>(p);
+      }
+      void* p = nullptr;
+      SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(float) * SPS_MLP_TUPLE * (size_t)cap));
+      c.cap_buf = static_cast<float*>(p);
+      SPS_CUDA_CHECK(cudaMemsetAsync(c.cap_cnt, 0, sizeof(unsigned long long), c.stream));
+      c.d.cap_buf = c.cap_buf;
+      c.d.cap_cnt = c.cap_cnt;
+      c.d.cap_max = cap;
+    }
+    if (c.graph) {  // kernel arguments changed
+      cudaGraphExecDestroy(c.graph);
+      c.graph = nullptr;
+    }
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_capture_read(sps_ctx* h, float* tuples, int64_t* n, int64_t* seen) {
+  if (!h || !n || *n < 0 || (*n > 0 && !tuples)) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!c.cap_buf) return fail(&c, SPS_ERR_STATE, "sps_capture_read without sps_capture");
+  try {
+    unsigned long long cnt = 0;
+    SPS_CUDA_CHECK(cudaMemcpyAsync(&cnt, c.cap_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    int64_t held = std::min<int64_t>((int64_t)cnt, c.d.cap_max);
+    int64_t k = std::min<int64_t>(held, *n);
+    if (k > 0)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(tuples, c.cap_buf, sizeof(float) * SPS_MLP_TUPLE * (size_t)k,
+                                     cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    *n = k;
+    if (seen) *seen = (int64_t)cnt;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
+  if (!h || (m && !o)) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (m && c.precision != SPS_PREC_FP32_FAST)
+    return fail(&c, SPS_ERR_UNSUPPORTED, "the surrogate runs in the FP32 form only");
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    if (m) {
+      if (!c.mlp_frag) {
+        void* p = nullptr;
+        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(uint2) * sps::MLP_FRAG_U2));
+        c.mlp_frag = static_cast<uint2*>(p);
+        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(float) * sps::MLP_BIAS));
+        c.mlp_bias = static_cast<float*>(p);
+        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(unsigned long long) * 4));
+        c.surr_cnt = static_cast<unsigned long long*>(p);
+      }
+      cudaStream_t ms = sps::mlp_stream(m);
+      SPS_CUDA_CHECK(cudaStreamSynchronize(ms));
+      sps::mlp_pack(m, c.mlp_frag, c.mlp_bias, ms);
+      SPS_CUDA_CHECK(cudaGetLastError());
+      SPS_CUDA_CHECK(cudaStreamSynchronize(ms));
+      SPS_CUDA_CHECK(cudaMemsetAsync(c.surr_cnt, 0, sizeof(unsigned long long) * 4, c.stream));
+      c.d.surr = 1;
+      c.d.mlp_frag = c.mlp_frag;
+      c.d.mlp_bias = c.mlp_bias;
+      c.d.surr_cnt = c.surr_cnt;
+      c.d.surr_tol = o->tol;
+      for (int k = 0; k < SPS_MLP_NIN; k++) {
+        c.d.env_lo[k] = o->env_lo[k];
+        c.d.env_hi[k] = o->env_hi[k];
+      }
+      c.d.out_max = o->out_max;
+    } else {
+      c.d.surr = 0;
+    }
+    if (c.graph) {
+      cudaGraphExecDestroy(c.graph);
+      c.graph = nullptr;
+    }
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_surrogate_stats(sps_ctx* h, int64_t* counts, int32_t reset) {
+  if (!h || !counts) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!c.surr_cnt) {
+    for (int k = 0; k < 4; k++) counts[k] = 0;
+    return SPS_OK;
+  }
+  try {
+    unsigned long long v[4];
+    SPS_CUDA_CHECK(cudaMemcpyAsync(v, c.surr_cnt, sizeof(v), cudaMemcpyDeviceToHost, c.stream));
+    if (reset) SPS_CUDA_CHECK(cudaMemsetAsync(c.surr_cnt, 0, sizeof(v), c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    for (int k = 0; k < 4; k++) counts[k] = (int64_t)v[k];
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
 }
 
 }  // extern "C"

@@ -7,6 +7,7 @@
 // -fmad=false) these reproduce the reference's rounding exactly.
 #pragma once
 #include "common.cuh"
+#include "mlp.cuh"
 
 namespace sps {
 
@@ -31,9 +32,22 @@ __device__ __forceinline__ void apply_bcs(const Dev& D, const StepScalars& sc, i
 }
 
 
-// stress-point tail: g = grad1(a,b) at a + 2b, AE = CSPM moments (used when cspm)
-__device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int t, double* g,
-                                        double* AE, double f2) {
+// training capture: the exact flow rule's inputs and its plastic source Gs, scaled
+__device__ __forceinline__ void capture_tuple(const Dev& D, int t, const double* s2v,
+                                              const double* g, const double* Gs) {
+  float x[16];
+  double scale = mlp_features(s2v, g, D.tanfi, D.coh, D.young, D.poiss, D.rho[t], x);
+  if (!(scale > 0.0)) return;
+  unsigned long long k = atomicAdd(D.cap_cnt, 1ull);
+  if ((long long)k >= D.cap_max) return;
+  float* o = D.cap_buf + (size_t)k * MLP_TUPLE;
+  for (int j = 0; j < MLP_NIN; j++) o[j] = x[j];
+  for (int j = 0; j < MLP_NOUT; j++) o[MLP_NIN + j] = (float)(Gs[j] / scale);
+}
+
+// stress-point gradient: CSPM correction of g = grad1(a,b) (at a + 2b) with the moments AE,
+// stored as grad_u
+__device__ __forceinline__ void tail_sp_grad(const Dev& D, int t, double* g, const double* AE) {
     if (D.cspm) {
       double A4 = AE[0] * AE[3] - AE[1] * AE[2];
       double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
@@ -56,6 +70,15 @@ __device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int
     gu[1] = g[1];
     gu[2] = g[2];
     gu[3] = g[3];
+}
+
+// stress-point rates after the gradient: D : grad(v), plastic_terms / drucker_prager,
+// Jaumann spin, RHS and RK4 accumulation.  Gs_net (may be null): a plastic source from the
+// learned surrogate that replaces the exact one (with its plastic strain rate der_net)
+__device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& sc, int t,
+                                              const double* g, double f2,
+                                              const double* Gs_net = nullptr,
+                                              double der_net = 0.0) {
     const double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
     double div1[4];
     div1[0] = -(D.D11 * g11 + D.D12 * g22);
@@ -74,10 +97,16 @@ __device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int
         drucker_prager(D, sc.time_sph, s2v, g, &f, G2, vivel);
         D.fdp[t] = f;
         for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
+        if (D.cap_buf && (G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0))
+          capture_tuple(D, t, s2v, g, Gs);
       }
       der = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
                   vivel[2] * vivel[2]) /
                  3.0);
+    }
+    if (Gs_net) {
+      for (int k = 0; k < 4; k++) Gs[k] = Gs_net[k];
+      der = der_net;
     }
     double spin[4] = {0.0, 0.0, 0.0, 0.0};
     if (D.update_x) {
@@ -97,6 +126,13 @@ __device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int
       D.RKr[t] = D.RKr[t] + f2 * D.RHSr[t];
       if (D.sle == 2) D.RKh[t] = D.RKh[t] + f2 * D.RHSh[t];
     }
+}
+
+// stress-point tail: g = grad1(a,b) at a + 2b, AE = CSPM moments (used when cspm)
+__device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int t, double* g,
+                                        double* AE, double f2) {
+  tail_sp_grad(D, t, g, AE);
+  tail_sp_rates(D, sc, t, g, f2);
 }
 
 // node tail: g2 = grad2(s,b) at s + 3b, AE = CSPM moments, av = artificial viscosity

@@ -29,6 +29,7 @@ def test_headers_declare_functions():
 
 
 @pytest.mark.parametrize("header,lib", [("sps.h", "libsps_gb300.so"),
+                                        ("sps_surrogate.h", "libsps_gb300.so"),
                                         ("sph_host.h", "libsph_host.so")])
 def test_library_exports_header(built, header, lib):
     import sps_gb300
