@@ -17,7 +17,14 @@ e2e    = the same metric through the C-ABI with host buffers: every step uploads
          state from pinned host memory (sps_upload), advances one step (sps_step) and
          downloads the fields (sps_download).
 --impl reference times the CPU restatement of the reference's step (the oracle; the
-         Fortran reference cannot be compiled on either machine) on a bounded sample.
+         Fortran reference cannot be compiled on either machine) on a bounded sample, as
+         independent single-threaded replicas on every host core the process may use.
+
+The headline runs the FP32 form with the learned Drucker-Prager surrogate installed
+(trained first, on the GPU, on tuples captured from coarse runs of the same slope with
+seeded material draws); the FP32 form without it and the FP64 plain form are timed beside
+it on the same workload, and the errors of both FP32 runs against the plain run are
+reported after the same number of steps.
 """
 import argparse
 import json
@@ -49,6 +56,8 @@ def parse():
     ap.add_argument("--dx", type=float, default=0.012)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate-tol", type=float, default=1e-6)
     return ap.parse_args()
 
 
@@ -153,6 +162,48 @@ def fp64_peak_tflops():
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+# material ranges of the surrogate's training runs (stratified draws bracket the slope's)
+SURR_RANGES = dict(phi_deg=(26.0, 34.0), cohesion=(6e3, 14e3), young=(14e6, 26e6),
+                   poiss=(0.27, 0.33), rho=(1800.0, 1900.0), k0=(0.42, 0.58))
+
+
+def train_surrogate(seed=0, nruns=6, dx=0.08, nsteps=2000, every=20, max_tuples=4000000,
+                    schedule=((10, 2e-3), (6, 5e-4), (4, 1e-4))):
+    """Capture tuples from coarse FP32 runs of the slope geometry with seeded materials and
+    train the network on the GPU; returns (net, envelope, summary)."""
+    import numpy as np
+    import sps_gb300
+    from sps_gb300 import _abi
+    from sps_gb300 import surrogate as sg
+    w0 = time.perf_counter()
+    runs = []
+    for mat in sg.stratified_materials(SURR_RANGES, nruns, seed):
+        prob = sps_gb300.Problem.slope(dx=dx, **dict(SLOPE, **mat))
+        runs.append(sg.sample_run(prob, _abi.SPS_PREC_FP32_FAST, nsteps, every))
+    data = np.concatenate(runs)
+    captured = len(data)
+    w1 = time.perf_counter()
+    idx = np.random.default_rng(seed).permutation(len(data))[:max_tuples]
+    nhold = min(20000, len(data) // 10)
+    hold, train = data[idx[:nhold]], data[idx[nhold:]]
+    net = sg.Mlp(batch=4096, seed=seed + 1)
+    net.set_data(train)
+    loss = net.fit(schedule)
+    w2 = time.perf_counter()
+    y = net.predict(hold[:, :sg.NIN])
+    t = hold[:, sg.NIN:].astype(np.float64)
+    held = float(np.linalg.norm(y - t) / max(np.linalg.norm(t), 1e-300))
+    summary = {"tuples": int(len(train)), "captured": int(captured), "runs": nruns,
+               "runs_desc": "slope geometry at dx %.3g m, %d steps, one step in %d captured, "
+                            "stratified draws of %s" % (dx, nsteps, every, SURR_RANGES),
+               "capture_s": round(w1 - w0, 2), "train_s": round(w2 - w1, 2),
+               "epochs": int(len(loss)), "schedule": [list(x) for x in schedule],
+               "loss_first_epoch": float(loss[0]),
+               "loss_last_epoch": float(loss[-1]), "heldout_rel_l2": round(held, 4),
+               "network": "14-128-128-128-4 SiLU, BF16 weights/activations, FP32 accumulate"}
+    return net, sg.Envelope.of(train), summary
+
+
 def workload(dx):
     import sps_gb300
     return sps_gb300.Problem.slope(dx=dx, **SLOPE)
@@ -232,13 +283,33 @@ def run_ours(args):
     nparticles = prob.nnode + prob.nstress
     fast = args.precision == "fast"
     prec = _abi.SPS_PREC_FP32_FAST if fast else _abi.SPS_PREC_FP64_PLAIN
+    use_surr = fast and not args.no_surrogate
+    surr = None
+    if use_surr:
+        from sps_gb300 import surrogate as sg
+        net, env, training = train_surrogate()
     ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", prob.params_copy(precision=prec))
     ctx.upload_problem(prob)
+    if use_surr:
+        sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
     t = ctx.step(max(args.warmup, 1), 0.0)  # warm-up (also instantiates the step graph)
     kps = sps_gb300.kernels_per_step(ctx)
+    if use_surr:
+        sg.stats(ctx, reset=True)
     t, ms_max, clk = timed_steps(ctx, args.steps, t, dist, local)
     value = nparticles * args.steps * world / (ms_max * 1e-3)
     nsteps_done = max(args.warmup, 1) + args.steps
+    if use_surr:
+        loading, answered, outside, rejected = sg.stats(ctx)
+        lf = max(loading, 1)
+        surr = {"tol": args.surrogate_tol,
+                "drift_test": "dt |grad f : (D:e + Gs)| / sqrt(J2) <= tol",
+                "training": training,
+                "timed_loading_evaluations": loading,
+                "answered_frac": round(answered / lf, 6),
+                "outside_envelope_frac": round(outside / lf, 6),
+                "drift_rejected_frac": round(rejected / lf, 6),
+                "fallback_rate": round(1.0 - answered / lf, 6)}
 
     plain = None
     errors = None
@@ -253,13 +324,29 @@ def run_ours(args):
                  "ms_per_step": round(ms_p / args.steps, 4), "dtype": "f64"}
         ff, fp = ctx.download(), cp.download()
         nt = prob.ntotal
-        sl2, sli = rel_errors(ff["stress"][:4 * nt], fp["stress"][:4 * nt])
-        vl2, vli = rel_errors(ff["vel"][:2 * nt], fp["vel"][:2 * nt])
-        dl2, dli = rel_errors(ff["displ"], fp["displ"])
-        errors = {"after_steps": nsteps_done, "time_s": t,
-                  "stress_rel_l2": sl2, "stress_rel_linf": sli, "vel_rel_l2": vl2,
-                  "vel_rel_linf": vli, "displ_rel_l2": dl2, "displ_rel_linf": dli,
-                  "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
+
+        def errs(a, b):
+            sl2, sli = rel_errors(a["stress"][:4 * nt], b["stress"][:4 * nt])
+            vl2, vli = rel_errors(a["vel"][:2 * nt], b["vel"][:2 * nt])
+            dl2, dli = rel_errors(a["displ"], b["displ"])
+            return {"after_steps": nsteps_done, "time_s": t,
+                    "stress_rel_l2": sl2, "stress_rel_linf": sli, "vel_rel_l2": vl2,
+                    "vel_rel_linf": vli, "displ_rel_l2": dl2, "displ_rel_linf": dli,
+                    "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
+        errors = errs(ff, fp)
+        if use_surr:
+            # the FP32 form without the surrogate, same workload and steps
+            cn = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                       prob.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+            cn.upload_problem(prob)
+            tn = cn.step(max(args.warmup, 1), 0.0)
+            tn, ms_n, _ = timed_steps(cn, args.steps, tn, dist, local)
+            v_n = nparticles * args.steps * world / (ms_n * 1e-3)
+            surr["fp32_without_surrogate"] = {
+                "value": round(v_n, 1), "ms_per_step": round(ms_n / args.steps, 4),
+                "error_vs_plain": errs(cn.download(), fp)}
+            surr["speed_with_over_without"] = round(value / v_n, 4)
+            cn.close()
         _, prof_p = sps_gb300.profile_steps(cp, 1, tp)
         plain["kernel_ms_per_step"] = {k: round(v[0], 4) for k, v in sorted(
             prof_p.items(), key=lambda kv: -kv[1][0])[:6]}
@@ -335,9 +422,10 @@ def run_ours(args):
                        "particles": nparticles, "pairs": deg["pairs"],
                        "l2": "state and pair tables (%.1f GB) larger than L2; no flush" % (
                            (prob.ntotal2 * (3 * 48 * 16 + 400)) / 1e9),
-                       "surrogate": "not built (exact Drucker-Prager return on every particle)",
+                       "surrogate": ("learned Drucker-Prager flow rule, exact fallback "
+                                     "(tol %g)" % args.surrogate_tol if use_surr else "off"),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "plain": plain, "error_vs_plain": errors,
+            "plain": plain, "error_vs_plain": errors, "surrogate": surr,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
             "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
             "kernel_ms_per_step": {k: round(v[0] / 2, 4) for k, v in sorted(
@@ -375,16 +463,34 @@ def cpu_baseline(args):
             "sample": sample}
 
 
+def _replica(seconds):
+    for p in (os.path.join(ROOT, "stress-particle-sph_gb300"), os.path.join(ROOT, "oracle")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    v, sample, steps = cpu_sample(seconds_target=seconds)
+    return v, sample, steps
+
+
 def run_reference(args):
     rank, world, dist = dist_init("gloo")
     if rank != 0:
         return
+    import multiprocessing as mp
     import orc
     orc.build()
     import sps_gb300
     sps_gb300.build_host()
-    per_step = max(2.0, 60.0 / max(args.steps + args.warmup, 1))
-    v, sample, steps = cpu_sample(seconds_target=per_step * args.steps)
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except AttributeError:
+        cores = os.cpu_count() or 1
+    seconds = min(60.0, max(10.0, 3.0 * args.steps))
+    # the reference step is single-threaded: one independent replica per host core
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_replica, [seconds] * cores)
+    v = sum(r[0] for r in res)
+    sample = "%d concurrent replicas (one per core) of: %s" % (cores, res[0][1])
+    steps = min(r[2] for r in res)
     line = {
         "metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world,
         "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
@@ -392,7 +498,7 @@ def run_reference(args):
         "impl": "reference",
         "config": {"workload": "vertical slope (same geometry and material), coarser sample",
                    "precision": "fp64 (reference mixed precision)"},
-        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": 1,
+        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": cores,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},

@@ -202,8 +202,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
     }
     double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
     double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
-    if (D.surr) tail_sp_grad(D, t, g, AE);  // the rates follow in k_fsp_tail
-    else tail_sp(D, sc, t, g, AE, f2);
+    tail_sp_grad(D, t, g, AE);  // the rates follow in k_fsp_tail
   } else if (is_node(tt)) {
     Kahan q0, q1, q2, q3, q4, q5, e0, e1, e2, e3;
     ProdSum sx, sy;
@@ -296,14 +295,16 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
   }
 }
 
-// Stress-point rates with the learned surrogate (FP32 form): one thread per stress-point,
-// one warp per 32 consecutive stress-points.  Loading stress-points whose inputs lie in the
-// training envelope are packed into 16-row tiles of the warp and sent through the network
-// together on the tensor cores (mma.m16n8k16, BF16 in, FP32 accumulate); a prediction is
-// kept when the yield-function drift it causes over one step,
+// Stress-point rates of the FP32 form (after k_fderivs has stored grad_u): one thread per
+// stress-point, one warp per 32 consecutive stress-points, so that the FP64 tail runs in
+// its own kernel on contiguous stress-points instead of diverging against the node branch
+// of k_fderivs.  With the learned surrogate installed, loading stress-points whose inputs
+// lie in the training envelope are packed into 16-row tiles of the warp and sent through
+// the network together on the tensor cores (mma.m16n8k16, BF16 in, FP32 accumulate); a
+// prediction is kept when the yield-function drift it causes over one step,
 //   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
 // is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
-// Every other stress-point takes the exact flow rule through the same tail as k_fderivs.
+// Every other stress-point takes the exact flow rule.
 __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   __shared__ float xs[4][32][16];
   __shared__ float ys[4][32][8];
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   float x[16];
   double scale = 0.0;
   bool loading = false, cand = false;
-  if (act && D.ntype_eco > 1 && D.ncrit == 12) {
+  if (act && D.surr && D.ntype_eco > 1 && D.ncrit == 12) {
     const double* gu = D.grad_u + 4 * (size_t)t;
     for (int k = 0; k < 4; k++) g[k] = gu[k];
     s2v[0] = D.s0[t];
@@ -376,7 +377,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     }
   }
   // counters: loading, answered, outside the envelope, drift-rejected
-  {
+  if (D.surr) {
     unsigned ml = __ballot_sync(0xffffffffu, loading), ma = __ballot_sync(0xffffffffu, accept),
              mc = __ballot_sync(0xffffffffu, cand);
     if (lane == 0 && ml) {

@@ -630,7 +630,7 @@ int launch_plain_step(Ctx& c) {
     c.mark("derivs");
     if (D.fast) launch_fderivs(c, stage);
     else k_derivs<<<nb2, kBlock, 0, st>>>(D, stage);
-    if (D.surr) {
+    if (D.fast) {
       c.mark("sp_tail");
       launch_fsp_tail(c, stage);
     }

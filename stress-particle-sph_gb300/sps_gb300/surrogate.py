@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .context import SpsError, gpu_lib
+from .context import SpsError, StepContext, gpu_lib
 
 NIN, NOUT, TUPLE, NPARAM = 14, 4, 18, 36232
 
@@ -194,3 +194,27 @@ def stats(ctx, reset=False):
     if rc != _abi.SPS_OK:
         raise SpsError("sps_surrogate_stats", rc, ctx._err())
     return tuple(int(v) for v in c)
+
+
+def sample_run(prob, precision, nsteps, every, cap=50000):
+    """Tuples of one step in every `every` over nsteps steps of a run of prob."""
+    ctx = StepContext(gpu_lib(), "sps", prob.params_copy(precision=precision))
+    ctx.upload_problem(prob)
+    out, t = [], 0.0
+    for _ in range(nsteps // every):
+        t = ctx.step(every - 1, t)
+        capture(ctx, cap)
+        t = ctx.step(1, t)
+        out.append(read_capture(ctx)[0])
+        capture(ctx, 0)
+    ctx.close()
+    return np.concatenate(out) if out else np.zeros((0, TUPLE), np.float32)
+
+
+def stratified_materials(ranges, n, seed):
+    """n material dicts: each parameter takes the n quantile mid-points of its (lo, hi)
+    range, in a seeded order, so that the draws bracket the middle of every range."""
+    rng = np.random.default_rng(seed)
+    q = (np.arange(n) + 0.5) / n
+    cols = {k: lo + (hi - lo) * rng.permutation(q) for k, (lo, hi) in ranges.items()}
+    return [{k: float(v[i]) for k, v in cols.items()} for i in range(n)]

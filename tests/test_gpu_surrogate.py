@@ -87,21 +87,6 @@ def test_captured_tuples_follow_flow_rule(built_gpu):
     assert all(r.tobytes() in held for r in tuples2)
 
 
-def sample_run(prob, precision, nsteps, every, cap=20000):
-    """Tuples of one step in every `every` over nsteps steps of a run."""
-    ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", prob.params_copy(precision=precision))
-    ctx.upload_problem(prob)
-    out, t = [], 0.0
-    for _ in range(nsteps // every):
-        t = ctx.step(every - 1, t)
-        sg.capture(ctx, cap)
-        t = ctx.step(1, t)
-        out.append(sg.read_capture(ctx)[0])
-        sg.capture(ctx, 0)
-    ctx.close()
-    return np.concatenate(out)
-
-
 # material ranges of the training draws; the evaluation column sits inside them
 RANGES = dict(phi_deg=(18, 34), cohesion=(0, 400), young=(4e6, 4e7), poiss=(0.22, 0.34),
               rho=(1900, 2700), k0=(0.3, 0.6))
@@ -109,16 +94,9 @@ EVAL_MATERIAL = dict(phi_deg=25.0, cohesion=150.0, young=1.5e7, poiss=0.28, rho=
 
 
 def training_set(seed=0, ncol=6, nsteps=1500, every=15):
-    """Tuples from column collapses with seeded, stratified material draws (each parameter
-    takes the ncol quantile mid-points of its range in a seeded order)."""
-    rng = np.random.default_rng(seed)
-    q = (np.arange(ncol) + 0.5) / ncol
-    cols = {k: lo + (hi - lo) * rng.permutation(q) for k, (lo, hi) in RANGES.items()}
-    out = []
-    for i in range(ncol):
-        mat = {k: float(v[i]) for k, v in cols.items()}
-        out.append(sample_run(cases.column(dx=0.004, **mat), _abi.SPS_PREC_FP32_FAST, nsteps,
-                              every))
+    """Tuples from column collapses with seeded, stratified material draws."""
+    out = [sg.sample_run(cases.column(dx=0.004, **mat), _abi.SPS_PREC_FP32_FAST, nsteps, every)
+           for mat in sg.stratified_materials(RANGES, ncol, seed)]
     return np.concatenate(out)
 
 
