@@ -78,6 +78,7 @@ struct Dev {
   double D11, D12, D22, D33, D41, D42;
   double tanfi, coh, young, poiss;
   double alpha2, kc;  // adapt_stress2 constants (FP64)
+  double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
   double xmin_dom[2], xmax_dom[2];
   double cgrav[2];
   int bcvar[kMaxBC];
@@ -272,15 +273,57 @@ __device__ __forceinline__ void adapt_stress(double alpha2, double kc, double& a
   }
 }
 
+// The same return for the FP32 form, without FP64 divisions or square roots in the common
+// path (GB300 issues FP64 at a small fraction of its FP32 rate): the mean by a product with
+// 1/3, the test yield < sqrt(J2) as yield^2 < J2 (yield >= 0), and for the stress-points
+// actually returned 1/sqrt(J2) from an FP32 seed refined by two Newton steps in FP64
+// (relative error ~1e-16).  Explicit fma() keeps the FMA where the unit disables it.
+__device__ __forceinline__ void adapt_stress_fast(double alpha2, double kc, double shift,
+                                                  double& a, double& b, double& c, double& d) {
+  const double third = 1.0 / 3.0;
+  double smean = ((a + b) + d) * third;
+  double d0 = a - smean, d1 = b - smean, d2 = c, d3 = d - smean;
+  double varj2 = fma(d2, d2, 0.5 * fma(d0, d0, fma(d1, d1, d3 * d3)));
+  double yield = fma(-3.0 * alpha2, smean, kc);
+  if (yield < 0) {
+    a = (a - smean) + shift;
+    b = (b - smean) + shift;
+    d = (d - smean) + shift;
+    smean = ((a + b) + d) * third;
+    d0 = a - smean;
+    d1 = b - smean;
+    d2 = c;
+    d3 = d - smean;
+    varj2 = fma(d2, d2, 0.5 * fma(d0, d0, fma(d1, d1, d3 * d3)));
+    yield = fma(-3.0 * alpha2, smean, kc);
+  }
+  if (yield < 0 || yield * yield < varj2) {
+    double rn = 0.0;
+    if (varj2 > (double)1e-5f * (double)1e-5f) {
+      double rs = (double)rsqrtf((float)varj2);
+      rs = rs * fma(-0.5 * varj2 * rs, rs, 1.5);
+      rs = rs * fma(-0.5 * varj2 * rs, rs, 1.5);
+      rn = yield * rs;
+    }
+    a = fma(rn, d0, smean);
+    b = fma(rn, d1, smean);
+    d = fma(rn, d3, smean);
+    c = rn * d2;
+  }
+}
+
 // drucker_prager (3_SPH_material_2018.f90:1958-2083): FP32 body.  s: stress (plane-stress
 // szz already substituted), gu: grad_u(2,2).  Updates *fdp, returns G and vivel.
+// FAST (the FP32 form): the FP64 mean by a product with 1/3 instead of a division.
+template <bool FAST = false>
 __device__ __forceinline__ void drucker_prager(const Dev& D, double time_sph, const double* s,
                                                const double* gu, double* fdp, double* G,
                                                double* vivel) {
   double f0 = *fdp;
   float tanfi = (float)D.tanfi, coh = (float)D.coh, young = (float)D.young,
         poiss = (float)D.poiss;
-  float smean = (float)(((s[0] + s[1]) + s[3]) / 3.0);
+  float smean = FAST ? (float)(((s[0] + s[1]) + s[3]) * (1.0 / 3.0))
+                     : (float)(((s[0] + s[1]) + s[3]) / 3.0);
   float dv0 = (float)(s[0] - (double)smean);
   float dv1 = (float)(s[1] - (double)smean);
   float dv2 = (float)s[2];

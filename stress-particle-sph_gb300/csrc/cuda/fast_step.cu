@@ -103,8 +103,9 @@ __global__ void k_finterp(Dev D) {
     }
     double norm = nm.val();
     if (norm != 0) {
-      D.vx[t] = ((double)ref.x + (double)ref.z) + v0.val() / norm;
-      D.vy[t] = ((double)ref.y + (double)ref.w) + v1.val() / norm;
+      double rn = 1.0 / norm;
+      D.vx[t] = ((double)ref.x + (double)ref.z) + v0.val() * rn;
+      D.vy[t] = ((double)ref.y + (double)ref.w) + v1.val() * rn;
     }
   } else {
     Kahan a, b, c, d, iv, rt, nm;
@@ -125,17 +126,18 @@ __global__ void k_finterp(Dev D) {
       nm.add(h1);
     }
     double norm = nm.val();
+    double rn = 1.0 / norm;
     if (norm != 0) {
-      D.s0[t] = a.val() / norm;
-      D.s1[t] = b.val() / norm;
-      D.s2[t] = c.val() / norm;
-      D.s3[t] = d.val() / norm;
-      D.iv1[t] = iv.val() / norm;
+      D.s0[t] = a.val() * rn;
+      D.s1[t] = b.val() * rn;
+      D.s2[t] = c.val() * rn;
+      D.s3[t] = d.val() * rn;
+      D.iv1[t] = iv.val() * rn;
     } else {
       D.vx[t] = 0.0;
       D.vy[t] = 0.0;
     }
-    if (D.cont_density) D.rho0[t] = rt.val() / norm;
+    if (D.cont_density) D.rho0[t] = rt.val() * rn;
   }
 }
 
@@ -233,12 +235,12 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
       } else if (ut == 25) {
         // the dummy carries the node's stress: A_u = sigma_t / rho_d^2
         bc_int = 1;
-        double rd = D.rho[u];
-        double rd2 = rd * rd;
+        double ri = D.rinv[u];
+        double ri2 = ri * ri;
         m = (float)D.mass[u];
-        d0 = (float)(D.s0[t] / rd2 - At[0]);
-        d1 = (float)(D.s1[t] / rd2 - At[1]);
-        d2 = (float)(D.s2[t] / rd2 - At[2]);
+        d0 = (float)fma(D.s0[t], ri2, -At[0]);
+        d1 = (float)fma(D.s1[t], ri2, -At[1]);
+        d2 = (float)fma(D.s2[t], ri2, -At[2]);
       } else {
         continue;
       }
@@ -305,6 +307,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
 //   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
 // is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
 // Every other stress-point takes the exact flow rule.
+template <bool SURR>
 __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   __shared__ float xs[4][32][16];
   __shared__ float ys[4][32][8];
@@ -319,7 +322,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   float x[16];
   double scale = 0.0;
   bool loading = false, cand = false;
-  if (act && D.surr && D.ntype_eco > 1 && D.ncrit == 12) {
+  if (SURR && act && D.ntype_eco > 1 && D.ncrit == 12) {
     const double* gu = D.grad_u + 4 * (size_t)t;
     for (int k = 0; k < 4; k++) g[k] = gu[k];
     s2v[0] = D.s0[t];
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     s2v[3] = D.s3[t];
     if (D.ntype_solid == 1) s2v[3] = D.poiss * (s2v[0] + s2v[1]);
     double f = D.fdp[t], G2[4], vivel[4];
-    drucker_prager(D, sc.time_sph, s2v, g, &f, G2, vivel);  // loading test only
+    drucker_prager<true>(D, sc.time_sph, s2v, g, &f, G2, vivel);  // loading test only
     loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
     if (loading) {
       scale = mlp_features(s2v, g, D.tanfi, D.coh, D.young, D.poiss, D.rho[t], x);
@@ -341,7 +344,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   const int nrows = __popc(mask);
   double Gnet[4];
   bool accept = false;
-  if (nrows) {  // warp-uniform
+  if (SURR && nrows) {  // warp-uniform
     const int row = __popc(mask & ((1u << lane) - 1u));
     const int ntile = (nrows + 15) >> 4;
     if (cand)
@@ -377,7 +380,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     }
   }
   // counters: loading, answered, outside the envelope, drift-rejected
-  if (D.surr) {
+  if (SURR) {
     unsigned ml = __ballot_sync(0xffffffffu, loading), ma = __ballot_sync(0xffffffffu, accept),
              mc = __ballot_sync(0xffffffffu, cand);
     if (lane == 0 && ml) {
@@ -394,9 +397,9 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     double v0 = -Gnet[0] / (2.0 * gm), v1 = -Gnet[1] / (2.0 * gm), v2 = -Gnet[2] / gm,
            v3 = -Gnet[3] / (2.0 * gm);
     double der = sqrt((2.0 * ((v0 * v0 + v1 * v1) + v3 * v3) + v2 * v2) / 3.0);
-    tail_sp_rates(D, sc, t, D.grad_u + 4 * (size_t)t, f2, Gnet, der);
+    tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, Gnet, der);
   } else {
-    tail_sp_rates(D, sc, t, D.grad_u + 4 * (size_t)t, f2);
+    tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2);
   }
 }
 
@@ -439,7 +442,9 @@ void launch_fderivs(Ctx& c, int stage) {
 }
 void launch_fsp_tail(Ctx& c, int stage) {
   int ns = c.d.NT - c.d.NN;
-  if (ns > 0) k_fsp_tail<<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  if (ns <= 0) return;
+  if (c.d.surr) k_fsp_tail<true><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  else k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
   k_fxsph<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);

@@ -29,6 +29,14 @@ namespace {
 
 constexpr int kBlock = 256;
 
+// adapt_stress2: the reference's FP64 arithmetic in the plain form, the division-free
+// variant in the FP32 form
+__device__ __forceinline__ void stress_return(const Dev& D, double& a, double& b, double& c,
+                                              double& d) {
+  if (D.fast) adapt_stress_fast(D.alpha2, D.kc, D.kc_shift, a, b, c, d);
+  else adapt_stress(D.alpha2, D.kc, a, b, c, d);
+}
+
 // FP32-form neighbour records of particle i (velocity, volume, stress, internal variable)
 __device__ __forceinline__ float4 split2(double x, double y) {
   float xh = (float)x, yh = (float)y;
@@ -195,7 +203,7 @@ __global__ void k_stage_begin(Dev D, int stage) {
       }
     }
   }
-  if (D.ncrit == 12) adapt_stress(D.alpha2, D.kc, a, b, c, d);
+  if (D.ncrit == 12) stress_return(D, a, b, c, d);
   apply_bcs(D, sc, i, vx, vy, a, b, c);
   D.vx[i] = vx;
   D.vy[i] = vy;
@@ -296,7 +304,7 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (D.sp_sph) {
-    if (D.ncrit == 12) adapt_stress(D.alpha2, D.kc, a, b, c, d);
+    if (D.ncrit == 12) stress_return(D, a, b, c, d);
     apply_bcs(D, sc, i, vx, vy, a, b, c);
     D.vx[i] = vx;
     D.vy[i] = vy;
@@ -306,16 +314,24 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
     D.s3[i] = d;
   }
   if (with_A) {
-    double r = D.rho[i];
-    double r2 = r * r;
-    D.A[0][i] = a / r2;
-    D.A[1][i] = b / r2;
-    D.A[2][i] = c / r2;
     if (D.fast) {
-      float h0 = (float)D.A[0][i], h1 = (float)D.A[1][i], h2 = (float)D.A[2][i];
+      // sigma / rho^2 as sigma (1/rho)^2: no FP64 division (the records carry ~48 bits)
+      double ri = D.rinv[i];
+      double ri2 = ri * ri;
+      double A0 = a * ri2, A1 = b * ri2, A2 = c * ri2;
+      D.A[0][i] = A0;
+      D.A[1][i] = A1;
+      D.A[2][i] = A2;
+      float h0 = (float)A0, h1 = (float)A1, h2 = (float)A2;
       D.recA[i] = make_float4(h0, h1, h2, (float)D.mass[i]);
-      D.recAl[i] = make_float4((float)(D.A[0][i] - (double)h0), (float)(D.A[1][i] - (double)h1),
-                               (float)(D.A[2][i] - (double)h2), 0.0f);
+      D.recAl[i] = make_float4((float)(A0 - (double)h0), (float)(A1 - (double)h1),
+                               (float)(A2 - (double)h2), 0.0f);
+    } else {
+      double r = D.rho[i];
+      double r2 = r * r;
+      D.A[0][i] = a / r2;
+      D.A[1][i] = b / r2;
+      D.A[2][i] = c / r2;
     }
   }
   if (D.fast) {
@@ -487,7 +503,7 @@ __global__ void k_rk_final(Dev D) {
     c = D.st0[2][i] + dt6 * D.RKs[2][i];
     d = D.st0[3][i] + dt6 * D.RKs[3][i];
   }
-  if (D.ncrit == 12) adapt_stress(D.alpha2, D.kc, a, b, c, d);
+  if (D.ncrit == 12) stress_return(D, a, b, c, d);
   apply_bcs(D, sc, i, vx, vy, a, b, c);
   D.vx[i] = vx;
   D.vy[i] = vy;

@@ -264,6 +264,7 @@ int sps_create(const sps_params* p, sps_ctx** out) {
       double den = std::sqrt(9.0 + 12.0 * (D.tanfi * D.tanfi));
       D.alpha2 = D.tanfi / den;
       D.kc = (3.0 * D.coh) / den;
+      D.kc_shift = D.alpha2 > 0.0 ? D.kc / (3.0 * D.alpha2) : 0.0;
     }
     for (int d = 0; d < 2; d++) {
       D.xmin_dom[d] = p->xmin_domain[d];

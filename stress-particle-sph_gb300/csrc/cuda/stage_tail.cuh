@@ -75,6 +75,9 @@ __device__ __forceinline__ void tail_sp_grad(const Dev& D, int t, double* g, con
 // stress-point rates after the gradient: D : grad(v), plastic_terms / drucker_prager,
 // Jaumann spin, RHS and RK4 accumulation.  Gs_net (may be null): a plastic source from the
 // learned surrogate that replaces the exact one (with its plastic strain rate der_net)
+// FAST (the FP32 form): the mean of drucker_prager by a product, the plastic strain-rate
+// norm in FP32.
+template <bool FAST = false>
 __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& sc, int t,
                                               const double* g, double f2,
                                               const double* Gs_net = nullptr,
@@ -94,15 +97,23 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
       double vivel[4] = {0.0, 0.0, 0.0, 0.0}, G2[4];
       if (D.ncrit == 12) {
         double f = D.fdp[t];
-        drucker_prager(D, sc.time_sph, s2v, g, &f, G2, vivel);
+        drucker_prager<FAST>(D, sc.time_sph, s2v, g, &f, G2, vivel);
         D.fdp[t] = f;
         for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
         if (D.cap_buf && (G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0))
           capture_tuple(D, t, s2v, g, Gs);
       }
-      der = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
-                  vivel[2] * vivel[2]) /
-                 3.0);
+      if (FAST) {
+        float v0 = (float)vivel[0], v1 = (float)vivel[1], v2 = (float)vivel[2],
+              v3 = (float)vivel[3];
+        // explicit fmaf: the same rounding in every kernel that inlines this tail
+        float q = fmaf(2.0f, fmaf(v0, v0, fmaf(v1, v1, __fmul_rn(v3, v3))), __fmul_rn(v2, v2));
+        der = (double)sqrtf(__fmul_rn(q, 1.0f / 3.0f));
+      } else {
+        der = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
+                    vivel[2] * vivel[2]) /
+                   3.0);
+      }
     }
     if (Gs_net) {
       for (int k = 0; k < 4; k++) Gs[k] = Gs_net[k];
