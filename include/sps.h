@@ -120,8 +120,9 @@ int sps_upload_bcs(sps_ctx* ctx, const int32_t* bc_or_not, const int32_t* bc_inf
 
 /* Advance nsteps steps.  Each step is `call time_integration` followed by
    `time_sph = time_sph + dt_sph` (code/1_SPH_2018.f90:82-83); *time_sph is read on entry
-   and holds the advanced time on return.  Itimestep bookkeeping of the pair list
-   (grid_find_NEW's linked-list reuse) is carried by the context across calls. */
+   and holds the advanced time on return (for a batch: time_sph[r] per realisation, each
+   advanced by its own dt_sph).  Itimestep bookkeeping of the pair list (grid_find_NEW's
+   linked-list reuse) is carried by the context across calls. */
 int sps_step(sps_ctx* ctx, int32_t nsteps, double* time_sph);
 
 /* Copy fields back; any pointer may be NULL to skip that field.
@@ -163,6 +164,28 @@ int sps_kernels_per_step(sps_ctx* ctx, int32_t* n);
 int sps_profile_step(sps_ctx* ctx, int32_t nsteps, double* time_sph, char* names,
                      int32_t names_len, double* ms, int32_t* launches, int32_t cap,
                      int32_t* nkernels);
+
+/* ---- batches (no reference counterpart: the reference runs one problem per process) ----
+   A batch packs nreal independent problems (realisations) into one context: one launch per
+   kernel and stage advances all of them, each with its own particle counts, material,
+   dt_sph, gravity curve and domain.  Every realisation keeps its own cell grid and its own
+   pair-list bookkeeping, so its results are bit-identical to a context holding it alone.
+   The realisations must share the solver flags (sp_sph, inside_approach, cspm, xsph,
+   update_x, cont_density, sle, skf, ntype_solid, precision, pi); boundary conditions
+   (no_bcs > 0) need a batch of one.  sps_create(p) is sps_create_batch(1, p). */
+int sps_create_batch(int32_t nreal, const sps_params* params, sps_ctx** out);
+/* sps_upload / sps_download / sps_dump_pairs for realisation r, with r's arrays in the
+   reference's layout and 1-based ids local to r. */
+int sps_upload_real(sps_ctx* ctx, int32_t r, const double* x, const double* vel,
+                    const double* stress, const double* mass, const double* rho,
+                    const double* hsml, const int32_t* itype, const double* intvars1,
+                    const double* f_drucker, const double* x00);
+int sps_download_real(sps_ctx* ctx, int32_t r, double* x, double* vel, double* stress,
+                      double* rho, double* intvars1, double* displ, int32_t* bc_or_not,
+                      double* f_drucker);
+int sps_dump_pairs_real(sps_ctx* ctx, int32_t r, int32_t* pair_i, int32_t* pair_j,
+                        int32_t* pint_type, float* w, float* dwdx, float* dwdy,
+                        int64_t* npairs);
 
 /* Copy the last error message of this context (or of the last failed sps_create when
    ctx is NULL) into buf (NUL-terminated, truncated to len). Returns its length. */

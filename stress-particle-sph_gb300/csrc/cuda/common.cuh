@@ -1,11 +1,17 @@
 // common.cuh -- device-side layout and shared device functions of the SPS step.
 //
-// Data layout in HBM (one context):
-//   particle state, reference id order (0-based), structure of arrays:
+// Data layout in HBM (one context = a batch of R realisations; a single problem is R = 1):
+//   particle ids: the nodes of every realisation, then their stress-points, then their
+//     dummies; realisation r owns the contiguous ranges [node0, +nnode), [sp0, +nsp),
+//     [dum0, +ndum) of its Real entry, and rid[id] = r.  For R = 1 this is the reference's
+//     own order (nodes, stress-points, dummies).
+//   particle state, structure of arrays:
 //     px,py  vx,vy  s0..s3 (sxx,syy,sxy,szz)  mass rho hsml itype  iv1 fdp  x00x,x00y ...
 //   per-step cell sort: cell_of[id], cell_start[c], sorted[s] (id at sorted position s),
-//     spos[id]; sorted order = cells ascending, particle id ascending within a cell,
-//     out-of-domain particles last.
+//     spos[id]; every realisation has its own grid (the reference's grid of that problem
+//     alone) whose cells are numbered from its cell0, so the sorted order is realisation by
+//     realisation, cells ascending, particle id ascending within a cell, out-of-domain
+//     particles of all realisations last.
 //   pair tables per step:
 //     half[s*capH + k]  pairs created by the particle at sorted position s (the reference's
 //                       grid_find_NEW creation order), 16 B {b sorted pos, w, dwdx, dwdy}
@@ -34,14 +40,15 @@ struct dfl {
   float hi, lo;
 };
 
+// the grid of one realisation for one step (grid_find_NEW)
 struct Grid {
   double xmin[2];
   double deltx[2];
   int ndiv[2];
-  int ncells;
-  int nactive;   // particles in cells (sorted positions below nactive)
-  int overflow;  // cells exceeded capacity
-  float xr0[2];  // origin of the FP32 prefilter coordinates (= xmin)
+  int ncells;    // cells of this realisation
+  int cell0;     // global number of its first cell
+  int overflow;  // no active particle (no cell size) or the cells exceed the capacity
+  float tau;     // width of the FP32 prefilter's guard band (relative to the support^2)
   // every active particle has the same smoothing length h this step: the kernel's
   // h-only subexpressions are formed once (same operations, same values)
   int uniform_h;
@@ -50,11 +57,33 @@ struct Grid {
   dfl df_h, df_yh, df_yhh, df_factor, df_factor6, df_c3, df_cell[2];
 };
 
-// pair bookkeeping of grid_find_NEW's linked list
+// totals over the realisations of a step
+struct GridTotal {
+  int ncells;    // cells of all realisations; the out-of-domain bucket is cell ncells
+  int nactive;   // particles in cells (sorted positions below nactive)
+  int overflow;  // cells exceeded the capacity
+};
+
+// pair bookkeeping of grid_find_NEW's linked list, per realisation
 struct PairMeta {
   int64_t n;       // pairs found this step
   int64_t m_prev;  // list nodes before this step (m_pairs)
   int64_t m;       // list nodes after this step
+  int64_t base;    // global creation index of the realisation's first pair this step
+};
+
+// constants of one realisation (a batch packs problems that share the solver flags but
+// not their sizes, material, time step, gravity or domain)
+struct Real {
+  int node0, nnode, sp0, nsp, dum0, ndum, ndum2;  // id ranges (ndum2: innermost layer)
+  int ntype_eco, ncrit, ntype_solid, ic_grav;
+  double dt, dx, alpha, beta, damping;
+  double D11, D12, D22, D33, D41, D42;
+  double tanfi, coh, young, poiss;
+  double alpha2, kc;  // adapt_stress2 constants (FP64)
+  double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
+  double xmin_dom[2], xmax_dom[2];
+  double cgrav[2];
 };
 
 enum ErrBits : int {
@@ -66,22 +95,19 @@ enum ErrBits : int {
 };
 
 struct Dev {
-  // sizes
-  int NN, NT, N2, ndummy2;
+  // sizes (all realisations)
+  int NN, NT, N2;  // nodes, nodes + stress-points, all particles
+  int R;           // realisations
   int capH, capC, capS;
   int cell_cap;
-  // flags and constants
+  // solver flags shared by the realisations
   int skf, scale_k, cspm, xsph, update_x, cont_density, sle, sp_sph, inside, no_bcs;
-  int ntype_eco, ncrit, ntype_solid, ic_grav;
   int bound_from_lists;
-  double pi, dt, alpha, beta, damping, dx;
-  double D11, D12, D22, D33, D41, D42;
-  double tanfi, coh, young, poiss;
-  double alpha2, kc;  // adapt_stress2 constants (FP64)
-  double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
-  double xmin_dom[2], xmax_dom[2];
-  double cgrav[2];
+  double pi;
   int bcvar[kMaxBC];
+  // per-realisation constants and the realisation of every particle
+  const Real* real;
+  const uint16_t* rid;
   // particle state (id order)
   double *px, *py, *vx, *vy, *s0, *s1, *s2, *s3;
   double *mass, *rho, *hsml, *iv1, *fdp, *x00x, *x00y, *dispx, *dispy;
@@ -124,17 +150,17 @@ struct Dev {
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
   float *xr, *yr, *hr;
   float *xrl, *yrl;  // FP32 form: low parts of the cell-relative offsets
-  Grid* grid;
-  double* bbox_part;  // per-block partial (minx, miny, -maxx, -maxy, -maxh)
-  int nbbox_blocks;
+  Grid* grid;                // per realisation
+  GridTotal* gtot;
+  unsigned long long* bbox;  // per realisation: ordered keys of minx, miny, -maxx, -maxy, -maxh, minh
   // pairs
   int4* half;
   int32_t* half_cnt;
   int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
   int4 *cross, *same;
   int32_t *degC, *degS;
-  PairMeta* meta;
-  // scalars of the current step
+  PairMeta* meta;  // per realisation
+  // scalars of the current step, per realisation (table: [step][realisation])
   const StepScalars* scal_table;
   int* step_idx;
   StepScalars* cur;
@@ -316,12 +342,12 @@ __device__ __forceinline__ void adapt_stress_fast(double alpha2, double kc, doub
 // szz already substituted), gu: grad_u(2,2).  Updates *fdp, returns G and vivel.
 // FAST (the FP32 form): the FP64 mean by a product with 1/3 instead of a division.
 template <bool FAST = false>
-__device__ __forceinline__ void drucker_prager(const Dev& D, double time_sph, const double* s,
+__device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, const double* s,
                                                const double* gu, double* fdp, double* G,
                                                double* vivel) {
   double f0 = *fdp;
-  float tanfi = (float)D.tanfi, coh = (float)D.coh, young = (float)D.young,
-        poiss = (float)D.poiss;
+  float tanfi = (float)M.tanfi, coh = (float)M.coh, young = (float)M.young,
+        poiss = (float)M.poiss;
   float smean = FAST ? (float)(((s[0] + s[1]) + s[3]) * (1.0 / 3.0))
                      : (float)(((s[0] + s[1]) + s[3]) / 3.0);
   float dv0 = (float)(s[0] - (double)smean);
@@ -366,6 +392,11 @@ __device__ __forceinline__ void drucker_prager(const Dev& D, double time_sph, co
     vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0;
   }
 }
+
+__device__ __forceinline__ const Real& real_of(const Dev& D, int i) { return D.real[D.rid[i]]; }
+// the node at the same place as a stress-point (and back), when every node has one
+__device__ __forceinline__ int node_of_sp(const Real& M, int t) { return M.node0 + (t - M.sp0); }
+__device__ __forceinline__ int sp_of_node(const Real& M, int n) { return M.sp0 + (n - M.node0); }
 
 __device__ __forceinline__ bool is_sp(int t) { return t == 1; }
 __device__ __forceinline__ bool is_node(int t) { return t == 2; }

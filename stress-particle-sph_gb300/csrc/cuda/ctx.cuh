@@ -10,19 +10,29 @@
 
 namespace sps {
 
-struct Ctx {
+// host copy of one realisation's problem description (the pointer fields of its params
+// point into the vectors here)
+struct HostReal {
   sps_params p{};
-  Dev d{};       // device pointers + constants, passed by value to kernels
+  std::vector<int32_t> nptstcurves;
+  std::vector<double> ttcurves, bc_list;
+  std::vector<float> ftcurves;
+  // extent and smoothing lengths of the uploaded state (capacity sizing)
+  double ncells_est = 0.0, hmax = 0.0, hmin_nd = 1e300;
+  bool uploaded = false;
+};
+
+struct Ctx {
+  sps_params p{};  // realisation 0 (the flags every realisation shares)
+  std::vector<HostReal> hr;
+  std::vector<Real> real;  // host copy of the per-realisation table
+  Dev d{};                 // device pointers + constants, passed by value to kernels
   Dev* d_dev = nullptr;
   cudaStream_t stream = nullptr;
   int device = 0;
   std::vector<void*> allocs;
-  // host copies of tables
-  std::vector<int32_t> nptstcurves;
-  std::vector<double> ttcurves, bc_list;
-  std::vector<float> ftcurves;
   StepScalars* d_scal_table = nullptr;
-  int scal_cap = 0;
+  int scal_cap = 0;  // steps
   std::vector<StepScalars> h_scal;
   int* h_err = nullptr;  // pinned
   double* stage = nullptr;  // device staging for interleaved host arrays (4 x ntotal2)

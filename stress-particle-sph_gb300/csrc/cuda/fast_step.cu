@@ -67,11 +67,12 @@ __global__ void k_finterp(Dev D) {
   if (t >= D.NT) return;
   int tt = D.itype[t];
   if (!D.sp_sph) {
+    const Real& M = real_of(D, t);
     if (t >= D.NN) {
-      D.vx[t] = D.vx[t - D.NN];
-      D.vy[t] = D.vy[t - D.NN];
+      D.vx[t] = D.vx[node_of_sp(M, t)];
+      D.vy[t] = D.vy[node_of_sp(M, t)];
     } else {
-      int sp = t + D.NN;
+      int sp = sp_of_node(M, t);
       D.s0[t] = D.s0[sp];
       D.s1[t] = D.s1[sp];
       D.s2[t] = D.s2[sp];
@@ -152,7 +153,8 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
   if (t >= D.NT) return;
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
-  const StepScalars& sc = *D.cur;
+  const Real& Mt = real_of(D, t);
+  const StepScalars& sc = D.cur[D.rid[t]];
   int tt = D.itype[t];
   int deg = D.degC[s];
   const double xt = D.px[t], yt = D.py[t];
@@ -255,7 +257,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
       sy.add(m, dwy);
     }
     double avx = 0.0, avy = 0.0;
-    if (D.alpha > 0 || D.beta > 0) {
+    if (Mt.alpha > 0 || Mt.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904) in FP32
       Kahan ax, ay;
       int degs = D.degS[s];
@@ -277,7 +279,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
         float theta = (h * div_u) / (sq2 + 0.01f * (h * h));
         float visc = 0.0f;
         if (div_u < 0)
-          visc = (-((float)D.alpha * 600.0f) * theta + (float)D.beta * (theta * theta)) / rho2;
+          visc = (-((float)Mt.alpha * 600.0f) * theta + (float)Mt.beta * (theta * theta)) / rho2;
         ax.add(visc * __int_as_float(e.z) * ri.w);
         ay.add(visc * __int_as_float(e.w) * ri.w);
       }
@@ -317,24 +319,25 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   const int t = D.NN + (act ? i : 0);
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
-  const StepScalars& sc = *D.cur;
+  const Real& M = real_of(D, t);
+  const StepScalars& sc = D.cur[D.rid[t]];
   double g[4] = {0.0, 0.0, 0.0, 0.0}, s2v[4] = {0.0, 0.0, 0.0, 0.0};
   float x[16];
   double scale = 0.0;
   bool loading = false, cand = false;
-  if (SURR && act && D.ntype_eco > 1 && D.ncrit == 12) {
+  if (SURR && act && M.ntype_eco > 1 && M.ncrit == 12) {
     const double* gu = D.grad_u + 4 * (size_t)t;
     for (int k = 0; k < 4; k++) g[k] = gu[k];
     s2v[0] = D.s0[t];
     s2v[1] = D.s1[t];
     s2v[2] = D.s2[t];
     s2v[3] = D.s3[t];
-    if (D.ntype_solid == 1) s2v[3] = D.poiss * (s2v[0] + s2v[1]);
+    if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
     double f = D.fdp[t], G2[4], vivel[4];
-    drucker_prager<true>(D, sc.time_sph, s2v, g, &f, G2, vivel);  // loading test only
+    drucker_prager<true>(M, sc.time_sph, s2v, g, &f, G2, vivel);  // loading test only
     loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
     if (loading) {
-      scale = mlp_features(s2v, g, D.tanfi, D.coh, D.young, D.poiss, D.rho[t], x);
+      scale = mlp_features(s2v, g, M.tanfi, M.coh, M.young, M.poiss, D.rho[t], x);
       cand = scale > 0.0;
       for (int k = 0; k < MLP_NIN && cand; k++)
         cand = x[k] >= D.env_lo[k] && x[k] <= D.env_hi[k];
@@ -367,13 +370,13 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
         double sm = ((s2v[0] + s2v[1]) + s2v[3]) / 3.0;
         double d0 = s2v[0] - sm, d1 = s2v[1] - sm, d2 = s2v[2], d3 = s2v[3] - sm;
         double sj = sqrt(d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3));
-        double e0 = D.D11 * g[0] + D.D12 * g[3] + Gnet[0];
-        double e1 = D.D12 * g[0] + D.D22 * g[3] + Gnet[1];
-        double e2 = D.D33 * g[1] + D.D33 * g[2] + Gnet[2];
-        double e3 = D.D41 * g[0] + D.D42 * g[3] + Gnet[3];
+        double e0 = M.D11 * g[0] + M.D12 * g[3] + Gnet[0];
+        double e1 = M.D12 * g[0] + M.D22 * g[3] + Gnet[1];
+        double e2 = M.D33 * g[1] + M.D33 * g[2] + Gnet[2];
+        double e3 = M.D41 * g[0] + M.D42 * g[3] + Gnet[3];
         double df = (d0 * e0 + d1 * e1 + d3 * e3 + 2.0 * d2 * e2) / (2.0 * sj) +
-                    D.alpha2 * (e0 + e1 + e3);
-        accept = sj > 0.0 && D.dt * fabs(df) <= D.surr_tol * sj;
+                    M.alpha2 * (e0 + e1 + e3);
+        accept = sj > 0.0 && M.dt * fabs(df) <= D.surr_tol * sj;
       } else {
         cand = false;  // counted as outside the envelope
       }
@@ -393,7 +396,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   if (!act) return;
   if (accept) {
     // plastic strain rate of the predicted source: e_p = G / (2 G_mod), shear G / G_mod
-    const double gm = D.young / (2.0 * (1.0 + D.poiss));
+    const double gm = M.young / (2.0 * (1.0 + M.poiss));
     double v0 = -Gnet[0] / (2.0 * gm), v1 = -Gnet[1] / (2.0 * gm), v2 = -Gnet[2] / gm,
            v3 = -Gnet[3] / (2.0 * gm);
     double der = sqrt((2.0 * ((v0 * v0 + v1 * v1) + v3 * v3) + v2 * v2) / 3.0);
@@ -427,8 +430,9 @@ __global__ void k_fxsph(Dev D) {
     if (t < D.NN && D.bc_or_not[u] == 2 && flag != 2) mark = true;
   }
   const double eps = 0.5;
-  D.px[t] = D.x0x[t] + D.dt * (vt0 + eps * s0.val());
-  D.py[t] = D.x0y[t] + D.dt * (vt1 + eps * s1.val());
+  const double dt = real_of(D, t).dt;
+  D.px[t] = D.x0x[t] + dt * (vt0 + eps * s0.val());
+  D.py[t] = D.x0y[t] + dt * (vt1 + eps * s1.val());
   if (mark) D.bc_or_not[t] = 3;
 }
 

@@ -24,11 +24,6 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__device__ __forceinline__ double warp_min(double v) {
-  for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
 // ---- double-float (unevaluated sum of two FP32 numbers) arithmetic: Dekker, "A floating-
 // point technique for extending the available precision", Numer. Math. 18, 1971, with the
 // FMA-based exact product.  Used by the FP32 form to produce the FP32 kernel values the
@@ -82,115 +77,180 @@ __device__ __forceinline__ dfl df_from(double v) {
   return {h, (float)(v - (double)h)};
 }
 
-// Check_Out_Domain + per-block partial bounding box (minx, miny, -maxx, -maxy, -maxh, minh)
+// ordered key of a double: unsigned order of the keys = numeric order of the values, so
+// that atomicMin on keys is an exact min over doubles
+__device__ __forceinline__ unsigned long long okey(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double unkey(unsigned long long k) {
+  unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+constexpr unsigned long long kNoKey = ~0ull;  // no active particle
+
+// Check_Out_Domain (2_SPH_main_2018.f90:1170) + the bounding box of the active particles of
+// every realisation: keys of (minx, miny, -maxx, -maxy, -maxh, minh), reduced over the warp
+// (or the block) when it holds one realisation, then atomicMin per realisation
 __global__ void k_bbox(Dev D) {
-  __shared__ double sh[6][kBlock / 32];
+  __shared__ unsigned long long sh[kBlock / 32][6];
+  __shared__ int shr[kBlock / 32];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
+  unsigned long long v[6] = {kNoKey, kNoKey, kNoKey, kNoKey, kNoKey, kNoKey};
+  int r = -1;
   if (i < D.N2) {
+    r = D.rid[i];
+    const Real& M = D.real[r];
     double x = D.px[i], y = D.py[i];
-    double dxx = (x - D.xmin_dom[0]) * (x - D.xmax_dom[0]);
-    double dyy = (y - D.xmin_dom[1]) * (y - D.xmax_dom[1]);
+    double dxx = (x - M.xmin_dom[0]) * (x - M.xmax_dom[0]);
+    double dyy = (y - M.xmin_dom[1]) * (y - M.xmax_dom[1]);
     uint8_t o = D.out[i];
     if (dxx > 0.0 || dyy > 0.0) o = 1;
     D.out[i] = o;
     if (!o) {
       double h = D.hsml[i];
-      v[0] = x;
-      v[1] = y;
-      v[2] = -x;
-      v[3] = -y;
-      v[4] = -h;
-      v[5] = h;
+      v[0] = okey(x);
+      v[1] = okey(y);
+      v[2] = okey(-x);
+      v[3] = okey(-y);
+      v[4] = okey(-h);
+      v[5] = okey(h);
     }
   }
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int k = 0; k < 6; k++) {
-    double r = warp_min(v[k]);
-    if (lane == 0) sh[k][wid] = r;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // the realisation of the warp (-1: several, or none active)
+  int r0 = __shfl_sync(0xffffffffu, r, 0);
+  for (int o = 16; o; o >>= 1) r0 = max(r0, __shfl_xor_sync(0xffffffffu, r0, o));
+  const bool uni = __all_sync(0xffffffffu, r < 0 || r == r0);
+  if (!uni) {
+    if (r >= 0 && v[0] != kNoKey)
+      for (int k = 0; k < 6; k++) atomicMin(&D.bbox[6 * (size_t)r + k], v[k]);
+    r0 = -1;
+  } else {
+    for (int k = 0; k < 6; k++)
+      for (int o = 16; o; o >>= 1) {
+        unsigned long long u = __shfl_xor_sync(0xffffffffu, v[k], o);
+        v[k] = u < v[k] ? u : v[k];
+      }
+  }
+  if (lane == 0) {
+    shr[wid] = r0;
+    for (int k = 0; k < 6; k++) sh[wid][k] = v[k];
   }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    for (int k = 0; k < 6; k++) {
-      double r = threadIdx.x < kBlock / 32 ? sh[k][threadIdx.x] : 1e300;
-      r = warp_min(r);
-      if (threadIdx.x == 0) D.bbox_part[6 * (size_t)blockIdx.x + k] = r;
+  if (threadIdx.x == 0) {
+    int rb = shr[0];
+    bool block_uni = rb >= 0;
+    for (int w = 1; w < kBlock / 32 && block_uni; w++) block_uni = shr[w] == rb;
+    if (block_uni) {
+      unsigned long long m[6];
+      for (int k = 0; k < 6; k++) {
+        m[k] = sh[0][k];
+        for (int w = 1; w < kBlock / 32; w++) m[k] = sh[w][k] < m[k] ? sh[w][k] : m[k];
+      }
+      if (m[0] != kNoKey)
+        for (int k = 0; k < 6; k++) atomicMin(&D.bbox[6 * (size_t)rb + k], m[k]);
+    } else {
+      for (int w = 0; w < kBlock / 32; w++)
+        if (shr[w] >= 0 && sh[w][0] != kNoKey)
+          for (int k = 0; k < 6; k++) atomicMin(&D.bbox[6 * (size_t)shr[w] + k], sh[w][k]);
     }
   }
 }
 
-// grid parameters (2_SPH_main_2018.f90:1230-1260)
+// grid parameters of every realisation (2_SPH_main_2018.f90:1230-1260) and the numbering
+// of their cells (one block; the bounding-box keys are reset for the next step)
 __global__ void k_grid(Dev D) {
-  __shared__ double sh[6][kBlock / 32];
-  double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
-  for (int b = threadIdx.x; b < D.nbbox_blocks; b += blockDim.x)
-    for (int k = 0; k < 6; k++) v[k] = fmin(v[k], D.bbox_part[6 * (size_t)b + k]);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int k = 0; k < 6; k++) {
-    double r = warp_min(v[k]);
-    if (lane == 0) sh[k][wid] = r;
+  __shared__ int sc[kBlock];
+  __shared__ int carry, bad;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    carry = 0;
+    bad = 0;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  double red[6];
-  for (int k = 0; k < 6; k++) {
-    double r = 1e300;
-    for (int w = 0; w < kBlock / 32; w++) r = fmin(r, sh[k][w]);
-    red[k] = r;
+  for (int base = 0; base < D.R; base += kBlock) {
+    const int r = base + tid;
+    int nc = 0;
+    Grid g;
+    if (r < D.R) {
+      double red[6];
+      for (int k = 0; k < 6; k++) {
+        unsigned long long key = D.bbox[6 * (size_t)r + k];
+        D.bbox[6 * (size_t)r + k] = kNoKey;
+        red[k] = key == kNoKey ? 1e300 : unkey(key);
+      }
+      double hmax = -red[4];
+      if (red[0] > 1e299) hmax = 0.0;  // no active particle
+      double cellsz = hmax * 2.0;
+      double ncd = 1.0;
+      for (int d = 0; d < 2; d++) {
+        double xmin = red[d] > 1e299 ? (double)1.e10f : red[d];
+        double xmax = red[d] > 1e299 ? -(double)1.e10f : -red[2 + d];
+        double length = xmax - xmin;
+        double qd = length / cellsz + 1.0;
+        int ndiv = (qd >= 1.0 && qd < 1.0e9) ? (int)qd : 1;
+        double length_new = (double)ndiv * cellsz;
+        g.xmin[d] = (xmin - (length_new - length) / 2.0) - (double)0.001f * length;
+        g.deltx[d] = cellsz;
+        g.ndiv[d] = ndiv;
+        ncd *= ndiv;
+      }
+      g.overflow = (ncd > (double)D.cell_cap || !(cellsz > 0.0)) ? 1 : 0;
+      nc = g.overflow ? 0 : (int)ncd;
+      if (g.overflow) bad = 1;
+      // uniform smoothing length: (h + h) / 2 == h, so every pair's kernel shares these
+      g.uniform_h = (D.skf == 1 && red[5] == hmax && hmax > 0.0) ? 1 : 0;
+      double h = hmax;
+      g.h = h;
+      g.yh = 1.0 / h;
+      g.hh = h * h;
+      g.yhh = 1.0 / g.hh;
+      g.factor = 15.0 / (7.0 * D.pi * h * h);
+      g.factor6 = g.factor / 6.0;
+      g.c3 = g.factor6 * 3.0;
+      g.df_h = df_from(g.h);
+      g.df_yh = df_from(g.yh);
+      g.df_yhh = df_from(g.yhh);
+      g.df_factor = df_from(g.factor);
+      g.df_factor6 = df_from(g.factor6);
+      g.df_c3 = df_from(g.c3);
+      g.df_cell[0] = df_from(g.deltx[0]);
+      g.df_cell[1] = df_from(g.deltx[1]);
+      // FP32 prefilter band: cell-relative offsets and the cell-corner shift each carry
+      // |err| <= 2^-24 * 2 cells; the band covers eight times that relative to the support
+      double ext = 2.0 * fmax(g.deltx[0], g.deltx[1]);
+      double smin = (double)D.scale_k * red[5];
+      g.tau = (float)((smin > 0) ? 8.0 * ext * 1.1920929e-07 / smin + 4e-6 : 1.0);
+    }
+    sc[tid] = nc;
+    __syncthreads();
+    for (int off = 1; off < kBlock; off <<= 1) {
+      int add = tid >= off ? sc[tid - off] : 0;
+      __syncthreads();
+      sc[tid] += add;
+      __syncthreads();
+    }
+    if (r < D.R) {
+      g.ncells = nc;
+      g.cell0 = carry + sc[tid] - nc;
+      D.grid[r] = g;
+    }
+    __syncthreads();
+    if (tid == kBlock - 1) carry += sc[tid];
+    __syncthreads();
   }
-  Grid g;
-  double hmax = -red[4];
-  if (red[0] > 1e299) {  // no active particle
-    hmax = 0.0;
+  if (tid == 0) {
+    GridTotal gt;
+    gt.overflow = (bad || carry > D.cell_cap) ? 1 : 0;
+    gt.ncells = gt.overflow ? 0 : carry;
+    gt.nactive = 0;
+    *D.gtot = gt;
+    if (gt.overflow) atomicOr(D.err, ERR_CELLS);
   }
-  double cellsz = hmax * 2.0;
-  double nc = 1.0;
-  for (int d = 0; d < 2; d++) {
-    double xmin = red[d] > 1e299 ? (double)1.e10f : red[d];
-    double xmax = red[d] > 1e299 ? -(double)1.e10f : -red[2 + d];
-    double length = xmax - xmin;
-    double qd = length / cellsz + 1.0;
-    int ndiv = (qd >= 1.0 && qd < 1.0e9) ? (int)qd : 1;
-    double length_new = (double)ndiv * cellsz;
-    g.xmin[d] = (xmin - (length_new - length) / 2.0) - (double)0.001f * length;
-    g.deltx[d] = cellsz;
-    g.ndiv[d] = ndiv;
-    g.xr0[d] = 0.0f;
-    nc *= ndiv;
-  }
-  g.overflow = (nc > (double)D.cell_cap || !(cellsz > 0.0)) ? 1 : 0;
-  g.ncells = g.overflow ? 0 : (int)nc;
-  g.nactive = 0;
-  // uniform smoothing length: (h + h) / 2 == h, so every pair's kernel shares these values
-  g.uniform_h = (D.skf == 1 && red[5] == hmax && hmax > 0.0) ? 1 : 0;
-  {
-    double h = hmax;
-    g.h = h;
-    g.yh = 1.0 / h;
-    g.hh = h * h;
-    g.yhh = 1.0 / g.hh;
-    g.factor = 15.0 / (7.0 * D.pi * h * h);
-    g.factor6 = g.factor / 6.0;
-    g.c3 = g.factor6 * 3.0;
-    g.df_h = df_from(g.h);
-    g.df_yh = df_from(g.yh);
-    g.df_yhh = df_from(g.yhh);
-    g.df_factor = df_from(g.factor);
-    g.df_factor6 = df_from(g.factor6);
-    g.df_c3 = df_from(g.c3);
-    g.df_cell[0] = df_from(g.deltx[0]);
-    g.df_cell[1] = df_from(g.deltx[1]);
-  }
-  if (g.overflow) atomicOr(D.err, ERR_CELLS);
-  *D.grid = g;
-  // FP32 prefilter band: cell-relative offsets and the cell-corner shift each carry
-  // |err| <= 2^-24 * 2 cells; the band covers eight times that relative to the support
-  double ext = 2.0 * fmax(g.deltx[0], g.deltx[1]);
-  double smin = (double)D.scale_k * red[5];
-  double tau = (smin > 0) ? 8.0 * ext * 1.1920929e-07 / smin + 4e-6 : 1.0;
-  D.bbox_part[0] = tau;  // reused as the band width of this step
 }
 
+// local cell of a position in a realisation's grid
 __device__ __forceinline__ int cell_index(const Grid& g, double x, double y) {
   double qx = (x - g.xmin[0]) / g.deltx[0] + 1.0;
   double qy = (y - g.xmin[1]) / g.deltx[1] + 1.0;
@@ -204,15 +264,16 @@ __device__ __forceinline__ int cell_index(const Grid& g, double x, double y) {
 __global__ void k_cell_count(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N2) return;
-  const Grid g = *D.grid;
+  const GridTotal gt = *D.gtot;
   int c;
-  if (D.out[i] || g.overflow) {
-    c = g.ncells;  // out-of-domain bucket, after every real cell
+  const Grid& g = D.grid[D.rid[i]];
+  if (D.out[i] || gt.overflow) {
+    c = gt.ncells;  // out-of-domain bucket, after every real cell
   } else {
     double x = D.px[i], y = D.py[i];
-    c = cell_index(g, x, y);
+    int cl = cell_index(g, x, y);
     // FP32 offsets from the particle's own cell corner (|offset| <= one cell)
-    int ix = c % g.ndiv[0], iy = c / g.ndiv[0];
+    int ix = cl % g.ndiv[0], iy = cl / g.ndiv[0];
     double ox = x - (g.xmin[0] + (double)ix * g.deltx[0]);
     double oy = y - (g.xmin[1] + (double)iy * g.deltx[1]);
     float oxh = (float)ox, oyh = (float)oy;
@@ -223,6 +284,7 @@ __global__ void k_cell_count(Dev D) {
       D.yrl[i] = (float)(oy - (double)oyh);
     }
     D.hr[i] = (float)D.hsml[i];
+    c = g.cell0 + cl;
   }
   D.cell_of[i] = c;
   atomicAdd(&D.cell_cnt[c], 1);
@@ -239,7 +301,7 @@ __global__ void k_cell_fill(Dev D) {
 // per cell: sort the ids ascending (list_picell order), write sorted[] and spos[]
 __global__ void k_cell_sort(Dev D) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const Grid g = *D.grid;
+  const GridTotal g = *D.gtot;
   if (c > g.ncells) return;
   int st = D.cell_start[c], n = D.cell_cnt[c];
   for (int a = 0; a < n; a++) {
@@ -251,7 +313,7 @@ __global__ void k_cell_sort(Dev D) {
     }
     D.sorted[st + b + 1] = v;
   }
-  if (c == g.ncells) D.grid->nactive = st;
+  if (c == g.ncells) D.gtot->nactive = st;
 }
 
 __global__ void k_spos(Dev D) {
@@ -379,14 +441,14 @@ template <bool FAST>
 __global__ void k_half(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
-  const Grid g = *D.grid;
-  if (s >= g.nactive) {
+  if (s >= D.gtot->nactive) {
     D.half_cnt[s] = 0;
     return;
   }
-  const float tau = (float)D.bbox_part[0];
   int a = D.sorted[s];
-  int c = D.cell_of[a];
+  const Grid g = D.grid[D.rid[a]];
+  const float tau = g.tau;
+  int c = D.cell_of[a] - g.cell0;  // local cell in the realisation's grid
   int nx = g.ndiv[0], ny = g.ndiv[1];
   int ix = c % nx, iy = c / nx;
   float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
@@ -399,7 +461,7 @@ __global__ void k_half(Dev D) {
   for (int q = 0; q < 5; q++) {
     int jx = ix + cells[q][0], jy = iy + cells[q][1];
     if (jx < 0 || jx >= nx || jy >= ny) continue;
-    int cc = jy * nx + jx;
+    int cc = g.cell0 + jy * nx + jx;
     int lo = (q == 0) ? s + 1 : D.cell_start[cc];
     int hi = D.cell_start[cc] + D.cell_cnt[cc];
     float cx = (float)cells[q][0] * cw, cy = (float)cells[q][1] * ch;
@@ -446,14 +508,24 @@ __global__ void k_half(Dev D) {
   D.half_cnt[s] = k;
 }
 
+// pair counts of every realisation (its pairs are the half lists of its sorted range)
 __global__ void k_pair_meta(Dev D) {
-  PairMeta m = *D.meta;
-  int64_t n = D.half_off[D.N2];
-  m.m_prev = m.m;
-  m.n = n;
-  if (n > m.m) m.m = n;
-  *D.meta = m;
-  if (n > 2147483647LL) atomicOr(D.err, ERR_NPAIRS);
+  const GridTotal gt = *D.gtot;
+  for (int r = threadIdx.x; r < D.R; r += blockDim.x) {
+    const Grid& g = D.grid[r];
+    int64_t lo = 0, hi = 0;
+    if (!gt.overflow) {
+      lo = D.half_off[D.cell_start[g.cell0]];
+      hi = D.half_off[D.cell_start[g.cell0 + g.ncells]];
+    }
+    PairMeta m = D.meta[r];
+    m.m_prev = m.m;
+    m.n = hi - lo;
+    m.base = lo;
+    if (m.n > m.m) m.m = m.n;
+    D.meta[r] = m;
+  }
+  if (threadIdx.x == 0 && D.half_off[D.N2] > 2147483647LL) atomicOr(D.err, ERR_NPAIRS);
 }
 
 __device__ __forceinline__ void reverse_ell(int4* base, int N2, int s, int lo, int hi) {
@@ -476,34 +548,36 @@ __device__ __forceinline__ void reverse_ell(int4* base, int N2, int s, int lo, i
 __global__ void k_lists(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
-  const Grid g = *D.grid;
   int nC = 0, nS = 0, newC = 0, newS = 0;
-  if (s < g.nactive) {
+  if (s < D.gtot->nactive) {
     int t = D.sorted[s];
     int tt = D.itype[t];
     if (!is_dummy(tt)) {
-      const PairMeta meta = *D.meta;
+      const int r = D.rid[t];
+      const Grid& g = D.grid[r];
+      const PairMeta meta = D.meta[r];
       const bool reorder = meta.n > meta.m_prev;
-      int c = D.cell_of[t];
+      const int c0g = g.cell0;
+      int c = D.cell_of[t] - c0g;  // local cell
       int nx = g.ndiv[0];
       int ix = c % nx, iy = c / nx;
       int lo[2], hi[2];
       if (iy > 0) {
-        int c0 = (iy - 1) * nx + (ix > 0 ? ix - 1 : 0);
-        int c1 = (iy - 1) * nx + (ix + 1 < nx ? ix + 1 : ix);
+        int c0 = c0g + (iy - 1) * nx + (ix > 0 ? ix - 1 : 0);
+        int c1 = c0g + (iy - 1) * nx + (ix + 1 < nx ? ix + 1 : ix);
         lo[0] = D.cell_start[c0];
         hi[0] = D.cell_start[c1] + D.cell_cnt[c1];
       } else {
         lo[0] = hi[0] = 0;
       }
-      lo[1] = D.cell_start[ix > 0 ? c - 1 : c];
+      lo[1] = D.cell_start[c0g + (ix > 0 ? c - 1 : c)];
       hi[1] = s;
       auto push = [&](int u, int w, float gx, float gy, int64_t cidx) {
         int ut = D.itype[u];
         int pt = pint_type(tt, ut);
         bool same = (pt == 2 || pt == 3);
         int4 e = make_int4(u, w, __float_as_int(gx), __float_as_int(gy));
-        bool isnew = reorder && cidx >= meta.m_prev;
+        bool isnew = reorder && cidx - meta.base >= meta.m_prev;
         if (same) {
           if (nS < D.capS) D.same[(size_t)nS * D.N2 + s] = e;
           nS++;
@@ -665,7 +739,7 @@ int launch_pair_build(Ctx& c) {
   c.mark("scan_half", 3);
   scan_i32_to_i64(c, D.half_cnt, D.half_off, D.N2);
   c.mark("pair_meta");
-  k_pair_meta<<<1, 1, 0, st>>>(D);
+  k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("lists");
   k_lists<<<nb, kBlock, 0, st>>>(D);
   return 0;

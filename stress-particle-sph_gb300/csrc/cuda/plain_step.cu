@@ -31,10 +31,10 @@ constexpr int kBlock = 256;
 
 // adapt_stress2: the reference's FP64 arithmetic in the plain form, the division-free
 // variant in the FP32 form
-__device__ __forceinline__ void stress_return(const Dev& D, double& a, double& b, double& c,
-                                              double& d) {
-  if (D.fast) adapt_stress_fast(D.alpha2, D.kc, D.kc_shift, a, b, c, d);
-  else adapt_stress(D.alpha2, D.kc, a, b, c, d);
+__device__ __forceinline__ void stress_return(const Dev& D, const Real& M, double& a,
+                                              double& b, double& c, double& d) {
+  if (D.fast) adapt_stress_fast(M.alpha2, M.kc, M.kc_shift, a, b, c, d);
+  else adapt_stress(M.alpha2, M.kc, a, b, c, d);
 }
 
 // FP32-form neighbour records of particle i (velocity, volume, stress, internal variable)
@@ -52,7 +52,7 @@ __device__ __forceinline__ void write_records(const Dev& D, int i, double vx, do
 
 __global__ void k_load_scalars(Dev D) {
   int k = *D.step_idx;
-  *D.cur = D.scal_table[k];
+  for (int r = threadIdx.x; r < D.R; r += blockDim.x) D.cur[r] = D.scal_table[(size_t)k * D.R + r];
 }
 
 __global__ void k_next_step(Dev D) { *D.step_idx += 1; }
@@ -98,9 +98,10 @@ __global__ void k_step_init(Dev D) {
 
 // boundary_forces, test == 2 (2_SPH_main_2018.f90:1117-1161): FP32 locals.  Only innermost
 // dummies closer than 0.75 dx give a non-zero term; they are summed in ascending id.
-__device__ __forceinline__ bool bound_term(const Dev& D, int i, int j, float& fx, float& fy) {
+__device__ __forceinline__ bool bound_term(const Dev& D, const Real& M, int i, int j, float& fx,
+                                           float& fy) {
   const float cc = 20.0f;
-  const float d0 = (float)(D.dx / 2.0);
+  const float d0 = (float)(M.dx / 2.0);
   float r0 = (float)(D.px[i] - D.px[j]);
   float r1 = (float)(D.py[i] - D.py[j]);
   float r2 = sqrtf(r0 * r0 + r1 * r1);
@@ -128,7 +129,8 @@ __global__ void k_bound(Dev D) {
   int ids[K];
   float tx[K], ty[K];
   int n = 0;
-  const int j0 = D.NT, j1 = D.NT + D.ndummy2;
+  const Real& M = real_of(D, i);
+  const int j0 = M.dum0, j1 = M.dum0 + M.ndum2;
   if (D.bound_from_lists) {
     int s = D.spos[i];
     int deg = D.degC[s];
@@ -136,7 +138,7 @@ __global__ void k_bound(Dev D) {
       int u = D.cross[(size_t)k * D.N2 + s].x;
       if (u < j0 || u >= j1) continue;
       float fx, fy;
-      if (!bound_term(D, i, u, fx, fy)) continue;
+      if (!bound_term(D, M, i, u, fx, fy)) continue;
       if (n < K) {
         int p = n++;
         while (p > 0 && ids[p - 1] > u) {
@@ -163,7 +165,7 @@ __global__ void k_bound(Dev D) {
     double bx = 0.0, by = 0.0;
     for (int j = j0; j < j1; j++) {
       float fx, fy;
-      if (!bound_term(D, i, j, fx, fy)) continue;
+      if (!bound_term(D, M, i, j, fx, fy)) continue;
       bx = bx + (double)fx;
       by = by + (double)fy;
     }
@@ -176,8 +178,10 @@ __global__ void k_stage_begin(Dev D, int stage) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
   const double f1rk[4] = {0.0, 0.5, 0.5, 1.0};
-  const double f1dt = f1rk[stage] * D.dt;
-  const StepScalars& sc = *D.cur;
+  const int r = D.rid[i];
+  const Real& M = D.real[r];
+  const double f1dt = f1rk[stage] * M.dt;
+  const StepScalars& sc = D.cur[r];
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (i < D.NN) {
@@ -203,7 +207,7 @@ __global__ void k_stage_begin(Dev D, int stage) {
       }
     }
   }
-  if (D.ncrit == 12) stress_return(D, a, b, c, d);
+  if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
   apply_bcs(D, sc, i, vx, vy, a, b, c);
   D.vx[i] = vx;
   D.vy[i] = vy;
@@ -222,12 +226,13 @@ __global__ void k_interp(Dev D) {
   int tt = D.itype[t];
   if (t >= D.NT) return;
   if (!D.sp_sph) {
+    const Real& M = real_of(D, t);
     if (t >= D.NN) {
-      int n = t - D.NN;
+      int n = node_of_sp(M, t);
       D.vx[t] = D.vx[n];
       D.vy[t] = D.vy[n];
     } else {
-      int sp = t + D.NN;
+      int sp = sp_of_node(M, t);
       D.s0[t] = D.s0[sp];
       D.s1[t] = D.s1[sp];
       D.s2[t] = D.s2[sp];
@@ -300,11 +305,13 @@ __global__ void k_node_rho(Dev D) {
 __global__ void k_adapt_bc(Dev D, int with_A) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
-  const StepScalars& sc = *D.cur;
+  const int r = D.rid[i];
+  const Real& M = D.real[r];
+  const StepScalars& sc = D.cur[r];
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (D.sp_sph) {
-    if (D.ncrit == 12) stress_return(D, a, b, c, d);
+    if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
     apply_bcs(D, sc, i, vx, vy, a, b, c);
     D.vx[i] = vx;
     D.vy[i] = vy;
@@ -362,7 +369,8 @@ __global__ void k_derivs(Dev D, int stage) {
   if (t >= D.NT) return;
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
-  const StepScalars& sc = *D.cur;
+  const Real& Mt = real_of(D, t);
+  const StepScalars& sc = D.cur[D.rid[t]];
   int tt = D.itype[t];
   int deg = D.degC[s];
   double AE[4] = {0.0, 0.0, 0.0, 0.0};
@@ -456,7 +464,7 @@ __global__ void k_derivs(Dev D, int stage) {
     }
     const double vtx = D.vx[t], vty = D.vy[t];
     double avx = 0.0, avy = 0.0;
-    if (D.alpha > 0 || D.beta > 0) {
+    if (Mt.alpha > 0 || Mt.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904): FP32 accumulators
       float ax = 0.0f, ay = 0.0f;
       int degs = D.degS[s];
@@ -473,7 +481,7 @@ __global__ void k_derivs(Dev D, int stage) {
         float theta = (h * div_u) / (sq * sq + 0.01f * (h * h));
         float visc = 0.0f;
         if (div_u < 0)
-          visc = (float)((-((D.alpha * 600.0) * (double)theta) + D.beta * (double)(theta * theta)) /
+          visc = (float)((-((Mt.alpha * 600.0) * (double)theta) + Mt.beta * (double)(theta * theta)) /
                          (double)rho2);
         float px = visc * __int_as_float(e.z), py = visc * __int_as_float(e.w);
         double mu = D.mass[u];
@@ -490,8 +498,10 @@ __global__ void k_derivs(Dev D, int stage) {
 __global__ void k_rk_final(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
-  const StepScalars& sc = *D.cur;
-  const double dt6 = D.dt / 6.0;
+  const int r = D.rid[i];
+  const Real& M = D.real[r];
+  const StepScalars& sc = D.cur[r];
+  const double dt6 = M.dt / 6.0;
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (i < D.NN) {
@@ -503,7 +513,7 @@ __global__ void k_rk_final(Dev D) {
     c = D.st0[2][i] + dt6 * D.RKs[2][i];
     d = D.st0[3][i] + dt6 * D.RKs[3][i];
   }
-  if (D.ncrit == 12) stress_return(D, a, b, c, d);
+  if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
   apply_bcs(D, sc, i, vx, vy, a, b, c);
   D.vx[i] = vx;
   D.vy[i] = vy;
@@ -521,7 +531,7 @@ __global__ void k_rk_final(Dev D) {
     }
     double dd = D.RKd[i] / 6.0;
     D.Ddev[i] = dd;
-    D.iv1[i] = D.iv1[i] + D.dt * dd;  // update_strain (3_SPH_material_2018.f90:1864)
+    D.iv1[i] = D.iv1[i] + M.dt * dd;  // update_strain (3_SPH_material_2018.f90:1864)
   }
   if (D.fast) write_records(D, i, vx, vy, a, b, c, d);
 }
@@ -532,8 +542,9 @@ __global__ void k_trapezoid(Dev D) {
   if (D.update_x) {
     float hx = (float)(0.5 * (D.vx0[i] + D.vx[i]));
     float hy = (float)(0.5 * (D.vy0[i] + D.vy[i]));
-    double x = D.x0x[i] + (double)hx * D.dt;
-    double y = D.x0y[i] + (double)hy * D.dt;
+    const double dt = real_of(D, i).dt;
+    double x = D.x0x[i] + (double)hx * dt;
+    double y = D.x0y[i] + (double)hy * dt;
     D.px[i] = x;
     D.py[i] = y;
   }
@@ -560,24 +571,26 @@ __global__ void k_xsph(Dev D) {
     if (t < D.NN && D.bc_or_not[u] == 2 && flag != 2) mark = true;
   }
   const double eps = 0.5;
-  D.px[t] = D.x0x[t] + D.dt * (vt0 + eps * s0);
-  D.py[t] = D.x0y[t] + D.dt * (vt1 + eps * s1);
+  const double dt = real_of(D, t).dt;
+  D.px[t] = D.x0x[t] + dt * (vt0 + eps * s0);
+  D.py[t] = D.x0y[t] + dt * (vt1 + eps * s1);
   if (mark) D.bc_or_not[t] = 3;
 }
 
 __global__ void k_displ(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NN) return;
+  const Real& M = real_of(D, i);
   if (D.update_x) {
     if (!D.sp_sph) {
-      D.px[D.NN + i] = D.px[i];
-      D.py[D.NN + i] = D.py[i];
+      D.px[sp_of_node(M, i)] = D.px[i];
+      D.py[sp_of_node(M, i)] = D.py[i];
     }
     D.dispx[i] = D.px[i] - D.x00x[i];
     D.dispy[i] = D.py[i] - D.x00y[i];
   } else {
-    D.dispx[i] = D.dispx[i] + (0.5 * (D.vx0[i] + D.vx[i])) * D.dt;
-    D.dispy[i] = D.dispy[i] + (0.5 * (D.vy0[i] + D.vy[i])) * D.dt;
+    D.dispx[i] = D.dispx[i] + (0.5 * (D.vx0[i] + D.vx[i])) * M.dt;
+    D.dispy[i] = D.dispy[i] + (0.5 * (D.vy0[i] + D.vy[i])) * M.dt;
   }
 }
 
@@ -623,7 +636,7 @@ int launch_plain_step(Ctx& c) {
   int nbN = (D.NN + kBlock - 1) / kBlock;
   int nb2 = (D.N2 + kBlock - 1) / kBlock;
   c.mark("load_scalars");
-  k_load_scalars<<<1, 1, 0, st>>>(D);
+  k_load_scalars<<<1, 128, 0, st>>>(D);
   launch_pair_build(c);
   c.mark("step_init");
   k_step_init<<<nbT, kBlock, 0, st>>>(D);

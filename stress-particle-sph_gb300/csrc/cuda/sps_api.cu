@@ -41,32 +41,33 @@ T* dalloc(sps::Ctx& c, size_t n) {
   return static_cast<T*>(p);
 }
 
-double tcurve_value(const sps::Ctx& c, int it, double t) {
-  int nc = c.p.ntcurves;
+double tcurve_value(const sps::HostReal& h, int it, double t) {
+  int nc = h.p.ntcurves;
   if (it < 1 || it > nc) return 0.0;
-  int npts = c.nptstcurves[it - 1];
+  int npts = h.nptstcurves[it - 1];
   double tt0 = 0, tt1 = 0;
   int ip;
   for (ip = 1; ip <= npts - 1; ip++) {
-    tt0 = c.ttcurves[(it - 1) + (size_t)(ip - 1) * nc];
-    tt1 = c.ttcurves[(it - 1) + (size_t)ip * nc];
+    tt0 = h.ttcurves[(it - 1) + (size_t)(ip - 1) * nc];
+    tt1 = h.ttcurves[(it - 1) + (size_t)ip * nc];
     if (t >= tt0 && t <= tt1) break;
     tt0 = -1000.0;
   }
   if (tt0 >= 0.0) {
     double xi = (t - tt0) / (tt1 - tt0);
-    return (1.0 - xi) * (double)c.ftcurves[(it - 1) + (size_t)(ip - 1) * nc] +
-           xi * (double)c.ftcurves[(it - 1) + (size_t)ip * nc];
+    return (1.0 - xi) * (double)h.ftcurves[(it - 1) + (size_t)(ip - 1) * nc] +
+           xi * (double)h.ftcurves[(it - 1) + (size_t)ip * nc];
   }
   return 0.0;
 }
 
-void fill_scalars(sps::Ctx& c, double t, sps::StepScalars& s) {
+// time-only scalars of one realisation at time t: gravity time-curve factor and BC values
+void fill_scalars(const sps::HostReal& h, double t, sps::StepScalars& s) {
   std::memset(&s, 0, sizeof(s));
   s.time_sph = t;
-  if (c.p.ic_grav != 0) s.factg = tcurve_value(c, c.p.tcurve_grav, t) * c.p.ft_grav;
-  for (int b = 0; b < c.p.no_bcs; b++) {
-    const double* q = &c.bc_list[8 * (size_t)b];
+  if (h.p.ic_grav != 0) s.factg = tcurve_value(h, h.p.tcurve_grav, t) * h.p.ft_grav;
+  for (int b = 0; b < h.p.no_bcs; b++) {
+    const double* q = &h.bc_list[8 * (size_t)b];
     int itc = (int)q[2];
     double val = 0.0;
     if (itc == 0) {
@@ -75,10 +76,32 @@ void fill_scalars(sps::Ctx& c, double t, sps::StepScalars& s) {
       double argum = w * t - phi;
       val = (a0 + a1 * std::sin(argum)) * fact;
     } else if (itc > 0) {
-      val = tcurve_value(c, itc, t) * q[3];
+      val = tcurve_value(h, itc, t) * q[3];
     }
     s.bcval[b] = val;
   }
+}
+
+// the per-step scalar table of nsteps steps from the times t[r] (advanced in place)
+void fill_table(sps::Ctx& c, int nsteps, double* t) {
+  const int R = c.d.R;
+  c.h_scal.resize((size_t)nsteps * R);
+  for (int k = 0; k < nsteps; k++)
+    for (int r = 0; r < R; r++) {
+      fill_scalars(c.hr[r], t[r], c.h_scal[(size_t)k * R + r]);
+      t[r] = t[r] + c.hr[r].p.dt_sph;
+    }
+}
+
+// the three id segments of realisation r: local start, count, global start
+struct Seg {
+  int64_t l, n, g;
+};
+void segments(const sps::Ctx& c, int r, Seg* s) {
+  const sps::Real& M = c.real[r];
+  s[0] = {0, M.nnode, M.node0};
+  s[1] = {M.nnode, M.nsp, M.sp0};
+  s[2] = {(int64_t)M.nnode + M.nsp, M.ndum, M.dum0};
 }
 
 __global__ void k_aos_to_soa2(const double* in, double* a, double* b, int n) {
@@ -150,7 +173,7 @@ void ensure_scal(sps::Ctx& c, int n) {
   if (n <= c.scal_cap) return;
   int cap = std::max(n, 256);
   void* p = nullptr;
-  SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(sps::StepScalars) * cap));
+  SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(sps::StepScalars) * (size_t)cap * c.d.R));
   c.allocs.push_back(p);
   c.d_scal_table = static_cast<sps::StepScalars*>(p);
   c.scal_cap = cap;
@@ -176,9 +199,10 @@ std::string err_text(int e) {
 
 extern "C" {
 
-int sps_create(const sps_params* p, sps_ctx** out) {
-  if (!p || !out) return fail(nullptr, SPS_ERR_ARG, "null argument");
-  *out = nullptr;
+namespace {
+
+// the checks sps_create makes on one problem
+int check_params(const sps_params* p) {
   if (p->ndimn != 2 || p->nstre != 4)
     return fail(nullptr, SPS_ERR_UNSUPPORTED, "only ndimn = 2, nstre = 4 are implemented");
   if (p->art_stress)
@@ -207,6 +231,39 @@ int sps_create(const sps_params* p, sps_ctx** out) {
       return fail(nullptr, SPS_ERR_UNSUPPORTED, "negative time-curve index in bc_list");
   if (p->ic_grav != 0 && (p->tcurve_grav < 1 || p->tcurve_grav > p->ntcurves))
     return fail(nullptr, SPS_ERR_ARG, "gravity time curve out of range");
+  return SPS_OK;
+}
+
+// the solver flags a batch must share
+bool same_flags(const sps_params& a, const sps_params& b) {
+  return a.sp_sph == b.sp_sph && a.inside_approach == b.inside_approach && a.cspm == b.cspm &&
+         a.xsph == b.xsph && a.update_x == b.update_x && a.cont_density == b.cont_density &&
+         a.sle == b.sle && a.skf == b.skf && a.precision == b.precision && a.pi == b.pi &&
+         a.ntype_solid == b.ntype_solid;
+}
+
+}  // namespace
+
+int sps_create(const sps_params* p, sps_ctx** out) { return sps_create_batch(1, p, out); }
+
+int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
+  if (!ps || !out || nreal < 1) return fail(nullptr, SPS_ERR_ARG, "null argument or no realisation");
+  *out = nullptr;
+  if (nreal > 65535) return fail(nullptr, SPS_ERR_ARG, "at most 65535 realisations");
+  int64_t NN = 0, NS = 0, ND = 0;
+  for (int r = 0; r < nreal; r++) {
+    int rc = check_params(&ps[r]);
+    if (rc != SPS_OK) return rc;
+    if (!same_flags(ps[0], ps[r]))
+      return fail(nullptr, SPS_ERR_ARG, "the realisations of a batch must share the solver flags");
+    if (nreal > 1 && ps[r].no_bcs > 0)
+      return fail(nullptr, SPS_ERR_UNSUPPORTED, "boundary conditions in a batch of several realisations");
+    NN += ps[r].nnode;
+    NS += ps[r].nstress;
+    ND += ps[r].ndummy;
+  }
+  if (NN + NS + ND > 2000000000LL) return fail(nullptr, SPS_ERR_ARG, "too many particles");
+  const sps_params* p = &ps[0];
   sps_ctx* h = nullptr;
   try {
     h = new sps_ctx();
@@ -217,18 +274,71 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
     c.device = dev;
     SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-    if (p->ntcurves > 0) {
-      size_t nt = (size_t)p->ntcurves * p->mptstcurves;
-      c.nptstcurves.assign(p->nptstcurves, p->nptstcurves + p->ntcurves);
-      c.ttcurves.assign(p->ttcurves, p->ttcurves + nt);
-      c.ftcurves.assign(p->ftcurves, p->ftcurves + nt);
-    }
-    if (p->no_bcs > 0) c.bc_list.assign(p->bc_list, p->bc_list + 8 * (size_t)p->no_bcs);
     sps::Dev& D = c.d;
-    D.NN = p->nnode;
-    D.NT = p->nnode + p->nstress;
-    D.N2 = D.NT + p->ndummy;
-    D.ndummy2 = p->ndummy2;
+    D.R = nreal;
+    D.NN = (int)NN;
+    D.NT = (int)(NN + NS);
+    D.N2 = (int)(NN + NS + ND);
+    c.hr.resize(nreal);
+    c.real.resize(nreal);
+    int64_t on = 0, os = NN, od = NN + NS;
+    for (int r = 0; r < nreal; r++) {
+      const sps_params& q = ps[r];
+      sps::HostReal& hr = c.hr[r];
+      hr.p = q;
+      if (q.ntcurves > 0) {
+        size_t nt = (size_t)q.ntcurves * q.mptstcurves;
+        hr.nptstcurves.assign(q.nptstcurves, q.nptstcurves + q.ntcurves);
+        hr.ttcurves.assign(q.ttcurves, q.ttcurves + nt);
+        hr.ftcurves.assign(q.ftcurves, q.ftcurves + nt);
+      }
+      if (q.no_bcs > 0) hr.bc_list.assign(q.bc_list, q.bc_list + 8 * (size_t)q.no_bcs);
+      hr.p.nptstcurves = hr.nptstcurves.data();
+      hr.p.ttcurves = hr.ttcurves.data();
+      hr.p.ftcurves = hr.ftcurves.data();
+      hr.p.bc_list = hr.bc_list.data();
+      hr.p.wall_position = nullptr;
+      hr.p.horizontal_or_not = nullptr;
+      sps::Real& M = c.real[r];
+      M.node0 = (int)on;
+      M.nnode = q.nnode;
+      M.sp0 = (int)os;
+      M.nsp = q.nstress;
+      M.dum0 = (int)od;
+      M.ndum = q.ndummy;
+      M.ndum2 = q.ndummy2;
+      on += q.nnode;
+      os += q.nstress;
+      od += q.ndummy;
+      M.ntype_eco = (int)q.props[0];
+      M.ncrit = (int)q.props[1];
+      M.ntype_solid = q.ntype_solid;
+      M.ic_grav = q.ic_grav;
+      M.dt = q.dt_sph;
+      M.dx = q.dx;
+      M.alpha = q.alpha;
+      M.beta = q.beta;
+      M.damping = q.damping;
+      M.D11 = q.D11;
+      M.D12 = q.D12;
+      M.D22 = q.D22;
+      M.D33 = q.D33;
+      M.D41 = q.D41;
+      M.D42 = q.D42;
+      M.tanfi = q.props[12];
+      M.coh = q.props[13];
+      M.young = q.props[2];
+      M.poiss = q.props[3];
+      double den = std::sqrt(9.0 + 12.0 * (M.tanfi * M.tanfi));
+      M.alpha2 = M.tanfi / den;
+      M.kc = (3.0 * M.coh) / den;
+      M.kc_shift = M.alpha2 > 0.0 ? M.kc / (3.0 * M.alpha2) : 0.0;
+      for (int d = 0; d < 2; d++) {
+        M.xmin_dom[d] = q.xmin_domain[d];
+        M.xmax_dom[d] = q.xmax_domain[d];
+        M.cgrav[d] = q.cgrav[d];
+      }
+    }
     D.capC = D.capS = D.capH = 0;  // sized at upload from the kernel support
     D.skf = p->skf;
     D.scale_k = p->skf == 1 ? 2 : 3;
@@ -240,39 +350,27 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     D.sp_sph = p->sp_sph;
     D.inside = p->inside_approach;
     D.no_bcs = p->no_bcs;
-    D.ntype_eco = ntype_eco;
-    D.ncrit = ncrit;
-    D.ntype_solid = p->ntype_solid;
-    D.ic_grav = p->ic_grav;
     D.pi = p->pi;
-    D.dt = p->dt_sph;
-    D.alpha = p->alpha;
-    D.beta = p->beta;
-    D.damping = p->damping;
-    D.dx = p->dx;
-    D.D11 = p->D11;
-    D.D12 = p->D12;
-    D.D22 = p->D22;
-    D.D33 = p->D33;
-    D.D41 = p->D41;
-    D.D42 = p->D42;
-    D.tanfi = p->props[12];
-    D.coh = p->props[13];
-    D.young = p->props[2];
-    D.poiss = p->props[3];
-    {
-      double den = std::sqrt(9.0 + 12.0 * (D.tanfi * D.tanfi));
-      D.alpha2 = D.tanfi / den;
-      D.kc = (3.0 * D.coh) / den;
-      D.kc_shift = D.alpha2 > 0.0 ? D.kc / (3.0 * D.alpha2) : 0.0;
-    }
-    for (int d = 0; d < 2; d++) {
-      D.xmin_dom[d] = p->xmin_domain[d];
-      D.xmax_dom[d] = p->xmax_domain[d];
-      D.cgrav[d] = p->cgrav[d];
-    }
     for (int b = 0; b < p->no_bcs; b++) D.bcvar[b] = (int)p->bc_list[8 * (size_t)b + 1];
-    const size_t N2 = D.N2, NT = D.NT, NN = D.NN;
+    const size_t N2 = D.N2, NT = D.NT, NN_ = D.NN;
+    {
+      sps::Real* rd = dalloc<sps::Real>(c, nreal);
+      SPS_CUDA_CHECK(cudaMemcpyAsync(rd, c.real.data(), sizeof(sps::Real) * nreal,
+                                     cudaMemcpyHostToDevice, c.stream));
+      D.real = rd;
+      std::vector<uint16_t> rid(N2);
+      for (int r = 0; r < nreal; r++) {
+        const sps::Real& M = c.real[r];
+        std::fill(rid.begin() + M.node0, rid.begin() + M.node0 + M.nnode, (uint16_t)r);
+        std::fill(rid.begin() + M.sp0, rid.begin() + M.sp0 + M.nsp, (uint16_t)r);
+        std::fill(rid.begin() + M.dum0, rid.begin() + M.dum0 + M.ndum, (uint16_t)r);
+      }
+      uint16_t* ridd = dalloc<uint16_t>(c, N2);
+      SPS_CUDA_CHECK(cudaMemcpyAsync(ridd, rid.data(), sizeof(uint16_t) * N2, cudaMemcpyHostToDevice,
+                                     c.stream));
+      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+      D.rid = ridd;
+    }
     D.px = dalloc<double>(c, N2);
     D.py = dalloc<double>(c, N2);
     D.vx = dalloc<double>(c, N2);
@@ -288,13 +386,13 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     D.fdp = dalloc<double>(c, NT);
     D.x00x = dalloc<double>(c, N2);
     D.x00y = dalloc<double>(c, N2);
-    D.dispx = dalloc<double>(c, NN);
-    D.dispy = dalloc<double>(c, NN);
+    D.dispx = dalloc<double>(c, NN_);
+    D.dispy = dalloc<double>(c, NN_);
     D.itype = dalloc<int32_t>(c, N2);
     D.out = dalloc<uint8_t>(c, N2);
     D.bc_or_not = dalloc<int32_t>(c, NT);
     D.bc_info = dalloc<int32_t>(c, 8 * NT);
-    D.bc_int = dalloc<int32_t>(c, NN);
+    D.bc_int = dalloc<int32_t>(c, NN_);
     D.wallpos = dalloc<float>(c, N2);
     D.horiz = dalloc<float>(c, N2);
     D.grad_u = dalloc<double>(c, 4 * NT);
@@ -318,8 +416,8 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     D.RKd = dalloc<double>(c, NT);
     D.RHSr = dalloc<double>(c, NT);
     D.RHSh = dalloc<double>(c, NT);
-    D.fbx = dalloc<double>(c, NN);
-    D.fby = dalloc<double>(c, NN);
+    D.fbx = dalloc<double>(c, NN_);
+    D.fby = dalloc<double>(c, NN_);
     D.Ddev = dalloc<double>(c, NT);
     D.vol = dalloc<double>(c, N2);
     D.rinv = dalloc<double>(c, N2);
@@ -340,31 +438,42 @@ int sps_create(const sps_params* p, sps_ctx** out) {
     D.hr = dalloc<float>(c, N2);
     D.xrl = dalloc<float>(c, N2);
     D.yrl = dalloc<float>(c, N2);
-    D.grid = dalloc<sps::Grid>(c, 1);
-    D.nbbox_blocks = (int)((N2 + kBlock - 1) / kBlock);
-    D.bbox_part = dalloc<double>(c, 6 * (size_t)D.nbbox_blocks + 8);
+    D.grid = dalloc<sps::Grid>(c, nreal);
+    D.gtot = dalloc<sps::GridTotal>(c, 1);
+    D.bbox = dalloc<unsigned long long>(c, 6 * (size_t)nreal);
     D.half_cnt = dalloc<int32_t>(c, N2);
     D.half_off = dalloc<int64_t>(c, N2 + 1);
     D.degC = dalloc<int32_t>(c, N2);
     D.degS = dalloc<int32_t>(c, N2);
-    D.meta = dalloc<sps::PairMeta>(c, 1);
+    D.meta = dalloc<sps::PairMeta>(c, nreal);
     D.step_idx = dalloc<int>(c, 1);
-    D.cur = dalloc<sps::StepScalars>(c, 1);
+    D.cur = dalloc<sps::StepScalars>(c, nreal);
     D.err = dalloc<int>(c, 1);
     D.scan_tmp = dalloc<int64_t>(c, (N2 + 4096) / 4096 + 64);
     c.stage = dalloc<double>(c, 4 * N2);
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.meta, 0, sizeof(sps::PairMeta), c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.meta, 0, sizeof(sps::PairMeta) * nreal, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.bbox, 0xff, sizeof(unsigned long long) * 6 * nreal, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.gtot, 0, sizeof(sps::GridTotal), c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.err, 0, sizeof(int), c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.grad_u, 0, sizeof(double) * 4 * NT, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_or_not, 0, sizeof(int32_t) * NT, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_info, 0, sizeof(int32_t) * 8 * NT, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_int, 0, sizeof(int32_t) * NN, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.fbx, 0, sizeof(double) * NN, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.fby, 0, sizeof(double) * NN, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_int, 0, sizeof(int32_t) * NN_, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.fbx, 0, sizeof(double) * NN_, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.fby, 0, sizeof(double) * NN_, c.stream));
     {
+      // dummy wall tables: realisation r's entries ntotal_r.. go to its dummy ids
       std::vector<float> wp(N2, 0.0f), ho(N2, 0.0f);
-      if (p->wall_position) std::copy(p->wall_position, p->wall_position + N2, wp.begin());
-      if (p->horizontal_or_not) std::copy(p->horizontal_or_not, p->horizontal_or_not + N2, ho.begin());
+      for (int r = 0; r < nreal; r++) {
+        const sps_params& q = ps[r];
+        const sps::Real& M = c.real[r];
+        size_t nt_r = (size_t)q.nnode + q.nstress;
+        if (q.wall_position)
+          std::copy(q.wall_position + nt_r, q.wall_position + nt_r + q.ndummy, wp.begin() + M.dum0);
+        if (q.horizontal_or_not)
+          std::copy(q.horizontal_or_not + nt_r, q.horizontal_or_not + nt_r + q.ndummy,
+                    ho.begin() + M.dum0);
+      }
       SPS_CUDA_CHECK(cudaMemcpyAsync(D.wallpos, wp.data(), sizeof(float) * N2, cudaMemcpyHostToDevice, c.stream));
       SPS_CUDA_CHECK(cudaMemcpyAsync(D.horiz, ho.data(), sizeof(float) * N2, cudaMemcpyHostToDevice, c.stream));
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
@@ -388,70 +497,108 @@ int sps_upload(sps_ctx* h, const double* x, const double* vel, const double* str
                const double* mass, const double* rho, const double* hsml, const int32_t* itype,
                const double* intvars1, const double* f_drucker, const double* x00) {
   if (!h) return SPS_ERR_ARG;
+  if (h->c.d.R != 1)
+    return fail(&h->c, SPS_ERR_ARG, "sps_upload: a batch takes sps_upload_real per realisation");
+  return sps_upload_real(h, 0, x, vel, stress, mass, rho, hsml, itype, intvars1, f_drucker, x00);
+}
+
+int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
+                    const double* stress, const double* mass, const double* rho,
+                    const double* hsml, const int32_t* itype, const double* intvars1,
+                    const double* f_drucker, const double* x00) {
+  if (!h) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
+  sps::Dev& D = c.d;
+  if (r < 0 || r >= D.R) return fail(&c, SPS_ERR_ARG, "sps_upload_real: no such realisation");
   if (!x || !vel || !stress || !mass || !rho || !hsml || !itype)
     return fail(&c, SPS_ERR_ARG, "sps_upload: null array");
-  sps::Dev& D = c.d;
-  const size_t N2 = D.N2, NT = D.NT;
-  for (size_t i = 0; i < N2; i++)
+  const sps::Real& M = c.real[r];
+  const size_t nn = M.nnode, nt = (size_t)M.nnode + M.nsp, n2 = nt + M.ndum;
+  for (size_t i = 0; i < n2; i++)
     if (itype[i] != 1 && itype[i] != 2 && itype[i] != 25)
       return fail(&c, SPS_ERR_ARG, "sps_upload: itype must be 1, 2 or 25");
-  for (size_t i = 0; i < N2; i++) {
-    int want = i < (size_t)D.NN ? 2 : i < NT ? 1 : 25;
+  for (size_t i = 0; i < n2; i++) {
+    int want = i < nn ? 2 : i < nt ? 1 : 25;
     if (itype[i] != want)
       return fail(&c, SPS_ERR_ARG, "sps_upload: particles must be ordered nodes, stress-points, dummies");
   }
+  Seg sg[3];
+  segments(c, r, sg);
   try {
-    // staging buffers: interleaved arrays are transposed on the device
+    // interleaved arrays are staged whole and transposed segment by segment
     double* stage = c.stage;
-    int nb = (int)((N2 + kBlock - 1) / kBlock);
+    auto nbk = [](int64_t n) { return (int)((n + kBlock - 1) / kBlock); };
     auto up2 = [&](const double* src, double* a, double* b) {
-      SPS_CUDA_CHECK(cudaMemcpyAsync(stage, src, sizeof(double) * 2 * N2, cudaMemcpyHostToDevice, c.stream));
-      k_aos_to_soa2<<<nb, kBlock, 0, c.stream>>>(stage, a, b, (int)N2);
+      SPS_CUDA_CHECK(cudaMemcpyAsync(stage, src, sizeof(double) * 2 * n2, cudaMemcpyHostToDevice, c.stream));
+      for (const Seg& q : sg)
+        if (q.n > 0)
+          k_aos_to_soa2<<<nbk(q.n), kBlock, 0, c.stream>>>(stage + 2 * q.l, a + q.g, b + q.g, (int)q.n);
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    };
+    auto up1 = [&](void* dst, const void* src, size_t esz, int nseg) {
+      for (int k = 0; k < nseg; k++)
+        if (sg[k].n > 0)
+          SPS_CUDA_CHECK(cudaMemcpyAsync((char*)dst + esz * sg[k].g, (const char*)src + esz * sg[k].l,
+                                         esz * sg[k].n, cudaMemcpyHostToDevice, c.stream));
     };
     up2(x, D.px, D.py);
     up2(vel, D.vx, D.vy);
     up2(x00 ? x00 : x, D.x00x, D.x00y);
-    SPS_CUDA_CHECK(cudaMemcpyAsync(stage, stress, sizeof(double) * 4 * N2, cudaMemcpyHostToDevice, c.stream));
-    k_aos_to_soa4<<<nb, kBlock, 0, c.stream>>>(stage, D.s0, D.s1, D.s2, D.s3, (int)N2);
-    SPS_CUDA_CHECK(cudaMemcpyAsync(D.mass, mass, sizeof(double) * N2, cudaMemcpyHostToDevice, c.stream));
-    SPS_CUDA_CHECK(cudaMemcpyAsync(D.rho, rho, sizeof(double) * N2, cudaMemcpyHostToDevice, c.stream));
-    SPS_CUDA_CHECK(cudaMemcpyAsync(D.hsml, hsml, sizeof(double) * N2, cudaMemcpyHostToDevice, c.stream));
-    SPS_CUDA_CHECK(cudaMemcpyAsync(D.itype, itype, sizeof(int32_t) * N2, cudaMemcpyHostToDevice, c.stream));
-    if (intvars1)
-      SPS_CUDA_CHECK(cudaMemcpyAsync(D.iv1, intvars1, sizeof(double) * NT, cudaMemcpyHostToDevice, c.stream));
-    else
-      SPS_CUDA_CHECK(cudaMemsetAsync(D.iv1, 0, sizeof(double) * NT, c.stream));
-    if (f_drucker)
-      SPS_CUDA_CHECK(cudaMemcpyAsync(D.fdp, f_drucker, sizeof(double) * NT, cudaMemcpyHostToDevice, c.stream));
-    else
-      SPS_CUDA_CHECK(cudaMemsetAsync(D.fdp, 0, sizeof(double) * NT, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.out, 0, N2, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.dispx, 0, sizeof(double) * D.NN, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(D.dispy, 0, sizeof(double) * D.NN, c.stream));
-    sps::launch_vol(c, 0, (int)N2);
+    SPS_CUDA_CHECK(cudaMemcpyAsync(stage, stress, sizeof(double) * 4 * n2, cudaMemcpyHostToDevice, c.stream));
+    for (const Seg& q : sg)
+      if (q.n > 0)
+        k_aos_to_soa4<<<nbk(q.n), kBlock, 0, c.stream>>>(stage + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
+                                                          D.s2 + q.g, D.s3 + q.g, (int)q.n);
+    up1(D.mass, mass, sizeof(double), 3);
+    up1(D.rho, rho, sizeof(double), 3);
+    up1(D.hsml, hsml, sizeof(double), 3);
+    up1(D.itype, itype, sizeof(int32_t), 3);
+    for (int k = 0; k < 2; k++) {  // nodes and stress-points
+      const Seg& q = sg[k];
+      if (q.n == 0) continue;
+      if (intvars1)
+        SPS_CUDA_CHECK(cudaMemcpyAsync(D.iv1 + q.g, intvars1 + q.l, sizeof(double) * q.n, cudaMemcpyHostToDevice, c.stream));
+      else
+        SPS_CUDA_CHECK(cudaMemsetAsync(D.iv1 + q.g, 0, sizeof(double) * q.n, c.stream));
+      if (f_drucker)
+        SPS_CUDA_CHECK(cudaMemcpyAsync(D.fdp + q.g, f_drucker + q.l, sizeof(double) * q.n, cudaMemcpyHostToDevice, c.stream));
+      else
+        SPS_CUDA_CHECK(cudaMemsetAsync(D.fdp + q.g, 0, sizeof(double) * q.n, c.stream));
+    }
+    for (const Seg& q : sg)
+      if (q.n > 0) SPS_CUDA_CHECK(cudaMemsetAsync(D.out + q.g, 0, q.n, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.dispx + M.node0, 0, sizeof(double) * nn, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.dispy + M.node0, 0, sizeof(double) * nn, c.stream));
+    for (const Seg& q : sg)
+      if (q.n > 0) sps::launch_vol(c, (int)q.g, (int)(q.g + q.n));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
-    // cell grid capacity from the uploaded extent (4x margin for spreading)
+    // this realisation's extent, for the cell grid capacity (4x margin for spreading)
+    sps::HostReal& hr = c.hr[r];
     double xmn[2] = {1e300, 1e300}, xmx[2] = {-1e300, -1e300}, hmax = 0, hmin_nd = 1e300;
-    for (size_t i = 0; i < N2; i++) {
+    for (size_t i = 0; i < n2; i++) {
       for (int d = 0; d < 2; d++) {
         xmn[d] = std::min(xmn[d], x[2 * i + d]);
         xmx[d] = std::max(xmx[d], x[2 * i + d]);
       }
       hmax = std::max(hmax, hsml[i]);
-      if (i < (size_t)D.NN || i >= NT) hmin_nd = std::min(hmin_nd, hsml[i]);
+      if (i < nn || i >= nt) hmin_nd = std::min(hmin_nd, hsml[i]);
     }
     double cell = 2.0 * hmax;
-    double nc = 1.0;
-    for (int d = 0; d < 2; d++) nc *= std::floor((xmx[d] - xmn[d]) / cell + 1.0) + 2.0;
+    double ncr = 1.0;
+    for (int d = 0; d < 2; d++) ncr *= std::floor((xmx[d] - xmn[d]) / cell + 1.0) + 2.0;
+    hr.ncells_est = ncr;
+    hr.hmax = hmax;
+    hr.hmin_nd = hmin_nd;
+    hr.uploaded = true;
+    double nc = 0.0;
+    for (const sps::HostReal& q : c.hr) nc += q.ncells_est;
     int cap = (int)std::min(4.0 * nc + 1024.0, 2.0e9 / 4.0);
     if (cap > D.cell_cap) {
       D.cell_cnt = dalloc<int32_t>(c, (size_t)cap + 2);
       D.cell_start = dalloc<int32_t>(c, (size_t)cap + 2);
       D.cell_cursor = dalloc<int32_t>(c, (size_t)cap + 2);
       D.cell_cap = cap;
-      size_t nscan = std::max<size_t>(N2, (size_t)cap + 2);
+      size_t nscan = std::max<size_t>((size_t)D.N2, (size_t)cap + 2);
       D.scan_tmp = dalloc<int64_t>(c, nscan / 4096 + 64);
       if (c.graph) {
         cudaGraphExecDestroy(c.graph);
@@ -462,14 +609,18 @@ int sps_upload(sps_ctx* h, const double* x, const double* vel, const double* str
     // support; 2x headroom plus the wall rows.  max_neighbours (total per particle) raises
     // or lowers the per-list capacity explicitly.
     {
-      double rs = (double)D.scale_k * hmax / c.p.dx;
-      int est = (int)std::ceil(2.0 * M_PI * rs * rs) + 8;
-      int cap = c.p.max_neighbours > 0 ? std::max(4, c.p.max_neighbours / 2) : std::max(48, est);
-      if (cap != D.capH) {
-        D.half = dalloc<int4>(c, N2 * (size_t)cap);
-        D.cross = dalloc<int4>(c, N2 * (size_t)cap);
-        D.same = dalloc<int4>(c, N2 * (size_t)cap);
-        D.capH = D.capC = D.capS = cap;
+      int est = 0;
+      for (int q = 0; q < D.R; q++) {
+        if (!c.hr[q].uploaded) continue;
+        double rs = (double)D.scale_k * c.hr[q].hmax / c.hr[q].p.dx;
+        est = std::max(est, (int)std::ceil(2.0 * M_PI * rs * rs) + 8);
+      }
+      int capn = c.p.max_neighbours > 0 ? std::max(4, c.p.max_neighbours / 2) : std::max(48, est);
+      if (capn > D.capH || (c.p.max_neighbours > 0 && capn != D.capH)) {
+        D.half = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
+        D.cross = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
+        D.same = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
+        D.capH = D.capC = D.capS = capn;
         if (c.graph) {
           cudaGraphExecDestroy(c.graph);
           c.graph = nullptr;
@@ -477,18 +628,28 @@ int sps_upload(sps_ctx* h, const double* x, const double* vel, const double* str
       }
     }
     // node-wall boundary force can use the pair lists when every node-dummy pair closer
-    // than 0.75 dx is inside the kernel support
-    D.bound_from_lists = ((double)D.scale_k * hmin_nd > 0.76 * D.dx) ? 1 : 0;
+    // than 0.75 dx is inside the kernel support (in every realisation)
+    int bfl = 1;
+    for (const sps::HostReal& q : c.hr)
+      if (q.uploaded && !((double)D.scale_k * q.hmin_nd > 0.76 * q.p.dx)) bfl = 0;
+    if (bfl != D.bound_from_lists && c.graph) {
+      cudaGraphExecDestroy(c.graph);
+      c.graph = nullptr;
+    }
+    D.bound_from_lists = bfl;
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
   }
-  c.uploaded = true;
+  bool all = true;
+  for (const sps::HostReal& q : c.hr) all = all && q.uploaded;
+  c.uploaded = all;
   return SPS_OK;
 }
 
 int sps_upload_bcs(sps_ctx* h, const int32_t* bc_or_not, const int32_t* bc_info) {
   if (!h) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
+  if (c.d.R != 1) return fail(&c, SPS_ERR_UNSUPPORTED, "boundary conditions in a batch");
   try {
     const size_t NT = c.d.NT;
     if (bc_or_not)
@@ -515,17 +676,16 @@ int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
   if (!c.uploaded) return fail(&c, SPS_ERR_STATE, "sps_step before sps_upload");
   if (nsteps == 0) return SPS_OK;
   try {
-    double t = *time_sph;
+    const int R = c.d.R;
+    std::vector<double> t(time_sph, time_sph + R);
+    const int chunk_max = std::max(16, std::min(4096, 65536 / R));
     int done = 0;
     while (done < nsteps) {
-      int chunk = std::min(nsteps - done, 4096);
+      int chunk = std::min(nsteps - done, chunk_max);
       ensure_scal(c, chunk);
-      c.h_scal.resize(chunk);
-      for (int k = 0; k < chunk; k++) {
-        fill_scalars(c, t, c.h_scal[k]);
-        t = t + c.p.dt_sph;
-      }
-      SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(), sizeof(sps::StepScalars) * chunk,
+      fill_table(c, chunk, t.data());
+      SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(),
+                                     sizeof(sps::StepScalars) * c.h_scal.size(),
                                      cudaMemcpyHostToDevice, c.stream));
       SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
       if (c.use_graph) {
@@ -545,7 +705,7 @@ int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
     SPS_CUDA_CHECK(cudaMemcpyAsync(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     c.steps_done += nsteps;
-    *time_sph = t;
+    for (int r = 0; r < R; r++) time_sph[r] = t[r];
     int e = *c.h_err;
     if (e) {
       SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
@@ -562,35 +722,56 @@ int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
 int sps_download(sps_ctx* h, double* x, double* vel, double* stress, double* rho,
                  double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker) {
   if (!h) return SPS_ERR_ARG;
+  if (h->c.d.R != 1)
+    return fail(&h->c, SPS_ERR_ARG, "sps_download: a batch takes sps_download_real per realisation");
+  return sps_download_real(h, 0, x, vel, stress, rho, intvars1, displ, bc_or_not, f_drucker);
+}
+
+int sps_download_real(sps_ctx* h, int32_t r, double* x, double* vel, double* stress, double* rho,
+                      double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker) {
+  if (!h) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
   sps::Dev& D = c.d;
-  const size_t N2 = D.N2, NT = D.NT, NN = D.NN;
+  if (r < 0 || r >= D.R) return fail(&c, SPS_ERR_ARG, "sps_download_real: no such realisation");
+  const sps::Real& M = c.real[r];
+  const size_t nn = M.nnode, nt = (size_t)M.nnode + M.nsp, n2 = nt + M.ndum;
+  Seg sg[3];
+  segments(c, r, sg);
   try {
     double* stage = c.stage;
-    int nb = (int)((N2 + kBlock - 1) / kBlock);
-    auto down2 = [&](double* dst, const double* a, const double* b, size_t n) {
-      k_soa_to_aos2<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, c.stream>>>(stage, a, b, (int)n);
+    auto nbk = [](int64_t n) { return (int)((n + kBlock - 1) / kBlock); };
+    auto down2 = [&](double* dst, const double* a, const double* b, int nseg, size_t n) {
+      for (int k = 0; k < nseg; k++)
+        if (sg[k].n > 0)
+          k_soa_to_aos2<<<nbk(sg[k].n), kBlock, 0, c.stream>>>(stage + 2 * sg[k].l, a + sg[k].g,
+                                                                b + sg[k].g, (int)sg[k].n);
       SPS_CUDA_CHECK(cudaMemcpyAsync(dst, stage, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c.stream));
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     };
-    if (x) down2(x, D.px, D.py, N2);
-    if (vel) down2(vel, D.vx, D.vy, N2);
-    if (displ) down2(displ, D.dispx, D.dispy, NN);
+    auto down1 = [&](void* dst, const void* src, size_t esz, int nseg) {
+      for (int k = 0; k < nseg; k++)
+        if (sg[k].n > 0)
+          SPS_CUDA_CHECK(cudaMemcpyAsync((char*)dst + esz * sg[k].l, (const char*)src + esz * sg[k].g,
+                                         esz * sg[k].n, cudaMemcpyDeviceToHost, c.stream));
+    };
+    if (x) down2(x, D.px, D.py, 3, n2);
+    if (vel) down2(vel, D.vx, D.vy, 3, n2);
+    if (displ) down2(displ, D.dispx, D.dispy, 1, nn);
     if (stress) {
-      k_soa_to_aos4<<<nb, kBlock, 0, c.stream>>>(stage, D.s0, D.s1, D.s2, D.s3, (int)N2);
-      SPS_CUDA_CHECK(cudaMemcpyAsync(stress, stage, sizeof(double) * 4 * N2, cudaMemcpyDeviceToHost, c.stream));
+      for (const Seg& q : sg)
+        if (q.n > 0)
+          k_soa_to_aos4<<<nbk(q.n), kBlock, 0, c.stream>>>(stage + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
+                                                            D.s2 + q.g, D.s3 + q.g, (int)q.n);
+      SPS_CUDA_CHECK(cudaMemcpyAsync(stress, stage, sizeof(double) * 4 * n2, cudaMemcpyDeviceToHost, c.stream));
     }
-    if (rho) SPS_CUDA_CHECK(cudaMemcpyAsync(rho, D.rho, sizeof(double) * N2, cudaMemcpyDeviceToHost, c.stream));
-    if (intvars1)
-      SPS_CUDA_CHECK(cudaMemcpyAsync(intvars1, D.iv1, sizeof(double) * NT, cudaMemcpyDeviceToHost, c.stream));
-    if (bc_or_not)
-      SPS_CUDA_CHECK(cudaMemcpyAsync(bc_or_not, D.bc_or_not, sizeof(int32_t) * NT, cudaMemcpyDeviceToHost, c.stream));
-    if (f_drucker)
-      SPS_CUDA_CHECK(cudaMemcpyAsync(f_drucker, D.fdp, sizeof(double) * NT, cudaMemcpyDeviceToHost, c.stream));
+    if (rho) down1(rho, D.rho, sizeof(double), 3);
+    if (intvars1) down1(intvars1, D.iv1, sizeof(double), 2);
+    if (bc_or_not) down1(bc_or_not, D.bc_or_not, sizeof(int32_t), 2);
+    if (f_drucker) down1(f_drucker, D.fdp, sizeof(double), 2);
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     if (stress) {
       // dummy stress is pair-local in the reference; report zero like its RK4 clear (:690)
-      for (size_t i = NT; i < N2; i++)
+      for (size_t i = nt; i < n2; i++)
         for (int k = 0; k < 4; k++) stress[4 * i + k] = 0.0;
     }
   } catch (const std::exception& e) {
@@ -601,31 +782,58 @@ int sps_download(sps_ctx* h, double* x, double* vel, double* stress, double* rho
 
 int sps_dump_pairs(sps_ctx* h, int32_t* pair_i, int32_t* pair_j, int32_t* pint_type, float* w,
                    float* dwdx, float* dwdy, int64_t* npairs) {
+  if (!h) return SPS_ERR_ARG;
+  if (h->c.d.R != 1)
+    return fail(&h->c, SPS_ERR_ARG, "sps_dump_pairs: a batch takes sps_dump_pairs_real");
+  return sps_dump_pairs_real(h, 0, pair_i, pair_j, pint_type, w, dwdx, dwdy, npairs);
+}
+
+int sps_dump_pairs_real(sps_ctx* h, int32_t r, int32_t* pair_i, int32_t* pair_j,
+                        int32_t* pint_type, float* w, float* dwdx, float* dwdy, int64_t* npairs) {
   if (!h || !npairs) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
   sps::Dev& D = c.d;
+  if (r < 0 || r >= D.R) return fail(&c, SPS_ERR_ARG, "sps_dump_pairs_real: no such realisation");
   try {
     sps::PairMeta meta;
-    SPS_CUDA_CHECK(cudaMemcpy(&meta, D.meta, sizeof(meta), cudaMemcpyDeviceToHost));
+    sps::Grid g;
+    sps::GridTotal gt;
+    SPS_CUDA_CHECK(cudaMemcpy(&meta, D.meta + r, sizeof(meta), cudaMemcpyDeviceToHost));
     if (!pair_i) {
       *npairs = meta.n;
       return SPS_OK;
     }
     if (*npairs < meta.n) return fail(&c, SPS_ERR_CAPACITY, "sps_dump_pairs: buffer too small");
-    const size_t N2 = D.N2;
+    SPS_CUDA_CHECK(cudaMemcpy(&g, D.grid + r, sizeof(g), cudaMemcpyDeviceToHost));
+    SPS_CUDA_CHECK(cudaMemcpy(&gt, D.gtot, sizeof(gt), cudaMemcpyDeviceToHost));
+    int32_t lohi[2] = {0, 0};
+    if (!gt.overflow) {
+      SPS_CUDA_CHECK(cudaMemcpy(&lohi[0], D.cell_start + g.cell0, sizeof(int32_t), cudaMemcpyDeviceToHost));
+      SPS_CUDA_CHECK(cudaMemcpy(&lohi[1], D.cell_start + g.cell0 + g.ncells, sizeof(int32_t),
+                                cudaMemcpyDeviceToHost));
+    }
+    const size_t N2 = D.N2, lo = lohi[0], hi = lohi[1];
     std::vector<int32_t> cnt(N2), sorted(N2), itype(N2);
-    std::vector<int4> half(N2 * D.capH);
+    std::vector<int4> half((hi - lo) * D.capH + 1);
     SPS_CUDA_CHECK(cudaMemcpy(cnt.data(), D.half_cnt, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost));
     SPS_CUDA_CHECK(cudaMemcpy(sorted.data(), D.sorted, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost));
     SPS_CUDA_CHECK(cudaMemcpy(itype.data(), D.itype, sizeof(int32_t) * N2, cudaMemcpyDeviceToHost));
-    SPS_CUDA_CHECK(cudaMemcpy(half.data(), D.half, sizeof(int4) * N2 * D.capH, cudaMemcpyDeviceToHost));
+    if (hi > lo)
+      SPS_CUDA_CHECK(cudaMemcpy(half.data(), D.half + lo * D.capH, sizeof(int4) * (hi - lo) * D.capH,
+                                cudaMemcpyDeviceToHost));
+    const sps::Real& M = c.real[r];
+    auto local = [&](int gid) -> int32_t {  // global id -> 1-based reference id of r
+      if (gid < D.NN) return gid - M.node0 + 1;
+      if (gid < D.NT) return M.nnode + (gid - M.sp0) + 1;
+      return M.nnode + M.nsp + (gid - M.dum0) + 1;
+    };
     // creation order
     std::vector<int32_t> ci, cj, ct;
     std::vector<float> cw, cx, cy;
     ci.reserve(meta.n);
-    for (size_t s = 0; s < N2; s++)
+    for (size_t s = lo; s < hi; s++)
       for (int k = 0; k < cnt[s]; k++) {
-        const int4 e = half[s * D.capH + k];
+        const int4 e = half[(s - lo) * D.capH + k];
         int a = sorted[s], b = sorted[e.x];
         float ww, gx, gy;
         std::memcpy(&ww, &e.y, 4);
@@ -641,8 +849,8 @@ int sps_dump_pairs(sps_ctx* h, int32_t* pair_i, int32_t* pair_j, int32_t* pint_t
         }
         int sum = ta + tb;
         int t = sum == 3 ? 1 : sum == 2 ? 2 : sum == 4 ? 3 : sum == 27 ? 6 : sum == 26 ? 9 : 0;
-        ci.push_back(a + 1);
-        cj.push_back(b + 1);
+        ci.push_back(local(a));
+        cj.push_back(local(b));
         ct.push_back(t);
         cw.push_back(ww);
         cx.push_back(gx);
@@ -713,14 +921,11 @@ int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, 
   std::vector<double> kms;
   std::vector<int> kl;
   try {
-    double t = *time_sph;
+    std::vector<double> t(time_sph, time_sph + c.d.R);
     ensure_scal(c, nsteps);
-    c.h_scal.resize(nsteps);
-    for (int k = 0; k < nsteps; k++) {
-      fill_scalars(c, t, c.h_scal[k]);
-      t = t + c.p.dt_sph;
-    }
-    SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(), sizeof(sps::StepScalars) * nsteps,
+    fill_table(c, nsteps, t.data());
+    SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(),
+                                   sizeof(sps::StepScalars) * c.h_scal.size(),
                                    cudaMemcpyHostToDevice, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
     c.profiling = true;
@@ -750,7 +955,7 @@ int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, 
     for (auto& pe : c.prof_events) cudaEventDestroy(pe.second);
     c.prof_events.clear();
     SPS_CUDA_CHECK(cudaMemcpy(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost));
-    *time_sph = t;
+    for (int r = 0; r < c.d.R; r++) time_sph[r] = t[r];
     c.steps_done += nsteps;
   } catch (const std::exception& e) {
     c.profiling = false;

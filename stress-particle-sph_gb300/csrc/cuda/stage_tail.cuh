@@ -36,7 +36,8 @@ __device__ __forceinline__ void apply_bcs(const Dev& D, const StepScalars& sc, i
 __device__ __forceinline__ void capture_tuple(const Dev& D, int t, const double* s2v,
                                               const double* g, const double* Gs) {
   float x[16];
-  double scale = mlp_features(s2v, g, D.tanfi, D.coh, D.young, D.poiss, D.rho[t], x);
+  const Real& M = real_of(D, t);
+  double scale = mlp_features(s2v, g, M.tanfi, M.coh, M.young, M.poiss, D.rho[t], x);
   if (!(scale > 0.0)) return;
   unsigned long long k = atomicAdd(D.cap_cnt, 1ull);
   if ((long long)k >= D.cap_max) return;
@@ -82,22 +83,23 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
                                               const double* g, double f2,
                                               const double* Gs_net = nullptr,
                                               double der_net = 0.0) {
+    const Real& M = real_of(D, t);
     const double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
     double div1[4];
-    div1[0] = -(D.D11 * g11 + D.D12 * g22);
-    div1[1] = -(D.D12 * g11 + D.D22 * g22);
-    div1[2] = -(D.D33 * g21 + D.D33 * g12);
-    div1[3] = -(D.D41 * g11 + D.D42 * g22);
+    div1[0] = -(M.D11 * g11 + M.D12 * g22);
+    div1[1] = -(M.D12 * g11 + M.D22 * g22);
+    div1[2] = -(M.D33 * g21 + M.D33 * g12);
+    div1[3] = -(M.D41 * g11 + M.D42 * g22);
     // plastic_terms (3_SPH_material_2018.f90:1884-1954)
     double st[4] = {D.s0[t], D.s1[t], D.s2[t], D.s3[t]};
     double Gs[4] = {0.0, 0.0, 0.0, 0.0}, der = 0.0;
-    if (D.ntype_eco > 1) {
+    if (M.ntype_eco > 1) {
       double s2v[4] = {st[0], st[1], st[2], st[3]};
-      if (D.ntype_solid == 1) s2v[3] = D.poiss * (s2v[0] + s2v[1]);
+      if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
       double vivel[4] = {0.0, 0.0, 0.0, 0.0}, G2[4];
-      if (D.ncrit == 12) {
+      if (M.ncrit == 12) {
         double f = D.fdp[t];
-        drucker_prager<FAST>(D, sc.time_sph, s2v, g, &f, G2, vivel);
+        drucker_prager<FAST>(M, sc.time_sph, s2v, g, &f, G2, vivel);
         D.fdp[t] = f;
         for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
         if (D.cap_buf && (G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0))
@@ -168,13 +170,14 @@ __device__ __forceinline__ void tail_node(const Dev& D, const StepScalars& sc, i
       g2[d + 3] = A4 * (A2 * g2[d] + A3 * g2[d + 3]);
     }
   }
+  const Real& M = real_of(D, t);
   double div2x = -(g2[0] + g2[2 + 3]);
   double div2y = -(g2[2] + g2[1 + 3]);
   const double vtx = D.vx[t], vty = D.vy[t];
-  double gx = (D.ic_grav == 1) ? sc.factg * D.cgrav[0] : 0.0;
-  double gy = (D.ic_grav == 1) ? sc.factg * D.cgrav[1] : 0.0;
-  gx = gx - D.damping * vtx;
-  gy = gy - D.damping * vty;
+  double gx = (M.ic_grav == 1) ? sc.factg * M.cgrav[0] : 0.0;
+  double gy = (M.ic_grav == 1) ? sc.factg * M.cgrav[1] : 0.0;
+  gx = gx - M.damping * vtx;
+  gy = gy - M.damping * vty;
   double rhsx = (((-div2x + gx) + avx) + D.fbx[t]) + 0.0;
   double rhsy = (((-div2y + gy) + avy) + D.fby[t]) + 0.0;
   D.RHS2[0][t] = rhsx;

@@ -29,6 +29,15 @@ def gpu_lib():
         lib.sps_profile_step.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                          C.c_char_p, C.c_int32, C.POINTER(C.c_double),
                                          C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]
+        P = C.POINTER
+        lib.sps_create_batch.argtypes = [C.c_int32, P(_abi.SpsParams), P(C.c_void_p)]
+        lib.sps_upload_real.argtypes = [C.c_void_p, C.c_int32] + [P(C.c_double)] * 6 + \
+            [P(C.c_int32)] + [P(C.c_double)] * 3
+        lib.sps_download_real.argtypes = [C.c_void_p, C.c_int32] + [P(C.c_double)] * 6 + \
+            [P(C.c_int32), P(C.c_double)]
+        lib.sps_dump_pairs_real.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32),
+                                            P(C.c_int32), P(C.c_float), P(C.c_float),
+                                            P(C.c_float), P(C.c_int64)]
         _GPU = lib
     return _GPU
 
@@ -174,6 +183,66 @@ def profile_steps(ctx, nsteps, time_sph):
     for k in range(nk.value):
         out[raw[k].decode()] = (ms[k], nl[k])
     return t.value, out
+
+
+class Batch(StepContext):
+    """A batch context (sps_create_batch): several problems advanced by the same launches,
+    each bit-identical to a context holding it alone."""
+
+    def __init__(self, problems, precision=_abi.SPS_PREC_FP64_PLAIN):
+        self._lib = gpu_lib()
+        self._pre = "sps"
+        self._h = C.c_void_p()
+        self.problems = list(problems)
+        R = len(self.problems)
+        self.params = (_abi.SpsParams * R)(*[p.params_copy(precision=precision)
+                                             for p in self.problems])
+        rc = self._lib.sps_create_batch(R, self.params, C.byref(self._h))
+        if rc != _abi.SPS_OK:
+            raise SpsError("sps_create_batch", rc, self._err())
+        self.times = [0.0] * R
+
+    def upload_all(self):
+        for r, prob in enumerate(self.problems):
+            st = prob.state()
+            arrs = [np.ascontiguousarray(st[k], dtype=np.float64)
+                    for k in ("x", "vel", "stress", "mass", "rho", "hsml")]
+            it = np.ascontiguousarray(st["itype"], dtype=np.int32)
+            rest = [np.ascontiguousarray(st[k], dtype=np.float64)
+                    for k in ("intvars1", "f_drucker", "x00")]
+            self._call("upload_real", self._h, r, *[_dp(a) for a in arrs], _ip(it),
+                       *[_dp(a) for a in rest])
+
+    def step(self, nsteps, times=None):
+        R = len(self.problems)
+        t = (C.c_double * R)(*(self.times if times is None else times))
+        self._call("step", self._h, int(nsteps), t)
+        self.times = list(t)
+        return self.times
+
+    def download(self, r):
+        prob = self.problems[r]
+        n2, nt, nn = prob.ntotal2, prob.ntotal, prob.nnode
+        out = dict(x=np.empty(2 * n2), vel=np.empty(2 * n2), stress=np.empty(4 * n2),
+                   rho=np.empty(n2), intvars1=np.empty(nt), displ=np.empty(2 * nn),
+                   bc_or_not=np.empty(nt, np.int32), f_drucker=np.empty(nt))
+        self._call("download_real", self._h, r, _dp(out["x"]), _dp(out["vel"]),
+                   _dp(out["stress"]), _dp(out["rho"]), _dp(out["intvars1"]),
+                   _dp(out["displ"]), _ip(out["bc_or_not"]), _dp(out["f_drucker"]))
+        return out
+
+    def dump_pairs(self, r):
+        n = C.c_int64(0)
+        N = None
+        self._call("dump_pairs_real", self._h, r, N, N, N, N, N, N, C.byref(n))
+        k = n.value
+        out = dict(pair_i=np.empty(k, np.int32), pair_j=np.empty(k, np.int32),
+                   pint_type=np.empty(k, np.int32), w=np.empty(k, np.float32),
+                   dwdx=np.empty(k, np.float32), dwdy=np.empty(k, np.float32))
+        self._call("dump_pairs_real", self._h, r, _ip(out["pair_i"]), _ip(out["pair_j"]),
+                   _ip(out["pint_type"]), _fp(out["w"]), _fp(out["dwdx"]), _fp(out["dwdy"]),
+                   C.byref(n))
+        return out
 
 
 class Solver(StepContext):
