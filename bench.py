@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-size", type=int, default=256)
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
     return ap.parse_args()
 
@@ -204,6 +206,63 @@ def train_surrogate(seed=0, nruns=6, dx=0.08, nsteps=2000, every=20, max_tuples=
     return net, sg.Envelope.of(train), summary
 
 
+def batch_problems(n=256, seed=0):
+    """Seeded 2D slopes: height U[2,10] m, face angle U[30,70] deg, U[2k,60k] velocity
+    particles each (spacing from the area), phi U[20,40] deg, c U[0,20] kPa, E U[10,50] MPa,
+    nu 0.3, rho U[1800,2000]; foundation half the height deep, crest half the height wide."""
+    import numpy as np
+    import sps_gb300
+    rng = np.random.default_rng(seed)
+    out, desc = [], []
+    for _ in range(n):
+        H, face, nt = rng.uniform(2, 10), rng.uniform(30, 70), rng.uniform(2000, 60000)
+        phi, coh, E, rho = (rng.uniform(20, 40), rng.uniform(0, 20e3), rng.uniform(10e6, 50e6),
+                            rng.uniform(1800, 2000))
+        run = H / np.tan(np.radians(face))
+        Hf, Ls = 0.5 * H, 0.5 * H
+        Lf = Ls + run + H
+        area = Lf * Hf + Ls * H + 0.5 * H * run
+        dx = float(np.sqrt(area / nt))
+        out.append(sps_gb300.Problem.slope(Lf=Lf, Hf=Hf, Ls=Ls, Hs=H, dx=dx, young=E, poiss=0.3,
+                                           rho=rho, phi_deg=phi, cohesion=coh, k0=0.5,
+                                           t_ramp=0.05, face_deg=face))
+    return out
+
+
+def run_batch(args, dist, local):
+    """The batched-realisations workload: one FP32 context holding every slope."""
+    import numpy as np
+    import sps_gb300
+    from sps_gb300 import _abi
+    w0 = time.perf_counter()
+    probs = batch_problems(args.batch_size)
+    b = sps_gb300.Batch(probs, precision=_abi.SPS_PREC_FP32_FAST)
+    b.upload_all()
+    w1 = time.perf_counter()
+    b.step(max(args.warmup, 1))
+    _, ms, clk = timed_steps(b, args.steps, None, dist, local)
+    n = sum(p.nnode + p.nstress for p in probs)
+    nv = sum(p.nnode for p in probs)
+    # two realisations against contexts holding them alone (bit-identical fields)
+    same = {}
+    done = max(args.warmup, 1) + args.steps
+    for r in (0, len(probs) // 2):
+        ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                    probs[r].params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+        ctx.upload_problem(probs[r])
+        ctx.step(done, 0.0)
+        a, bb = ctx.download(), b.download(r)
+        same[str(r)] = bool(all(np.array_equal(a[k], bb[k]) for k in ("x", "vel", "stress")))
+        ctx.close()
+    b.close()
+    return {"realisations": len(probs), "particles": int(n), "velocity_particles": int(nv),
+            "value": round(n * args.steps / (ms * 1e-3), 1), "unit": "particle-steps/s",
+            "ms_per_step": round(ms / args.steps, 4), "steps": args.steps,
+            "setup_s": round(w1 - w0, 2), "precision": "fp32 form",
+            "bit_identical_to_single_runs": same, "clocks": clk,
+            "workload": batch_problems.__doc__.split("\n")[0]}
+
+
 def workload(dx):
     import sps_gb300
     return sps_gb300.Problem.slope(dx=dx, **SLOPE)
@@ -242,7 +301,8 @@ def kernel_bytes(name, prob, deg, fast=False):
 
 def timed_steps(ctx, nsteps, t, dist, local):
     """Device time (ms, max over ranks) of nsteps graph-launched steps on the context's
-    own stream; clocks sampled meanwhile."""
+    own stream; clocks sampled meanwhile.  t: the start time (None for a batch, which keeps
+    its own times)."""
     import torch
     import sps_gb300
     stream = torch.cuda.ExternalStream(sps_gb300.stream_of(ctx))
@@ -252,7 +312,7 @@ def timed_steps(ctx, nsteps, t, dist, local):
     torch.cuda.synchronize()
     clocks.start()
     e0.record(stream)
-    t = ctx.step(nsteps, t)
+    t = ctx.step(nsteps) if t is None else ctx.step(nsteps, t)
     e1.record(stream)
     e1.synchronize()
     clk = clocks.stop()
@@ -405,6 +465,10 @@ def run_ours(args):
            "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
            "path": "sps_upload (pinned host) + sps_step(1) + sps_download, every step"}
 
+    batch = None
+    if fast and not args.no_batch:
+        batch = run_batch(args, dist, local)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args)
@@ -425,7 +489,7 @@ def run_ours(args):
                        "surrogate": ("learned Drucker-Prager flow rule, exact fallback "
                                      "(tol %g)" % args.surrogate_tol if use_surr else "off"),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "plain": plain, "error_vs_plain": errors, "surrogate": surr,
+            "plain": plain, "error_vs_plain": errors, "surrogate": surr, "batch": batch,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
             "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
             "kernel_ms_per_step": {k: round(v[0] / 2, 4) for k, v in sorted(

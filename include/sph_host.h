@@ -74,6 +74,9 @@ typedef struct sph_slope_spec {
   double dt; /* 0 -> 0.1 h / sqrt(E/rho) */
   double alpha, beta, damping;
   int32_t xsph;
+  double face_deg; /* angle of the slope face from the horizontal; 0 or 90: vertical face
+                      at x = Ls, else the face runs from the crest (Ls, Hf + Hs) down to
+                      the toe (Ls + Hs / tan(face), Hf), which must lie on the foundation */
 } sph_slope_spec;
 int sph_problem_slope(const sph_slope_spec* spec, sph_problem** out);
 

@@ -105,9 +105,11 @@ struct Dev {
   int bound_from_lists;
   double pi;
   int bcvar[kMaxBC];
-  // per-realisation constants and the realisation of every particle
+  // per-realisation constants and the realisation of every particle; a single problem
+  // (R = 1) also carries its entry here, in the kernel parameters (constant bank)
   const Real* real;
   const uint16_t* rid;
+  Real real0;
   // particle state (id order)
   double *px, *py, *vx, *vy, *s0, *s1, *s2, *s3;
   double *mass, *rho, *hsml, *iv1, *fdp, *x00x, *x00y, *dispx, *dispy;
@@ -393,7 +395,9 @@ __device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, c
   }
 }
 
-__device__ __forceinline__ const Real& real_of(const Dev& D, int i) { return D.real[D.rid[i]]; }
+__device__ __forceinline__ const Real& real_of(const Dev& D, int i) {
+  return D.R == 1 ? D.real0 : D.real[D.rid[i]];
+}
 // the node at the same place as a stress-point (and back), when every node has one
 __device__ __forceinline__ int node_of_sp(const Real& M, int t) { return M.node0 + (t - M.sp0); }
 __device__ __forceinline__ int sp_of_node(const Real& M, int n) { return M.sp0 + (n - M.node0); }

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
   const Real& Mt = real_of(D, t);
-  const StepScalars& sc = D.cur[D.rid[t]];
+  const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   int tt = D.itype[t];
   int deg = D.degC[s];
   const double xt = D.px[t], yt = D.py[t];
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
   const Real& M = real_of(D, t);
-  const StepScalars& sc = D.cur[D.rid[t]];
+  const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   double g[4] = {0.0, 0.0, 0.0, 0.0}, s2v[4] = {0.0, 0.0, 0.0, 0.0};
   float x[16];
   double scale = 0.0;

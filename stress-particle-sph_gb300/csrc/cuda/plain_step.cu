@@ -178,8 +178,8 @@ __global__ void k_stage_begin(Dev D, int stage) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
   const double f1rk[4] = {0.0, 0.5, 0.5, 1.0};
-  const int r = D.rid[i];
-  const Real& M = D.real[r];
+  const int r = D.R == 1 ? 0 : D.rid[i];
+  const Real& M = real_of(D, i);
   const double f1dt = f1rk[stage] * M.dt;
   const StepScalars& sc = D.cur[r];
   double vx = D.vx[i], vy = D.vy[i];
@@ -305,8 +305,8 @@ __global__ void k_node_rho(Dev D) {
 __global__ void k_adapt_bc(Dev D, int with_A) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
-  const int r = D.rid[i];
-  const Real& M = D.real[r];
+  const int r = D.R == 1 ? 0 : D.rid[i];
+  const Real& M = real_of(D, i);
   const StepScalars& sc = D.cur[r];
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
@@ -370,7 +370,7 @@ __global__ void k_derivs(Dev D, int stage) {
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
   const Real& Mt = real_of(D, t);
-  const StepScalars& sc = D.cur[D.rid[t]];
+  const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   int tt = D.itype[t];
   int deg = D.degC[s];
   double AE[4] = {0.0, 0.0, 0.0, 0.0};
@@ -498,8 +498,8 @@ __global__ void k_derivs(Dev D, int stage) {
 __global__ void k_rk_final(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
-  const int r = D.rid[i];
-  const Real& M = D.real[r];
+  const int r = D.R == 1 ? 0 : D.rid[i];
+  const Real& M = real_of(D, i);
   const StepScalars& sc = D.cur[r];
   const double dt6 = M.dt / 6.0;
   double vx = D.vx[i], vy = D.vy[i];

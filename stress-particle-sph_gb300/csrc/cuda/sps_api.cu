@@ -358,6 +358,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
       SPS_CUDA_CHECK(cudaMemcpyAsync(rd, c.real.data(), sizeof(sps::Real) * nreal,
                                      cudaMemcpyHostToDevice, c.stream));
       D.real = rd;
+      D.real0 = c.real[0];
       std::vector<uint16_t> rid(N2);
       for (int r = 0; r < nreal; r++) {
         const sps::Real& M = c.real[r];

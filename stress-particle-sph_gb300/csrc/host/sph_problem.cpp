@@ -785,10 +785,14 @@ int sph_problem_slope(const sph_slope_spec* s, sph_problem** out) {
   const int nfx = (int)std::lround(s->Lf / dx), nfy = (int)std::lround(s->Hf / dx);
   const int nsx = (int)std::lround(s->Ls / dx), nsy = (int)std::lround(s->Hs / dx);
   const int ny_tot = nfy + nsy;
+  // inclined face: horizontal run per unit height (0 for a vertical face)
+  const double cot = (s->face_deg > 0.0 && s->face_deg < 90.0)
+                         ? 1.0 / std::tan(s->face_deg * M_PI / 180.0) : 0.0;
+  if ((double)nsx + (double)nsy * cot > (double)nfx) return SPS_ERR_ARG;  // toe off the foundation
   auto node_in = [&](int i, int j) {
     if (i < 0 || j < 0 || i > nfx || j > ny_tot) return false;
     if (j <= nfy) return true;
-    return i <= nsx;
+    return (double)i <= (double)nsx + (double)(ny_tot - j) * cot + 1e-9;
   };
   auto cell_in = [&](int i, int j) {  // cell with lower-left node (i,j)
     return node_in(i, j) && node_in(i + 1, j) && node_in(i, j + 1) && node_in(i + 1, j + 1);
@@ -905,7 +909,9 @@ int sph_problem_slope(const sph_slope_spec* s, sph_problem** out) {
   const double g = 9.81;
   for (int ip = 0; ip < ntotal; ip++) {
     double xx = Q.x[2 * (size_t)ip], yy = Q.x[2 * (size_t)ip + 1];
-    double top = (xx <= s->Ls + 1e-12) ? s->Hf + s->Hs : s->Hf;
+    double top = s->Hf;
+    if (xx <= s->Ls + 1e-12) top = s->Hf + s->Hs;
+    else if (cot > 0.0 && xx < s->Ls + s->Hs * cot) top = s->Hf + s->Hs - (xx - s->Ls) / cot;
     double depth = top - yy;
     if (depth < 0) depth = 0;
     double syy = -s->rho * g * depth;

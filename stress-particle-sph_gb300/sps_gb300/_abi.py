@@ -156,6 +156,7 @@ class SphSlopeSpec(C.Structure):
         ("beta", c_double),
         ("damping", c_double),
         ("xsph", c_int32),
+        ("face_deg", c_double),
     ]
 
 

@@ -123,10 +123,11 @@ class Problem:
     @classmethod
     def slope(cls, Lf=20.0, Hf=5.0, Ls=4.4, Hs=10.0, dx=0.012, sml=1.2, young=20e6, poiss=0.3,
               rho=1850.0, phi_deg=30.0, cohesion=10e3, k0=0.5, t_ramp=0.05, dt=0.0, alpha=0.0,
-              beta=0.0, damping=0.0, xsph=False):
-        """Vertical slope (block Ls x Hs) on a foundation (Lf x Hf), gravity ramped in."""
+              beta=0.0, damping=0.0, xsph=False, face_deg=90.0):
+        """Slope (crest block Ls x Hs, face at face_deg from the horizontal, 90 = vertical) on
+        a foundation (Lf x Hf), gravity ramped in."""
         spec = _abi.SphSlopeSpec(Lf, Hf, Ls, Hs, dx, sml, young, poiss, rho, phi_deg, cohesion,
-                                 k0, t_ramp, dt, alpha, beta, damping, int(xsph))
+                                 k0, t_ramp, dt, alpha, beta, damping, int(xsph), face_deg)
         h = C.c_void_p()
         rc = host_lib().sph_problem_slope(C.byref(spec), C.byref(h))
         if rc:
