@@ -153,6 +153,13 @@ int sps_get_stream(sps_ctx* ctx, void** stream);
    differ in any bit. */
 int sps_selftest_division(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* Self-test (no reference counterpart): compare, on the device, the FP64 <-> FP32
+   conversions the FP32 form does on the integer pipe (round-to-nearest double -> float,
+   the hi/lo split of a double into two floats, float -> double) with the hardware
+   conversions, on n pseudo-random values; *mismatches counts results that differ in any
+   bit. */
+int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
+
 /* Number of this library's kernels one step launches (no reference counterpart). */
 int sps_kernels_per_step(sps_ctx* ctx, int32_t* n);
 

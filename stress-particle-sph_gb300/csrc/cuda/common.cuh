@@ -189,6 +189,54 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
   return fma(r, y, q);
 }
 
+// ---- FP64 <-> FP32 conversions on the integer pipe --------------------------------------
+// GB300 issues double/float conversions on its FP64 pipe (2 per SM per clock); the FP32
+// form converts every record it writes, so these do the same roundings with 32-bit integer
+// operations on the bit patterns.  Values outside the range handled (zero, float
+// subnormals, overflow, Inf/NaN) take the hardware conversion.
+
+// RN-even double -> float, identical to (float)x
+__device__ __forceinline__ float f32_rn(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
+  const int E = (int)((h32 >> 20) & 0x7FFu);
+  if (E < 897 || E > 1150) return (float)x;
+  const unsigned f23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
+  const unsigned rem = l32 & 0x1FFFFFFFu;
+  const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (f23 & 1u));
+  return __uint_as_float(((h32 & 0x80000000u) | ((unsigned)(E - 896) << 23) | f23) + up);
+}
+
+// hi = (float)x, lo = (float)(x - (double)hi): the exact remainder x - hi is the dropped
+// significand bits (minus one float ulp when hi was rounded up), scaled by 2^(E-1075)
+__device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
+  const int E = (int)((h32 >> 20) & 0x7FFu);
+  if (E < 949 || E > 1150) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+    return;
+  }
+  const unsigned f23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
+  const unsigned rem = l32 & 0x1FFFFFFFu;
+  const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (f23 & 1u));
+  hi = __uint_as_float(((h32 & 0x80000000u) | ((unsigned)(E - 896) << 23) | f23) + up);
+  int r = (int)rem - (up ? 0x20000000 : 0);
+  if (h32 & 0x80000000u) r = -r;
+  lo = __int2float_rn(r) * __uint_as_float((unsigned)(E - 948) << 23);
+}
+
+// exact float -> double, identical to (double)f
+__device__ __forceinline__ double f64_of(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  if (e == 0u || e == 255u) return (double)f;
+  const unsigned h32 = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+  const unsigned l32 = b << 29;
+  return __longlong_as_double((long long)(((unsigned long long)h32 << 32) | l32));
+}
+
 // ----------------------------------------------------------------------------------------
 // kernel (example_problems/soil_failure_bui_et_al_2008/2_SPH_main_2018.f90:1440-1538).
 // FP64 with the FP32 literal 2./3. (:1480); x**n expanded into multiplications.
@@ -348,28 +396,30 @@ __device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, c
                                                const double* gu, double* fdp, double* G,
                                                double* vivel) {
   double f0 = *fdp;
-  float tanfi = (float)M.tanfi, coh = (float)M.coh, young = (float)M.young,
-        poiss = (float)M.poiss;
+  auto tof = [](double v) { return (float)v; };
+  auto tod = [](float v) { return (double)v; };
+  float tanfi = tof(M.tanfi), coh = tof(M.coh), young = tof(M.young), poiss = tof(M.poiss);
   float smean = FAST ? (float)(((s[0] + s[1]) + s[3]) * (1.0 / 3.0))
                      : (float)(((s[0] + s[1]) + s[3]) / 3.0);
-  float dv0 = (float)(s[0] - (double)smean);
-  float dv1 = (float)(s[1] - (double)smean);
-  float dv2 = (float)s[2];
-  float dv3 = (float)(s[3] - (double)smean);
+  const double smd = tod(smean);
+  float dv0 = tof(s[0] - smd);
+  float dv1 = tof(s[1] - smd);
+  float dv2 = tof(s[2]);
+  float dv3 = tof(s[3] - smd);
   float varj2 = dv2 * dv2 + 0.5f * ((dv0 * dv0 + dv1 * dv1) + dv3 * dv3);
   float vari1 = 3.0f * smean;
-  float eps11 = (float)gu[0];
-  float eps12 = (float)(0.5 * (gu[2] + gu[1]));
-  float eps22 = (float)gu[3];
+  float eps11 = tof(gu[0]);
+  float eps12 = tof(0.5 * (gu[2] + gu[1]));
+  float eps22 = tof(gu[3]);
   float emean = eps11 + eps22;
   float den = sqrtf(9.0f + 12.0f * (tanfi * tanfi));
   float alpha2 = tanfi / den;
   float kc = (3.0f * coh) / den;
   float yield = -(alpha2 * vari1) + kc;
   float sj = sqrtf(varj2);
-  *fdp = (double)(sj - yield);
-  float f1 = (float)(*fdp);
-  double df = (double)f1 - f0;
+  *fdp = tod(sj - yield);
+  float f1 = sj - yield;  // (float)(double)x == x
+  double df = tod(f1) - f0;
   float G_mod = young / (2.0f * (1.0f + poiss));
   float K_mod = young / (3.0f * (1.0f - 2.0f * poiss));
   float s_eps = (dv0 * eps11 + (2.0f * dv2) * eps12) + dv1 * eps22;
@@ -378,17 +428,17 @@ __device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, c
     float lambda_1 = ((3.0f * alpha2) * K_mod) * emean;
     float lambda_2 = gs * s_eps;
     float G2 = (lambda_1 + lambda_2) / G_mod;
-    G[0] = (double)((gs * dv0) * G2);
-    G[1] = (double)((gs * dv1) * G2);
-    G[2] = (double)((gs * dv2) * G2);
-    G[3] = (double)((gs * dv3) * G2);
+    G[0] = tod((gs * dv0) * G2);
+    G[1] = tod((gs * dv1) * G2);
+    G[2] = tod((gs * dv2) * G2);
+    G[3] = tod((gs * dv3) * G2);
     const float sixth = 1.0f / 6.0f;
     float rs = 1.0f / sj;
-    double g2 = (double)G2;
-    vivel[0] = (double)((sixth * rs) * ((2.0f * dv0 - dv1) - dv3)) * g2;
-    vivel[1] = (double)((sixth * rs) * ((2.0f * dv1 - dv0) - dv3)) * g2;
-    vivel[2] = (double)(rs * dv2) * g2;
-    vivel[3] = (double)((sixth * rs) * ((2.0f * dv3 - dv0) - dv1)) * g2;
+    double g2 = tod(G2);
+    vivel[0] = tod((sixth * rs) * ((2.0f * dv0 - dv1) - dv3)) * g2;
+    vivel[1] = tod((sixth * rs) * ((2.0f * dv1 - dv0) - dv3)) * g2;
+    vivel[2] = tod(rs * dv2) * g2;
+    vivel[3] = tod((sixth * rs) * ((2.0f * dv3 - dv0) - dv1)) * g2;
   } else {
     G[0] = G[1] = G[2] = G[3] = 0.0;
     vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0;
@@ -426,4 +476,5 @@ void launch_fderivs(Ctx& c, int stage);
 void launch_fsp_tail(Ctx& c, int stage);
 void launch_fxsph(Ctx& c);
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
+void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 }  // namespace sps

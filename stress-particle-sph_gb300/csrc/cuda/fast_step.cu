@@ -414,8 +414,9 @@ __global__ void k_fxsph(Dev D) {
   if (t >= D.NT) return;
   int deg = D.degS[s];
   const double vt0 = D.vx[t], vt1 = D.vy[t];
-  const float vh0 = (float)vt0, vh1 = (float)vt1;
-  const float vl0 = (float)(vt0 - (double)vh0), vl1 = (float)(vt1 - (double)vh1);
+  float vh0, vh1, vl0, vl1;
+  f32_split(vt0, vh0, vl0);
+  f32_split(vt1, vh1, vl1);
   Kahan s0, s1;
   int flag = D.bc_or_not[t];
   bool mark = false;

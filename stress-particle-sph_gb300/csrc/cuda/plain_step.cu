@@ -39,15 +39,22 @@ __device__ __forceinline__ void stress_return(const Dev& D, const Real& M, doubl
 
 // FP32-form neighbour records of particle i (velocity, volume, stress, internal variable)
 __device__ __forceinline__ float4 split2(double x, double y) {
-  float xh = (float)x, yh = (float)y;
-  return make_float4(xh, yh, (float)(x - (double)xh), (float)(y - (double)yh));
+  float xh, xl, yh, yl;
+  f32_split(x, xh, xl);
+  f32_split(y, yh, yl);
+  return make_float4(xh, yh, xl, yl);
 }
 
-__device__ __forceinline__ void write_records(const Dev& D, int i, double vx, double vy, double a,
-                                              double b, double c, double d) {
-  D.recV[i] = split2(vx, vy);
-  D.recS[i] = make_float4((float)a, (float)b, (float)c, (float)d);
-  D.recI[i] = make_float4((float)D.iv1[i], (float)D.vol[i], (float)D.rho[i], (float)D.mass[i]);
+// Only the records a later kernel reads are written (every FP64 -> FP32 conversion costs
+// an FP64-pipe issue): node velocities always, stress-point velocities for XSPH, stress of
+// stress-points, and {iv1, m/rho, rho, m} where those change (rec_i).
+__device__ __forceinline__ void write_records(const Dev& D, int i, bool rec_i, double vx,
+                                              double vy, double a, double b, double c, double d) {
+  const bool sp = i >= D.NN;
+  if (!sp || D.xsph) D.recV[i] = split2(vx, vy);
+  if (sp) D.recS[i] = make_float4(f32_rn(a), f32_rn(b), f32_rn(c), f32_rn(d));
+  if (rec_i)
+    D.recI[i] = make_float4(f32_rn(D.iv1[i]), f32_rn(D.vol[i]), f32_rn(D.rho[i]), f32_rn(D.mass[i]));
 }
 
 __global__ void k_load_scalars(Dev D) {
@@ -215,7 +222,7 @@ __global__ void k_stage_begin(Dev D, int stage) {
   D.s1[i] = b;
   D.s2[i] = c;
   D.s3[i] = d;
-  if (D.fast) write_records(D, i, vx, vy, a, b, c, d);
+  if (D.fast) write_records(D, i, D.cont_density, vx, vy, a, b, c, d);
 }
 
 // stress_point_update (2_SPH_main_2018.f90:403-482) as a gather per target
@@ -329,10 +336,12 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
       D.A[0][i] = A0;
       D.A[1][i] = A1;
       D.A[2][i] = A2;
-      float h0 = (float)A0, h1 = (float)A1, h2 = (float)A2;
-      D.recA[i] = make_float4(h0, h1, h2, (float)D.mass[i]);
-      D.recAl[i] = make_float4((float)(A0 - (double)h0), (float)(A1 - (double)h1),
-                               (float)(A2 - (double)h2), 0.0f);
+      float h0, h1, h2, l0, l1, l2;
+      f32_split(A0, h0, l0);
+      f32_split(A1, h1, l1);
+      f32_split(A2, h2, l2);
+      D.recA[i] = make_float4(h0, h1, h2, f32_rn(D.mass[i]));
+      D.recAl[i] = make_float4(l0, l1, l2, 0.0f);
     } else {
       double r = D.rho[i];
       double r2 = r * r;
@@ -342,8 +351,9 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
     }
   }
   if (D.fast) {
-    D.recV[i] = split2(vx, vy);
-    D.recI[i] = make_float4((float)D.iv1[i], (float)D.vol[i], (float)D.rho[i], (float)D.mass[i]);
+    if (i < D.NN || D.xsph) D.recV[i] = split2(vx, vy);
+    if (D.cont_density)
+      D.recI[i] = make_float4(f32_rn(D.iv1[i]), f32_rn(D.vol[i]), f32_rn(D.rho[i]), f32_rn(D.mass[i]));
   }
 }
 
@@ -533,7 +543,7 @@ __global__ void k_rk_final(Dev D) {
     D.Ddev[i] = dd;
     D.iv1[i] = D.iv1[i] + M.dt * dd;  // update_strain (3_SPH_material_2018.f90:1864)
   }
-  if (D.fast) write_records(D, i, vx, vy, a, b, c, d);
+  if (D.fast) write_records(D, i, i >= D.NN || D.cont_density, vx, vy, a, b, c, d);
 }
 
 __global__ void k_trapezoid(Dev D) {
@@ -619,6 +629,34 @@ __global__ void k_selftest_div(int64_t n, uint64_t seed, unsigned long long* bad
     if (__double_as_longlong(q1) != __double_as_longlong(q2)) nb++;
   }
   if (nb) atomicAdd(bad, nb);
+}
+
+// the integer-pipe conversions against the hardware ones on n pseudo-random doubles
+// (log-uniform magnitudes 1e-45..1e45, both signs) and their float roundings
+__global__ void k_selftest_conv(int64_t n, uint64_t seed, unsigned long long* bad) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long nb = 0;
+  for (; i < n; i += stride) {
+    uint64_t r1 = mix64(seed ^ (uint64_t)i), r2 = mix64(r1);
+    double e = -45.0 + 90.0 * ((r1 >> 11) * 0x1.0p-53);
+    double x = exp2(e * 3.3219280948873622) * ((r2 & 1) ? -1.0 : 1.0);
+    if ((r2 & 0xF0) == 0) x = (double)(float)x;  // exact floats and halfway cases nearby
+    if ((r2 & 0xF00) == 0) x = x + x * 0x1.0p-24;
+    float h = f32_rn(x), hs, ls;
+    f32_split(x, hs, ls);
+    float hr = (float)x, lr = (float)(x - (double)hr);
+    double b = f64_of(hr);
+    if (__float_as_uint(h) != __float_as_uint(hr) || __float_as_uint(hs) != __float_as_uint(hr) ||
+        __float_as_uint(ls) != __float_as_uint(lr) ||
+        __double_as_longlong(b) != __double_as_longlong((double)hr))
+      nb++;
+  }
+  if (nb) atomicAdd(bad, nb);
+}
+
+void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad) {
+  k_selftest_conv<<<152 * 8, 256, 0, c.stream>>>(n, seed, d_bad);
 }
 
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad) {

@@ -906,6 +906,25 @@ int sps_selftest_division(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatc
   return SPS_OK;
 }
 
+int sps_selftest_convert(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatches) {
+  if (!h || !mismatches || n < 0) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  try {
+    unsigned long long* d = nullptr;
+    SPS_CUDA_CHECK(cudaMalloc(&d, sizeof(unsigned long long)));
+    SPS_CUDA_CHECK(cudaMemsetAsync(d, 0, sizeof(unsigned long long), c.stream));
+    sps::launch_selftest_conv(c, n, seed, d);
+    unsigned long long v = 0;
+    SPS_CUDA_CHECK(cudaMemcpyAsync(&v, d, sizeof(v), cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    cudaFree(d);
+    *mismatches = (int64_t)v;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
 int sps_get_stream(sps_ctx* h, void** stream) {
   if (!h || !stream) return SPS_ERR_ARG;
   *stream = (void*)h->c.stream;

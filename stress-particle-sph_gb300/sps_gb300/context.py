@@ -26,6 +26,8 @@ def gpu_lib():
         lib.sps_kernels_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         lib.sps_selftest_division.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
                                               C.POINTER(C.c_int64)]
+        lib.sps_selftest_convert.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
+                                             C.POINTER(C.c_int64)]
         lib.sps_profile_step.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                          C.c_char_p, C.c_int32, C.POINTER(C.c_double),
                                          C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]
@@ -159,6 +161,13 @@ def selftest_division(ctx, n, seed=1):
     """Mismatching results of the corrected division versus IEEE division on n operands."""
     m = C.c_int64(0)
     ctx._call("selftest_division", ctx._h, int(n), int(seed), C.byref(m))
+    return m.value
+
+
+def selftest_convert(ctx, n, seed=1):
+    """Mismatching results of the integer-pipe conversions versus the hardware ones."""
+    m = C.c_int64(0)
+    ctx._call("selftest_convert", ctx._h, int(n), int(seed), C.byref(m))
     return m.value
 
 

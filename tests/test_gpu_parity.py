@@ -134,3 +134,11 @@ def test_corrected_division_matches_ieee(built_gpu):
     p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
     g = _gpu_ctx(p)
     assert sps_gb300.selftest_division(g, 200_000_000, seed=12345) == 0
+
+
+def test_integer_pipe_conversions_match_hardware(built_gpu):
+    # the FP32 form converts its records with integer operations on the bit patterns; they
+    # must round exactly as the hardware conversions
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
+    g = _gpu_ctx(p)
+    assert sps_gb300.selftest_convert(g, 100_000_000, seed=777) == 0
