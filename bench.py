@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-size", type=int, default=256)
+    ap.add_argument("--error-steps", type=int, default=0,
+                    help="instead of timing: advance the FP64 plain and the FP32 forms this "
+                         "many steps side by side and report their relative errors")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
     return ap.parse_args()
 
@@ -238,6 +241,7 @@ def run_batch(args, dist, local):
     probs = batch_problems(args.batch_size)
     b = sps_gb300.Batch(probs, precision=_abi.SPS_PREC_FP32_FAST)
     b.upload_all()
+    tuned = sps_gb300.autotune(b, 2)
     w1 = time.perf_counter()
     b.step(max(args.warmup, 1))
     _, ms, clk = timed_steps(b, args.steps, None, dist, local)
@@ -258,7 +262,7 @@ def run_batch(args, dist, local):
     return {"realisations": len(probs), "particles": int(n), "velocity_particles": int(nv),
             "value": round(n * args.steps / (ms * 1e-3), 1), "unit": "particle-steps/s",
             "ms_per_step": round(ms / args.steps, 4), "steps": args.steps,
-            "setup_s": round(w1 - w0, 2), "precision": "fp32 form",
+            "setup_s": round(w1 - w0, 2), "precision": "fp32 form", "autotuned_blocks": tuned,
             "bit_identical_to_single_runs": same, "clocks": clk,
             "workload": batch_problems.__doc__.split("\n")[0]}
 
@@ -352,6 +356,7 @@ def run_ours(args):
     ctx.upload_problem(prob)
     if use_surr:
         sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
+    tuned = sps_gb300.autotune(ctx, 2)  # launch shapes; the state is restored
     t = ctx.step(max(args.warmup, 1), 0.0)  # warm-up (also instantiates the step graph)
     kps = sps_gb300.kernels_per_step(ctx)
     if use_surr:
@@ -399,6 +404,7 @@ def run_ours(args):
             cn = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
                                        prob.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
             cn.upload_problem(prob)
+            sps_gb300.autotune(cn, 2)
             tn = cn.step(max(args.warmup, 1), 0.0)
             tn, ms_n, _ = timed_steps(cn, args.steps, tn, dist, local)
             v_n = nparticles * args.steps * world / (ms_n * 1e-3)
@@ -491,6 +497,7 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "plain": plain, "error_vs_plain": errors, "surrogate": surr, "batch": batch,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
+            "autotuned_blocks": tuned,
             "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
             "kernel_ms_per_step": {k: round(v[0] / 2, 4) for k, v in sorted(
                 prof.items(), key=lambda kv: -kv[1][0])},
@@ -570,8 +577,57 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_errors(args):
+    """FP32 form (optionally with the surrogate) against the FP64 plain form over a long
+    run of the slope workload, with relative L2 / Linf errors at checkpoints."""
+    import numpy as np
+    import sps_gb300
+    from sps_gb300 import _abi
+    sps_gb300.build_all()
+    prob = workload(args.dx)
+    ctxs = {}
+    # "floor": the FP64 plain form again, from initial stresses perturbed by a relative
+    # 2^-52 (one FP64 rounding): how far two runs that differ by rounding drift apart
+    for name, prec in (("plain", _abi.SPS_PREC_FP64_PLAIN), ("fp32", _abi.SPS_PREC_FP32_FAST),
+                       ("floor", _abi.SPS_PREC_FP64_PLAIN)):
+        ctxs[name] = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                           prob.params_copy(precision=prec))
+        st = prob.state()
+        if name == "floor":
+            rng = np.random.default_rng(1)
+            st["stress"] = st["stress"] * (1.0 + 2.0 ** -52 * rng.uniform(-1, 1, st["stress"].shape))
+        ctxs[name].upload(**st)
+        ctxs[name].upload_bcs(prob.bc_or_not, prob.bc_info)
+    n = args.error_steps
+    marks = sorted({max(1, n * k // 20) for k in range(1, 21)})
+    nt = prob.ntotal
+    out, done, t = [], 0, {k: 0.0 for k in ctxs}
+    w0 = time.perf_counter()
+    for m in marks:
+        for name, c in ctxs.items():
+            t[name] = c.step(m - done, t[name])
+        done = m
+        b = ctxs["plain"].download()
+        row = {"steps": m, "time_s": t["plain"]}
+        for arm in ("fp32", "floor"):
+            a = ctxs[arm].download()
+            for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
+                          ("displ", slice(None))):
+                l2, li = rel_errors(a[k][sl], b[k][sl])
+                row[arm + "_" + k + "_rel_l2"] = l2
+                row[arm + "_" + k + "_rel_linf"] = li
+        out.append(row)
+    print(json.dumps({"error_run": {"workload": workload_name(prob, args.dx),
+                                    "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)",
+                                    "checkpoints": out,
+                                    "wall_s": round(time.perf_counter() - w0, 1)}}))
+
+
 def main():
     args = parse()
+    if args.error_steps > 0:
+        run_errors(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -160,6 +160,15 @@ int sps_selftest_division(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* misma
    bit. */
 int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* Launch-shape autotuner (no reference counterpart): time each tunable kernel (the pair
+   search and lists, the interpolation, the derivative sums, the stress-return and RK
+   kernels, XSPH) at block sizes 64, 128, 256 and 512 over nsteps profiled steps of the
+   uploaded state, keep the fastest size per kernel, and restore the state, so the results
+   of later steps are the same as without tuning.  blocks (may be NULL) receives the 8
+   chosen sizes in that order.  The cell size is not tuned: the reference's pair order
+   depends on it. */
+int sps_autotune(sps_ctx* ctx, int32_t nsteps, int32_t* blocks);
+
 /* Number of this library's kernels one step launches (no reference counterpart). */
 int sps_kernels_per_step(sps_ctx* ctx, int32_t* n);
 

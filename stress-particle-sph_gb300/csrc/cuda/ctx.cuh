@@ -10,6 +10,14 @@
 
 namespace sps {
 
+// kernels whose block size the autotuner chooses (sps_autotune)
+enum TunedKernel { TK_HALF, TK_LISTS, TK_INTERP, TK_DERIVS, TK_ADAPT, TK_STAGE, TK_RKFINAL,
+                   TK_XSPH, TK_N };
+constexpr const char* kTunedNames[TK_N] = {"half", "lists", "interp", "derivs",
+                                           "adapt_bc", "stage_begin", "rk_final", "xsph"};
+// largest block each accepts (launch bounds)
+constexpr int kTunedMax[TK_N] = {1024, 1024, 1024, 256, 1024, 1024, 1024, 1024};
+
 // host copy of one realisation's problem description (the pointer fields of its params
 // point into the vectors here)
 struct HostReal {
@@ -54,6 +62,8 @@ struct Ctx {
   uint2* mlp_frag = nullptr;
   float* mlp_bias = nullptr;
   unsigned long long* surr_cnt = nullptr;
+  int blk[TK_N] = {256, 256, 256, 256, 256, 256, 256, 256};  // block sizes (sps_autotune)
+  int grid_of(int k, int n) const { return (n + blk[k] - 1) / blk[k]; }
   int64_t kernels_launched = 0;  // kernels enqueued by the launch functions
   int kernels_per_step = 0;
   // called before each kernel group: counts its kernels and, when profiling, records an

@@ -440,10 +440,10 @@ __global__ void k_fxsph(Dev D) {
 }  // namespace
 
 void launch_finterp(Ctx& c) {
-  k_finterp<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);
+  k_finterp<<<c.grid_of(TK_INTERP, c.d.N2), c.blk[TK_INTERP], 0, c.stream>>>(c.d);
 }
 void launch_fderivs(Ctx& c, int stage) {
-  k_fderivs<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d, stage);
+  k_fderivs<<<c.grid_of(TK_DERIVS, c.d.N2), c.blk[TK_DERIVS], 0, c.stream>>>(c.d, stage);
 }
 void launch_fsp_tail(Ctx& c, int stage) {
   int ns = c.d.NT - c.d.NN;
@@ -452,7 +452,7 @@ void launch_fsp_tail(Ctx& c, int stage) {
   else k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
-  k_fxsph<<<(c.d.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);
+  k_fxsph<<<c.grid_of(TK_XSPH, c.d.N2), c.blk[TK_XSPH], 0, c.stream>>>(c.d);
 }
 
 int launch_fast_step(Ctx& c) { return launch_plain_step(c); }

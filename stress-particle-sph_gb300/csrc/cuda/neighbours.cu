@@ -734,14 +734,15 @@ int launch_pair_build(Ctx& c) {
   c.mark("spos");
   k_spos<<<nb, kBlock, 0, st>>>(D);
   c.mark("half");
-  if (c.precision == SPS_PREC_FP32_FAST) k_half<true><<<nb, kBlock, 0, st>>>(D);
-  else k_half<false><<<nb, kBlock, 0, st>>>(D);
+  if (c.precision == SPS_PREC_FP32_FAST)
+    k_half<true><<<c.grid_of(TK_HALF, D.N2), c.blk[TK_HALF], 0, st>>>(D);
+  else k_half<false><<<c.grid_of(TK_HALF, D.N2), c.blk[TK_HALF], 0, st>>>(D);
   c.mark("scan_half", 3);
   scan_i32_to_i64(c, D.half_cnt, D.half_off, D.N2);
   c.mark("pair_meta");
   k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("lists");
-  k_lists<<<nb, kBlock, 0, st>>>(D);
+  k_lists<<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
   return 0;
 }
 

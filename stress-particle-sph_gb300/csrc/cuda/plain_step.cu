@@ -672,7 +672,6 @@ int launch_plain_step(Ctx& c) {
   cudaStream_t st = c.stream;
   int nbT = (D.NT + kBlock - 1) / kBlock;
   int nbN = (D.NN + kBlock - 1) / kBlock;
-  int nb2 = (D.N2 + kBlock - 1) / kBlock;
   c.mark("load_scalars");
   k_load_scalars<<<1, 128, 0, st>>>(D);
   launch_pair_build(c);
@@ -684,41 +683,41 @@ int launch_plain_step(Ctx& c) {
   }
   for (int stage = 0; stage < 4; stage++) {
     c.mark("stage_begin");
-    k_stage_begin<<<nbT, kBlock, 0, st>>>(D, stage);
+    k_stage_begin<<<c.grid_of(TK_STAGE, D.NT), c.blk[TK_STAGE], 0, st>>>(D, stage);
     c.mark("interp");
     if (D.fast) launch_finterp(c);
-    else k_interp<<<nb2, kBlock, 0, st>>>(D);
+    else k_interp<<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, st>>>(D);
     if (D.cont_density && D.sp_sph) {
       c.mark("node_rho");
       k_node_rho<<<nbN, kBlock, 0, st>>>(D);
     }
     c.mark("adapt_bc");
-    k_adapt_bc<<<nbT, kBlock, 0, st>>>(D, 1);
+    k_adapt_bc<<<c.grid_of(TK_ADAPT, D.NT), c.blk[TK_ADAPT], 0, st>>>(D, 1);
     c.mark("derivs");
     if (D.fast) launch_fderivs(c, stage);
-    else k_derivs<<<nb2, kBlock, 0, st>>>(D, stage);
+    else k_derivs<<<c.grid_of(TK_DERIVS, D.N2), c.blk[TK_DERIVS], 0, st>>>(D, stage);
     if (D.fast) {
       c.mark("sp_tail");
       launch_fsp_tail(c, stage);
     }
   }
   c.mark("rk_final");
-  k_rk_final<<<nbT, kBlock, 0, st>>>(D);
+  k_rk_final<<<c.grid_of(TK_RKFINAL, D.NT), c.blk[TK_RKFINAL], 0, st>>>(D);
   c.mark("interp");
   if (D.fast) launch_finterp(c);
-  else k_interp<<<nb2, kBlock, 0, st>>>(D);
+  else k_interp<<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, st>>>(D);
   if (D.cont_density && D.sp_sph) {
     c.mark("node_rho");
     k_node_rho<<<nbN, kBlock, 0, st>>>(D);
   }
   if (D.sp_sph || D.fast) {
     c.mark("adapt_bc");
-    k_adapt_bc<<<nbT, kBlock, 0, st>>>(D, 0);
+    k_adapt_bc<<<c.grid_of(TK_ADAPT, D.NT), c.blk[TK_ADAPT], 0, st>>>(D, 0);
   }
   if (D.update_x && D.xsph) {
     c.mark("xsph");
     if (D.fast) launch_fxsph(c);
-    else k_xsph<<<nb2, kBlock, 0, st>>>(D);
+    else k_xsph<<<c.grid_of(TK_XSPH, D.N2), c.blk[TK_XSPH], 0, st>>>(D);
   } else {
     c.mark("trapezoid");
     k_trapezoid<<<nbT, kBlock, 0, st>>>(D);

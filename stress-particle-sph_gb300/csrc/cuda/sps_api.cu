@@ -931,6 +931,11 @@ int sps_get_stream(sps_ctx* h, void** stream) {
   return SPS_OK;
 }
 
+namespace {
+void profile_run(sps::Ctx& c, int nsteps, double* t, std::vector<std::string>& kn,
+                 std::vector<double>& kms, std::vector<int>& kl);
+}  // namespace
+
 int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, int32_t names_len,
                      double* ms, int32_t* launches, int32_t cap, int32_t* nkernels) {
   if (!h || !time_sph || nsteps <= 0 || !names || !ms || !launches || !nkernels)
@@ -942,38 +947,7 @@ int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, 
   std::vector<int> kl;
   try {
     std::vector<double> t(time_sph, time_sph + c.d.R);
-    ensure_scal(c, nsteps);
-    fill_table(c, nsteps, t.data());
-    SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(),
-                                   sizeof(sps::StepScalars) * c.h_scal.size(),
-                                   cudaMemcpyHostToDevice, c.stream));
-    SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
-    c.profiling = true;
-    for (int k = 0; k < nsteps; k++) {
-      if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
-      else sps::launch_fast_step(c);
-      c.mark("end");
-    }
-    c.profiling = false;
-    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
-    SPS_CUDA_CHECK(cudaGetLastError());
-    for (size_t k = 0; k + 1 < c.prof_events.size(); k++) {
-      const char* nm = c.prof_events[k].first;
-      if (std::strcmp(nm, "end") == 0) continue;
-      float e = 0.0f;
-      cudaEventElapsedTime(&e, c.prof_events[k].second, c.prof_events[k + 1].second);
-      size_t q = 0;
-      while (q < kn.size() && kn[q] != nm) q++;
-      if (q == kn.size()) {
-        kn.push_back(nm);
-        kms.push_back(0.0);
-        kl.push_back(0);
-      }
-      kms[q] += e;
-      kl[q] += 1;
-    }
-    for (auto& pe : c.prof_events) cudaEventDestroy(pe.second);
-    c.prof_events.clear();
+    profile_run(c, nsteps, t.data(), kn, kms, kl);
     SPS_CUDA_CHECK(cudaMemcpy(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost));
     for (int r = 0; r < c.d.R; r++) time_sph[r] = t[r];
     c.steps_done += nsteps;
@@ -997,6 +971,135 @@ int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, 
     int e = *c.h_err;
     cudaMemset(c.d.err, 0, sizeof(int));
     return fail(&c, SPS_ERR_CAPACITY, err_text(e));
+  }
+  return SPS_OK;
+}
+
+namespace {
+
+// nsteps steps with CUDA events around every kernel group (no graph): per-group totals
+void profile_run(sps::Ctx& c, int nsteps, double* t, std::vector<std::string>& kn,
+                 std::vector<double>& kms, std::vector<int>& kl) {
+  ensure_scal(c, nsteps);
+  fill_table(c, nsteps, t);
+  SPS_CUDA_CHECK(cudaMemcpyAsync(c.d_scal_table, c.h_scal.data(),
+                                 sizeof(sps::StepScalars) * c.h_scal.size(),
+                                 cudaMemcpyHostToDevice, c.stream));
+  SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
+  c.profiling = true;
+  for (int k = 0; k < nsteps; k++) {
+    if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
+    else sps::launch_fast_step(c);
+    c.mark("end");
+  }
+  c.profiling = false;
+  SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  SPS_CUDA_CHECK(cudaGetLastError());
+  for (size_t k = 0; k + 1 < c.prof_events.size(); k++) {
+    const char* nm = c.prof_events[k].first;
+    if (std::strcmp(nm, "end") == 0) continue;
+    float e = 0.0f;
+    cudaEventElapsedTime(&e, c.prof_events[k].second, c.prof_events[k + 1].second);
+    size_t q = 0;
+    while (q < kn.size() && kn[q] != nm) q++;
+    if (q == kn.size()) {
+      kn.push_back(nm);
+      kms.push_back(0.0);
+      kl.push_back(0);
+    }
+    kms[q] += e;
+    kl[q] += 1;
+  }
+  for (auto& pe : c.prof_events) cudaEventDestroy(pe.second);
+  c.prof_events.clear();
+}
+
+// the device arrays a step carries over from the previous step (or the upload)
+std::vector<std::pair<void*, size_t>> carried_state(sps::Ctx& c) {
+  sps::Dev& D = c.d;
+  const size_t N2 = D.N2, NT = D.NT, NN = D.NN, d8 = sizeof(double);
+  std::vector<std::pair<void*, size_t>> v = {
+      {D.px, d8 * N2},   {D.py, d8 * N2},    {D.vx, d8 * N2},      {D.vy, d8 * N2},
+      {D.s0, d8 * N2},   {D.s1, d8 * N2},    {D.s2, d8 * N2},      {D.s3, d8 * N2},
+      {D.rho, d8 * N2},  {D.hsml, d8 * N2},  {D.vol, d8 * N2},     {D.rinv, d8 * N2},
+      {D.iv1, d8 * NT},  {D.fdp, d8 * NT},   {D.grad_u, 4 * d8 * NT},
+      {D.dispx, d8 * NN}, {D.dispy, d8 * NN}, {D.bc_or_not, sizeof(int32_t) * NT},
+      {D.out, N2},       {D.meta, sizeof(sps::PairMeta) * D.R}};
+  if (D.fast) {
+    v.push_back({D.recV, sizeof(float4) * N2});
+    v.push_back({D.recS, sizeof(float4) * NT});
+    v.push_back({D.recI, sizeof(float4) * N2});
+    v.push_back({D.recA, sizeof(float4) * NT});
+    v.push_back({D.recAl, sizeof(float4) * NT});
+  }
+  if (c.surr_cnt) v.push_back({c.surr_cnt, 4 * sizeof(unsigned long long)});
+  if (c.cap_cnt) v.push_back({c.cap_cnt, sizeof(unsigned long long)});
+  return v;
+}
+
+}  // namespace
+
+int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
+  if (!h || nsteps <= 0) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!c.uploaded) return fail(&c, SPS_ERR_STATE, "sps_autotune before sps_upload");
+  void* snap = nullptr;
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    auto st = carried_state(c);
+    size_t total = 0;
+    for (auto& a : st) total += (a.second + 255) & ~size_t(255);
+    SPS_CUDA_CHECK(cudaMalloc(&snap, total));
+    auto copy = [&](bool save) {
+      size_t off = 0;
+      for (auto& a : st) {
+        char* sp = static_cast<char*>(snap) + off;
+        if (save) SPS_CUDA_CHECK(cudaMemcpyAsync(sp, a.first, a.second, cudaMemcpyDeviceToDevice, c.stream));
+        else SPS_CUDA_CHECK(cudaMemcpyAsync(a.first, sp, a.second, cudaMemcpyDeviceToDevice, c.stream));
+        off += (a.second + 255) & ~size_t(255);
+      }
+      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    };
+    copy(true);
+    const int cand[] = {64, 128, 256, 512};
+    int best[sps::TK_N];
+    double best_ms[sps::TK_N];
+    for (int k = 0; k < sps::TK_N; k++) {
+      best[k] = c.blk[k];
+      best_ms[k] = 1e300;
+    }
+    std::vector<double> t(c.d.R, 0.0);
+    for (int b : cand) {
+      for (int k = 0; k < sps::TK_N; k++) c.blk[k] = std::min(b, sps::kTunedMax[k]);
+      std::vector<std::string> kn;
+      std::vector<double> kms;
+      std::vector<int> kl;
+      std::fill(t.begin(), t.end(), 0.0);
+      profile_run(c, nsteps, t.data(), kn, kms, kl);
+      copy(false);
+      for (int k = 0; k < sps::TK_N; k++)
+        for (size_t q = 0; q < kn.size(); q++)
+          if (kn[q] == sps::kTunedNames[k] && kms[q] < best_ms[k]) {
+            best_ms[k] = kms[q];
+            best[k] = c.blk[k];
+          }
+    }
+    for (int k = 0; k < sps::TK_N; k++) {
+      c.blk[k] = best[k];
+      if (blocks) blocks[k] = best[k];
+    }
+    SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    cudaFree(snap);
+    snap = nullptr;
+    if (c.graph) {
+      cudaGraphExecDestroy(c.graph);
+      c.graph = nullptr;
+    }
+  } catch (const std::exception& e) {
+    c.profiling = false;
+    if (snap) cudaFree(snap);
+    return fail(&c, SPS_ERR_CUDA, e.what());
   }
   return SPS_OK;
 }

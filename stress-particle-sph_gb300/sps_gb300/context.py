@@ -28,6 +28,7 @@ def gpu_lib():
                                               C.POINTER(C.c_int64)]
         lib.sps_selftest_convert.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
                                              C.POINTER(C.c_int64)]
+        lib.sps_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
         lib.sps_profile_step.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                          C.c_char_p, C.c_int32, C.POINTER(C.c_double),
                                          C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32)]
@@ -169,6 +170,17 @@ def selftest_convert(ctx, n, seed=1):
     m = C.c_int64(0)
     ctx._call("selftest_convert", ctx._h, int(n), int(seed), C.byref(m))
     return m.value
+
+
+TUNED_KERNELS = ("half", "lists", "interp", "derivs", "adapt_bc", "stage_begin", "rk_final",
+                 "xsph")
+
+
+def autotune(ctx, nsteps=2):
+    """sps_autotune: {kernel: chosen block size}; the context's state is unchanged."""
+    b = (C.c_int32 * len(TUNED_KERNELS))()
+    ctx._call("autotune", ctx._h, int(nsteps), b)
+    return dict(zip(TUNED_KERNELS, list(b)))
 
 
 def kernels_per_step(ctx):
