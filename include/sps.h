@@ -134,6 +134,13 @@ int sps_step(sps_ctx* ctx, int32_t nsteps, double* time_sph);
 int sps_download(sps_ctx* ctx, double* x, double* vel, double* stress, double* rho,
                  double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker);
 
+/* The module arrays of get_nodes_on_free_surface (code/3_SPH_material_2018.f90:1135),
+   which every step with update_x recomputes after the position update, for realisation r
+   (0 for a single problem): normal(2,ntotal) (unit outward normal on surface particles, 0
+   inside) and subset(ntotal) (1 on the free surface, 2 inside).  The routine's
+   bc_or_not update (2 on the surface) is returned by sps_download. */
+int sps_download_surface(sps_ctx* ctx, int32_t r, double* normal, int32_t* subset);
+
 /* Test hook: the pair list of the last step in the reference's traversal order (the
    order its linked list `last -> next` is walked), after Pint_Update
    (code/3_SPH_material_2018.f90:1574): 1-based pair_i, pair_j, pint_type, and the FP32

@@ -49,6 +49,7 @@ struct orc_ctx {
   int32_t *itype, *out_domain, *bc_or_not, *bc_info, *bc_int;
   double *intvars1, *f_drucker, *grad_u, *Ddev;
   double *f_bound, *art_visc;
+  double *normal, *subset; /* module arrays of get_nodes_on_free_surface, (2,ntotal), (ntotal) */
   /* pair list, creation order */
   int64_t npairs, cap, m_pairs;
   int32_t *pi, *pj, *ptype;
@@ -754,6 +755,13 @@ static void normal_bcs(orc_ctx* c) {
   }
 }
 
+/* BCs (3_SPH_material_2018.f90:1640-1660) */
+static void apply_stress_free(orc_ctx* c);
+static void bcs(orc_ctx* c) {
+  normal_bcs(c);
+  if (c->p.ifsigman == 1) apply_stress_free(c);
+}
+
 static void adapt_all(orc_ctx* c) {
   double a2, kc;
   dp_constants(c->p.props[12], c->p.props[13], &a2, &kc);
@@ -809,11 +817,11 @@ static void rk4(orc_ctx* c) {
       }
     }
     if (ncrit == 12) adapt_all(c);
-    if (c->p.no_bcs > 0) normal_bcs(c);
+    if (c->p.no_bcs > 0) bcs(c);
     stress_point_update(c);
     if (c->p.sp_sph) {
       if (ncrit == 12) adapt_all(c);
-      if (c->p.no_bcs > 0) normal_bcs(c);
+      if (c->p.no_bcs > 0) bcs(c);
     }
     get_derivatives(c, div1, div2);
     for (int j = NN; j < NT; j++) {
@@ -862,7 +870,7 @@ static void rk4(orc_ctx* c) {
     for (int s = 0; s < 4; s++)
       S(c, s, i) = st0[s + 4 * (size_t)i] + (dt / 6.0) * RKs[s + 4 * (size_t)i];
   if (ncrit == 12) adapt_all(c);
-  if (c->p.no_bcs > 0) normal_bcs(c);
+  if (c->p.no_bcs > 0) bcs(c);
   if (c->p.cont_density) {
     for (int i = NN; i < NT; i++) c->rho[i] = rho0[i] + (dt / 6.0) * RKr[i];
     if (c->p.sle == 2)
@@ -887,6 +895,170 @@ static void rk4(orc_ctx* c) {
   free(src);
   free(spin);
   free(grav);
+}
+
+/* get_nodes_on_free_surface (3_SPH_material_2018.f90:1135-1430).  Its locals are `real`
+   (FP32); the module arrays normal and subset are FP64.  An FP32 accumulation with an FP64
+   operand is evaluated in FP64 and rounded once, as Fortran's mixed-kind expressions are.
+   `x**0.5` is taken as the square root. */
+static void free_surface(orc_ctx* c) {
+  const int NT = c->NT;
+  float* A = xcalloc(4 * (size_t)NT, sizeof(float));
+  float* ff = xcalloc(2 * (size_t)NT, sizeof(float));
+  float* f_int = xcalloc((size_t)NT, sizeof(float));
+  float* gf = xcalloc(2 * (size_t)NT, sizeof(float));
+  float* nb = xcalloc((size_t)NT, sizeof(float));
+  float* tt = xcalloc(2 * (size_t)NT, sizeof(float));
+  float* tau = xcalloc(2 * (size_t)NT, sizeof(float));
+  double* nrm = c->normal;
+  for (int i = 0; i < NT; i++) c->subset[i] = 0.0;
+  /* step 1: renormalisation matrix and kernel-gradient sums over types 1, 2, 3 */
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    int t = c->ptype[q];
+    if (t != 1 && t != 2 && t != 3) continue;
+    int i = c->pi[q], j = c->pj[q];
+    float gx = c->pdx[q], gy = c->pdy[q];
+    float hf1i = (float)(c->mass[j] * (double)gx / c->rho[j]);
+    float hf1j = (float)(-(c->mass[i] * (double)gx / c->rho[i]));
+    float hf2i = (float)(c->mass[j] * (double)gy / c->rho[j]);
+    float hf2j = (float)(-(c->mass[i] * (double)gy / c->rho[i]));
+    double dxij = X(c, 0, j) - X(c, 0, i), dyij = X(c, 1, j) - X(c, 1, i);
+    double dxji = X(c, 0, i) - X(c, 0, j), dyji = X(c, 1, i) - X(c, 1, j);
+    A[0 + 4 * (size_t)i] = (float)((double)A[0 + 4 * (size_t)i] + dxij * (double)hf1i);
+    A[0 + 4 * (size_t)j] = (float)((double)A[0 + 4 * (size_t)j] + dxji * (double)hf1j);
+    ff[0 + 2 * (size_t)i] = ff[0 + 2 * (size_t)i] + hf1i;
+    ff[0 + 2 * (size_t)j] = ff[0 + 2 * (size_t)j] + hf1j;
+    A[1 + 4 * (size_t)i] = (float)((double)A[1 + 4 * (size_t)i] + dyij * (double)hf1i);
+    A[2 + 4 * (size_t)i] = (float)((double)A[2 + 4 * (size_t)i] + dxij * (double)hf2i);
+    A[3 + 4 * (size_t)i] = (float)((double)A[3 + 4 * (size_t)i] + dyij * (double)hf2i);
+    A[1 + 4 * (size_t)j] = (float)((double)A[1 + 4 * (size_t)j] + dyji * (double)hf1j);
+    A[2 + 4 * (size_t)j] = (float)((double)A[2 + 4 * (size_t)j] + dxji * (double)hf2j);
+    A[3 + 4 * (size_t)j] = (float)((double)A[3 + 4 * (size_t)j] + dyji * (double)hf2j);
+    ff[1 + 2 * (size_t)i] = ff[1 + 2 * (size_t)i] + hf2i;
+    ff[1 + 2 * (size_t)j] = ff[1 + 2 * (size_t)j] + hf2j;
+  }
+  /* step 2: first normal estimate; step 3 set-up: scan point and tangent */
+  for (int i = 0; i < NT; i++) {
+    float* a = &A[4 * (size_t)i];
+    for (int r = 0; r < 4; r++)
+      if (fabsf(a[r]) <= 1.e-8f) a[r] = 0.0f;
+    float f0 = ff[2 * (size_t)i], f1 = ff[2 * (size_t)i + 1];
+    float v0 = -(a[0] * f0 + a[1] * f1);
+    float v1 = -(a[2] * f0 + a[3] * f1);
+    float v2 = sqrtf(v0 * v0 + v1 * v1);
+    nrm[2 * (size_t)i] = (double)(v0 / v2);
+    nrm[2 * (size_t)i + 1] = (double)(v1 / v2);
+    tt[2 * (size_t)i] = (float)(X(c, 0, i) + c->hsml[i] * nrm[2 * (size_t)i]);
+    tt[2 * (size_t)i + 1] = (float)(X(c, 1, i) + c->hsml[i] * nrm[2 * (size_t)i + 1]);
+    tau[2 * (size_t)i] = (float)(-nrm[2 * (size_t)i + 1]);
+    tau[2 * (size_t)i + 1] = (float)nrm[2 * (size_t)i];
+  }
+  /* step 3: a particle with a neighbour in its scan region is inside */
+  const float sqrt2 = sqrtf(2.0f);
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    int t = c->ptype[q];
+    int i = c->pi[q], j = c->pj[q];
+    int side[2] = {0, 0}; /* check i against j, check j against i */
+    if (t == 2 || t == 3) side[0] = side[1] = 1;
+    else if (t == 6 || t == 9) side[1] = 1;
+    for (int sdx = 0; sdx < 2; sdx++) {
+      if (!side[sdx]) continue;
+      int a = sdx == 0 ? i : j, b = sdx == 0 ? j : i;
+      if (c->subset[a] != 0.0) continue;
+      double ddx = X(c, 0, b) - X(c, 0, a), ddy = X(c, 1, b) - X(c, 1, a);
+      float xba = (float)sqrt(ddx * ddx + ddy * ddy);
+      float xbt0 = (float)(X(c, 0, b) - (double)tt[2 * (size_t)a]);
+      float xbt1 = (float)(X(c, 1, b) - (double)tt[2 * (size_t)a + 1]);
+      float xbt_norm = sqrtf(xbt0 * xbt0 + xbt1 * xbt1);
+      float prod = (float)(fabs(nrm[2 * (size_t)a] * (double)xbt0 + nrm[2 * (size_t)a + 1] * (double)xbt1) +
+                           (double)fabsf(tau[2 * (size_t)a] * xbt0 + tau[2 * (size_t)a + 1] * xbt1));
+      float limit = (float)((double)sqrt2 * c->hsml[a]);
+      if (xba >= limit && (double)xbt_norm < c->hsml[a]) {
+        c->subset[a] = 2.0;
+        f_int[a] = -1.0f;
+      } else if (xba < limit && (double)prod < c->hsml[a]) {
+        c->subset[a] = 2.0;
+        f_int[a] = -1.0f;
+      }
+    }
+  }
+  for (int i = 0; i < NT; i++)
+    if (c->subset[i] == 0.0) c->subset[i] = 1.0;
+  for (int i = 0; i < NT; i++)
+    if (c->bc_or_not[i] != 1) c->bc_or_not[i] = 0;
+  for (int i = 0; i < NT; i++) {
+    if (c->subset[i] == 2.0 && c->bc_or_not[i] != 1) c->bc_or_not[i] = 0;
+    else if (c->subset[i] == 1.0 && c->bc_or_not[i] != 1) c->bc_or_not[i] = 2;
+    else if (c->subset[i] == 1.0 && c->bc_or_not[i] == 1) c->subset[i] = 2.0;
+  }
+  /* step 4: normals of the surface particles from their surface neighbours */
+  for (int i = 0; i < 2 * NT; i++) nrm[i] = 0.0;
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    int t = c->ptype[q];
+    if (t != 1 && t != 2 && t != 3) continue;
+    int i = c->pi[q], j = c->pj[q];
+    if (c->subset[i] == 1.0 && c->subset[j] == 1.0) {
+      float x1 = (float)X(c, 0, i), y1 = (float)X(c, 1, i);
+      float x2 = (float)X(c, 0, j), y2 = (float)X(c, 1, j);
+      float xv = x2 - x1, yv = y2 - y1;
+      nrm[2 * (size_t)i] = nrm[2 * (size_t)i] - (double)yv;
+      nrm[2 * (size_t)i + 1] = nrm[2 * (size_t)i + 1] + (double)xv;
+      nrm[2 * (size_t)j] = nrm[2 * (size_t)j] - (double)yv;
+      nrm[2 * (size_t)j + 1] = nrm[2 * (size_t)j + 1] + (double)xv;
+      nb[i] = nb[i] + 1.0f;
+      nb[j] = nb[j] + 1.0f;
+    }
+    float gx = c->pdx[q], gy = c->pdy[q];
+    float hf1i = (float)(c->mass[j] * (double)gx / c->rho[j]);
+    float hf1j = (float)(-(c->mass[i] * (double)gx / c->rho[i]));
+    float hf2i = (float)(c->mass[j] * (double)gy / c->rho[j]);
+    float hf2j = (float)(-(c->mass[i] * (double)gy / c->rho[i]));
+    gf[2 * (size_t)i] = gf[2 * (size_t)i] + (f_int[j] - f_int[i]) * hf1i;
+    gf[2 * (size_t)j] = gf[2 * (size_t)j] + (f_int[i] - f_int[j]) * hf1j;
+    gf[2 * (size_t)i + 1] = gf[2 * (size_t)i + 1] + (f_int[j] - f_int[i]) * hf2i;
+    gf[2 * (size_t)j + 1] = gf[2 * (size_t)j + 1] + (f_int[i] - f_int[j]) * hf2j;
+  }
+  for (int i = 0; i < NT; i++) {
+    if (c->subset[i] != 1.0) continue;
+    double* n = &nrm[2 * (size_t)i];
+    n[0] = n[0] / (double)nb[i];
+    n[1] = n[1] / (double)nb[i];
+    float norm_vect = (float)sqrt(n[0] * n[0] + n[1] * n[1]);
+    n[0] = n[0] / (double)norm_vect;
+    n[1] = n[1] / (double)norm_vect;
+    float p_scal = (float)((double)gf[2 * (size_t)i] * n[0] + (double)gf[2 * (size_t)i + 1] * n[1]);
+    if (p_scal < 0) {
+      n[0] = -n[0];
+      n[1] = -n[1];
+    }
+  }
+  free(A);
+  free(ff);
+  free(f_int);
+  free(gf);
+  free(nb);
+  free(tt);
+  free(tau);
+}
+
+/* apply_stress_free (3_SPH_material_2018.f90:1775-1858): zero normal and shear traction
+   on free-surface nodes away from walls (called inside BCs when ifsigman = 1) */
+static void apply_stress_free(orc_ctx* c) {
+  for (int ip = 0; ip < c->NN; ip++) {
+    if (!(c->bc_or_not[ip] == 2 && c->bc_int[ip] != 1)) continue;
+    double costh = c->normal[2 * (size_t)ip], sinth = c->normal[2 * (size_t)ip + 1];
+    if (isnan(costh) || isnan(sinth)) continue;
+    double s2 = sinth * sinth, c2 = costh * costh, sc = sinth * costh;
+    double sxx0 = S(c, 0, ip), syy0 = S(c, 1, ip), sxy0 = S(c, 2, ip);
+    double stt = (s2 * sxx0 - (2.0 * sc) * sxy0) + c2 * syy0;
+    S(c, 0, ip) = s2 * stt;
+    S(c, 1, ip) = c2 * stt;
+    S(c, 2, ip) = -(sc * stt);
+    S(c, 3, ip) = c2 * stt;
+  }
 }
 
 /* XSPH_update (2_SPH_main_2018.f90:189-239) */
@@ -938,7 +1110,7 @@ static int time_integration(orc_ctx* c) {
   stress_point_update(c);
   if (c->p.sp_sph) {
     if (ncrit == 12) adapt_all(c);
-    if (c->p.no_bcs > 0) normal_bcs(c);
+    if (c->p.no_bcs > 0) bcs(c);
   }
   if (c->p.update_x) {
     if (c->p.xsph) {
@@ -950,6 +1122,7 @@ static int time_integration(orc_ctx* c) {
           X(c, d, i) = c->x0[d + 2 * (size_t)i] + (double)vh * c->p.dt_sph;
         }
     }
+    free_surface(c); /* ndimn == 2 */
     if (!c->p.sp_sph)
       for (int i = 0; i < NN; i++)
         for (int d = 0; d < 2; d++) X(c, d, NN + i) = X(c, d, i);
@@ -979,7 +1152,6 @@ int orc_create(const sps_params* p, orc_ctx** out) {
   int ntype_eco = (int)p->props[0], ncrit = (int)p->props[1];
   if (ntype_eco > 1 && ncrit != 12) return SPS_ERR_UNSUPPORTED;
   if (p->skf < 1 || p->skf > 3) return SPS_ERR_ARG;
-  if (p->ifsigman) return SPS_ERR_UNSUPPORTED;
   if (!p->sp_sph && p->nstress != p->nnode) return SPS_ERR_ARG;
   orc_ctx* c = xcalloc(1, sizeof(orc_ctx));
   if (!c) return SPS_ERR_ARG;
@@ -1027,6 +1199,8 @@ int orc_create(const sps_params* p, orc_ctx** out) {
   c->bc_or_not = xcalloc(NT, sizeof(int32_t));
   c->bc_info = xcalloc(8 * NT, sizeof(int32_t));
   c->bc_int = xcalloc(NN, sizeof(int32_t));
+  c->normal = xcalloc(2 * (size_t)NT, sizeof(double));
+  c->subset = xcalloc((size_t)NT, sizeof(double));
   c->intvars1 = xcalloc(NT, sizeof(double));
   c->f_drucker = xcalloc(NT, sizeof(double));
   c->grad_u = xcalloc(4 * NT, sizeof(double));
@@ -1118,12 +1292,21 @@ int orc_dump_pairs(orc_ctx* c, int32_t* pair_i, int32_t* pair_j, int32_t* pint_t
   return SPS_OK;
 }
 
+int orc_download_surface(orc_ctx* c, double* normal, int32_t* subset) {
+  if (!c) return SPS_ERR_ARG;
+  if (normal) memcpy(normal, c->normal, 2 * (size_t)c->NT * sizeof(double));
+  if (subset)
+    for (int i = 0; i < c->NT; i++) subset[i] = (int32_t)c->subset[i];
+  return SPS_OK;
+}
+
 void orc_destroy(orc_ctx* c) {
   if (!c) return;
   void* ptrs[] = {c->nptstcurves, c->ttcurves, c->ftcurves, c->bc_list, c->wall_position,
                   c->horizontal_or_not, c->x, c->vel, c->stress, c->mass, c->rho, c->hsml,
                   c->x00, c->x0, c->vx0, c->displ, c->itype, c->out_domain, c->bc_or_not,
                   c->bc_info, c->bc_int, c->intvars1, c->f_drucker, c->grad_u, c->Ddev,
+                  c->normal, c->subset,
                   c->f_bound, c->art_visc, c->pi, c->pj, c->ptype, c->pw, c->pdx, c->pdy,
                   c->order, c->which_cell, c->cell_cnt, c->cell_start, c->cell_list};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);

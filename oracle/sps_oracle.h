@@ -33,6 +33,9 @@ int orc_upload_bcs(orc_ctx* c, const int32_t* bc_or_not, const int32_t* bc_info)
 int orc_step(orc_ctx* c, int32_t nsteps, double* time_sph);
 int orc_download(orc_ctx* c, double* x, double* vel, double* stress, double* rho,
                  double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker);
+/* the module arrays of get_nodes_on_free_surface after the last step: normal(2,ntotal),
+   subset(ntotal) (1 = on the free surface, 2 = inside) */
+int orc_download_surface(orc_ctx* c, double* normal, int32_t* subset);
 int orc_dump_pairs(orc_ctx* c, int32_t* pair_i, int32_t* pair_j, int32_t* pint_type, float* w,
                    float* dwdx, float* dwdy, int64_t* npairs);
 void orc_destroy(orc_ctx* c);

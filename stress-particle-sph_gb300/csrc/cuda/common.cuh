@@ -160,7 +160,13 @@ struct Dev {
   int32_t* half_cnt;
   int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
   int4 *cross, *same;
+  int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)
   int32_t *degC, *degS;
+  // get_nodes_on_free_surface: normal (module FP64), subset (1 surface, 2 inside), f_int
+  double *nrmx, *nrmy;
+  int8_t* subset;
+  float* fint;
+  int ifsigman;
   PairMeta* meta;  // per realisation
   // scalars of the current step, per realisation (table: [step][realisation])
   const StepScalars* scal_table;
@@ -474,6 +480,8 @@ void launch_vol(Ctx& c, int lo, int hi);
 void launch_finterp(Ctx& c);
 void launch_fderivs(Ctx& c, int stage);
 void launch_fsp_tail(Ctx& c, int stage);
+void launch_surface(Ctx& c);
+void launch_lists_keys(Ctx& c);
 void launch_fxsph(Ctx& c);
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);

@@ -28,6 +28,12 @@ struct HostReal {
   // extent and smoothing lengths of the uploaded state (capacity sizing)
   double ncells_est = 0.0, hmax = 0.0, hmin_nd = 1e300;
   bool uploaded = false;
+  // get_nodes_on_free_surface: every step when a later step reads its output (the
+  // traction-free BC, or XSPH's marks next to BC particles, or standard SPH's position
+  // copy after it); otherwise on demand when the state is downloaded, which gives the same
+  // values because nothing else in the step reads them
+  bool surf_every = false;
+  bool surf_stale = false;
 };
 
 struct Ctx {
@@ -45,6 +51,12 @@ struct Ctx {
   int* h_err = nullptr;  // pinned
   double* stage = nullptr;  // device staging for interleaved host arrays (4 x ntotal2)
   bool uploaded = false;
+  // get_nodes_on_free_surface: every step when a later step reads its output (the
+  // traction-free BC, or XSPH's marks next to BC particles, or standard SPH's position
+  // copy after it); otherwise on demand when the state is downloaded, which gives the same
+  // values because nothing else in the step reads them
+  bool surf_every = false;
+  bool surf_stale = false;
   int64_t steps_done = 0;
   int precision = SPS_PREC_FP64_PLAIN;
   std::string last_error;

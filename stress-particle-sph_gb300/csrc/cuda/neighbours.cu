@@ -525,16 +525,24 @@ __global__ void k_pair_meta(Dev D) {
     if (m.n > m.m) m.m = m.n;
     D.meta[r] = m;
   }
-  if (threadIdx.x == 0 && D.half_off[D.N2] > 2147483647LL) atomicOr(D.err, ERR_NPAIRS);
+  // walk-order keys hold 2 x position in 32 bits
+  if (threadIdx.x == 0 && D.half_off[D.N2] > 1073741823LL) atomicOr(D.err, ERR_NPAIRS);
 }
 
-__device__ __forceinline__ void reverse_ell(int4* base, int N2, int s, int lo, int hi) {
-  // reverse entries [lo, hi) of column s
+template <bool KEYS>
+__device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, int s, int lo,
+                                            int hi) {
+  // reverse entries [lo, hi) of column s (and their keys)
   hi--;
   while (lo < hi) {
     int4 t = base[(size_t)lo * N2 + s];
     base[(size_t)lo * N2 + s] = base[(size_t)hi * N2 + s];
     base[(size_t)hi * N2 + s] = t;
+    if (KEYS) {
+      int32_t k = key[(size_t)lo * N2 + s];
+      key[(size_t)lo * N2 + s] = key[(size_t)hi * N2 + s];
+      key[(size_t)hi * N2 + s] = k;
+    }
     lo++;
     hi--;
   }
@@ -545,6 +553,8 @@ __device__ __forceinline__ void reverse_ell(int4* base, int N2, int s, int lo, i
 // t's own half list.  The linked list of the reference is walked as: pairs created this
 // step beyond the previous list length m (newest first), then pairs 0..m-1 in creation
 // order; the lists are written in that walk order.
+// KEYS: also write the walk-order key of every entry (for the free-surface detection)
+template <bool KEYS>
 __global__ void k_lists(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
@@ -572,18 +582,31 @@ __global__ void k_lists(Dev D) {
       }
       lo[1] = D.cell_start[c0g + (ix > 0 ? c - 1 : c)];
       hi[1] = s;
-      auto push = [&](int u, int w, float gx, float gy, int64_t cidx) {
+      // key of an entry: its position in the walk order of the realisation's list, and
+      // whether the target is pair_i (creator of a same-type pair; the stress-point of a
+      // node--stress-point pair)
+      auto push = [&](int u, int w, float gx, float gy, int64_t cidx, bool own) {
         int ut = D.itype[u];
         int pt = pint_type(tt, ut);
         bool same = (pt == 2 || pt == 3);
         int4 e = make_int4(u, w, __float_as_int(gx), __float_as_int(gy));
-        bool isnew = reorder && cidx - meta.base >= meta.m_prev;
+        const int64_t rel = cidx - meta.base;
+        bool isnew = reorder && rel >= meta.m_prev;
+        int64_t wp = !reorder ? rel : isnew ? meta.n - 1 - rel : (meta.n - meta.m_prev) + rel;
+        int role = same ? (own ? 1 : 0) : (pt == 1 && is_sp(tt) ? 1 : 0);
+        int32_t key = (int32_t)(2 * wp + role);
         if (same) {
-          if (nS < D.capS) D.same[(size_t)nS * D.N2 + s] = e;
+          if (nS < D.capS) {
+            D.same[(size_t)nS * D.N2 + s] = e;
+            if (KEYS) D.keyS[(size_t)nS * D.N2 + s] = key;
+          }
           nS++;
           newS += isnew;
         } else if (pt != 0) {
-          if (nC < D.capC) D.cross[(size_t)nC * D.N2 + s] = e;
+          if (nC < D.capC) {
+            D.cross[(size_t)nC * D.N2 + s] = e;
+            if (KEYS) D.keyC[(size_t)nC * D.N2 + s] = key;
+          }
           nC++;
           newC += isnew;
         }
@@ -602,7 +625,7 @@ __global__ void k_lists(Dev D) {
           if (l < n && h[l].x == s) {
             int4 e = h[l];
             push(D.sorted[as], e.y, -__int_as_float(e.z), -__int_as_float(e.w),
-                 D.half_off[as] + l);
+                 D.half_off[as] + l, false);
           }
         }
       {
@@ -610,7 +633,8 @@ __global__ void k_lists(Dev D) {
         const int4* h = D.half + (size_t)s * D.capH;
         for (int k = 0; k < n; k++) {
           int4 e = h[k];
-          push(D.sorted[e.x], e.y, __int_as_float(e.z), __int_as_float(e.w), D.half_off[s] + k);
+          push(D.sorted[e.x], e.y, __int_as_float(e.z), __int_as_float(e.w), D.half_off[s] + k,
+               true);
         }
       }
       if (nC > D.capC || nS > D.capS) {
@@ -621,12 +645,12 @@ __global__ void k_lists(Dev D) {
       }
       // walk order: [new entries, descending creation] + [old entries, ascending]
       if (newC > 0) {
-        reverse_ell(D.cross, D.N2, s, 0, nC);
-        reverse_ell(D.cross, D.N2, s, newC, nC);
+        reverse_ell<KEYS>(D.cross, D.keyC, D.N2, s, 0, nC);
+        reverse_ell<KEYS>(D.cross, D.keyC, D.N2, s, newC, nC);
       }
       if (newS > 0) {
-        reverse_ell(D.same, D.N2, s, 0, nS);
-        reverse_ell(D.same, D.N2, s, newS, nS);
+        reverse_ell<KEYS>(D.same, D.keyS, D.N2, s, 0, nS);
+        reverse_ell<KEYS>(D.same, D.keyS, D.N2, s, newS, nS);
       }
     }
   }
@@ -742,8 +766,15 @@ int launch_pair_build(Ctx& c) {
   c.mark("pair_meta");
   k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("lists");
-  k_lists<<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
+  if (c.surf_every) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
+  else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
   return 0;
+}
+
+// the lists of the last step again, now with their walk-order keys (the on-demand
+// free-surface detection; the lists are rebuilt identically)
+void launch_lists_keys(Ctx& c) {
+  k_lists<true><<<c.grid_of(TK_LISTS, c.d.N2), c.blk[TK_LISTS], 0, c.stream>>>(c.d);
 }
 
 }  // namespace sps

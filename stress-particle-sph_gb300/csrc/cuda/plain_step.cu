@@ -215,7 +215,7 @@ __global__ void k_stage_begin(Dev D, int stage) {
     }
   }
   if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
-  apply_bcs(D, sc, i, vx, vy, a, b, c);
+  apply_bcs(D, sc, i, vx, vy, a, b, c, d);
   D.vx[i] = vx;
   D.vy[i] = vy;
   D.s0[i] = a;
@@ -319,7 +319,7 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (D.sp_sph) {
     if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
-    apply_bcs(D, sc, i, vx, vy, a, b, c);
+    apply_bcs(D, sc, i, vx, vy, a, b, c, d);
     D.vx[i] = vx;
     D.vy[i] = vy;
     D.s0[i] = a;
@@ -524,7 +524,7 @@ __global__ void k_rk_final(Dev D) {
     d = D.st0[3][i] + dt6 * D.RKs[3][i];
   }
   if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
-  apply_bcs(D, sc, i, vx, vy, a, b, c);
+  apply_bcs(D, sc, i, vx, vy, a, b, c, d);
   D.vx[i] = vx;
   D.vy[i] = vy;
   D.s0[i] = a;
@@ -722,6 +722,9 @@ int launch_plain_step(Ctx& c) {
     c.mark("trapezoid");
     k_trapezoid<<<nbT, kBlock, 0, st>>>(D);
   }
+  // get_nodes_on_free_surface after the position update (2_SPH_main_2018.f90:153); on
+  // demand instead when no later step reads it (Ctx::surf_every)
+  if (D.update_x && c.surf_every) launch_surface(c);
   c.mark("displ");
   k_displ<<<nbN, kBlock, 0, st>>>(D);
   c.mark("next_step");

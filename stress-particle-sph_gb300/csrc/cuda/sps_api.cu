@@ -189,7 +189,7 @@ std::string err_text(int e) {
   if (e & sps::ERR_HALF_CAP) m += "half-stencil pair capacity exceeded; ";
   if (e & sps::ERR_LIST_CAP) m += "neighbour list capacity exceeded (raise max_neighbours); ";
   if (e & sps::ERR_CELLS) m += "cell grid capacity exceeded; ";
-  if (e & sps::ERR_NPAIRS) m += "more than 2^31 pairs; ";
+  if (e & sps::ERR_NPAIRS) m += "more than 2^30 pairs; ";
   if (e & sps::ERR_BOUND) m += "more than 8 wall particles within 0.75 dx of a node; ";
   if (e & (1 << 20)) m += "non-finite value in the particle state; ";
   return m;
@@ -214,8 +214,6 @@ int check_params(const sps_params* p) {
     return fail(nullptr, SPS_ERR_UNSUPPORTED,
                 "only the Drucker-Prager law (ncrit = 12) or elastic (ntype_eco = 1) is implemented");
   if (p->skf < 1 || p->skf > 3) return fail(nullptr, SPS_ERR_ARG, "skf must be 1, 2 or 3");
-  if (p->ifsigman)
-    return fail(nullptr, SPS_ERR_UNSUPPORTED, "stress-free surface BC (ifsigman = 1) not implemented");
   if (p->no_bcs > sps::kMaxBC) return fail(nullptr, SPS_ERR_UNSUPPORTED, "more than 16 BCs");
   if (p->no_bcs > 0 && !p->bc_list) return fail(nullptr, SPS_ERR_ARG, "bc_list missing");
   if (!p->sp_sph && p->nstress != p->nnode)
@@ -350,6 +348,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.sp_sph = p->sp_sph;
     D.inside = p->inside_approach;
     D.no_bcs = p->no_bcs;
+    D.ifsigman = p->ifsigman;
+    c.surf_every = p->update_x && (p->ifsigman == 1 || (p->xsph && p->no_bcs > 0) || !p->sp_sph);
     D.pi = p->pi;
     for (int b = 0; b < p->no_bcs; b++) D.bcvar[b] = (int)p->bc_list[8 * (size_t)b + 1];
     const size_t N2 = D.N2, NT = D.NT, NN_ = D.NN;
@@ -397,6 +397,10 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.wallpos = dalloc<float>(c, N2);
     D.horiz = dalloc<float>(c, N2);
     D.grad_u = dalloc<double>(c, 4 * NT);
+    D.nrmx = dalloc<double>(c, NT);
+    D.nrmy = dalloc<double>(c, NT);
+    D.subset = dalloc<int8_t>(c, NT);
+    D.fint = dalloc<float>(c, NT);
     D.x0x = dalloc<double>(c, NT);
     D.x0y = dalloc<double>(c, NT);
     D.vx0 = dalloc<double>(c, NT);
@@ -457,6 +461,10 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     SPS_CUDA_CHECK(cudaMemsetAsync(D.gtot, 0, sizeof(sps::GridTotal), c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.err, 0, sizeof(int), c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.grad_u, 0, sizeof(double) * 4 * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.nrmx, 0, sizeof(double) * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.nrmy, 0, sizeof(double) * NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.subset, 0, NT, c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(D.fint, 0, sizeof(float) * NT, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_or_not, 0, sizeof(int32_t) * NT, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_info, 0, sizeof(int32_t) * 8 * NT, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bc_int, 0, sizeof(int32_t) * NN_, c.stream));
@@ -493,6 +501,18 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
   *out = h;
   return SPS_OK;
 }
+
+namespace {
+// the free-surface detection of the last step, when it was left for the download
+void refresh_surface(sps::Ctx& c) {
+  if (!c.surf_stale) return;
+  sps::launch_lists_keys(c);
+  sps::launch_surface(c);
+  SPS_CUDA_CHECK(cudaGetLastError());
+  SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  c.surf_stale = false;
+}
+}  // namespace
 
 int sps_upload(sps_ctx* h, const double* x, const double* vel, const double* stress,
                const double* mass, const double* rho, const double* hsml, const int32_t* itype,
@@ -621,6 +641,8 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
         D.half = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
         D.cross = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
         D.same = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
+        D.keyC = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
+        D.keyS = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.capH = D.capC = D.capS = capn;
         if (c.graph) {
           cudaGraphExecDestroy(c.graph);
@@ -644,6 +666,7 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
   bool all = true;
   for (const sps::HostReal& q : c.hr) all = all && q.uploaded;
   c.uploaded = all;
+  c.surf_stale = false;  // an uploaded state carries its own bc_or_not
   return SPS_OK;
 }
 
@@ -706,6 +729,7 @@ int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
     SPS_CUDA_CHECK(cudaMemcpyAsync(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     c.steps_done += nsteps;
+    if (c.d.update_x && !c.surf_every) c.surf_stale = true;
     for (int r = 0; r < R; r++) time_sph[r] = t[r];
     int e = *c.h_err;
     if (e) {
@@ -739,6 +763,7 @@ int sps_download_real(sps_ctx* h, int32_t r, double* x, double* vel, double* str
   Seg sg[3];
   segments(c, r, sg);
   try {
+    if (bc_or_not) refresh_surface(c);
     double* stage = c.stage;
     auto nbk = [](int64_t n) { return (int)((n + kBlock - 1) / kBlock); };
     auto down2 = [&](double* dst, const double* a, const double* b, int nseg, size_t n) {
@@ -774,6 +799,39 @@ int sps_download_real(sps_ctx* h, int32_t r, double* x, double* vel, double* str
       // dummy stress is pair-local in the reference; report zero like its RK4 clear (:690)
       for (size_t i = nt; i < n2; i++)
         for (int k = 0; k < 4; k++) stress[4 * i + k] = 0.0;
+    }
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_download_surface(sps_ctx* h, int32_t r, double* normal, int32_t* subset) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  sps::Dev& D = c.d;
+  if (r < 0 || r >= D.R) return fail(&c, SPS_ERR_ARG, "sps_download_surface: no such realisation");
+  Seg sg[3];
+  segments(c, r, sg);
+  try {
+    refresh_surface(c);
+    for (int k = 0; k < 2; k++) {  // nodes and stress-points
+      const Seg& q = sg[k];
+      if (q.n == 0) continue;
+      if (normal) {
+        std::vector<double> nx(q.n), ny(q.n);
+        SPS_CUDA_CHECK(cudaMemcpy(nx.data(), D.nrmx + q.g, sizeof(double) * q.n, cudaMemcpyDeviceToHost));
+        SPS_CUDA_CHECK(cudaMemcpy(ny.data(), D.nrmy + q.g, sizeof(double) * q.n, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < q.n; i++) {
+          normal[2 * (q.l + i)] = nx[i];
+          normal[2 * (q.l + i) + 1] = ny[i];
+        }
+      }
+      if (subset) {
+        std::vector<int8_t> sb(q.n);
+        SPS_CUDA_CHECK(cudaMemcpy(sb.data(), D.subset + q.g, q.n, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < q.n; i++) subset[q.l + i] = sb[i];
+      }
     }
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
@@ -951,6 +1009,7 @@ int sps_profile_step(sps_ctx* h, int32_t nsteps, double* time_sph, char* names, 
     SPS_CUDA_CHECK(cudaMemcpy(c.h_err, c.d.err, sizeof(int), cudaMemcpyDeviceToHost));
     for (int r = 0; r < c.d.R; r++) time_sph[r] = t[r];
     c.steps_done += nsteps;
+    if (c.d.update_x && !c.surf_every) c.surf_stale = true;
   } catch (const std::exception& e) {
     c.profiling = false;
     return fail(&c, SPS_ERR_CUDA, e.what());
@@ -1024,7 +1083,8 @@ std::vector<std::pair<void*, size_t>> carried_state(sps::Ctx& c) {
       {D.rho, d8 * N2},  {D.hsml, d8 * N2},  {D.vol, d8 * N2},     {D.rinv, d8 * N2},
       {D.iv1, d8 * NT},  {D.fdp, d8 * NT},   {D.grad_u, 4 * d8 * NT},
       {D.dispx, d8 * NN}, {D.dispy, d8 * NN}, {D.bc_or_not, sizeof(int32_t) * NT},
-      {D.out, N2},       {D.meta, sizeof(sps::PairMeta) * D.R}};
+      {D.out, N2},       {D.meta, sizeof(sps::PairMeta) * D.R},
+      {D.nrmx, d8 * NT}, {D.nrmy, d8 * NT}, {D.subset, NT}, {D.fint, sizeof(float) * NT}};
   if (D.fast) {
     v.push_back({D.recV, sizeof(float4) * N2});
     v.push_back({D.recS, sizeof(float4) * NT});
@@ -1061,6 +1121,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     };
     copy(true);
+    const bool stale = c.surf_stale;
     const int cand[] = {64, 128, 256, 512};
     int best[sps::TK_N];
     double best_ms[sps::TK_N];
@@ -1088,6 +1149,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       c.blk[k] = best[k];
       if (blocks) blocks[k] = best[k];
     }
+    c.surf_stale = stale;
     SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     cudaFree(snap);

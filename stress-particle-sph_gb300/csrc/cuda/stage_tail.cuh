@@ -11,23 +11,37 @@
 
 namespace sps {
 
-// Normal_BCs (3_SPH_material_2018.f90:1665-1770) for one particle
+// BCs (3_SPH_material_2018.f90:1640-1660) for one particle: Normal_BCs (:1665-1770), then
+// with ifsigman = 1 apply_stress_free (:1775-1858): a free-surface node away from the walls
+// keeps only the stress component along the surface (zero normal and shear traction)
 __device__ __forceinline__ void apply_bcs(const Dev& D, const StepScalars& sc, int ip, double& vx,
-                                          double& vy, double& s0, double& s1, double& s2) {
+                                          double& vy, double& s0, double& s1, double& s2,
+                                          double& s3) {
   if (D.no_bcs <= 0) return;
-  if (D.bc_or_not[ip] != 1) return;
-  const int32_t* bi = D.bc_info + 8 * (size_t)ip;
-  if (bi[1] == 0) return;
-  for (int r = 0; r < 5; r++) {
-    int bt = bi[r + 2];
-    if (bt == 0) continue;
-    double val = sc.bcval[bt - 1];
-    int var = D.bcvar[bt - 1];
-    if (var == 5) vx = val;
-    else if (var == 6) vy = val;
-    else if (var == 1) s0 = val;
-    else if (var == 3) s2 = val;
-    else if (var == 2) s1 = val;
+  const int bc = D.bc_or_not[ip];
+  if (bc == 1) {
+    const int32_t* bi = D.bc_info + 8 * (size_t)ip;
+    if (bi[1] == 0) return;
+    for (int r = 0; r < 5; r++) {
+      int bt = bi[r + 2];
+      if (bt == 0) continue;
+      double val = sc.bcval[bt - 1];
+      int var = D.bcvar[bt - 1];
+      if (var == 5) vx = val;
+      else if (var == 6) vy = val;
+      else if (var == 1) s0 = val;
+      else if (var == 3) s2 = val;
+      else if (var == 2) s1 = val;
+    }
+  } else if (D.ifsigman == 1 && bc == 2 && ip < D.NN && D.bc_int[ip] != 1) {
+    const double costh = D.nrmx[ip], sinth = D.nrmy[ip];
+    if (isnan(costh) || isnan(sinth)) return;
+    const double s2_ = sinth * sinth, c2 = costh * costh, sc_ = sinth * costh;
+    const double stt = (s2_ * s0 - (2.0 * sc_) * s2) + c2 * s1;
+    s0 = s2_ * stt;
+    s1 = c2 * stt;
+    s2 = -(sc_ * stt);
+    s3 = c2 * stt;
   }
 }
 

@@ -1,0 +1,192 @@
+// surface.cu -- get_nodes_on_free_surface (3_SPH_material_2018.f90:1135-1430) as gathers per
+// particle (compiled with -fmad=false: the reference's rounding, both forms).
+//
+// The routine's locals are `real` (FP32) and its module arrays normal and subset FP64; an
+// FP32 accumulation with an FP64 operand is evaluated in FP64 and rounded once.  Steps 1 and
+// 4 accumulate over node--stress-point and same-type pairs in the order of the reference's
+// linked list: a particle merges its two neighbour lists by their walk-order keys (written
+// by k_lists), which restores that order.  Step 3 (is a neighbour inside the particle's scan
+// region?) does not depend on the order.
+//   k_fs_normal0  steps 1-2: renormalisation matrix, kernel-gradient sums, first normal
+//   k_fs_scan     step 3 + the bc_or_not update: subset (1 surface, 2 inside), f_int
+//   k_fs_normal   step 4: normals of surface particles from their surface neighbours
+#include <cuda_runtime.h>
+
+#include "ctx.cuh"
+
+namespace sps {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+// the merged walk over a target's node--stress-point (cross, non-dummy neighbour) and
+// same-type entries, in ascending key; f(u, gx, gy, is_pair_i)
+template <typename F>
+__device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
+  const int nC = D.degC[s], nS = D.degS[s];
+  int a = 0, b = 0;
+  int32_t ka = 0, kb = 0;
+  int4 ea = make_int4(0, 0, 0, 0), eb = make_int4(0, 0, 0, 0);
+  auto next_cross = [&]() {
+    while (a < nC) {
+      ea = D.cross[(size_t)a * D.N2 + s];
+      if (!is_dummy(D.itype[ea.x])) {
+        ka = D.keyC[(size_t)a * D.N2 + s];
+        return;
+      }
+      a++;
+    }
+  };
+  next_cross();
+  if (b < nS) {
+    eb = D.same[(size_t)b * D.N2 + s];
+    kb = D.keyS[(size_t)b * D.N2 + s];
+  }
+  while (a < nC || b < nS) {
+    bool takeC = (a < nC) && (b >= nS || ka < kb);
+    if (takeC) {
+      f(ea.x, __int_as_float(ea.z), __int_as_float(ea.w), (ka & 1) != 0);
+      a++;
+      next_cross();
+    } else {
+      f(eb.x, __int_as_float(eb.z), __int_as_float(eb.w), (kb & 1) != 0);
+      b++;
+      if (b < nS) {
+        eb = D.same[(size_t)b * D.N2 + s];
+        kb = D.keyS[(size_t)b * D.N2 + s];
+      }
+    }
+  }
+}
+
+// hf = (m_u G / rho_u) rounded to FP32; G is the gradient with respect to the target, which
+// gives the reference's hf1i (target pair_i) and hf1j = -(m_i gradW / rho_i) (target pair_j).
+// The quotient is the corrected division by the exact reciprocal 1/rho_u (the IEEE quotient,
+// bit for bit) instead of an FP64 division per neighbour.
+__device__ __forceinline__ float hf_of(const Dev& D, int u, float g) {
+  return (float)div_rcp(D.mass[u] * (double)g, D.rho[u], D.rinv[u]);
+}
+
+__global__ void k_fs_normal0(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int t = D.sorted[s];
+  if (t >= D.NT) return;
+  const double xt = D.px[t], yt = D.py[t];
+  float A0 = 0.0f, A1 = 0.0f, A2 = 0.0f, A3 = 0.0f, f0 = 0.0f, f1 = 0.0f;
+  walk_123(D, s, [&](int u, float gx, float gy, bool) {
+    float h1 = hf_of(D, u, gx), h2 = hf_of(D, u, gy);
+    double dx = D.px[u] - xt, dy = D.py[u] - yt;
+    A0 = (float)((double)A0 + dx * (double)h1);
+    A1 = (float)((double)A1 + dy * (double)h1);
+    A2 = (float)((double)A2 + dx * (double)h2);
+    A3 = (float)((double)A3 + dy * (double)h2);
+    f0 = f0 + h1;
+    f1 = f1 + h2;
+  });
+  if (fabsf(A0) <= 1.e-8f) A0 = 0.0f;
+  if (fabsf(A1) <= 1.e-8f) A1 = 0.0f;
+  if (fabsf(A2) <= 1.e-8f) A2 = 0.0f;
+  if (fabsf(A3) <= 1.e-8f) A3 = 0.0f;
+  float v0 = -(A0 * f0 + A1 * f1);
+  float v1 = -(A2 * f0 + A3 * f1);
+  float v2 = sqrtf(v0 * v0 + v1 * v1);
+  D.nrmx[t] = (double)(v0 / v2);
+  D.nrmy[t] = (double)(v1 / v2);
+}
+
+// scan region of particle a against a neighbour at (xb, yb): true when the neighbour lies in
+// it (then a is not on the surface)
+__device__ __forceinline__ bool in_scan_region(const Dev& D, int a, double xb, double yb) {
+  const double nx = D.nrmx[a], ny = D.nrmy[a], ha = D.hsml[a];
+  const float tt0 = (float)(D.px[a] + ha * nx), tt1 = (float)(D.py[a] + ha * ny);
+  const float tau0 = (float)(-ny), tau1 = (float)nx;
+  double ddx = xb - D.px[a], ddy = yb - D.py[a];
+  float xba = (float)sqrt(ddx * ddx + ddy * ddy);
+  float xbt0 = (float)(xb - (double)tt0), xbt1 = (float)(yb - (double)tt1);
+  float xbt_norm = sqrtf(xbt0 * xbt0 + xbt1 * xbt1);
+  float prod = (float)(fabs(nx * (double)xbt0 + ny * (double)xbt1) +
+                       (double)fabsf(tau0 * xbt0 + tau1 * xbt1));
+  float limit = (float)((double)sqrtf(2.0f) * ha);
+  if (xba >= limit && (double)xbt_norm < ha) return true;
+  if (xba < limit && (double)prod < ha) return true;
+  return false;
+}
+
+__global__ void k_fs_scan(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int t = D.sorted[s];
+  if (t >= D.NT) return;
+  bool inside = false;
+  const int nS = D.degS[s], nC = D.degC[s];
+  for (int k = 0; k < nS && !inside; k++) {
+    int u = D.same[(size_t)k * D.N2 + s].x;
+    inside = in_scan_region(D, t, D.px[u], D.py[u]);
+  }
+  for (int k = 0; k < nC && !inside; k++) {
+    int u = D.cross[(size_t)k * D.N2 + s].x;
+    if (is_dummy(D.itype[u])) inside = in_scan_region(D, t, D.px[u], D.py[u]);
+  }
+  int sub = inside ? 2 : 1;
+  D.fint[t] = inside ? -1.0f : 0.0f;
+  int bc = D.bc_or_not[t];
+  if (bc != 1) bc = (sub == 1) ? 2 : 0;
+  else if (sub == 1) sub = 2;
+  D.bc_or_not[t] = bc;
+  D.subset[t] = (int8_t)sub;
+}
+
+__global__ void k_fs_normal(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int t = D.sorted[s];
+  if (t >= D.NT) return;
+  const bool surf = D.subset[t] == 1;
+  const float ft = D.fint[t];
+  const float xtf = (float)D.px[t], ytf = (float)D.py[t];
+  double nx = 0.0, ny = 0.0;
+  float nb = 0.0f, g0 = 0.0f, g1 = 0.0f;
+  walk_123(D, s, [&](int u, float gx, float gy, bool pair_i) {
+    if (surf && D.subset[u] == 1) {
+      // the reference adds the same vector x_j - x_i to both particles of the pair
+      float xu = (float)D.px[u], yu = (float)D.py[u];
+      float xv = pair_i ? xu - xtf : xtf - xu;
+      float yv = pair_i ? yu - ytf : ytf - yu;
+      nx = nx - (double)yv;
+      ny = ny + (double)xv;
+      nb = nb + 1.0f;
+    }
+    float h1 = hf_of(D, u, gx), h2 = hf_of(D, u, gy);
+    float df = D.fint[u] - ft;
+    g0 = g0 + df * h1;
+    g1 = g1 + df * h2;
+  });
+  if (surf) {
+    nx = nx / (double)nb;
+    ny = ny / (double)nb;
+    float nv = (float)sqrt(nx * nx + ny * ny);
+    nx = nx / (double)nv;
+    ny = ny / (double)nv;
+    float p = (float)((double)g0 * nx + (double)g1 * ny);
+    if (p < 0) {
+      nx = -nx;
+      ny = -ny;
+    }
+  }
+  D.nrmx[t] = nx;
+  D.nrmy[t] = ny;
+}
+
+}  // namespace
+
+void launch_surface(Ctx& c) {
+  const int nb = (c.d.N2 + kBlock - 1) / kBlock;
+  c.mark("surface", 3);
+  k_fs_normal0<<<nb, kBlock, 0, c.stream>>>(c.d);
+  k_fs_scan<<<nb, kBlock, 0, c.stream>>>(c.d);
+  k_fs_normal<<<nb, kBlock, 0, c.stream>>>(c.d);
+}
+
+}  // namespace sps

@@ -183,6 +183,10 @@ def declare_step_api(lib, prefix):
     f.argtypes = [vp, P(c_int32), P(c_int32), P(c_int32), P(c_float), P(c_float), P(c_float),
                   P(C.c_int64)]
     f.restype = C.c_int
+    f = getattr(lib, prefix + "_download_surface")
+    f.argtypes = ([vp] + ([c_int32] if prefix == "sps" else []) +
+                  [P(c_double), P(c_int32)])
+    f.restype = C.c_int
     f = getattr(lib, prefix + "_destroy")
     f.argtypes = [vp]
     f.restype = None

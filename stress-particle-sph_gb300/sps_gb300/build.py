@@ -27,6 +27,7 @@ CUDA_UNITS = [
     ("cuda/neighbours.cu", ["-fmad=false"]),
     ("cuda/plain_step.cu", ["-fmad=false"]),
     ("cuda/fast_step.cu", []),
+    ("cuda/surface.cu", ["-fmad=false"]),
     ("cuda/mlp_train.cu", []),
     ("cuda/neighbour_stats_static.cu", ["-fmad=false"]),
 ]

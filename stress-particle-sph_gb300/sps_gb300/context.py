@@ -124,6 +124,15 @@ class StepContext:
                    _ip(out["bc_or_not"]), _dp(out["f_drucker"]))
         return out
 
+    def download_surface(self, r=0):
+        """(normal (2,ntotal), subset (ntotal)) of the last free-surface detection."""
+        nt = self.ntotal if not hasattr(self, "problems") else self.problems[r].ntotal
+        normal = np.empty(2 * nt)
+        subset = np.empty(nt, np.int32)
+        args = ([r] if self._pre == "sps" else []) + [_dp(normal), _ip(subset)]
+        self._call("download_surface", self._h, *args)
+        return normal, subset
+
     def dump_pairs(self):
         n = C.c_int64(0)
         N = None

@@ -38,6 +38,10 @@ def _compare(problem, nsteps, chunks=None, pairs=True, **over):
     fg, fo = g.download(), o.download()
     cases.assert_bitwise(fg, fo, problem.ntotal)
     np.testing.assert_array_equal(fg["bc_or_not"], fo["bc_or_not"])
+    (ng, sg), (no, so) = g.download_surface(), o.download_surface()
+    np.testing.assert_array_equal(sg, so, err_msg="subset")
+    same = (ng.view(np.int64) == no.view(np.int64)) | (np.isnan(ng) & np.isnan(no))
+    assert same.all(), ("surface normal", np.nonzero(~same)[0][:10])
     return fg
 
 
@@ -83,6 +87,14 @@ def test_boundary_conditions(built_gpu):
     _compare(p, 20, chunks=[20])
 
 
+def test_stress_free_surface(built_gpu):
+    # ifsigman = 1: free-surface nodes away from the walls get zero normal and shear
+    # traction after every BC application (apply_stress_free)
+    p = cases.bc_case(plastic=True, cspm=False, xsph=True)
+    f = _compare(p, 20, chunks=[5, 15], ifsigman=1)
+    assert (f["bc_or_not"] == 2).any()
+
+
 def test_standard_sph(built_gpu):
     p = cases.standard_sph()
     _compare(p, 6)
@@ -115,7 +127,7 @@ def test_capacity_error(built_gpu):
 
 def test_unsupported_options(built_gpu):
     p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
-    for over in (dict(art_stress=1), dict(ifsigman=1), dict(inside_approach=0), dict(skf=7)):
+    for over in (dict(art_stress=1), dict(inside_approach=0), dict(skf=7)):
         with pytest.raises(sps_gb300.SpsError):
             _gpu_ctx(p, **over)
 
