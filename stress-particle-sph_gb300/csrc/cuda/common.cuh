@@ -162,6 +162,9 @@ struct Dev {
   int4 *cross, *same;
   int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)
   int32_t *degC, *degS;
+  // FP32 form: sorted positions of the stress-point and of the node targets (each in
+  // sorted order), so that the gathers run one kind per warp
+  int32_t *tgtS, *tgtN, *tflag, *toff;
   // get_nodes_on_free_surface: normal (module FP64), subset (1 surface, 2 inside), f_int
   double *nrmx, *nrmy;
   int8_t* subset;

@@ -60,9 +60,19 @@ __device__ __forceinline__ float dfdiff(float ah, float al, float bh, float bl) 
 // stress_point_update (2_SPH_main_2018.f90:403-482), FP32 sums.  A stress-point's velocity
 // is the weighted mean of its nodes' velocities; it is formed as the first node's velocity
 // plus the weighted mean of the deviations, which are small and exact in double-float.
-__global__ void k_finterp(Dev D) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
+// KIND 0: every particle (sorted positions); 1: the stress-point targets tgt[0..n); 2: the
+// node targets (no divergence between the two branches inside a warp)
+template <int KIND>
+__global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int s;
+  if (KIND == 0) {
+    s = k;
+    if (s >= D.N2) return;
+  } else {
+    if (k >= ntgt) return;
+    s = tgt[k];
+  }
   int t = D.sorted[s];
   if (t >= D.NT) return;
   int tt = D.itype[t];
@@ -83,7 +93,7 @@ __global__ void k_finterp(Dev D) {
     return;
   }
   int deg = D.degC[s];
-  if (is_sp(tt)) {
+  if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     Kahan v0, v1, nm;
     bool have = false;
     float4 ref = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -146,11 +156,14 @@ __global__ void k_finterp(Dev D) {
 // Node side: sum_u m (A_t + A_u) dW = sum_u m (A_u - A_t) dW + 2 A_t sum_u m dW, with
 // A = sigma / rho^2.  The first sum has small terms (double-float differences); the second
 // is a sum of exact products.  This keeps the near-cancelling stress divergence accurate.
-__global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
+// KIND 1: the stress-point targets tgt[0..n), 2: the node targets
+template <int KIND>
+__global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage,
+                                                    const int32_t* __restrict__ tgt, int ntgt) {
+  const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k0 >= ntgt) return;
+  const int s = tgt[k0];
   int t = D.sorted[s];
-  if (t >= D.NT) return;
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
   const double f2 = f2rk[stage];
   const Real& Mt = real_of(D, t);
@@ -158,7 +171,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
   int tt = D.itype[t];
   int deg = D.degC[s];
   const double xt = D.px[t], yt = D.py[t];
-  if (is_sp(tt)) {
+  if (KIND == 1) {
     Kahan g0, g1, g2, g3, e0, e1, e2, e3;
     const double vtx = D.vx[t], vty = D.vy[t];
     const float vh0 = (float)vtx, vh1 = (float)vty;
@@ -207,7 +220,7 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage) {
     double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
     double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
     tail_sp_grad(D, t, g, AE);  // the rates follow in k_fsp_tail
-  } else if (is_node(tt)) {
+  } else {
     Kahan q0, q1, q2, q3, q4, q5, e0, e1, e2, e3;
     ProdSum sx, sy;
     const float4 ah = D.recA[t], al = D.recAl[t];
@@ -439,11 +452,24 @@ __global__ void k_fxsph(Dev D) {
 
 }  // namespace
 
+// the targets split by kind (k_split_targets) after the pair build; one launch per kind
 void launch_finterp(Ctx& c) {
-  k_finterp<<<c.grid_of(TK_INTERP, c.d.N2), c.blk[TK_INTERP], 0, c.stream>>>(c.d);
+  const Dev& D = c.d;
+  const int ns = D.NT - D.NN, b = c.blk[TK_INTERP];
+  if (!D.sp_sph) {
+    k_finterp<0><<<c.grid_of(TK_INTERP, D.N2), b, 0, c.stream>>>(D, nullptr, 0);
+    return;
+  }
+  c.kernels_launched += 1;
+  if (ns > 0) k_finterp<1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, D.tgtS, ns);
+  k_finterp<2><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, D.tgtN, D.NN);
 }
 void launch_fderivs(Ctx& c, int stage) {
-  k_fderivs<<<c.grid_of(TK_DERIVS, c.d.N2), c.blk[TK_DERIVS], 0, c.stream>>>(c.d, stage);
+  const Dev& D = c.d;
+  const int ns = D.NT - D.NN, b = c.blk[TK_DERIVS];
+  c.kernels_launched += 1;
+  if (ns > 0) k_fderivs<1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
+  k_fderivs<2><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
 }
 void launch_fsp_tail(Ctx& c, int stage) {
   int ns = c.d.NT - c.d.NN;

@@ -737,6 +737,21 @@ void scan_impl(Ctx& c, const TI* in, TO* out, int n) {
 void scan_i32_to_i32(Ctx& c, const int32_t* in, int32_t* out, int n) { scan_impl(c, in, out, n); }
 void scan_i32_to_i64(Ctx& c, const int32_t* in, int64_t* out, int n) { scan_impl(c, in, out, n); }
 
+// FP32 form: flags (stress-point, node) of every sorted position, for the compaction below
+__global__ void k_target_flags(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  int t = D.sorted[s];
+  D.tflag[s] = (t >= D.NN && t < D.NT) ? 1 : 0;
+  D.tflag[D.N2 + s] = t < D.NN ? 1 : 0;
+}
+__global__ void k_target_scatter(Dev D) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  if (D.tflag[s]) D.tgtS[D.toff[s]] = s;
+  if (D.tflag[D.N2 + s]) D.tgtN[D.toff[D.N2 + 1 + s]] = s;
+}
+
 int launch_pair_build(Ctx& c) {
   Dev& D = c.d;
   cudaStream_t st = c.stream;
@@ -768,6 +783,13 @@ int launch_pair_build(Ctx& c) {
   c.mark("lists");
   if (c.surf_every) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
   else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
+  if (D.fast && D.sp_sph) {
+    c.mark("split_targets", 8);
+    k_target_flags<<<nb, kBlock, 0, st>>>(D);
+    scan_i32_to_i32(c, D.tflag, D.toff, D.N2);
+    scan_i32_to_i32(c, D.tflag + D.N2, D.toff + D.N2 + 1, D.N2);
+    k_target_scatter<<<nb, kBlock, 0, st>>>(D);
+  }
   return 0;
 }
 

@@ -214,7 +214,10 @@ __global__ void k_stage_begin(Dev D, int stage) {
       }
     }
   }
-  if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
+  // the FP32 form returns only stress that changed since the last return: a node's
+  // stress is unchanged since the previous k_adapt_bc (or zero after k_step_init), and
+  // returning it again would change it by rounding only
+  if (M.ncrit == 12 && (!D.fast || i >= D.NN)) stress_return(D, M, a, b, c, d);
   apply_bcs(D, sc, i, vx, vy, a, b, c, d);
   D.vx[i] = vx;
   D.vy[i] = vy;
@@ -318,7 +321,9 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (D.sp_sph) {
-    if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
+    // FP32 form: a stress-point's stress is unchanged since k_stage_begin / k_rk_final
+    // returned it; only the interpolated node stress needs the return here
+    if (M.ncrit == 12 && (!D.fast || i < D.NN)) stress_return(D, M, a, b, c, d);
     apply_bcs(D, sc, i, vx, vy, a, b, c, d);
     D.vx[i] = vx;
     D.vy[i] = vy;
@@ -523,7 +528,8 @@ __global__ void k_rk_final(Dev D) {
     c = D.st0[2][i] + dt6 * D.RKs[2][i];
     d = D.st0[3][i] + dt6 * D.RKs[3][i];
   }
-  if (M.ncrit == 12) stress_return(D, M, a, b, c, d);
+  // FP32 form: node stress is unchanged since the last k_adapt_bc
+  if (M.ncrit == 12 && (!D.fast || i >= D.NN)) stress_return(D, M, a, b, c, d);
   apply_bcs(D, sc, i, vx, vy, a, b, c, d);
   D.vx[i] = vx;
   D.vy[i] = vy;
