@@ -81,6 +81,31 @@ typedef struct sph_slope_spec {
 int sph_problem_slope(const sph_slope_spec* spec, sph_problem** out);
 
 const sps_params* sph_problem_params(const sph_problem* p);
+
+/* The output flags read by problem_input_data (code/3_SPH_material_2018.f90:333-336):
+   stress_out(1:4), vel_out(1:2), strain_out, rho_out, sml_out, disp_out. */
+int sph_problem_output_flags(const sph_problem* p, int32_t* flags);
+
+/* OutputRes (code/3_SPH_material_2018.f90:2750-3010) for a driver without the Fortran
+   writers.  In directory dir: nodes.csv.NNNNNN, stress_points.csv.NNNNNN and
+   surface_points.csv.NNNNNN (NNNNNN = itimestep) with the columns the output flags select,
+   F16.8 fields, separators and headers as the reference writes them; and the step's GiD
+   result blocks (displacement, velocity, sxx/syy/sxy, plastic strain) appended to
+   <name>.post.res.  Arrays in the reference layout as sps_download returns them: x, vel
+   (2,ntotal2), stress (4,ntotal2), intvars1, rho, hsml, bc_or_not (ntotal), displ
+   (2,nnode); intvars1, rho, hsml, bc_or_not and displ may be NULL (written as 0).  The
+   list-directed lines (surface points, GiD) have compiler-specific spacing in the
+   reference; here each value is one blank-separated field with 17 significant digits. */
+int sph_write_output(sph_problem* p, const char* dir, int32_t itimestep, double time_sph,
+                     const double* x, const double* vel, const double* stress,
+                     const double* intvars1, const double* rho, const double* hsml,
+                     const int32_t* bc_or_not, const double* displ);
+
+/* OutputMesh (code/3_SPH_material_2018.f90:2707-2744): <name>.post.msh with the initial
+   node coordinates and, for problems built by the rectangle generator, its quadrilateral
+   cells numbered as Read_2DMesh numbers them (code/3_SPH_material_2018.f90:515-532); then
+   starts <name>.post.res with the GiD header. */
+int sph_write_mesh(sph_problem* p, const char* dir);
 int sph_problem_get_arrays(sph_problem* p, sph_problem_arrays* out);
 int32_t sph_problem_nblocks(const sph_problem* p);
 int sph_problem_block(const sph_problem* p, int32_t i, sph_run_block* out);

@@ -210,6 +210,30 @@ int sps_dump_pairs_real(sps_ctx* ctx, int32_t r, int32_t* pair_i, int32_t* pair_
                         int32_t* pint_type, float* w, float* dwdx, float* dwdy,
                         int64_t* npairs);
 
+/* Output staging without a host stall (no reference counterpart: the reference writes
+   its output files from host arrays between steps: out_plot -> OutputRes,
+   code/1_SPH_2018.f90:90-93,117-121 and code/3_SPH_material_2018.f90:2919).  sps_snapshot enqueues on
+   the context stream a device-to-device copy of the fields sps_download returns (for every
+   realisation; the free surface is refreshed first when it was left for the download),
+   then copies that buffer to pinned host memory on a second stream, so that the
+   sps_step calls that follow run while the copy is in flight.  sps_snapshot_wait blocks
+   until the copy has finished and returns realisation r's fields exactly as
+   sps_download_real would have at the snapshot (same arguments, any may be NULL);
+   *step (may be NULL) receives the number of steps the context had taken then.  One
+   snapshot is held: waiting again returns the same one, a new sps_snapshot replaces it. */
+int sps_snapshot(sps_ctx* ctx);
+int sps_snapshot_wait(sps_ctx* ctx, int32_t r, double* x, double* vel, double* stress,
+                      double* rho, double* intvars1, double* displ, int32_t* bc_or_not,
+                      double* f_drucker, int64_t* step);
+/* sps_snapshot_wait without the copy: blocks the same way, then points each non-NULL
+   argument at realisation r's field inside the snapshot's pinned host buffer (same layout
+   as sps_download).  The pointers stay valid until the next sps_snapshot or
+   sps_destroy. */
+int sps_snapshot_view(sps_ctx* ctx, int32_t r, const double** x, const double** vel,
+                      const double** stress, const double** rho, const double** intvars1,
+                      const double** displ, const int32_t** bc_or_not, const double** f_drucker,
+                      int64_t* step);
+
 /* Copy the last error message of this context (or of the last failed sps_create when
    ctx is NULL) into buf (NUL-terminated, truncated to len). Returns its length. */
 int sps_last_error(sps_ctx* ctx, char* buf, int32_t len);

@@ -246,6 +246,24 @@ __device__ __forceinline__ double f64_of(float f) {
   return __longlong_as_double((long long)(((unsigned long long)h32 << 32) | l32));
 }
 
+// (float)(a / b) of the IEEE double quotient, given y = RN(1/b), with one FP64 multiply in
+// almost every case.  q = RN(a y) is within 3 double ulps of RN(a / b) (y and the product
+// each add at most half an ulp of relative error).  When the 29 significand bits that the
+// float rounding drops are at least 8 away from the float rounding boundaries (0, the
+// half-way point, 2^29: the low 28 of them in [8, 2^28 - 8]), every double within 3 ulps of q
+// has the same exponent and rounds to the same float, so f32_rn(q) is the answer.
+// Otherwise (about one case in 2^24), and outside f32_rn's exponent range (zero included),
+// the correctly rounded quotient div_rcp(a, b, y) is rounded instead.  Checked against the
+// IEEE division bit for bit by sps_selftest_division.
+__device__ __forceinline__ float div_rcp_f32(double a, double b, double y) {
+  const double q = a * y;
+  const unsigned long long u = (unsigned long long)__double_as_longlong(q);
+  const int E = (int)((u >> 52) & 0x7FFu);
+  const unsigned m28 = (unsigned)u & 0x0FFFFFFFu;
+  if (E >= 897 && E <= 1150 && (m28 - 8u) <= 0x0FFFFFF0u) return f32_rn(q);
+  return f32_rn(div_rcp(a, b, y));
+}
+
 // ----------------------------------------------------------------------------------------
 // kernel (example_problems/soil_failure_bui_et_al_2008/2_SPH_main_2018.f90:1440-1538).
 // FP64 with the FP32 literal 2./3. (:1480); x**n expanded into multiplications.

@@ -49,7 +49,9 @@ struct Ctx {
   int scal_cap = 0;  // steps
   std::vector<StepScalars> h_scal;
   int* h_err = nullptr;  // pinned
-  double* stage = nullptr;  // device staging for interleaved host arrays (4 x ntotal2)
+  unsigned long long* h_chk = nullptr;  // pinned: upload checks and extents
+  unsigned long long* d_chk = nullptr;
+  double* stage = nullptr;  // device staging for interleaved host arrays (10 x ntotal2)
   bool uploaded = false;
   // get_nodes_on_free_surface: every step when a later step reads its output (the
   // traction-free BC, or XSPH's marks next to BC particles, or standard SPH's position
@@ -74,6 +76,17 @@ struct Ctx {
   uint2* mlp_frag = nullptr;
   float* mlp_bias = nullptr;
   unsigned long long* surr_cnt = nullptr;
+  // output snapshot (sps_snapshot): device copy of the output fields, pinned host copy,
+  // the stream that moves one to the other, and the events that order them
+  char* snap_dev = nullptr;
+  char* snap_host = nullptr;
+  size_t snap_bytes = 0;
+  std::vector<int64_t> snap_roff;  // byte offset of each realisation's block
+  cudaStream_t snap_stream = nullptr;
+  cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
+  bool snap_pending = false;  // a snapshot was taken and not yet waited for
+  bool snap_valid = false;    // snap_host holds a completed snapshot
+  int64_t snap_step = 0;      // steps_done when it was taken
   int blk[TK_N] = {256, 256, 256, 256, 256, 256, 256, 256};  // block sizes (sps_autotune)
   int grid_of(int k, int n) const { return (n + blk[k] - 1) / blk[k]; }
   int64_t kernels_launched = 0;  // kernels enqueued by the launch functions

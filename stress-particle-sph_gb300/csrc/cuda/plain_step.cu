@@ -633,6 +633,14 @@ __global__ void k_selftest_div(int64_t n, uint64_t seed, unsigned long long* bad
     double y = 1.0 / b;
     double q1 = div_rcp(a, b, y), q2 = a / b;
     if (__double_as_longlong(q1) != __double_as_longlong(q2)) nb++;
+    // the float rounding of the quotient, also where the float boundary is near: a scaled
+    // so that a / b sits within a few double ulps of a float or of a float half-way point
+    if (__float_as_uint(div_rcp_f32(a, b, y)) != __float_as_uint((float)q2)) nb++;
+    const float f2 = (float)q2;
+    const double near = (r3 & 4) ? 0.5 * ((double)f2 + (double)nextafterf(f2, 2.0f * f2)) : (double)f2;
+    const double a2 = near * b + (double)((int)((r3 >> 8) & 7) - 3) * ldexp(near * b, -52);
+    const double q3 = a2 / b;
+    if (__float_as_uint(div_rcp_f32(a2, b, y)) != __float_as_uint((float)q3)) nb++;
   }
   if (nb) atomicAdd(bad, nb);
 }

@@ -118,6 +118,146 @@ __global__ void k_soa_to_aos2(double* out, const double* a, const double* b, int
     out[2 * (size_t)i + 1] = b[i];
   }
 }
+
+// ordered key of a double: unsigned order of the keys = numeric order of the values
+__device__ __forceinline__ unsigned long long up_key(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+double up_unkey(unsigned long long k) {
+  unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+__device__ __forceinline__ bool up_nonfinite(double v) {
+  return ((unsigned long long)__double_as_longlong(v) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+}
+
+// the checks and extents of an upload, over the realisation's local ids l (nodes, then
+// stress-points, then dummies, at global ids g0[k] + offset): out[0..5] = min x, min y,
+// max x, max y, max h, min h over nodes and dummies (keys; the complement of the key for
+// the maxima); out[6] = particles whose itype does not match their place (2 nodes,
+// 1 stress-points, 25 dummies); out[7] = particles with a non-finite x, y or h
+__global__ void k_upload_check(const int32_t* itype, const double* px, const double* py,
+                               const double* hsml, int64_t g0n, int64_t nn, int64_t g0s,
+                               int64_t ns, int64_t g0d, int64_t nd, unsigned long long* out) {
+  unsigned long long v[6] = {~0ull, ~0ull, ~0ull, ~0ull, ~0ull, ~0ull};
+  unsigned long long bad = 0, nonfin = 0;
+  const int64_t n2 = nn + ns + nd;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n2;
+       l += (int64_t)gridDim.x * blockDim.x) {
+    int64_t g;
+    int want;
+    if (l < nn) {
+      g = g0n + l;
+      want = 2;
+    } else if (l < nn + ns) {
+      g = g0s + (l - nn);
+      want = 1;
+    } else {
+      g = g0d + (l - nn - ns);
+      want = 25;
+    }
+    bad += itype[g] != want;
+    double x = px[g], y = py[g], h = hsml[g];
+    if (up_nonfinite(x) || up_nonfinite(y) || up_nonfinite(h)) {
+      nonfin++;
+      continue;
+    }
+    unsigned long long k[5] = {up_key(x), up_key(y), ~up_key(x), ~up_key(y), ~up_key(h)};
+    for (int q = 0; q < 5; q++) v[q] = k[q] < v[q] ? k[q] : v[q];
+    if (want != 1) {
+      unsigned long long kh = up_key(h);
+      v[5] = kh < v[5] ? kh : v[5];
+    }
+  }
+  __shared__ unsigned long long sh[32][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 16; o; o >>= 1) {
+    for (int q = 0; q < 6; q++) {
+      unsigned long long u = __shfl_xor_sync(0xffffffffu, v[q], o);
+      v[q] = u < v[q] ? u : v[q];
+    }
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    nonfin += __shfl_xor_sync(0xffffffffu, nonfin, o);
+  }
+  if (lane == 0) {
+    for (int q = 0; q < 6; q++) sh[w][q] = v[q];
+    sh[w][6] = bad;
+    sh[w][7] = nonfin;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int q = 0; q < 8; q++) {
+      const bool sum = q >= 6;
+      unsigned long long a = lane < nw ? sh[lane][q] : (sum ? 0ull : ~0ull);
+      for (int o = 16; o; o >>= 1) {
+        unsigned long long u = __shfl_xor_sync(0xffffffffu, a, o);
+        a = sum ? a + u : (u < a ? u : a);
+      }
+      if (lane == 0) {
+        if (sum) {
+          if (a) atomicAdd(&out[q], a);
+        } else {
+          atomicMin(&out[q], a);
+        }
+      }
+    }
+  }
+}
+
+// Output snapshot: every realisation's fields in the layout sps_download returns them, one
+// block per realisation at byte offset roff[r]: x(2,n2) vel(2,n2) stress(4,n2) rho(n2)
+// intvars1(nt) f_drucker(nt) displ(2,nn) bc_or_not(nt) (dummy stress written as 0)
+struct SnapBlock {
+  size_t x, vel, stress, rho, iv1, fdp, displ, bc, bytes;
+};
+__host__ __device__ inline SnapBlock snap_block(int64_t nn, int64_t nt, int64_t n2) {
+  SnapBlock b;
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  b.x = 0;
+  b.vel = b.x + up(16 * n2);
+  b.stress = b.vel + up(16 * n2);
+  b.rho = b.stress + up(32 * n2);
+  b.iv1 = b.rho + up(8 * n2);
+  b.fdp = b.iv1 + up(8 * nt);
+  b.displ = b.fdp + up(8 * nt);
+  b.bc = b.displ + up(16 * nn);
+  b.bytes = b.bc + up(4 * nt);
+  return b;
+}
+__global__ void k_snap_pack(sps::Dev D, char* out, const int64_t* roff) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= D.N2) return;
+  const int r = D.R == 1 ? 0 : D.rid[g];
+  const sps::Real& M = sps::real_of(D, g);
+  const int64_t nn = M.nnode, nt = nn + M.nsp, n2 = nt + M.ndum;
+  int64_t l;
+  if (g < D.NN) l = g - M.node0;
+  else if (g < D.NT) l = nn + (g - M.sp0);
+  else l = nt + (g - M.dum0);
+  const SnapBlock b = snap_block(nn, nt, n2);
+  char* base = out + roff[r];
+  double2* x = reinterpret_cast<double2*>(base + b.x);
+  double2* v = reinterpret_cast<double2*>(base + b.vel);
+  double4* s = reinterpret_cast<double4*>(base + b.stress);
+  x[l] = make_double2(D.px[g], D.py[g]);
+  v[l] = make_double2(D.vx[g], D.vy[g]);
+  reinterpret_cast<double*>(base + b.rho)[l] = D.rho[g];
+  if (g < D.NT) {
+    s[l] = make_double4(D.s0[g], D.s1[g], D.s2[g], D.s3[g]);
+    reinterpret_cast<double*>(base + b.iv1)[l] = D.iv1[g];
+    reinterpret_cast<double*>(base + b.fdp)[l] = D.fdp[g];
+    reinterpret_cast<int32_t*>(base + b.bc)[l] = D.bc_or_not[g];
+    if (g < D.NN)
+      reinterpret_cast<double2*>(base + b.displ)[l] = make_double2(D.dispx[g], D.dispy[g]);
+  } else {
+    s[l] = make_double4(0.0, 0.0, 0.0, 0.0);
+  }
+}
 __global__ void k_aos_to_soa4(const double* in, double* a, double* b, double* c, double* d, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -459,7 +599,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.cur = dalloc<sps::StepScalars>(c, nreal);
     D.err = dalloc<int>(c, 1);
     D.scan_tmp = dalloc<int64_t>(c, (N2 + 4096) / 4096 + 64);
-    c.stage = dalloc<double>(c, 4 * N2);
+    c.stage = dalloc<double>(c, 10 * (size_t)N2);  // x, vel, x00 (2 each) and stress (4)
+    c.d_chk = dalloc<unsigned long long>(c, 8);
     SPS_CUDA_CHECK(cudaMemsetAsync(D.meta, 0, sizeof(sps::PairMeta) * nreal, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bbox, 0xff, sizeof(unsigned long long) * 6 * nreal, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.gtot, 0, sizeof(sps::GridTotal), c.stream));
@@ -492,6 +633,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     }
     SPS_CUDA_CHECK(cudaMallocHost(&c.h_err, sizeof(int)));
+    SPS_CUDA_CHECK(cudaMallocHost(&c.h_chk, 8 * sizeof(unsigned long long)));
     ensure_scal(c, 256);
     D.cell_cap = 0;  // sized at upload
     c.d_dev = nullptr;
@@ -508,12 +650,12 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
 
 namespace {
 // the free-surface detection of the last step, when it was left for the download
-void refresh_surface(sps::Ctx& c) {
+void refresh_surface(sps::Ctx& c, bool sync = true) {
   if (!c.surf_stale) return;
   sps::launch_lists_keys(c);
   sps::launch_surface(c);
   SPS_CUDA_CHECK(cudaGetLastError());
-  SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  if (sync) SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
   c.surf_stale = false;
 }
 }  // namespace
@@ -539,26 +681,21 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
     return fail(&c, SPS_ERR_ARG, "sps_upload: null array");
   const sps::Real& M = c.real[r];
   const size_t nn = M.nnode, nt = (size_t)M.nnode + M.nsp, n2 = nt + M.ndum;
-  for (size_t i = 0; i < n2; i++)
-    if (itype[i] != 1 && itype[i] != 2 && itype[i] != 25)
-      return fail(&c, SPS_ERR_ARG, "sps_upload: itype must be 1, 2 or 25");
-  for (size_t i = 0; i < n2; i++) {
-    int want = i < nn ? 2 : i < nt ? 1 : 25;
-    if (itype[i] != want)
-      return fail(&c, SPS_ERR_ARG, "sps_upload: particles must be ordered nodes, stress-points, dummies");
-  }
   Seg sg[3];
   segments(c, r, sg);
   try {
-    // interleaved arrays are staged whole and transposed segment by segment
-    double* stage = c.stage;
+    // one pass of copies: the interleaved arrays are staged side by side and transposed
+    // segment by segment; the checks and extents are reduced on the device; one sync
+    double* st_x = c.stage;
+    double* st_v = st_x + 2 * n2;
+    double* st_0 = st_v + 2 * n2;
+    double* st_s = st_0 + 2 * n2;
     auto nbk = [](int64_t n) { return (int)((n + kBlock - 1) / kBlock); };
-    auto up2 = [&](const double* src, double* a, double* b) {
-      SPS_CUDA_CHECK(cudaMemcpyAsync(stage, src, sizeof(double) * 2 * n2, cudaMemcpyHostToDevice, c.stream));
+    auto up2 = [&](const double* src, double* st, double* a, double* b) {
+      SPS_CUDA_CHECK(cudaMemcpyAsync(st, src, sizeof(double) * 2 * n2, cudaMemcpyHostToDevice, c.stream));
       for (const Seg& q : sg)
         if (q.n > 0)
-          k_aos_to_soa2<<<nbk(q.n), kBlock, 0, c.stream>>>(stage + 2 * q.l, a + q.g, b + q.g, (int)q.n);
-      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+          k_aos_to_soa2<<<nbk(q.n), kBlock, 0, c.stream>>>(st + 2 * q.l, a + q.g, b + q.g, (int)q.n);
     };
     auto up1 = [&](void* dst, const void* src, size_t esz, int nseg) {
       for (int k = 0; k < nseg; k++)
@@ -566,13 +703,13 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
           SPS_CUDA_CHECK(cudaMemcpyAsync((char*)dst + esz * sg[k].g, (const char*)src + esz * sg[k].l,
                                          esz * sg[k].n, cudaMemcpyHostToDevice, c.stream));
     };
-    up2(x, D.px, D.py);
-    up2(vel, D.vx, D.vy);
-    up2(x00 ? x00 : x, D.x00x, D.x00y);
-    SPS_CUDA_CHECK(cudaMemcpyAsync(stage, stress, sizeof(double) * 4 * n2, cudaMemcpyHostToDevice, c.stream));
+    up2(x, st_x, D.px, D.py);
+    up2(vel, st_v, D.vx, D.vy);
+    up2(x00 ? x00 : x, st_0, D.x00x, D.x00y);
+    SPS_CUDA_CHECK(cudaMemcpyAsync(st_s, stress, sizeof(double) * 4 * n2, cudaMemcpyHostToDevice, c.stream));
     for (const Seg& q : sg)
       if (q.n > 0)
-        k_aos_to_soa4<<<nbk(q.n), kBlock, 0, c.stream>>>(stage + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
+        k_aos_to_soa4<<<nbk(q.n), kBlock, 0, c.stream>>>(st_s + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
                                                           D.s2 + q.g, D.s3 + q.g, (int)q.n);
     up1(D.mass, mass, sizeof(double), 3);
     up1(D.rho, rho, sizeof(double), 3);
@@ -596,18 +733,35 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
     SPS_CUDA_CHECK(cudaMemsetAsync(D.dispy + M.node0, 0, sizeof(double) * nn, c.stream));
     for (const Seg& q : sg)
       if (q.n > 0) sps::launch_vol(c, (int)q.g, (int)(q.g + q.n));
+    SPS_CUDA_CHECK(cudaMemsetAsync(c.d_chk, 0xff, 6 * sizeof(unsigned long long), c.stream));
+    SPS_CUDA_CHECK(cudaMemsetAsync(c.d_chk + 6, 0, 2 * sizeof(unsigned long long), c.stream));
+    if (n2 > 0)
+      k_upload_check<<<std::min(nbk((int64_t)n2), 4 * 152), kBlock, 0, c.stream>>>(
+          D.itype, D.px, D.py, D.hsml, sg[0].g, sg[0].n, sg[1].g, sg[1].n, sg[2].g, sg[2].n,
+          c.d_chk);
+    SPS_CUDA_CHECK(cudaGetLastError());
+    SPS_CUDA_CHECK(cudaMemcpyAsync(c.h_chk, c.d_chk, 8 * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
-    // this realisation's extent, for the cell grid capacity (4x margin for spreading)
     sps::HostReal& hr = c.hr[r];
-    double xmn[2] = {1e300, 1e300}, xmx[2] = {-1e300, -1e300}, hmax = 0, hmin_nd = 1e300;
-    for (size_t i = 0; i < n2; i++) {
-      for (int d = 0; d < 2; d++) {
-        xmn[d] = std::min(xmn[d], x[2 * i + d]);
-        xmx[d] = std::max(xmx[d], x[2 * i + d]);
-      }
-      hmax = std::max(hmax, hsml[i]);
-      if (i < nn || i >= nt) hmin_nd = std::min(hmin_nd, hsml[i]);
+    if (c.h_chk[6]) {
+      // the device state of r now holds the rejected arrays: r needs a valid upload
+      hr.uploaded = false;
+      c.uploaded = false;
+      return fail(&c, SPS_ERR_ARG,
+                  "sps_upload: itype must be 2 (nodes), then 1 (stress-points), then 25 (dummies)");
     }
+    if (c.h_chk[7]) {
+      hr.uploaded = false;
+      c.uploaded = false;
+      return fail(&c, SPS_ERR_ARG, "sps_upload: non-finite position or smoothing length");
+    }
+    double xmn[2] = {up_unkey(c.h_chk[0]), up_unkey(c.h_chk[1])};
+    double xmx[2] = {up_unkey(~c.h_chk[2]), up_unkey(~c.h_chk[3])};
+    double hmax = n2 ? up_unkey(~c.h_chk[4]) : 0.0;
+    double hmin_nd = c.h_chk[5] == ~0ull ? 1e300 : up_unkey(c.h_chk[5]);
+    if (n2 == 0) xmn[0] = xmn[1] = xmx[0] = xmx[1] = 0.0;
+    // this realisation's extent, for the cell grid capacity (4x margin for spreading)
     double cell = 2.0 * hmax;
     double ncr = 1.0;
     for (int d = 0; d < 2; d++) ncr *= std::floor((xmx[d] - xmn[d]) / cell + 1.0) + 2.0;
@@ -767,16 +921,20 @@ int sps_download_real(sps_ctx* h, int32_t r, double* x, double* vel, double* str
   Seg sg[3];
   segments(c, r, sg);
   try {
-    if (bc_or_not) refresh_surface(c);
-    double* stage = c.stage;
+    if (bc_or_not) refresh_surface(c, false);
+    // the interleaved outputs are transposed into the staging buffer side by side, every
+    // copy is enqueued, and the stream is synchronised once
+    double* st_x = c.stage;
+    double* st_v = st_x + 2 * n2;
+    double* st_s = st_v + 2 * n2;
+    double* st_d = st_s + 4 * n2;
     auto nbk = [](int64_t n) { return (int)((n + kBlock - 1) / kBlock); };
-    auto down2 = [&](double* dst, const double* a, const double* b, int nseg, size_t n) {
+    auto down2 = [&](double* dst, double* st, const double* a, const double* b, int nseg, size_t n) {
       for (int k = 0; k < nseg; k++)
         if (sg[k].n > 0)
-          k_soa_to_aos2<<<nbk(sg[k].n), kBlock, 0, c.stream>>>(stage + 2 * sg[k].l, a + sg[k].g,
+          k_soa_to_aos2<<<nbk(sg[k].n), kBlock, 0, c.stream>>>(st + 2 * sg[k].l, a + sg[k].g,
                                                                 b + sg[k].g, (int)sg[k].n);
-      SPS_CUDA_CHECK(cudaMemcpyAsync(dst, stage, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c.stream));
-      SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+      SPS_CUDA_CHECK(cudaMemcpyAsync(dst, st, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c.stream));
     };
     auto down1 = [&](void* dst, const void* src, size_t esz, int nseg) {
       for (int k = 0; k < nseg; k++)
@@ -784,29 +942,150 @@ int sps_download_real(sps_ctx* h, int32_t r, double* x, double* vel, double* str
           SPS_CUDA_CHECK(cudaMemcpyAsync((char*)dst + esz * sg[k].l, (const char*)src + esz * sg[k].g,
                                          esz * sg[k].n, cudaMemcpyDeviceToHost, c.stream));
     };
-    if (x) down2(x, D.px, D.py, 3, n2);
-    if (vel) down2(vel, D.vx, D.vy, 3, n2);
-    if (displ) down2(displ, D.dispx, D.dispy, 1, nn);
+    if (x) down2(x, st_x, D.px, D.py, 3, n2);
+    if (vel) down2(vel, st_v, D.vx, D.vy, 3, n2);
+    if (displ) down2(displ, st_d, D.dispx, D.dispy, 1, nn);
     if (stress) {
-      for (const Seg& q : sg)
+      for (int k = 0; k < 2; k++) {
+        const Seg& q = sg[k];
         if (q.n > 0)
-          k_soa_to_aos4<<<nbk(q.n), kBlock, 0, c.stream>>>(stage + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
+          k_soa_to_aos4<<<nbk(q.n), kBlock, 0, c.stream>>>(st_s + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
                                                             D.s2 + q.g, D.s3 + q.g, (int)q.n);
-      SPS_CUDA_CHECK(cudaMemcpyAsync(stress, stage, sizeof(double) * 4 * n2, cudaMemcpyDeviceToHost, c.stream));
+      }
+      // dummy stress is pair-local in the reference; report zero like its RK4 clear (:690)
+      if (n2 > nt)
+        SPS_CUDA_CHECK(cudaMemsetAsync(st_s + 4 * nt, 0, sizeof(double) * 4 * (n2 - nt), c.stream));
+      SPS_CUDA_CHECK(cudaMemcpyAsync(stress, st_s, sizeof(double) * 4 * n2, cudaMemcpyDeviceToHost, c.stream));
     }
     if (rho) down1(rho, D.rho, sizeof(double), 3);
     if (intvars1) down1(intvars1, D.iv1, sizeof(double), 2);
     if (bc_or_not) down1(bc_or_not, D.bc_or_not, sizeof(int32_t), 2);
     if (f_drucker) down1(f_drucker, D.fdp, sizeof(double), 2);
+    SPS_CUDA_CHECK(cudaGetLastError());
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
-    if (stress) {
-      // dummy stress is pair-local in the reference; report zero like its RK4 clear (:690)
-      for (size_t i = nt; i < n2; i++)
-        for (int k = 0; k < 4; k++) stress[4 * i + k] = 0.0;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+// ---- output snapshot -------------------------------------------------------------------
+
+int sps_snapshot(sps_ctx* h) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (!c.uploaded) return fail(&c, SPS_ERR_STATE, "sps_snapshot before sps_upload");
+  sps::Dev& D = c.d;
+  try {
+    if (!c.snap_dev) {
+      // one block per realisation in the layout sps_download returns
+      std::vector<int64_t> roff(D.R + 1, 0);
+      for (int r = 0; r < D.R; r++) {
+        const sps::Real& M = c.real[r];
+        const int64_t nt = (int64_t)M.nnode + M.nsp;
+        roff[r + 1] = roff[r] + (int64_t)snap_block(M.nnode, nt, nt + M.ndum).bytes;
+      }
+      c.snap_roff = roff;
+      c.snap_bytes = (size_t)roff[D.R];
+      void* p = nullptr;
+      SPS_CUDA_CHECK(cudaMalloc(&p, c.snap_bytes + sizeof(int64_t) * (D.R + 1)));
+      c.snap_dev = static_cast<char*>(p);
+      SPS_CUDA_CHECK(cudaMemcpy(c.snap_dev + c.snap_bytes, roff.data(), sizeof(int64_t) * (D.R + 1),
+                                cudaMemcpyHostToDevice));
+      SPS_CUDA_CHECK(cudaMallocHost(&p, c.snap_bytes));
+      c.snap_host = static_cast<char*>(p);
+      SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.snap_stream, cudaStreamNonBlocking));
+      SPS_CUDA_CHECK(cudaEventCreateWithFlags(&c.snap_ready, cudaEventDisableTiming));
+      SPS_CUDA_CHECK(cudaEventCreateWithFlags(&c.snap_done, cudaEventDisableTiming));
+    }
+    // the host copy of an earlier snapshot must have left the device buffer
+    if (c.snap_pending) SPS_CUDA_CHECK(cudaStreamWaitEvent(c.stream, c.snap_done, 0));
+    refresh_surface(c, false);
+    if (D.N2 > 0)
+      k_snap_pack<<<(D.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(
+          D, c.snap_dev, reinterpret_cast<const int64_t*>(c.snap_dev + c.snap_bytes));
+    SPS_CUDA_CHECK(cudaGetLastError());
+    SPS_CUDA_CHECK(cudaEventRecord(c.snap_ready, c.stream));
+    SPS_CUDA_CHECK(cudaStreamWaitEvent(c.snap_stream, c.snap_ready, 0));
+    SPS_CUDA_CHECK(cudaMemcpyAsync(c.snap_host, c.snap_dev, c.snap_bytes, cudaMemcpyDeviceToHost,
+                                   c.snap_stream));
+    SPS_CUDA_CHECK(cudaEventRecord(c.snap_done, c.snap_stream));
+    c.snap_pending = true;
+    c.snap_valid = false;
+    c.snap_step = c.steps_done;
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+namespace {
+// block until the snapshot has reached host memory
+int snapshot_ready(sps::Ctx& c, int32_t r, const char* who) {
+  if (r < 0 || r >= c.d.R) return fail(&c, SPS_ERR_ARG, std::string(who) + ": no such realisation");
+  if (!c.snap_pending && !c.snap_valid)
+    return fail(&c, SPS_ERR_STATE, std::string(who) + " without sps_snapshot");
+  try {
+    if (c.snap_pending) {
+      SPS_CUDA_CHECK(cudaEventSynchronize(c.snap_done));
+      c.snap_pending = false;
+      c.snap_valid = true;
     }
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
   }
+  return SPS_OK;
+}
+}  // namespace
+
+int sps_snapshot_view(sps_ctx* h, int32_t r, const double** x, const double** vel,
+                      const double** stress, const double** rho, const double** intvars1,
+                      const double** displ, const int32_t** bc_or_not, const double** f_drucker,
+                      int64_t* step) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  int rc = snapshot_ready(c, r, "sps_snapshot_view");
+  if (rc != SPS_OK) return rc;
+  const sps::Real& M = c.real[r];
+  const int64_t nn = M.nnode, nt = nn + M.nsp, n2 = nt + M.ndum;
+  const SnapBlock b = snap_block(nn, nt, n2);
+  const char* base = c.snap_host + c.snap_roff[r];
+  auto D = [&](size_t off) { return reinterpret_cast<const double*>(base + off); };
+  if (x) *x = D(b.x);
+  if (vel) *vel = D(b.vel);
+  if (stress) *stress = D(b.stress);
+  if (rho) *rho = D(b.rho);
+  if (intvars1) *intvars1 = D(b.iv1);
+  if (displ) *displ = D(b.displ);
+  if (bc_or_not) *bc_or_not = reinterpret_cast<const int32_t*>(base + b.bc);
+  if (f_drucker) *f_drucker = D(b.fdp);
+  if (step) *step = c.snap_step;
+  return SPS_OK;
+}
+
+int sps_snapshot_wait(sps_ctx* h, int32_t r, double* x, double* vel, double* stress, double* rho,
+                      double* intvars1, double* displ, int32_t* bc_or_not, double* f_drucker,
+                      int64_t* step) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  int rc = snapshot_ready(c, r, "sps_snapshot_wait");
+  if (rc != SPS_OK) return rc;
+  const sps::Real& M = c.real[r];
+  const int64_t nn = M.nnode, nt = nn + M.nsp, n2 = nt + M.ndum;
+  const SnapBlock b = snap_block(nn, nt, n2);
+  const char* base = c.snap_host + c.snap_roff[r];
+  auto put = [&](void* dst, size_t off, size_t bytes) {
+    if (dst && bytes) std::memcpy(dst, base + off, bytes);
+  };
+  put(x, b.x, 16 * n2);
+  put(vel, b.vel, 16 * n2);
+  put(stress, b.stress, 32 * n2);
+  put(rho, b.rho, 8 * n2);
+  put(intvars1, b.iv1, 8 * nt);
+  put(f_drucker, b.fdp, 8 * nt);
+  put(displ, b.displ, 16 * nn);
+  put(bc_or_not, b.bc, 4 * nt);
+  if (step) *step = c.snap_step;
   return SPS_OK;
 }
 
@@ -1191,6 +1470,15 @@ void sps_destroy(sps_ctx* h) {
     if (p) cudaFree(p);
   for (void* p : c.allocs) cudaFree(p);
   if (c.h_err) cudaFreeHost(c.h_err);
+  if (c.h_chk) cudaFreeHost(c.h_chk);
+  if (c.snap_stream) {
+    cudaStreamSynchronize(c.snap_stream);
+    cudaStreamDestroy(c.snap_stream);
+  }
+  if (c.snap_ready) cudaEventDestroy(c.snap_ready);
+  if (c.snap_done) cudaEventDestroy(c.snap_done);
+  if (c.snap_dev) cudaFree(c.snap_dev);
+  if (c.snap_host) cudaFreeHost(c.snap_host);
   if (c.stream) cudaStreamDestroy(c.stream);
   delete h;
 }

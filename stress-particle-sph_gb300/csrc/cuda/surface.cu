@@ -44,13 +44,17 @@ __device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
     kb = D.keyS[(size_t)b * D.N2 + s];
   }
   while (a < nC || b < nS) {
-    bool takeC = (a < nC) && (b >= nS || ka < kb);
+    // one call site for both lists, so that a warp whose lanes take different lists runs
+    // the body once
+    const bool takeC = (a < nC) && (b >= nS || ka < kb);
+    const int u = takeC ? ea.x : eb.x;
+    const int gx = takeC ? ea.z : eb.z, gy = takeC ? ea.w : eb.w;
+    const int32_t key = takeC ? ka : kb;
+    f(u, __int_as_float(gx), __int_as_float(gy), (key & 1) != 0);
     if (takeC) {
-      f(ea.x, __int_as_float(ea.z), __int_as_float(ea.w), (ka & 1) != 0);
       a++;
       next_cross();
     } else {
-      f(eb.x, __int_as_float(eb.z), __int_as_float(eb.w), (kb & 1) != 0);
       b++;
       if (b < nS) {
         eb = D.same[(size_t)b * D.N2 + s];
@@ -62,10 +66,16 @@ __device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
 
 // hf = (m_u G / rho_u) rounded to FP32; G is the gradient with respect to the target, which
 // gives the reference's hf1i (target pair_i) and hf1j = -(m_i gradW / rho_i) (target pair_j).
-// The quotient is the corrected division by the exact reciprocal 1/rho_u (the IEEE quotient,
-// bit for bit) instead of an FP64 division per neighbour.
-__device__ __forceinline__ float hf_of(const Dev& D, int u, float g) {
-  return (float)div_rcp(D.mass[u] * (double)g, D.rho[u], D.rinv[u]);
+// The float rounding of the IEEE quotient comes from the reciprocal 1/rho_u (div_rcp_f32),
+// the float -> double conversion from the integer pipe: two FP64 multiplies per value.
+__device__ __forceinline__ float hf_of(double m, double rho, double rinv, float g) {
+  return div_rcp_f32(m * f64_of(g), rho, rinv);
+}
+
+// (float)((double)acc + d * (double)h): the FP32 accumulation of an FP64 term, with the
+// conversions on the integer pipe
+__device__ __forceinline__ float acc_f64(float acc, double d, float h) {
+  return f32_rn(f64_of(acc) + d * f64_of(h));
 }
 
 __global__ void k_fs_normal0(Dev D) {
@@ -76,12 +86,13 @@ __global__ void k_fs_normal0(Dev D) {
   const double xt = D.px[t], yt = D.py[t];
   float A0 = 0.0f, A1 = 0.0f, A2 = 0.0f, A3 = 0.0f, f0 = 0.0f, f1 = 0.0f;
   walk_123(D, s, [&](int u, float gx, float gy, bool) {
-    float h1 = hf_of(D, u, gx), h2 = hf_of(D, u, gy);
+    const double m = D.mass[u], rho = D.rho[u], ri = D.rinv[u];
+    float h1 = hf_of(m, rho, ri, gx), h2 = hf_of(m, rho, ri, gy);
     double dx = D.px[u] - xt, dy = D.py[u] - yt;
-    A0 = (float)((double)A0 + dx * (double)h1);
-    A1 = (float)((double)A1 + dy * (double)h1);
-    A2 = (float)((double)A2 + dx * (double)h2);
-    A3 = (float)((double)A3 + dy * (double)h2);
+    A0 = acc_f64(A0, dx, h1);
+    A1 = acc_f64(A1, dy, h1);
+    A2 = acc_f64(A2, dx, h2);
+    A3 = acc_f64(A3, dy, h2);
     f0 = f0 + h1;
     f1 = f1 + h2;
   });
@@ -96,22 +107,43 @@ __global__ void k_fs_normal0(Dev D) {
   D.nrmy[t] = (double)(v1 / v2);
 }
 
-// scan region of particle a against a neighbour at (xb, yb): true when the neighbour lies in
-// it (then a is not on the surface)
-__device__ __forceinline__ bool in_scan_region(const Dev& D, int a, double xb, double yb) {
-  const double nx = D.nrmx[a], ny = D.nrmy[a], ha = D.hsml[a];
-  const float tt0 = (float)(D.px[a] + ha * nx), tt1 = (float)(D.py[a] + ha * ny);
-  const float tau0 = (float)(-ny), tau1 = (float)nx;
-  double ddx = xb - D.px[a], ddy = yb - D.py[a];
+// the scan region of particle a: its position, normal and smoothing length, the point
+// T = x_a + h_a n_a and the tangent, in the precisions the reference holds them
+struct ScanRegion {
+  double xa, ya, nx, ny, ha;
+  double tt0, tt1;  // FP32 values of T, widened
+  float tau0, tau1, limit;
+};
+__device__ __forceinline__ ScanRegion scan_region(const Dev& D, int a) {
+  ScanRegion R;
+  R.xa = D.px[a];
+  R.ya = D.py[a];
+  R.nx = D.nrmx[a];
+  R.ny = D.nrmy[a];
+  R.ha = D.hsml[a];
+  R.tt0 = (double)(float)(R.xa + R.ha * R.nx);
+  R.tt1 = (double)(float)(R.ya + R.ha * R.ny);
+  R.tau0 = (float)(-R.ny);
+  R.tau1 = (float)R.nx;
+  R.limit = (float)((double)sqrtf(2.0f) * R.ha);
+  return R;
+}
+
+// true when a neighbour at (xb, yb) lies in the scan region (then a is not on the surface)
+__device__ __forceinline__ bool in_scan_region(const ScanRegion& R, double xb, double yb) {
+  double ddx = xb - R.xa, ddy = yb - R.ya;
   float xba = (float)sqrt(ddx * ddx + ddy * ddy);
-  float xbt0 = (float)(xb - (double)tt0), xbt1 = (float)(yb - (double)tt1);
-  float xbt_norm = sqrtf(xbt0 * xbt0 + xbt1 * xbt1);
-  float prod = (float)(fabs(nx * (double)xbt0 + ny * (double)xbt1) +
-                       (double)fabsf(tau0 * xbt0 + tau1 * xbt1));
-  float limit = (float)((double)sqrtf(2.0f) * ha);
-  if (xba >= limit && (double)xbt_norm < ha) return true;
-  if (xba < limit && (double)prod < ha) return true;
-  return false;
+  float xbt0 = f32_rn(xb - R.tt0), xbt1 = f32_rn(yb - R.tt1);
+  if (xba >= R.limit) {
+    float xbt_norm = sqrtf(xbt0 * xbt0 + xbt1 * xbt1);
+    return (double)xbt_norm < R.ha;
+  }
+  if (xba < R.limit) {
+    float prod = f32_rn(fabs(R.nx * f64_of(xbt0) + R.ny * f64_of(xbt1)) +
+                        f64_of(fabsf(R.tau0 * xbt0 + R.tau1 * xbt1)));
+    return (double)prod < R.ha;
+  }
+  return false;  // a NaN distance lies in neither part of the region
 }
 
 __global__ void k_fs_scan(Dev D) {
@@ -121,13 +153,14 @@ __global__ void k_fs_scan(Dev D) {
   if (t >= D.NT) return;
   bool inside = false;
   const int nS = D.degS[s], nC = D.degC[s];
+  const ScanRegion R = scan_region(D, t);
   for (int k = 0; k < nS && !inside; k++) {
     int u = D.same[(size_t)k * D.N2 + s].x;
-    inside = in_scan_region(D, t, D.px[u], D.py[u]);
+    inside = in_scan_region(R, D.px[u], D.py[u]);
   }
   for (int k = 0; k < nC && !inside; k++) {
     int u = D.cross[(size_t)k * D.N2 + s].x;
-    if (is_dummy(D.itype[u])) inside = in_scan_region(D, t, D.px[u], D.py[u]);
+    if (is_dummy(D.itype[u])) inside = in_scan_region(R, D.px[u], D.py[u]);
   }
   int sub = inside ? 2 : 1;
   D.fint[t] = inside ? -1.0f : 0.0f;
@@ -158,7 +191,8 @@ __global__ void k_fs_normal(Dev D) {
       ny = ny + (double)xv;
       nb = nb + 1.0f;
     }
-    float h1 = hf_of(D, u, gx), h2 = hf_of(D, u, gy);
+    const double m = D.mass[u], rho = D.rho[u], ri = D.rinv[u];
+    float h1 = hf_of(m, rho, ri, gx), h2 = hf_of(m, rho, ri, gy);
     float df = D.fint[u] - ft;
     g0 = g0 + df * h1;
     g1 = g1 + df * h2;

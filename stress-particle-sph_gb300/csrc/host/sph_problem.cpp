@@ -137,6 +137,13 @@ struct sph_problem {
   std::vector<double> ttcurves, bc_list, segment_bcs, nodal_bcs;
   std::vector<float> ftcurves;
   std::vector<sph_run_block> blocks;
+  // output flags of problem_input_data (3_SPH_material_2018.f90:333-336): stress_out(1:4),
+  // vel_out(1:2), strain_out, rho_out, sml_out, disp_out
+  int32_t out_flags[10] = {1, 1, 1, 1, 1, 1, 1, 0, 0, 0};
+  bool gid_started = false;
+  // node lattice of the rectangle generator (ndivx columns of ndivy nodes), for the GiD
+  // elements of OutputMesh; 0 when the nodes came from elsewhere
+  int ndivx = 0, ndivy = 0;
   void fix_pointers() {
     p.nptstcurves = nptstcurves.empty() ? nullptr : nptstcurves.data();
     p.ttcurves = ttcurves.empty() ? nullptr : ttcurves.data();
@@ -164,6 +171,8 @@ void build_rectangle(sph_problem& P, double x1, double x4, double y1, double y4,
   int ndivx = (int)(lx / dx + 1.0);
   int ndivy = (int)(ly / dy + 1.0);
   int nnode = ndivx * ndivy;
+  P.ndivx = ndivx;
+  P.ndivy = ndivy;
   int nstress;
   if (inside) nstress = npoints * (ndivx - 1) * (ndivy - 1);
   else nstress = npoints * nnode;
@@ -620,6 +629,12 @@ void parse_all(sph_problem& P, const std::string& in_txt, const std::string& dat
     P.p.tcurve_grav = dat.to_i(g[2]);
     P.p.ft_grav = dat.to_d(g[3]);
   }
+  dat.text();
+  dat.text();
+  {
+    auto of = dat.read(10);
+    for (int k = 0; k < 10; k++) P.out_flags[k] = dat.to_i(of[k]);
+  }
   // driver time blocks (code/1_SPH_2018.f90:50-106)
   for (;;) {
     in.text();
@@ -727,7 +742,8 @@ int sph_problem_column(const sph_column_spec* s, sph_problem** out) {
       fmt("2 2 1 1 %s T %s\n", s->cspm ? "T" : "F", s->xsph ? "T" : "F") +
       "summ cont\nF F\ndamping\n" + fmt("%.17g\n", s->damping) + "alpha beta\n" +
       fmt("%.17g %.17g\n", s->alpha, s->beta) +
-      "ic_grav\n1\ngx gy timecurve factor\n0 -9.81 1 1.\noutput\n1 1 1 1 1 1 1 0 0 0\n";
+      "ic_grav\n1\ngx gy timecurve factor\n0 -9.81 1 1.\noutput\n"
+      "sxx syy sxy szz vx vy strain rho sml disp\n1 1 1 1 1 1 1 0 0 0\n";
   std::string in = "problem name\ncolumn\nSP_SPH art_stress particle_shift\nT F F\n"
                    "inside_approach\nT\nnpoints\n1\nsml\n" +
                    fmt("%.17g\n", s->sml) + "dt\n" + fmt("%.17g,1e9,1000000000\n", dt) +
@@ -937,6 +953,215 @@ int sph_problem_slope(const sph_slope_spec* s, sph_problem** out) {
 }
 
 const sps_params* sph_problem_params(const sph_problem* p) { return p ? &p->p : nullptr; }
+
+int sph_problem_output_flags(const sph_problem* p, int32_t* flags) {
+  if (!p || !flags) return SPS_ERR_ARG;
+  for (int k = 0; k < 10; k++) flags[k] = p->out_flags[k];
+  return SPS_OK;
+}
+
+namespace {
+
+// the F16.8 edit descriptor: 16 wide, 8 decimals, 16 asterisks when the value does not fit
+void put_f16_8(std::string& o, double v) {
+  char b[64];
+  int n = std::snprintf(b, sizeof b, "%16.8f", v);
+  if (n > 16) o.append(16, '*');
+  else o.append(b, (size_t)n);
+}
+
+// list-directed output (write(u,*)): a leading blank, then each item; reals with 17
+// significant digits.  The spacing of list-directed output is compiler-specific; readers of
+// these files split on blanks and commas.
+void put_ld_real(std::string& o, double v) {
+  char b[64];
+  std::snprintf(b, sizeof b, " %24.16E", v);
+  o += b;
+}
+void put_ld_int(std::string& o, long v) {
+  char b[32];
+  std::snprintf(b, sizeof b, " %11ld", v);
+  o += b;
+}
+
+bool write_file(const std::string& path, const std::string& text, bool append) {
+  FILE* f = std::fopen(path.c_str(), append ? "ab" : "wb");
+  if (!f) return false;
+  bool ok = std::fwrite(text.data(), 1, text.size(), f) == text.size();
+  return std::fclose(f) == 0 && ok;
+}
+
+}  // namespace
+
+int sph_write_output(sph_problem* p, const char* dir, int32_t itimestep, double time_sph,
+                     const double* x, const double* vel, const double* stress,
+                     const double* intvars1, const double* rho, const double* hsml,
+                     const int32_t* bc_or_not, const double* displ) {
+  if (!p || !dir || !x || !vel || !stress) return SPS_ERR_ARG;
+  const int32_t* f = p->out_flags;  // sxx syy sxy szz vx vy strain rho sml disp
+  const int nn = p->p.nnode, nt = p->ntotal;
+  auto iv = [&](int i) { return intvars1 ? intvars1[i] : 0.0; };
+  auto dsp = [&](int i, int k) { return displ ? displ[2 * (size_t)i + k] : 0.0; };
+  char suffix[32];
+  std::snprintf(suffix, sizeof suffix, "%06d", (int)itimestep);
+  const std::string d = std::string(dir) + "/";
+  const char* sname[4] = {"sxx", "syy", "sxy", "szz"};
+  // nodes.csv: the header and the separators as the reference's node file has them (a comma
+  // before each column after the first; its header starts "x-coord,,y-coord")
+  std::string o = "x-coord,,y-coord";
+  if (f[4] == 1) o += ",x-vel";
+  if (f[5] == 1) o += ",y-vel";
+  for (int k = 0; k < 4; k++)
+    if (f[k] == 1) (o += ',') += sname[k];
+  if (f[6] == 1) o += ",strain";
+  if (f[9] == 1) o += ",disp";
+  if (f[7] == 1) o += ",density";
+  if (f[8] == 1) o += ",sml";
+  o += "  \n";  // write(u,*) ' '
+  auto col = [&](double v) {
+    o += ',';
+    put_f16_8(o, v);
+  };
+  for (int i = 0; i < nn; i++) {
+    put_f16_8(o, x[2 * (size_t)i]);
+    col(x[2 * (size_t)i + 1]);
+    for (int k = 0; k < 2; k++)
+      if (f[4 + k] == 1) col(vel[2 * (size_t)i + k]);
+    for (int k = 0; k < 4; k++)
+      if (f[k] == 1) col(stress[4 * (size_t)i + k]);
+    if (f[6] == 1) col(iv(i));
+    if (f[9] == 1) col(std::sqrt(dsp(i, 0) * dsp(i, 0) + dsp(i, 1) * dsp(i, 1)));
+    if (f[7] == 1) col(rho ? rho[i] : 0.0);
+    if (f[8] == 1) col(hsml ? hsml[i] : 0.0);
+    o += "  \n";
+  }
+  if (!write_file(d + "nodes.csv." + suffix, o, false)) return SPS_ERR_ARG;
+  // stress_points.csv: a comma after every column, no displacement column
+  o = "x-coord,y-coord,";
+  if (f[4] == 1) o += "x-vel,";
+  if (f[5] == 1) o += "y-vel,";
+  for (int k = 0; k < 4; k++)
+    if (f[k] == 1) (o += sname[k]) += ',';
+  if (f[6] == 1) o += "strain,";
+  if (f[7] == 1) o += "density,";
+  if (f[8] == 1) o += "sml,";
+  o += "  \n";
+  auto colt = [&](double v) {
+    put_f16_8(o, v);
+    o += ',';
+  };
+  for (int i = nn; i < nt; i++) {
+    colt(x[2 * (size_t)i]);
+    colt(x[2 * (size_t)i + 1]);
+    for (int k = 0; k < 2; k++)
+      if (f[4 + k] == 1) colt(vel[2 * (size_t)i + k]);
+    for (int k = 0; k < 4; k++)
+      if (f[k] == 1) colt(stress[4 * (size_t)i + k]);
+    if (f[6] == 1) colt(iv(i));
+    if (f[7] == 1) colt(rho ? rho[i] : 0.0);
+    if (f[8] == 1) colt(hsml ? hsml[i] : 0.0);
+    o += "  \n";
+  }
+  if (!write_file(d + "stress_points.csv." + suffix, o, false)) return SPS_ERR_ARG;
+  // surface_points.csv: nodes with bc_or_not == 2 (list-directed lines)
+  o = " x-coord,y-coord,\n";
+  for (int i = 0; i < nn; i++)
+    if (bc_or_not && bc_or_not[i] == 2) {
+      put_ld_real(o, x[2 * (size_t)i]);
+      o += " ,";
+      put_ld_real(o, x[2 * (size_t)i + 1]);
+      o += '\n';
+    }
+  if (!write_file(d + "surface_points.csv." + suffix, o, false)) return SPS_ERR_ARG;
+  // GiD results: displacement (x - x00 when positions are updated, else displ) and velocity
+  // always, then sxx, syy, sxy and the plastic strain as the flags select
+  o.clear();
+  if (!p->gid_started) {  // written by OutputMesh before the first results
+    o += " GiD Post Results File 1.0\n GaussPoints \"Group1\" ElemType  Quadrilateral\n"
+         " Number Of Gauss Points: 1\n Natural Coordinates: Internal\n End GaussPoints\n";
+    p->gid_started = true;
+  }
+  auto header = [&](const char* what) {
+    (o += " Result ") += what;
+    put_ld_real(o, time_sph);
+    o += "  Vector OnNodes \"where\" \n  Values \n";
+  };
+  header("\"disp\" \"disp\" ");
+  for (int i = 0; i < nn; i++) {
+    double dx_ = p->p.update_x ? x[2 * (size_t)i] - p->x00[2 * (size_t)i] : dsp(i, 0);
+    double dy_ = p->p.update_x ? x[2 * (size_t)i + 1] - p->x00[2 * (size_t)i + 1] : dsp(i, 1);
+    put_ld_int(o, i + 1);
+    put_ld_real(o, dx_);
+    put_ld_real(o, dy_);
+    o += " 0.\n";
+  }
+  o += "  End Values \n";
+  header("\"vel\" \"veloc\" ");
+  for (int i = 0; i < nn; i++) {
+    double ux = vel[2 * (size_t)i], uy = vel[2 * (size_t)i + 1];
+    put_ld_int(o, i + 1);
+    put_ld_real(o, ux);
+    put_ld_real(o, uy);
+    put_ld_real(o, std::sqrt(ux * ux + uy * uy));
+    o += '\n';
+  }
+  o += "  End Values \n";
+  const char* gname[3] = {"\"sigmaxx\" \"sxx\" ", "\"sigmayy\" \"syy\" ",
+                          "\"sigmaxy\" \"sxy\" "};
+  for (int k = 0; k < 3; k++)
+    if (f[k] == 1) {
+      header(gname[k]);
+      for (int i = 0; i < nn; i++) {
+        put_ld_int(o, i + 1);
+        put_ld_real(o, stress[4 * (size_t)i + k]);
+        o += "  0.   0.   \n";
+      }
+      o += "  End Values \n";
+    }
+  if (f[6] == 1) {
+    header("\"plastic strain\" \"esp\" ");
+    for (int i = 0; i < nn; i++) {
+      put_ld_int(o, i + 1);
+      put_ld_real(o, iv(i));
+      o += "  0.  0.   \n";
+    }
+    o += "  End Values \n";
+  }
+  if (!write_file(d + p->name + ".post.res", o, true)) return SPS_ERR_ARG;
+  return SPS_OK;
+}
+
+int sph_write_mesh(sph_problem* p, const char* dir) {
+  if (!p || !dir) return SPS_ERR_ARG;
+  const int nn = p->p.nnode;
+  std::string o = " MESH    dimension 3 ElemType Quadrilateral  Nnode 4 \n  coordinates\n";
+  for (int i = 0; i < nn; i++) {
+    put_ld_int(o, i + 1);
+    put_ld_real(o, p->x[2 * (size_t)i]);
+    put_ld_real(o, p->x[2 * (size_t)i + 1]);
+    put_ld_real(o, 0.0);
+    o += '\n';
+  }
+  o += "  End coordinates\n  Elements\n";
+  // the lattice cells, numbered and ordered as Read_2DMesh numbers them
+  const int nx = p->ndivx, ny = p->ndivy;
+  long e = 1;
+  for (int i = 2; i <= nx; i++)
+    for (int k = (i - 1) * ny + 2; k <= i * ny; k++) {
+      put_ld_int(o, e++);
+      for (long v : {(long)k, (long)k - ny, (long)k - ny - 1, (long)k - 1}) put_ld_int(o, v);
+      o += "  1\n";
+    }
+  o += "  End elements\n";
+  const std::string d = std::string(dir) + "/";
+  if (!write_file(d + p->name + ".post.msh", o, false)) return SPS_ERR_ARG;
+  // OutputMesh then starts the results file
+  o = " GiD Post Results File 1.0\n GaussPoints \"Group1\" ElemType  Quadrilateral\n"
+      " Number Of Gauss Points: 1\n Natural Coordinates: Internal\n End GaussPoints\n";
+  if (!write_file(d + p->name + ".post.res", o, false)) return SPS_ERR_ARG;
+  p->gid_started = true;
+  return SPS_OK;
+}
 
 int sph_problem_get_arrays(sph_problem* p, sph_problem_arrays* o) {
   if (!p || !o) return SPS_ERR_ARG;

@@ -38,6 +38,11 @@ def gpu_lib():
             [P(C.c_int32)] + [P(C.c_double)] * 3
         lib.sps_download_real.argtypes = [C.c_void_p, C.c_int32] + [P(C.c_double)] * 6 + \
             [P(C.c_int32), P(C.c_double)]
+        lib.sps_snapshot.argtypes = [C.c_void_p]
+        lib.sps_snapshot_view.argtypes = [C.c_void_p, C.c_int32] + \
+            [P(P(C.c_double))] * 6 + [P(P(C.c_int32)), P(P(C.c_double)), P(C.c_int64)]
+        lib.sps_snapshot_wait.argtypes = [C.c_void_p, C.c_int32] + [P(C.c_double)] * 6 + \
+            [P(C.c_int32), P(C.c_double), P(C.c_int64)]
         lib.sps_dump_pairs_real.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32),
                                             P(C.c_int32), P(C.c_float), P(C.c_float),
                                             P(C.c_float), P(C.c_int64)]
@@ -114,15 +119,66 @@ class StepContext:
         self._call("step", self._h, int(nsteps), C.byref(t))
         return t.value
 
-    def download(self):
-        n2, nt, nn = self.ntotal2, self.ntotal, self.nnode
-        out = dict(x=np.empty(2 * n2), vel=np.empty(2 * n2), stress=np.empty(4 * n2),
-                   rho=np.empty(n2), intvars1=np.empty(nt), displ=np.empty(2 * nn),
-                   bc_or_not=np.empty(nt, np.int32), f_drucker=np.empty(nt))
+    def _out(self, r, out):
+        """Output arrays of realisation r: `out` (checked) or new ones."""
+        n2, nt, nn = self._sizes(r)
+        want = dict(x=(2 * n2, np.float64), vel=(2 * n2, np.float64),
+                    stress=(4 * n2, np.float64), rho=(n2, np.float64),
+                    intvars1=(nt, np.float64), displ=(2 * nn, np.float64),
+                    bc_or_not=(nt, np.int32), f_drucker=(nt, np.float64))
+        if out is None:
+            return {k: np.empty(n, dt) for k, (n, dt) in want.items()}
+        for k, (n, dt) in want.items():
+            a = out[k]
+            if a.dtype != dt or a.size != n or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("download: out[%r] must be a contiguous %s array of %d" % (
+                    k, np.dtype(dt).name, n))
+        return out
+
+    def download(self, out=None):
+        """The fields after the last step; `out` (e.g. pinned arrays) is filled in place."""
+        out = self._out(0, out)
         self._call("download", self._h, _dp(out["x"]), _dp(out["vel"]), _dp(out["stress"]),
                    _dp(out["rho"]), _dp(out["intvars1"]), _dp(out["displ"]),
                    _ip(out["bc_or_not"]), _dp(out["f_drucker"]))
         return out
+
+    def _sizes(self, r):
+        if hasattr(self, "problems"):
+            p = self.problems[r]
+            return p.ntotal2, p.ntotal, p.nnode
+        return self.ntotal2, self.ntotal, self.nnode
+
+    def snapshot(self):
+        """Stage the output fields (sps_snapshot); later steps run while they copy out."""
+        self._call("snapshot", self._h)
+
+    def snapshot_wait(self, r=0, out=None):
+        """(fields of realisation r as download() returns them, step count at the snapshot)."""
+        out = self._out(r, out)
+        step = C.c_int64(0)
+        self._call("snapshot_wait", self._h, r, _dp(out["x"]), _dp(out["vel"]),
+                   _dp(out["stress"]), _dp(out["rho"]), _dp(out["intvars1"]),
+                   _dp(out["displ"]), _ip(out["bc_or_not"]), _dp(out["f_drucker"]),
+                   C.byref(step))
+        return out, step.value
+
+    def snapshot_view(self, r=0):
+        """snapshot_wait without the copy: read-only numpy views into the snapshot's pinned
+        host buffer, valid until the next snapshot() or close()."""
+        n2, nt, nn = self._sizes(r)
+        names = ("x", "vel", "stress", "rho", "intvars1", "displ", "bc_or_not", "f_drucker")
+        sizes = (2 * n2, 2 * n2, 4 * n2, n2, nt, 2 * nn, nt, nt)
+        ptrs = [C.POINTER(C.c_int32 if k == "bc_or_not" else C.c_double)() for k in names]
+        step = C.c_int64(0)
+        self._call("snapshot_view", self._h, r, *[C.byref(p) for p in ptrs], C.byref(step))
+        out = {}
+        for k, n, p in zip(names, sizes, ptrs):
+            a = np.ctypeslib.as_array(p, shape=(n,)) if n else np.zeros(
+                0, np.int32 if k == "bc_or_not" else np.float64)
+            a.flags.writeable = False
+            out[k] = a
+        return out, step.value
 
     def download_surface(self, r=0):
         """(normal (2,ntotal), subset (ntotal)) of the last free-surface detection."""
@@ -250,12 +306,8 @@ class Batch(StepContext):
         self.times = list(t)
         return self.times
 
-    def download(self, r):
-        prob = self.problems[r]
-        n2, nt, nn = prob.ntotal2, prob.ntotal, prob.nnode
-        out = dict(x=np.empty(2 * n2), vel=np.empty(2 * n2), stress=np.empty(4 * n2),
-                   rho=np.empty(n2), intvars1=np.empty(nt), displ=np.empty(2 * nn),
-                   bc_or_not=np.empty(nt, np.int32), f_drucker=np.empty(nt))
+    def download(self, r, out=None):
+        out = self._out(r, out)
         self._call("download_real", self._h, r, _dp(out["x"]), _dp(out["vel"]),
                    _dp(out["stress"]), _dp(out["rho"]), _dp(out["intvars1"]),
                    _dp(out["displ"]), _ip(out["bc_or_not"]), _dp(out["f_drucker"]))

@@ -32,6 +32,11 @@ def host_lib():
         lib.sph_problem_block.argtypes = [vp, C.c_int32, P(_abi.SphRunBlock)]
         lib.sph_problem_name.argtypes = [vp]
         lib.sph_problem_name.restype = C.c_char_p
+        lib.sph_problem_output_flags.argtypes = [vp, P(C.c_int32)]
+        dp, ip = P(C.c_double), P(C.c_int32)
+        lib.sph_write_output.argtypes = [vp, C.c_char_p, C.c_int32, C.c_double, dp, dp, dp, dp,
+                                         dp, dp, ip, dp]
+        lib.sph_write_mesh.argtypes = [vp, C.c_char_p]
         lib.sph_problem_free.argtypes = [vp]
         lib.sph_problem_free.restype = None
         _HOST = lib
@@ -142,6 +147,41 @@ class Problem:
         for k, v in overrides.items():
             setattr(p, k, v)
         return p
+
+    OUTPUT_FIELDS = ("sxx", "syy", "sxy", "szz", "vx", "vy", "strain", "rho", "sml", "disp")
+
+    def output_flags(self):
+        """The output selection of the .dat file: {field: 0/1} over OUTPUT_FIELDS."""
+        f = (C.c_int32 * 10)()
+        host_lib().sph_problem_output_flags(self._h, f)
+        return dict(zip(self.OUTPUT_FIELDS, list(f)))
+
+    def write_output(self, directory, itimestep, time_sph, fields, hsml=None):
+        """OutputRes: the CSV files of step itimestep and the GiD blocks appended to
+        <name>.post.res, from `fields` as download() / snapshot_wait() return them."""
+        def arr(k, dt=np.float64):
+            a = fields.get(k)
+            return None if a is None else np.ascontiguousarray(a, dtype=dt)
+
+        a = dict(x=arr("x"), vel=arr("vel"), stress=arr("stress"), iv=arr("intvars1"),
+                 rho=arr("rho"), h=None if hsml is None else np.ascontiguousarray(hsml, np.float64),
+                 bc=arr("bc_or_not", np.int32), d=arr("displ"))
+
+        def p(v, t=C.c_double):
+            return None if v is None else v.ctypes.data_as(C.POINTER(t))
+
+        rc = host_lib().sph_write_output(self._h, str(directory).encode(), int(itimestep),
+                                         float(time_sph), p(a["x"]), p(a["vel"]), p(a["stress"]),
+                                         p(a["iv"]), p(a["rho"]), p(a["h"]),
+                                         p(a["bc"], C.c_int32), p(a["d"]))
+        if rc:
+            raise OSError("sph_write_output(%s) failed (%d)" % (directory, rc))
+
+    def write_mesh(self, directory):
+        """OutputMesh: <name>.post.msh, and the header that starts <name>.post.res."""
+        rc = host_lib().sph_write_mesh(self._h, str(directory).encode())
+        if rc:
+            raise OSError("sph_write_mesh(%s) failed (%d)" % (directory, rc))
 
     def state(self):
         """Copies of the dynamic state arrays, in sps_upload order."""

@@ -1,0 +1,54 @@
+"""GPU: the checks of sps_upload (done on the device, one host synchronisation) and the
+download into caller-provided arrays."""
+import numpy as np
+import pytest
+
+import cases
+import sps_gb300
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(prob):
+    return sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", prob.params_copy())
+
+
+def test_rejected_upload_then_valid_upload(built_gpu):
+    prob = cases.bui_like()
+    ctx = _ctx(prob)
+    st = prob.state()
+    bad = dict(st)
+    bad["itype"] = st["itype"].copy()
+    bad["itype"][prob.nnode + 3] = 2  # a node among the stress-points
+    with pytest.raises(sps_gb300.SpsError, match="itype"):
+        ctx.upload(**bad)
+    with pytest.raises(sps_gb300.SpsError):
+        ctx.step(1, 0.0)  # the context holds no valid state
+    nan = dict(st)
+    nan["x"] = st["x"].copy()
+    nan["x"][5] = np.nan
+    with pytest.raises(sps_gb300.SpsError, match="non-finite"):
+        ctx.upload(**nan)
+    ctx.upload_problem(prob)
+    ctx.step(4, 0.0)
+    ref = _ctx(prob)
+    ref.upload_problem(prob)
+    ref.step(4, 0.0)
+    cases.assert_bitwise(ctx.download(), ref.download(), prob.ntotal)
+    ctx.close()
+    ref.close()
+
+
+def test_download_into_given_arrays(built_gpu):
+    prob = cases.bui_like()
+    ctx = _ctx(prob)
+    ctx.upload_problem(prob)
+    ctx.step(3, 0.0)
+    want = ctx.download()
+    out = {k: np.full_like(v, 7) for k, v in want.items()}
+    got = ctx.download(out=out)
+    assert got is out
+    cases.assert_bitwise(got, want, prob.ntotal)
+    with pytest.raises(ValueError):
+        ctx.download(out=dict(out, rho=np.empty(3)))
+    ctx.close()
