@@ -49,6 +49,9 @@ def lib():
                                          P(C.c_double), P(C.c_double), P(C.c_double),
                                          P(C.c_double)]
         L.orc_drucker_prager.restype = None
+        L.orc_viscoplastic.argtypes = [P(C.c_double), C.c_int, P(C.c_double), C.c_double,
+                                       P(C.c_double), P(C.c_double)]
+        L.orc_viscoplastic.restype = None
         _LIB = L
     return _LIB
 

@@ -223,6 +223,175 @@ void orc_drucker_prager(const double* props, double time_sph, const double* stre
   drucker_prager(props, time_sph, stress4, grad_u4, f_drucker, G, vivel);
 }
 
+/* The viscoplastic laws (ncrit 1 Tresca, 2 von Mises, 3 Mohr-Coulomb, 4 Drucker-Prager;
+   Perzyna flow), 2D branches (ntype_solid 1-3), in the reference's operation order:
+     Get_Vivel :2165-2228, invar09 :2233-2377, yieldf09 :2381-2556, flowvp09 :2560-2609,
+     Get_Dmatx :2614-2691 (3_SPH_material_2018.f90).
+   The same routines, with the same 2D arithmetic, are in the strain-localisation and
+   vertical-slope examples' copies, whose inputs use them.  FP32 literals are kept as
+   floats: root3 = sqrt(3.00) is an FP32 square root, the degree factor 0.017453292, the
+   radian factor 57.29577951308, the flow rule's root3 = 1.73205080757 and allow = 0.01 are
+   FP32 constants widened to FP64.  props: 3 E, 4 nu, 7 yield stress, 8 hardening modulus,
+   9 friction angle (degrees), 10 gamma, 11 delta, 12 n (1-based as in the .dat file). */
+#define VP_RAD ((double)0.017453292f)
+static double vp_root3(void) { return (double)sqrtf(3.0f); }
+
+/* invar09 (2D): invariants, the yield function value and the current yield-surface size */
+static void vp_invar(const double* props, const double* s, double iv1, double* devia,
+                     double* smean, double* varj2, double* sint3, double* theta, double* steff,
+                     double* yield, double* fdatm) {
+  const double root3 = vp_root3();
+  const int ncrit = (int)props[1];
+  *smean = ((s[0] + s[1]) + s[3]) / 3.0;
+  devia[0] = s[0] - *smean;
+  devia[1] = s[1] - *smean;
+  devia[2] = s[2];
+  devia[3] = s[3] - *smean;
+  *varj2 = devia[2] * devia[2] +
+           0.5 * ((devia[0] * devia[0] + devia[1] * devia[1]) + devia[3] * devia[3]);
+  const double varj3 = devia[3] * (devia[3] * devia[3] - *varj2);
+  *steff = sqrt(*varj2);
+  if (*steff != 0.0) {
+    *sint3 = -(((3.0 * root3) * varj3) / ((2.0 * *varj2) * *steff));
+    if (*sint3 > 1.0) *sint3 = 1.0;
+  } else {
+    *sint3 = 0.0;
+  }
+  if (*sint3 < -1.0) *sint3 = -1.0;
+  if (*sint3 > 1.0) *sint3 = 1.0;
+  *theta = asin(*sint3) / 3.0;
+  double snphi;
+  switch (ncrit) {
+    case 1:
+      *yield = (2.0 * cos(*theta)) * *steff;
+      break;
+    case 2:
+      *yield = root3 * *steff;
+      break;
+    case 3:
+      snphi = sin(props[8] * VP_RAD);
+      *yield = *smean * snphi + *steff * (cos(*theta) - (sin(*theta) * snphi) / root3);
+      break;
+    default: /* 4 */
+      snphi = sin(props[8] * VP_RAD);
+      *yield = ((6.0 * *smean) * snphi) / (root3 * (3.0 - snphi)) + *steff;
+      break;
+  }
+  /* linear hardening, limited to a tenth of the initial size (the reference stops the run
+     when the initial size is not above 0.001; sps_create rejects such materials) */
+  const double fdatm0 = props[6], hards = props[7];
+  double f = fdatm0 + hards * iv1;
+  double fact = fabs(f) / fabs(fdatm0);
+  if (fact < (double)0.1f) fact = (double)0.1f;
+  *fdatm = fdatm0 * fact;
+}
+
+/* yieldf09 (2D): the flow vector df/ds */
+static void vp_avect(const double* props, const double* devia, double varj2, double theta,
+                     double steff, double* avect) {
+  const double root3 = vp_root3();
+  const int ncrit = (int)props[1];
+  const double frict = props[8];
+  const double tanth = tan(theta), tant3 = tan(3.0 * theta), sinth = sin(theta),
+               costh = cos(theta), cost3 = cos(3.0 * theta);
+  const double veca1[4] = {1.0, 1.0, 0.0, 1.0};
+  double veca2[4] = {0.0, 0.0, 0.0, 0.0}, veca3[4];
+  if (steff > 0) {
+    for (int i = 0; i < 4; i++) veca2[i] = devia[i] / (2.0 * steff);
+    veca2[2] = devia[2] / steff;
+  }
+  veca3[0] = devia[1] * devia[3] + varj2 / 3.0;
+  veca3[1] = devia[0] * devia[3] + varj2 / 3.0;
+  veca3[2] = -((2.0 * devia[2]) * devia[3]);
+  veca3[3] = (devia[0] * devia[1] - devia[2] * devia[2]) + varj2 / 3.0;
+  double cons1 = 0.0, cons2 = 0.0, cons3 = 0.0;
+  const double abthe = fabs(theta * (double)57.29577951308f);
+  if (ncrit == 1) {
+    if (abthe >= 29.0) {
+      cons2 = root3;
+      cons3 = 0.0;
+    } else {
+      cons2 = 2.0 * (costh + sinth * tant3);
+      cons3 = (root3 * sinth) / (varj2 * cost3);
+    }
+  } else if (ncrit == 2) {
+    cons2 = root3;
+  } else if (ncrit == 3) {
+    cons1 = sin(frict * VP_RAD) / 3.0;
+    if (abthe >= 29.0) {
+      double plumi = 1.0;
+      if (theta > 0.0) plumi = -1.0;
+      cons2 = 0.5 * (root3 + (plumi * cons1) * root3);
+      cons3 = 0.0;
+    } else {
+      cons2 = costh * ((1.0 + tanth * tant3) + (cons1 * (tant3 - tanth)) * root3);
+      cons3 = (root3 * sinth + (3.0 * cons1) * costh) / ((2.0 * varj2) * cost3);
+    }
+  } else { /* 4 */
+    const double snphi = sin(frict * VP_RAD);
+    cons1 = (2.0 * snphi) / (root3 * (3.0 - snphi));
+    cons2 = 1.0;
+  }
+  for (int i = 0; i < 4; i++) avect[i] = (cons1 * veca1[i] + cons2 * veca2[i]) + cons3 * veca3[i];
+}
+
+/* Get_Vivel (2D) with flowvp09: the viscoplastic strain rate */
+static void vp_vivel(const double* props, const double* s, double iv1, double* vivel) {
+  double devia[4], smean, varj2, sint3, theta, steff, yield, fdatm;
+  for (int i = 0; i < 4; i++) vivel[i] = 0.0;
+  vp_invar(props, s, iv1, devia, &smean, &varj2, &sint3, &theta, &steff, &yield, &fdatm);
+  if (!(yield > fdatm)) return;
+  double avect[4];
+  vp_avect(props, devia, varj2, theta, steff, avect);
+  const double gamma = props[9], delta = props[10], nflow = props[11];
+  const double fnorm = (yield - fdatm) / fdatm;
+  if (fnorm >= (double)0.01f) {
+    double cmult;
+    if (nflow != 1) cmult = gamma * (exp(delta * fnorm) - 1.0);
+    else cmult = gamma * pow(fnorm, delta);
+    for (int i = 0; i < 4; i++) vivel[i] = cmult * avect[i];
+  }
+}
+
+/* Get_Dmatx (2D): the isotropic elastic matrix */
+static void vp_dmatx(const double* props, int ntype_solid, double D[4][4]) {
+  const double young = props[2], poiss = props[3];
+  memset(D, 0, sizeof(double) * 16);
+  if (ntype_solid == 1) {
+    const double c = young / (1.0 - poiss * poiss);
+    D[0][0] = c;
+    D[1][1] = c;
+    D[0][1] = c * poiss;
+    D[1][0] = c * poiss;
+    D[2][2] = ((1.0 - poiss) * c) / 2.0;
+  } else {
+    const double c = (young * (1.0 - poiss)) / ((1.0 + poiss) * (1.0 - 2.0 * poiss));
+    const double cp = (c * poiss) / (1.0 - poiss);
+    D[0][0] = c;
+    D[1][1] = c;
+    D[0][1] = cp;
+    D[1][0] = cp;
+    D[0][3] = cp;
+    D[1][3] = cp;
+    D[3][0] = cp;
+    D[3][1] = cp;
+    D[3][3] = c;
+    if (ntype_solid == 2) D[2][2] = ((1.0 - 2.0 * poiss) * c) / (2.0 * (1.0 - poiss));
+    else D[2][2] = (c * (1.0 - 2.0 * poiss)) / (2.0 * (1.0 - poiss));
+  }
+}
+
+void orc_viscoplastic(const double* props, int ntype_solid, const double* stress4, double iv1,
+                      double* vivel, double* Gs) {
+  double D[4][4];
+  vp_vivel(props, stress4, iv1, vivel);
+  vp_dmatx(props, ntype_solid, D);
+  for (int i = 0; i < 4; i++) {
+    Gs[i] = 0.0;
+    for (int j = 0; j < 4; j++) Gs[i] = Gs[i] - D[i][j] * vivel[j];
+  }
+}
+
 /* plastic_terms (3_SPH_material_2018.f90:1884-1954) + Get_derivative_intvars 2D branch
    (:2767-2775).  Returns Gs (= -G) and der_intvars(1). */
 static void plastic_terms(orc_ctx* c, int ie, const double* fi, double* Gs, double* der1) {
@@ -235,7 +404,9 @@ static void plastic_terms(orc_ctx* c, int ie, const double* fi, double* Gs, doub
     double poiss = props[3];
     double s2[4] = {fi[0], fi[1], fi[2], fi[3]};
     if (c->p.ntype_solid == 1) s2[3] = poiss * (s2[0] + s2[1]);
-    if (ncrit == 12) {
+    if (ncrit <= 5) {
+      orc_viscoplastic(props, c->p.ntype_solid, s2, c->intvars1[ie], vivel, Gs);
+    } else if (ncrit == 12) {
       drucker_prager(props, c->time_sph, s2, &c->grad_u[4 * (size_t)ie], &c->f_drucker[ie], G2,
                      vivel);
       for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
@@ -1150,7 +1321,12 @@ int orc_create(const sps_params* p, orc_ctx** out) {
       p->ndummy2 > p->ndummy)
     return SPS_ERR_ARG;
   int ntype_eco = (int)p->props[0], ncrit = (int)p->props[1];
-  if (ntype_eco > 1 && ncrit != 12) return SPS_ERR_UNSUPPORTED;
+  /* Cam Clay (5) is not supported: its yield-surface size Internal_Vars(3) is never
+     integrated by the reference and stays 0 */
+  if (ntype_eco > 1 && !((ncrit >= 1 && ncrit <= 4) || ncrit == 12)) return SPS_ERR_UNSUPPORTED;
+  if (ntype_eco > 1 && ncrit <= 4 && !(p->props[6] > (double)0.001f)) return SPS_ERR_ARG;
+  if (ntype_eco > 1 && ncrit <= 4 && (p->ntype_solid < 1 || p->ntype_solid > 3))
+    return SPS_ERR_UNSUPPORTED;
   if (p->skf < 1 || p->skf > 3) return SPS_ERR_ARG;
   if (!p->sp_sph && p->nstress != p->nnode) return SPS_ERR_ARG;
   orc_ctx* c = xcalloc(1, sizeof(orc_ctx));

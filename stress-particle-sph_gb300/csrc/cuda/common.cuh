@@ -84,6 +84,13 @@ struct Real {
   double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
   double xmin_dom[2], xmax_dom[2];
   double cgrav[2];
+  // viscoplastic laws (ncrit 1-4): props 7, 8, 10-12, and the material constants that the
+  // reference recomputes per call, evaluated once on the host with the same expressions
+  double vp_fdatm0, vp_hards, vp_gamma, vp_delta, vp_nflow;
+  double vp_snphi;  // sin(phi 0.017453292)
+  double vp_den;    // root3 (3 - sin phi): the Drucker-Prager yield denominator
+  double vp_cons1;  // yieldf09's cons1 (Mohr-Coulomb sin phi / 3, Drucker-Prager)
+  double vp_D[16];  // Get_Dmatx, row-major
 };
 
 enum ErrBits : int {
@@ -412,6 +419,102 @@ __device__ __forceinline__ void adapt_stress_fast(double alpha2, double kc, doub
     b = fma(rn, d1, smean);
     d = fma(rn, d3, smean);
     c = rn * d2;
+  }
+}
+
+// The viscoplastic laws of plastic_terms for ncrit <= 4 (3_SPH_material_2018.f90): Get_Vivel
+// :2165, invar09 :2233, yieldf09 :2381, flowvp09 :2560, then Gs = -Dmatx vivel (:1930-1934).
+// 2D branches, FP64 with the reference's FP32 constants (root3 = sqrt(3.00) in FP32,
+// 0.01 and 0.1 as FP32 values).  Lode-angle functions are evaluated only for the laws that
+// read them (Tresca, Mohr-Coulomb); von Mises and Drucker-Prager never use them.  Perzyna
+// exponent n = 1 with delta = 1 takes fnorm itself (the reference's fnorm**1.0).
+// s: stress (plane-stress szz substituted), iv1: accumulated deviatoric plastic strain.
+__device__ __forceinline__ void viscoplastic(const Real& M, const double* s, double iv1,
+                                             double* vivel, double* Gs) {
+  const double root3 = (double)sqrtf(3.0f);
+  for (int i = 0; i < 4; i++) vivel[i] = 0.0;
+  // invar09
+  const double smean = ((s[0] + s[1]) + s[3]) / 3.0;
+  double dv[4] = {s[0] - smean, s[1] - smean, s[2], s[3] - smean};
+  const double varj2 = dv[2] * dv[2] + 0.5 * ((dv[0] * dv[0] + dv[1] * dv[1]) + dv[3] * dv[3]);
+  const double steff = sqrt(varj2);
+  const bool lode = M.ncrit == 1 || M.ncrit == 3;
+  double theta = 0.0;
+  if (lode) {
+    const double varj3 = dv[3] * (dv[3] * dv[3] - varj2);
+    double sint3;
+    if (steff != 0.0) {
+      sint3 = -(((3.0 * root3) * varj3) / ((2.0 * varj2) * steff));
+      if (sint3 > 1.0) sint3 = 1.0;
+    } else {
+      sint3 = 0.0;
+    }
+    if (sint3 < -1.0) sint3 = -1.0;
+    if (sint3 > 1.0) sint3 = 1.0;
+    theta = asin(sint3) / 3.0;
+  }
+  double yield;
+  if (M.ncrit == 1) yield = (2.0 * cos(theta)) * steff;
+  else if (M.ncrit == 2) yield = root3 * steff;
+  else if (M.ncrit == 3)
+    yield = smean * M.vp_snphi + steff * (cos(theta) - (sin(theta) * M.vp_snphi) / root3);
+  else yield = ((6.0 * smean) * M.vp_snphi) / M.vp_den + steff;
+  double fdatm = M.vp_fdatm0 + M.vp_hards * iv1;
+  double fact = fabs(fdatm) / fabs(M.vp_fdatm0);
+  if (fact < (double)0.1f) fact = (double)0.1f;
+  fdatm = M.vp_fdatm0 * fact;
+  if (yield > fdatm) {
+    // flowvp09
+    const double fnorm = (yield - fdatm) / fdatm;
+    if (fnorm >= (double)0.01f) {
+      double cmult;
+      if (M.vp_nflow != 1.0) cmult = M.vp_gamma * (exp(M.vp_delta * fnorm) - 1.0);
+      else cmult = M.vp_gamma * (M.vp_delta == 1.0 ? fnorm : pow(fnorm, M.vp_delta));
+      // yieldf09
+      double va2[4] = {0.0, 0.0, 0.0, 0.0};
+      if (steff > 0) {
+        for (int i = 0; i < 4; i++) va2[i] = dv[i] / (2.0 * steff);
+        va2[2] = dv[2] / steff;
+      }
+      double cons1 = 0.0, cons2, cons3 = 0.0;
+      const double va3[4] = {dv[1] * dv[3] + varj2 / 3.0, dv[0] * dv[3] + varj2 / 3.0,
+                             -((2.0 * dv[2]) * dv[3]), (dv[0] * dv[1] - dv[2] * dv[2]) + varj2 / 3.0};
+      if (lode) {
+        const double tanth = tan(theta), tant3 = tan(3.0 * theta), sinth = sin(theta),
+                     costh = cos(theta), cost3 = cos(3.0 * theta);
+        const double abthe = fabs(theta * (double)57.29577951308f);
+        if (M.ncrit == 1) {
+          if (abthe >= 29.0) {
+            cons2 = root3;
+          } else {
+            cons2 = 2.0 * (costh + sinth * tant3);
+            cons3 = (root3 * sinth) / (varj2 * cost3);
+          }
+        } else {
+          cons1 = M.vp_cons1;
+          if (abthe >= 29.0) {
+            const double plumi = theta > 0.0 ? -1.0 : 1.0;
+            cons2 = 0.5 * (root3 + (plumi * cons1) * root3);
+          } else {
+            cons2 = costh * ((1.0 + tanth * tant3) + (cons1 * (tant3 - tanth)) * root3);
+            cons3 = (root3 * sinth + (3.0 * cons1) * costh) / ((2.0 * varj2) * cost3);
+          }
+        }
+      } else if (M.ncrit == 2) {
+        cons2 = root3;
+      } else {
+        cons1 = M.vp_cons1;
+        cons2 = 1.0;
+      }
+      const double va1[4] = {1.0, 1.0, 0.0, 1.0};
+      for (int i = 0; i < 4; i++)
+        vivel[i] = cmult * ((cons1 * va1[i] + cons2 * va2[i]) + cons3 * va3[i]);
+    }
+  }
+  for (int i = 0; i < 4; i++) {
+    double g = 0.0;
+    for (int j = 0; j < 4; j++) g = g - M.vp_D[4 * i + j] * vivel[j];
+    Gs[i] = g;
   }
 }
 

@@ -341,6 +341,45 @@ extern "C" {
 
 namespace {
 
+// the per-material constants of the viscoplastic laws (invar09, yieldf09, Get_Dmatx in
+// 3_SPH_material_2018.f90), with the expressions the reference evaluates per call
+void viscoplastic_constants(const sps_params& q, sps::Real& M) {
+  const double root3 = (double)std::sqrt(3.0f);
+  const double young = q.props[2], poiss = q.props[3];
+  M.vp_fdatm0 = q.props[6];
+  M.vp_hards = q.props[7];
+  M.vp_gamma = q.props[9];
+  M.vp_delta = q.props[10];
+  M.vp_nflow = q.props[11];
+  M.vp_snphi = std::sin(q.props[8] * (double)0.017453292f);
+  M.vp_den = root3 * (3.0 - M.vp_snphi);
+  M.vp_cons1 = M.ncrit == 3 ? M.vp_snphi / 3.0 : (2.0 * M.vp_snphi) / M.vp_den;
+  double* D = M.vp_D;
+  for (int k = 0; k < 16; k++) D[k] = 0.0;
+  if (q.ntype_solid == 1) {  // plane stress
+    const double c = young / (1.0 - poiss * poiss);
+    D[0] = c;
+    D[5] = c;
+    D[1] = c * poiss;
+    D[4] = c * poiss;
+    D[10] = ((1.0 - poiss) * c) / 2.0;
+  } else {  // plane strain (2), axisymmetric (3)
+    const double c = (young * (1.0 - poiss)) / ((1.0 + poiss) * (1.0 - 2.0 * poiss));
+    const double cp = (c * poiss) / (1.0 - poiss);
+    D[0] = c;
+    D[5] = c;
+    D[1] = cp;
+    D[4] = cp;
+    D[3] = cp;
+    D[7] = cp;
+    D[12] = cp;
+    D[13] = cp;
+    D[15] = c;
+    D[10] = q.ntype_solid == 2 ? ((1.0 - 2.0 * poiss) * c) / (2.0 * (1.0 - poiss))
+                               : (c * (1.0 - 2.0 * poiss)) / (2.0 * (1.0 - poiss));
+  }
+}
+
 // the checks sps_create makes on one problem
 int check_params(const sps_params* p) {
   if (p->ndimn != 2 || p->nstre != 4)
@@ -350,9 +389,18 @@ int check_params(const sps_params* p) {
   if (p->nnode <= 0 || p->nstress < 0 || p->ndummy < 0 || p->ndummy2 < 0 || p->ndummy2 > p->ndummy)
     return fail(nullptr, SPS_ERR_ARG, "inconsistent particle counts");
   int ntype_eco = (int)p->props[0], ncrit = (int)p->props[1];
-  if (ntype_eco > 1 && ncrit != 12)
+  if (ntype_eco > 1 && ncrit == 5)
     return fail(nullptr, SPS_ERR_UNSUPPORTED,
-                "only the Drucker-Prager law (ncrit = 12) or elastic (ntype_eco = 1) is implemented");
+                "Modified Cam Clay (ncrit = 5): the reference never integrates its yield-surface "
+                "size Internal_Vars(3), which stays 0 and divides yieldf09's flow vector");
+  if (ntype_eco > 1 && !((ncrit >= 1 && ncrit <= 4) || ncrit == 12))
+    return fail(nullptr, SPS_ERR_UNSUPPORTED,
+                "material law: ncrit must be 1-4 (viscoplastic) or 12 (Drucker-Prager)");
+  if (ntype_eco > 1 && ncrit <= 4 && !(p->props[6] > (double)0.001f))
+    return fail(nullptr, SPS_ERR_ARG,
+                "viscoplastic law: initial yield stress must exceed 0.001 (invar09 stops)");
+  if (ntype_eco > 1 && ncrit <= 4 && (p->ntype_solid < 1 || p->ntype_solid > 3))
+    return fail(nullptr, SPS_ERR_UNSUPPORTED, "viscoplastic law: ntype_solid must be 1, 2 or 3");
   if (p->skf < 1 || p->skf > 3) return fail(nullptr, SPS_ERR_ARG, "skf must be 1, 2 or 3");
   if (p->no_bcs > sps::kMaxBC) return fail(nullptr, SPS_ERR_UNSUPPORTED, "more than 16 BCs");
   if (p->no_bcs > 0 && !p->bc_list) return fail(nullptr, SPS_ERR_ARG, "bc_list missing");
@@ -476,6 +524,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
         M.xmax_dom[d] = q.xmax_domain[d];
         M.cgrav[d] = q.cgrav[d];
       }
+      viscoplastic_constants(q, M);
     }
     D.capC = D.capS = D.capH = 0;  // sized at upload from the kernel support
     D.skf = p->skf;

@@ -111,7 +111,9 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
       double s2v[4] = {st[0], st[1], st[2], st[3]};
       if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
       double vivel[4] = {0.0, 0.0, 0.0, 0.0}, G2[4];
-      if (M.ncrit == 12) {
+      if (M.ncrit <= 4) {
+        viscoplastic(M, s2v, D.iv1[t], vivel, Gs);
+      } else if (M.ncrit == 12) {
         double f = D.fdp[t];
         drucker_prager<FAST>(M, sc.time_sph, s2v, g, &f, G2, vivel);
         D.fdp[t] = f;

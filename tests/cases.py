@@ -60,10 +60,13 @@ def bui_like(width=4.0, height=2.0, dx=0.1, young=1.8e6, poiss=0.3, rho=1850.0,
 
 
 def bc_case(width=0.5, height=1.0, dx=0.05, young=8e7, poiss=0.25, rho=2000.0, dt=1e-5,
-            plastic=False, cspm=True, xsph=False, sml=1.2):
+            plastic=False, cspm=True, xsph=False, sml=1.2, ncrit=12, yield_stress=5e5,
+            hards=0.0, phi_deg=0.0, gamma=50.0, delta=1.0, nflow=1, ntype_solid=2):
     """Biaxial-style sample without walls and with segment and nodal boundary conditions,
     a time-curve platen velocity, a sinusoidal lateral stress and a time-curve stress,
-    in the style of the strain-localisation example's input."""
+    in the style of the strain-localisation example's input.  ncrit 12: Drucker-Prager
+    (tan phi 0.7, c 100 Pa); ncrit 1-4: the viscoplastic laws with the yield stress,
+    hardening modulus, friction angle and Perzyna parameters given."""
     pts = "\n".join([
         "geom_type", "1", "x1 x2 x3 x4 dx",
         "0 %s 0 %s %s" % (_fmt(width), _fmt(width), _fmt(dx)),
@@ -71,12 +74,14 @@ def bc_case(width=0.5, height=1.0, dx=0.05, young=8e7, poiss=0.25, rho=2000.0, d
         "0 0 %s %s %s" % (_fmt(height), _fmt(height), _fmt(dx)),
         "dummy_nodes", "F", ""])
     W, H = _fmt(width), _fmt(height)
+    law = ["tan(phi) cohesion", "0.7 100.0 0 0 0 0 0 0"] if ncrit in (5, 12) else []
     dat = "\n".join([
-        "1", "bc test", "ndimn", "2", "ntype_solid nstre nmats", "2 4 1",
+        "1", "bc test", "ndimn", "2", "ntype_solid nstre nmats", "%d 4 1" % ntype_solid,
         "mater. eco law E Poiss b rho yield H fi gamma delta n",
-        "1 %d 12 %s %s 1. %s 5.e5 0 0. 50. 1. 1" % (2 if plastic else 1, _fmt(young),
-                                                   _fmt(poiss), _fmt(rho)),
-        "tan(phi) cohesion", "0.7 100.0 0 0 0 0 0 0",
+        "1 %d %d %s %s 1. %s %s %s %s %s %s %d" % (
+            2 if plastic else 1, ncrit, _fmt(young), _fmt(poiss), _fmt(rho),
+            _fmt(yield_stress), _fmt(hards), _fmt(phi_deg), _fmt(gamma), _fmt(delta), nflow)
+    ] + law + [
         "ic_unks", "0", "no. of BC's Sigman=0", "6 0",
         "nber var t_variation a1 a0 w fi Tf",
         "1 5 1 0 0 0 0 0",

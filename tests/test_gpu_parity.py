@@ -95,6 +95,56 @@ def test_stress_free_surface(built_gpu):
     assert (f["bc_or_not"] == 2).any()
 
 
+def _visco(ncrit, **kw):
+    # an initial deviatoric stress above the yield surface of each law, a Perzyna fluidity
+    # small enough for the explicit step to stay stable, and softening as in the
+    # strain-localisation example
+    base = dict(plastic=True, cspm=False, ncrit=ncrit, hards=-8e5, phi_deg=30.0, gamma=0.5,
+                delta=1.0, nflow=1, yield_stress={1: 1.5e4, 2: 1.5e4, 3: 1e3, 4: 1e3}[ncrit])
+    base.update(kw)
+    p = cases.bc_case(**base)
+    p.stress[:4 * p.ntotal] = np.tile([-4e4, -1e4, 5e3, -1.25e4], p.ntotal)  # initial stress
+    return p
+
+
+@pytest.mark.parametrize("ncrit", [2, 4])
+def test_viscoplastic_bitwise(built_gpu, ncrit):
+    # von Mises and Drucker-Prager viscoplasticity with Perzyna n = 1, delta = 1: no
+    # transcendental function is evaluated, so the path is bit-exact
+    p = _visco(ncrit)
+    f = _compare(p, 20, chunks=[6, 14])
+    o = _orc_ctx(p)
+    o.upload_problem(p)
+    o.step(20, 0.0)
+    assert (o.download()["intvars1"][p.nnode:] > 0).any()  # plastic flow took place
+
+
+def _close(problem, nsteps, rtol):
+    g = _gpu_ctx(problem)
+    o = _orc_ctx(problem)
+    cases.run_pair(problem, nsteps, [g, o])
+    fg, fo = g.download(), o.download()
+    for k in ("x", "vel", "stress", "intvars1"):
+        a, b = fg[k], fo[k]
+        if k == "stress":
+            a, b = a[:4 * problem.ntotal], b[:4 * problem.ntotal]
+        scale = np.abs(b).max() + 1e-300
+        assert np.abs(a - b).max() <= rtol * scale, (k, np.abs(a - b).max() / scale)
+    return fo
+
+
+@pytest.mark.parametrize("ncrit,extra", [(1, {}), (3, {}), (2, dict(nflow=2, delta=1.5)),
+                                         (4, dict(delta=2.0))],
+                         ids=["tresca", "mohr_coulomb", "vm_exp_flow", "dp_power_flow"])
+def test_viscoplastic_close(built_gpu, ncrit, extra):
+    # Tresca and Mohr-Coulomb read the Lode angle through asin, sin, cos and tan, and the
+    # other Perzyna forms call exp or pow: CUDA's and the host libm's results may differ in
+    # the last bit, so these are compared with a relative tolerance of 1e-9
+    p = _visco(ncrit, **extra)
+    fo = _close(p, 20, 1e-9)
+    assert (fo["intvars1"][p.nnode:] > 0).any()
+
+
 def test_standard_sph(built_gpu):
     p = cases.standard_sph()
     _compare(p, 6)
@@ -127,6 +177,12 @@ def test_capacity_error(built_gpu):
 
 def test_unsupported_options(built_gpu):
     p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
+    cam_clay = cases.bc_case(plastic=True, ncrit=5)
+    with pytest.raises(sps_gb300.SpsError, match="Cam Clay"):
+        _gpu_ctx(cam_clay)
+    weak = _visco(2, yield_stress=1e-4)  # invar09 stops below 0.001
+    with pytest.raises(sps_gb300.SpsError):
+        _gpu_ctx(weak)
     for over in (dict(art_stress=1), dict(inside_approach=0), dict(skf=7)):
         with pytest.raises(sps_gb300.SpsError):
             _gpu_ctx(p, **over)
