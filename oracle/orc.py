@@ -52,6 +52,8 @@ def lib():
         L.orc_viscoplastic.argtypes = [P(C.c_double), C.c_int, P(C.c_double), C.c_double,
                                        P(C.c_double), P(C.c_double)]
         L.orc_viscoplastic.restype = None
+        L.orc_artificial_force.argtypes = [C.c_void_p, P(C.c_double)]
+        L.orc_artificial_force.restype = None
         _LIB = L
     return _LIB
 

@@ -48,7 +48,7 @@ struct orc_ctx {
   double *x, *vel, *stress, *mass, *rho, *hsml, *x00, *x0, *vx0, *displ;
   int32_t *itype, *out_domain, *bc_or_not, *bc_info, *bc_int;
   double *intvars1, *f_drucker, *grad_u, *Ddev;
-  double *f_bound, *art_visc;
+  double *f_bound, *art_visc, *art_force;
   double *normal, *subset; /* module arrays of get_nodes_on_free_surface, (2,ntotal), (ntotal) */
   /* pair list, creation order */
   int64_t npairs, cap, m_pairs;
@@ -859,6 +859,68 @@ static void boundary_forces(orc_ctx* c) {
   }
 }
 
+/* artificial_force (2_SPH_main_2018.f90:908-1016): Monaghan's artificial stress over the
+   node-node pairs in walk order.  Per particle, the principal stresses of the in-plane
+   stress (angle 0.5 atan(2 s12 / (s11 - s22)), 0 unless s11 - s22 >= 1e-8), their tensile
+   parts scaled by -eps / rho^2, and the reference's rotation back (whose second component
+   is R2(1) (cos^2 + sin^2)); per pair, f = W / W(dx, h0) with h0 = 1.2 dx and the power
+   n = 2.55.  eps, n, 1.2 and 1e-8 are FP32 literals. */
+static void art_R(const orc_ctx* c, int i, double* R) {
+  const double eps = (double)0.1f;
+  const double s12 = S(c, 0, i) - S(c, 1, i);
+  double th = 0.0;
+  if (s12 >= (double)1e-08f) th = 0.5 * atan((2.0 * S(c, 2, i)) / s12);
+  const double co = cos(th), si = sin(th), cc = co * co, ss = si * si;
+  const double cs2 = (2.0 * co) * si;
+  double sig[2], R2[2];
+  sig[0] = (cc * S(c, 0, i) + cs2 * S(c, 2, i)) + ss * S(c, 1, i);
+  sig[1] = (ss * S(c, 0, i) - cs2 * S(c, 2, i)) + cc * S(c, 1, i);
+  for (int k = 0; k < 2; k++)
+    R2[k] = sig[k] > 0 ? -(eps * (sig[k] / (c->rho[i] * c->rho[i]))) : 0.0;
+  R[0] = R2[0] * cc + R2[1] * ss;
+  R[1] = R2[0] * (cc + ss);
+  R[2] = (R2[0] - R2[1]) * (co * si);
+}
+
+static void artificial_force(orc_ctx* c) {
+  const int NN = c->NN;
+  const double n = (double)2.55f;
+  const double hsml0 = (double)1.2f * c->p.dx;
+  const double dx2[2] = {c->p.dx, c->p.dy};
+  double w2, g2[2];
+  orc_kernel(c->p.skf, c->p.pi, c->p.dx, dx2, hsml0, &w2, g2);
+  double* tmp = xcalloc(6 * (size_t)NN, sizeof(double)); /* (istre, d, i) */
+#define T(k, d, i) tmp[(k) + 3 * ((d) + 2 * (size_t)(i))]
+  for (int64_t k = 0; k < c->npairs; k++) {
+    int64_t q = c->order[k];
+    if (c->ptype[q] != 3) continue;
+    const int i = c->pi[q], j = c->pj[q];
+    double Ri[3], Rj[3];
+    art_R(c, i, Ri);
+    art_R(c, j, Rj);
+    const double fn = pow((double)c->pw[q] / w2, n);
+    for (int st = 0; st < 3; st++) {
+      const double h1 = ((double)c->pdx[q] * fn) * (Ri[st] + Rj[st]);
+      T(st, 0, i) = T(st, 0, i) + c->mass[j] * h1;
+      T(st, 0, j) = T(st, 0, j) - c->mass[i] * h1;
+      const double h2 = ((double)c->pdy[q] * fn) * (Ri[st] + Rj[st]);
+      T(st, 1, i) = T(st, 1, i) + c->mass[j] * h2;
+      T(st, 1, j) = T(st, 1, j) - c->mass[i] * h2;
+    }
+  }
+  for (int i = 0; i < NN; i++) {
+    c->art_force[0 + 2 * (size_t)i] = T(0, 0, i) + T(2, 1, i);
+    c->art_force[1 + 2 * (size_t)i] = T(2, 0, i) + T(1, 1, i);
+  }
+#undef T
+  free(tmp);
+}
+
+void orc_artificial_force(orc_ctx* c, double* out) {
+  artificial_force(c);
+  memcpy(out, c->art_force, sizeof(double) * 2 * (size_t)c->NN);
+}
+
 /* artificial_viscosity (2_SPH_main_2018.f90:826-904): FP32 accumulators */
 static void artificial_viscosity(orc_ctx* c) {
   const int NN = c->NN;
@@ -1004,6 +1066,7 @@ static void rk4(orc_ctx* c) {
     gravity_force(c, grav);
     if (c->p.inside_approach) boundary_forces(c);
     if (c->p.alpha > 0 || c->p.beta > 0) artificial_viscosity(c);
+    if (c->p.art_stress) artificial_force(c);
     if (c->p.update_x) {
       for (int i = NN; i < NT; i++) {
         const double* g = &c->grad_u[4 * (size_t)i];
@@ -1022,7 +1085,7 @@ static void rk4(orc_ctx* c) {
     for (int i = 0; i < NN; i++)
       for (int d = 0; d < 2; d++) {
         size_t o = d + 2 * (size_t)i;
-        RHS2[o] = (((-div2[o] + grav[o]) + c->art_visc[o]) + c->f_bound[o]) + 0.0;
+        RHS2[o] = (((-div2[o] + grav[o]) + c->art_visc[o]) + c->f_bound[o]) + c->art_force[o];
       }
     for (int i = 0; i < NN; i++)
       for (int d = 0; d < 2; d++) RKv[d + 2 * (size_t)i] += f2rk[st] * RHS2[d + 2 * (size_t)i];
@@ -1316,7 +1379,6 @@ int orc_create(const sps_params* p, orc_ctx** out) {
   if (!p || !out) return SPS_ERR_ARG;
   *out = NULL;
   if (p->ndimn != 2 || p->nstre != 4) return SPS_ERR_UNSUPPORTED;
-  if (p->art_stress) return SPS_ERR_UNSUPPORTED;
   if (p->nnode <= 0 || p->nstress < 0 || p->ndummy < 0 || p->ndummy2 < 0 ||
       p->ndummy2 > p->ndummy)
     return SPS_ERR_ARG;
@@ -1383,6 +1445,7 @@ int orc_create(const sps_params* p, orc_ctx** out) {
   c->Ddev = xcalloc(NT, sizeof(double));
   c->f_bound = xcalloc(2 * NN, sizeof(double));
   c->art_visc = xcalloc(2 * NN, sizeof(double));
+  c->art_force = xcalloc(2 * NN, sizeof(double));
   c->which_cell = xcalloc(N2, sizeof(int32_t));
   c->cell_list = xcalloc(N2, sizeof(int32_t));
   for (size_t i = 0; i < NT; i++) c->bc_info[8 * i] = (int32_t)(i + 1);
@@ -1483,7 +1546,7 @@ void orc_destroy(orc_ctx* c) {
                   c->x00, c->x0, c->vx0, c->displ, c->itype, c->out_domain, c->bc_or_not,
                   c->bc_info, c->bc_int, c->intvars1, c->f_drucker, c->grad_u, c->Ddev,
                   c->normal, c->subset,
-                  c->f_bound, c->art_visc, c->pi, c->pj, c->ptype, c->pw, c->pdx, c->pdy,
+                  c->f_bound, c->art_visc, c->art_force, c->pi, c->pj, c->ptype, c->pw, c->pdx, c->pdy,
                   c->order, c->which_cell, c->cell_cnt, c->cell_start, c->cell_list};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(c);

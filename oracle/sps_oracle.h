@@ -45,6 +45,8 @@ void orc_kernel(int32_t skf, double pi, double r, const double* dx2, double hsml
                 double* dwdx);
 /* adapt_stress2 (3_SPH_material_2018.f90:2087) on one stress vector, for invariant tests */
 void orc_adapt_stress(double tanfi, double coh, double* stress4);
+/* artificial_force over the current pair list and state: art_force (2,nnode) */
+void orc_artificial_force(orc_ctx* c, double* out);
 /* the viscoplastic laws of plastic_terms (ncrit 1-4): vivel and Gs = -Dmatx vivel */
 void orc_viscoplastic(const double* props, int ntype_solid, const double* stress4, double iv1,
                       double* vivel, double* Gs);

@@ -132,6 +132,8 @@ struct Dev {
   double *RKv[2], *RKs[4], *RKr, *RKh, *RKd;
   double *RHS1[4], *RHS2[2], *RHSr, *RHSh;
   double *fbx, *fby;  // boundary force (nodes), once per step
+  int art_stress;      // artificial_force on (input.txt art_stress)
+  double* artR;        // its per-node rotated tensile stresses R(3) of the stage, (3, NN)
   double *vol, *rinv;  // m / rho and 1 / rho per particle (refreshed when rho changes)
   double* A[3];        // sigma_k / (rho * rho) of the stage, per particle
   // FP32 form: packed neighbour records (written by the per-particle kernels)

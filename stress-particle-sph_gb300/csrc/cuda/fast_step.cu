@@ -308,7 +308,9 @@ __global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage,
     g2v[4] = -(q4.val() + 2.0 * At[1] * Sy);
     g2v[5] = -(q5.val() + 2.0 * At[2] * Sy);
     double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
-    tail_node(D, sc, t, g2v, AE, bc_int, avx, avy, f2);
+    double afx = 0.0, afy = 0.0;
+    if (D.art_stress) art_force_node(D, s, t, &afx, &afy);
+    tail_node(D, sc, t, g2v, AE, bc_int, avx, avy, f2, afx, afy);
   }
 }
 

@@ -376,6 +376,29 @@ __global__ void k_vol(Dev D, int lo, int hi) {
   }
 }
 
+// artificial_force's per-particle part (2_SPH_main_2018.f90:930-981) for every node, from
+// the stage's node stresses: the principal stresses at angle 0.5 atan(2 s12 / (s11 - s22))
+// (0 unless s11 - s22 >= 1e-8), their tensile parts times -eps / rho^2 (eps = 0.1), rotated
+// back as the reference does (its second component is R2(1) (cos^2 + sin^2))
+__global__ void k_art_R(Dev D) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.NN) return;
+  const double eps = (double)0.1f;
+  const double s0 = D.s0[i], s1 = D.s1[i], s2 = D.s2[i], rho = D.rho[i];
+  const double s12 = s0 - s1;
+  double th = 0.0;
+  if (s12 >= (double)1e-08f) th = 0.5 * atan((2.0 * s2) / s12);
+  const double co = cos(th), si = sin(th), cc = co * co, ss = si * si;
+  const double cs2 = (2.0 * co) * si;
+  const double sig0 = (cc * s0 + cs2 * s2) + ss * s1;
+  const double sig1 = (ss * s0 - cs2 * s2) + cc * s1;
+  const double R20 = sig0 > 0 ? -(eps * (sig0 / (rho * rho))) : 0.0;
+  const double R21 = sig1 > 0 ? -(eps * (sig1 / (rho * rho))) : 0.0;
+  D.artR[i] = R20 * cc + R21 * ss;
+  D.artR[D.NN + i] = R20 * (cc + ss);
+  D.artR[2 * (size_t)D.NN + i] = (R20 - R21) * (co * si);
+}
+
 // get_derivatives (2_SPH_main_2018.f90:487-648) + the per-particle stage work of RK4
 __global__ void k_derivs(Dev D, int stage) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -506,7 +529,9 @@ __global__ void k_derivs(Dev D, int stage) {
       avx = -(double)ax;
       avy = -(double)ay;
     }
-    tail_node(D, sc, t, g2, AE, bc_int, avx, avy, f2);
+    double afx = 0.0, afy = 0.0;
+    if (D.art_stress) art_force_node(D, s, t, &afx, &afy);
+    tail_node(D, sc, t, g2, AE, bc_int, avx, avy, f2, afx, afy);
   }
 }
 
@@ -707,6 +732,10 @@ int launch_plain_step(Ctx& c) {
     }
     c.mark("adapt_bc");
     k_adapt_bc<<<c.grid_of(TK_ADAPT, D.NT), c.blk[TK_ADAPT], 0, st>>>(D, 1);
+    if (D.art_stress) {
+      c.mark("art_R");
+      k_art_R<<<nbN, kBlock, 0, st>>>(D);
+    }
     c.mark("derivs");
     if (D.fast) launch_fderivs(c, stage);
     else k_derivs<<<c.grid_of(TK_DERIVS, D.N2), c.blk[TK_DERIVS], 0, st>>>(D, stage);

@@ -384,8 +384,6 @@ void viscoplastic_constants(const sps_params& q, sps::Real& M) {
 int check_params(const sps_params* p) {
   if (p->ndimn != 2 || p->nstre != 4)
     return fail(nullptr, SPS_ERR_UNSUPPORTED, "only ndimn = 2, nstre = 4 are implemented");
-  if (p->art_stress)
-    return fail(nullptr, SPS_ERR_UNSUPPORTED, "artificial stress is outside the hot path");
   if (p->nnode <= 0 || p->nstress < 0 || p->ndummy < 0 || p->ndummy2 < 0 || p->ndummy2 > p->ndummy)
     return fail(nullptr, SPS_ERR_ARG, "inconsistent particle counts");
   int ntype_eco = (int)p->props[0], ncrit = (int)p->props[1];
@@ -425,7 +423,7 @@ bool same_flags(const sps_params& a, const sps_params& b) {
   return a.sp_sph == b.sp_sph && a.inside_approach == b.inside_approach && a.cspm == b.cspm &&
          a.xsph == b.xsph && a.update_x == b.update_x && a.cont_density == b.cont_density &&
          a.sle == b.sle && a.skf == b.skf && a.precision == b.precision && a.pi == b.pi &&
-         a.ntype_solid == b.ntype_solid;
+         a.ntype_solid == b.ntype_solid && a.art_stress == b.art_stress;
 }
 
 }  // namespace
@@ -611,6 +609,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.RHSr = dalloc<double>(c, NT);
     D.RHSh = dalloc<double>(c, NT);
     D.fbx = dalloc<double>(c, NN_);
+    D.art_stress = p->art_stress ? 1 : 0;
+    D.artR = D.art_stress ? dalloc<double>(c, 3 * (size_t)NN_) : nullptr;
     D.fby = dalloc<double>(c, NN_);
     D.Ddev = dalloc<double>(c, NT);
     D.vol = dalloc<double>(c, N2);

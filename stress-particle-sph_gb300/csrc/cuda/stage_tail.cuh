@@ -164,10 +164,40 @@ __device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int
   tail_sp_rates(D, sc, t, g, f2);
 }
 
-// node tail: g2 = grad2(s,b) at s + 3b, AE = CSPM moments, av = artificial viscosity
+// artificial_force (2_SPH_main_2018.f90:908-1016) on node t (sorted slot s): the node-node
+// pairs in the reference's walk order, h = (dW f^n) (R_t + R_u) with f = W / W(dx, 1.2 dx)
+// and n = 2.55, dW taken w.r.t. t (so t's side of the pair gets + m_u h as pair_i and
+// - m_u h as pair_j, the same numbers); art_force = (T11 + T32, T31 + T22).
+__device__ __forceinline__ void art_force_node(const Dev& D, int s, int t, double* afx,
+                                               double* afy) {
+  const Real& M = real_of(D, t);
+  double w2, g0, g1;
+  sph_kernel(D.skf, D.pi, M.dx, M.dx, M.dx, (double)1.2f * M.dx, &w2, &g0, &g1);
+  const double n = (double)2.55f;
+  const double Rt[3] = {D.artR[t], D.artR[D.NN + t], D.artR[2 * (size_t)D.NN + t]};
+  double T[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+  const int degs = D.degS[s];
+  for (int k = 0; k < degs; k++) {
+    const int4 e = D.same[(size_t)k * D.N2 + s];
+    const int u = e.x;
+    const double fn = pow((double)__int_as_float(e.y) / w2, n);
+    const double mu = D.mass[u];
+    const double gx = (double)__int_as_float(e.z), gy = (double)__int_as_float(e.w);
+    for (int q = 0; q < 3; q++) {
+      const double r = Rt[q] + D.artR[(size_t)q * D.NN + u];
+      T[q][0] = T[q][0] + mu * ((gx * fn) * r);
+      T[q][1] = T[q][1] + mu * ((gy * fn) * r);
+    }
+  }
+  *afx = T[0][0] + T[2][1];
+  *afy = T[2][0] + T[1][1];
+}
+
+// node tail: g2 = grad2(s,b) at s + 3b, AE = CSPM moments, av = artificial viscosity,
+// af = artificial force
 __device__ __forceinline__ void tail_node(const Dev& D, const StepScalars& sc, int t, double* g2,
                                           double* AE, int bc_int, double avx, double avy,
-                                          double f2) {
+                                          double f2, double afx = 0.0, double afy = 0.0) {
   D.bc_int[t] = bc_int;
   if (D.cspm) {
     double A4 = AE[0] * AE[3] - AE[1] * AE[2];
@@ -194,8 +224,8 @@ __device__ __forceinline__ void tail_node(const Dev& D, const StepScalars& sc, i
   double gy = (M.ic_grav == 1) ? sc.factg * M.cgrav[1] : 0.0;
   gx = gx - M.damping * vtx;
   gy = gy - M.damping * vty;
-  double rhsx = (((-div2x + gx) + avx) + D.fbx[t]) + 0.0;
-  double rhsy = (((-div2y + gy) + avy) + D.fby[t]) + 0.0;
+  double rhsx = (((-div2x + gx) + avx) + D.fbx[t]) + afx;
+  double rhsy = (((-div2y + gy) + avy) + D.fby[t]) + afy;
   D.RHS2[0][t] = rhsx;
   D.RHS2[1][t] = rhsy;
   D.RKv[0][t] = D.RKv[0][t] + f2 * rhsx;

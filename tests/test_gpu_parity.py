@@ -145,6 +145,40 @@ def test_viscoplastic_close(built_gpu, ncrit, extra):
     assert (fo["intvars1"][p.nnode:] > 0).any()
 
 
+def _tensile(**kw):
+    # a cohesive block with a tensile initial stress (admissible: below the tension-cut
+    # apex), so that the nodes' principal tensile stresses drive the artificial force
+    p = cases.bui_like(art_stress=True, **kw)
+    p.stress[:4 * p.ntotal] = np.tile([2e3, -1e3, 5e2, 3e2], p.ntotal)
+    return p
+
+
+@pytest.mark.parametrize("precision", ["plain", "fp32"])
+def test_artificial_stress_close(built_gpu, precision):
+    # artificial_force calls atan, cos, sin and pow: CUDA's and the host libm's results may
+    # differ in the last bit, so the plain path is compared at 1e-10 relative; the FP32
+    # form at its own accuracy
+    p = _tensile()
+    if precision == "plain":
+        fo = _close(p, 12, 1e-10)
+    else:
+        g = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                  p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+        o = _orc_ctx(p)
+        cases.run_pair(p, 12, [g, o])
+        fg, fo = g.download(), o.download()
+        for k in ("x", "vel"):
+            scale = np.abs(fo[k]).max() + 1e-300
+            assert np.abs(fg[k] - fo[k]).max() <= 1e-4 * scale, k
+    # the force acts: the run differs from the same run without it
+    q = cases.bui_like()
+    q.stress[:4 * q.ntotal] = p.stress[:4 * p.ntotal]
+    o2 = _orc_ctx(q)
+    o2.upload_problem(q)
+    o2.step(12, 0.0)
+    assert not np.array_equal(o2.download()["vel"], fo["vel"])
+
+
 def test_standard_sph(built_gpu):
     p = cases.standard_sph()
     _compare(p, 6)
@@ -183,7 +217,7 @@ def test_unsupported_options(built_gpu):
     weak = _visco(2, yield_stress=1e-4)  # invar09 stops below 0.001
     with pytest.raises(sps_gb300.SpsError):
         _gpu_ctx(weak)
-    for over in (dict(art_stress=1), dict(inside_approach=0), dict(skf=7)):
+    for over in (dict(inside_approach=0), dict(skf=7)):
         with pytest.raises(sps_gb300.SpsError):
             _gpu_ctx(p, **over)
 
