@@ -82,6 +82,9 @@ int sph_problem_slope(const sph_slope_spec* spec, sph_problem** out);
 
 const sps_params* sph_problem_params(const sph_problem* p);
 
+/* sizeof(sps_params) as this library was compiled, for bindings that mirror the struct */
+int32_t sph_sizeof_params(void);
+
 /* The output flags read by problem_input_data (code/3_SPH_material_2018.f90:333-336):
    stress_out(1:4), vel_out(1:2), strain_out, rho_out, sml_out, disp_out. */
 int sph_problem_output_flags(const sph_problem* p, int32_t* flags);

@@ -60,7 +60,7 @@ typedef struct sps_params {
 
   /* solver flags (.dat `pa_sph nnps sle skf CSPM update_x XSPH`, input.txt) */
   int32_t sp_sph, inside_approach, cspm, xsph, update_x, cont_density, sle, skf;
-  int32_t art_stress; /* must be 0 (artificial stress is not in the hot path) */
+  int32_t art_stress; /* Monaghan's artificial stress (artificial_force)              */
 
   /* material props(1,1..20): 1 ntype_eco, 2 ncrit, 3 E, 4 nu, 6 rho, 13 tan(phi), 14 c */
   double props[20];
@@ -98,6 +98,17 @@ typedef struct sps_params {
   int32_t precision;      /* SPS_PREC_*                                      */
   int32_t max_neighbours; /* neighbour capacity per particle (two lists of half this size);
                              0 = sized from the kernel support at upload */
+
+  /* outside approach (inside_approach = 0): input.txt `SPH_shifting vel_vector
+     shift_update rx_factor ry_factor disp_tol` (code/3_SPH_material_2018.f90:388-396);
+     stress-point j of node i is particle nnode + npoints*(i-1) + j */
+  int32_t npoints;      /* stress-points per node (2 with vel_vector)                  */
+  int32_t sph_shift;    /* SPH_shift: re-interpolate the step after a shift            */
+  int32_t vel_vector;   /* orient the two stress-points along the node velocity        */
+  int32_t shift_update; /* reposition the stress-points every shift_update steps (>= 1) */
+  double r_x, r_y;      /* shift distances dx*rx_factor, dx*ry_factor                  */
+  double disp_tol;      /* vel_vector: node displacement since the last shift, in dx,
+                           above which its stress-points are repositioned              */
 } sps_params;
 
 typedef struct sps_ctx sps_ctx;

@@ -49,6 +49,10 @@ struct orc_ctx {
   int32_t *itype, *out_domain, *bc_or_not, *bc_info, *bc_int;
   double *intvars1, *f_drucker, *grad_u, *Ddev;
   double *f_bound, *art_visc, *art_force;
+  /* outside approach: itimestep_sph of the step being taken (0 before the first step after
+     an upload), and the velocity-vector variant's x_10(2,nnode), disp_10(nnode) */
+  int64_t itimestep;
+  double *x10, *disp10;
   double *normal, *subset; /* module arrays of get_nodes_on_free_surface, (2,ntotal), (ntotal) */
   /* pair list, creation order */
   int64_t npairs, cap, m_pairs;
@@ -1330,13 +1334,101 @@ static void xsph_update(orc_ctx* c) {
   free(xl);
 }
 
+/* shift_stress_points (2_SPH_main_2018.f90:244-368) with isolated_nodes (:373-398): every
+   shift_update steps the stress-points are placed again around their nodes (fixed offsets
+   r_x, r_y, or along the node velocity with the velocity-vector variant); then, every step,
+   the stress-points of nodes next to a wall moving faster than 0.4 and of nodes with fewer
+   than two node neighbours are put on their node.  cos_theta, sin_theta, r_x2 and abs_vel
+   are FP32 in the reference. */
+static void shift_stress_points(orc_ctx* c) {
+  const int NN = c->NN, np = c->p.npoints;
+  const double dx = c->p.dx, rx = c->p.r_x, ry = c->p.r_y;
+  if (c->itimestep % c->p.shift_update == 0) {
+    if (c->p.vel_vector) {
+      for (int i = 0; i < NN; i++) {
+        const double ex = X(c, 0, i) - c->x10[2 * (size_t)i];
+        const double ey = X(c, 1, i) - c->x10[2 * (size_t)i + 1];
+        c->disp10[i] = sqrt(ex * ex + ey * ey) / dx;
+      }
+      for (int i = 0; i < NN; i++) {
+        c->x10[2 * (size_t)i] = X(c, 0, i);
+        c->x10[2 * (size_t)i + 1] = X(c, 1, i);
+      }
+      for (int i = 0; i < NN; i++) {
+        const double v0 = V(c, 0, i), v1 = V(c, 1, i);
+        const float ct = (float)(v0 / sqrt(v0 * v0 + v1 * v1));
+        const float st = (float)(v1 / sqrt(v0 * v0 + v1 * v1));
+        float r0 = (float)((dx / 2) * (double)ct), r1 = (float)((dx / 2) * (double)st);
+        if (r0 > 0 && r0 < dx / 5) r0 = (float)((double)r0 + dx / 3.0);
+        if (r1 > 0 && r1 < dx / 5) r1 = (float)((double)r1 + dx / 3.0);
+        if (r0 < 0 && r0 > -(dx / 5)) r0 = (float)((double)r0 - dx / 3.0);
+        if (r1 < 0 && r1 > -(dx / 5)) r1 = (float)((double)r1 - dx / 3.0);
+        if (c->disp10[i] > c->p.disp_tol) {
+          const int k = NN + 2 * i;
+          X(c, 0, k) = X(c, 0, i) + (double)r0;
+          X(c, 1, k) = X(c, 1, i) + (double)r1;
+          X(c, 0, k + 1) = X(c, 0, i) - (double)r0;
+          X(c, 1, k + 1) = X(c, 1, i) - (double)r1;
+        }
+      }
+    } else {
+      for (int i = 0; i < NN; i++) {
+        const int k = NN + np * i;
+        if (np == 1) {
+          X(c, 0, k) = X(c, 0, i) + rx;
+          X(c, 1, k) = X(c, 1, i) + ry;
+        } else if (np == 2) { /* the second point's y offset is r_x in the reference */
+          X(c, 0, k) = X(c, 0, i) + rx;
+          X(c, 1, k) = X(c, 1, i) + ry;
+          X(c, 0, k + 1) = X(c, 0, i) - rx;
+          X(c, 1, k + 1) = X(c, 1, i) - rx;
+        } else if (np == 3) {
+          X(c, 0, k) = X(c, 0, i);
+          X(c, 1, k) = X(c, 1, i) + ry;
+          X(c, 0, k + 1) = X(c, 0, i) - rx;
+          X(c, 1, k + 1) = X(c, 1, i) - ry;
+          X(c, 0, k + 2) = X(c, 0, i) + rx;
+          X(c, 1, k + 2) = X(c, 1, i) - ry;
+        }
+      }
+    }
+  }
+  /* n_int: node-node pairs of each node (isolated_nodes; artificial_viscosity and
+     XSPH_update count the same pairs) */
+  int32_t* n_int = xcalloc((size_t)NN, sizeof(int32_t));
+  for (int64_t k = 0; k < c->npairs; k++)
+    if (c->ptype[k] == 3) {
+      n_int[c->pi[k]]++;
+      n_int[c->pj[k]]++;
+    }
+  for (int i = 0; i < NN; i++) {
+    const double v0 = V(c, 0, i), v1 = V(c, 1, i);
+    const float abs_vel = (float)sqrt(v0 * v0 + v1 * v1);
+    const int k = NN + np * i;
+    const int off = (c->bc_int[i] == 1 && abs_vel > 0.4f) || n_int[i] < 2;
+    if (off)
+      for (int q = 0; q < np && q < 3; q++) {
+        X(c, 0, k + q) = X(c, 0, i);
+        X(c, 1, k + q) = X(c, 1, i);
+      }
+  }
+  free(n_int);
+}
+
 /* time_integration (2_SPH_main_2018.f90:78-184) */
 static int time_integration(orc_ctx* c) {
   const int NN = c->NN, NT = c->NT;
   const int ncrit = (int)c->p.props[1];
+  const int outside = c->p.sp_sph && !c->p.inside_approach;
+  c->itimestep++;
   check_out_domain(c);
   if (grid_find_new(c)) return SPS_ERR_CAPACITY;
   pint_update(c);
+  if (outside && c->p.sph_shift && c->itimestep > 1 &&
+      (c->itimestep - 1) % c->p.shift_update == 0) {
+    stress_point_update(c);
+    if (ncrit == 12) adapt_all(c);
+  }
   memcpy(c->vx0, c->vel, 2 * (size_t)NT * sizeof(double));
   memcpy(c->x0, c->x, 2 * (size_t)NT * sizeof(double));
   rk4(c);
@@ -1357,6 +1449,7 @@ static int time_integration(orc_ctx* c) {
         }
     }
     free_surface(c); /* ndimn == 2 */
+    if (outside) shift_stress_points(c);
     if (!c->p.sp_sph)
       for (int i = 0; i < NN; i++)
         for (int d = 0; d < 2; d++) X(c, d, NN + i) = X(c, d, i);
@@ -1391,6 +1484,10 @@ int orc_create(const sps_params* p, orc_ctx** out) {
     return SPS_ERR_UNSUPPORTED;
   if (p->skf < 1 || p->skf > 3) return SPS_ERR_ARG;
   if (!p->sp_sph && p->nstress != p->nnode) return SPS_ERR_ARG;
+  if (p->sp_sph && !p->inside_approach &&
+      (p->npoints < 1 || p->npoints > 4 || p->shift_update < 1 ||
+       p->nstress != p->npoints * p->nnode || (p->vel_vector && p->npoints != 2)))
+    return SPS_ERR_ARG;
   orc_ctx* c = xcalloc(1, sizeof(orc_ctx));
   if (!c) return SPS_ERR_ARG;
   c->p = *p;
@@ -1446,6 +1543,8 @@ int orc_create(const sps_params* p, orc_ctx** out) {
   c->f_bound = xcalloc(2 * NN, sizeof(double));
   c->art_visc = xcalloc(2 * NN, sizeof(double));
   c->art_force = xcalloc(2 * NN, sizeof(double));
+  c->x10 = xcalloc(2 * NN, sizeof(double));
+  c->disp10 = xcalloc(NN, sizeof(double));
   c->which_cell = xcalloc(N2, sizeof(int32_t));
   c->cell_list = xcalloc(N2, sizeof(int32_t));
   for (size_t i = 0; i < NT; i++) c->bc_info[8 * i] = (int32_t)(i + 1);
@@ -1470,6 +1569,10 @@ int orc_upload(orc_ctx* c, const double* x, const double* vel, const double* str
   memcpy(c->x00, x00 ? x00 : x, 2 * N2 * sizeof(double));
   memset(c->out_domain, 0, N2 * sizeof(int32_t));
   memset(c->displ, 0, 2 * (size_t)c->NN * sizeof(double));
+  /* Setup_Global_Arrays (3_SPH_material_2018.f90:1032): x_10 starts at the node positions */
+  memcpy(c->x10, c->x, 2 * (size_t)c->NN * sizeof(double));
+  memset(c->disp10, 0, (size_t)c->NN * sizeof(double));
+  c->itimestep = 0;
   c->uploaded = 1;
   return SPS_OK;
 }
@@ -1546,7 +1649,7 @@ void orc_destroy(orc_ctx* c) {
                   c->x00, c->x0, c->vx0, c->displ, c->itype, c->out_domain, c->bc_or_not,
                   c->bc_info, c->bc_int, c->intvars1, c->f_drucker, c->grad_u, c->Ddev,
                   c->normal, c->subset,
-                  c->f_bound, c->art_visc, c->art_force, c->pi, c->pj, c->ptype, c->pw, c->pdx, c->pdy,
+                  c->f_bound, c->art_visc, c->art_force, c->x10, c->disp10, c->pi, c->pj, c->ptype, c->pw, c->pdx, c->pdy,
                   c->order, c->which_cell, c->cell_cnt, c->cell_start, c->cell_list};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(c);

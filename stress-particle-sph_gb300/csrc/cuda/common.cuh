@@ -91,6 +91,8 @@ struct Real {
   double vp_den;    // root3 (3 - sin phi): the Drucker-Prager yield denominator
   double vp_cons1;  // yieldf09's cons1 (Mohr-Coulomb sin phi / 3, Drucker-Prager)
   double vp_D[16];  // Get_Dmatx, row-major
+  // outside approach: stress-point shift distances and the velocity-vector tolerance
+  double r_x, r_y, disp_tol;
 };
 
 enum ErrBits : int {
@@ -132,6 +134,9 @@ struct Dev {
   double *RKv[2], *RKs[4], *RKr, *RKh, *RKd;
   double *RHS1[4], *RHS2[2], *RHSr, *RHSh;
   double *fbx, *fby;  // boundary force (nodes), once per step
+  // outside approach (stress-points attached to nodes, npoints each, shifted with them)
+  int outside, npoints, vel_vector;
+  double *x10x, *x10y, *disp10;  // velocity-vector variant: x_10(2,nnode), disp_10(nnode)
   int art_stress;      // artificial_force on (input.txt art_stress)
   double* artR;        // its per-node rotated tensile stresses R(3) of the stage, (3, NN)
   double *vol, *rinv;  // m / rho and 1 / rho per particle (refreshed when rho changes)

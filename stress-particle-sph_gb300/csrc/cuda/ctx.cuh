@@ -36,6 +36,9 @@ struct HostReal {
   bool surf_stale = false;
 };
 
+struct Ctx;
+void drop_graphs(Ctx& c);
+
 struct Ctx {
   sps_params p{};  // realisation 0 (the flags every realisation shares)
   std::vector<HostReal> hr;
@@ -62,8 +65,11 @@ struct Ctx {
   int64_t steps_done = 0;
   int precision = SPS_PREC_FP64_PLAIN;
   std::string last_error;
-  // graph of one step
-  cudaGraphExec_t graph = nullptr;
+  // graphs of one step, one per step variant (bit 0: the outside approach's
+  // re-interpolation at the start of the step, bit 1: its stress-point shift at the end)
+  cudaGraphExec_t graphs[4] = {nullptr, nullptr, nullptr, nullptr};
+  int step_variant = 0;    // the variant launch_*_step enqueues
+  int64_t itimestep = 0;   // itimestep_sph of the last step (0 after an upload)
   bool use_graph = true;
   // scratch for scans
   int scan_blocks = 0;

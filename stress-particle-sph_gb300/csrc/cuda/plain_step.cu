@@ -312,7 +312,7 @@ __global__ void k_node_rho(Dev D) {
 
 // adapt_stress2 + BCs after the interpolation (SP-SPH only), then sigma / rho^2 of the
 // stage for get_derivatives (the same quotient the reference forms per pair)
-__global__ void k_adapt_bc(Dev D, int with_A) {
+__global__ void k_adapt_bc(Dev D, int with_A, int bcs = 1) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
   const int r = D.R == 1 ? 0 : D.rid[i];
@@ -324,7 +324,7 @@ __global__ void k_adapt_bc(Dev D, int with_A) {
     // FP32 form: a stress-point's stress is unchanged since k_stage_begin / k_rk_final
     // returned it; only the interpolated node stress needs the return here
     if (M.ncrit == 12 && (!D.fast || i < D.NN)) stress_return(D, M, a, b, c, d);
-    apply_bcs(D, sc, i, vx, vy, a, b, c, d);
+    if (bcs) apply_bcs(D, sc, i, vx, vy, a, b, c, d);
     D.vx[i] = vx;
     D.vy[i] = vy;
     D.s0[i] = a;
@@ -397,6 +397,68 @@ __global__ void k_art_R(Dev D) {
   D.artR[i] = R20 * cc + R21 * ss;
   D.artR[D.NN + i] = R20 * (cc + ss);
   D.artR[2 * (size_t)D.NN + i] = (R20 - R21) * (co * si);
+}
+
+// shift_stress_points (2_SPH_main_2018.f90:244-368) for node i and its stress-points
+// (ids sp0 + npoints (i - node0) + q): with `reposition`, the points are placed again at the
+// fixed offsets (npoints 1-3; the second point of two takes r_x as its y offset, as in the
+// reference) or, with the velocity-vector variant, along the node velocity when the node
+// moved more than disp_tol dx since the last shift; then, every step, they are put on the
+// node when it is next to a wall and moves faster than 0.4, or has fewer than two node
+// neighbours (isolated_nodes: its node-node pairs, the node's same-type list).  cos_theta,
+// sin_theta, r_x2 and abs_vel are FP32 in the reference.
+__global__ void k_shift(Dev D, int reposition) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.NN) return;
+  const Real& M = real_of(D, i);
+  const int np = D.npoints;
+  const int k = M.sp0 + np * (i - M.node0);
+  const double xi = D.px[i], yi = D.py[i], v0 = D.vx[i], v1 = D.vy[i];
+  if (reposition) {
+    if (D.vel_vector) {
+      const double ex = xi - D.x10x[i], ey = yi - D.x10y[i];
+      const double d10 = sqrt(ex * ex + ey * ey) / M.dx;
+      D.disp10[i] = d10;
+      D.x10x[i] = xi;
+      D.x10y[i] = yi;
+      const double dx = M.dx;
+      const float ct = (float)(v0 / sqrt(v0 * v0 + v1 * v1));
+      const float st = (float)(v1 / sqrt(v0 * v0 + v1 * v1));
+      float r0 = (float)((dx / 2) * (double)ct), r1 = (float)((dx / 2) * (double)st);
+      if (r0 > 0 && r0 < dx / 5) r0 = (float)((double)r0 + dx / 3.0);
+      if (r1 > 0 && r1 < dx / 5) r1 = (float)((double)r1 + dx / 3.0);
+      if (r0 < 0 && r0 > -(dx / 5)) r0 = (float)((double)r0 - dx / 3.0);
+      if (r1 < 0 && r1 > -(dx / 5)) r1 = (float)((double)r1 - dx / 3.0);
+      if (d10 > M.disp_tol) {
+        D.px[k] = xi + (double)r0;
+        D.py[k] = yi + (double)r1;
+        D.px[k + 1] = xi - (double)r0;
+        D.py[k + 1] = yi - (double)r1;
+      }
+    } else if (np == 1) {
+      D.px[k] = xi + M.r_x;
+      D.py[k] = yi + M.r_y;
+    } else if (np == 2) {
+      D.px[k] = xi + M.r_x;
+      D.py[k] = yi + M.r_y;
+      D.px[k + 1] = xi - M.r_x;
+      D.py[k + 1] = yi - M.r_x;
+    } else if (np == 3) {
+      D.px[k] = xi;
+      D.py[k] = yi + M.r_y;
+      D.px[k + 1] = xi - M.r_x;
+      D.py[k + 1] = yi - M.r_y;
+      D.px[k + 2] = xi + M.r_x;
+      D.py[k + 2] = yi - M.r_y;
+    }
+  }
+  const float abs_vel = (float)sqrt(v0 * v0 + v1 * v1);
+  const int n_int = D.degS[D.spos[i]];
+  if ((D.bc_int[i] == 1 && abs_vel > 0.4f) || n_int < 2)
+    for (int q = 0; q < np && q < 3; q++) {
+      D.px[k + q] = xi;
+      D.py[k + q] = yi;
+    }
 }
 
 // get_derivatives (2_SPH_main_2018.f90:487-648) + the per-particle stage work of RK4
@@ -714,6 +776,19 @@ int launch_plain_step(Ctx& c) {
   c.mark("load_scalars");
   k_load_scalars<<<1, 128, 0, st>>>(D);
   launch_pair_build(c);
+  if (c.step_variant & 1) {
+    // the outside approach re-interpolates after a shift: stress_point_update and
+    // adapt_stress2 (2_SPH_main_2018.f90:99-108)
+    c.mark("interp");
+    if (D.fast) launch_finterp(c);
+    else k_interp<<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, st>>>(D);
+    if (D.cont_density) {
+      c.mark("node_rho");
+      k_node_rho<<<nbN, kBlock, 0, st>>>(D);
+    }
+    c.mark("adapt_bc");
+    k_adapt_bc<<<c.grid_of(TK_ADAPT, D.NT), c.blk[TK_ADAPT], 0, st>>>(D, 0, 0);
+  }
   c.mark("step_init");
   k_step_init<<<nbT, kBlock, 0, st>>>(D);
   if (D.inside) {
@@ -768,6 +843,10 @@ int launch_plain_step(Ctx& c) {
   // get_nodes_on_free_surface after the position update (2_SPH_main_2018.f90:153); on
   // demand instead when no later step reads it (Ctx::surf_every)
   if (D.update_x && c.surf_every) launch_surface(c);
+  if (D.update_x && D.outside) {
+    c.mark("shift");
+    k_shift<<<nbN, kBlock, 0, st>>>(D, (c.step_variant & 2) ? 1 : 0);
+  }
   c.mark("displ");
   k_displ<<<nbN, kBlock, 0, st>>>(D);
   c.mark("next_step");

@@ -26,6 +26,16 @@ struct sps_ctx {
   sps::Ctx c;
 };
 
+namespace sps {
+void drop_graphs(Ctx& c) {
+  for (auto& g : c.graphs)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+}  // namespace sps
+
 namespace {
 
 std::mutex g_err_mu;
@@ -293,11 +303,36 @@ int fail(sps::Ctx* c, int rc, const std::string& msg) {
   return rc;
 }
 
-void build_graph(sps::Ctx& c) {
-  if (c.graph) {
-    cudaGraphExecDestroy(c.graph);
-    c.graph = nullptr;
+void build_graph(sps::Ctx& c);
+
+// the step variant of itimestep_sph `it` (time_integration, 2_SPH_main_2018.f90:99-108 and
+// shift_stress_points :258): bit 0 re-interpolates at the start (SPH_shift, it > 1,
+// mod(it - 1, shift_update) == 0), bit 1 repositions the stress-points at the end
+// (mod(it, shift_update) == 0, with update_x)
+int variant_of(const sps::Ctx& c, int64_t it) {
+  const sps::Dev& D = c.d;
+  if (!D.outside) return 0;
+  int v = 0;
+  if (c.p.sph_shift && it > 1 && (it - 1) % c.p.shift_update == 0) v |= 1;
+  if (D.update_x && it % c.p.shift_update == 0) v |= 2;
+  return v;
+}
+
+// enqueue one step (itimestep_sph advanced first) as its variant's graph, or directly
+void enqueue_step(sps::Ctx& c) {
+  c.itimestep += 1;
+  c.step_variant = variant_of(c, c.itimestep);
+  if (c.use_graph && !c.profiling) {
+    if (!c.graphs[c.step_variant]) build_graph(c);
+    SPS_CUDA_CHECK(cudaGraphLaunch(c.graphs[c.step_variant], c.stream));
+  } else if (c.precision == SPS_PREC_FP64_PLAIN) {
+    sps::launch_plain_step(c);
+  } else {
+    sps::launch_fast_step(c);
   }
+}
+
+void build_graph(sps::Ctx& c) {
   cudaGraph_t g;
   SPS_CUDA_CHECK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
   int64_t k0 = c.kernels_launched;
@@ -305,7 +340,7 @@ void build_graph(sps::Ctx& c) {
   else sps::launch_fast_step(c);
   c.kernels_per_step = (int)(c.kernels_launched - k0);
   SPS_CUDA_CHECK(cudaStreamEndCapture(c.stream, &g));
-  SPS_CUDA_CHECK(cudaGraphInstantiate(&c.graph, g, 0));
+  SPS_CUDA_CHECK(cudaGraphInstantiate(&c.graphs[c.step_variant], g, 0));
   cudaGraphDestroy(g);
 }
 
@@ -318,10 +353,7 @@ void ensure_scal(sps::Ctx& c, int n) {
   c.d_scal_table = static_cast<sps::StepScalars*>(p);
   c.scal_cap = cap;
   c.d.scal_table = c.d_scal_table;
-  if (c.graph) {
-    cudaGraphExecDestroy(c.graph);
-    c.graph = nullptr;
-  }
+  drop_graphs(c);
 }
 
 std::string err_text(int e) {
@@ -404,10 +436,14 @@ int check_params(const sps_params* p) {
   if (p->no_bcs > 0 && !p->bc_list) return fail(nullptr, SPS_ERR_ARG, "bc_list missing");
   if (!p->sp_sph && p->nstress != p->nnode)
     return fail(nullptr, SPS_ERR_ARG, "standard SPH needs nstress == nnode");
+  if (p->sp_sph && !p->inside_approach &&
+      (p->npoints < 1 || p->npoints > 4 || p->shift_update < 1 ||
+       p->nstress != p->npoints * p->nnode || (p->vel_vector && p->npoints != 2)))
+    return fail(nullptr, SPS_ERR_ARG,
+                "outside approach: npoints 1-4 per node (2 with vel_vector), nstress = "
+                "npoints * nnode, shift_update >= 1");
   if (!p->sp_sph && p->inside_approach)
     return fail(nullptr, SPS_ERR_ARG, "standard SPH has no inside approach");
-  if (p->sp_sph && !p->inside_approach)
-    return fail(nullptr, SPS_ERR_UNSUPPORTED, "outside approach (stress-point shifting) not implemented");
   if (p->precision != SPS_PREC_FP64_PLAIN && p->precision != SPS_PREC_FP32_FAST)
     return fail(nullptr, SPS_ERR_ARG, "unknown precision");
   for (int b = 0; b < p->no_bcs; b++)
@@ -423,7 +459,10 @@ bool same_flags(const sps_params& a, const sps_params& b) {
   return a.sp_sph == b.sp_sph && a.inside_approach == b.inside_approach && a.cspm == b.cspm &&
          a.xsph == b.xsph && a.update_x == b.update_x && a.cont_density == b.cont_density &&
          a.sle == b.sle && a.skf == b.skf && a.precision == b.precision && a.pi == b.pi &&
-         a.ntype_solid == b.ntype_solid && a.art_stress == b.art_stress;
+         a.ntype_solid == b.ntype_solid && a.art_stress == b.art_stress &&
+         (a.inside_approach || !a.sp_sph ||
+          (a.npoints == b.npoints && a.sph_shift == b.sph_shift &&
+           a.vel_vector == b.vel_vector && a.shift_update == b.shift_update));
 }
 
 }  // namespace
@@ -523,6 +562,9 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
         M.cgrav[d] = q.cgrav[d];
       }
       viscoplastic_constants(q, M);
+      M.r_x = q.r_x;
+      M.r_y = q.r_y;
+      M.disp_tol = q.disp_tol;
     }
     D.capC = D.capS = D.capH = 0;  // sized at upload from the kernel support
     D.skf = p->skf;
@@ -536,7 +578,10 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.inside = p->inside_approach;
     D.no_bcs = p->no_bcs;
     D.ifsigman = p->ifsigman;
-    c.surf_every = p->update_x && (p->ifsigman == 1 || (p->xsph && p->no_bcs > 0) || !p->sp_sph);
+    // (the outside approach shifts the stress-points right after the detection, so the
+    // detection cannot wait for the download)
+    c.surf_every = p->update_x && (p->ifsigman == 1 || (p->xsph && p->no_bcs > 0) ||
+                                   !p->sp_sph || !p->inside_approach);
     D.pi = p->pi;
     for (int b = 0; b < p->no_bcs; b++) D.bcvar[b] = (int)p->bc_list[8 * (size_t)b + 1];
     const size_t N2 = D.N2, NT = D.NT, NN_ = D.NN;
@@ -610,6 +655,15 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.RHSh = dalloc<double>(c, NT);
     D.fbx = dalloc<double>(c, NN_);
     D.art_stress = p->art_stress ? 1 : 0;
+    D.outside = p->sp_sph && !p->inside_approach;
+    D.npoints = D.outside ? p->npoints : 1;
+    D.vel_vector = D.outside && p->vel_vector;
+    if (D.vel_vector) {
+      D.x10x = dalloc<double>(c, NN_);
+      D.x10y = dalloc<double>(c, NN_);
+      D.disp10 = dalloc<double>(c, NN_);
+      SPS_CUDA_CHECK(cudaMemsetAsync(D.disp10, 0, sizeof(double) * NN_, c.stream));
+    }
     D.artR = D.art_stress ? dalloc<double>(c, 3 * (size_t)NN_) : nullptr;
     D.fby = dalloc<double>(c, NN_);
     D.Ddev = dalloc<double>(c, NT);
@@ -754,6 +808,13 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
     };
     up2(x, st_x, D.px, D.py);
     up2(vel, st_v, D.vx, D.vy);
+    if (D.vel_vector && nn > 0) {  // Setup_Global_Arrays (3_SPH_material_2018.f90:1032)
+      SPS_CUDA_CHECK(cudaMemcpyAsync(D.x10x + M.node0, D.px + M.node0, sizeof(double) * nn,
+                                     cudaMemcpyDeviceToDevice, c.stream));
+      SPS_CUDA_CHECK(cudaMemcpyAsync(D.x10y + M.node0, D.py + M.node0, sizeof(double) * nn,
+                                     cudaMemcpyDeviceToDevice, c.stream));
+      SPS_CUDA_CHECK(cudaMemsetAsync(D.disp10 + M.node0, 0, sizeof(double) * nn, c.stream));
+    }
     up2(x00 ? x00 : x, st_0, D.x00x, D.x00y);
     SPS_CUDA_CHECK(cudaMemcpyAsync(st_s, stress, sizeof(double) * 4 * n2, cudaMemcpyHostToDevice, c.stream));
     for (const Seg& q : sg)
@@ -828,10 +889,7 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
       D.cell_cap = cap;
       size_t nscan = std::max<size_t>((size_t)D.N2, (size_t)cap + 2);
       D.scan_tmp = dalloc<int64_t>(c, nscan / 4096 + 64);
-      if (c.graph) {
-        cudaGraphExecDestroy(c.graph);
-        c.graph = nullptr;
-      }
+      drop_graphs(c);
     }
     // neighbour capacities: one species holds about pi (scale_k h / dx)^2 partners in the
     // support; 2x headroom plus the wall rows.  max_neighbours (total per particle) raises
@@ -841,7 +899,9 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
       for (int q = 0; q < D.R; q++) {
         if (!c.hr[q].uploaded) continue;
         double rs = (double)D.scale_k * c.hr[q].hmax / c.hr[q].p.dx;
-        est = std::max(est, (int)std::ceil(2.0 * M_PI * rs * rs) + 8);
+        // npoints stress-points per node spacing (both approaches)
+        const double np = (double)std::max(1, c.hr[q].p.npoints);
+        est = std::max(est, (int)std::ceil(2.0 * M_PI * rs * rs * np) + 8);
       }
       int capn = c.p.max_neighbours > 0 ? std::max(4, c.p.max_neighbours / 2) : std::max(48, est);
       if (capn > D.capH || (c.p.max_neighbours > 0 && capn != D.capH)) {
@@ -851,10 +911,7 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
         D.keyC = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.keyS = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.capH = D.capC = D.capS = capn;
-        if (c.graph) {
-          cudaGraphExecDestroy(c.graph);
-          c.graph = nullptr;
-        }
+        drop_graphs(c);
       }
     }
     // node-wall boundary force can use the pair lists when every node-dummy pair closer
@@ -862,10 +919,7 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
     int bfl = 1;
     for (const sps::HostReal& q : c.hr)
       if (q.uploaded && !((double)D.scale_k * q.hmin_nd > 0.76 * q.p.dx)) bfl = 0;
-    if (bfl != D.bound_from_lists && c.graph) {
-      cudaGraphExecDestroy(c.graph);
-      c.graph = nullptr;
-    }
+    if (bfl != D.bound_from_lists) drop_graphs(c);
     D.bound_from_lists = bfl;
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
@@ -874,6 +928,7 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
   for (const sps::HostReal& q : c.hr) all = all && q.uploaded;
   c.uploaded = all;
   c.surf_stale = false;  // an uploaded state carries its own bc_or_not
+  c.itimestep = 0;       // the next step is the first of the run
   return SPS_OK;
 }
 
@@ -919,15 +974,7 @@ int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
                                      sizeof(sps::StepScalars) * c.h_scal.size(),
                                      cudaMemcpyHostToDevice, c.stream));
       SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
-      if (c.use_graph) {
-        if (!c.graph) build_graph(c);
-        for (int k = 0; k < chunk; k++) SPS_CUDA_CHECK(cudaGraphLaunch(c.graph, c.stream));
-      } else {
-        for (int k = 0; k < chunk; k++) {
-          if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
-          else sps::launch_fast_step(c);
-        }
-      }
+      for (int k = 0; k < chunk; k++) enqueue_step(c);
       done += chunk;
     }
     int nb = (c.d.NT + kBlock - 1) / kBlock;
@@ -1269,7 +1316,7 @@ int sps_dump_pairs_real(sps_ctx* h, int32_t r, int32_t* pair_i, int32_t* pair_j,
 int sps_kernels_per_step(sps_ctx* h, int32_t* n) {
   if (!h || !n) return SPS_ERR_ARG;
   try {
-    if (!h->c.graph) build_graph(h->c);
+    if (!h->c.graphs[h->c.step_variant]) build_graph(h->c);
   } catch (const std::exception& e) {
     return fail(&h->c, SPS_ERR_CUDA, e.what());
   }
@@ -1379,8 +1426,7 @@ void profile_run(sps::Ctx& c, int nsteps, double* t, std::vector<std::string>& k
   SPS_CUDA_CHECK(cudaMemsetAsync(c.d.step_idx, 0, sizeof(int), c.stream));
   c.profiling = true;
   for (int k = 0; k < nsteps; k++) {
-    if (c.precision == SPS_PREC_FP64_PLAIN) sps::launch_plain_step(c);
-    else sps::launch_fast_step(c);
+    enqueue_step(c);
     c.mark("end");
   }
   c.profiling = false;
@@ -1416,7 +1462,13 @@ std::vector<std::pair<void*, size_t>> carried_state(sps::Ctx& c) {
       {D.iv1, d8 * NT},  {D.fdp, d8 * NT},   {D.grad_u, 4 * d8 * NT},
       {D.dispx, d8 * NN}, {D.dispy, d8 * NN}, {D.bc_or_not, sizeof(int32_t) * NT},
       {D.out, N2},       {D.meta, sizeof(sps::PairMeta) * D.R},
-      {D.nrmx, d8 * NT}, {D.nrmy, d8 * NT}, {D.subset, NT}, {D.fint, sizeof(float) * NT}};
+      {D.nrmx, d8 * NT}, {D.nrmy, d8 * NT}, {D.subset, NT}, {D.fint, sizeof(float) * NT},
+      {D.bc_int, sizeof(int32_t) * NN}};
+  if (D.vel_vector) {
+    v.push_back({D.x10x, d8 * NN});
+    v.push_back({D.x10y, d8 * NN});
+    v.push_back({D.disp10, d8 * NN});
+  }
   if (D.fast) {
     v.push_back({D.recV, sizeof(float4) * N2});
     v.push_back({D.recS, sizeof(float4) * NT});
@@ -1454,6 +1506,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     };
     copy(true);
     const bool stale = c.surf_stale;
+    const int64_t it0 = c.itimestep;
     const int cand[] = {64, 128, 256, 512};
     int best[sps::TK_N];
     double best_ms[sps::TK_N];
@@ -1468,6 +1521,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       std::vector<double> kms;
       std::vector<int> kl;
       std::fill(t.begin(), t.end(), 0.0);
+      c.itimestep = it0;
       profile_run(c, nsteps, t.data(), kn, kms, kl);
       copy(false);
       for (int k = 0; k < sps::TK_N; k++)
@@ -1482,14 +1536,12 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       if (blocks) blocks[k] = best[k];
     }
     c.surf_stale = stale;
+    c.itimestep = it0;
     SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     cudaFree(snap);
     snap = nullptr;
-    if (c.graph) {
-      cudaGraphExecDestroy(c.graph);
-      c.graph = nullptr;
-    }
+    drop_graphs(c);
   } catch (const std::exception& e) {
     c.profiling = false;
     if (snap) cudaFree(snap);
@@ -1512,7 +1564,7 @@ int sps_last_error(sps_ctx* h, char* buf, int32_t len) {
 void sps_destroy(sps_ctx* h) {
   if (!h) return;
   sps::Ctx& c = h->c;
-  if (c.graph) cudaGraphExecDestroy(c.graph);
+  sps::drop_graphs(c);
   if (c.stream) cudaStreamSynchronize(c.stream);
   for (void* p : {(void*)c.cap_buf, (void*)c.cap_cnt, (void*)c.mlp_frag, (void*)c.mlp_bias,
                   (void*)c.surr_cnt})
@@ -1557,10 +1609,7 @@ int sps_capture(sps_ctx* h, int64_t cap) {
       c.d.cap_cnt = c.cap_cnt;
       c.d.cap_max = cap;
     }
-    if (c.graph) {  // kernel arguments changed
-      cudaGraphExecDestroy(c.graph);
-      c.graph = nullptr;
-    }
+    drop_graphs(c);
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
@@ -1626,10 +1675,7 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
     } else {
       c.d.surr = 0;
     }
-    if (c.graph) {
-      cudaGraphExecDestroy(c.graph);
-      c.graph = nullptr;
-    }
+    drop_graphs(c);
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());

@@ -430,9 +430,9 @@ void parse_all(sph_problem& P, const std::string& in_txt, const std::string& dat
   auto f3 = in.read(3);
   bool sp_sph = in.to_l(f3[0]);
   bool art_stress = in.to_l(f3[1]);
-  bool inside = false, vel_vector = false;
-  int npoints = 1;
-  double rx = 0, ry = 0;
+  bool inside = false, vel_vector = false, sph_shift = false;
+  int npoints = 1, shift_update = 1;
+  double rx = 0, ry = 0, disp_tol = 0;
   if (sp_sph) {
     in.text();
     inside = in.logical();
@@ -441,14 +441,22 @@ void parse_all(sph_problem& P, const std::string& in_txt, const std::string& dat
     if (!inside) {
       in.text();
       auto v = in.read(6);
+      sph_shift = in.to_l(v[0]);
       vel_vector = in.to_l(v[1]);
+      shift_update = in.to_i(v[2]);
       rx = in.to_d(v[3]);
       ry = in.to_d(v[4]);
+      disp_tol = in.to_d(v[5]);
     }
   }
   if (vel_vector) npoints = 2;
   if (!sp_sph) npoints = 1;
   P.npoints = npoints;
+  P.p.npoints = npoints;
+  P.p.sph_shift = sph_shift;
+  P.p.vel_vector = vel_vector;
+  P.p.shift_update = shift_update;
+  P.p.disp_tol = disp_tol;
   pts.text();
   pts.integer();  // geom_type: always a rectangle in the reference
   pts.text();
@@ -475,6 +483,8 @@ void parse_all(sph_problem& P, const std::string& in_txt, const std::string& dat
   P.p.sp_sph = sp_sph;
   P.p.inside_approach = inside;
   P.p.art_stress = art_stress;
+  P.p.r_x = dx * rx;  // Read_2DMesh (:628)
+  P.p.r_y = dx * ry;
   if (!sp_sph) {
     // Standard SPH: stress-points coincide with nodes (outside approach with zero shift)
     build_rectangle(P, x1, x4, y1, y4, dx, dy, false, 1, 0.0, 0.0, walls);
@@ -953,6 +963,8 @@ int sph_problem_slope(const sph_slope_spec* s, sph_problem** out) {
 }
 
 const sps_params* sph_problem_params(const sph_problem* p) { return p ? &p->p : nullptr; }
+
+int32_t sph_sizeof_params(void) { return (int32_t)sizeof(sps_params); }
 
 int sph_problem_output_flags(const sph_problem* p, int32_t* flags) {
   if (!p || !flags) return SPS_ERR_ARG;

@@ -80,6 +80,13 @@ class SpsParams(C.Structure):
         ("horizontal_or_not", C.POINTER(c_float)),
         ("precision", c_int32),
         ("max_neighbours", c_int32),
+        ("npoints", c_int32),
+        ("sph_shift", c_int32),
+        ("vel_vector", c_int32),
+        ("shift_update", c_int32),
+        ("r_x", c_double),
+        ("r_y", c_double),
+        ("disp_tol", c_double),
     ]
 
 

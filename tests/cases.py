@@ -18,7 +18,7 @@ def bui_like(width=4.0, height=2.0, dx=0.1, young=1.8e6, poiss=0.3, rho=1850.0,
              tanphi=0.466308, coh=5000.0, xsph=True, cspm=False, alpha=0.1, beta=0.1,
              damping=0.0, dt=1.5e-4, sml=1.2, skf=1, cont_density=False, sle=1,
              ntype_solid=2, npoints=1, floor_to=9.0, ntype_eco=2, ncrit=12,
-             output_flags="1 1 1 1 1 1 1 0 0 0", art_stress=False):
+             output_flags="1 1 1 1 1 1 1 0 0 0", art_stress=False, outside=None):
     """Cohesive soil block on a floor with a left wall: the layout of the Drucker-Prager
     example (inside approach, three dummy rows) with every parameter adjustable."""
     pts = "\n".join([
@@ -50,9 +50,17 @@ def bui_like(width=4.0, height=2.0, dx=0.1, young=1.8e6, poiss=0.3, rho=1850.0,
         "%s %s" % (_fmt(alpha), _fmt(beta)), "ic_grav", "1", "gx gy timecurve factor",
         "0 -9.81 1 1.", "output values", "sxx syy sxy szz ux uy strain rho sml disp_10",
         output_flags, ""])
+    # outside approach: dict(sph_shift, vel_vector, shift_update, rx, ry, disp_tol), the
+    # line of the outside-approach example's input.txt
+    shift = [] if outside is None else [
+        "SPH_shifting vel_vector shift_update rx_factor ry_factor disp_tol",
+        "%s %s %d %s %s %s" % (L(outside["sph_shift"]), L(outside["vel_vector"]),
+                               outside["shift_update"], _fmt(outside["rx"]), _fmt(outside["ry"]),
+                               _fmt(outside["disp_tol"]))]
     inp = "\n".join([
         "problem name", "gen", "SP_SPH art_stress particle_shift", "T %s F" % L(art_stress),
-        "inside_approach", "T", "number of stress points", str(npoints), "smoothing length factor",
+        "inside_approach", "T" if outside is None else "F", "number of stress points",
+        str(npoints)] + shift + ["smoothing length factor",
         _fmt(sml), "time step, time for end, max number of time steps",
         "%s,2.5,10" % _fmt(dt), "print, save, plot", "1,1,1", "if end of simulation:", "-1,1,1",
         ""])

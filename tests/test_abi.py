@@ -39,3 +39,15 @@ def test_library_exports_header(built, header, lib):
     dll = C.CDLL(_build.lib_path(lib))
     missing = [n for n in declared(header) if not hasattr(dll, n)]
     assert not missing, missing
+
+
+def test_params_layout_matches_binding(built):
+    # the ctypes mirror of sps_params must have the C struct's size (a missing or reordered
+    # field would shift every later one)
+    import sps_gb300
+    from sps_gb300 import _abi
+    from sps_gb300 import build as _build
+    sps_gb300.build_host()
+    dll = C.CDLL(_build.lib_path("libsph_host.so"))
+    dll.sph_sizeof_params.restype = C.c_int32
+    assert dll.sph_sizeof_params() == C.sizeof(_abi.SpsParams)

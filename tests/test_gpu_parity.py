@@ -179,6 +179,35 @@ def test_artificial_stress_close(built_gpu, precision):
     assert not np.array_equal(o2.download()["vel"], fo["vel"])
 
 
+OUTSIDE = dict(sph_shift=True, vel_vector=False, shift_update=1, rx=1 / 3, ry=1 / 3,
+               disp_tol=0.125)
+
+
+@pytest.mark.parametrize("npoints,extra", [
+    (1, {}), (2, {}), (3, {}), (2, dict(vel_vector=True, disp_tol=0.0)),
+    (2, dict(vel_vector=True, disp_tol=0.5, shift_update=2)),
+    (1, dict(sph_shift=False, shift_update=3))],
+    ids=["np1", "np2", "np3", "vel_vector", "vel_vector_tol", "no_reinterp"])
+def test_outside_approach(built_gpu, npoints, extra):
+    # stress-points attached to their nodes and placed again every shift_update steps,
+    # with the re-interpolation at the start of the following step (plain: bit-exact)
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05, outside=dict(OUTSIDE, **extra),
+                       npoints=npoints)
+    _compare(p, 12, chunks=[5, 7])
+
+
+def test_outside_approach_fp32(built_gpu):
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05, outside=OUTSIDE, npoints=2)
+    g = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                              p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+    o = _orc_ctx(p)
+    cases.run_pair(p, 12, [g, o])
+    fg, fo = g.download(), o.download()
+    for k in ("x", "vel"):
+        scale = np.abs(fo[k]).max() + 1e-300
+        assert np.abs(fg[k] - fo[k]).max() <= 1e-4 * scale, k
+
+
 def test_standard_sph(built_gpu):
     p = cases.standard_sph()
     _compare(p, 6)
@@ -217,7 +246,7 @@ def test_unsupported_options(built_gpu):
     weak = _visco(2, yield_stress=1e-4)  # invar09 stops below 0.001
     with pytest.raises(sps_gb300.SpsError):
         _gpu_ctx(weak)
-    for over in (dict(inside_approach=0), dict(skf=7)):
+    for over in (dict(inside_approach=0), dict(skf=7)):  # inside_approach 0: no npoints
         with pytest.raises(sps_gb300.SpsError):
             _gpu_ctx(p, **over)
 
