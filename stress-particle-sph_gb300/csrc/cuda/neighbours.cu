@@ -458,7 +458,9 @@ __global__ void k_half(Dev D) {
   int4* out = D.half + (size_t)s * D.capH;
   // stencil cells in creation order: (dix, diy) and the first sorted position to scan
   int cells[5][2] = {{0, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+  int gstart[5] = {0, 0, 0, 0, 0};  // where each stencil cell's pairs start in the list
   for (int q = 0; q < 5; q++) {
+    gstart[q] = min(k, D.capH);
     int jx = ix + cells[q][0], jy = iy + cells[q][1];
     if (jx < 0 || jx >= nx || jy >= ny) continue;
     int cc = g.cell0 + jy * nx + jx;
@@ -506,6 +508,8 @@ __global__ void k_half(Dev D) {
     k = D.capH;
   }
   D.half_cnt[s] = k;
+  D.half_grp[s] = make_ushort4((unsigned short)gstart[1], (unsigned short)gstart[2],
+                               (unsigned short)gstart[3], (unsigned short)gstart[4]);
 }
 
 // pair counts of every realisation (its pairs are the half lists of its sorted range)
@@ -555,9 +559,7 @@ __device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, in
 // order; the lists are written in that walk order.
 // KEYS: also write the walk-order key of every entry (for the free-surface detection)
 template <bool KEYS>
-__global__ void k_lists(Dev D) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
+__device__ __forceinline__ void lists_target(const Dev& D, int s) {
   int nC = 0, nS = 0, newC = 0, newS = 0;
   if (s < D.gtot->nactive) {
     int t = D.sorted[s];
@@ -611,23 +613,68 @@ __global__ void k_lists(Dev D) {
           newC += isnew;
         }
       };
-      for (int rgn = 0; rgn < 2; rgn++)
-        for (int as = lo[rgn]; as < hi[rgn]; as++) {
-          int n = D.half_cnt[as];
-          const int4* h = D.half + (size_t)as * D.capH;
-          // binary search for s among the (ascending) partner positions of as
-          int l = 0, r = n;
-          while (l < r) {
-            int m = (l + r) >> 1;
-            if (h[m].x < s) l = m + 1;
-            else r = m;
-          }
-          if (l < n && h[l].x == s) {
-            int4 e = h[l];
-            push(D.sorted[as], e.y, -__int_as_float(e.z), -__int_as_float(e.w),
-                 D.half_off[as] + l, false);
-          }
+      // the creators before s, in ascending sorted position: each holds s at most once in
+      // its (ascending) half list, among the pairs it made with s's cell, whose place in
+      // the list k_half recorded (half_grp: the starts of its five stencil cells).  The
+      // stencil cell of s seen from a creator follows from the creator's cell: below-left,
+      // below, below-right (region 0), left, own (region 1).  kG lower-bound searches run
+      // interleaved, so that their dependent loads overlap; the hits are pushed in creator
+      // order.
+      constexpr int kG = 4;
+      const int n0 = hi[0] - lo[0], ncand = n0 + (hi[1] - lo[1]);
+      const int rowb = c0g + (iy - 1) * nx;  // first cell of the row below
+      const int b1 = iy > 0 ? D.cell_start[rowb + ix] : 0;  // the cell below s's cell
+      const int b2 = (iy > 0 && ix + 1 < nx) ? D.cell_start[rowb + ix + 1] : hi[0];
+      const int own0 = D.cell_start[c0g + c];
+      for (int i0 = 0; i0 < ncand; i0 += kG) {
+        int as[kG], pos[kG], len[kG], cnt[kG];
+        ushort4 gr[kG];
+#pragma unroll
+        for (int q = 0; q < kG; q++) {
+          const int i = i0 + q;
+          as[q] = i < n0 ? lo[0] + i : lo[1] + (i - n0);
+          cnt[q] = i < ncand ? D.half_cnt[as[q]] : 0;
+          gr[q] = i < ncand ? D.half_grp[as[q]] : make_ushort4(0, 0, 0, 0);
         }
+#pragma unroll
+        for (int q = 0; q < kG; q++) {
+          const int i = i0 + q;
+          // stencil cell of s from the creator: 0 own, 1 right, 2 up-left, 3 up, 4 up-right
+          const int st = i < n0 ? (as[q] < b1 ? 4 : as[q] < b2 ? 3 : 2) : (as[q] < own0 ? 1 : 0);
+          const int g0 = st == 0 ? 0 : st == 1 ? gr[q].x : st == 2 ? gr[q].y : st == 3 ? gr[q].z : gr[q].w;
+          const int g1 = st == 0 ? gr[q].x : st == 1 ? gr[q].y : st == 2 ? gr[q].z : st == 3 ? gr[q].w : cnt[q];
+          pos[q] = g0;
+          len[q] = i < ncand ? max(g1 - g0, 0) : 0;
+        }
+        bool more = true;
+        while (more) {
+          int v[kG];
+#pragma unroll
+          for (int q = 0; q < kG; q++)
+            v[q] = len[q] > 0 ? D.half[(size_t)as[q] * D.capH + pos[q] + (len[q] >> 1)].x : 0;
+          more = false;
+#pragma unroll
+          for (int q = 0; q < kG; q++)
+            if (len[q] > 0) {
+              const int half = len[q] >> 1;
+              if (v[q] < s) {
+                pos[q] += half + 1;
+                len[q] -= half + 1;
+              } else {
+                len[q] = half;
+              }
+              more |= len[q] > 0;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kG; q++)
+          if (pos[q] < cnt[q]) {
+            const int4 e = D.half[(size_t)as[q] * D.capH + pos[q]];
+            if (e.x == s)
+              push(D.sorted[as[q]], e.y, -__int_as_float(e.z), -__int_as_float(e.w),
+                   D.half_off[as[q]] + pos[q], false);
+          }
+      }
       {
         int n = D.half_cnt[s];
         const int4* h = D.half + (size_t)s * D.capH;
@@ -656,6 +703,12 @@ __global__ void k_lists(Dev D) {
   }
   D.degC[s] = nC;
   D.degS[s] = nS;
+}
+
+template <bool KEYS>
+__global__ void k_lists(Dev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < D.N2) lists_target<KEYS>(D, s);
 }
 
 // ------------------------------------------------------------------------ scans
@@ -752,6 +805,13 @@ __global__ void k_target_scatter(Dev D) {
   if (D.tflag[D.N2 + s]) D.tgtN[D.toff[D.N2 + 1 + s]] = s;
 }
 
+// per-target lists (k_lists), one thread per sorted position
+void launch_lists(Ctx& c, bool keys) {
+  const Dev& D = c.d;
+  if (keys) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, c.stream>>>(D);
+  else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, c.stream>>>(D);
+}
+
 int launch_pair_build(Ctx& c) {
   Dev& D = c.d;
   cudaStream_t st = c.stream;
@@ -781,8 +841,7 @@ int launch_pair_build(Ctx& c) {
   c.mark("pair_meta");
   k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("lists");
-  if (c.surf_every) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
-  else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, st>>>(D);
+  launch_lists(c, c.surf_every);
   if (D.fast && D.sp_sph) {
     c.mark("split_targets", 8);
     k_target_flags<<<nb, kBlock, 0, st>>>(D);
@@ -795,8 +854,6 @@ int launch_pair_build(Ctx& c) {
 
 // the lists of the last step again, now with their walk-order keys (the on-demand
 // free-surface detection; the lists are rebuilt identically)
-void launch_lists_keys(Ctx& c) {
-  k_lists<true><<<c.grid_of(TK_LISTS, c.d.N2), c.blk[TK_LISTS], 0, c.stream>>>(c.d);
-}
+void launch_lists_keys(Ctx& c) { launch_lists(c, true); }
 
 }  // namespace sps

@@ -694,6 +694,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.gtot = dalloc<sps::GridTotal>(c, 1);
     D.bbox = dalloc<unsigned long long>(c, 6 * (size_t)nreal);
     D.half_cnt = dalloc<int32_t>(c, N2);
+    D.half_grp = dalloc<ushort4>(c, N2);
     D.half_off = dalloc<int64_t>(c, N2 + 1);
     D.degC = dalloc<int32_t>(c, N2);
     D.degS = dalloc<int32_t>(c, N2);
@@ -904,6 +905,7 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
         est = std::max(est, (int)std::ceil(2.0 * M_PI * rs * rs * np) + 8);
       }
       int capn = c.p.max_neighbours > 0 ? std::max(4, c.p.max_neighbours / 2) : std::max(48, est);
+      capn = std::min(capn, 65535);  // half-list positions are kept in 16 bits
       if (capn > D.capH || (c.p.max_neighbours > 0 && capn != D.capH)) {
         D.half = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
         D.cross = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
