@@ -467,16 +467,35 @@ __global__ void k_half(Dev D) {
     int lo = (q == 0) ? s + 1 : D.cell_start[cc];
     int hi = D.cell_start[cc] + D.cell_cnt[cc];
     float cx = (float)cells[q][0] * cw, cy = (float)cells[q][1] * ch;
+    // phase 1: the accepted partners in creation order (sorted position, stencil cell);
+    // the kernel values follow in phase 2, so that the lanes of a warp evaluate them
+    // together instead of each time one lane accepts a candidate
     for (int bs = lo; bs < hi; bs++) {
       int b = D.sorted[bs];
       float fx, fy;
       int pf = prefilter(D, xa, ya, ha, b, cx, cy, tau, fx, fy);
       if (pf == 0) continue;
-      double r, dx, dy, mh;
-      if (pf == 2 || !FAST) {
-        bool acc = exact_test(D, a, b, r, dx, dy, mh);
-        if (!acc) continue;
+      if (pf == 2) {
+        double r, dx, dy, mh;
+        if (!exact_test(D, a, b, r, dx, dy, mh)) continue;
       }
+      if (k < D.capH) out[k] = make_int4(bs, q, 0, 0);
+      k++;
+    }
+  }
+  // phase 2: kernel values of the accepted pairs
+  const int kk = min(k, D.capH);
+  for (int m = 0; m < kk; m++) {
+    const int4 e0 = out[m];
+    const int bs = e0.x, q = e0.y;
+    const int b = D.sorted[bs];
+    // the stencil cell's offset (cells[q]) without indexing a local array
+    const int qx = (q == 1 || q == 4) ? 1 : (q == 2 ? -1 : 0), qy = q >= 2 ? 1 : 0;
+    {
+      const float cx = (float)qx * cw, cy = (float)qy * ch;
+      const float fx = (xa - D.xr[b]) - cx, fy = (ya - D.yr[b]) - cy;
+      double r, dx, dy, mh;
+      if (!FAST) exact_test(D, a, b, r, dx, dy, mh);
       float wf, d0f, d1f;
       if (!FAST) {
         double w, dw0, dw1;
@@ -489,18 +508,16 @@ __global__ void k_half(Dev D) {
         // separation as double-float from the cell-relative hi/lo offsets
         // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float
         dfl ddx = df_add(df_add({xa, xal}, {-D.xr[b], -D.xrl[b]}),
-                         {-(float)cells[q][0] * g.df_cell[0].hi, -(float)cells[q][0] * g.df_cell[0].lo});
+                         {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
         dfl ddy = df_add(df_add({ya, yal}, {-D.yr[b], -D.yrl[b]}),
-                         {-(float)cells[q][1] * g.df_cell[1].hi, -(float)cells[q][1] * g.df_cell[1].lo});
+                         {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
         cubic_df(g, ddx, ddy, &wf, &d0f, &d1f);
       } else {
         float hm = (ha + D.hr[b]) * 0.5f;
         float rf = sqrtf(fx * fx + fy * fy);
         sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
       }
-      if (k < D.capH)
-        out[k] = make_int4(bs, __float_as_int(wf), __float_as_int(d0f), __float_as_int(d1f));
-      k++;
+      out[m] = make_int4(bs, __float_as_int(wf), __float_as_int(d0f), __float_as_int(d1f));
     }
   }
   if (k > D.capH) {
