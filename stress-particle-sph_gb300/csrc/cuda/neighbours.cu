@@ -859,7 +859,7 @@ int launch_pair_build(Ctx& c) {
   k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("lists");
   launch_lists(c, c.surf_every);
-  if (D.fast && D.sp_sph) {
+  if (D.sp_sph) {
     c.mark("split_targets", 8);
     k_target_flags<<<nb, kBlock, 0, st>>>(D);
     scan_i32_to_i32(c, D.tflag, D.toff, D.N2);

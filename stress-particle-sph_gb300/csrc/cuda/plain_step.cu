@@ -229,9 +229,19 @@ __global__ void k_stage_begin(Dev D, int stage) {
 }
 
 // stress_point_update (2_SPH_main_2018.f90:403-482) as a gather per target
-__global__ void k_interp(Dev D) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
+// KIND 0: every sorted position; 1: the stress-point targets tgt[0..ntgt); 2: the node
+// targets (a warp then runs one branch only: the FP64 pipe is not shared by both)
+template <int KIND>
+__global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
+  const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int s;
+  if (KIND == 0) {
+    s = k0;
+    if (s >= D.N2) return;
+  } else {
+    if (k0 >= ntgt) return;
+    s = tgt[k0];
+  }
   int t = D.sorted[s];
   int tt = D.itype[t];
   if (t >= D.NT) return;
@@ -253,7 +263,7 @@ __global__ void k_interp(Dev D) {
     return;
   }
   int deg = D.degC[s];
-  if (is_sp(tt)) {
+  if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     double v0 = 0.0, v1 = 0.0, norm = 0.0;
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
@@ -461,10 +471,19 @@ __global__ void k_shift(Dev D, int reposition) {
     }
 }
 
-// get_derivatives (2_SPH_main_2018.f90:487-648) + the per-particle stage work of RK4
-__global__ void k_derivs(Dev D, int stage) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
+// get_derivatives (2_SPH_main_2018.f90:487-648) + the per-particle stage work of RK4.
+// KIND as k_interp.
+template <int KIND>
+__global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int ntgt) {
+  const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int s;
+  if (KIND == 0) {
+    s = k0;
+    if (s >= D.N2) return;
+  } else {
+    if (k0 >= ntgt) return;
+    s = tgt[k0];
+  }
   int t = D.sorted[s];
   if (t >= D.NT) return;
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
@@ -475,7 +494,7 @@ __global__ void k_derivs(Dev D, int stage) {
   int deg = D.degC[s];
   double AE[4] = {0.0, 0.0, 0.0, 0.0};
   const double xt = D.px[t], yt = D.py[t];
-  if (is_sp(tt)) {
+  if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     double g[4] = {0.0, 0.0, 0.0, 0.0};  // grad1(a,b) at a + 2b
     const double vt[2] = {D.vx[t], D.vy[t]};
     for (int k = 0; k < deg; k++) {
@@ -768,6 +787,30 @@ void launch_vol(Ctx& c, int lo, int hi) {
   if (hi > lo) k_vol<<<(hi - lo + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d, lo, hi);
 }
 
+// the plain interpolation and derivative kernels, split by target kind like the FP32 form's
+void launch_pinterp(Ctx& c) {
+  const Dev& D = c.d;
+  const int b = c.blk[TK_INTERP], ns = D.NT - D.NN;
+  if (!D.sp_sph) {
+    k_interp<0><<<c.grid_of(TK_INTERP, D.N2), b, 0, c.stream>>>(D, nullptr, 0);
+    return;
+  }
+  c.kernels_launched += 1;
+  if (ns > 0) k_interp<1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, D.tgtS, ns);
+  k_interp<2><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, D.tgtN, D.NN);
+}
+void launch_pderivs(Ctx& c, int stage) {
+  const Dev& D = c.d;
+  const int b = c.blk[TK_DERIVS], ns = D.NT - D.NN;
+  if (!D.sp_sph) {
+    k_derivs<0><<<c.grid_of(TK_DERIVS, D.N2), b, 0, c.stream>>>(D, stage, nullptr, 0);
+    return;
+  }
+  c.kernels_launched += 1;
+  if (ns > 0) k_derivs<1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
+  k_derivs<2><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
+}
+
 int launch_plain_step(Ctx& c) {
   Dev& D = c.d;
   cudaStream_t st = c.stream;
@@ -781,7 +824,7 @@ int launch_plain_step(Ctx& c) {
     // adapt_stress2 (2_SPH_main_2018.f90:99-108)
     c.mark("interp");
     if (D.fast) launch_finterp(c);
-    else k_interp<<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, st>>>(D);
+    else launch_pinterp(c);
     if (D.cont_density) {
       c.mark("node_rho");
       k_node_rho<<<nbN, kBlock, 0, st>>>(D);
@@ -800,7 +843,7 @@ int launch_plain_step(Ctx& c) {
     k_stage_begin<<<c.grid_of(TK_STAGE, D.NT), c.blk[TK_STAGE], 0, st>>>(D, stage);
     c.mark("interp");
     if (D.fast) launch_finterp(c);
-    else k_interp<<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, st>>>(D);
+    else launch_pinterp(c);
     if (D.cont_density && D.sp_sph) {
       c.mark("node_rho");
       k_node_rho<<<nbN, kBlock, 0, st>>>(D);
@@ -813,7 +856,7 @@ int launch_plain_step(Ctx& c) {
     }
     c.mark("derivs");
     if (D.fast) launch_fderivs(c, stage);
-    else k_derivs<<<c.grid_of(TK_DERIVS, D.N2), c.blk[TK_DERIVS], 0, st>>>(D, stage);
+    else launch_pderivs(c, stage);
     if (D.fast) {
       c.mark("sp_tail");
       launch_fsp_tail(c, stage);
@@ -823,7 +866,7 @@ int launch_plain_step(Ctx& c) {
   k_rk_final<<<c.grid_of(TK_RKFINAL, D.NT), c.blk[TK_RKFINAL], 0, st>>>(D);
   c.mark("interp");
   if (D.fast) launch_finterp(c);
-  else k_interp<<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, st>>>(D);
+  else launch_pinterp(c);
   if (D.cont_density && D.sp_sph) {
     c.mark("node_rho");
     k_node_rho<<<nbN, kBlock, 0, st>>>(D);

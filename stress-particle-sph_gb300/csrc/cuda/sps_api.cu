@@ -671,11 +671,12 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.rinv = dalloc<double>(c, N2);
     for (int k = 0; k < 3; k++) D.A[k] = dalloc<double>(c, NT);
     D.fast = (p->precision == SPS_PREC_FP32_FAST) ? 1 : 0;
+    // stress-point and node targets in sorted order (both forms)
+    D.tgtS = dalloc<int32_t>(c, NT - NN_ + 1);
+    D.tgtN = dalloc<int32_t>(c, NN_ + 1);
+    D.tflag = dalloc<int32_t>(c, 2 * N2);
+    D.toff = dalloc<int32_t>(c, 2 * N2 + 2);
     if (D.fast) {
-      D.tgtS = dalloc<int32_t>(c, NT - NN_ + 1);
-      D.tgtN = dalloc<int32_t>(c, NN_ + 1);
-      D.tflag = dalloc<int32_t>(c, 2 * N2);
-      D.toff = dalloc<int32_t>(c, 2 * N2 + 2);
       D.recV = dalloc<float4>(c, N2);
       D.recS = dalloc<float4>(c, NT);
       D.recI = dalloc<float4>(c, N2);
