@@ -26,9 +26,8 @@ constexpr int kBlock = 256;
 
 // ---- double-float (unevaluated sum of two FP32 numbers) arithmetic: Dekker, "A floating-
 // point technique for extending the available precision", Numer. Math. 18, 1971, with the
-// FMA-based exact product.  Used by the FP32 form to produce the FP32 kernel values the
-// reference stores (FP64 evaluation rounded to FP32): a double-float result (~44 bits)
-// rounds the same way except within ~1e-12 of an FP32 rounding boundary.
+// FMA-based exact product.  Used by the FP32 form for the separations and r/h of its pairs
+// (cubic_mixed).
 __device__ __forceinline__ dfl df_fast2sum(float a, float b) {
   float s = a + b;
   return {s, b - (s - a)};
@@ -52,17 +51,6 @@ __device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
   float e = fmaf(x.hi, y.hi, -p);
   e += x.hi * y.lo + x.lo * y.hi;
   return df_fast2sum(p, e);
-}
-// quotient seeds may be approximate: each residual step corrects them
-__device__ __forceinline__ dfl df_div(dfl x, dfl y) {
-  float yi = __frcp_rn(y.hi);
-  float q1 = x.hi * yi;
-  dfl r = df_add(x, df_neg(df_mul(y, {q1, 0.0f})));
-  float q2 = r.hi * yi;
-  r = df_add(r, df_neg(df_mul(y, {q2, 0.0f})));
-  float q3 = r.hi * yi;
-  dfl q = df_fast2sum(q1, q2);
-  return df_add(q, {q3, 0.0f});
 }
 __device__ __forceinline__ dfl df_sqrt(dfl x) {
   if (x.hi <= 0.0f) return {0.0f, 0.0f};
@@ -404,39 +392,39 @@ __device__ __forceinline__ void sph_kernel_f32(int skf, float pi, float r, float
   }
 }
 
-// the reference's cubic kernel for a uniform h (2_SPH_main_2018.f90:1468-1492) in
-// double-float, returning the FP32-rounded W and dW (the hi parts)
-__device__ __forceinline__ void cubic_df(const Grid& g, dfl dx, dfl dy, float* w, float* dw0,
-                                         float* dw1) {
-  dfl r = df_sqrt(df_add(df_mul(dx, dx), df_mul(dy, dy)));
-  dfl q = df_mul(r, g.df_yh);
-  q = df_add(q, df_neg(df_mul(df_add(df_mul(q, g.df_h), df_neg(r)), g.df_yh)));  // refine r/h
+// the reference's cubic kernel for a uniform h (2_SPH_main_2018.f90:1468-1492) for the FP32
+// form: the separation, r and q = r/h in double-float, which removes the cancellations (of
+// the cell-relative offsets and of 2 - q near the edge of the support), then the
+// polynomial and the gradient in FP32 from the accurate q: W and dW within a few FP32 ulps
+// of the FP64 evaluation
+__device__ __forceinline__ void cubic_mixed(const Grid& g, dfl dx, dfl dy, float* w, float* dw0,
+                                            float* dw1) {
+  const dfl r = df_sqrt(df_add(df_mul(dx, dx), df_mul(dy, dy)));
+  const dfl q = df_mul(r, g.df_yh);
   *w = 0.0f;
   *dw0 = 0.0f;
   *dw1 = 0.0f;
   if (q.hi < 1.0f || (q.hi == 1.0f && q.lo <= 0.0f)) {
-    dfl q2 = df_mul(q, q);
-    dfl q3 = df_mul(q2, q);
-    dfl in = df_add(df_add({2.0f / 3.0f, 0.0f}, df_neg(q2)), {0.5f * q3.hi, 0.5f * q3.lo});
-    *w = df_mul(g.df_factor, in).hi;
-    dfl a = df_mul(df_mul(g.df_factor, df_add({-2.0f, 0.0f}, df_mul({1.5f, 0.0f}, q))), g.df_yhh);
-    *dw0 = (dx.hi == 0.0f) ? -0.0f : df_mul(a, dx).hi;  // a < 0: a * (+0) = -0
-    *dw1 = (dy.hi == 0.0f) ? -0.0f : df_mul(a, dy).hi;
+    const float qh = q.hi, q2 = qh * qh;
+    *w = g.df_factor.hi * ((2.0f / 3.0f - q2) + 0.5f * (q2 * qh));
+    const float a = (g.df_factor.hi * (-2.0f + 1.5f * qh)) * g.df_yhh.hi;
+    *dw0 = a * dx.hi;
+    *dw1 = a * dy.hi;
   } else if (q.hi < 2.0f || (q.hi == 2.0f && q.lo <= 0.0f)) {
-    dfl t = df_add({2.0f, 0.0f}, df_neg(q));
-    dfl t2 = df_mul(t, t);
-    *w = df_mul(g.df_factor6, df_mul(t2, t)).hi;
-    dfl a = df_mul(df_mul(g.df_c3, t2), g.df_yh);
-    dfl ar = df_div(a, r);
-    *dw0 = (dx.hi == 0.0f) ? -0.0f : -df_mul(ar, dx).hi;  // -(a * (+0)) = -0
-    *dw1 = (dy.hi == 0.0f) ? -0.0f : -df_mul(ar, dy).hi;
+    const float t = (2.0f - q.hi) - q.lo;  // 2 - q.hi is exact
+    const float t2 = t * t;
+    *w = g.df_factor6.hi * (t2 * t);
+    const float ar = ((g.df_c3.hi * t2) * g.df_yh.hi) / r.hi;
+    *dw0 = -(ar * dx.hi);
+    *dw1 = -(ar * dy.hi);
   }
 }
 
 // Pairs created by the particle at sorted position s, in the reference's creation order:
 // the rest of its own cell, the cell to its right, then the three cells of the row above.
 // FAST = false: W and dW from the reference's FP64 kernel, stored in FP32 (the plain
-// form); FAST = true: kernel evaluated in FP32 (the FP32 form).  The pair set is the same.
+// form); FAST = true: the FP32 form's evaluation (cubic_mixed, or FP32 for a varying h).
+// The pair set is the same.
 template <bool FAST>
 __global__ void k_half(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -511,7 +499,7 @@ __global__ void k_half(Dev D) {
                          {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
         dfl ddy = df_add(df_add({ya, yal}, {-D.yr[b], -D.yrl[b]}),
                          {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
-        cubic_df(g, ddx, ddy, &wf, &d0f, &d1f);
+        cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
       } else {
         float hm = (ha + D.hr[b]) * 0.5f;
         float rf = sqrtf(fx * fx + fy * fy);

@@ -87,15 +87,13 @@ def test_fast_pairs_identical(built_gpu):
     cf, _ = run(p, _abi.SPS_PREC_FP32_FAST, 1)
     cp, _ = run(p, _abi.SPS_PREC_FP64_PLAIN, 1)
     a, b = cf.dump_pairs(), cp.dump_pairs()
-    # the FP32 form evaluates the kernel in double-float and reproduces the FP32-stored
-    # values of the FP64 evaluation, except where neither is accurate to an FP32 rounding
-    # boundary: near the edge of the support t = 2 - q cancels, and the FP64 evaluation
-    # itself carries a relative error of ~1e-16 / t there (about 2 in 10^4 values differ
-    # by one FP32 ulp)
+    # the FP32 form forms r and q = r/h in double-float (no cancellation of 2 - q near the
+    # edge of the support) and the polynomial in FP32: every value within a few FP32 ulps
+    # of the FP64 evaluation rounded to FP32 (about half of them identical)
     for k in ("w", "dwdx", "dwdy"):
         same = a[k].view(np.int32) == b[k].view(np.int32)
-        assert same.mean() >= 0.999, (k, same.mean())
-        np.testing.assert_allclose(a[k], b[k], rtol=3e-7, atol=1e-30)
+        assert same.mean() >= 0.25, (k, same.mean())
+        np.testing.assert_allclose(a[k], b[k], rtol=6e-7, atol=1e-30)
 
 
 def test_fast_column(built_gpu):
