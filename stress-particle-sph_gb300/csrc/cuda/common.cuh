@@ -166,6 +166,8 @@ struct Dev {
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
   float *xr, *yr, *hr;
   float *xrl, *yrl;  // FP32 form: low parts of the cell-relative offsets
+  float4* srec;       // by sorted position: (xr, yr, hr, 0) of the particle there
+  float2* srecl;      // by sorted position, FP32 form: (xrl, yrl)
   Grid* grid;                // per realisation
   GridTotal* gtot;
   unsigned long long* bbox;  // per realisation: ordered keys of minx, miny, -maxx, -maxy, -maxh, minh

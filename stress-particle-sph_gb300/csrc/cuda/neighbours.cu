@@ -304,10 +304,15 @@ __global__ void k_cell_sort(Dev D) {
   if (c == g.ncells) D.gtot->nactive = st;
 }
 
+// sorted position of every particle, and the pair search's per-particle values in sorted
+// order (the candidates of a cell are then read contiguously)
 __global__ void k_spos(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
-  D.spos[D.sorted[s]] = s;
+  const int t = D.sorted[s];
+  D.spos[t] = s;
+  D.srec[s] = make_float4(D.xr[t], D.yr[t], D.hr[t], 0.0f);
+  if (D.fast) D.srecl[s] = make_float2(D.xrl[t], D.yrl[t]);
 }
 
 // exact distance test of the reference (2_SPH_main_2018.f90:1345-1353) on the pair
@@ -326,12 +331,12 @@ __device__ __forceinline__ bool exact_test(const Dev& D, int a, int b, double& r
 // 0 = reject, 1 = accept, 2 = undecided (inside the guard band).  (cx, cy) is the corner
 // of b's cell relative to a's in FP32 (multiples of the cell size); fx, fy return the
 // FP32 separation x_a - x_b.
-__device__ __forceinline__ int prefilter(const Dev& D, float xa, float ya, float ha, int b,
+__device__ __forceinline__ int prefilter(const Dev& D, float xa, float ya, float ha, float4 rb,
                                          float cx, float cy, float tau, float& fx, float& fy) {
-  fx = (xa - D.xr[b]) - cx;
-  fy = (ya - D.yr[b]) - cy;
+  fx = (xa - rb.x) - cx;
+  fy = (ya - rb.y) - cy;
   float d2 = fx * fx + fy * fy;
-  float s = (float)D.scale_k * ((ha + D.hr[b]) * 0.5f);
+  float s = (float)D.scale_k * ((ha + rb.z) * 0.5f);
   float s2 = s * s;
   if (d2 < s2 * (1.0f - tau)) return 1;
   if (d2 > s2 * (1.0f + tau)) return 0;
@@ -459,13 +464,12 @@ __global__ void k_half(Dev D) {
     // the kernel values follow in phase 2, so that the lanes of a warp evaluate them
     // together instead of each time one lane accepts a candidate
     for (int bs = lo; bs < hi; bs++) {
-      int b = D.sorted[bs];
       float fx, fy;
-      int pf = prefilter(D, xa, ya, ha, b, cx, cy, tau, fx, fy);
+      int pf = prefilter(D, xa, ya, ha, D.srec[bs], cx, cy, tau, fx, fy);
       if (pf == 0) continue;
       if (pf == 2) {
         double r, dx, dy, mh;
-        if (!exact_test(D, a, b, r, dx, dy, mh)) continue;
+        if (!exact_test(D, a, D.sorted[bs], r, dx, dy, mh)) continue;
       }
       if (k < D.capH) out[k] = make_int4(bs, q, 0, 0);
       k++;
@@ -481,7 +485,8 @@ __global__ void k_half(Dev D) {
     const int qx = (q == 1 || q == 4) ? 1 : (q == 2 ? -1 : 0), qy = q >= 2 ? 1 : 0;
     {
       const float cx = (float)qx * cw, cy = (float)qy * ch;
-      const float fx = (xa - D.xr[b]) - cx, fy = (ya - D.yr[b]) - cy;
+      const float4 rb = D.srec[bs];
+      const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
       double r, dx, dy, mh;
       if (!FAST) exact_test(D, a, b, r, dx, dy, mh);
       float wf, d0f, d1f;
@@ -495,13 +500,14 @@ __global__ void k_half(Dev D) {
       } else if (g.uniform_h) {
         // separation as double-float from the cell-relative hi/lo offsets
         // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float
-        dfl ddx = df_add(df_add({xa, xal}, {-D.xr[b], -D.xrl[b]}),
+        const float2 rl = D.srecl[bs];
+        dfl ddx = df_add(df_add({xa, xal}, {-rb.x, -rl.x}),
                          {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
-        dfl ddy = df_add(df_add({ya, yal}, {-D.yr[b], -D.yrl[b]}),
+        dfl ddy = df_add(df_add({ya, yal}, {-rb.y, -rl.y}),
                          {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
         cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
       } else {
-        float hm = (ha + D.hr[b]) * 0.5f;
+        float hm = (ha + rb.z) * 0.5f;
         float rf = sqrtf(fx * fx + fy * fy);
         sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
       }

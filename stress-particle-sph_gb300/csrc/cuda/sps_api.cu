@@ -690,6 +690,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.yr = dalloc<float>(c, N2);
     D.hr = dalloc<float>(c, N2);
     D.xrl = dalloc<float>(c, N2);
+    D.srec = dalloc<float4>(c, N2);
+    D.srecl = dalloc<float2>(c, N2);
     D.yrl = dalloc<float>(c, N2);
     D.grid = dalloc<sps::Grid>(c, nreal);
     D.gtot = dalloc<sps::GridTotal>(c, 1);
