@@ -158,7 +158,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
 // is a sum of exact products.  This keeps the near-cancelling stress divergence accurate.
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets
 template <int KIND>
-__global__ void __launch_bounds__(256, 3) k_fderivs(Dev D, int stage,
+__global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int stage,
                                                     const int32_t* __restrict__ tgt, int ntgt) {
   const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (k0 >= ntgt) return;
