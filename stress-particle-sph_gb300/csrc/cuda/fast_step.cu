@@ -100,7 +100,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      if (D.itype[u] != 2) continue;
+      if (e.y < 0) continue;  // a dummy partner
       float w = __int_as_float(e.y);
       float4 r = D.recV[u];
       if (!have) {
@@ -123,7 +123,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      if (D.itype[u] != 1) continue;
+      if (e.y < 0) continue;  // a dummy partner
       float w = __int_as_float(e.y);
       float4 rs = D.recS[u];
       float4 ri = D.recI[u];
@@ -179,10 +179,10 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      int ut = D.itype[u];
+      const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       float Gx = __int_as_float(e.z), Gy = __int_as_float(e.w);
       float vol = D.recI[u].y;
-      if (ut == 2) {
+      if (!wall) {
         float4 r = D.recV[u];
         float h1 = Gx * vol, h2 = Gy * vol;
         float du0 = dfdiff(r.x, r.z, vh0, vl0), du1 = dfdiff(r.y, r.w, vh1, vl1);
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
           e2.add(xu * h2);
           e3.add(yu * h2);
         }
-      } else if (ut == 25) {
+      } else {
         double wall = (double)D.wallpos[u];
         double da, db;
         if (D.horiz[u] == 1.0f) {
@@ -229,10 +229,10 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      int ut = D.itype[u];
+      const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       float dwx = -__int_as_float(e.z), dwy = -__int_as_float(e.w);
       float m, d0, d1, d2;
-      if (ut == 1) {
+      if (!wall) {
         float4 ra = D.recA[u], rl = D.recAl[u];
         m = ra.w;
         d0 = dfdiff(ra.x, rl.x, ah.x, al.x);
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
           e2.add(xu * h2b);
           e3.add(yu * h2b);
         }
-      } else if (ut == 25) {
+      } else {
         // the dummy carries the node's stress: A_u = sigma_t / rho_d^2
         bc_int = 1;
         double ri = D.rinv[u];
@@ -256,8 +256,6 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         d0 = (float)fma(D.s0[t], ri2, -At[0]);
         d1 = (float)fma(D.s1[t], ri2, -At[1]);
         d2 = (float)fma(D.s2[t], ri2, -At[2]);
-      } else {
-        continue;
       }
       float mx = m * dwx, my = m * dwy;
       q0.add(mx * d0);

@@ -602,7 +602,10 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         int ut = D.itype[u];
         int pt = pint_type(tt, ut);
         bool same = (pt == 2 || pt == 3);
-        int4 e = make_int4(u, w, __float_as_int(gx), __float_as_int(gy));
+        // a wall (dummy) partner is marked by the sign bit of W (W >= 0): readers skip or
+        // branch on it without loading the partner's type
+        int4 e = make_int4(u, is_dummy(ut) ? (int)((unsigned)w | 0x80000000u) : w,
+                           __float_as_int(gx), __float_as_int(gy));
         const int64_t rel = cidx - meta.base;
         bool isnew = reorder && rel >= meta.m_prev;
         int64_t wp = !reorder ? rel : isnew ? meta.n - 1 - rel : (meta.n - meta.m_prev) + rel;

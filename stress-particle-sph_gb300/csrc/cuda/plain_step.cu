@@ -268,7 +268,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      if (D.itype[u] != 2) continue;
+      if (e.y < 0) continue;  // a dummy partner (sign bit of W)
       double w = (double)__int_as_float(e.y);
       double h2 = D.vol[u] * w;  // (mass/rho)*w with mass/rho formed once per particle
       v0 = v0 + D.vx[u] * h2;
@@ -284,7 +284,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      if (D.itype[u] != 1) continue;
+      if (e.y < 0) continue;  // a dummy partner (sign bit of W)
       double w = (double)__int_as_float(e.y);
       double ru = D.rho[u];
       double h1 = D.vol[u] * w;
@@ -500,10 +500,10 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      int ut = D.itype[u];
+      const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       double Gx = (double)__int_as_float(e.z), Gy = (double)__int_as_float(e.w);
       double mu = D.mass[u], ru = D.rho[u], iu = D.rinv[u];
-      if (ut == 2) {  // node -- stress-point (target is pair_i)
+      if (!wall) {  // node -- stress-point (target is pair_i)
         double h1 = div_rcp(Gx * mu, ru, iu);
         double h2 = div_rcp(Gy * mu, ru, iu);
         double du0 = D.vx[u] - vt[0], du1 = D.vy[u] - vt[1];
@@ -518,7 +518,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
           AE[2] = AE[2] + xu * h2;
           AE[3] = AE[3] + yu * h2;
         }
-      } else if (ut == 25) {  // stress-point -- dummy (dummy is pair_i)
+      } else {  // stress-point -- dummy (dummy is pair_i)
         double wall = (double)D.wallpos[u];
         double da, db;
         if (D.horiz[u] == 1.0f) {
@@ -550,10 +550,10 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
     for (int k = 0; k < deg; k++) {
       int4 e = D.cross[(size_t)k * D.N2 + s];
       int u = e.x;
-      int ut = D.itype[u];
+      const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       double dwx = -(double)__int_as_float(e.z), dwy = -(double)__int_as_float(e.w);
       double mu = D.mass[u];
-      if (ut == 1) {  // node -- stress-point (stress-point is pair_i)
+      if (!wall) {  // node -- stress-point (stress-point is pair_i)
         const double au[3] = {D.A[0][u], D.A[1][u], D.A[2][u]};
         for (int q = 0; q < 3; q++) {
           double sum = at[q] + au[q];
@@ -570,7 +570,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
           AE[2] = AE[2] + xu * h2b;
           AE[3] = AE[3] + yu * h2b;
         }
-      } else if (ut == 25) {  // node -- dummy: the dummy carries the node's stress
+      } else {  // node -- dummy: the dummy carries the node's stress
         bc_int = 1;
         double ru = D.rho[u];
         double ru2 = ru * ru;

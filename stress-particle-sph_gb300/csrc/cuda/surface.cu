@@ -31,7 +31,7 @@ __device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
   auto next_cross = [&]() {
     while (a < nC) {
       ea = D.cross[(size_t)a * D.N2 + s];
-      if (!is_dummy(D.itype[ea.x])) {
+      if (ea.y >= 0) {  // not a dummy partner (sign bit of W)
         ka = D.keyC[(size_t)a * D.N2 + s];
         return;
       }
@@ -159,8 +159,8 @@ __global__ void k_fs_scan(Dev D) {
     inside = in_scan_region(R, D.px[u], D.py[u]);
   }
   for (int k = 0; k < nC && !inside; k++) {
-    int u = D.cross[(size_t)k * D.N2 + s].x;
-    if (is_dummy(D.itype[u])) inside = in_scan_region(R, D.px[u], D.py[u]);
+    const int4 e = D.cross[(size_t)k * D.N2 + s];
+    if (e.y < 0) inside = in_scan_region(R, D.px[e.x], D.py[e.x]);  // dummy partners
   }
   int sub = inside ? 2 : 1;
   D.fint[t] = inside ? -1.0f : 0.0f;
