@@ -66,8 +66,16 @@ struct Ctx {
   int precision = SPS_PREC_FP64_PLAIN;
   std::string last_error;
   // graphs of one step, one per step variant (bit 0: the outside approach's
-  // re-interpolation at the start of the step, bit 1: its stress-point shift at the end)
-  cudaGraphExec_t graphs[4] = {nullptr, nullptr, nullptr, nullptr};
+  // re-interpolation at the start of the step, bit 1: its stress-point shift at the end,
+  // bit 2: the lists written with their walk-order keys)
+  cudaGraphExec_t graphs[8] = {nullptr, nullptr, nullptr, nullptr,
+                               nullptr, nullptr, nullptr, nullptr};
+  // keys in the step: when the state is downloaded (or snapshotted) with its free surface
+  // after every step, the step writes the lists' keys (a few percent of the list build)
+  // so that the detection need not rebuild the lists
+  bool keys_in_step = false;   // steps write keys
+  bool keys_written = false;   // the last step wrote them
+  int64_t last_refresh = -1;   // steps_done at the last on-demand detection
   int step_variant = 0;    // the variant launch_*_step enqueues
   int64_t itimestep = 0;   // itimestep_sph of the last step (0 after an upload)
   bool use_graph = true;

@@ -855,7 +855,7 @@ int launch_pair_build(Ctx& c) {
   c.mark("pair_meta");
   k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("lists");
-  launch_lists(c, c.surf_every);
+  launch_lists(c, c.surf_every || (c.step_variant & 4));
   if (D.sp_sph) {
     c.mark("split_targets", 8);
     k_target_flags<<<nb, kBlock, 0, st>>>(D);

@@ -321,7 +321,8 @@ int variant_of(const sps::Ctx& c, int64_t it) {
 // enqueue one step (itimestep_sph advanced first) as its variant's graph, or directly
 void enqueue_step(sps::Ctx& c) {
   c.itimestep += 1;
-  c.step_variant = variant_of(c, c.itimestep);
+  c.step_variant = variant_of(c, c.itimestep) | (c.keys_in_step ? 4 : 0);
+  c.keys_written = c.keys_in_step || c.surf_every;
   if (c.use_graph && !c.profiling) {
     if (!c.graphs[c.step_variant]) build_graph(c);
     SPS_CUDA_CHECK(cudaGraphLaunch(c.graphs[c.step_variant], c.stream));
@@ -759,7 +760,10 @@ namespace {
 // the free-surface detection of the last step, when it was left for the download
 void refresh_surface(sps::Ctx& c, bool sync = true) {
   if (!c.surf_stale) return;
-  sps::launch_lists_keys(c);
+  // detections one or two steps apart: let the following steps write the keys
+  c.keys_in_step = c.last_refresh >= 0 && c.steps_done - c.last_refresh <= 2;
+  c.last_refresh = c.steps_done;
+  if (!c.keys_written) sps::launch_lists_keys(c);
   sps::launch_surface(c);
   SPS_CUDA_CHECK(cudaGetLastError());
   if (sync) SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
@@ -1510,8 +1514,11 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     };
     copy(true);
+    // the profiled steps overwrite the pair tables: detect a pending free surface first
+    refresh_surface(c);
     const bool stale = c.surf_stale;
     const int64_t it0 = c.itimestep;
+    const bool kin = c.keys_in_step, kw = c.keys_written;
     const int cand[] = {64, 128, 256, 512};
     int best[sps::TK_N];
     double best_ms[sps::TK_N];
@@ -1542,6 +1549,8 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     }
     c.surf_stale = stale;
     c.itimestep = it0;
+    c.keys_in_step = kin;
+    c.keys_written = kw;
     SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     cudaFree(snap);

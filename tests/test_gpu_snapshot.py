@@ -106,3 +106,21 @@ def test_snapshot_to_writer(built_gpu, tmp_path):
     res = (tmp_path / (prob.name + ".post.res")).read_text()
     assert res.count('Result "vel"') == 3
     ctx.close()
+
+
+def test_surface_every_step_matches(built_gpu):
+    """Downloads with the free surface after every step (the context then writes the list
+    keys during the steps) give the same fields as one download at the end."""
+    prob = cases.bui_like()
+    a, b = _ctx(prob, _abi.SPS_PREC_FP64_PLAIN), _ctx(prob, _abi.SPS_PREC_FP64_PLAIN)
+    t = 0.0
+    for _ in range(6):
+        t = a.step(1, t)
+        fa = a.download()
+    b.step(6, 0.0)
+    _same(fa, b.download(), prob.ntotal)
+    (na, sa), (nb, sb) = a.download_surface(), b.download_surface()
+    np.testing.assert_array_equal(sa, sb)
+    np.testing.assert_array_equal(na, nb)
+    a.close()
+    b.close()
