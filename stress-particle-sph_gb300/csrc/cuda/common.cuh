@@ -221,12 +221,25 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
 // operations on the bit patterns.  Values outside the range handled (zero, float
 // subnormals, overflow, Inf/NaN) take the hardware conversion.
 
+// The rare cases take the hardware conversions out of line: inlined, the compiler may
+// evaluate both sides of the branch and keep the FP64 pipe busy with a conversion whose
+// result is then discarded.  Zeros, which are common, are handled on the integer pipe.
+static __device__ __noinline__ float f32_rn_hw(double x) { return (float)x; }
+static __device__ __noinline__ double f64_of_hw(float f) { return (double)f; }
+static __device__ __noinline__ void f32_split_hw(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
 // RN-even double -> float, identical to (float)x
 __device__ __forceinline__ float f32_rn(double x) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
   const int E = (int)((h32 >> 20) & 0x7FFu);
-  if (E < 897 || E > 1150) return (float)x;
+  if (E < 897 || E > 1150) {
+    if ((u << 1) == 0ull) return __uint_as_float(h32 & 0x80000000u);  // +-0
+    return f32_rn_hw(x);
+  }
   const unsigned f23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
   const unsigned rem = l32 & 0x1FFFFFFFu;
   const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (f23 & 1u));
@@ -240,8 +253,12 @@ __device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
   const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
   const int E = (int)((h32 >> 20) & 0x7FFu);
   if (E < 949 || E > 1150) {
-    hi = (float)x;
-    lo = (float)(x - (double)hi);
+    if ((u << 1) == 0ull) {  // +-0: hi keeps the sign, x - hi = +0
+      hi = __uint_as_float(h32 & 0x80000000u);
+      lo = 0.0f;
+      return;
+    }
+    f32_split_hw(x, hi, lo);
     return;
   }
   const unsigned f23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
@@ -257,7 +274,11 @@ __device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
 __device__ __forceinline__ double f64_of(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned e = (b >> 23) & 0xFFu;
-  if (e == 0u || e == 255u) return (double)f;
+  if (e == 0u || e == 255u) {
+    if ((b << 1) == 0u)  // +-0
+      return __longlong_as_double((long long)((unsigned long long)(b & 0x80000000u) << 32));
+    return f64_of_hw(f);
+  }
   const unsigned h32 = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
   const unsigned l32 = b << 29;
   return __longlong_as_double((long long)(((unsigned long long)h32 << 32) | l32));
@@ -272,13 +293,16 @@ __device__ __forceinline__ double f64_of(float f) {
 // Otherwise (about one case in 2^24), and outside f32_rn's exponent range (zero included),
 // the correctly rounded quotient div_rcp(a, b, y) is rounded instead.  Checked against the
 // IEEE division bit for bit by sps_selftest_division.
+static __device__ __noinline__ float div_rcp_f32_slow(double a, double b, double y) {
+  return f32_rn(div_rcp(a, b, y));
+}
 __device__ __forceinline__ float div_rcp_f32(double a, double b, double y) {
   const double q = a * y;
   const unsigned long long u = (unsigned long long)__double_as_longlong(q);
   const int E = (int)((u >> 52) & 0x7FFu);
   const unsigned m28 = (unsigned)u & 0x0FFFFFFFu;
   if (E >= 897 && E <= 1150 && (m28 - 8u) <= 0x0FFFFFF0u) return f32_rn(q);
-  return f32_rn(div_rcp(a, b, y));
+  return div_rcp_f32_slow(a, b, y);
 }
 
 // ----------------------------------------------------------------------------------------

@@ -763,6 +763,7 @@ __global__ void k_selftest_conv(int64_t n, uint64_t seed, unsigned long long* ba
     double x = exp2(e * 3.3219280948873622) * ((r2 & 1) ? -1.0 : 1.0);
     if ((r2 & 0xF0) == 0) x = (double)(float)x;  // exact floats and halfway cases nearby
     if ((r2 & 0xF00) == 0) x = x + x * 0x1.0p-24;
+    if ((r2 & 0xF000) == 0) x = (r2 & 1) ? -0.0 : 0.0;  // signed zeros (an integer-pipe case)
     float h = f32_rn(x), hs, ls;
     f32_split(x, hs, ls);
     float hr = (float)x, lr = (float)(x - (double)hr);
