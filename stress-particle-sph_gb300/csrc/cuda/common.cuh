@@ -387,8 +387,24 @@ __device__ __forceinline__ void cubic_uniform(const Grid& g, double r, double dx
 }
 
 // adapt_stress2 body (3_SPH_material_2018.f90:2087-2161), FP64
+static __device__ __noinline__ void adapt_stress_full(double alpha2, double kc, double& a,
+                                                      double& b, double& c, double& d);
+// Inside the cone, clearly: yield >= 0 and yield^2 >= varj2 (1 + 2^-49) imply
+// yield >= RN(sqrt(varj2)) whatever the roundings of the two products (each within 2^-53),
+// so adapt_stress2 leaves the stress as it is and neither its square root nor its tension
+// cut (both out of line, below) need to run.  Bit-identical to the full routine.
 __device__ __forceinline__ void adapt_stress(double alpha2, double kc, double& a, double& b,
                                              double& c, double& d) {
+  const double smean = ((a + b) + d) / 3.0;
+  const double d0 = a - smean, d1 = b - smean, d2 = c, d3 = d - smean;
+  const double varj2 = d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3);
+  const double yield = -((alpha2 * 3.0) * smean) + kc;
+  if (yield > 1e-100 && yield < 1e100 && yield * yield >= varj2 * (1.0 + 0x1.0p-49)) return;
+  adapt_stress_full(alpha2, kc, a, b, c, d);
+}
+// adapt_stress2 (3_SPH_material_2018.f90:2087-2161) in the reference's FP64 arithmetic
+static __device__ __noinline__ void adapt_stress_full(double alpha2, double kc, double& a,
+                                                      double& b, double& c, double& d) {
   double smean = ((a + b) + d) / 3.0;
   double d0 = a - smean, d1 = b - smean, d2 = c, d3 = d - smean;
   double varj2 = d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3);
@@ -422,8 +438,22 @@ __device__ __forceinline__ void adapt_stress(double alpha2, double kc, double& a
 // 1/3, the test yield < sqrt(J2) as yield^2 < J2 (yield >= 0), and for the stress-points
 // actually returned 1/sqrt(J2) from an FP32 seed refined by two Newton steps in FP64
 // (relative error ~1e-16).  Explicit fma() keeps the FMA where the unit disables it.
+static __device__ __noinline__ void adapt_stress_fast_return(double alpha2, double kc,
+                                                             double shift, double& a,
+                                                             double& b, double& c, double& d);
 __device__ __forceinline__ void adapt_stress_fast(double alpha2, double kc, double shift,
                                                   double& a, double& b, double& c, double& d) {
+  const double third = 1.0 / 3.0;
+  const double smean = ((a + b) + d) * third;
+  const double d0 = a - smean, d1 = b - smean, d2 = c, d3 = d - smean;
+  const double varj2 = fma(d2, d2, 0.5 * fma(d0, d0, fma(d1, d1, d3 * d3)));
+  const double yield = fma(-3.0 * alpha2, smean, kc);
+  // the returned points (few: the loading ones) take the return out of line
+  if (yield < 0 || yield * yield < varj2) adapt_stress_fast_return(alpha2, kc, shift, a, b, c, d);
+}
+static __device__ __noinline__ void adapt_stress_fast_return(double alpha2, double kc,
+                                                             double shift, double& a,
+                                                             double& b, double& c, double& d) {
   const double third = 1.0 / 3.0;
   double smean = ((a + b) + d) * third;
   double d0 = a - smean, d1 = b - smean, d2 = c, d3 = d - smean;
