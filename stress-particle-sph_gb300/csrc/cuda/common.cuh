@@ -590,8 +590,9 @@ __device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, c
                                                const double* gu, double* fdp, double* G,
                                                double* vivel) {
   double f0 = *fdp;
-  auto tof = [](double v) { return (float)v; };
-  auto tod = [](float v) { return (double)v; };
+  // FP32 form: the conversions on the integer pipe (bit-identical to the hardware ones)
+  auto tof = [](double v) { return FAST ? f32_rn(v) : (float)v; };
+  auto tod = [](float v) { return FAST ? f64_of(v) : (double)v; };
   float tanfi = tof(M.tanfi), coh = tof(M.coh), young = tof(M.young), poiss = tof(M.poiss);
   float smean = FAST ? (float)(((s[0] + s[1]) + s[3]) * (1.0 / 3.0))
                      : (float)(((s[0] + s[1]) + s[3]) / 3.0);

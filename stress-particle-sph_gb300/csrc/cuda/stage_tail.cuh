@@ -122,11 +122,11 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
           capture_tuple(D, t, s2v, g, Gs);
       }
       if (FAST) {
-        float v0 = (float)vivel[0], v1 = (float)vivel[1], v2 = (float)vivel[2],
-              v3 = (float)vivel[3];
+        float v0 = f32_rn(vivel[0]), v1 = f32_rn(vivel[1]), v2 = f32_rn(vivel[2]),
+              v3 = f32_rn(vivel[3]);
         // explicit fmaf: the same rounding in every kernel that inlines this tail
         float q = fmaf(2.0f, fmaf(v0, v0, fmaf(v1, v1, __fmul_rn(v3, v3))), __fmul_rn(v2, v2));
-        der = (double)sqrtf(__fmul_rn(q, 1.0f / 3.0f));
+        der = f64_of(sqrtf(__fmul_rn(q, 1.0f / 3.0f)));
       } else {
         der = sqrt((2.0 * ((vivel[0] * vivel[0] + vivel[1] * vivel[1]) + vivel[3] * vivel[3]) +
                     vivel[2] * vivel[2]) /
