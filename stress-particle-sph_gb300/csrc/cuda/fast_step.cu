@@ -97,20 +97,38 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     Kahan v0, v1, nm;
     bool have = false;
     float4 ref = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
-      int u = e.x;
-      if (e.y < 0) continue;  // a dummy partner
-      float w = __int_as_float(e.y);
-      float4 r = D.recV[u];
+    auto term = [&](float w, float4 r, float vol) {
       if (!have) {
         ref = r;
         have = true;
       }
-      float h2 = D.recI[u].y * w;
+      float h2 = vol * w;
       v0.add(dfdiff(r.x, r.z, ref.x, ref.z) * h2);
       v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
       nm.add(h2);
+    };
+    // two neighbours a pass: their entries and records are loaded before either is summed,
+    // so that the loads overlap (the sum order is unchanged)
+    int k = 0;
+    for (; k + 1 < deg; k += 2) {
+      const int4 ea = D.cross[(size_t)k * D.N2 + s], eb = D.cross[(size_t)(k + 1) * D.N2 + s];
+      const bool va = ea.y >= 0, vb = eb.y >= 0;  // not dummy partners
+      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+      float ia = 0.f, ib = 0.f;
+      if (va) {
+        ra = D.recV[ea.x];
+        ia = D.recI[ea.x].y;
+      }
+      if (vb) {
+        rb = D.recV[eb.x];
+        ib = D.recI[eb.x].y;
+      }
+      if (va) term(__int_as_float(ea.y), ra, ia);
+      if (vb) term(__int_as_float(eb.y), rb, ib);
+    }
+    if (k < deg) {
+      const int4 e = D.cross[(size_t)k * D.N2 + s];
+      if (e.y >= 0) term(__int_as_float(e.y), D.recV[e.x], D.recI[e.x].y);
     }
     double norm = nm.val();
     if (norm != 0) {
@@ -120,13 +138,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     }
   } else {
     Kahan a, b, c, d, iv, rt, nm;
-    for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
-      int u = e.x;
-      if (e.y < 0) continue;  // a dummy partner
-      float w = __int_as_float(e.y);
-      float4 rs = D.recS[u];
-      float4 ri = D.recI[u];
+    auto term = [&](float w, float4 rs, float4 ri) {
       float h1 = ri.y * w;
       a.add(rs.x * h1);
       b.add(rs.y * h1);
@@ -135,6 +147,26 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       iv.add(ri.x * h1);
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
+    };
+    int k = 0;  // two neighbours a pass, as above
+    for (; k + 1 < deg; k += 2) {
+      const int4 ea = D.cross[(size_t)k * D.N2 + s], eb = D.cross[(size_t)(k + 1) * D.N2 + s];
+      const bool va = ea.y >= 0, vb = eb.y >= 0;
+      float4 sa = make_float4(0.f, 0.f, 0.f, 0.f), sb = sa, ja = sa, jb = sa;
+      if (va) {
+        sa = D.recS[ea.x];
+        ja = D.recI[ea.x];
+      }
+      if (vb) {
+        sb = D.recS[eb.x];
+        jb = D.recI[eb.x];
+      }
+      if (va) term(__int_as_float(ea.y), sa, ja);
+      if (vb) term(__int_as_float(eb.y), sb, jb);
+    }
+    if (k < deg) {
+      const int4 e = D.cross[(size_t)k * D.N2 + s];
+      if (e.y >= 0) term(__int_as_float(e.y), D.recS[e.x], D.recI[e.x]);
     }
     double norm = nm.val();
     double rn = 1.0 / norm;
