@@ -258,14 +258,12 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     const float4 ah = D.recA[t], al = D.recAl[t];
     const double At[3] = {D.A[0][t], D.A[1][t], D.A[2][t]};
     int bc_int = 0;
-    for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
-      int u = e.x;
+    auto term = [&](int4 e, float4 ra, float4 rl) {
+      const int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       float dwx = -__int_as_float(e.z), dwy = -__int_as_float(e.w);
       float m, d0, d1, d2;
       if (!wall) {
-        float4 ra = D.recA[u], rl = D.recAl[u];
         m = ra.w;
         d0 = dfdiff(ra.x, rl.x, ah.x, al.x);
         d1 = dfdiff(ra.y, rl.y, ah.y, al.y);
@@ -298,6 +296,28 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       q5.add(my * d2);
       sx.add(m, dwx);
       sy.add(m, dwy);
+    };
+    // two neighbours a pass: entries and records loaded before either is summed
+    int k = 0;
+    for (; k + 1 < deg; k += 2) {
+      const int4 ea = D.cross[(size_t)k * D.N2 + s], eb = D.cross[(size_t)(k + 1) * D.N2 + s];
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 aa = z, la = z, ab = z, lb = z;
+      if (ea.y >= 0) {
+        aa = D.recA[ea.x];
+        la = D.recAl[ea.x];
+      }
+      if (eb.y >= 0) {
+        ab = D.recA[eb.x];
+        lb = D.recAl[eb.x];
+      }
+      term(ea, aa, la);
+      term(eb, ab, lb);
+    }
+    if (k < deg) {
+      const int4 e = D.cross[(size_t)k * D.N2 + s];
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      term(e, e.y >= 0 ? D.recA[e.x] : z, e.y >= 0 ? D.recAl[e.x] : z);
     }
     double avx = 0.0, avy = 0.0;
     if (Mt.alpha > 0 || Mt.beta > 0) {
