@@ -23,6 +23,9 @@ namespace sps {
 namespace {
 
 constexpr int kBlock = 256;
+// half-list entries: partner id in the low 28 bits, pair type (pint_type) in the top 4
+constexpr int kHalfTypeShift = 28;
+constexpr unsigned kHalfIdMask = (1u << kHalfTypeShift) - 1u;
 
 // ---- double-float (unevaluated sum of two FP32 numbers) arithmetic: Dekker, "A floating-
 // point technique for extending the available precision", Numer. Math. 18, 1971, with the
@@ -475,8 +478,12 @@ __global__ void k_half(Dev D) {
       k++;
     }
   }
-  // phase 2: kernel values of the accepted pairs
+  // phase 2: kernel values of the accepted pairs.  The finished entry holds the partner's
+  // id with the pair type in its top bits (kHalfIdMask), so that the list build needs
+  // neither the partner's id nor its type from memory; within one stencil cell the
+  // entries ascend in id (a cell is sorted by id) as they do in sorted position.
   const int kk = min(k, D.capH);
+  const int ta = D.itype[a];
   for (int m = 0; m < kk; m++) {
     const int4 e0 = out[m];
     const int bs = e0.x, q = e0.y;
@@ -511,7 +518,9 @@ __global__ void k_half(Dev D) {
         float rf = sqrtf(fx * fx + fy * fy);
         sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
       }
-      out[m] = make_int4(bs, __float_as_int(wf), __float_as_int(d0f), __float_as_int(d1f));
+      const int pt = pint_type(ta, D.itype[b]);
+      out[m] = make_int4((int)((unsigned)b | ((unsigned)pt << kHalfTypeShift)), __float_as_int(wf),
+                         __float_as_int(d0f), __float_as_int(d1f));
     }
   }
   if (k > D.capH) {
@@ -598,13 +607,11 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
       // key of an entry: its position in the walk order of the realisation's list, and
       // whether the target is pair_i (creator of a same-type pair; the stress-point of a
       // node--stress-point pair)
-      auto push = [&](int u, int w, float gx, float gy, int64_t cidx, bool own) {
-        int ut = D.itype[u];
-        int pt = pint_type(tt, ut);
+      auto push = [&](int u, int pt, int w, float gx, float gy, int64_t cidx, bool own) {
         bool same = (pt == 2 || pt == 3);
-        // a wall (dummy) partner is marked by the sign bit of W (W >= 0): readers skip or
-        // branch on it without loading the partner's type
-        int4 e = make_int4(u, is_dummy(ut) ? (int)((unsigned)w | 0x80000000u) : w,
+        // a wall (dummy) partner (pair types 6 and 9 of a non-dummy target) is marked by the
+        // sign bit of W (W >= 0): readers skip or branch on it without loading its type
+        int4 e = make_int4(u, (pt == 6 || pt == 9) ? (int)((unsigned)w | 0x80000000u) : w,
                            __float_as_int(gx), __float_as_int(gy));
         const int64_t rel = cidx - meta.base;
         bool isnew = reorder && rel >= meta.m_prev;
@@ -665,13 +672,15 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
           int v[kG];
 #pragma unroll
           for (int q = 0; q < kG; q++)
-            v[q] = len[q] > 0 ? D.half[(size_t)as[q] * D.capH + pos[q] + (len[q] >> 1)].x : 0;
+            v[q] = len[q] > 0 ? (int)((unsigned)D.half[(size_t)as[q] * D.capH + pos[q] +
+                                                       (len[q] >> 1)].x & kHalfIdMask)
+                              : 0;
           more = false;
 #pragma unroll
           for (int q = 0; q < kG; q++)
             if (len[q] > 0) {
               const int half = len[q] >> 1;
-              if (v[q] < s) {
+              if (v[q] < t) {
                 pos[q] += half + 1;
                 len[q] -= half + 1;
               } else {
@@ -684,9 +693,9 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         for (int q = 0; q < kG; q++)
           if (pos[q] < cnt[q]) {
             const int4 e = D.half[(size_t)as[q] * D.capH + pos[q]];
-            if (e.x == s)
-              push(D.sorted[as[q]], e.y, -__int_as_float(e.z), -__int_as_float(e.w),
-                   D.half_off[as[q]] + pos[q], false);
+            if ((int)((unsigned)e.x & kHalfIdMask) == t)
+              push(D.sorted[as[q]], (int)((unsigned)e.x >> kHalfTypeShift), e.y,
+                   -__int_as_float(e.z), -__int_as_float(e.w), D.half_off[as[q]] + pos[q], false);
           }
       }
       {
@@ -694,8 +703,8 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         const int4* h = D.half + (size_t)s * D.capH;
         for (int k = 0; k < n; k++) {
           int4 e = h[k];
-          push(D.sorted[e.x], e.y, __int_as_float(e.z), __int_as_float(e.w), D.half_off[s] + k,
-               true);
+          push((int)((unsigned)e.x & kHalfIdMask), (int)((unsigned)e.x >> kHalfTypeShift), e.y,
+               __int_as_float(e.z), __int_as_float(e.w), D.half_off[s] + k, true);
         }
       }
       if (nC > D.capC || nS > D.capS) {

@@ -486,7 +486,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     NS += ps[r].nstress;
     ND += ps[r].ndummy;
   }
-  if (NN + NS + ND > 2000000000LL) return fail(nullptr, SPS_ERR_ARG, "too many particles");
+  if (NN + NS + ND >= (1LL << 28))  // half-list entries keep particle ids in 28 bits
+    return fail(nullptr, SPS_ERR_ARG, "too many particles (at most 2^28 - 1 per context)");
   const sps_params* p = &ps[0];
   sps_ctx* h = nullptr;
   try {
@@ -1281,7 +1282,7 @@ int sps_dump_pairs_real(sps_ctx* h, int32_t r, int32_t* pair_i, int32_t* pair_j,
     for (size_t s = lo; s < hi; s++)
       for (int k = 0; k < cnt[s]; k++) {
         const int4 e = half[(s - lo) * D.capH + k];
-        int a = sorted[s], b = sorted[e.x];
+        int a = sorted[s], b = (int)((unsigned)e.x & ((1u << 28) - 1u));  // the partner's id
         float ww, gx, gy;
         std::memcpy(&ww, &e.y, 4);
         std::memcpy(&gx, &e.z, 4);
