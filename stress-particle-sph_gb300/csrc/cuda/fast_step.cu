@@ -107,26 +107,30 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
       nm.add(h2);
     };
-    // two neighbours a pass: their entries and records are loaded before either is summed,
-    // so that the loads overlap (the sum order is unchanged)
+    // kP neighbours a pass: their entries and records are loaded before any is summed, so
+    // that the loads overlap (the sum order is unchanged)
+    constexpr int kP = 4;
     int k = 0;
-    for (; k + 1 < deg; k += 2) {
-      const int4 ea = D.cross[(size_t)k * D.N2 + s], eb = D.cross[(size_t)(k + 1) * D.N2 + s];
-      const bool va = ea.y >= 0, vb = eb.y >= 0;  // not dummy partners
-      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
-      float ia = 0.f, ib = 0.f;
-      if (va) {
-        ra = D.recV[ea.x];
-        ia = D.recI[ea.x].y;
+    for (; k + kP - 1 < deg; k += kP) {
+      int4 e[kP];
+      float4 r[kP];
+      float vol[kP];
+#pragma unroll
+      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + s];
+#pragma unroll
+      for (int q = 0; q < kP; q++) {
+        r[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        vol[q] = 0.f;
+        if (e[q].y >= 0) {  // not a dummy partner
+          r[q] = D.recV[e[q].x];
+          vol[q] = D.recI[e[q].x].y;
+        }
       }
-      if (vb) {
-        rb = D.recV[eb.x];
-        ib = D.recI[eb.x].y;
-      }
-      if (va) term(__int_as_float(ea.y), ra, ia);
-      if (vb) term(__int_as_float(eb.y), rb, ib);
+#pragma unroll
+      for (int q = 0; q < kP; q++)
+        if (e[q].y >= 0) term(__int_as_float(e[q].y), r[q], vol[q]);
     }
-    if (k < deg) {
+    for (; k < deg; k++) {
       const int4 e = D.cross[(size_t)k * D.N2 + s];
       if (e.y >= 0) term(__int_as_float(e.y), D.recV[e.x], D.recI[e.x].y);
     }
@@ -148,23 +152,26 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
     };
-    int k = 0;  // two neighbours a pass, as above
-    for (; k + 1 < deg; k += 2) {
-      const int4 ea = D.cross[(size_t)k * D.N2 + s], eb = D.cross[(size_t)(k + 1) * D.N2 + s];
-      const bool va = ea.y >= 0, vb = eb.y >= 0;
-      float4 sa = make_float4(0.f, 0.f, 0.f, 0.f), sb = sa, ja = sa, jb = sa;
-      if (va) {
-        sa = D.recS[ea.x];
-        ja = D.recI[ea.x];
+    constexpr int kP = 4;  // neighbours a pass, as above
+    int k = 0;
+    for (; k + kP - 1 < deg; k += kP) {
+      int4 e[kP];
+      float4 rs[kP], ri[kP];
+#pragma unroll
+      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + s];
+#pragma unroll
+      for (int q = 0; q < kP; q++) {
+        rs[q] = ri[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (e[q].y >= 0) {
+          rs[q] = D.recS[e[q].x];
+          ri[q] = D.recI[e[q].x];
+        }
       }
-      if (vb) {
-        sb = D.recS[eb.x];
-        jb = D.recI[eb.x];
-      }
-      if (va) term(__int_as_float(ea.y), sa, ja);
-      if (vb) term(__int_as_float(eb.y), sb, jb);
+#pragma unroll
+      for (int q = 0; q < kP; q++)
+        if (e[q].y >= 0) term(__int_as_float(e[q].y), rs[q], ri[q]);
     }
-    if (k < deg) {
+    for (; k < deg; k++) {
       const int4 e = D.cross[(size_t)k * D.N2 + s];
       if (e.y >= 0) term(__int_as_float(e.y), D.recS[e.x], D.recI[e.x]);
     }
