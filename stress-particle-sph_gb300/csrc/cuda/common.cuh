@@ -174,7 +174,8 @@ struct Dev {
   // pairs
   int4* half;
   int32_t* half_cnt;
-  ushort4* half_grp;  // per creator: where its pairs with stencil cells 1-4 start
+  int4* half_meta;    // per creator (sorted position): group starts 1-4 (16 bits each),
+                      // pair count, id
   int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
   int4 *cross, *same;
   int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)

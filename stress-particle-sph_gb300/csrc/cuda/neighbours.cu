@@ -528,8 +528,10 @@ __global__ void k_half(Dev D) {
     k = D.capH;
   }
   D.half_cnt[s] = k;
-  D.half_grp[s] = make_ushort4((unsigned short)gstart[1], (unsigned short)gstart[2],
-                               (unsigned short)gstart[3], (unsigned short)gstart[4]);
+  // what the list build reads of a creator, in one 16-byte record: where its pairs with
+  // stencil cells 1-4 start, its pair count and its id
+  D.half_meta[s] = make_int4((int)((unsigned)gstart[1] | ((unsigned)gstart[2] << 16)),
+                             (int)((unsigned)gstart[3] | ((unsigned)gstart[4] << 16)), k, a);
 }
 
 // pair counts of every realisation (its pairs are the half lists of its sorted range)
@@ -636,7 +638,7 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
       };
       // the creators before s, in ascending sorted position: each holds s at most once in
       // its (ascending) half list, among the pairs it made with s's cell, whose place in
-      // the list k_half recorded (half_grp: the starts of its five stencil cells).  The
+      // the list k_half recorded (half_meta: the starts of its five stencil cells).  The
       // stencil cell of s seen from a creator follows from the creator's cell: below-left,
       // below, below-right (region 0), left, own (region 1).  kG lower-bound searches run
       // interleaved, so that their dependent loads overlap; the hits are pushed in creator
@@ -648,22 +650,26 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
       const int b2 = (iy > 0 && ix + 1 < nx) ? D.cell_start[rowb + ix + 1] : hi[0];
       const int own0 = D.cell_start[c0g + c];
       for (int i0 = 0; i0 < ncand; i0 += kG) {
-        int as[kG], pos[kG], len[kG], cnt[kG];
-        ushort4 gr[kG];
+        int as[kG], pos[kG], len[kG], cnt[kG], cid[kG];
+        int4 mt[kG];
 #pragma unroll
         for (int q = 0; q < kG; q++) {
           const int i = i0 + q;
           as[q] = i < n0 ? lo[0] + i : lo[1] + (i - n0);
-          cnt[q] = i < ncand ? D.half_cnt[as[q]] : 0;
-          gr[q] = i < ncand ? D.half_grp[as[q]] : make_ushort4(0, 0, 0, 0);
+          mt[q] = i < ncand ? D.half_meta[as[q]] : make_int4(0, 0, 0, 0);
+          cnt[q] = mt[q].z;
+          cid[q] = mt[q].w;
         }
 #pragma unroll
         for (int q = 0; q < kG; q++) {
           const int i = i0 + q;
+          const unsigned g12 = (unsigned)mt[q].x, g34 = (unsigned)mt[q].y;
+          const int gs[6] = {0, (int)(g12 & 0xFFFFu), (int)(g12 >> 16), (int)(g34 & 0xFFFFu),
+                             (int)(g34 >> 16), cnt[q]};
           // stencil cell of s from the creator: 0 own, 1 right, 2 up-left, 3 up, 4 up-right
           const int st = i < n0 ? (as[q] < b1 ? 4 : as[q] < b2 ? 3 : 2) : (as[q] < own0 ? 1 : 0);
-          const int g0 = st == 0 ? 0 : st == 1 ? gr[q].x : st == 2 ? gr[q].y : st == 3 ? gr[q].z : gr[q].w;
-          const int g1 = st == 0 ? gr[q].x : st == 1 ? gr[q].y : st == 2 ? gr[q].z : st == 3 ? gr[q].w : cnt[q];
+          const int g0 = st == 0 ? gs[0] : st == 1 ? gs[1] : st == 2 ? gs[2] : st == 3 ? gs[3] : gs[4];
+          const int g1 = st == 0 ? gs[1] : st == 1 ? gs[2] : st == 2 ? gs[3] : st == 3 ? gs[4] : gs[5];
           pos[q] = g0;
           len[q] = i < ncand ? max(g1 - g0, 0) : 0;
         }
@@ -694,7 +700,7 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
           if (pos[q] < cnt[q]) {
             const int4 e = D.half[(size_t)as[q] * D.capH + pos[q]];
             if ((int)((unsigned)e.x & kHalfIdMask) == t)
-              push(D.sorted[as[q]], (int)((unsigned)e.x >> kHalfTypeShift), e.y,
+              push(cid[q], (int)((unsigned)e.x >> kHalfTypeShift), e.y,
                    -__int_as_float(e.z), -__int_as_float(e.w), D.half_off[as[q]] + pos[q], false);
           }
       }

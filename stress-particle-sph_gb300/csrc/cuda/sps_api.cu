@@ -699,7 +699,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.gtot = dalloc<sps::GridTotal>(c, 1);
     D.bbox = dalloc<unsigned long long>(c, 6 * (size_t)nreal);
     D.half_cnt = dalloc<int32_t>(c, N2);
-    D.half_grp = dalloc<ushort4>(c, N2);
+    D.half_meta = dalloc<int4>(c, N2);
     D.half_off = dalloc<int64_t>(c, N2 + 1);
     D.degC = dalloc<int32_t>(c, N2);
     D.degS = dalloc<int32_t>(c, N2);
