@@ -303,6 +303,17 @@ def kernel_bytes(name, prob, deg, fast=False):
     return None
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum per launch group) over the
+# algorithmic bytes of kernel_bytes, from one `ncu --set full` capture of the FP32 form on
+# the same slope at dx 0.03 m (321,848 particles, 5.78M pairs; the full-size workload is
+# too large to capture with ~40 passes).  Scaled to a full launch by the algorithmic bytes,
+# which grow with the list entries, as the traffic does.
+NCU_TRAFFIC_RATIO = {"lists": 561745408 / 276326496, "half": 118874368 / 105543208,
+                     "interp": 182772991 / 98788384, "derivs": 214352128 / 184740096}
+NCU_TRAFFIC_SOURCE = ("ncu --set full, FP32 form, slope at dx 0.03 m (5.78M pairs), "
+                      "scaled by algorithmic bytes")
+
+
 def timed_steps(ctx, nsteps, t, dist, local, mark=False):
     """Device time (ms, max over ranks) of nsteps graph-launched steps on the context's
     own stream; clocks sampled meanwhile.  t: the start time (None for a batch, which keeps
@@ -439,7 +450,11 @@ def run_ours(args):
         ach = b / (per_launch_ms * 1e-3) / 1e9
         roof = {"kernel": "k_" + top, "bound": "hbm", "achieved": round(ach, 1),
                 "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                "frac": round(ach / peaks.get("hbm_gbs"), 4), "traffic": None,
+                "frac": round(ach / peaks.get("hbm_gbs"), 4),
+                "traffic": int(b * NCU_TRAFFIC_RATIO[top]) if fast and top in
+                NCU_TRAFFIC_RATIO else None,
+                "traffic_source": NCU_TRAFFIC_SOURCE if fast and top in NCU_TRAFFIC_RATIO
+                else None,
                 "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(b),
                 "per_launch_ms": round(per_launch_ms, 4), "launches_per_step": top_n / 2,
                 "share_of_step": round(top_ms / sum(v[0] for v in prof.values()), 3)}
