@@ -14,10 +14,12 @@
 //     particles of all realisations last.
 //   pair tables per step:
 //     half[s*capH + k]  pairs created by the particle at sorted position s (the reference's
-//                       grid_find_NEW creation order), 16 B {b sorted pos, w, dwdx, dwdy}
-//     cross/same lists  ELL layout entry[k*N2 + s]: per target, the neighbours it meets in
-//                       the reference's linked-list walk order, 16 B {u id, w, Gx, Gy} with
-//                       G the kernel gradient with respect to the target.
+//                       grid_find_NEW creation order), 16 B {partner id | pair type << 28,
+//                       w, dwdx, dwdy}
+//     cross/same lists  ELL layout entry[k*N2 + lcol[s]]: per target, the neighbours it
+//                       meets in the reference's linked-list walk order, 16 B
+//                       {u id, w, Gx, Gy} with G the kernel gradient with respect to the
+//                       target; columns are grouped by target kind (Dev::lcol).
 // The FP64 plain kernels reproduce the reference's arithmetic operation by operation
 // (compiled with -fmad=false: no multiply-add contraction).
 #pragma once
@@ -178,11 +180,17 @@ struct Dev {
                       // pair count, id
   int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
   int4 *cross, *same;
+  // per-target lists in ELL layout: entry k of the target in list column c at k * N2 + c
   int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)
-  int32_t *degC, *degS;
-  // FP32 form: sorted positions of the stress-point and of the node targets (each in
-  // sorted order), so that the gathers run one kind per warp
+  int32_t *degC, *degS;  // by list column
+  // sorted positions of the stress-point and of the node targets (each in sorted order), so
+  // that the gathers run one kind per warp
   int32_t *tgtS, *tgtN, *tflag, *toff;
+  // list column of every sorted position: the stress-points first, then the nodes (each in
+  // sorted order, as tgtS and tgtN), then the rest.  The k-th target of a one-kind launch
+  // has column k (stress-points) or NT - NN + k (nodes), so a warp reads its targets' list
+  // entries as one contiguous run per slot.
+  int32_t* lcol;
   // get_nodes_on_free_surface: normal (module FP64), subset (1 surface, 2 inside), f_int
   double *nrmx, *nrmy;
   int8_t* subset;
@@ -647,6 +655,13 @@ __device__ __forceinline__ const Real& real_of(const Dev& D, int i) {
 // the node at the same place as a stress-point (and back), when every node has one
 __device__ __forceinline__ int node_of_sp(const Real& M, int t) { return M.node0 + (t - M.sp0); }
 __device__ __forceinline__ int sp_of_node(const Real& M, int n) { return M.sp0 + (n - M.node0); }
+
+// list column (Dev::lcol) of the k-th target of a launch: KIND 1 over tgtS, 2 over tgtN,
+// 0 over every sorted position s
+template <int KIND>
+__device__ __forceinline__ int list_col(const Dev& D, int k, int s) {
+  return KIND == 1 ? k : KIND == 2 ? (D.NT - D.NN) + k : D.lcol[s];
+}
 
 __device__ __forceinline__ bool is_sp(int t) { return t == 1; }
 __device__ __forceinline__ bool is_node(int t) { return t == 2; }

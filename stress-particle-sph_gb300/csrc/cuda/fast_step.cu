@@ -92,7 +92,8 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     }
     return;
   }
-  int deg = D.degC[s];
+  const int col = list_col<KIND>(D, k, s);
+  int deg = D.degC[col];
   if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     Kahan v0, v1, nm;
     bool have = false;
@@ -116,7 +117,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       float4 r[kP];
       float vol[kP];
 #pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + s];
+      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + col];
 #pragma unroll
       for (int q = 0; q < kP; q++) {
         r[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -131,7 +132,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
         if (e[q].y >= 0) term(__int_as_float(e[q].y), r[q], vol[q]);
     }
     for (; k < deg; k++) {
-      const int4 e = D.cross[(size_t)k * D.N2 + s];
+      const int4 e = D.cross[(size_t)k * D.N2 + col];
       if (e.y >= 0) term(__int_as_float(e.y), D.recV[e.x], D.recI[e.x].y);
     }
     double norm = nm.val();
@@ -158,7 +159,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       int4 e[kP];
       float4 rs[kP], ri[kP];
 #pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + s];
+      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + col];
 #pragma unroll
       for (int q = 0; q < kP; q++) {
         rs[q] = ri[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -172,7 +173,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
         if (e[q].y >= 0) term(__int_as_float(e[q].y), rs[q], ri[q]);
     }
     for (; k < deg; k++) {
-      const int4 e = D.cross[(size_t)k * D.N2 + s];
+      const int4 e = D.cross[(size_t)k * D.N2 + col];
       if (e.y >= 0) term(__int_as_float(e.y), D.recS[e.x], D.recI[e.x]);
     }
     double norm = nm.val();
@@ -208,7 +209,8 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
   const Real& Mt = real_of(D, t);
   const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   int tt = D.itype[t];
-  int deg = D.degC[s];
+  const int col = list_col<KIND>(D, k0, s);
+  int deg = D.degC[col];
   const double xt = D.px[t], yt = D.py[t];
   if (KIND == 1) {
     Kahan g0, g1, g2, g3, e0, e1, e2, e3;
@@ -216,7 +218,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     const float vh0 = (float)vtx, vh1 = (float)vty;
     const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int4 e = D.cross[(size_t)k * D.N2 + col];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       float Gx = __int_as_float(e.z), Gy = __int_as_float(e.w);
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     // two neighbours a pass: entries and records loaded before either is summed
     int k = 0;
     for (; k + 1 < deg; k += 2) {
-      const int4 ea = D.cross[(size_t)k * D.N2 + s], eb = D.cross[(size_t)(k + 1) * D.N2 + s];
+      const int4 ea = D.cross[(size_t)k * D.N2 + col], eb = D.cross[(size_t)(k + 1) * D.N2 + col];
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       float4 aa = z, la = z, ab = z, lb = z;
       if (ea.y >= 0) {
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       term(eb, ab, lb);
     }
     if (k < deg) {
-      const int4 e = D.cross[(size_t)k * D.N2 + s];
+      const int4 e = D.cross[(size_t)k * D.N2 + col];
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       term(e, e.y >= 0 ? D.recA[e.x] : z, e.y >= 0 ? D.recAl[e.x] : z);
     }
@@ -330,13 +332,13 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     if (Mt.alpha > 0 || Mt.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904) in FP32
       Kahan ax, ay;
-      int degs = D.degS[s];
+      int degs = D.degS[col];
       const double vtx = D.vx[t], vty = D.vy[t];
       const float vh0 = (float)vtx, vh1 = (float)vty;
       const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
       const float ht = (float)D.hsml[t], rt = (float)D.rho[t];
       for (int k = 0; k < degs; k++) {
-        int4 e = D.same[(size_t)k * D.N2 + s];
+        int4 e = D.same[(size_t)k * D.N2 + col];
         int u = e.x;
         float4 r = D.recV[u];
         float4 ri = D.recI[u];
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     g2v[5] = -(q5.val() + 2.0 * At[2] * Sy);
     double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
     double afx = 0.0, afy = 0.0;
-    if (D.art_stress) art_force_node(D, s, t, &afx, &afy);
+    if (D.art_stress) art_force_node(D, col, t, &afx, &afy);
     tail_node(D, sc, t, g2v, AE, bc_int, avx, avy, f2, afx, afy);
   }
 }
@@ -484,7 +486,8 @@ __global__ void k_fxsph(Dev D) {
   if (s >= D.N2) return;
   int t = D.sorted[s];
   if (t >= D.NT) return;
-  int deg = D.degS[s];
+  const int col = D.lcol[s];
+  int deg = D.degS[col];
   const double vt0 = D.vx[t], vt1 = D.vy[t];
   float vh0, vh1, vl0, vl1;
   f32_split(vt0, vh0, vl0);
@@ -493,7 +496,7 @@ __global__ void k_fxsph(Dev D) {
   int flag = D.bc_or_not[t];
   bool mark = false;
   for (int k = 0; k < deg; k++) {
-    int4 e = D.same[(size_t)k * D.N2 + s];
+    int4 e = D.same[(size_t)k * D.N2 + col];
     int u = e.x;
     float w = __int_as_float(e.y);
     float4 r = D.recV[u];

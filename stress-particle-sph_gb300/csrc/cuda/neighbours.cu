@@ -556,18 +556,18 @@ __global__ void k_pair_meta(Dev D) {
 }
 
 template <bool KEYS>
-__device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, int s, int lo,
+__device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, int col, int lo,
                                             int hi) {
-  // reverse entries [lo, hi) of column s (and their keys)
+  // reverse entries [lo, hi) of list column col (and their keys)
   hi--;
   while (lo < hi) {
-    int4 t = base[(size_t)lo * N2 + s];
-    base[(size_t)lo * N2 + s] = base[(size_t)hi * N2 + s];
-    base[(size_t)hi * N2 + s] = t;
+    int4 t = base[(size_t)lo * N2 + col];
+    base[(size_t)lo * N2 + col] = base[(size_t)hi * N2 + col];
+    base[(size_t)hi * N2 + col] = t;
     if (KEYS) {
-      int32_t k = key[(size_t)lo * N2 + s];
-      key[(size_t)lo * N2 + s] = key[(size_t)hi * N2 + s];
-      key[(size_t)hi * N2 + s] = k;
+      int32_t k = key[(size_t)lo * N2 + col];
+      key[(size_t)lo * N2 + col] = key[(size_t)hi * N2 + col];
+      key[(size_t)hi * N2 + col] = k;
     }
     lo++;
     hi--;
@@ -583,6 +583,7 @@ __device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, in
 template <bool KEYS>
 __device__ __forceinline__ void lists_target(const Dev& D, int s) {
   int nC = 0, nS = 0, newC = 0, newS = 0;
+  const int col = D.lcol[s];
   if (s < D.gtot->nactive) {
     int t = D.sorted[s];
     int tt = D.itype[t];
@@ -622,15 +623,15 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         int32_t key = (int32_t)(2 * wp + role);
         if (same) {
           if (nS < D.capS) {
-            D.same[(size_t)nS * D.N2 + s] = e;
-            if (KEYS) D.keyS[(size_t)nS * D.N2 + s] = key;
+            D.same[(size_t)nS * D.N2 + col] = e;
+            if (KEYS) D.keyS[(size_t)nS * D.N2 + col] = key;
           }
           nS++;
           newS += isnew;
         } else if (pt != 0) {
           if (nC < D.capC) {
-            D.cross[(size_t)nC * D.N2 + s] = e;
-            if (KEYS) D.keyC[(size_t)nC * D.N2 + s] = key;
+            D.cross[(size_t)nC * D.N2 + col] = e;
+            if (KEYS) D.keyC[(size_t)nC * D.N2 + col] = key;
           }
           nC++;
           newC += isnew;
@@ -721,17 +722,17 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
       }
       // walk order: [new entries, descending creation] + [old entries, ascending]
       if (newC > 0) {
-        reverse_ell<KEYS>(D.cross, D.keyC, D.N2, s, 0, nC);
-        reverse_ell<KEYS>(D.cross, D.keyC, D.N2, s, newC, nC);
+        reverse_ell<KEYS>(D.cross, D.keyC, D.N2, col, 0, nC);
+        reverse_ell<KEYS>(D.cross, D.keyC, D.N2, col, newC, nC);
       }
       if (newS > 0) {
-        reverse_ell<KEYS>(D.same, D.keyS, D.N2, s, 0, nS);
-        reverse_ell<KEYS>(D.same, D.keyS, D.N2, s, newS, nS);
+        reverse_ell<KEYS>(D.same, D.keyS, D.N2, col, 0, nS);
+        reverse_ell<KEYS>(D.same, D.keyS, D.N2, col, newS, nS);
       }
     }
   }
-  D.degC[s] = nC;
-  D.degS[s] = nS;
+  D.degC[col] = nC;
+  D.degS[col] = nS;
 }
 
 template <bool KEYS>
@@ -819,7 +820,7 @@ void scan_impl(Ctx& c, const TI* in, TO* out, int n) {
 void scan_i32_to_i32(Ctx& c, const int32_t* in, int32_t* out, int n) { scan_impl(c, in, out, n); }
 void scan_i32_to_i64(Ctx& c, const int32_t* in, int64_t* out, int n) { scan_impl(c, in, out, n); }
 
-// FP32 form: flags (stress-point, node) of every sorted position, for the compaction below
+// flags (stress-point, node) of every sorted position, for the compaction below
 __global__ void k_target_flags(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
@@ -830,8 +831,18 @@ __global__ void k_target_flags(Dev D) {
 __global__ void k_target_scatter(Dev D) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
-  if (D.tflag[s]) D.tgtS[D.toff[s]] = s;
-  if (D.tflag[D.N2 + s]) D.tgtN[D.toff[D.N2 + 1 + s]] = s;
+  const int a = D.toff[s], b = D.toff[D.N2 + 1 + s];  // stress-points, nodes before s
+  int col;
+  if (D.tflag[s]) {
+    D.tgtS[a] = s;
+    col = a;
+  } else if (D.tflag[D.N2 + s]) {
+    D.tgtN[b] = s;
+    col = (D.NT - D.NN) + b;
+  } else {
+    col = D.NT + (s - a - b);
+  }
+  D.lcol[s] = col;
 }
 
 // per-target lists (k_lists), one thread per sorted position
@@ -869,15 +880,13 @@ int launch_pair_build(Ctx& c) {
   scan_i32_to_i64(c, D.half_cnt, D.half_off, D.N2);
   c.mark("pair_meta");
   k_pair_meta<<<1, 128, 0, st>>>(D);
+  c.mark("split_targets", 8);
+  k_target_flags<<<nb, kBlock, 0, st>>>(D);
+  scan_i32_to_i32(c, D.tflag, D.toff, D.N2);
+  scan_i32_to_i32(c, D.tflag + D.N2, D.toff + D.N2 + 1, D.N2);
+  k_target_scatter<<<nb, kBlock, 0, st>>>(D);
   c.mark("lists");
   launch_lists(c, c.surf_every || (c.step_variant & 4));
-  if (D.sp_sph) {
-    c.mark("split_targets", 8);
-    k_target_flags<<<nb, kBlock, 0, st>>>(D);
-    scan_i32_to_i32(c, D.tflag, D.toff, D.N2);
-    scan_i32_to_i32(c, D.tflag + D.N2, D.toff + D.N2 + 1, D.N2);
-    k_target_scatter<<<nb, kBlock, 0, st>>>(D);
-  }
   return 0;
 }
 

@@ -139,10 +139,10 @@ __global__ void k_bound(Dev D) {
   const Real& M = real_of(D, i);
   const int j0 = M.dum0, j1 = M.dum0 + M.ndum2;
   if (D.bound_from_lists) {
-    int s = D.spos[i];
-    int deg = D.degC[s];
+    const int col = D.lcol[D.spos[i]];
+    int deg = D.degC[col];
     for (int k = 0; k < deg; k++) {
-      int u = D.cross[(size_t)k * D.N2 + s].x;
+      int u = D.cross[(size_t)k * D.N2 + col].x;
       if (u < j0 || u >= j1) continue;
       float fx, fy;
       if (!bound_term(D, M, i, u, fx, fy)) continue;
@@ -262,11 +262,12 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     }
     return;
   }
-  int deg = D.degC[s];
+  const int col = list_col<KIND>(D, k0, s);
+  int deg = D.degC[col];
   if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     double v0 = 0.0, v1 = 0.0, norm = 0.0;
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int4 e = D.cross[(size_t)k * D.N2 + col];
       int u = e.x;
       if (e.y < 0) continue;  // a dummy partner (sign bit of W)
       double w = (double)__int_as_float(e.y);
@@ -282,7 +283,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
   } else {
     double a = 0.0, b = 0.0, c = 0.0, d = 0.0, iv = 0.0, rt = 0.0, norm = 0.0;
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int4 e = D.cross[(size_t)k * D.N2 + col];
       int u = e.x;
       if (e.y < 0) continue;  // a dummy partner (sign bit of W)
       double w = (double)__int_as_float(e.y);
@@ -463,7 +464,7 @@ __global__ void k_shift(Dev D, int reposition) {
     }
   }
   const float abs_vel = (float)sqrt(v0 * v0 + v1 * v1);
-  const int n_int = D.degS[D.spos[i]];
+  const int n_int = D.degS[D.lcol[D.spos[i]]];
   if ((D.bc_int[i] == 1 && abs_vel > 0.4f) || n_int < 2)
     for (int q = 0; q < np && q < 3; q++) {
       D.px[k + q] = xi;
@@ -491,14 +492,15 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
   const Real& Mt = real_of(D, t);
   const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   int tt = D.itype[t];
-  int deg = D.degC[s];
+  const int col = list_col<KIND>(D, k0, s);
+  int deg = D.degC[col];
   double AE[4] = {0.0, 0.0, 0.0, 0.0};
   const double xt = D.px[t], yt = D.py[t];
   if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     double g[4] = {0.0, 0.0, 0.0, 0.0};  // grad1(a,b) at a + 2b
     const double vt[2] = {D.vx[t], D.vy[t]};
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int4 e = D.cross[(size_t)k * D.N2 + col];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       double Gx = (double)__int_as_float(e.z), Gy = (double)__int_as_float(e.w);
@@ -548,7 +550,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
     const double stt[3] = {D.s0[t], D.s1[t], D.s2[t]};
     int bc_int = 0;
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + s];
+      int4 e = D.cross[(size_t)k * D.N2 + col];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       double dwx = -(double)__int_as_float(e.z), dwy = -(double)__int_as_float(e.w);
@@ -586,9 +588,9 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
     if (Mt.alpha > 0 || Mt.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904): FP32 accumulators
       float ax = 0.0f, ay = 0.0f;
-      int degs = D.degS[s];
+      int degs = D.degS[col];
       for (int k = 0; k < degs; k++) {
-        int4 e = D.same[(size_t)k * D.N2 + s];
+        int4 e = D.same[(size_t)k * D.N2 + col];
         int u = e.x;
         float xij = (float)(xt - D.px[u]);
         float yij = (float)(yt - D.py[u]);
@@ -611,7 +613,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
       avy = -(double)ay;
     }
     double afx = 0.0, afy = 0.0;
-    if (D.art_stress) art_force_node(D, s, t, &afx, &afy);
+    if (D.art_stress) art_force_node(D, col, t, &afx, &afy);
     tail_node(D, sc, t, g2, AE, bc_int, avx, avy, f2, afx, afy);
   }
 }
@@ -678,13 +680,14 @@ __global__ void k_xsph(Dev D) {
   if (s >= D.N2) return;
   int t = D.sorted[s];
   if (t >= D.NT) return;
-  int deg = D.degS[s];
+  const int col = D.lcol[s];
+  int deg = D.degS[col];
   const double vt0 = D.vx[t], vt1 = D.vy[t];
   double s0 = 0.0, s1 = 0.0;
   int flag = D.bc_or_not[t];
   bool mark = false;
   for (int k = 0; k < deg; k++) {
-    int4 e = D.same[(size_t)k * D.N2 + s];
+    int4 e = D.same[(size_t)k * D.N2 + col];
     int u = e.x;
     double w = (double)__int_as_float(e.y);
     double vol = D.vol[u];

@@ -678,6 +678,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.tgtN = dalloc<int32_t>(c, NN_ + 1);
     D.tflag = dalloc<int32_t>(c, 2 * N2);
     D.toff = dalloc<int32_t>(c, 2 * N2 + 2);
+    D.lcol = dalloc<int32_t>(c, N2);
     if (D.fast) {
       D.recV = dalloc<float4>(c, N2);
       D.recS = dalloc<float4>(c, NT);

@@ -168,7 +168,7 @@ __device__ __forceinline__ void tail_sp(const Dev& D, const StepScalars& sc, int
 // pairs in the reference's walk order, h = (dW f^n) (R_t + R_u) with f = W / W(dx, 1.2 dx)
 // and n = 2.55, dW taken w.r.t. t (so t's side of the pair gets + m_u h as pair_i and
 // - m_u h as pair_j, the same numbers); art_force = (T11 + T32, T31 + T22).
-__device__ __forceinline__ void art_force_node(const Dev& D, int s, int t, double* afx,
+__device__ __forceinline__ void art_force_node(const Dev& D, int col, int t, double* afx,
                                                double* afy) {
   const Real& M = real_of(D, t);
   double w2, g0, g1;
@@ -176,9 +176,9 @@ __device__ __forceinline__ void art_force_node(const Dev& D, int s, int t, doubl
   const double n = (double)2.55f;
   const double Rt[3] = {D.artR[t], D.artR[D.NN + t], D.artR[2 * (size_t)D.NN + t]};
   double T[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
-  const int degs = D.degS[s];
+  const int degs = D.degS[col];
   for (int k = 0; k < degs; k++) {
-    const int4 e = D.same[(size_t)k * D.N2 + s];
+    const int4 e = D.same[(size_t)k * D.N2 + col];
     const int u = e.x;
     const double fn = pow((double)__int_as_float(e.y) / w2, n);
     const double mu = D.mass[u];

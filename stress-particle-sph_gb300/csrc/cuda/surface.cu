@@ -23,16 +23,16 @@ constexpr int kBlock = 256;
 // the merged walk over a target's node--stress-point (cross, non-dummy neighbour) and
 // same-type entries, in ascending key; f(u, gx, gy, is_pair_i)
 template <typename F>
-__device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
-  const int nC = D.degC[s], nS = D.degS[s];
+__device__ __forceinline__ void walk_123(const Dev& D, int col, F&& f) {
+  const int nC = D.degC[col], nS = D.degS[col];
   int a = 0, b = 0;
   int32_t ka = 0, kb = 0;
   int4 ea = make_int4(0, 0, 0, 0), eb = make_int4(0, 0, 0, 0);
   auto next_cross = [&]() {
     while (a < nC) {
-      ea = D.cross[(size_t)a * D.N2 + s];
+      ea = D.cross[(size_t)a * D.N2 + col];
       if (ea.y >= 0) {  // not a dummy partner (sign bit of W)
-        ka = D.keyC[(size_t)a * D.N2 + s];
+        ka = D.keyC[(size_t)a * D.N2 + col];
         return;
       }
       a++;
@@ -40,8 +40,8 @@ __device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
   };
   next_cross();
   if (b < nS) {
-    eb = D.same[(size_t)b * D.N2 + s];
-    kb = D.keyS[(size_t)b * D.N2 + s];
+    eb = D.same[(size_t)b * D.N2 + col];
+    kb = D.keyS[(size_t)b * D.N2 + col];
   }
   while (a < nC || b < nS) {
     // one call site for both lists, so that a warp whose lanes take different lists runs
@@ -57,8 +57,8 @@ __device__ __forceinline__ void walk_123(const Dev& D, int s, F&& f) {
     } else {
       b++;
       if (b < nS) {
-        eb = D.same[(size_t)b * D.N2 + s];
-        kb = D.keyS[(size_t)b * D.N2 + s];
+        eb = D.same[(size_t)b * D.N2 + col];
+        kb = D.keyS[(size_t)b * D.N2 + col];
       }
     }
   }
@@ -85,7 +85,7 @@ __global__ void k_fs_normal0(Dev D) {
   if (t >= D.NT) return;
   const double xt = D.px[t], yt = D.py[t];
   float A0 = 0.0f, A1 = 0.0f, A2 = 0.0f, A3 = 0.0f, f0 = 0.0f, f1 = 0.0f;
-  walk_123(D, s, [&](int u, float gx, float gy, bool) {
+  walk_123(D, D.lcol[s], [&](int u, float gx, float gy, bool) {
     const double m = D.mass[u], rho = D.rho[u], ri = D.rinv[u];
     float h1 = hf_of(m, rho, ri, gx), h2 = hf_of(m, rho, ri, gy);
     double dx = D.px[u] - xt, dy = D.py[u] - yt;
@@ -152,14 +152,15 @@ __global__ void k_fs_scan(Dev D) {
   const int t = D.sorted[s];
   if (t >= D.NT) return;
   bool inside = false;
-  const int nS = D.degS[s], nC = D.degC[s];
+  const int col = D.lcol[s];
+  const int nS = D.degS[col], nC = D.degC[col];
   const ScanRegion R = scan_region(D, t);
   for (int k = 0; k < nS && !inside; k++) {
-    int u = D.same[(size_t)k * D.N2 + s].x;
+    int u = D.same[(size_t)k * D.N2 + col].x;
     inside = in_scan_region(R, D.px[u], D.py[u]);
   }
   for (int k = 0; k < nC && !inside; k++) {
-    const int4 e = D.cross[(size_t)k * D.N2 + s];
+    const int4 e = D.cross[(size_t)k * D.N2 + col];
     if (e.y < 0) inside = in_scan_region(R, D.px[e.x], D.py[e.x]);  // dummy partners
   }
   int sub = inside ? 2 : 1;
@@ -181,7 +182,7 @@ __global__ void k_fs_normal(Dev D) {
   const float xtf = (float)D.px[t], ytf = (float)D.py[t];
   double nx = 0.0, ny = 0.0;
   float nb = 0.0f, g0 = 0.0f, g1 = 0.0f;
-  walk_123(D, s, [&](int u, float gx, float gy, bool pair_i) {
+  walk_123(D, D.lcol[s], [&](int u, float gx, float gy, bool pair_i) {
     if (surf && D.subset[u] == 1) {
       // the reference adds the same vector x_j - x_i to both particles of the pair
       float xu = (float)D.px[u], yu = (float)D.py[u];
