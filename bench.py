@@ -63,6 +63,12 @@ def parse():
                     help="instead of timing: advance the FP64 plain and the FP32 forms this "
                          "many steps side by side and report their relative errors")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
+    ap.add_argument("--workload", default="slope", choices=["slope", "column-batch"],
+                    help="slope: the headline (one 2M-particle slope); column-batch: the "
+                         "combined form (batched columns, FP32 + surrogate vs FP64 plain)")
+    ap.add_argument("--columns", type=int, default=16)
+    ap.add_argument("--combined-steps", type=int, default=2000,
+                    help="column-batch: steps of both forms before their fields are compared")
     return ap.parse_args()
 
 
@@ -173,17 +179,23 @@ SURR_RANGES = dict(phi_deg=(26.0, 34.0), cohesion=(6e3, 14e3), young=(14e6, 26e6
 
 
 def train_surrogate(seed=0, nruns=6, dx=0.08, nsteps=2000, every=20, max_tuples=4000000,
-                    schedule=((10, 2e-3), (6, 5e-4), (4, 1e-4))):
-    """Capture tuples from coarse FP32 runs of the slope geometry with seeded materials and
-    train the network on the GPU; returns (net, envelope, summary)."""
+                    schedule=((10, 2e-3), (6, 5e-4), (4, 1e-4)), make=None, ranges=None,
+                    geometry="slope geometry"):
+    """Capture tuples from coarse FP32 runs of a geometry (default: the slope) with seeded
+    materials and train the network on the GPU; returns (net, envelope, summary).
+    make(dx, material) builds one training problem; ranges are the material draws."""
     import numpy as np
     import sps_gb300
     from sps_gb300 import _abi
     from sps_gb300 import surrogate as sg
+    if make is None:
+        def make(dx, mat):
+            return sps_gb300.Problem.slope(dx=dx, **dict(SLOPE, **mat))
+    ranges = SURR_RANGES if ranges is None else ranges
     w0 = time.perf_counter()
     runs = []
-    for mat in sg.stratified_materials(SURR_RANGES, nruns, seed):
-        prob = sps_gb300.Problem.slope(dx=dx, **dict(SLOPE, **mat))
+    for mat in sg.stratified_materials(ranges, nruns, seed):
+        prob = make(dx, mat)
         runs.append(sg.sample_run(prob, _abi.SPS_PREC_FP32_FAST, nsteps, every))
     data = np.concatenate(runs)
     captured = len(data)
@@ -199,8 +211,8 @@ def train_surrogate(seed=0, nruns=6, dx=0.08, nsteps=2000, every=20, max_tuples=
     t = hold[:, sg.NIN:].astype(np.float64)
     held = float(np.linalg.norm(y - t) / max(np.linalg.norm(t), 1e-300))
     summary = {"tuples": int(len(train)), "captured": int(captured), "runs": nruns,
-               "runs_desc": "slope geometry at dx %.3g m, %d steps, one step in %d captured, "
-                            "stratified draws of %s" % (dx, nsteps, every, SURR_RANGES),
+               "runs_desc": "%s at dx %.3g m, %d steps, one step in %d captured, "
+                            "stratified draws of %s" % (geometry, dx, nsteps, every, ranges),
                "capture_s": round(w1 - w0, 2), "train_s": round(w2 - w1, 2),
                "epochs": int(len(loss)), "schedule": [list(x) for x in schedule],
                "loss_first_epoch": float(loss[0]),
@@ -265,6 +277,114 @@ def run_batch(args, dist, local):
             "setup_s": round(w1 - w0, 2), "precision": "fp32 form", "autotuned_blocks": tuned,
             "bit_identical_to_single_runs": same, "clocks": clk,
             "workload": batch_problems.__doc__.split("\n")[0]}
+
+
+# the combined form: batched granular columns of the column-collapse material, friction
+# drawn per column; the surrogate is trained on coarse columns that bracket the draws
+COLUMN = dict(width=0.5, height=0.25, young=5.84e6, poiss=0.3, rho=2650.0, cohesion=0.0, k0=0.5)
+COLUMN_SURR_RANGES = dict(phi_deg=(19.0, 35.0), k0=(0.42, 0.58))
+
+
+def column_batch_problems(n=16, dx=0.001, seed=0):
+    """Granular columns 0.5 m wide x 0.25 m high at dx 1 mm (125,751 velocity + 125,000
+    stress particles each), left wall and a 2 m floor, rho 2650, E 5.84 MPa, nu 0.3, c 0,
+    K0 0.5, phi U[19,35] deg per column."""
+    import numpy as np
+    import sps_gb300
+    rng = np.random.default_rng(seed)
+    phis = rng.uniform(19.0, 35.0, n)
+    return [sps_gb300.Problem.column(dx=dx, phi_deg=float(p), **COLUMN) for p in phis], phis
+
+
+def run_combined(args):
+    """The combined form: a batch of granular columns advanced by the FP32 form with the
+    surrogate (exact fallback) and by the FP64 plain form, both as one batch context with a
+    graph-launched step; particle-steps/s of each, the fallback rate, and the runout and
+    field errors of the FP32 run against the plain run after the same steps."""
+    import numpy as np
+    import torch
+    import sps_gb300
+    from sps_gb300 import _abi
+    from sps_gb300 import surrogate as sg
+    rank, world, dist = dist_init("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sps_gb300.build_all()
+    w0 = time.perf_counter()
+    probs, phis = column_batch_problems(args.columns, seed=rank)
+    n = sum(p.nnode + p.nstress for p in probs)
+    net, env, training = train_surrogate(
+        dx=0.005, make=lambda dx, m: sps_gb300.Problem.column(dx=dx, **dict(COLUMN, **m)),
+        ranges=COLUMN_SURR_RANGES, geometry="column 0.5 x 0.25 m")
+    setup_s = time.perf_counter() - w0
+    nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
+    arms, fields, surr = {}, {}, None
+    for name, prec, use in (("fp32_surrogate", _abi.SPS_PREC_FP32_FAST, True),
+                            ("fp64_plain", _abi.SPS_PREC_FP64_PLAIN, False),
+                            ("fp32", _abi.SPS_PREC_FP32_FAST, False)):
+        b = sps_gb300.Batch(probs, precision=prec)
+        b.upload_all()
+        if use:
+            sg.install(b, net, tol=args.surrogate_tol, envelope=env)
+        sps_gb300.autotune(b, 2)
+        b.step(max(args.warmup, 1))
+        if use:
+            sg.stats(b, reset=True)
+        _, ms, clk = timed_steps(b, args.steps, None, dist, local)
+        arms[name] = {"value": round(n * args.steps * world / (ms * 1e-3), 1),
+                      "ms_per_step": round(ms / args.steps, 4), "clocks": clk}
+        if name != "fp32":
+            b.step(nlong - max(args.warmup, 1) - args.steps)
+            torch.cuda.synchronize()
+            fields[name] = [b.download(r) for r in range(len(probs))]
+            arms[name]["simulated_s"] = b.times[0]
+        if use:
+            loading, answered, outside, rejected = sg.stats(b)
+            lf = max(loading, 1)
+            surr = {"tol": args.surrogate_tol, "training": training,
+                    "loading_evaluations": loading, "answered_frac": round(answered / lf, 6),
+                    "outside_envelope_frac": round(outside / lf, 6),
+                    "fallback_rate": round(1.0 - answered / lf, 6)}
+        b.close()
+    per, pooled = [], {k: [0.0, 0.0] for k in ("stress", "vel", "displ")}
+    for r, p in enumerate(probs):
+        a, b = fields["fp32_surrogate"][r], fields["fp64_plain"][r]
+        nt, nn = p.nnode + p.nstress, p.nnode
+        row = {"phi_deg": round(float(phis[r]), 3)}
+        # runout: the front of the velocity particles (largest x) beyond the column's width
+        fa, fb = float(a["x"][0:2 * nn:2].max()), float(b["x"][0:2 * nn:2].max())
+        row["runout_plain_m"] = fb - COLUMN["width"]
+        row["runout_abs_err_m"] = abs(fa - fb)
+        for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
+                      ("displ", slice(None))):
+            d = a[k][sl] - b[k][sl]
+            pooled[k][0] += float(np.dot(d, d))
+            pooled[k][1] += float(np.dot(b[k][sl], b[k][sl]))
+            row[k + "_rel_l2"] = float(np.linalg.norm(d) / max(np.linalg.norm(b[k][sl]), 1e-300))
+        per.append(row)
+    errors = {"after_steps": nlong, "time_s": arms["fp64_plain"]["simulated_s"],
+              "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)",
+              "pooled": {k + "_rel_l2": float(np.sqrt(v[0] / max(v[1], 1e-300)))
+                         for k, v in pooled.items()},
+              "max_runout_abs_err_m": max(r["runout_abs_err_m"] for r in per),
+              "per_column": per}
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": arms["fp32_surrogate"]["value"],
+            "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": arms["fp32_surrogate"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (generated column geometry, no dataset)",
+            "config": {"workload": "combined form: %d granular columns in one batch context, "
+                                   "%d particles (%d velocity) in all; %s"
+                                   % (len(probs), n, sum(p.nnode for p in probs),
+                                      column_batch_problems.__doc__.split("\n")[0]),
+                       "precision": "fp32 neighbour sums (Kahan), fp64 state and stress "
+                                    "return, learned flow rule with exact fallback",
+                       "l2": "state and pair tables larger than L2; no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "arms": arms, "surrogate": surr, "error_vs_plain": errors,
+            "setup_s": round(setup_s, 1)}))
 
 
 def workload(dx):
@@ -680,6 +800,8 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "column-batch":
+        run_combined(args)
     else:
         run_ours(args)
 
