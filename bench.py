@@ -63,12 +63,14 @@ def parse():
                     help="instead of timing: advance the FP64 plain and the FP32 forms this "
                          "many steps side by side and report their relative errors")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
-    ap.add_argument("--workload", default="slope", choices=["slope", "column-batch"],
+    ap.add_argument("--workload", default="slope", choices=["slope", "column-batch", "biaxial"],
                     help="slope: the headline (one 2M-particle slope); column-batch: the "
-                         "combined form (batched columns, FP32 + surrogate vs FP64 plain)")
+                         "combined form (batched columns, FP32 + surrogate vs FP64 plain); "
+                         "biaxial: the surrogate's biaxial sample")
     ap.add_argument("--columns", type=int, default=16)
     ap.add_argument("--combined-steps", type=int, default=2000,
-                    help="column-batch: steps of both forms before their fields are compared")
+                    help="column-batch, biaxial: steps of the FP32 + surrogate and FP64 "
+                         "plain runs before their fields are compared")
     return ap.parse_args()
 
 
@@ -296,6 +298,115 @@ def column_batch_problems(n=16, dx=0.001, seed=0):
     return [sps_gb300.Problem.column(dx=dx, phi_deg=float(p), **COLUMN) for p in phis], phis
 
 
+def three_arms(args, make, n, net, env, training, dist, local, world):
+    """The FP32 form with the surrogate installed, the FP64 plain form and the FP32 form
+    alone on the same problem(s): each timed over args.steps graph-launched steps after the
+    warm-up; the first two then advance to args.combined_steps steps in all and their fields
+    are downloaded (one dict per realisation).  make(precision) -> uploaded context."""
+    import torch
+    from sps_gb300 import _abi
+    from sps_gb300 import surrogate as sg
+    import sps_gb300
+    nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
+    arms, fields, surr = {}, {}, None
+    for name, prec, use in (("fp32_surrogate", _abi.SPS_PREC_FP32_FAST, True),
+                            ("fp64_plain", _abi.SPS_PREC_FP64_PLAIN, False),
+                            ("fp32", _abi.SPS_PREC_FP32_FAST, False)):
+        b = make(prec)
+        if use:
+            sg.install(b, net, tol=args.surrogate_tol, envelope=env)
+        sps_gb300.autotune(b, 2)
+        single = not isinstance(b, sps_gb300.Batch)
+        t = b.step(max(args.warmup, 1), 0.0) if single else b.step(max(args.warmup, 1))
+        if use:
+            sg.stats(b, reset=True)
+        t, ms, clk = timed_steps(b, args.steps, t if single else None, dist, local)
+        arms[name] = {"value": round(n * args.steps * world / (ms * 1e-3), 1),
+                      "ms_per_step": round(ms / args.steps, 4), "clocks": clk}
+        if name != "fp32":
+            rest = nlong - max(args.warmup, 1) - args.steps
+            t = b.step(rest, t) if single else b.step(rest)
+            torch.cuda.synchronize()
+            fields[name] = [b.download()] if single else \
+                [b.download(r) for r in range(len(b.problems))]
+            arms[name]["simulated_s"] = t if single else b.times[0]
+        if use:
+            loading, answered, outside, rejected = sg.stats(b)
+            lf = max(loading, 1)
+            surr = {"tol": args.surrogate_tol, "training": training,
+                    "loading_evaluations": loading, "answered_frac": round(answered / lf, 6),
+                    "outside_envelope_frac": round(outside / lf, 6),
+                    "fallback_rate": round(1.0 - answered / lf, 6) if loading else None}
+        b.close()
+    return arms, fields, surr
+
+
+# the biaxial sample: the surrogate is trained on coarse samples with seeded materials and
+# faster platens (plastic within the captured steps)
+BIAXIAL = dict(width=0.05, height=0.10, young=50e6, poiss=0.25, rho=2000.0, phi_deg=35.0,
+               cohesion=0.0, platen_v=0.05, t_ramp=1e-4)
+BIAXIAL_SURR_RANGES = dict(phi_deg=(30.0, 40.0), young=(40e6, 60e6), poiss=(0.22, 0.28),
+                           rho=(1900.0, 2100.0))
+
+
+def run_biaxial(args):
+    """The surrogate's own configuration: a biaxial sample 0.05 m x 0.10 m at dx 0.1 mm
+    (501,501 velocity + 500,000 stress particles), rough platens closing at 0.05 m/s each,
+    cohesionless Drucker-Prager (phi 35 deg, E 50 MPa, nu 0.25, rho 2000).  The network is
+    trained on the GPU on up to 20M tuples captured from eight coarse samples (dx 1 mm,
+    platens 0.5 m/s, 12,000 steps, one in ten captured) with seeded material draws; then the
+    FP32 form with it, the FP64 plain form and the FP32 form alone are timed and compared."""
+    import numpy as np
+    import torch
+    import sps_gb300
+    rank, world, dist = dist_init("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    sps_gb300.build_all()
+    w0 = time.perf_counter()
+    prob = sps_gb300.Problem.biaxial(dx=1e-4, **BIAXIAL)
+    n = prob.nnode + prob.nstress
+    net, env, training = train_surrogate(
+        dx=0.001, nruns=8, nsteps=12000, every=10, max_tuples=20000000,
+        make=lambda dx, m: sps_gb300.Problem.biaxial(dx=dx, **dict(
+            BIAXIAL, platen_v=0.5, t_ramp=2e-5, **m)),
+        ranges=BIAXIAL_SURR_RANGES, geometry="biaxial sample 0.05 x 0.10 m, platens 0.5 m/s")
+    setup_s = time.perf_counter() - w0
+
+    def single(prec):
+        c = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", prob.params_copy(precision=prec))
+        c.upload_problem(prob)
+        return c
+
+    arms, fields, surr = three_arms(args, single, n, net, env, training, dist, local, world)
+    nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
+    a, b = fields["fp32_surrogate"][0], fields["fp64_plain"][0]
+    nt = prob.ntotal
+    errors = {"after_steps": nlong, "time_s": arms["fp64_plain"]["simulated_s"],
+              "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
+    for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
+                  ("displ", slice(None))):
+        l2, li = rel_errors(a[k][sl], b[k][sl])
+        errors[k + "_rel_l2"], errors[k + "_rel_linf"] = l2, li
+    errors["plastic_stress_points_plain"] = int((b["intvars1"][prob.nnode:nt] > 0).sum())
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": arms["fp32_surrogate"]["value"],
+            "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": arms["fp32_surrogate"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (generated biaxial sample, no dataset)",
+            "config": {"workload": "biaxial sample 0.05 x 0.10 m at dx 0.1 mm, %d velocity + "
+                                   "%d stress particles, platens 0.05 m/s"
+                                   % (prob.nnode, prob.nstress),
+                       "precision": "fp32 neighbour sums (Kahan), fp64 state and stress "
+                                    "return, learned flow rule with exact fallback",
+                       "l2": "state and pair tables larger than L2; no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "arms": arms, "surrogate": surr, "error_vs_plain": errors,
+            "setup_s": round(setup_s, 1)}))
+
+
 def run_combined(args):
     """The combined form: a batch of granular columns advanced by the FP32 form with the
     surrogate (exact fallback) and by the FP64 plain form, both as one batch context with a
@@ -317,35 +428,14 @@ def run_combined(args):
         dx=0.005, make=lambda dx, m: sps_gb300.Problem.column(dx=dx, **dict(COLUMN, **m)),
         ranges=COLUMN_SURR_RANGES, geometry="column 0.5 x 0.25 m")
     setup_s = time.perf_counter() - w0
-    nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
-    arms, fields, surr = {}, {}, None
-    for name, prec, use in (("fp32_surrogate", _abi.SPS_PREC_FP32_FAST, True),
-                            ("fp64_plain", _abi.SPS_PREC_FP64_PLAIN, False),
-                            ("fp32", _abi.SPS_PREC_FP32_FAST, False)):
+
+    def batch(prec):
         b = sps_gb300.Batch(probs, precision=prec)
         b.upload_all()
-        if use:
-            sg.install(b, net, tol=args.surrogate_tol, envelope=env)
-        sps_gb300.autotune(b, 2)
-        b.step(max(args.warmup, 1))
-        if use:
-            sg.stats(b, reset=True)
-        _, ms, clk = timed_steps(b, args.steps, None, dist, local)
-        arms[name] = {"value": round(n * args.steps * world / (ms * 1e-3), 1),
-                      "ms_per_step": round(ms / args.steps, 4), "clocks": clk}
-        if name != "fp32":
-            b.step(nlong - max(args.warmup, 1) - args.steps)
-            torch.cuda.synchronize()
-            fields[name] = [b.download(r) for r in range(len(probs))]
-            arms[name]["simulated_s"] = b.times[0]
-        if use:
-            loading, answered, outside, rejected = sg.stats(b)
-            lf = max(loading, 1)
-            surr = {"tol": args.surrogate_tol, "training": training,
-                    "loading_evaluations": loading, "answered_frac": round(answered / lf, 6),
-                    "outside_envelope_frac": round(outside / lf, 6),
-                    "fallback_rate": round(1.0 - answered / lf, 6)}
-        b.close()
+        return b
+
+    arms, fields, surr = three_arms(args, batch, n, net, env, training, dist, local, world)
+    nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
     per, pooled = [], {k: [0.0, 0.0] for k in ("stress", "vel", "displ")}
     for r, p in enumerate(probs):
         a, b = fields["fp32_surrogate"][r], fields["fp64_plain"][r]
@@ -802,6 +892,8 @@ def main():
         run_reference(args)
     elif args.workload == "column-batch":
         run_combined(args)
+    elif args.workload == "biaxial":
+        run_biaxial(args)
     else:
         run_ours(args)
 

@@ -63,6 +63,27 @@ typedef struct sph_column_spec {
 } sph_column_spec;
 int sph_problem_column(const sph_column_spec* spec, sph_problem** out);
 
+/* Biaxial compression sample [0,width]x[0,height], no walls or gravity: the top and bottom
+   node rows are rough platens (vx = 0, vy = -/+ platen_v ramped in linearly over t_ramp),
+   the side columns carry the normal stress sxx = -confining and sxy = 0, all as the
+   reference's segment BCs (Normal_BCs, 3_SPH_material_2018.f90:1666), the layout of its
+   strain-localisation example.  Initial stress sxx = szz = -confining, syy = -confining -
+   q_ratio * q_y, with q_y the axial excess that puts the state on the Drucker-Prager cone
+   (0 <= q_ratio < 1).  A stress BC sets the boundary nodes' stress; it does not add the
+   traction to their momentum balance, whose neighbour sums stay one-sided, so a compressive
+   confining value pushes the sides outwards instead of confining the sample: the
+   localisation example uses 0, as do the defaults of the bindings. */
+typedef struct sph_biaxial_spec {
+  double width, height, dx, sml;
+  double young, poiss, rho, phi_deg, cohesion;
+  double confining;  /* Pa, > 0 in compression */
+  double platen_v;   /* m/s, each platen towards the middle */
+  double t_ramp;     /* s, > 0 */
+  double q_ratio;
+  double dt;         /* 0 -> 0.1 h / sqrt(E/rho) */
+} sph_biaxial_spec;
+int sph_problem_biaxial(const sph_biaxial_spec* spec, sph_problem** out);
+
 /* Vertical slope: a foundation [0,Lf]x[0,Hf] with a block [0,Ls]x[Hf,Hf+Hs] on top (vertical
    face at x = Ls), floor and side walls around the foundation, K0 stress, gravity ramped
    from 0 to 1 over t_ramp by a time curve. Masses follow the reference's rule (each node

@@ -776,6 +776,84 @@ int sph_problem_column(const sph_column_spec* s, sph_problem** out) {
   return SPS_OK;
 }
 
+int sph_problem_biaxial(const sph_biaxial_spec* s, sph_problem** out) {
+  if (!s || !out || s->dx <= 0 || s->width <= 0 || s->height <= 0 || s->confining < 0 ||
+      s->q_ratio < 0 || s->q_ratio >= 1 || s->t_ramp <= 0)
+    return SPS_ERR_ARG;
+  *out = nullptr;
+  const double h = s->sml * s->dx;
+  const double dt = s->dt > 0 ? s->dt : 0.1 * h / std::sqrt(s->young / s->rho);
+  const double tanphi = std::tan(s->phi_deg * M_PI / 180.0);
+  std::string pts = "geom_type\n1\nx1 x2 x3 x4 dx\n" +
+                    fmt("0 %.17g 0 %.17g %.17g\n", s->width, s->width, s->dx) +
+                    "y1 y2 y3 y4 dy\n" +
+                    fmt("0 0 %.17g %.17g %.17g\n", s->height, s->height, s->dx) +
+                    "dummy_nodes\nF\n";
+  std::string in = "problem name\nbiaxial\nSP_SPH art_stress particle_shift\nT F F\n"
+                   "inside_approach\nT\nnpoints\n1\nsml\n" +
+                   fmt("%.17g\n", s->sml) + "dt\n" + fmt("%.17g,1e9,1000000000\n", dt) +
+                   "print save plot\n1000000000,1000000000,1000000000\nend\n-1,1,1\n";
+  auto dat_text = [&](double xr, double yt) {
+    // BCs of Normal_BCs (3_SPH_material_2018.f90:1666-1773): var 5 = vx, 6 = vy, 1 = sxx,
+    // 3 = sxy; curve 1 ramps the platen velocity in over t_ramp, curve 2 holds the
+    // confining stress.  The segments lie on the outermost node rows and columns (their
+    // coordinates as generated), which Get_BCs_on_node's exact collinearity test needs.
+    std::string bcs = "BC's\n5 0\nnber var t_variation a1 a0 w fi Tf\n" +
+                      fmt("1 5 1 0 0 0 0 0\n2 6 1 %.17g 0 0 0 0\n3 6 1 %.17g 0 0 0 0\n",
+                          -s->platen_v, s->platen_v) +
+                      fmt("4 1 2 %.17g 0 0 0 0\n5 3 2 0 0 0 0 0\n", -s->confining) +
+                      "segments\n8\nx1 y1 x2 y2 bc\n" +
+                      fmt("0 %.17g %.17g %.17g 1\n0 %.17g %.17g %.17g 2\n", yt, xr, yt, yt, xr,
+                          yt) +
+                      fmt("0 0 %.17g 0 1\n0 0 %.17g 0 3\n", xr, xr) +
+                      fmt("0 0 0 %.17g 4\n0 0 0 %.17g 5\n", yt, yt) +
+                      fmt("%.17g 0 %.17g %.17g 4\n%.17g 0 %.17g %.17g 5\n", xr, xr, yt, xr, xr,
+                          yt);
+    return "1\nbiaxial compression\nndimn\n2\nntype_solid nstre nmats\n2 4 1\n"
+           "mater. eco law E Poiss b rho yield H ? gamma delta n\n" +
+           fmt("1 2 12 %.17g %.17g 1. %.17g 2000. 0 0. 5. 1. 1\n", s->young, s->poiss,
+               s->rho) +
+           "tan(phi) cohesion\n" + fmt("%.17g %.17g 0 0 0 0 0 0\n", tanphi, s->cohesion) +
+           "ic_unks\n0\n" + bcs + "nodes\n0\nic_tcurve\n1\ncurves\n2 100\npts\n3\ntimes\n" +
+           fmt("0 %.17g 1e9\n0 1 1\n", s->t_ramp) + "pts\n2\ntimes\n0 1e9\n1 1\n" +
+           "domain\n-1e6 -1e6 1e6 1e6\nIC\n2\n"
+           "s11\n0\ns22\n0\ns12\n0\ns33\n0\nw1\n0\nv2\n0\n"
+           "pa_sph nnps sle skf cspm update_x XSPH\n2 2 1 1 F T F\n"
+           "summ cont\nF F\ndamping\n0\nalpha beta\n0 0\nic_grav\n0\noutput\n"
+           "sxx syy sxy szz vx vy strain rho sml disp\n1 1 1 1 1 1 1 0 0 0\n";
+  };
+  // the node lattice as generated: its last column and row carry the platen and side BCs
+  sph_problem* P0 = nullptr;
+  int rc = sph_problem_parse(in.c_str(), dat_text(s->width, s->height).c_str(), pts.c_str(),
+                             &P0, nullptr, 0);
+  if (rc) return rc;
+  double xr = 0.0, yt = 0.0;
+  for (int ip = 0; ip < P0->p.nnode; ip++) {
+    xr = std::max(xr, P0->x[2 * (size_t)ip]);
+    yt = std::max(yt, P0->x[2 * (size_t)ip + 1]);
+  }
+  sph_problem_free(P0);
+  sph_problem* P = nullptr;
+  rc = sph_problem_parse(in.c_str(), dat_text(xr, yt).c_str(), pts.c_str(), &P, nullptr, 0);
+  if (rc) return rc;
+  // initial stress (an extension of the reference's zero/constant initial conditions):
+  // confining pressure p on every face plus an axial excess q_ratio * q_y, where q_y is the
+  // axial excess at which the Drucker-Prager function sqrt(J2) + alpha I1 - k_c reaches 0
+  // (sxx = szz = -p, syy = -p - q: sqrt(J2) = q / sqrt(3), I1 = -3p - q)
+  const double root = std::sqrt(9.0 + 12.0 * tanphi * tanphi);
+  const double alpha = tanphi / root, kc = 3.0 * s->cohesion / root;
+  const double qy = (3.0 * alpha * s->confining + kc) / (1.0 / std::sqrt(3.0) - alpha);
+  const double q = s->q_ratio * qy;
+  for (int ip = 0; ip < P->ntotal; ip++) {
+    P->stress[0 + 4 * (size_t)ip] = -s->confining;
+    P->stress[1 + 4 * (size_t)ip] = -s->confining - q;
+    P->stress[2 + 4 * (size_t)ip] = 0.0;
+    P->stress[3 + 4 * (size_t)ip] = -s->confining;
+  }
+  *out = P;
+  return SPS_OK;
+}
+
 int sph_problem_slope(const sph_slope_spec* s, sph_problem** out) {
   if (!s || !out || s->dx <= 0 || s->Lf <= 0 || s->Hf <= 0 || s->Ls < 0 || s->Hs < 0 ||
       s->Ls > s->Lf)

@@ -143,6 +143,12 @@ class SphColumnSpec(C.Structure):
     ]
 
 
+class SphBiaxialSpec(C.Structure):
+    _fields_ = [(k, c_double) for k in ("width", "height", "dx", "sml", "young", "poiss", "rho",
+                                        "phi_deg", "cohesion", "confining", "platen_v",
+                                        "t_ramp", "q_ratio", "dt")]
+
+
 class SphSlopeSpec(C.Structure):
     _fields_ = [
         ("Lf", c_double),

@@ -25,6 +25,7 @@ def host_lib():
                                           C.c_int32]
         lib.sph_problem_column.argtypes = [P(_abi.SphColumnSpec), P(vp)]
         lib.sph_problem_slope.argtypes = [P(_abi.SphSlopeSpec), P(vp)]
+        lib.sph_problem_biaxial.argtypes = [P(_abi.SphBiaxialSpec), P(vp)]
         lib.sph_problem_params.argtypes = [vp]
         lib.sph_problem_params.restype = P(_abi.SpsParams)
         lib.sph_problem_get_arrays.argtypes = [vp, P(_abi.SphProblemArrays)]
@@ -137,6 +138,24 @@ class Problem:
         rc = host_lib().sph_problem_slope(C.byref(spec), C.byref(h))
         if rc:
             raise ValueError("sph_problem_slope failed (%d)" % rc)
+        return cls(h.value)
+
+    @classmethod
+    def biaxial(cls, width=0.05, height=0.10, dx=1e-4, sml=1.2, young=50e6, poiss=0.25,
+                rho=2000.0, phi_deg=35.0, cohesion=0.0, confining=0.0, platen_v=0.05,
+                t_ramp=1e-4, q_ratio=0.0, dt=0.0):
+        """Biaxial compression sample: rough platens top and bottom moving towards each other
+        at platen_v, the side stress BC sxx = -confining, initial stress from the confining
+        value and an axial excess q_ratio of the one that reaches the Drucker-Prager cone.
+        The side BC sets the boundary nodes' stress only (their neighbour sums stay
+        one-sided), so a compressive confining value does not confine; 0 is the traction of
+        the reference's strain-localisation example."""
+        spec = _abi.SphBiaxialSpec(width, height, dx, sml, young, poiss, rho, phi_deg, cohesion,
+                                   confining, platen_v, t_ramp, q_ratio, dt)
+        h = C.c_void_p()
+        rc = host_lib().sph_problem_biaxial(C.byref(spec), C.byref(h))
+        if rc:
+            raise ValueError("sph_problem_biaxial failed (%d)" % rc)
         return cls(h.value)
 
     # ------------------------------------------------------------------ helpers

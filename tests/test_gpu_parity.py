@@ -87,6 +87,14 @@ def test_boundary_conditions(built_gpu):
     _compare(p, 20, chunks=[20])
 
 
+def test_biaxial_platens(built_gpu):
+    # biaxial sample: rough platens driven by ramped segment velocity BCs, side stress BCs,
+    # cohesionless Drucker-Prager (plastic near the platens within the run)
+    p = sps_gb300.Problem.biaxial(dx=0.002, platen_v=0.5, t_ramp=2e-5)
+    f = _compare(p, 40, chunks=[15, 25])
+    assert (f["intvars1"] > 0).any()
+
+
 def test_stress_free_surface(built_gpu):
     # ifsigman = 1: free-surface nodes away from the walls get zero normal and shear
     # traction after every BC application (apply_stress_free)

@@ -143,3 +143,37 @@ def test_slope_generator(built):
     area = 2.0 * 0.5 + 0.45 * 1.0
     assert abs(p.mass[:nn].sum() - 1850.0 * area) < 1e-6 * 1850 * area
     assert abs(p.mass[nn:p.ntotal].sum() - 1850.0 * area) < 1e-6 * 1850 * area
+
+
+def test_biaxial_generator(built):
+    # 0.05 x 0.10 m at 2 mm: 26 x 51 nodes, 25 x 50 stress-points, no dummies
+    p = sps_gb300.Problem.biaxial(dx=0.002, confining=50e3, q_ratio=0.5, phi_deg=35.0,
+                                  cohesion=2e3)
+    assert (p.nnode, p.nstress, p.ntotal2) == (26 * 51, 25 * 50, 26 * 51 + 25 * 50)
+    nn = p.nnode
+    X = p.x.reshape(-1, 2)[:p.ntotal]
+    bi = p.bc_info.reshape(-1, 8)[:p.ntotal]
+    top, bot = X[:, 1] == X[:nn, 1].max(), X[:, 1] == 0.0
+    side = (X[:, 0] == 0.0) | (X[:, 0] == X[:nn, 0].max())
+    # the segments catch exactly the outer node rows and columns (stress-points sit inside)
+    assert np.array_equal(p.bc_or_not[:p.ntotal] == 1, top | bot | side)
+    assert not (top | bot | side)[nn:].any()
+    bcs = lambda m: {frozenset(r[2:2 + r[1]]) for r in bi[m]}
+    assert bcs(top & ~side) == {frozenset({1, 2})} and bcs(bot & ~side) == {frozenset({1, 3})}
+    assert bcs(side & ~top & ~bot) == {frozenset({4, 5})}
+    assert bcs(top & side) == {frozenset({1, 2, 4, 5})}
+    bl = np.asarray(p.params.bc_list[0:40]).reshape(5, 8)
+    # (var, time curve, a1): vx = 0 and vy = -/+ v on the platens, sxx = -p and sxy = 0
+    assert [tuple(r[1:4]) for r in bl] == [(5, 1, 0), (6, 1, -0.05), (6, 1, 0.05),
+                                           (1, 2, -50e3), (3, 2, 0)]
+    # initial stress: half way (in axial excess) from the confining state to the cone
+    st = p.stress.reshape(-1, 4)[:p.ntotal]
+    t = math.tan(math.radians(35.0))
+    root = math.sqrt(9 + 12 * t * t)
+    alpha, kc = t / root, 3 * 2e3 / root
+    s = st[0]
+    mean = (s[0] + s[1] + s[3]) / 3
+    j2 = 0.5 * ((s[0] - mean) ** 2 + (s[1] - mean) ** 2 + (s[3] - mean) ** 2) + s[2] ** 2
+    f = math.sqrt(j2) + alpha * 3 * mean - kc
+    assert abs(f - (-0.5) * (3 * alpha * 50e3 + kc)) < 1e-6 * 50e3
+    assert np.all(st == st[0])
