@@ -301,8 +301,8 @@ def column_batch_problems(n=16, dx=0.001, seed=0):
 def three_arms(args, make, n, net, env, training, dist, local, world):
     """The FP32 form with the surrogate installed, the FP64 plain form and the FP32 form
     alone on the same problem(s): each timed over args.steps graph-launched steps after the
-    warm-up; the first two then advance to args.combined_steps steps in all and their fields
-    are downloaded (one dict per realisation).  make(precision) -> uploaded context."""
+    warm-up; each then advances to args.combined_steps steps in all and its fields are
+    downloaded (one dict per realisation).  make(precision) -> uploaded context."""
     import torch
     from sps_gb300 import _abi
     from sps_gb300 import surrogate as sg
@@ -323,13 +323,12 @@ def three_arms(args, make, n, net, env, training, dist, local, world):
         t, ms, clk = timed_steps(b, args.steps, t if single else None, dist, local)
         arms[name] = {"value": round(n * args.steps * world / (ms * 1e-3), 1),
                       "ms_per_step": round(ms / args.steps, 4), "clocks": clk}
-        if name != "fp32":
-            rest = nlong - max(args.warmup, 1) - args.steps
-            t = b.step(rest, t) if single else b.step(rest)
-            torch.cuda.synchronize()
-            fields[name] = [b.download()] if single else \
-                [b.download(r) for r in range(len(b.problems))]
-            arms[name]["simulated_s"] = t if single else b.times[0]
+        rest = nlong - max(args.warmup, 1) - args.steps
+        t = b.step(rest, t) if single else b.step(rest)
+        torch.cuda.synchronize()
+        fields[name] = [b.download()] if single else \
+            [b.download(r) for r in range(len(b.problems))]
+        arms[name]["simulated_s"] = t if single else b.times[0]
         if use:
             loading, answered, outside, rejected = sg.stats(b)
             lf = max(loading, 1)
@@ -380,14 +379,17 @@ def run_biaxial(args):
 
     arms, fields, surr = three_arms(args, single, n, net, env, training, dist, local, world)
     nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
-    a, b = fields["fp32_surrogate"][0], fields["fp64_plain"][0]
+    b = fields["fp64_plain"][0]
     nt = prob.ntotal
     errors = {"after_steps": nlong, "time_s": arms["fp64_plain"]["simulated_s"],
               "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
-    for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
-                  ("displ", slice(None))):
-        l2, li = rel_errors(a[k][sl], b[k][sl])
-        errors[k + "_rel_l2"], errors[k + "_rel_linf"] = l2, li
+    for arm in ("fp32_surrogate", "fp32"):
+        a, e = fields[arm][0], {}
+        for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
+                      ("displ", slice(None))):
+            l2, li = rel_errors(a[k][sl], b[k][sl])
+            e[k + "_rel_l2"], e[k + "_rel_linf"] = l2, li
+        errors[arm] = e
     errors["plastic_stress_points_plain"] = int((b["intvars1"][prob.nnode:nt] > 0).sum())
     if rank == 0:
         print(json.dumps({
@@ -436,28 +438,30 @@ def run_combined(args):
 
     arms, fields, surr = three_arms(args, batch, n, net, env, training, dist, local, world)
     nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
-    per, pooled = [], {k: [0.0, 0.0] for k in ("stress", "vel", "displ")}
-    for r, p in enumerate(probs):
-        a, b = fields["fp32_surrogate"][r], fields["fp64_plain"][r]
-        nt, nn = p.nnode + p.nstress, p.nnode
-        row = {"phi_deg": round(float(phis[r]), 3)}
-        # runout: the front of the velocity particles (largest x) beyond the column's width
-        fa, fb = float(a["x"][0:2 * nn:2].max()), float(b["x"][0:2 * nn:2].max())
-        row["runout_plain_m"] = fb - COLUMN["width"]
-        row["runout_abs_err_m"] = abs(fa - fb)
-        for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
-                      ("displ", slice(None))):
-            d = a[k][sl] - b[k][sl]
-            pooled[k][0] += float(np.dot(d, d))
-            pooled[k][1] += float(np.dot(b[k][sl], b[k][sl]))
-            row[k + "_rel_l2"] = float(np.linalg.norm(d) / max(np.linalg.norm(b[k][sl]), 1e-300))
-        per.append(row)
     errors = {"after_steps": nlong, "time_s": arms["fp64_plain"]["simulated_s"],
-              "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)",
-              "pooled": {k + "_rel_l2": float(np.sqrt(v[0] / max(v[1], 1e-300)))
-                         for k, v in pooled.items()},
-              "max_runout_abs_err_m": max(r["runout_abs_err_m"] for r in per),
-              "per_column": per}
+              "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
+    for arm in ("fp32_surrogate", "fp32"):
+        per, pooled = [], {k: [0.0, 0.0] for k in ("stress", "vel", "displ")}
+        for r, p in enumerate(probs):
+            a, b = fields[arm][r], fields["fp64_plain"][r]
+            nt, nn = p.nnode + p.nstress, p.nnode
+            row = {"phi_deg": round(float(phis[r]), 3)}
+            # runout: the front of the velocity particles (largest x) beyond the column
+            fa, fb = float(a["x"][0:2 * nn:2].max()), float(b["x"][0:2 * nn:2].max())
+            row["runout_plain_m"] = fb - COLUMN["width"]
+            row["runout_abs_err_m"] = abs(fa - fb)
+            for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
+                          ("displ", slice(None))):
+                d = a[k][sl] - b[k][sl]
+                pooled[k][0] += float(np.dot(d, d))
+                pooled[k][1] += float(np.dot(b[k][sl], b[k][sl]))
+                row[k + "_rel_l2"] = float(np.linalg.norm(d) /
+                                           max(np.linalg.norm(b[k][sl]), 1e-300))
+            per.append(row)
+        errors[arm] = {"pooled": {k + "_rel_l2": float(np.sqrt(v[0] / max(v[1], 1e-300)))
+                                  for k, v in pooled.items()},
+                       "max_runout_abs_err_m": max(r["runout_abs_err_m"] for r in per),
+                       "per_column": per}
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": arms["fp32_surrogate"]["value"],
