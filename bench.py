@@ -497,35 +497,43 @@ def workload_name(prob, dx):
 def kernel_bytes(name, prob, deg, fast=False):
     nn, ns, n2 = prob.nnode, prob.nstress, prob.ntotal2
     ent = 16.0
+    # the node-node list is read by the derivative sums only for artificial viscosity
+    visc = prob.params.alpha > 0 or prob.params.beta > 0
     if fast and name == "derivs":
         # entries + one 16 B record per neighbour-visible particle + per-particle FP64
         # state read/written once (SP: v, s, grad_u, RHS1, RKs, fdp, RKd; node: v, RHS2, RKv)
-        return ent * deg["cross"] + ent * deg["same_nodes"] + 16 * (nn + ns) + \
-            ns * (16 + 32 + 32 + 32 + 64 + 16 + 16) + nn * (16 + 16 + 32 + 16)
+        return ent * deg["cross"] + (ent * deg["same_nodes"] if visc else 0) + \
+            16 * (nn + ns) + ns * (16 + 32 + 32 + 32 + 64 + 16 + 16) + nn * (16 + 16 + 32 + 16)
     if fast and name == "interp":
         return ent * deg["cross"] + 16 * nn + 32 * ns + ns * 16 + nn * 40
     if name == "derivs":
         # entries + SP (v,s,m,rho,grad_u w, RHS1 w, RKs rw, fdp rw, RKd rw) + node terms
         return ent * deg["cross"] + ns * (16 + 32 + 16 + 32 + 32 + 64 + 16 + 16) + \
-            nn * (16 + 32 + 16 + 16 + 32 + 16) + ent * deg["same_nodes"]
+            nn * (16 + 32 + 16 + 16 + 32 + 16) + (ent * deg["same_nodes"] if visc else 0)
     if name == "interp":
         return ent * deg["cross"] + ns * (16 + 16) + nn * (40 + 16 + 16)
     if name == "half":
         return n2 * (4 * 8 + 8) + ent * deg["pairs"]
     if name == "lists":
-        return ent * (deg["cross"] + deg["same"]) * 1.5
+        # entries written (the same-kind lists' only when a step kernel reads them: XSPH,
+        # artificial viscosity or stress), and the creators' half-list entries read,
+        # counted as half an entry per list entry (each pair's entry serves two lists)
+        p = prob.params
+        same_written = p.xsph or p.art_stress or p.alpha > 0 or p.beta > 0
+        return ent * (deg["cross"] + (deg["same"] if same_written else 0)) + \
+            0.5 * ent * (deg["cross"] + deg["same"])
     return None
 
 
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum per launch group) over the
-# algorithmic bytes of kernel_bytes, from one `ncu --set full` capture of the FP32 form on
-# the same slope at dx 0.03 m (321,848 particles, 5.78M pairs; the full-size workload is
-# too large to capture with ~40 passes).  Scaled to a full launch by the algorithmic bytes,
-# which grow with the list entries, as the traffic does.
-NCU_TRAFFIC_RATIO = {"lists": 561745408 / 276326496, "half": 118874368 / 105543208,
-                     "interp": 182772991 / 98788384, "derivs": 214352128 / 184740096}
-NCU_TRAFFIC_SOURCE = ("ncu --set full, FP32 form, slope at dx 0.03 m (5.78M pairs), "
-                      "scaled by algorithmic bytes")
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch group of the FP32
+# form on the full-size slope (dx 0.012 m), from one ncu pass over the first timed stage
+# (profiles/dram_traffic_fp32_slope_2M.md); the neighbour sums' group is the stress-point
+# and the node launch of one stage.  Valid for that workload and this code state only.
+NCU_TRAFFIC_FULL = {"derivs": 337870000 + 22314496 + 429512000 + 40800256,
+                    "interp": 304895000 + 10182656 + 306204000 + 27824384,
+                    "lists": 1154587000 + 665827584, "half": 231094000 + 687190528}
+NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (1 pass), "
+                      "FP32 form, this slope at dx 0.012 m, first timed stage")
 
 
 def timed_steps(ctx, nsteps, t, dist, local, mark=False):
@@ -659,19 +667,28 @@ def run_ours(args):
     per_launch_ms = top_ms / top_n
     peaks, peak_kind = measured_peaks()
     b = kernel_bytes(top, prob, deg, fast)
+    full_size = fast and abs(args.dx - 0.012) < 1e-12
     roof = None
     if b is not None:
         ach = b / (per_launch_ms * 1e-3) / 1e9
-        roof = {"kernel": "k_" + top, "bound": "hbm", "achieved": round(ach, 1),
+        # a profiled region holds the launches of one phase: the neighbour sums launch once
+        # for the stress-point targets and once for the node targets, back to back
+        label = {"derivs": "k_fderivs<1> + k_fderivs<2>" if fast else "k_derivs (both kinds)",
+                 "interp": "k_finterp<1> + k_finterp<2>" if fast else "k_interp (both kinds)"}
+        roof = {"kernel": label.get(top, "k_" + top), "bound": "hbm", "achieved": round(ach, 1),
                 "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": round(ach / peaks.get("hbm_gbs"), 4),
-                "traffic": int(b * NCU_TRAFFIC_RATIO[top]) if fast and top in
-                NCU_TRAFFIC_RATIO else None,
-                "traffic_source": NCU_TRAFFIC_SOURCE if fast and top in NCU_TRAFFIC_RATIO
+                "traffic": NCU_TRAFFIC_FULL[top] if full_size and top in NCU_TRAFFIC_FULL
+                else None,
+                "traffic_source": NCU_TRAFFIC_SOURCE if full_size and top in NCU_TRAFFIC_FULL
                 else None,
                 "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(b),
                 "per_launch_ms": round(per_launch_ms, 4), "launches_per_step": top_n / 2,
+                "launch": "one RK stage's stress-point and node launches together"
+                if top in label else "one launch",
                 "share_of_step": round(top_ms / sum(v[0] for v in prof.values()), 3)}
+    alg_bytes = {k: int(v) for k in prof for v in [kernel_bytes(k, prob, deg, fast)]
+                 if v is not None}
     try:
         f64 = fp64_peak_tflops()
     except Exception:
@@ -761,7 +778,7 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "plain": plain, "error_vs_plain": errors, "surrogate": surr, "batch": batch,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
-            "autotuned_blocks": tuned,
+            "autotuned_blocks": tuned, "algorithmic_bytes_per_launch": alg_bytes,
             "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
             "kernel_ms_per_step": {k: round(v[0] / 2, 4) for k, v in sorted(
                 prof.items(), key=lambda kv: -kv[1][0])},

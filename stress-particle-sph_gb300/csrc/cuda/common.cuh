@@ -140,6 +140,9 @@ struct Dev {
   int outside, npoints, vel_vector;
   double *x10x, *x10y, *disp10;  // velocity-vector variant: x_10(2,nnode), disp_10(nnode)
   int art_stress;      // artificial_force on (input.txt art_stress)
+  int same_entries;    // k_lists writes the same-kind lists' entries only when a step kernel
+                      // reads them (XSPH, artificial viscosity or stress) or with keys;
+                      // their lengths (degS) always
   double* artR;        // its per-node rotated tensile stresses R(3) of the stage, (3, NN)
   double *vol, *rinv;  // m / rho and 1 / rho per particle (refreshed when rho changes)
   double* A[3];        // sigma_k / (rho * rho) of the stage, per particle

@@ -622,7 +622,7 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         int role = same ? (own ? 1 : 0) : (pt == 1 && is_sp(tt) ? 1 : 0);
         int32_t key = (int32_t)(2 * wp + role);
         if (same) {
-          if (nS < D.capS) {
+          if (nS < D.capS && (KEYS || D.same_entries)) {
             D.same[(size_t)nS * D.N2 + col] = e;
             if (KEYS) D.keyS[(size_t)nS * D.N2 + col] = key;
           }
@@ -725,7 +725,7 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         reverse_ell<KEYS>(D.cross, D.keyC, D.N2, col, 0, nC);
         reverse_ell<KEYS>(D.cross, D.keyC, D.N2, col, newC, nC);
       }
-      if (newS > 0) {
+      if (newS > 0 && (KEYS || D.same_entries)) {
         reverse_ell<KEYS>(D.same, D.keyS, D.N2, col, 0, nS);
         reverse_ell<KEYS>(D.same, D.keyS, D.N2, col, newS, nS);
       }

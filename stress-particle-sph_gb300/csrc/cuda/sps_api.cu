@@ -657,6 +657,12 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.RHSh = dalloc<double>(c, NT);
     D.fbx = dalloc<double>(c, NN_);
     D.art_stress = p->art_stress ? 1 : 0;
+    // the same-kind lists (node-node, stress-point-stress-point) are read within a step only
+    // by XSPH, artificial viscosity and artificial stress; the free-surface detection
+    // builds its own lists with walk-order keys, which always carry them
+    D.same_entries = (p->xsph || D.art_stress) ? 1 : 0;
+    for (int r = 0; r < nreal; r++)
+      if (ps[r].alpha > 0 || ps[r].beta > 0) D.same_entries = 1;
     D.outside = p->sp_sph && !p->inside_approach;
     D.npoints = D.outside ? p->npoints : 1;
     D.vel_vector = D.outside && p->vel_vector;
