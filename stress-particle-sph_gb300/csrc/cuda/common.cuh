@@ -183,7 +183,8 @@ struct Dev {
                       // pair count, id
   int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
   int4 *cross, *same;
-  // per-target lists in ELL layout: entry k of the target in list column c at k * N2 + c
+  // per-target lists, entries in pairs: entries 2j and 2j+1 of list column c side by side
+  // at (j * N2 + c) * 2 (ell()), one 32-byte sector; keys flat at k * N2 + c
   int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)
   int32_t *degC, *degS;  // by list column
   // sorted positions of the stress-point and of the node targets (each in sorted order), so
@@ -208,6 +209,14 @@ struct Dev {
   // scan scratch
   int64_t* scan_tmp;
 };
+
+// Index of entry k of list column col in the per-target lists (cross, same).  Entries 2j and
+// 2j+1 of a column share one 32-byte sector, so that the list build, which appends a
+// target's entries one by one, writes whole sectors; the columns of consecutive targets
+// stay adjacent, so a warp reading entry k of its targets still reads one contiguous run.
+__device__ __forceinline__ size_t ell(int k, int col, int N2) {
+  return (((size_t)(k >> 1) * (size_t)N2 + (size_t)col) << 1) | (size_t)(k & 1);
+}
 
 // Correctly rounded a / b given y = RN(1/b), by Markstein's theorem (P. Markstein, "Computation
 // of elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),

@@ -117,7 +117,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       float4 r[kP];
       float vol[kP];
 #pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + col];
+      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
 #pragma unroll
       for (int q = 0; q < kP; q++) {
         r[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -132,7 +132,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
         if (e[q].y >= 0) term(__int_as_float(e[q].y), r[q], vol[q]);
     }
     for (; k < deg; k++) {
-      const int4 e = D.cross[(size_t)k * D.N2 + col];
+      const int4 e = D.cross[ell(k, col, D.N2)];
       if (e.y >= 0) term(__int_as_float(e.y), D.recV[e.x], D.recI[e.x].y);
     }
     double norm = nm.val();
@@ -159,7 +159,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       int4 e[kP];
       float4 rs[kP], ri[kP];
 #pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[(size_t)(k + q) * D.N2 + col];
+      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
 #pragma unroll
       for (int q = 0; q < kP; q++) {
         rs[q] = ri[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -173,7 +173,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
         if (e[q].y >= 0) term(__int_as_float(e[q].y), rs[q], ri[q]);
     }
     for (; k < deg; k++) {
-      const int4 e = D.cross[(size_t)k * D.N2 + col];
+      const int4 e = D.cross[ell(k, col, D.N2)];
       if (e.y >= 0) term(__int_as_float(e.y), D.recS[e.x], D.recI[e.x]);
     }
     double norm = nm.val();
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     const float vh0 = (float)vtx, vh1 = (float)vty;
     const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + col];
+      int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       float Gx = __int_as_float(e.z), Gy = __int_as_float(e.w);
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     // two neighbours a pass: entries and records loaded before either is summed
     int k = 0;
     for (; k + 1 < deg; k += 2) {
-      const int4 ea = D.cross[(size_t)k * D.N2 + col], eb = D.cross[(size_t)(k + 1) * D.N2 + col];
+      const int4 ea = D.cross[ell(k, col, D.N2)], eb = D.cross[ell(k + 1, col, D.N2)];
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       float4 aa = z, la = z, ab = z, lb = z;
       if (ea.y >= 0) {
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       term(eb, ab, lb);
     }
     if (k < deg) {
-      const int4 e = D.cross[(size_t)k * D.N2 + col];
+      const int4 e = D.cross[ell(k, col, D.N2)];
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       term(e, e.y >= 0 ? D.recA[e.x] : z, e.y >= 0 ? D.recAl[e.x] : z);
     }
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
       const float ht = (float)D.hsml[t], rt = (float)D.rho[t];
       for (int k = 0; k < degs; k++) {
-        int4 e = D.same[(size_t)k * D.N2 + col];
+        int4 e = D.same[ell(k, col, D.N2)];
         int u = e.x;
         float4 r = D.recV[u];
         float4 ri = D.recI[u];
@@ -496,7 +496,7 @@ __global__ void k_fxsph(Dev D) {
   int flag = D.bc_or_not[t];
   bool mark = false;
   for (int k = 0; k < deg; k++) {
-    int4 e = D.same[(size_t)k * D.N2 + col];
+    int4 e = D.same[ell(k, col, D.N2)];
     int u = e.x;
     float w = __int_as_float(e.y);
     float4 r = D.recV[u];

@@ -555,15 +555,23 @@ __global__ void k_pair_meta(Dev D) {
   if (threadIdx.x == 0 && D.half_off[D.N2] > 1073741823LL) atomicOr(D.err, ERR_NPAIRS);
 }
 
+// entries 2j and 2j+1 of a list column in one 32-byte store (ell(): one sector, 32-byte
+// aligned), so that no sector of the lists is ever written in halves
+__device__ __forceinline__ void store_pair(int4* dst, int4 a, int4 b) {
+  asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst), "r"(a.x),
+               "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+               : "memory");
+}
+
 template <bool KEYS>
 __device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, int col, int lo,
                                             int hi) {
   // reverse entries [lo, hi) of list column col (and their keys)
   hi--;
   while (lo < hi) {
-    int4 t = base[(size_t)lo * N2 + col];
-    base[(size_t)lo * N2 + col] = base[(size_t)hi * N2 + col];
-    base[(size_t)hi * N2 + col] = t;
+    int4 t = base[ell(lo, col, N2)];
+    base[ell(lo, col, N2)] = base[ell(hi, col, N2)];
+    base[ell(hi, col, N2)] = t;
     if (KEYS) {
       int32_t k = key[(size_t)lo * N2 + col];
       key[(size_t)lo * N2 + col] = key[(size_t)hi * N2 + col];
@@ -581,7 +589,7 @@ __device__ __forceinline__ void reverse_ell(int4* base, int32_t* key, int N2, in
 // order; the lists are written in that walk order.
 // KEYS: also write the walk-order key of every entry (for the free-surface detection)
 template <bool KEYS>
-__device__ __forceinline__ void lists_target(const Dev& D, int s) {
+__device__ __forceinline__ void lists_target(const Dev& D, int s, int4& pendC, int4& pendS) {
   int nC = 0, nS = 0, newC = 0, newS = 0;
   const int col = D.lcol[s];
   if (s < D.gtot->nactive) {
@@ -621,16 +629,20 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
         int64_t wp = !reorder ? rel : isnew ? meta.n - 1 - rel : (meta.n - meta.m_prev) + rel;
         int role = same ? (own ? 1 : 0) : (pt == 1 && is_sp(tt) ? 1 : 0);
         int32_t key = (int32_t)(2 * wp + role);
+        // an even entry waits in pendS / pendC for its odd partner, and the two are stored
+        // together; a last even entry is stored alone after the walk
         if (same) {
           if (nS < D.capS && (KEYS || D.same_entries)) {
-            D.same[(size_t)nS * D.N2 + col] = e;
+            if (nS & 1) store_pair(D.same + ell(nS - 1, col, D.N2), pendS, e);
+            else pendS = e;
             if (KEYS) D.keyS[(size_t)nS * D.N2 + col] = key;
           }
           nS++;
           newS += isnew;
         } else if (pt != 0) {
           if (nC < D.capC) {
-            D.cross[(size_t)nC * D.N2 + col] = e;
+            if (nC & 1) store_pair(D.cross + ell(nC - 1, col, D.N2), pendC, e);
+            else pendC = e;
             if (KEYS) D.keyC[(size_t)nC * D.N2 + col] = key;
           }
           nC++;
@@ -714,6 +726,11 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
                __int_as_float(e.z), __int_as_float(e.w), D.half_off[s] + k, true);
         }
       }
+      {
+        const int wc = min(nC, D.capC), ws = min(nS, D.capS);
+        if (wc & 1) D.cross[ell(wc - 1, col, D.N2)] = pendC;
+        if ((ws & 1) && (KEYS || D.same_entries)) D.same[ell(ws - 1, col, D.N2)] = pendS;
+      }
       if (nC > D.capC || nS > D.capS) {
         atomicOr(D.err, ERR_LIST_CAP);
         nC = min(nC, D.capC);
@@ -735,10 +752,15 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s) {
   D.degS[col] = nS;
 }
 
+// dynamic shared memory: 2 x blockDim int4, the waiting even entries of each thread's two
+// lists (in registers they cost the list build, which waits on its gathers, an eighth of
+// its resident warps)
 template <bool KEYS>
 __global__ void k_lists(Dev D) {
+  extern __shared__ int4 lists_pend[];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < D.N2) lists_target<KEYS>(D, s);
+  if (s < D.N2)
+    lists_target<KEYS>(D, s, lists_pend[threadIdx.x], lists_pend[blockDim.x + threadIdx.x]);
 }
 
 // ------------------------------------------------------------------------ scans
@@ -848,8 +870,9 @@ __global__ void k_target_scatter(Dev D) {
 // per-target lists (k_lists), one thread per sorted position
 void launch_lists(Ctx& c, bool keys) {
   const Dev& D = c.d;
-  if (keys) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, c.stream>>>(D);
-  else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], 0, c.stream>>>(D);
+  const size_t pend = 2 * sizeof(int4) * (size_t)c.blk[TK_LISTS];
+  if (keys) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], pend, c.stream>>>(D);
+  else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], pend, c.stream>>>(D);
 }
 
 int launch_pair_build(Ctx& c) {

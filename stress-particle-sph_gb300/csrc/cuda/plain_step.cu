@@ -142,7 +142,7 @@ __global__ void k_bound(Dev D) {
     const int col = D.lcol[D.spos[i]];
     int deg = D.degC[col];
     for (int k = 0; k < deg; k++) {
-      int u = D.cross[(size_t)k * D.N2 + col].x;
+      int u = D.cross[ell(k, col, D.N2)].x;
       if (u < j0 || u >= j1) continue;
       float fx, fy;
       if (!bound_term(D, M, i, u, fx, fy)) continue;
@@ -267,7 +267,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
   if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     double v0 = 0.0, v1 = 0.0, norm = 0.0;
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + col];
+      int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       if (e.y < 0) continue;  // a dummy partner (sign bit of W)
       double w = (double)__int_as_float(e.y);
@@ -283,7 +283,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
   } else {
     double a = 0.0, b = 0.0, c = 0.0, d = 0.0, iv = 0.0, rt = 0.0, norm = 0.0;
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + col];
+      int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       if (e.y < 0) continue;  // a dummy partner (sign bit of W)
       double w = (double)__int_as_float(e.y);
@@ -500,7 +500,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
     double g[4] = {0.0, 0.0, 0.0, 0.0};  // grad1(a,b) at a + 2b
     const double vt[2] = {D.vx[t], D.vy[t]};
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + col];
+      int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       double Gx = (double)__int_as_float(e.z), Gy = (double)__int_as_float(e.w);
@@ -550,7 +550,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
     const double stt[3] = {D.s0[t], D.s1[t], D.s2[t]};
     int bc_int = 0;
     for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[(size_t)k * D.N2 + col];
+      int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       double dwx = -(double)__int_as_float(e.z), dwy = -(double)__int_as_float(e.w);
@@ -590,7 +590,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
       float ax = 0.0f, ay = 0.0f;
       int degs = D.degS[col];
       for (int k = 0; k < degs; k++) {
-        int4 e = D.same[(size_t)k * D.N2 + col];
+        int4 e = D.same[ell(k, col, D.N2)];
         int u = e.x;
         float xij = (float)(xt - D.px[u]);
         float yij = (float)(yt - D.py[u]);
@@ -687,7 +687,7 @@ __global__ void k_xsph(Dev D) {
   int flag = D.bc_or_not[t];
   bool mark = false;
   for (int k = 0; k < deg; k++) {
-    int4 e = D.same[(size_t)k * D.N2 + col];
+    int4 e = D.same[ell(k, col, D.N2)];
     int u = e.x;
     double w = (double)__int_as_float(e.y);
     double vol = D.vol[u];

@@ -923,8 +923,10 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
       capn = std::min(capn, 65535);  // half-list positions are kept in 16 bits
       if (capn > D.capH || (c.p.max_neighbours > 0 && capn != D.capH)) {
         D.half = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
-        D.cross = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
-        D.same = dalloc<int4>(c, (size_t)D.N2 * (size_t)capn);
+        // the lists hold their entries in pairs (ell()): an even number of rows
+        const size_t rows = (size_t)capn + (capn & 1);
+        D.cross = dalloc<int4>(c, (size_t)D.N2 * rows);
+        D.same = dalloc<int4>(c, (size_t)D.N2 * rows);
         D.keyC = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.keyS = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.capH = D.capC = D.capS = capn;

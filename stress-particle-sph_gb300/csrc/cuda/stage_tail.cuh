@@ -178,7 +178,7 @@ __device__ __forceinline__ void art_force_node(const Dev& D, int col, int t, dou
   double T[3][2] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
   const int degs = D.degS[col];
   for (int k = 0; k < degs; k++) {
-    const int4 e = D.same[(size_t)k * D.N2 + col];
+    const int4 e = D.same[ell(k, col, D.N2)];
     const int u = e.x;
     const double fn = pow((double)__int_as_float(e.y) / w2, n);
     const double mu = D.mass[u];

@@ -30,7 +30,7 @@ __device__ __forceinline__ void walk_123(const Dev& D, int col, F&& f) {
   int4 ea = make_int4(0, 0, 0, 0), eb = make_int4(0, 0, 0, 0);
   auto next_cross = [&]() {
     while (a < nC) {
-      ea = D.cross[(size_t)a * D.N2 + col];
+      ea = D.cross[ell(a, col, D.N2)];
       if (ea.y >= 0) {  // not a dummy partner (sign bit of W)
         ka = D.keyC[(size_t)a * D.N2 + col];
         return;
@@ -40,7 +40,7 @@ __device__ __forceinline__ void walk_123(const Dev& D, int col, F&& f) {
   };
   next_cross();
   if (b < nS) {
-    eb = D.same[(size_t)b * D.N2 + col];
+    eb = D.same[ell(b, col, D.N2)];
     kb = D.keyS[(size_t)b * D.N2 + col];
   }
   while (a < nC || b < nS) {
@@ -57,7 +57,7 @@ __device__ __forceinline__ void walk_123(const Dev& D, int col, F&& f) {
     } else {
       b++;
       if (b < nS) {
-        eb = D.same[(size_t)b * D.N2 + col];
+        eb = D.same[ell(b, col, D.N2)];
         kb = D.keyS[(size_t)b * D.N2 + col];
       }
     }
@@ -156,11 +156,11 @@ __global__ void k_fs_scan(Dev D) {
   const int nS = D.degS[col], nC = D.degC[col];
   const ScanRegion R = scan_region(D, t);
   for (int k = 0; k < nS && !inside; k++) {
-    int u = D.same[(size_t)k * D.N2 + col].x;
+    int u = D.same[ell(k, col, D.N2)].x;
     inside = in_scan_region(R, D.px[u], D.py[u]);
   }
   for (int k = 0; k < nC && !inside; k++) {
-    const int4 e = D.cross[(size_t)k * D.N2 + col];
+    const int4 e = D.cross[ell(k, col, D.N2)];
     if (e.y < 0) inside = in_scan_region(R, D.px[e.x], D.py[e.x]);  // dummy partners
   }
   int sub = inside ? 2 : 1;
