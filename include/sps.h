@@ -160,6 +160,16 @@ int sps_download_surface(sps_ctx* ctx, int32_t r, double* normal, int32_t* subse
 int sps_dump_pairs(sps_ctx* ctx, int32_t* pair_i, int32_t* pair_j, int32_t* pint_type,
                    float* w, float* dwdx, float* dwdy, int64_t* npairs);
 
+/* Which free-surface detection the FP32 form runs when a download or snapshot needs the
+   surface of the last step (no reference counterpart: the reference has one precision).
+   exact = 0 (the default): FP32 arithmetic, lists walked without the walk-order merge, so
+   bc_or_not, subset and normals can differ from get_nodes_on_free_surface
+   (code/3_SPH_material_2018.f90:1135) for particles at the scan region's edge; exact = 1:
+   the reference's rounding and order, as in the FP64 plain form.  A detection that a later
+   step reads (the traction-free BC, XSPH with BCs, the outside approach) is always exact.
+   Takes effect from the next detection; the plain form ignores it. */
+int sps_set_surface_detection(sps_ctx* ctx, int32_t exact);
+
 /* The CUDA stream (a cudaStream_t) every launch of this context is issued on, so that a
    caller can order its own work or record CUDA events against it.  No reference
    counterpart (the reference has no device). */

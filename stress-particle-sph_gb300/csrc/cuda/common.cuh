@@ -199,6 +199,7 @@ struct Dev {
   double *nrmx, *nrmy;
   int8_t* subset;
   float* fint;
+  float* vol32;  // FP32 form: m / rho per particle for the FP32 free-surface detection
   int ifsigman;
   PairMeta* meta;  // per realisation
   // scalars of the current step, per realisation (table: [step][realisation])
@@ -698,7 +699,9 @@ void launch_finterp(Ctx& c);
 void launch_fderivs(Ctx& c, int stage);
 void launch_fsp_tail(Ctx& c, int stage);
 void launch_surface(Ctx& c);
+void launch_surface_f32(Ctx& c);
 void launch_lists_keys(Ctx& c);
+void launch_lists_same(Ctx& c);
 void launch_fxsph(Ctx& c);
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);

@@ -73,8 +73,13 @@ struct Ctx {
   // keys in the step: when the state is downloaded (or snapshotted) with its free surface
   // after every step, the step writes the lists' keys (a few percent of the list build)
   // so that the detection need not rebuild the lists
-  bool keys_in_step = false;   // steps write keys
-  bool keys_written = false;   // the last step wrote them
+  bool keys_in_step = false;   // steps write keys (the FP32 detection: the same-kind entries)
+  bool keys_written = false;   // the last step wrote the keys
+  bool same_written = false;   // the last step wrote the same-kind entries
+  // the on-demand detection of the FP32 form runs in FP32 (launch_surface_f32) unless the
+  // exact one is asked for (sps_set_surface_detection); the plain form's is always exact
+  bool surface_exact = false;
+  bool surface_f32() const { return precision == SPS_PREC_FP32_FAST && !surface_exact; }
   int64_t last_refresh = -1;   // steps_done at the last on-demand detection
   int step_variant = 0;    // the variant launch_*_step enqueues
   int64_t itimestep = 0;   // itimestep_sph of the last step (0 after an upload)

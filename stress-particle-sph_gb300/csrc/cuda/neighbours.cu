@@ -867,9 +867,12 @@ __global__ void k_target_scatter(Dev D) {
   D.lcol[s] = col;
 }
 
-// per-target lists (k_lists), one thread per sorted position
-void launch_lists(Ctx& c, bool keys) {
-  const Dev& D = c.d;
+// per-target lists (k_lists), one thread per sorted position; keys: with the walk-order
+// keys (and the same-kind entries); same: the same-kind entries even when no step kernel
+// reads them (the FP32 free-surface detection does)
+void launch_lists(Ctx& c, bool keys, bool same = false) {
+  Dev D = c.d;
+  if (same) D.same_entries = 1;
   const size_t pend = 2 * sizeof(int4) * (size_t)c.blk[TK_LISTS];
   if (keys) k_lists<true><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], pend, c.stream>>>(D);
   else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], pend, c.stream>>>(D);
@@ -909,12 +912,18 @@ int launch_pair_build(Ctx& c) {
   scan_i32_to_i32(c, D.tflag + D.N2, D.toff + D.N2 + 1, D.N2);
   k_target_scatter<<<nb, kBlock, 0, st>>>(D);
   c.mark("lists");
-  launch_lists(c, c.surf_every || (c.step_variant & 4));
+  // variant bit 2: a download follows most steps; the exact detection wants the keys, the
+  // FP32 detection only the same-kind entries
+  const bool want = (c.step_variant & 4) != 0;
+  launch_lists(c, c.surf_every || (want && !c.surface_f32()), want);
   return 0;
 }
 
 // the lists of the last step again, now with their walk-order keys (the on-demand
 // free-surface detection; the lists are rebuilt identically)
 void launch_lists_keys(Ctx& c) { launch_lists(c, true); }
+
+// the lists of the last step again with the same-kind entries (the FP32 detection)
+void launch_lists_same(Ctx& c) { launch_lists(c, false, true); }
 
 }  // namespace sps

@@ -322,7 +322,8 @@ int variant_of(const sps::Ctx& c, int64_t it) {
 void enqueue_step(sps::Ctx& c) {
   c.itimestep += 1;
   c.step_variant = variant_of(c, c.itimestep) | (c.keys_in_step ? 4 : 0);
-  c.keys_written = c.keys_in_step || c.surf_every;
+  c.keys_written = (c.keys_in_step && !c.surface_f32()) || c.surf_every;
+  c.same_written = c.keys_in_step || c.surf_every || c.d.same_entries;
   if (c.use_graph && !c.profiling) {
     if (!c.graphs[c.step_variant]) build_graph(c);
     SPS_CUDA_CHECK(cudaGraphLaunch(c.graphs[c.step_variant], c.stream));
@@ -635,6 +636,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.nrmy = dalloc<double>(c, NT);
     D.subset = dalloc<int8_t>(c, NT);
     D.fint = dalloc<float>(c, NT);
+    D.vol32 = p->precision == SPS_PREC_FP32_FAST ? dalloc<float>(c, NT) : nullptr;
     D.x0x = dalloc<double>(c, NT);
     D.x0y = dalloc<double>(c, NT);
     D.vx0 = dalloc<double>(c, NT);
@@ -771,8 +773,15 @@ void refresh_surface(sps::Ctx& c, bool sync = true) {
   // detections one or two steps apart: let the following steps write the keys
   c.keys_in_step = c.last_refresh >= 0 && c.steps_done - c.last_refresh <= 2;
   c.last_refresh = c.steps_done;
-  if (!c.keys_written) sps::launch_lists_keys(c);
-  sps::launch_surface(c);
+  if (c.surface_f32()) {
+    // the FP32 detection walks the same-kind lists: the steps wrote them (with or without
+    // keys) or the lists are built again with them
+    if (!c.same_written) sps::launch_lists_same(c);
+    sps::launch_surface_f32(c);
+  } else {
+    if (!c.keys_written) sps::launch_lists_keys(c);
+    sps::launch_surface(c);
+  }
   SPS_CUDA_CHECK(cudaGetLastError());
   if (sync) SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
   c.surf_stale = false;
@@ -1381,6 +1390,22 @@ int sps_selftest_convert(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatch
   return SPS_OK;
 }
 
+int sps_set_surface_detection(sps_ctx* h, int32_t exact) {
+  if (!h || (exact != 0 && exact != 1)) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (c.surface_exact == (exact != 0)) return SPS_OK;
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    c.surface_exact = exact != 0;
+    // the step graphs that write the lists for a download differ between the two
+    c.keys_written = c.same_written = false;
+    drop_graphs(c);
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
 int sps_get_stream(sps_ctx* h, void** stream) {
   if (!h || !stream) return SPS_ERR_ARG;
   *stream = (void*)h->c.stream;
@@ -1528,7 +1553,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     refresh_surface(c);
     const bool stale = c.surf_stale;
     const int64_t it0 = c.itimestep;
-    const bool kin = c.keys_in_step, kw = c.keys_written;
+    const bool kin = c.keys_in_step, kw = c.keys_written, sw = c.same_written;
     const int cand[] = {64, 128, 256, 512};
     int best[sps::TK_N];
     double best_ms[sps::TK_N];
@@ -1561,6 +1586,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     c.itimestep = it0;
     c.keys_in_step = kin;
     c.keys_written = kw;
+    c.same_written = sw;
     SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     cudaFree(snap);

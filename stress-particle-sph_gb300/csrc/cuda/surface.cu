@@ -214,7 +214,149 @@ __global__ void k_fs_normal(Dev D) {
   D.nrmy[t] = ny;
 }
 
+// ---- FP32 detection (the FP32 form's on-demand detection, for output only) -------------
+// The same three steps with the arithmetic in FP32: m/rho per particle, separations from
+// one FP64 subtraction each, FP32 sums.  The node--stress-point and same-type lists are
+// walked one after the other instead of merged by walk-order key (the sums are FP32
+// roundings apart from the exact detection's), and a pair's orientation comes from its
+// type: pair_i is the stress-point of a node--stress-point pair and the creator (the lower
+// sorted position) of a same-type pair, as in the walk-order keys.
+
+__global__ void k_fs_vol32(Dev D) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < D.NT) D.vol32[t] = (float)(D.mass[t] / D.rho[t]);
+}
+
+// f(u, gx, gy, is_same) over the non-dummy cross entries, then the same-type entries
+template <typename F>
+__device__ __forceinline__ void walk_123_f32(const Dev& D, int col, F&& f) {
+  const int nC = D.degC[col], nS = D.degS[col];
+  for (int a = 0; a < nC; a++) {
+    const int4 e = D.cross[ell(a, col, D.N2)];
+    if (e.y >= 0) f(e.x, __int_as_float(e.z), __int_as_float(e.w), false);
+  }
+  for (int b = 0; b < nS; b++) {
+    const int4 e = D.same[ell(b, col, D.N2)];
+    f(e.x, __int_as_float(e.z), __int_as_float(e.w), true);
+  }
+}
+
+__global__ void k_fs_normal0_f32(Dev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int t = D.sorted[s];
+  if (t >= D.NT) return;
+  const double xt = D.px[t], yt = D.py[t];
+  float A0 = 0.0f, A1 = 0.0f, A2 = 0.0f, A3 = 0.0f, f0 = 0.0f, f1 = 0.0f;
+  walk_123_f32(D, D.lcol[s], [&](int u, float gx, float gy, bool) {
+    const float v = D.vol32[u];
+    const float h1 = v * gx, h2 = v * gy;
+    const float dx = f32_rn(D.px[u] - xt), dy = f32_rn(D.py[u] - yt);
+    A0 = fmaf(dx, h1, A0);
+    A1 = fmaf(dy, h1, A1);
+    A2 = fmaf(dx, h2, A2);
+    A3 = fmaf(dy, h2, A3);
+    f0 += h1;
+    f1 += h2;
+  });
+  if (fabsf(A0) <= 1.e-8f) A0 = 0.0f;
+  if (fabsf(A1) <= 1.e-8f) A1 = 0.0f;
+  if (fabsf(A2) <= 1.e-8f) A2 = 0.0f;
+  if (fabsf(A3) <= 1.e-8f) A3 = 0.0f;
+  const float v0 = -(A0 * f0 + A1 * f1);
+  const float v1 = -(A2 * f0 + A3 * f1);
+  const float v2 = sqrtf(v0 * v0 + v1 * v1);
+  D.nrmx[t] = (double)(v0 / v2);
+  D.nrmy[t] = (double)(v1 / v2);
+}
+
+__global__ void k_fs_scan_f32(Dev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int t = D.sorted[s];
+  if (t >= D.NT) return;
+  const int col = D.lcol[s];
+  const int nS = D.degS[col], nC = D.degC[col];
+  const double xa = D.px[t], ya = D.py[t];
+  const float nx = (float)D.nrmx[t], ny = (float)D.nrmy[t], ha = (float)D.hsml[t];
+  const float limit = sqrtf(2.0f) * ha;
+  // T = x_a + h_a n_a relative to x_a, the tangent (-ny, nx)
+  const float T0 = ha * nx, T1 = ha * ny;
+  auto in_region = [&](int u) {
+    const float ddx = f32_rn(D.px[u] - xa), ddy = f32_rn(D.py[u] - ya);
+    const float xba = sqrtf(ddx * ddx + ddy * ddy);
+    const float xbt0 = ddx - T0, xbt1 = ddy - T1;
+    if (xba >= limit) return sqrtf(xbt0 * xbt0 + xbt1 * xbt1) < ha;
+    if (xba < limit) return fabsf(nx * xbt0 + ny * xbt1) + fabsf(-ny * xbt0 + nx * xbt1) < ha;
+    return false;
+  };
+  bool inside = false;
+  for (int k = 0; k < nS && !inside; k++) inside = in_region(D.same[ell(k, col, D.N2)].x);
+  for (int k = 0; k < nC && !inside; k++) {
+    const int4 e = D.cross[ell(k, col, D.N2)];
+    if (e.y < 0) inside = in_region(e.x);  // dummy partners
+  }
+  int sub = inside ? 2 : 1;
+  D.fint[t] = inside ? -1.0f : 0.0f;
+  int bc = D.bc_or_not[t];
+  if (bc != 1) bc = (sub == 1) ? 2 : 0;
+  else if (sub == 1) sub = 2;
+  D.bc_or_not[t] = bc;
+  D.subset[t] = (int8_t)sub;
+}
+
+__global__ void k_fs_normal_f32(Dev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int t = D.sorted[s];
+  if (t >= D.NT) return;
+  const bool surf = D.subset[t] == 1;
+  const bool t_sp = is_sp(D.itype[t]);
+  const float ft = D.fint[t];
+  const double xt = D.px[t], yt = D.py[t];
+  float nx = 0.0f, ny = 0.0f, nb = 0.0f, g0 = 0.0f, g1 = 0.0f;
+  walk_123_f32(D, D.lcol[s], [&](int u, float gx, float gy, bool same) {
+    if (surf && D.subset[u] == 1) {
+      // the reference adds the same vector x_j - x_i to both particles of the pair
+      const bool pair_i = same ? s < D.spos[u] : t_sp;
+      const float xv = f32_rn(pair_i ? D.px[u] - xt : xt - D.px[u]);
+      const float yv = f32_rn(pair_i ? D.py[u] - yt : yt - D.py[u]);
+      nx -= yv;
+      ny += xv;
+      nb += 1.0f;
+    }
+    const float v = D.vol32[u];
+    const float df = D.fint[u] - ft;
+    g0 = fmaf(df, v * gx, g0);
+    g1 = fmaf(df, v * gy, g1);
+  });
+  double dnx = 0.0, dny = 0.0;
+  if (surf) {
+    dnx = (double)nx / (double)nb;
+    dny = (double)ny / (double)nb;
+    const float nv = (float)sqrt(dnx * dnx + dny * dny);
+    dnx = dnx / (double)nv;
+    dny = dny / (double)nv;
+    const float p = (float)((double)g0 * dnx + (double)g1 * dny);
+    if (p < 0) {
+      dnx = -dnx;
+      dny = -dny;
+    }
+  }
+  D.nrmx[t] = dnx;
+  D.nrmy[t] = dny;
+}
+
 }  // namespace
+
+void launch_surface_f32(Ctx& c) {
+  const int nb = (c.d.N2 + kBlock - 1) / kBlock;
+  c.mark("surface", 4);
+  k_fs_vol32<<<(c.d.NT + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);
+  k_fs_normal0_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
+  k_fs_scan_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
+  k_fs_normal_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
+}
 
 void launch_surface(Ctx& c) {
   const int nb = (c.d.N2 + kBlock - 1) / kBlock;

@@ -23,6 +23,7 @@ def gpu_lib():
         lib.sps_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_int32]
         lib.sps_last_error.restype = C.c_int
         lib.sps_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        lib.sps_set_surface_detection.argtypes = [C.c_void_p, C.c_int32]
         lib.sps_kernels_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         lib.sps_selftest_division.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
                                               C.POINTER(C.c_int64)]
@@ -214,6 +215,12 @@ class StepContext:
             self.close()
         except Exception:
             pass
+
+
+def set_surface_detection(ctx, exact):
+    """The FP32 form's on-demand free-surface detection: exact=False (default) in FP32,
+    exact=True with the reference's rounding and order (as the plain form)."""
+    ctx._call("set_surface_detection", ctx._h, 1 if exact else 0)
 
 
 def stream_of(ctx):

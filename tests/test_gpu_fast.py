@@ -117,3 +117,36 @@ def test_fast_bui_like(built_gpu):
 def test_fast_cspm_bcs(built_gpu):
     compare(cases.bc_case(), 60)
     compare(cases.bui_like(width=1.0, height=0.5, dx=0.05, cspm=True, dt=5e-5), 60)
+
+
+@pytest.mark.parametrize("make,nsteps", [(lambda: cases.column(dx=0.004), 30),
+                                         (lambda: cases.bui_like(), 20)],
+                         ids=["column", "bui_like"])
+def test_fast_surface_detection_fp32(built_gpu, make, nsteps):
+    # the FP32 form's on-demand free-surface detection in FP32 against its exact detection
+    # on the same state: nothing in the step reads it here, so every other field is
+    # bit-identical; flags may differ only at the scan region's edge, and the normals of
+    # particles flagged alike agree to FP32 rounding of their sums
+    p = make()
+    out = []
+    for exact in (True, False):
+        ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                    p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+        sps_gb300.set_surface_detection(ctx, exact)
+        ctx.upload_problem(p)
+        t = 0.0
+        for _ in range(nsteps):  # a download after every step, as an output loop does
+            t = ctx.step(1, t)
+            f = ctx.download()
+        out.append((f, ctx.download_surface()))
+    (fe, (ne, se)), (ff, (nf, sf)) = out
+    for k in ("x", "vel", "stress", "rho", "intvars1", "displ", "f_drucker"):
+        np.testing.assert_array_equal(fe[k].view(np.int64), ff[k].view(np.int64), err_msg=k)
+    nt = p.ntotal
+    differ = (fe["bc_or_not"] != ff["bc_or_not"]).sum() + (se != sf).sum()
+    assert differ <= max(2, nt // 2000), differ
+    assert (se == 1).sum() > 0
+    both = (se == 1) & (sf == 1)
+    ne2, nf2 = ne.reshape(-1, 2)[both], nf.reshape(-1, 2)[both]
+    cosang = (ne2 * nf2).sum(axis=1)
+    assert np.all(cosang > 1.0 - 1e-6), cosang.min()
