@@ -529,9 +529,9 @@ def kernel_bytes(name, prob, deg, fast=False):
 # form on the full-size slope (dx 0.012 m), from one ncu pass over the first timed stage
 # (profiles/dram_traffic_fp32_slope_2M.md); the neighbour sums' group is the stress-point
 # and the node launch of one stage.  Valid for that workload and this code state only.
-NCU_TRAFFIC_FULL = {"derivs": 337870000 + 22314496 + 429512000 + 40800256,
-                    "interp": 304895000 + 10182656 + 306204000 + 27824384,
-                    "lists": 1154587000 + 665827584, "half": 231094000 + 687190528}
+NCU_TRAFFIC_FULL = {"derivs": 337758000 + 22606080 + 429369000 + 40654848,
+                    "interp": 304817000 + 10200320 + 306133000 + 27445248,
+                    "lists": 1009711000 + 493658624, "half": 230960000 + 686468352}
 NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (1 pass), "
                       "FP32 form, this slope at dx 0.012 m, first timed stage")
 

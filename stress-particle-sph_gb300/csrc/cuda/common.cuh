@@ -46,6 +46,7 @@ struct dfl {
 struct Grid {
   double xmin[2];
   double deltx[2];
+  double rdeltx[2];  // RN(1 / deltx): the cell index divides by the cell size with div_rcp
   int ndiv[2];
   int ncells;    // cells of this realisation
   int cell0;     // global number of its first cell

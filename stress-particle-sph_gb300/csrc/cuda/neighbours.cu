@@ -184,6 +184,7 @@ __global__ void k_grid(Dev D) {
         double length_new = (double)ndiv * cellsz;
         g.xmin[d] = (xmin - (length_new - length) / 2.0) - (double)0.001f * length;
         g.deltx[d] = cellsz;
+        g.rdeltx[d] = 1.0 / cellsz;
         g.ndiv[d] = ndiv;
         ncd *= ndiv;
       }
@@ -241,10 +242,17 @@ __global__ void k_grid(Dev D) {
   }
 }
 
+// (x - xmin) / deltx of the reference's cell index (2_SPH_main_2018.f90:1280), correctly
+// rounded by div_rcp from the cell size's reciprocal (an IEEE division costs GB300's FP64
+// pipe about ten times as much); non-finite offsets take the IEEE division
+__device__ __forceinline__ double cell_quot(double a, double b, double y) {
+  return isfinite(a) ? div_rcp(a, b, y) : a / b;
+}
+
 // local cell of a position in a realisation's grid
 __device__ __forceinline__ int cell_index(const Grid& g, double x, double y) {
-  double qx = (x - g.xmin[0]) / g.deltx[0] + 1.0;
-  double qy = (y - g.xmin[1]) / g.deltx[1] + 1.0;
+  double qx = cell_quot(x - g.xmin[0], g.deltx[0], g.rdeltx[0]) + 1.0;
+  double qy = cell_quot(y - g.xmin[1], g.deltx[1], g.rdeltx[1]) + 1.0;
   // particles inside the bounding box give 1 <= q < ndiv + 1; the clamps only guard
   // against non-finite coordinates
   int ix = (qx >= 1.0) ? (qx < (double)g.ndiv[0] ? (int)qx : g.ndiv[0]) : 1;
