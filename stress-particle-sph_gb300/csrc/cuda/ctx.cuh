@@ -102,6 +102,10 @@ struct Ctx {
   size_t snap_bytes = 0;
   std::vector<int64_t> snap_roff;  // byte offset of each realisation's block
   cudaStream_t snap_stream = nullptr;
+  // uploads: the host arrays are copied into the staging area on their own stream, which
+  // may run while the previous step computes; the context stream waits for up_ready
+  cudaStream_t up_stream = nullptr;
+  cudaEvent_t up_ready = nullptr;
   cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
   bool snap_pending = false;  // a snapshot was taken and not yet waited for
   bool snap_valid = false;    // snap_host holds a completed snapshot

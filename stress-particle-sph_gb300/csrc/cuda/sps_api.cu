@@ -500,6 +500,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
     c.device = dev;
     SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.up_stream, cudaStreamNonBlocking));
+    SPS_CUDA_CHECK(cudaEventCreateWithFlags(&c.up_ready, cudaEventDisableTiming));
     sps::Dev& D = c.d;
     D.R = nreal;
     D.NN = (int)NN;
@@ -717,7 +719,9 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.cur = dalloc<sps::StepScalars>(c, nreal);
     D.err = dalloc<int>(c, 1);
     D.scan_tmp = dalloc<int64_t>(c, (N2 + 4096) / 4096 + 64);
-    c.stage = dalloc<double>(c, 10 * (size_t)N2);  // x, vel, x00 (2 each) and stress (4)
+    // upload staging: x, vel, x00 (2 each), stress (4), mass, rho, hsml, intvars1,
+    // f_drucker (1 each) as doubles, itype as int32
+    c.stage = dalloc<double>(c, 16 * (size_t)N2);
     c.d_chk = dalloc<unsigned long long>(c, 8);
     SPS_CUDA_CHECK(cudaMemsetAsync(D.meta, 0, sizeof(sps::PairMeta) * nreal, c.stream));
     SPS_CUDA_CHECK(cudaMemsetAsync(D.bbox, 0xff, sizeof(unsigned long long) * 6 * nreal, c.stream));
@@ -812,27 +816,49 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
   Seg sg[3];
   segments(c, r, sg);
   try {
-    // one pass of copies: the interleaved arrays are staged side by side and transposed
-    // segment by segment; the checks and extents are reduced on the device; one sync
+    // every host array is copied into the staging area on the upload stream, which may
+    // run while the previous step still computes (the state it reads is untouched); the
+    // context stream waits for the copies, transposes the interleaved arrays and moves
+    // the others into the state, reduces the checks and extents, and synchronises once
     double* st_x = c.stage;
     double* st_v = st_x + 2 * n2;
     double* st_0 = st_v + 2 * n2;
     double* st_s = st_0 + 2 * n2;
+    double* st_m = st_s + 4 * n2;
+    double* st_r = st_m + n2;
+    double* st_h = st_r + n2;
+    double* st_i = st_h + n2;
+    double* st_f = st_i + n2;
+    int32_t* st_t = reinterpret_cast<int32_t*>(st_f + n2);
     auto nbk = [](int64_t n) { return (int)((n + kBlock - 1) / kBlock); };
-    auto up2 = [&](const double* src, double* st, double* a, double* b) {
-      SPS_CUDA_CHECK(cudaMemcpyAsync(st, src, sizeof(double) * 2 * n2, cudaMemcpyHostToDevice, c.stream));
+    auto h2d = [&](void* dst, const void* src, size_t bytes) {
+      if (bytes) SPS_CUDA_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c.up_stream));
+    };
+    h2d(st_x, x, sizeof(double) * 2 * n2);
+    h2d(st_v, vel, sizeof(double) * 2 * n2);
+    h2d(st_0, x00 ? x00 : x, sizeof(double) * 2 * n2);
+    h2d(st_s, stress, sizeof(double) * 4 * n2);
+    h2d(st_m, mass, sizeof(double) * n2);
+    h2d(st_r, rho, sizeof(double) * n2);
+    h2d(st_h, hsml, sizeof(double) * n2);
+    h2d(st_t, itype, sizeof(int32_t) * n2);
+    if (intvars1) h2d(st_i, intvars1, sizeof(double) * nt);
+    if (f_drucker) h2d(st_f, f_drucker, sizeof(double) * nt);
+    SPS_CUDA_CHECK(cudaEventRecord(c.up_ready, c.up_stream));
+    SPS_CUDA_CHECK(cudaStreamWaitEvent(c.stream, c.up_ready, 0));
+    auto soa2 = [&](double* st, double* a, double* b) {
       for (const Seg& q : sg)
         if (q.n > 0)
           k_aos_to_soa2<<<nbk(q.n), kBlock, 0, c.stream>>>(st + 2 * q.l, a + q.g, b + q.g, (int)q.n);
     };
-    auto up1 = [&](void* dst, const void* src, size_t esz, int nseg) {
+    auto d2d = [&](void* dst, const void* src, size_t esz, int nseg) {
       for (int k = 0; k < nseg; k++)
         if (sg[k].n > 0)
           SPS_CUDA_CHECK(cudaMemcpyAsync((char*)dst + esz * sg[k].g, (const char*)src + esz * sg[k].l,
-                                         esz * sg[k].n, cudaMemcpyHostToDevice, c.stream));
+                                         esz * sg[k].n, cudaMemcpyDeviceToDevice, c.stream));
     };
-    up2(x, st_x, D.px, D.py);
-    up2(vel, st_v, D.vx, D.vy);
+    soa2(st_x, D.px, D.py);
+    soa2(st_v, D.vx, D.vy);
     if (D.vel_vector && nn > 0) {  // Setup_Global_Arrays (3_SPH_material_2018.f90:1032)
       SPS_CUDA_CHECK(cudaMemcpyAsync(D.x10x + M.node0, D.px + M.node0, sizeof(double) * nn,
                                      cudaMemcpyDeviceToDevice, c.stream));
@@ -840,25 +866,24 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
                                      cudaMemcpyDeviceToDevice, c.stream));
       SPS_CUDA_CHECK(cudaMemsetAsync(D.disp10 + M.node0, 0, sizeof(double) * nn, c.stream));
     }
-    up2(x00 ? x00 : x, st_0, D.x00x, D.x00y);
-    SPS_CUDA_CHECK(cudaMemcpyAsync(st_s, stress, sizeof(double) * 4 * n2, cudaMemcpyHostToDevice, c.stream));
+    soa2(st_0, D.x00x, D.x00y);
     for (const Seg& q : sg)
       if (q.n > 0)
         k_aos_to_soa4<<<nbk(q.n), kBlock, 0, c.stream>>>(st_s + 4 * q.l, D.s0 + q.g, D.s1 + q.g,
                                                           D.s2 + q.g, D.s3 + q.g, (int)q.n);
-    up1(D.mass, mass, sizeof(double), 3);
-    up1(D.rho, rho, sizeof(double), 3);
-    up1(D.hsml, hsml, sizeof(double), 3);
-    up1(D.itype, itype, sizeof(int32_t), 3);
+    d2d(D.mass, st_m, sizeof(double), 3);
+    d2d(D.rho, st_r, sizeof(double), 3);
+    d2d(D.hsml, st_h, sizeof(double), 3);
+    d2d(D.itype, st_t, sizeof(int32_t), 3);
     for (int k = 0; k < 2; k++) {  // nodes and stress-points
       const Seg& q = sg[k];
       if (q.n == 0) continue;
       if (intvars1)
-        SPS_CUDA_CHECK(cudaMemcpyAsync(D.iv1 + q.g, intvars1 + q.l, sizeof(double) * q.n, cudaMemcpyHostToDevice, c.stream));
+        SPS_CUDA_CHECK(cudaMemcpyAsync(D.iv1 + q.g, st_i + q.l, sizeof(double) * q.n, cudaMemcpyDeviceToDevice, c.stream));
       else
         SPS_CUDA_CHECK(cudaMemsetAsync(D.iv1 + q.g, 0, sizeof(double) * q.n, c.stream));
       if (f_drucker)
-        SPS_CUDA_CHECK(cudaMemcpyAsync(D.fdp + q.g, f_drucker + q.l, sizeof(double) * q.n, cudaMemcpyHostToDevice, c.stream));
+        SPS_CUDA_CHECK(cudaMemcpyAsync(D.fdp + q.g, st_f + q.l, sizeof(double) * q.n, cudaMemcpyDeviceToDevice, c.stream));
       else
         SPS_CUDA_CHECK(cudaMemsetAsync(D.fdp + q.g, 0, sizeof(double) * q.n, c.stream));
     }
@@ -1630,6 +1655,8 @@ void sps_destroy(sps_ctx* h) {
   if (c.snap_done) cudaEventDestroy(c.snap_done);
   if (c.snap_dev) cudaFree(c.snap_dev);
   if (c.snap_host) cudaFreeHost(c.snap_host);
+  if (c.up_stream) cudaStreamDestroy(c.up_stream);
+  if (c.up_ready) cudaEventDestroy(c.up_ready);
   if (c.stream) cudaStreamDestroy(c.stream);
   delete h;
 }
