@@ -193,9 +193,21 @@ int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismat
    kernels, XSPH) at block sizes 64, 128, 256 and 512 over nsteps profiled steps of the
    uploaded state, keep the fastest size per kernel, and restore the state, so the results
    of later steps are the same as without tuning.  blocks (may be NULL) receives the 8
-   chosen sizes in that order.  The cell size is not tuned: the reference's pair order
-   depends on it. */
+   chosen sizes in that order.  The FP32 form then tunes its neighbour sums' look-ahead
+   the same way (sps_tuned_lookahead).  The cell size is not tuned: the reference's pair
+   order depends on it. */
 int sps_autotune(sps_ctx* ctx, int32_t nsteps, int32_t* blocks);
+
+/* The look-ahead of the FP32 form's neighbour sums that sps_autotune chose after the
+   block sizes (no reference counterpart): ahead[0] neighbours a pass in the interpolation
+   (2, 4 or 8), ahead[1] in the node derivative sums (1, 2 or 4); a pass loads its
+   neighbours' list entries and records before it sums any of them, in the same order, so
+   the results do not depend on these.  Defaults before tuning: 4 and 2. */
+int sps_tuned_lookahead(sps_ctx* ctx, int32_t* ahead);
+
+/* Sets that look-ahead directly (interp 2, 4 or 8; derivs 1, 2 or 4), e.g. to reuse the
+   values tuned on one context in another of the same workload. */
+int sps_set_lookahead(sps_ctx* ctx, int32_t interp, int32_t derivs);
 
 /* Number of this library's kernels one step launches (no reference counterpart). */
 int sps_kernels_per_step(sps_ctx* ctx, int32_t* n);

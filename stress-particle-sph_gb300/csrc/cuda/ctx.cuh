@@ -84,6 +84,10 @@ struct Ctx {
   int step_variant = 0;    // the variant launch_*_step enqueues
   int64_t itimestep = 0;   // itimestep_sph of the last step (0 after an upload)
   bool use_graph = true;
+  // FP32 form: neighbours a pass of the interpolation (2, 4, 8) and of the node derivative
+  // sums (1, 2, 4), whose entries and records are loaded before any is summed; chosen by
+  // sps_autotune (results do not depend on them)
+  int ahead[2] = {4, 2};
   // scratch for scans
   int scan_blocks = 0;
   // per-kernel event timing (sps_profile_step)

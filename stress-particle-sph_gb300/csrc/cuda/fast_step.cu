@@ -62,7 +62,9 @@ __device__ __forceinline__ float dfdiff(float ah, float al, float bh, float bl) 
 // plus the weighted mean of the deviations, which are small and exact in double-float.
 // KIND 0: every particle (sorted positions); 1: the stress-point targets tgt[0..n); 2: the
 // node targets (no divergence between the two branches inside a warp)
-template <int KIND>
+// KP: neighbours a pass whose entries and records are loaded before any is summed (the
+// autotuner's look-ahead; the sum order, and so the result, does not depend on it)
+template <int KIND, int KP>
 __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   int s;
@@ -110,7 +112,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     };
     // kP neighbours a pass: their entries and records are loaded before any is summed, so
     // that the loads overlap (the sum order is unchanged)
-    constexpr int kP = 4;
+    constexpr int kP = KP;
     int k = 0;
     for (; k + kP - 1 < deg; k += kP) {
       int4 e[kP];
@@ -153,7 +155,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
     };
-    constexpr int kP = 4;  // neighbours a pass, as above
+    constexpr int kP = KP;  // neighbours a pass, as above
     int k = 0;
     for (; k + kP - 1 < deg; k += kP) {
       int4 e[kP];
@@ -197,7 +199,8 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
 // A = sigma / rho^2.  The first sum has small terms (double-float differences); the second
 // is a sum of exact products.  This keeps the near-cancelling stress divergence accurate.
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets
-template <int KIND>
+// KP: neighbours a pass, loaded before any is summed (as in k_finterp)
+template <int KIND, int KP>
 __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int stage,
                                                     const int32_t* __restrict__ tgt, int ntgt) {
   const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -217,14 +220,11 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     const double vtx = D.vx[t], vty = D.vy[t];
     const float vh0 = (float)vtx, vh1 = (float)vty;
     const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
-    for (int k = 0; k < deg; k++) {
-      int4 e = D.cross[ell(k, col, D.N2)];
-      int u = e.x;
+    auto term = [&](const int4& e, float vol, float4 r) {
+      const int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
       float Gx = __int_as_float(e.z), Gy = __int_as_float(e.w);
-      float vol = D.recI[u].y;
       if (!wall) {
-        float4 r = D.recV[u];
         float h1 = Gx * vol, h2 = Gy * vol;
         float du0 = dfdiff(r.x, r.z, vh0, vl0), du1 = dfdiff(r.y, r.w, vh1, vl1);
         g0.add(du0 * h1);
@@ -257,6 +257,26 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         g1.add(du1 * hh1);
         g3.add(du1 * hh2);
       }
+    };
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    int k = 0;
+    for (; k + KP - 1 < deg; k += KP) {
+      int4 e[KP];
+      float vol[KP];
+      float4 r[KP];
+#pragma unroll
+      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
+#pragma unroll
+      for (int q = 0; q < KP; q++) {
+        vol[q] = D.recI[e[q].x].y;
+        r[q] = e[q].y >= 0 ? D.recV[e[q].x] : z;
+      }
+#pragma unroll
+      for (int q = 0; q < KP; q++) term(e[q], vol[q], r[q]);
+    }
+    for (; k < deg; k++) {
+      const int4 e = D.cross[ell(k, col, D.N2)];
+      term(e, D.recI[e.x].y, e.y >= 0 ? D.recV[e.x] : z);
     }
     double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
     double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
@@ -306,24 +326,26 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       sx.add(m, dwx);
       sy.add(m, dwy);
     };
-    // two neighbours a pass: entries and records loaded before either is summed
+    // KP neighbours a pass: entries and records loaded before any is summed
     int k = 0;
-    for (; k + 1 < deg; k += 2) {
-      const int4 ea = D.cross[ell(k, col, D.N2)], eb = D.cross[ell(k + 1, col, D.N2)];
+    for (; k + KP - 1 < deg; k += KP) {
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      float4 aa = z, la = z, ab = z, lb = z;
-      if (ea.y >= 0) {
-        aa = D.recA[ea.x];
-        la = D.recAl[ea.x];
+      int4 e[KP];
+      float4 a[KP], l[KP];
+#pragma unroll
+      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
+#pragma unroll
+      for (int q = 0; q < KP; q++) {
+        a[q] = l[q] = z;
+        if (e[q].y >= 0) {
+          a[q] = D.recA[e[q].x];
+          l[q] = D.recAl[e[q].x];
+        }
       }
-      if (eb.y >= 0) {
-        ab = D.recA[eb.x];
-        lb = D.recAl[eb.x];
-      }
-      term(ea, aa, la);
-      term(eb, ab, lb);
+#pragma unroll
+      for (int q = 0; q < KP; q++) term(e[q], a[q], l[q]);
     }
-    if (k < deg) {
+    for (; k < deg; k++) {
       const int4 e = D.cross[ell(k, col, D.N2)];
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       term(e, e.y >= 0 ? D.recA[e.x] : z, e.y >= 0 ? D.recAl[e.x] : z);
@@ -515,23 +537,41 @@ __global__ void k_fxsph(Dev D) {
 }  // namespace
 
 // the targets split by kind (k_split_targets) after the pair build; one launch per kind
-void launch_finterp(Ctx& c) {
+template <int KP>
+void launch_finterp_kp(Ctx& c) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_INTERP];
+  c.kernels_launched += 1;
+  if (ns > 0) k_finterp<1, KP><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, D.tgtS, ns);
+  k_finterp<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, D.tgtN, D.NN);
+}
+void launch_finterp(Ctx& c) {
+  const Dev& D = c.d;
   if (!D.sp_sph) {
-    k_finterp<0><<<c.grid_of(TK_INTERP, D.N2), b, 0, c.stream>>>(D, nullptr, 0);
+    k_finterp<0, 4><<<c.grid_of(TK_INTERP, D.N2), c.blk[TK_INTERP], 0, c.stream>>>(D, nullptr, 0);
     return;
   }
-  c.kernels_launched += 1;
-  if (ns > 0) k_finterp<1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, D.tgtS, ns);
-  k_finterp<2><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, D.tgtN, D.NN);
+  switch (c.ahead[0]) {
+    case 2: launch_finterp_kp<2>(c); break;
+    case 8: launch_finterp_kp<8>(c); break;
+    default: launch_finterp_kp<4>(c);
+  }
 }
-void launch_fderivs(Ctx& c, int stage) {
+template <int KP>
+void launch_fderivs_kp(Ctx& c, int stage) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_DERIVS];
   c.kernels_launched += 1;
-  if (ns > 0) k_fderivs<1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
-  k_fderivs<2><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
+  // the stress-point sums (64 registers) load one neighbour ahead; more spill
+  if (ns > 0) k_fderivs<1, 1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
+  k_fderivs<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
+}
+void launch_fderivs(Ctx& c, int stage) {
+  switch (c.ahead[1]) {
+    case 1: launch_fderivs_kp<1>(c, stage); break;
+    case 4: launch_fderivs_kp<4>(c, stage); break;
+    default: launch_fderivs_kp<2>(c, stage);
+  }
 }
 void launch_fsp_tail(Ctx& c, int stage) {
   int ns = c.d.NT - c.d.NN;

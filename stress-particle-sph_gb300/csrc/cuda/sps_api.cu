@@ -1431,6 +1431,29 @@ int sps_set_surface_detection(sps_ctx* h, int32_t exact) {
   return SPS_OK;
 }
 
+int sps_tuned_lookahead(sps_ctx* h, int32_t* ahead) {
+  if (!h || !ahead) return SPS_ERR_ARG;
+  ahead[0] = h->c.ahead[0];
+  ahead[1] = h->c.ahead[1];
+  return SPS_OK;
+}
+
+int sps_set_lookahead(sps_ctx* h, int32_t interp, int32_t derivs) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if ((interp != 2 && interp != 4 && interp != 8) || (derivs != 1 && derivs != 2 && derivs != 4))
+    return fail(&c, SPS_ERR_ARG, "sps_set_lookahead: interp 2, 4 or 8; derivs 1, 2 or 4");
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    c.ahead[0] = interp;
+    c.ahead[1] = derivs;
+    drop_graphs(c);
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
 int sps_get_stream(sps_ctx* h, void** stream) {
   if (!h || !stream) return SPS_ERR_ARG;
   *stream = (void*)h->c.stream;
@@ -1606,6 +1629,33 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     for (int k = 0; k < sps::TK_N; k++) {
       c.blk[k] = best[k];
       if (blocks) blocks[k] = best[k];
+    }
+    // FP32 form: the neighbour sums' look-ahead (neighbours loaded before any is summed),
+    // at the chosen block sizes; the two groups are timed in the same profiled steps
+    if (c.precision == SPS_PREC_FP32_FAST && c.d.sp_sph) {
+      const int la[3][2] = {{2, 1}, {4, 2}, {8, 4}};
+      int best_la[2] = {c.ahead[0], c.ahead[1]};
+      double best_la_ms[2] = {1e300, 1e300};
+      const char* names[2] = {"interp", "derivs"};
+      for (const auto& v : la) {
+        c.ahead[0] = v[0];
+        c.ahead[1] = v[1];
+        std::vector<std::string> kn;
+        std::vector<double> kms;
+        std::vector<int> kl;
+        std::fill(t.begin(), t.end(), 0.0);
+        c.itimestep = it0;
+        profile_run(c, nsteps, t.data(), kn, kms, kl);
+        copy(false);
+        for (int g = 0; g < 2; g++)
+          for (size_t q = 0; q < kn.size(); q++)
+            if (kn[q] == names[g] && kms[q] < best_la_ms[g]) {
+              best_la_ms[g] = kms[q];
+              best_la[g] = v[g];
+            }
+      }
+      c.ahead[0] = best_la[0];
+      c.ahead[1] = best_la[1];
     }
     c.surf_stale = stale;
     c.itimestep = it0;

@@ -24,6 +24,8 @@ def gpu_lib():
         lib.sps_last_error.restype = C.c_int
         lib.sps_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         lib.sps_set_surface_detection.argtypes = [C.c_void_p, C.c_int32]
+        lib.sps_tuned_lookahead.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        lib.sps_set_lookahead.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         lib.sps_kernels_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         lib.sps_selftest_division.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
                                               C.POINTER(C.c_int64)]
@@ -253,6 +255,18 @@ def autotune(ctx, nsteps=2):
     b = (C.c_int32 * len(TUNED_KERNELS))()
     ctx._call("autotune", ctx._h, int(nsteps), b)
     return dict(zip(TUNED_KERNELS, list(b)))
+
+
+def lookahead(ctx):
+    """The FP32 neighbour sums' look-ahead: {"interp": n, "derivs": n} (sps_tuned_lookahead)."""
+    a = (C.c_int32 * 2)()
+    ctx._call("tuned_lookahead", ctx._h, a)
+    return {"interp": a[0], "derivs": a[1]}
+
+
+def set_lookahead(ctx, interp, derivs):
+    """sps_set_lookahead: neighbours a pass of the interpolation and node derivative sums."""
+    ctx._call("set_lookahead", ctx._h, int(interp), int(derivs))
 
 
 def kernels_per_step(ctx):

@@ -55,3 +55,31 @@ def test_tuned_batch_equals_untuned(built_gpu):
     for r in range(len(probs)):
         for k in FIELDS:
             np.testing.assert_array_equal(res[0][r][k], res[1][r][k], err_msg="%d %s" % (r, k))
+
+
+def test_lookahead_changes_nothing(built_gpu):
+    # the FP32 neighbour sums load 1-8 neighbours before summing any, in the same order:
+    # every look-ahead gives the same bits, so the autotuner may choose any
+    p = cases.bui_like()
+    res = []
+    for interp, derivs in ((4, 2), (2, 1), (8, 4)):
+        ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                    p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+        sps_gb300.set_lookahead(ctx, interp, derivs)
+        assert sps_gb300.lookahead(ctx) == {"interp": interp, "derivs": derivs}
+        ctx.upload_problem(p)
+        ctx.step(10, 0.0)
+        res.append(ctx.download())
+        ctx.close()
+    for r in res[1:]:
+        for k in FIELDS:
+            np.testing.assert_array_equal(r[k], res[0][k], err_msg=k)
+    ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+    ctx.upload_problem(p)
+    sps_gb300.autotune(ctx, 2)
+    la = sps_gb300.lookahead(ctx)
+    assert la["interp"] in (2, 4, 8) and la["derivs"] in (1, 2, 4), la
+    with pytest.raises(sps_gb300.SpsError):
+        sps_gb300.set_lookahead(ctx, 3, 2)
+    ctx.close()
