@@ -421,6 +421,9 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   float x[16];
   double scale = 0.0;
   bool loading = false, cand = false;
+  // drucker_prager's results (G, vivel, f), handed to the tail, which would repeat them
+  double dp[9];
+  bool have_dp = false;
   if (SURR && act && M.ntype_eco > 1 && M.ncrit == 12) {
     const double* gu = D.grad_u + 4 * (size_t)t;
     for (int k = 0; k < 4; k++) g[k] = gu[k];
@@ -430,8 +433,14 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     s2v[3] = D.s3[t];
     if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
     double f = D.fdp[t], G2[4], vivel[4];
-    drucker_prager<true>(M, sc.time_sph, s2v, g, &f, G2, vivel);  // loading test only
+    drucker_prager<true>(M, sc.time_sph, s2v, g, &f, G2, vivel);  // the exact rule
     loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
+    for (int k = 0; k < 4; k++) {
+      dp[k] = G2[k];
+      dp[4 + k] = vivel[k];
+    }
+    dp[8] = f;
+    have_dp = true;
     if (loading) {
       scale = mlp_features(s2v, g, M.tanfi, M.coh, M.young, M.poiss, D.rho[t], x);
       cand = scale > 0.0;
@@ -496,9 +505,10 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     double v0 = -Gnet[0] / (2.0 * gm), v1 = -Gnet[1] / (2.0 * gm), v2 = -Gnet[2] / gm,
            v3 = -Gnet[3] / (2.0 * gm);
     double der = sqrt((2.0 * ((v0 * v0 + v1 * v1) + v3 * v3) + v2 * v2) / 3.0);
-    tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, Gnet, der);
+    tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, Gnet, der, have_dp ? dp : nullptr);
   } else {
-    tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2);
+    tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, nullptr, 0.0,
+                        have_dp ? dp : nullptr);
   }
 }
 

@@ -92,11 +92,14 @@ __device__ __forceinline__ void tail_sp_grad(const Dev& D, int t, double* g, con
 // learned surrogate that replaces the exact one (with its plastic strain rate der_net)
 // FAST (the FP32 form): the mean of drucker_prager by a product, the plastic strain-rate
 // norm in FP32.
+// dp (FP32 form with the surrogate): drucker_prager's results for this stress-point,
+// already evaluated on the same inputs by the caller: G (4), vivel (4), the updated f
 template <bool FAST = false>
 __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& sc, int t,
                                               const double* g, double f2,
                                               const double* Gs_net = nullptr,
-                                              double der_net = 0.0) {
+                                              double der_net = 0.0,
+                                              const double* dp = nullptr) {
     const Real& M = real_of(D, t);
     const double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
     double div1[4];
@@ -114,8 +117,17 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
       if (M.ncrit <= 4) {
         viscoplastic(M, s2v, D.iv1[t], vivel, Gs);
       } else if (M.ncrit == 12) {
-        double f = D.fdp[t];
-        drucker_prager<FAST>(M, sc.time_sph, s2v, g, &f, G2, vivel);
+        double f;
+        if (dp) {
+          for (int k = 0; k < 4; k++) {
+            G2[k] = dp[k];
+            vivel[k] = dp[4 + k];
+          }
+          f = dp[8];
+        } else {
+          f = D.fdp[t];
+          drucker_prager<FAST>(M, sc.time_sph, s2v, g, &f, G2, vivel);
+        }
         D.fdp[t] = f;
         for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
         if (D.cap_buf && (G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0))
