@@ -241,14 +241,18 @@ __device__ __forceinline__ void walk_123_f32(const Dev& D, int col, F&& f) {
   }
 }
 
-__global__ void k_fs_normal0_f32(Dev D) {
+// steps 1-3 for one particle: its first normal from the kernel-gradient sums, then, with
+// that normal (the scan region needs the particle's own normal only), whether a neighbour
+// lies in its scan region
+__global__ void k_fs_normal_scan_f32(Dev D) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
   const int t = D.sorted[s];
   if (t >= D.NT) return;
+  const int col = D.lcol[s];
   const double xt = D.px[t], yt = D.py[t];
   float A0 = 0.0f, A1 = 0.0f, A2 = 0.0f, A3 = 0.0f, f0 = 0.0f, f1 = 0.0f;
-  walk_123_f32(D, D.lcol[s], [&](int u, float gx, float gy, bool) {
+  walk_123_f32(D, col, [&](int u, float gx, float gy, bool) {
     const float v = D.vol32[u];
     const float h1 = v * gx, h2 = v * gy;
     const float dx = f32_rn(D.px[u] - xt), dy = f32_rn(D.py[u] - yt);
@@ -266,24 +270,17 @@ __global__ void k_fs_normal0_f32(Dev D) {
   const float v0 = -(A0 * f0 + A1 * f1);
   const float v1 = -(A2 * f0 + A3 * f1);
   const float v2 = sqrtf(v0 * v0 + v1 * v1);
-  D.nrmx[t] = (double)(v0 / v2);
-  D.nrmy[t] = (double)(v1 / v2);
-}
-
-__global__ void k_fs_scan_f32(Dev D) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
-  const int t = D.sorted[s];
-  if (t >= D.NT) return;
-  const int col = D.lcol[s];
+  const float nx = v0 / v2, ny = v1 / v2;
+  D.nrmx[t] = (double)nx;
+  D.nrmy[t] = (double)ny;
+  // step 3: the scan region of t
   const int nS = D.degS[col], nC = D.degC[col];
-  const double xa = D.px[t], ya = D.py[t];
-  const float nx = (float)D.nrmx[t], ny = (float)D.nrmy[t], ha = (float)D.hsml[t];
+  const float ha = (float)D.hsml[t];
   const float limit = sqrtf(2.0f) * ha;
-  // T = x_a + h_a n_a relative to x_a, the tangent (-ny, nx)
+  // T = x_t + h_t n_t relative to x_t, the tangent (-ny, nx)
   const float T0 = ha * nx, T1 = ha * ny;
   auto in_region = [&](int u) {
-    const float ddx = f32_rn(D.px[u] - xa), ddy = f32_rn(D.py[u] - ya);
+    const float ddx = f32_rn(D.px[u] - xt), ddy = f32_rn(D.py[u] - yt);
     const float xba = sqrtf(ddx * ddx + ddy * ddy);
     const float xbt0 = ddx - T0, xbt1 = ddy - T1;
     if (xba >= limit) return sqrtf(xbt0 * xbt0 + xbt1 * xbt1) < ha;
@@ -351,10 +348,9 @@ __global__ void k_fs_normal_f32(Dev D) {
 
 void launch_surface_f32(Ctx& c) {
   const int nb = (c.d.N2 + kBlock - 1) / kBlock;
-  c.mark("surface", 4);
+  c.mark("surface", 3);
   k_fs_vol32<<<(c.d.NT + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(c.d);
-  k_fs_normal0_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
-  k_fs_scan_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
+  k_fs_normal_scan_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
   k_fs_normal_f32<<<nb, kBlock, 0, c.stream>>>(c.d);
 }
 
