@@ -246,21 +246,42 @@ def batch_problems(n=256, seed=0):
     return out
 
 
+def shard(probs, dist):
+    """This rank's share of a batch of realisations (partitioned by particle count, no
+    exchange between ranks) and their indices; the whole batch on one rank."""
+    import sps_gb300
+    if dist is None:
+        return probs, list(range(len(probs)))
+    mine = sps_gb300.partition_by_size([p.nnode + p.nstress for p in probs],
+                                       dist.get_world_size())[dist.get_rank()]
+    return [probs[i] for i in mine], mine
+
+
+def reduce_sum(dist, v, device=None):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def run_batch(args, dist, local):
-    """The batched-realisations workload: one FP32 context holding every slope."""
+    """The batched-realisations workload: one FP32 context holding every slope (under
+    torchrun, this rank's share of them)."""
     import numpy as np
     import sps_gb300
     from sps_gb300 import _abi
     w0 = time.perf_counter()
-    probs = batch_problems(args.batch_size)
+    probs, _ = shard(batch_problems(args.batch_size), dist)
     b = sps_gb300.Batch(probs, precision=_abi.SPS_PREC_FP32_FAST)
     b.upload_all()
     tuned = sps_gb300.autotune(b, 2)
     w1 = time.perf_counter()
     b.step(max(args.warmup, 1))
     _, ms, clk = timed_steps(b, args.steps, None, dist, local)
-    n = sum(p.nnode + p.nstress for p in probs)
-    nv = sum(p.nnode for p in probs)
+    n = reduce_sum(dist, sum(p.nnode + p.nstress for p in probs), device="cuda")
+    nv = reduce_sum(dist, sum(p.nnode for p in probs), device="cuda")
     # two realisations against contexts holding them alone (bit-identical fields)
     same = {}
     done = max(args.warmup, 1) + args.steps
@@ -273,7 +294,8 @@ def run_batch(args, dist, local):
         same[str(r)] = bool(all(np.array_equal(a[k], bb[k]) for k in ("x", "vel", "stress")))
         ctx.close()
     b.close()
-    return {"realisations": len(probs), "particles": int(n), "velocity_particles": int(nv),
+    return {"realisations": args.batch_size, "realisations_per_rank": len(probs),
+            "particles": int(n), "velocity_particles": int(nv),
             "value": round(n * args.steps / (ms * 1e-3), 1), "unit": "particle-steps/s",
             "ms_per_step": round(ms / args.steps, 4), "steps": args.steps,
             "setup_s": round(w1 - w0, 2), "precision": "fp32 form", "autotuned_blocks": tuned,
@@ -300,7 +322,8 @@ def column_batch_problems(n=16, dx=0.001, seed=0):
 
 def three_arms(args, make, n, net, env, training, dist, local, world):
     """The FP32 form with the surrogate installed, the FP64 plain form and the FP32 form
-    alone on the same problem(s): each timed over args.steps graph-launched steps after the
+    alone on the same problem(s) (n: the particles of the whole job, all ranks): each timed
+    over args.steps graph-launched steps after the
     warm-up; each then advances to args.combined_steps steps in all and its fields are
     downloaded (one dict per realisation).  make(precision) -> uploaded context."""
     import torch
@@ -321,7 +344,7 @@ def three_arms(args, make, n, net, env, training, dist, local, world):
         if use:
             sg.stats(b, reset=True)
         t, ms, clk = timed_steps(b, args.steps, t if single else None, dist, local)
-        arms[name] = {"value": round(n * args.steps * world / (ms * 1e-3), 1),
+        arms[name] = {"value": round(n * args.steps / (ms * 1e-3), 1),
                       "ms_per_step": round(ms / args.steps, 4), "clocks": clk}
         rest = nlong - max(args.warmup, 1) - args.steps
         t = b.step(rest, t) if single else b.step(rest)
@@ -377,7 +400,9 @@ def run_biaxial(args):
         c.upload_problem(prob)
         return c
 
-    arms, fields, surr = three_arms(args, single, n, net, env, training, dist, local, world)
+    # every rank runs a replica of the sample
+    arms, fields, surr = three_arms(args, single, n * world, net, env, training, dist, local,
+                                    world)
     nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
     b = fields["fp64_plain"][0]
     nt = prob.ntotal
@@ -424,8 +449,11 @@ def run_combined(args):
     torch.cuda.set_device(local)
     sps_gb300.build_all()
     w0 = time.perf_counter()
-    probs, phis = column_batch_problems(args.columns, seed=rank)
-    n = sum(p.nnode + p.nstress for p in probs)
+    probs, phis = column_batch_problems(args.columns)
+    probs, mine = shard(probs, dist)
+    phis = [phis[i] for i in mine]
+    n = reduce_sum(dist, sum(p.nnode + p.nstress for p in probs), device="cuda")
+    nv_all = int(reduce_sum(dist, sum(p.nnode for p in probs), device="cuda"))
     net, env, training = train_surrogate(
         dx=0.005, make=lambda dx, m: sps_gb300.Problem.column(dx=dx, **dict(COLUMN, **m)),
         ranges=COLUMN_SURR_RANGES, geometry="column 0.5 x 0.25 m")
@@ -469,9 +497,9 @@ def run_combined(args):
             "warmup": args.warmup, "ms_per_step": arms["fp32_surrogate"]["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (generated column geometry, no dataset)",
-            "config": {"workload": "combined form: %d granular columns in one batch context, "
-                                   "%d particles (%d velocity) in all; %s"
-                                   % (len(probs), n, sum(p.nnode for p in probs),
+            "config": {"workload": "combined form: %d granular columns in one batch context "
+                                   "per rank, %d particles (%d velocity) in all; %s"
+                                   % (args.columns, n, nv_all,
                                       column_batch_problems.__doc__.split("\n")[0]),
                        "precision": "fp32 neighbour sums (Kahan), fp64 state and stress "
                                     "return, learned flow rule with exact fallback",

@@ -208,3 +208,22 @@ class Problem:
                     mass=self.mass.copy(), rho=self.rho.copy(), hsml=self.hsml.copy(),
                     itype=self.itype.copy(), intvars1=self.intvars1.copy(),
                     f_drucker=self.f_drucker.copy(), x00=self.x00.copy())
+
+
+def partition_by_size(sizes, nparts):
+    """Split realisations over nparts ranks by particle count: largest first, each to the
+    rank with the fewest particles so far (ties to the lower rank), so every rank gets a
+    batch of whole, independent realisations and no exchange is needed between ranks.
+    Returns one ascending index list per rank; deterministic, so every rank computes the
+    same split from the same sizes."""
+    if nparts < 1:
+        raise ValueError("nparts must be at least 1")
+    order = sorted(range(len(sizes)), key=lambda i: (-int(sizes[i]), i))
+    load = [0] * nparts
+    parts = [[] for _ in range(nparts)]
+    for i in order:
+        r = min(range(nparts), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += int(sizes[i])
+    return [sorted(q) for q in parts]
+
