@@ -16,10 +16,11 @@
 //     half[s*capH + k]  pairs created by the particle at sorted position s (the reference's
 //                       grid_find_NEW creation order), 16 B {partner id | pair type << 28,
 //                       w, dwdx, dwdy}
-//     cross/same lists  ELL layout entry[k*N2 + lcol[s]]: per target, the neighbours it
-//                       meets in the reference's linked-list walk order, 16 B
+//     cross/same lists  entry k of list column lcol[s] at ell(k, col, N2): per target, the
+//                       neighbours it meets in the reference's linked-list walk order, 16 B
 //                       {u id, w, Gx, Gy} with G the kernel gradient with respect to the
-//                       target; columns are grouped by target kind (Dev::lcol).
+//                       target, entries 2j and 2j+1 side by side in one 32-byte sector;
+//                       columns are grouped by target kind (Dev::lcol).
 // The FP64 plain kernels reproduce the reference's arithmetic operation by operation
 // (compiled with -fmad=false: no multiply-add contraction).
 #pragma once
