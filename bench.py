@@ -320,12 +320,12 @@ def column_batch_problems(n=16, dx=0.001, seed=0):
     return [sps_gb300.Problem.column(dx=dx, phi_deg=float(p), **COLUMN) for p in phis], phis
 
 
-def three_arms(args, make, n, net, env, training, dist, local, world):
+def three_arms(args, make, n, net, env, training, dist, local):
     """The FP32 form with the surrogate installed, the FP64 plain form and the FP32 form
-    alone on the same problem(s) (n: the particles of the whole job, all ranks): each timed
-    over args.steps graph-launched steps after the
-    warm-up; each then advances to args.combined_steps steps in all and its fields are
-    downloaded (one dict per realisation).  make(precision) -> uploaded context."""
+    alone on the same problem(s) (n: the particles of the whole job, all ranks): each is
+    timed over args.steps graph-launched steps after the warm-up, then advances to
+    args.combined_steps steps in all, and its fields are downloaded (one dict per
+    realisation).  make(precision) -> uploaded context."""
     import torch
     from sps_gb300 import _abi
     from sps_gb300 import surrogate as sg
@@ -401,8 +401,7 @@ def run_biaxial(args):
         return c
 
     # every rank runs a replica of the sample
-    arms, fields, surr = three_arms(args, single, n * world, net, env, training, dist, local,
-                                    world)
+    arms, fields, surr = three_arms(args, single, n * world, net, env, training, dist, local)
     nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
     b = fields["fp64_plain"][0]
     nt = prob.ntotal
@@ -464,7 +463,7 @@ def run_combined(args):
         b.upload_all()
         return b
 
-    arms, fields, surr = three_arms(args, batch, n, net, env, training, dist, local, world)
+    arms, fields, surr = three_arms(args, batch, n, net, env, training, dist, local)
     nlong = max(args.combined_steps, max(args.warmup, 1) + args.steps)
     errors = {"after_steps": nlong, "time_s": arms["fp64_plain"]["simulated_s"],
               "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)"}
