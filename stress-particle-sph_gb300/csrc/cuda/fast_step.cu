@@ -24,8 +24,6 @@ namespace sps {
 
 namespace {
 
-constexpr int kBlock = 256;
-
 struct Kahan {
   float s = 0.0f, c = 0.0f;
   __device__ __forceinline__ void add(float x) {
@@ -211,7 +209,6 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
   const double f2 = f2rk[stage];
   const Real& Mt = real_of(D, t);
   const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
-  int tt = D.itype[t];
   const int col = list_col<KIND>(D, k0, s);
   int deg = D.degC[col];
   const double xt = D.px[t], yt = D.py[t];

@@ -48,7 +48,6 @@ __device__ __forceinline__ dfl df_add(dfl x, dfl y) {
   s.lo += t.lo;
   return df_fast2sum(s.hi, s.lo);
 }
-__device__ __forceinline__ dfl df_neg(dfl x) { return {-x.hi, -x.lo}; }
 __device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
   float p = x.hi * y.hi;
   float e = fmaf(x.hi, y.hi, -p);
