@@ -109,6 +109,20 @@ typedef struct sps_params {
   double r_x, r_y;      /* shift distances dx*rx_factor, dx*ry_factor                  */
   double disp_tol;      /* vel_vector: node displacement since the last shift, in dx,
                            above which its stress-points are repositioned              */
+
+  /* Two constants that differ between the reference's source copies and that no input
+     file carries; a caller passes the values of the copy it replaces.
+     cspm_det_min: the CSPM determinant below which get_derivatives skips the correction,
+       the default-real literal 1e-07 of the Drucker-Prager example's copy
+       (example_problems/soil_failure_bui_et_al_2008/2_SPH_main_2018.f90:599) or 1e-03 of
+       code/, the strain-localisation and the vertical-slope copies (same line), widened to
+       double: (double)1e-07f or (double)1e-03f.
+     bc_nodes_only: 1 when Normal_BCs applies the boundary conditions to the nodes only
+       (`do ipoin = 1,nnode`: code/3_SPH_material_2018.f90:1664 and the strain-localisation
+       copy), 0 when it applies them to nodes and stress-points (`1,ntotal`: the
+       Drucker-Prager copy's 3_SPH_material_2018.f90:1683, the vertical-slope copy's :1664). */
+  double cspm_det_min;
+  int32_t bc_nodes_only;
 } sps_params;
 
 typedef struct sps_ctx sps_ctx;
@@ -298,9 +312,10 @@ void sps_destroy(sps_ctx* ctx);
    than SPS_STATIC_MAX_CELLS cells of the grid, SPS_ERR_ARG for bad
    arguments (NULL pointers, skf outside 1..3, a non-finite position or a non-positive
    smoothing length), SPS_ERR_CUDA for a runtime failure.
-   The first call on each device looks the scratch array's address up
-   (cudaGetSymbolAddress), which may load this library's device code onto that device;
-   make that first call before any stream capture begins.  Every call on a device shares
+   Every call looks the scratch array's address up in the current device's context
+   (cudaGetSymbolAddress); the first call on a device, and the first after its context was
+   reset, may load this library's device code there: make that call before any stream
+   capture begins.  Every call on a device shares
    the one scratch array, so calls that overlapped would race on it: each call holds a
    process-wide lock and synchronises its stream before it returns, so calls from several
    host threads run one after another. */

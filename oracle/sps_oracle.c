@@ -742,7 +742,9 @@ static void get_derivatives(orc_ctx* c, double* div1, double* div2) {
     for (int i = 0; i < NT; i++) {
       double* A = &AE[5 * (size_t)i];
       A[4] = A[0] * A[3] - A[1] * A[2];
-      if (fabs(A[4]) < (double)1e-07f) {
+      /* the copy's threshold: (double)1e-07f (2_SPH_main_2018.f90:599 of the
+         Drucker-Prager example) or (double)1e-03f (code/ and the other copies) */
+      if (fabs(A[4]) < c->p.cspm_det_min) {
         A[4] = 1;
         A[0] = 1;
         A[1] = 0;
@@ -960,11 +962,14 @@ static void artificial_viscosity(orc_ctx* c) {
 }
 
 /* Normal_BCs (3_SPH_material_2018.f90:1665-1770); ic_time is an uninitialised local in the
-   reference and is taken as 0, so t_actual = time_sph. */
+   reference and is taken as 0, so t_actual = time_sph.  The loop runs over 1..ntotal
+   (:1683) or, with bc_nodes_only, over the nodes 1..nnode as in code/ and the
+   strain-localisation copy (code/3_SPH_material_2018.f90:1664). */
 static void normal_bcs(orc_ctx* c) {
   if (c->p.no_bcs <= 0) return;
   double t = c->time_sph;
-  for (int ip = 0; ip < c->NT; ip++) {
+  const int nloop = c->p.bc_nodes_only ? c->NN : c->NT;
+  for (int ip = 0; ip < nloop; ip++) {
     int nber = c->bc_info[1 + 8 * (size_t)ip];
     if (c->bc_or_not[ip] != 1) continue;
     if (nber == 0) continue;

@@ -115,6 +115,8 @@ struct Dev {
   int cell_cap;
   // solver flags shared by the realisations
   int skf, scale_k, cspm, xsph, update_x, cont_density, sle, sp_sph, inside, no_bcs;
+  double cspm_det;    // CSPM determinant threshold of the replaced source copy
+  int bc_nodes_only;  // Normal_BCs over the nodes only (code/, strain-localisation copy)
   int bound_from_lists;
   double pi;
   int bcvar[kMaxBC];

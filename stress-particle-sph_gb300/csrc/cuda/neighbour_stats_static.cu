@@ -51,24 +51,18 @@ static_assert(kScratchBytes == SPS_STATIC_SCRATCH_BYTES, "scratch layout and hea
 // device address: the address comes from cudaGetSymbolAddress (scratch_on_current_device).
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;                    // serialises calls: they share g_scratch
-void* g_addr[kMaxDevices] = {};     // device address of g_scratch, per device ordinal
+std::mutex g_mu;  // serialises calls: they share g_scratch
 
-// Looks the scratch address up once per device, with that device current.  Called with
+// The device address of g_scratch in the current device's context, looked up on every call
+// (cheap once this library's device code is loaded there): an address kept from an earlier
+// call would be stale after the context was reset (cudaDeviceReset), since the module is
+// then loaded again.  The first lookup on a device may load the device code.  Called with
 // g_mu held.
 cudaError_t scratch_on_current_device(unsigned char** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return e;
-    g_addr[dev] = p;
-  }
-  *out = static_cast<unsigned char*>(g_addr[dev]);
+  *out = static_cast<unsigned char*>(p);
   return cudaSuccess;
 }
 
@@ -256,9 +250,13 @@ extern "C" int sps_neighbour_stats_static(int32_t n, const double* x, const doub
             cudaSuccess)
       e = cudaStreamSynchronize(st);
   }
-  if (e != cudaSuccess)
+  if (e != cudaSuccess) {
+    // wait for what this call enqueued before the failure, so that none of its work still
+    // uses the scratch array when the lock is released (the first error is the one reported)
+    cudaStreamSynchronize(st);
     return say(msg, msg_len, SPS_ERR_CUDA, "sps_neighbour_stats_static: %s",
                cudaGetErrorString(e));
+  }
   int64_t total = 0;
   for (int a = 0; a < n; a++) total += degree[a];
   *npairs = total / 2;

@@ -453,6 +453,10 @@ int check_params(const sps_params* p) {
       return fail(nullptr, SPS_ERR_UNSUPPORTED, "negative time-curve index in bc_list");
   if (p->ic_grav != 0 && (p->tcurve_grav < 1 || p->tcurve_grav > p->ntcurves))
     return fail(nullptr, SPS_ERR_ARG, "gravity time curve out of range");
+  if (!(p->cspm_det_min >= 0.0 && p->cspm_det_min < 1e300))
+    return fail(nullptr, SPS_ERR_ARG, "cspm_det_min must be finite and >= 0");
+  if (p->bc_nodes_only != 0 && p->bc_nodes_only != 1)
+    return fail(nullptr, SPS_ERR_ARG, "bc_nodes_only must be 0 or 1");
   return SPS_OK;
 }
 
@@ -462,6 +466,7 @@ bool same_flags(const sps_params& a, const sps_params& b) {
          a.xsph == b.xsph && a.update_x == b.update_x && a.cont_density == b.cont_density &&
          a.sle == b.sle && a.skf == b.skf && a.precision == b.precision && a.pi == b.pi &&
          a.ntype_solid == b.ntype_solid && a.art_stress == b.art_stress &&
+         a.cspm_det_min == b.cspm_det_min && a.bc_nodes_only == b.bc_nodes_only &&
          (a.inside_approach || !a.sp_sph ||
           (a.npoints == b.npoints && a.sph_shift == b.sph_shift &&
            a.vel_vector == b.vel_vector && a.shift_update == b.shift_update));
@@ -583,6 +588,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.inside = p->inside_approach;
     D.no_bcs = p->no_bcs;
     D.ifsigman = p->ifsigman;
+    D.cspm_det = p->cspm_det_min;
+    D.bc_nodes_only = p->bc_nodes_only;
     // (the outside approach shifts the stress-points right after the detection, so the
     // detection cannot wait for the download)
     c.surf_every = p->update_x && (p->ifsigman == 1 || (p->xsph && p->no_bcs > 0) ||

@@ -20,6 +20,7 @@ __device__ __forceinline__ void apply_bcs(const Dev& D, const StepScalars& sc, i
   if (D.no_bcs <= 0) return;
   const int bc = D.bc_or_not[ip];
   if (bc == 1) {
+    if (D.bc_nodes_only && ip >= D.NN) return;  // Normal_BCs over 1..nnode
     const int32_t* bi = D.bc_info + 8 * (size_t)ip;
     if (bi[1] == 0) return;
     for (int r = 0; r < 5; r++) {
@@ -66,7 +67,7 @@ __device__ __forceinline__ void tail_sp_grad(const Dev& D, int t, double* g, con
     if (D.cspm) {
       double A4 = AE[0] * AE[3] - AE[1] * AE[2];
       double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
-      if (fabs(A4) < (double)1e-07f) {
+      if (fabs(A4) < D.cspm_det) {
         A4 = 1;
         A0 = 1;
         A1 = 0;
@@ -214,7 +215,7 @@ __device__ __forceinline__ void tail_node(const Dev& D, const StepScalars& sc, i
   if (D.cspm) {
     double A4 = AE[0] * AE[3] - AE[1] * AE[2];
     double A0 = AE[0], A1 = AE[1], A2 = AE[2], A3 = AE[3];
-    if (fabs(A4) < (double)1e-07f) {
+    if (fabs(A4) < D.cspm_det) {
       A4 = 1;
       A0 = 1;
       A1 = 0;

@@ -379,6 +379,11 @@ void defaults(sph_problem& P) {
   P.p.nstre = 4;
   P.p.pi = (double)(4.0f * std::atan(1.0f));
   P.p.precision = SPS_PREC_FP64_PLAIN;
+  // the Drucker-Prager example's copy (the header with ntype_solid): CSPM determinant
+  // threshold 1e-07 (2_SPH_main_2018.f90:599), Normal_BCs over nodes and stress-points
+  // (3_SPH_material_2018.f90:1683)
+  P.p.cspm_det_min = (double)1e-07f;
+  P.p.bc_nodes_only = 0;
 }
 
 void parse_all(sph_problem& P, const std::string& in_txt, const std::string& dat_txt,
@@ -401,9 +406,21 @@ void parse_all(sph_problem& P, const std::string& in_txt, const std::string& dat
     nstre = dat.to_i(v[1]);
     nmats = dat.to_i(v[2]);
   } else {
+    // the header of code/ and of the strain-localisation and vertical-slope copies
+    // (`nstre, nmats`, code/3_SPH_material_2018.f90:101).  The strain-localisation copy's
+    // constitutive routines are the plane-strain branch without a test ("nstre = 4 --
+    // plane strain (only current functioning option)"), i.e. ntype_solid 2 here; the
+    // vertical-slope copy never reads ntype_solid (0), which its elastic example reaches
+    // no branch of.  The CSPM threshold of all three is 1e-03 (2_SPH_main_2018.f90:599);
+    // code/ and the strain-localisation copy apply Normal_BCs to the nodes only
+    // (3_SPH_material_2018.f90:1664), the vertical-slope copy to 1..ntotal: a caller
+    // replacing that copy sets bc_nodes_only = 0.
     auto v = dat.read(2);
     nstre = dat.to_i(v[0]);
     nmats = dat.to_i(v[1]);
+    ntype_solid = 2;
+    P.p.cspm_det_min = (double)1e-03f;
+    P.p.bc_nodes_only = 1;
   }
   P.p.ntype_solid = ntype_solid;
   if (ntype_solid == 4) nstre = 6;

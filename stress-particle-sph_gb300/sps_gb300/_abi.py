@@ -87,6 +87,8 @@ class SpsParams(C.Structure):
         ("r_x", c_double),
         ("r_y", c_double),
         ("disp_tol", c_double),
+        ("cspm_det_min", c_double),
+        ("bc_nodes_only", c_int32),
     ]
 
 

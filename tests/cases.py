@@ -18,9 +18,12 @@ def bui_like(width=4.0, height=2.0, dx=0.1, young=1.8e6, poiss=0.3, rho=1850.0,
              tanphi=0.466308, coh=5000.0, xsph=True, cspm=False, alpha=0.1, beta=0.1,
              damping=0.0, dt=1.5e-4, sml=1.2, skf=1, cont_density=False, sle=1,
              ntype_solid=2, npoints=1, floor_to=9.0, ntype_eco=2, ncrit=12,
-             output_flags="1 1 1 1 1 1 1 0 0 0", art_stress=False, outside=None):
+             output_flags="1 1 1 1 1 1 1 0 0 0", art_stress=False, outside=None,
+             domain=(-10, -10, 41, 41), gravity_curve=((0, 1, 500), (1, 1, 1))):
     """Cohesive soil block on a floor with a left wall: the layout of the Drucker-Prager
-    example (inside approach, three dummy rows) with every parameter adjustable."""
+    example (inside approach, three dummy rows) with every parameter adjustable.
+    domain: xmin, ymin, xmax, ymax of the domain box (Check_Out_Domain); gravity_curve:
+    the times and factors of the gravity time curve."""
     pts = "\n".join([
         "geom_type", "1", "x1 x2 x3 x4 dx",
         "0.0 %s 0.0 %s %s" % (_fmt(width), _fmt(width), _fmt(dx)),
@@ -41,8 +44,10 @@ def bui_like(width=4.0, height=2.0, dx=0.1, young=1.8e6, poiss=0.3, rho=1850.0,
         "tan(phi) cohesion",
         "%s %s 0 0 0 0 0 0 0 0" % (_fmt(tanphi), _fmt(coh)),
         "ic_unks", "0", "BC's: nprer Sigman=0", "0 0", "segments", "0", "nodes", "0",
-        "ic_tcurve", "1", "ntcurves mpts", "1 100", "pts in curve 1", "3", "times and factors",
-        "0 1 500", "1 1 1", "xmin domain xmax domain", "-10 -10 41 41",
+        "ic_tcurve", "1", "ntcurves mpts", "1 100", "pts in curve 1",
+        str(len(gravity_curve[0])), "times and factors",
+        " ".join(_fmt(v) for v in gravity_curve[0]), " ".join(_fmt(v) for v in gravity_curve[1]),
+        "xmin domain xmax domain", " ".join(_fmt(v) for v in domain),
         "Initial conditions index", "2", "s11", "0", "s22", "0", "s12", "0", "s33", "0", "w1", "0",
         "v2", "0", "pa_sph nnps sle skf cspm update_x XSPH",
         "2 2 %d %d %s T %s" % (sle, skf, L(cspm), L(xsph)),

@@ -69,6 +69,32 @@ def test_column_k0(built_gpu):
     _compare(p, 30, chunks=[10, 20])
 
 
+def test_leaving_the_domain(built_gpu):
+    # Check_Out_Domain (2_SPH_main_2018.f90:1186-1192): the block moves right at 1 m/s and
+    # its right-hand columns cross xmax = 1.0005 m within the run; a particle that leaves
+    # is excluded from the cell grid and the pair search for good (the floor ends under
+    # the block, so no wall particle starts outside)
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05, dt=5e-5, floor_to=1.0,
+                       domain=(-10, -10, 1.0005, 41))
+    p.vel[0:2 * p.ntotal:2] = 1.0
+    f = _compare(p, 30, chunks=[10, 20])
+    x = f["x"].reshape(-1, 2)[:p.ntotal, 0]
+    assert (x > 1.0005).sum() >= 10  # the right-hand column of nodes left
+
+
+def test_damping_and_ramped_gravity(built_gpu):
+    # gravity_force (3_SPH_material_2018.f90:2809-2870) with DampingTG = 50 and the gravity
+    # factor ramped from 0 to 1 over 10 ms by its time curve, on the plastic block
+    p = cases.bui_like(width=1.0, height=0.5, dx=0.05, dt=5e-5, damping=50.0,
+                       gravity_curve=((0, 0.01, 500), (0, 1, 1)))
+    f = _compare(p, 40, chunks=[15, 25])
+    q = cases.bui_like(width=1.0, height=0.5, dx=0.05, dt=5e-5)
+    o = _orc_ctx(q)
+    o.upload_problem(q)
+    o.step(40, 0.0)
+    assert not np.array_equal(o.download()["vel"], f["vel"])  # the terms act
+
+
 def test_cspm_cont_density(built_gpu):
     p = cases.bui_like(width=1.0, height=0.5, dx=0.05, cspm=True, cont_density=True, sle=2,
                        dt=5e-5)

@@ -5,6 +5,7 @@ import pytest
 
 import cases
 import sps_gb300
+from sps_gb300 import _abi
 
 pytestmark = pytest.mark.gpu
 
@@ -52,3 +53,27 @@ def test_download_into_given_arrays(built_gpu):
     with pytest.raises(ValueError):
         ctx.download(out=dict(out, rho=np.empty(3)))
     ctx.close()
+
+
+def test_nonfinite_state_after_a_step(built_gpu):
+    # a NaN stress is accepted by the upload (it checks positions and smoothing lengths
+    # only); the step propagates it into velocities and positions, and the finiteness check
+    # after the step reports SPS_ERR_NONFINITE.  The context stays usable: a valid upload
+    # then steps exactly as a fresh context.
+    prob = cases.bui_like()
+    ctx = _ctx(prob)
+    st = prob.state()
+    st["stress"] = st["stress"].copy()
+    st["stress"][4 * (prob.nnode + 7) + 1] = np.nan
+    ctx.upload(**st)
+    with pytest.raises(sps_gb300.SpsError) as e:
+        ctx.step(1, 0.0)
+    assert e.value.rc == _abi.SPS_ERR_NONFINITE
+    ctx.upload_problem(prob)
+    ctx.step(3, 0.0)
+    ref = _ctx(prob)
+    ref.upload_problem(prob)
+    ref.step(3, 0.0)
+    cases.assert_bitwise(ctx.download(), ref.download(), prob.ntotal)
+    ctx.close()
+    ref.close()

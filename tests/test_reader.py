@@ -3,37 +3,65 @@
 Every input set of the reference's examples must parse, and the generated counts, masses
 and dummy layout must follow the reference's formulas
 (example_problems/soil_failure_bui_et_al_2008/3_SPH_material_2018.f90:431-461, :682-733,
-:795-879).  The example inputs are read from the reference checkout when it is present.
+:795-879).  The example inputs are the copies under tests/golden/example_problems.
 """
-import glob
 import math
-import os
 
 import numpy as np
 import pytest
 
 import cases
+import examples
+import orc
 import sps_gb300
 
-REF = "/root/reference/example_problems"
 
-
-def example_dirs():
-    if not os.path.isdir(REF):
-        return []
-    # input sets are the directories holding input.txt next to a .dat and a .pts file
-    return sorted(os.path.dirname(p) for p in glob.glob(REF + "/**/input.txt", recursive=True)
-                  if glob.glob(os.path.join(os.path.dirname(p), "*.dat")))
-
-
-@pytest.mark.parametrize("d", example_dirs() or [None])
-def test_reference_inputs_parse(built, d):
-    if d is None:
-        pytest.skip("reference example inputs not present on this machine")
-    p = sps_gb300.Problem.from_dir(d)
+@pytest.mark.parametrize("rel", examples.example_sets())
+def test_reference_inputs_parse(built, rel):
+    p = examples.load(rel)
     par = p.params
     assert par.nnode > 0 and p.ntotal2 >= p.ntotal
     assert len(p.blocks) >= 1 and p.blocks[0]["dt"] > 0
+    # the source copy's constants: the Drucker-Prager copy's header carries ntype_solid,
+    # the others' (code/, strain localisation, vertical cut) do not and are plane strain
+    if rel.startswith("soil_failure"):
+        assert par.cspm_det_min == float(np.float32(1e-7)) and par.bc_nodes_only == 0
+    else:
+        assert par.ntype_solid == 2
+        assert par.cspm_det_min == float(np.float32(1e-3)) and par.bc_nodes_only == 1
+
+
+def test_example_sets_present():
+    sets = examples.example_sets()
+    assert len(sets) == 16
+    for fam in ("soil_failure_bui_et_al_2008", "strain_localisation_in_soil_sample",
+                "vertical_slope"):
+        assert any(s.startswith(fam) for s in sets)
+
+
+@pytest.mark.parametrize("rel", examples.example_sets())
+def test_reference_inputs_step_on_oracle(built, rel):
+    # two steps of every set on the oracle with its copy's constants: the set-up path and
+    # the options each set turns on (BCs, CSPM, viscoplasticity, outside approach, standard
+    # SPH) run and keep the state finite
+    p = examples.load(rel)
+    o = orc.context(p.params_copy(**examples.overrides(rel)))
+    o.upload_problem(p)
+    o.step(2, 0.0)
+    f = o.download()
+    assert np.isfinite(f["x"]).all() and np.isfinite(f["vel"]).all()
+    assert np.isfinite(f["stress"][:4 * p.ntotal]).all()
+    o.close()
+
+
+def test_own_steps_follow_the_driver_loop(built):
+    # code/1_SPH_2018.f90:72-88: up to maxtimestep steps, leaving after the step whose FP64
+    # time first exceeds time_end
+    lengths = {r: examples.own_steps(examples.load(r)) for r in examples.example_sets()}
+    assert lengths["soil_failure_bui_et_al_2008/inside_approach/SP1"] == 10
+    assert lengths["strain_localisation_in_soil_sample/SP1"] == 2101
+    assert lengths["vertical_slope/SP1"] == 2001
+    assert lengths["soil_failure_bui_et_al_2008/standard_sph"] == 16667
 
 
 def test_bui_counts_and_masses(built):

@@ -60,8 +60,9 @@ def pair_list_stats(problem):
 
 @pytest.mark.parametrize("make", [lambda: cases.bui_like(),
                                   lambda: cases.column(dx=0.004),
-                                  lambda: cases.bui_like(width=1.0, height=0.5, dx=0.05, skf=2)],
-                         ids=["bui_cubic", "column_cubic", "bui_gauss"])
+                                  lambda: cases.bui_like(width=1.0, height=0.5, dx=0.05, skf=2),
+                                  lambda: cases.bui_like(width=1.0, height=0.5, dx=0.05, skf=3)],
+                         ids=["bui_cubic", "column_cubic", "bui_gauss", "bui_quintic"])
 def test_static_matches_pair_list(built_gpu, make):
     prob = make()
     deg_ref, ws_ref, np_ref = pair_list_stats(prob)
