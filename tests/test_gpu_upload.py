@@ -59,21 +59,26 @@ def test_nonfinite_state_after_a_step(built_gpu):
     # a NaN stress is accepted by the upload (it checks positions and smoothing lengths
     # only); the step propagates it into velocities and positions, and the finiteness check
     # after the step reports SPS_ERR_NONFINITE.  The context stays usable: a valid upload
-    # then steps exactly as a fresh context.
+    # then steps exactly as the oracle does after the same sequence (the pair list's
+    # bookkeeping carries over an upload in both, as the reference's linked list carries
+    # over its steps)
+    import orc
     prob = cases.bui_like()
     ctx = _ctx(prob)
+    ref = orc.context(prob.params_copy())
     st = prob.state()
     st["stress"] = st["stress"].copy()
     st["stress"][4 * (prob.nnode + 7) + 1] = np.nan
     ctx.upload(**st)
+    ref.upload(**st)
     with pytest.raises(sps_gb300.SpsError) as e:
         ctx.step(1, 0.0)
     assert e.value.rc == _abi.SPS_ERR_NONFINITE
-    ctx.upload_problem(prob)
-    ctx.step(3, 0.0)
-    ref = _ctx(prob)
-    ref.upload_problem(prob)
-    ref.step(3, 0.0)
+    ref.step(1, 0.0)
+    assert not np.isfinite(ref.download()["x"]).all()
+    for c in (ctx, ref):
+        c.upload_problem(prob)
+        c.step(3, 0.0)
     cases.assert_bitwise(ctx.download(), ref.download(), prob.ntotal)
     ctx.close()
     ref.close()
