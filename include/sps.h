@@ -202,6 +202,15 @@ int sps_selftest_division(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* misma
    bit. */
 int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* Self-test (no reference counterpart): the FP32 form's stress return first certifies in
+   FP32 that a stress lies inside the Drucker-Prager cone with a margin covering its
+   roundings, and then skips the FP64 test of adapt_stress2.  On n pseudo-random materials
+   and stresses (a quarter of them within a relative 1e-3 .. 1e-9 of the cone), *mismatches
+   counts stresses certified inside that the FP64 test would return (must be 0) and
+   *certified the stresses certified. */
+int sps_selftest_cone(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches,
+                      int64_t* certified);
+
 /* Launch-shape autotuner (no reference counterpart): time each tunable kernel (the pair
    search and lists, the interpolation, the derivative sums, the stress-return and RK
    kernels, XSPH) at block sizes 64, 128, 256 and 512 over nsteps profiled steps of the
@@ -212,14 +221,17 @@ int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismat
    order depends on it. */
 int sps_autotune(sps_ctx* ctx, int32_t nsteps, int32_t* blocks);
 
-/* The look-ahead of the FP32 form's neighbour sums that sps_autotune chose after the
-   block sizes (no reference counterpart): ahead[0] neighbours a pass in the interpolation
-   (2, 4 or 8), ahead[1] in the node derivative sums (1, 2 or 4); a pass loads its
-   neighbours' list entries and records before it sums any of them, in the same order, so
-   the results do not depend on these.  Defaults before tuning: 4 and 2. */
+/* How the FP32 form's neighbour sums walk their lists, as sps_autotune chose it after the
+   block sizes (no reference counterpart): ahead[0] for the interpolation, ahead[1] for
+   the derivative sums.  0: the staged walk -- every thread copies its list entries into
+   shared memory with asynchronous copies (cp.async) eight entries ahead of its sum, and
+   loads the records of two neighbours at a time; 2, 4 or 8 (interpolation), 1, 2 or 4
+   (derivatives): that many neighbours' entries and records are loaded before any of them
+   is summed.  Every choice sums the neighbours in the same order, so the results do not
+   depend on it.  Defaults before tuning: 4 and 2. */
 int sps_tuned_lookahead(sps_ctx* ctx, int32_t* ahead);
 
-/* Sets that look-ahead directly (interp 2, 4 or 8; derivs 1, 2 or 4), e.g. to reuse the
+/* Sets that choice directly (interp 0, 2, 4 or 8; derivs 0, 1, 2 or 4), e.g. to reuse the
    values tuned on one context in another of the same workload. */
 int sps_set_lookahead(sps_ctx* ctx, int32_t interp, int32_t derivs);
 

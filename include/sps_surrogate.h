@@ -112,7 +112,22 @@ typedef struct sps_surrogate_opts {
    m == NULL uninstalls.  SPS_ERR_UNSUPPORTED for the FP64 plain form. */
 int sps_surrogate_install(sps_ctx* ctx, sps_mlp* m, const sps_surrogate_opts* opts);
 
-/* counts[0] = loading stress-point evaluations since install (or the last reset),
+/* The gate that keeps the network from costing time where it does not pay (no reference
+   counterpart): a step runs the network only while it answers at least min_answered of
+   that step's loading evaluations; after a step below that, the exact rule alone runs for
+   a period of steps and then the network is tried for one step again, the period
+   doubling up to max_period steps while these tries keep failing and returning to 1 after
+   one that passes.  The decision is taken on the device at the end of every step.
+   min_answered <= 0 keeps the network on in every step.  Defaults at install: 0.5 and 64.
+   Setting it restarts the gate (on, period 1). */
+int sps_surrogate_gate(sps_ctx* ctx, double min_answered, int32_t max_period);
+
+/* steps[0] = steps run with the network since install, steps[1] = steps run without it
+   (gate closed). */
+int sps_surrogate_gate_stats(sps_ctx* ctx, int64_t* steps);
+
+/* counts[0] = loading stress-point evaluations since install (or the last reset) in the
+   steps that ran the network,
    counts[1] = those answered by the network, counts[2] = outside the envelope,
    counts[3] = rejected by the drift test.  reset != 0 zeroes them after reading. */
 int sps_surrogate_stats(sps_ctx* ctx, int64_t* counts, int32_t reset);

@@ -85,6 +85,7 @@ struct Real {
   double D11, D12, D22, D33, D41, D42;
   double tanfi, coh, young, poiss;
   double alpha2, kc;  // adapt_stress2 constants (FP64)
+  float alpha2f, kcf; // the same rounded to FP32 (the FP32 form's inside-the-cone test)
   double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
   double xmin_dom[2], xmax_dom[2];
   double cgrav[2];
@@ -105,6 +106,18 @@ enum ErrBits : int {
   ERR_CELLS = 4,
   ERR_NPAIRS = 8,
   ERR_BOUND = 16,
+};
+
+// The surrogate's gate (sps_surrogate_gate): the network runs in a step only while it
+// answers at least min_frac of the step's loading evaluations.  After a step below that it
+// is off for `period` steps and then runs one step again (a probe); the period doubles, up
+// to max_period, while probes keep failing, and returns to 1 after a step that passes.
+// Updated on the device at the end of every step, so no host synchronisation is needed.
+struct SurrGate {
+  int on, wait, period, max_period;
+  double min_frac;                          // <= 0: always on
+  unsigned long long load0, ans0;           // the counters at the start of the step
+  unsigned long long steps_on, steps_off;   // steps with and without the network
 };
 
 struct Dev {
@@ -171,6 +184,7 @@ struct Dev {
   float env_lo[14], env_hi[14], out_max;
   double surr_tol;
   unsigned long long* surr_cnt;  // loading, answered, outside envelope, drift-rejected
+  struct SurrGate* surr_gate;    // whether this step runs the network (sps_surrogate_gate)
   // cells
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
   float *xr, *yr, *hr;
@@ -459,6 +473,39 @@ static __device__ __noinline__ void adapt_stress_full(double alpha2, double kc, 
   }
 }
 
+// FP32 value of x with the significand truncated (relative error below 2^-23), on the
+// integer pipe; NaN outside the normal FP32 range (zero excepted), which fails every test
+// that uses it
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(u >> 32), l32 = (unsigned)u;
+  const int E = (int)((h32 >> 20) & 0x7FFu);
+  if (E < 897 || E > 1150) return (u << 1) == 0ull ? 0.0f : __uint_as_float(0x7FC00000u);
+  return __uint_as_float((h32 & 0x80000000u) | ((unsigned)(E - 896) << 23) |
+                         ((h32 & 0xFFFFFu) << 3) | (l32 >> 29));
+}
+
+// True when the stress (a, b, c, d) lies inside the Drucker-Prager cone with a margin that
+// covers every rounding of this FP32 evaluation: then yield >= 0 and yield^2 >= J2 hold in
+// exact arithmetic with a relative margin far above the FP64 test's roundings, so the FP64
+// return below leaves the stress unchanged and may be skipped (the result is bit-identical).
+// Error bounds, u = 2^-24, M = max |component|: the truncated inputs carry 2u M; the mean
+// 16u M; each deviator component 24u M (|d| <= 2.1 M); J2 = d2^2 + (d0^2 + d1^2 + d3^2)/2
+// therefore 256u M^2; yield = kc - 3 alpha smean 4u kc + 64u alpha M.  Anything outside
+// the FP32 range fails the test and takes the FP64 path.
+__device__ __forceinline__ bool inside_cone_f32(float alpha2, float kc, double a, double b,
+                                                double c, double d) {
+  const float af = f32_trunc(a), bf = f32_trunc(b), cf = f32_trunc(c), df = f32_trunc(d);
+  const float m = fmaxf(fmaxf(fabsf(af), fabsf(bf)), fmaxf(fabsf(cf), fabsf(df)));
+  const float u = 5.9604645e-08f;  // 2^-24
+  const float smean = ((af + bf) + df) * (1.0f / 3.0f);
+  const float d0 = af - smean, d1 = bf - smean, d3 = df - smean;
+  const float j2 = fmaf(cf, cf, 0.5f * fmaf(d0, d0, fmaf(d1, d1, d3 * d3)));
+  const float yl = (kc - (3.0f * alpha2) * smean) - (4.0f * u * kc + 64.0f * u * alpha2 * m);
+  const float ej = 256.0f * u * (m * m);
+  return yl > 0.0f && yl * yl > (j2 + ej) * (1.0f + 16.0f * u);
+}
+
 // The same return for the FP32 form, without FP64 divisions or square roots in the common
 // path (GB300 issues FP64 at a small fraction of its FP32 rate): the mean by a product with
 // 1/3, the test yield < sqrt(J2) as yield^2 < J2 (yield >= 0), and for the stress-points
@@ -702,6 +749,7 @@ void launch_vol(Ctx& c, int lo, int hi);
 void launch_finterp(Ctx& c);
 void launch_fderivs(Ctx& c, int stage);
 void launch_fsp_tail(Ctx& c, int stage);
+int set_staged_limits();  // cudaError_t of raising the staged walk's shared-memory limits
 void launch_surface(Ctx& c);
 void launch_surface_f32(Ctx& c);
 void launch_lists_keys(Ctx& c);
@@ -709,4 +757,5 @@ void launch_lists_same(Ctx& c);
 void launch_fxsph(Ctx& c);
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
+void launch_selftest_cone(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_out);
 }  // namespace sps

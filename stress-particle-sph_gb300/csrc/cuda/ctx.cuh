@@ -98,7 +98,9 @@ struct Ctx {
   unsigned long long* cap_cnt = nullptr;
   uint2* mlp_frag = nullptr;
   float* mlp_bias = nullptr;
-  unsigned long long* surr_cnt = nullptr;
+  unsigned long long* surr_cnt = nullptr;  // the 4 counters, then the gate (SurrGate)
+  double gate_min_frac = 0.5;               // sps_surrogate_gate
+  int gate_max_period = 64;
   // output snapshot (sps_snapshot): device copy of the output fields, pinned host copy,
   // the stream that moves one to the other, and the events that order them
   char* snap_dev = nullptr;

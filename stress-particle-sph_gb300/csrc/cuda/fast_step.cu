@@ -55,6 +55,66 @@ __device__ __forceinline__ float dfdiff(float ah, float al, float bh, float bl) 
   return (ah - bh) + (al - bl);
 }
 
+// ---- the staged neighbour walk ------------------------------------------------------------
+// A neighbour sum waits on two dependent loads per neighbour: its list entry, streamed from
+// DRAM, and then the neighbour's records, gathered mostly from L1/L2.  In the staged walk
+// every thread copies its own list entries into shared memory with cp.async, kDE entries
+// ahead of the one it sums, so that the DRAM stream runs in the background; the records of
+// kSP entries at a time are then loaded together from the staged entries.  A thread reads
+// only its own slots, so no barrier between threads is needed, and the neighbours are
+// summed in list order, so every result bit is that of the direct walk.
+constexpr int kDE = 8, kSP = 2;
+static_assert(kDE % kSP == 0, "entries are staged in groups of kSP");
+constexpr int kStagedSlots = kDE;  // 16-byte shared-memory slots per thread
+
+__device__ __forceinline__ void cp_async16_cg(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Walks the deg entries of list column col in order.  load(e, r0, r1) loads the records of
+// entry e's neighbour (issued for kSP entries before any is summed); sum(e, r0, r1) adds
+// it.  smem: kDE x blockDim.x 16-byte slots.  Group g of the cp.async groups holds entries
+// g kSP .. g kSP + kSP - 1: the prologue commits groups 0 .. kDE/kSP - 1, pass m commits
+// group m + kDE/kSP, and pass m waits for group m.
+template <class Load, class Sum>
+__device__ __forceinline__ void staged_walk(const int4* __restrict__ list, int col, int N2,
+                                            int deg, int4* smem, Load load, Sum sum) {
+  const int B = blockDim.x, tid = threadIdx.x;
+  for (int g = 0; g < kDE / kSP; g++) {
+    for (int q = 0; q < kSP; q++) {
+      const int k = g * kSP + q;
+      if (k < deg) cp_async16_cg(&smem[k * B + tid], &list[ell(k, col, N2)]);
+    }
+    cp_async_commit();
+  }
+  for (int k = 0; k < deg; k += kSP) {
+    cp_async_wait<kDE / kSP - 1>();
+    float4 r0[kSP], r1[kSP];
+#pragma unroll
+    for (int q = 0; q < kSP; q++)
+      if (k + q < deg) load(smem[((k + q) % kDE) * B + tid], r0[q], r1[q]);
+    // the entries are read again for the sums rather than kept in registers
+    asm volatile("" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < kSP; q++)
+      if (k + q < deg) sum(smem[((k + q) % kDE) * B + tid], r0[q], r1[q]);
+#pragma unroll
+    for (int q = 0; q < kSP; q++)
+      if (k + q + kDE < deg)
+        cp_async16_cg(&smem[((k + q) % kDE) * B + tid], &list[ell(k + q + kDE, col, N2)]);
+    cp_async_commit();
+  }
+  cp_async_wait<0>();
+}
+
 // stress_point_update (2_SPH_main_2018.f90:403-482), FP32 sums.  A stress-point's velocity
 // is the weighted mean of its nodes' velocities; it is formed as the first node's velocity
 // plus the weighted mean of the deviations, which are small and exact in double-float.
@@ -108,9 +168,24 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
       nm.add(h2);
     };
+    if (KP == 0) {  // the staged walk: records {recV, recI} of the non-wall partners
+      extern __shared__ int4 staged_smem[];
+      staged_walk(
+          D.cross, col, D.N2, deg, staged_smem,
+          [&](const int4& e, float4& r, float4& ri) {
+            if (e.y >= 0) {
+              r = D.recV[e.x];
+              ri = D.recI[e.x];
+            }
+          },
+          [&](const int4& e, const float4& r, const float4& ri) {
+            if (e.y >= 0) term(__int_as_float(e.y), r, ri.y);
+          });
+      deg = 0;  // walked
+    }
     // kP neighbours a pass: their entries and records are loaded before any is summed, so
     // that the loads overlap (the sum order is unchanged)
-    constexpr int kP = KP;
+    constexpr int kP = KP > 0 ? KP : 1;
     int k = 0;
     for (; k + kP - 1 < deg; k += kP) {
       int4 e[kP];
@@ -153,7 +228,22 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
     };
-    constexpr int kP = KP;  // neighbours a pass, as above
+    if (KP == 0) {  // the staged walk: records {recS, recI} of the non-wall partners
+      extern __shared__ int4 staged_smem[];
+      staged_walk(
+          D.cross, col, D.N2, deg, staged_smem,
+          [&](const int4& e, float4& rs, float4& ri) {
+            if (e.y >= 0) {
+              rs = D.recS[e.x];
+              ri = D.recI[e.x];
+            }
+          },
+          [&](const int4& e, const float4& rs, const float4& ri) {
+            if (e.y >= 0) term(__int_as_float(e.y), rs, ri);
+          });
+      deg = 0;  // walked
+    }
+    constexpr int kP = KP > 0 ? KP : 1;  // neighbours a pass, as above
     int k = 0;
     for (; k + kP - 1 < deg; k += kP) {
       int4 e[kP];
@@ -199,7 +289,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets
 // KP: neighbours a pass, loaded before any is summed (as in k_finterp)
 template <int KIND, int KP>
-__global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int stage,
+__global__ void __launch_bounds__(256, KIND == 1 ? 4 : (KP == 0 ? 2 : 3)) k_fderivs(Dev D, int stage,
                                                     const int32_t* __restrict__ tgt, int ntgt) {
   const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (k0 >= ntgt) return;
@@ -256,20 +346,32 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       }
     };
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (KP == 0) {  // the staged walk: records {recV, recI}; a wall partner reads its volume
+      extern __shared__ int4 staged_smem[];
+      staged_walk(
+          D.cross, col, D.N2, deg, staged_smem,
+          [&](const int4& e, float4& r, float4& ri) {
+            ri = D.recI[e.x];
+            r = e.y >= 0 ? D.recV[e.x] : z;
+          },
+          [&](const int4& e, const float4& r, const float4& ri) { term(e, ri.y, r); });
+      deg = 0;  // walked
+    }
+    constexpr int kP = KP > 0 ? KP : 1;
     int k = 0;
-    for (; k + KP - 1 < deg; k += KP) {
-      int4 e[KP];
-      float vol[KP];
-      float4 r[KP];
+    for (; k + kP - 1 < deg; k += kP) {
+      int4 e[kP];
+      float vol[kP];
+      float4 r[kP];
 #pragma unroll
-      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
+      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
 #pragma unroll
-      for (int q = 0; q < KP; q++) {
+      for (int q = 0; q < kP; q++) {
         vol[q] = D.recI[e[q].x].y;
         r[q] = e[q].y >= 0 ? D.recV[e[q].x] : z;
       }
 #pragma unroll
-      for (int q = 0; q < KP; q++) term(e[q], vol[q], r[q]);
+      for (int q = 0; q < kP; q++) term(e[q], vol[q], r[q]);
     }
     for (; k < deg; k++) {
       const int4 e = D.cross[ell(k, col, D.N2)];
@@ -323,16 +425,32 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       sx.add(m, dwx);
       sy.add(m, dwy);
     };
-    // KP neighbours a pass: entries and records loaded before any is summed
-    int k = 0;
-    for (; k + KP - 1 < deg; k += KP) {
+    if (KP == 0) {  // the staged walk: records {recA, recAl} of the non-wall partners
+      extern __shared__ int4 staged_smem[];
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      int4 e[KP];
-      float4 a[KP], l[KP];
+      staged_walk(
+          D.cross, col, D.N2, deg, staged_smem,
+          [&](const int4& e, float4& a, float4& l) {
+            a = l = z;
+            if (e.y >= 0) {
+              a = D.recA[e.x];
+              l = D.recAl[e.x];
+            }
+          },
+          [&](const int4& e, const float4& a, const float4& l) { term(e, a, l); });
+      deg = 0;  // walked
+    }
+    // KP neighbours a pass: entries and records loaded before any is summed
+    constexpr int kP = KP > 0 ? KP : 1;
+    int k = 0;
+    for (; k + kP - 1 < deg; k += kP) {
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      int4 e[kP];
+      float4 a[kP], l[kP];
 #pragma unroll
-      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
+      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
 #pragma unroll
-      for (int q = 0; q < KP; q++) {
+      for (int q = 0; q < kP; q++) {
         a[q] = l[q] = z;
         if (e[q].y >= 0) {
           a[q] = D.recA[e[q].x];
@@ -340,7 +458,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         }
       }
 #pragma unroll
-      for (int q = 0; q < KP; q++) term(e[q], a[q], l[q]);
+      for (int q = 0; q < kP; q++) term(e[q], a[q], l[q]);
     }
     for (; k < deg; k++) {
       const int4 e = D.cross[ell(k, col, D.N2)];
@@ -402,10 +520,13 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
 //   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
 // is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
 // Every other stress-point takes the exact flow rule.
+// With the surrogate installed both variants are launched: the one the gate selects for
+// this step runs, the other returns at once (whole blocks).
 template <bool SURR>
 __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   __shared__ float xs[4][32][16];
   __shared__ float ys[4][32][8];
+  if (D.surr && (D.surr_gate->on != 0) != SURR) return;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = i < D.NT - D.NN;
@@ -543,14 +664,34 @@ __global__ void k_fxsph(Dev D) {
 
 }  // namespace
 
-// the targets split by kind (k_split_targets) after the pair build; one launch per kind
+// dynamic shared memory of a staged-walk launch of b threads
+inline size_t staged_bytes(int b) { return (size_t)kStagedSlots * sizeof(int4) * b; }
+
+// raises the staged kernels' dynamic shared-memory limit to what their largest block needs
+// (512 threads; 256 for the derivative sums, whose launch bounds cap the block there);
+// called once per context, on its device, before any launch or capture
+int set_staged_limits() {
+  const int lim = (int)staged_bytes(512), lim256 = (int)staged_bytes(256);
+  const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaSuccess;
+  for (cudaError_t r : {cudaFuncSetAttribute(k_finterp<1, 0>, attr, lim),
+                        cudaFuncSetAttribute(k_finterp<2, 0>, attr, lim),
+                        cudaFuncSetAttribute(k_fderivs<1, 0>, attr, lim256),
+                        cudaFuncSetAttribute(k_fderivs<2, 0>, attr, lim256)})
+    if (r != cudaSuccess && e == cudaSuccess) e = r;
+  return (int)e;
+}
+
+// the targets split by kind (k_split_targets) after the pair build; one launch per kind.
+// KP 0: the staged walk; otherwise KP neighbours loaded ahead of their sums
 template <int KP>
 void launch_finterp_kp(Ctx& c) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_INTERP];
+  const size_t sm = KP == 0 ? staged_bytes(b) : 0;
   c.kernels_launched += 1;
-  if (ns > 0) k_finterp<1, KP><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, D.tgtS, ns);
-  k_finterp<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, D.tgtN, D.NN);
+  if (ns > 0) k_finterp<1, KP><<<(ns + b - 1) / b, b, sm, c.stream>>>(D, D.tgtS, ns);
+  k_finterp<2, KP><<<(D.NN + b - 1) / b, b, sm, c.stream>>>(D, D.tgtN, D.NN);
 }
 void launch_finterp(Ctx& c) {
   const Dev& D = c.d;
@@ -559,6 +700,7 @@ void launch_finterp(Ctx& c) {
     return;
   }
   switch (c.ahead[0]) {
+    case 0: launch_finterp_kp<0>(c); break;
     case 2: launch_finterp_kp<2>(c); break;
     case 8: launch_finterp_kp<8>(c); break;
     default: launch_finterp_kp<4>(c);
@@ -569,12 +711,19 @@ void launch_fderivs_kp(Ctx& c, int stage) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_DERIVS];
   c.kernels_launched += 1;
+  if (KP == 0) {
+    const size_t sm = staged_bytes(b);
+    if (ns > 0) k_fderivs<1, 0><<<(ns + b - 1) / b, b, sm, c.stream>>>(D, stage, D.tgtS, ns);
+    k_fderivs<2, 0><<<(D.NN + b - 1) / b, b, sm, c.stream>>>(D, stage, D.tgtN, D.NN);
+    return;
+  }
   // the stress-point sums (64 registers) load one neighbour ahead; more spill
   if (ns > 0) k_fderivs<1, 1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
   k_fderivs<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
 }
 void launch_fderivs(Ctx& c, int stage) {
   switch (c.ahead[1]) {
+    case 0: launch_fderivs_kp<0>(c, stage); break;
     case 1: launch_fderivs_kp<1>(c, stage); break;
     case 4: launch_fderivs_kp<4>(c, stage); break;
     default: launch_fderivs_kp<2>(c, stage);
@@ -583,8 +732,11 @@ void launch_fderivs(Ctx& c, int stage) {
 void launch_fsp_tail(Ctx& c, int stage) {
   int ns = c.d.NT - c.d.NN;
   if (ns <= 0) return;
-  if (c.d.surr) k_fsp_tail<true><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
-  else k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  if (c.d.surr) {
+    c.kernels_launched += 1;
+    k_fsp_tail<true><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  }
+  k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
   k_fxsph<<<c.grid_of(TK_XSPH, c.d.N2), c.blk[TK_XSPH], 0, c.stream>>>(c.d);

@@ -30,11 +30,16 @@ namespace {
 constexpr int kBlock = 256;
 
 // adapt_stress2: the reference's FP64 arithmetic in the plain form, the division-free
-// variant in the FP32 form
+// variant in the FP32 form, which first certifies in FP32 the stresses clearly inside the
+// cone (most of them) and leaves those unchanged without any FP64 arithmetic
 __device__ __forceinline__ void stress_return(const Dev& D, const Real& M, double& a,
                                               double& b, double& c, double& d) {
-  if (D.fast) adapt_stress_fast(M.alpha2, M.kc, M.kc_shift, a, b, c, d);
-  else adapt_stress(M.alpha2, M.kc, a, b, c, d);
+  if (D.fast) {
+    if (!inside_cone_f32(M.alpha2f, M.kcf, a, b, c, d))
+      adapt_stress_fast(M.alpha2, M.kc, M.kc_shift, a, b, c, d);
+  } else {
+    adapt_stress(M.alpha2, M.kc, a, b, c, d);
+  }
 }
 
 // FP32-form neighbour records of particle i (velocity, volume, stress, internal variable)
@@ -62,7 +67,31 @@ __global__ void k_load_scalars(Dev D) {
   for (int r = threadIdx.x; r < D.R; r += blockDim.x) D.cur[r] = D.scal_table[(size_t)k * D.R + r];
 }
 
-__global__ void k_next_step(Dev D) { *D.step_idx += 1; }
+// end of a step: the step counter, and the surrogate's gate for the next step
+__global__ void k_next_step(Dev D) {
+  *D.step_idx += 1;
+  if (!D.surr) return;
+  SurrGate& g = *D.surr_gate;
+  const unsigned long long l = D.surr_cnt[0], a = D.surr_cnt[1];
+  if (g.on) {
+    g.steps_on += 1;
+    // deltas of this step (the counters restart from 0 when the host resets them)
+    const unsigned long long dl = l >= g.load0 ? l - g.load0 : l;
+    const unsigned long long da = a >= g.ans0 ? a - g.ans0 : a;
+    if (g.min_frac > 0.0 && dl > 0 && (double)da < g.min_frac * (double)dl) {
+      g.on = 0;
+      g.wait = g.period;
+      g.period = g.period * 2 < g.max_period ? g.period * 2 : g.max_period;
+    } else if (dl > 0) {
+      g.period = 1;
+    }
+  } else {
+    g.steps_off += 1;
+    if (--g.wait <= 0) g.on = 1;
+  }
+  g.load0 = l;
+  g.ans0 = a;
+}
 
 __global__ void k_step_init(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -777,6 +806,68 @@ __global__ void k_selftest_conv(int64_t n, uint64_t seed, unsigned long long* ba
       nb++;
   }
   if (nb) atomicAdd(bad, nb);
+}
+
+// the FP32 inside-the-cone certification of the FP32 form's stress return against the FP64
+// test it stands in for, on n pseudo-random Drucker-Prager materials and stresses, a
+// quarter of them placed within a relative 1e-3 .. 1e-9 of the cone and a quarter nearly
+// hydrostatic: bad counts stresses certified inside that the FP64 test (yield >= 0 and
+// yield^2 >= J2, adapt_stress_fast) would return; certified counts the certified ones
+__global__ void k_selftest_cone(int64_t n, uint64_t seed, unsigned long long* bad,
+                                unsigned long long* certified) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  unsigned long long nb = 0, nc = 0;
+  for (; i < n; i += stride) {
+    uint64_t r1 = mix64(seed ^ (uint64_t)i), r2 = mix64(r1), r3 = mix64(r2), r4 = mix64(r3);
+    auto uni = [](uint64_t r) { return (double)(r >> 11) * 0x1.0p-53; };
+    const double tanfi = 0.05 + 1.2 * uni(r1);
+    const double coh = (r1 & 3) == 0 ? 0.0 : 1e5 * uni(mix64(r1 ^ 7));
+    const double den = sqrt(9.0 + 12.0 * (tanfi * tanfi));
+    const double alpha2 = tanfi / den, kc = (3.0 * coh) / den;
+    const double scale = exp2(-10.0 + 40.0 * uni(r2));  // stress magnitudes 1e-3 .. 1e9
+    const double p = -scale * (uni(r3) - 0.1);         // mostly compressive mean stress
+    double s0 = scale * (2.0 * uni(mix64(r3 ^ 1)) - 1.0), s1 = scale * (2.0 * uni(mix64(r3 ^ 2)) - 1.0);
+    double s2 = scale * (2.0 * uni(mix64(r3 ^ 3)) - 1.0);
+    const int mode = (int)(r4 & 3);
+    if (mode == 3) {  // nearly hydrostatic
+      const double f = exp2(-30.0 * uni(mix64(r4 ^ 5)));
+      s0 *= f;
+      s1 *= f;
+      s2 *= f;
+    }
+    // deviator (s0, s1, -(s0 + s1), s2): sxx, syy, szz around the mean p, and sxy
+    double a = p + s0, b = p + s1, d = p - (s0 + s1), c = s2;
+    if (mode == 2) {  // onto the cone, then off it by a relative 1e-3 .. 1e-9 either way
+      const double smean = ((a + b) + d) / 3.0;
+      const double d0 = a - smean, d1 = b - smean, d3 = d - smean;
+      const double sj = sqrt(c * c + 0.5 * (d0 * d0 + d1 * d1 + d3 * d3));
+      const double y = kc - 3.0 * alpha2 * smean;
+      if (sj > 0.0 && y > 0.0) {
+        const double eps = exp2(-10.0 - 20.0 * uni(mix64(r4 ^ 9))) * ((r4 & 4) ? 1.0 : -1.0);
+        const double k = (y / sj) * (1.0 + eps);
+        a = smean + k * d0;
+        b = smean + k * d1;
+        d = smean + k * d3;
+        c = k * c;
+      }
+    }
+    if (inside_cone_f32((float)alpha2, (float)kc, a, b, c, d)) {
+      nc++;
+      const double third = 1.0 / 3.0;
+      const double smean = ((a + b) + d) * third;
+      const double d0 = a - smean, d1 = b - smean, d3 = d - smean;
+      const double varj2 = fma(c, c, 0.5 * fma(d0, d0, fma(d1, d1, d3 * d3)));
+      const double yield = fma(-3.0 * alpha2, smean, kc);
+      if (yield < 0 || yield * yield < varj2) nb++;
+    }
+  }
+  if (nb) atomicAdd(bad, nb);
+  if (nc) atomicAdd(certified, nc);
+}
+
+void launch_selftest_cone(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_out) {
+  k_selftest_cone<<<152 * 8, 256, 0, c.stream>>>(n, seed, d_out, d_out + 1);
 }
 
 void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad) {

@@ -504,6 +504,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
     c.device = dev;
+    SPS_CUDA_CHECK((cudaError_t)sps::set_staged_limits());
     SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.up_stream, cudaStreamNonBlocking));
     SPS_CUDA_CHECK(cudaEventCreateWithFlags(&c.up_ready, cudaEventDisableTiming));
@@ -566,6 +567,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
       M.alpha2 = M.tanfi / den;
       M.kc = (3.0 * M.coh) / den;
       M.kc_shift = M.alpha2 > 0.0 ? M.kc / (3.0 * M.alpha2) : 0.0;
+      M.alpha2f = (float)M.alpha2;
+      M.kcf = (float)M.kc;
       for (int d = 0; d < 2; d++) {
         M.xmin_dom[d] = q.xmin_domain[d];
         M.xmax_dom[d] = q.xmax_domain[d];
@@ -1403,6 +1406,28 @@ int sps_selftest_division(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatc
   return SPS_OK;
 }
 
+int sps_selftest_cone(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatches,
+                      int64_t* certified) {
+  if (!h || !mismatches || !certified || n < 0) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  try {
+    unsigned long long* d = nullptr;
+    SPS_CUDA_CHECK(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+    SPS_CUDA_CHECK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), c.stream));
+    sps::launch_selftest_cone(c, n, seed, d);
+    SPS_CUDA_CHECK(cudaGetLastError());
+    unsigned long long v[2] = {0, 0};
+    SPS_CUDA_CHECK(cudaMemcpyAsync(v, d, sizeof(v), cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    cudaFree(d);
+    *mismatches = (int64_t)v[0];
+    *certified = (int64_t)v[1];
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
 int sps_selftest_convert(sps_ctx* h, int64_t n, uint64_t seed, int64_t* mismatches) {
   if (!h || !mismatches || n < 0) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
@@ -1448,8 +1473,9 @@ int sps_tuned_lookahead(sps_ctx* h, int32_t* ahead) {
 int sps_set_lookahead(sps_ctx* h, int32_t interp, int32_t derivs) {
   if (!h) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
-  if ((interp != 2 && interp != 4 && interp != 8) || (derivs != 1 && derivs != 2 && derivs != 4))
-    return fail(&c, SPS_ERR_ARG, "sps_set_lookahead: interp 2, 4 or 8; derivs 1, 2 or 4");
+  if ((interp != 0 && interp != 2 && interp != 4 && interp != 8) ||
+      (derivs != 0 && derivs != 1 && derivs != 2 && derivs != 4))
+    return fail(&c, SPS_ERR_ARG, "sps_set_lookahead: interp 0, 2, 4 or 8; derivs 0, 1, 2 or 4");
   try {
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     c.ahead[0] = interp;
@@ -1550,6 +1576,21 @@ void profile_run(sps::Ctx& c, int nsteps, double* t, std::vector<std::string>& k
   c.prof_events.clear();
 }
 
+// the surrogate's counters and its gate, one allocation
+constexpr size_t kSurrBytes = 4 * sizeof(unsigned long long) + sizeof(sps::SurrGate);
+
+// the gate's starting state: on, probing every step, with the context's policy
+void reset_gate(sps::Ctx& c) {
+  sps::SurrGate g = {};
+  g.on = 1;
+  g.wait = 0;
+  g.period = 1;
+  g.max_period = c.gate_max_period;
+  g.min_frac = c.gate_min_frac;
+  SPS_CUDA_CHECK(cudaMemcpyAsync(c.d.surr_gate, &g, sizeof(g), cudaMemcpyHostToDevice, c.stream));
+  SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+}
+
 // the device arrays a step carries over from the previous step (or the upload)
 std::vector<std::pair<void*, size_t>> carried_state(sps::Ctx& c) {
   sps::Dev& D = c.d;
@@ -1575,7 +1616,7 @@ std::vector<std::pair<void*, size_t>> carried_state(sps::Ctx& c) {
     v.push_back({D.recA, sizeof(float4) * NT});
     v.push_back({D.recAl, sizeof(float4) * NT});
   }
-  if (c.surr_cnt) v.push_back({c.surr_cnt, 4 * sizeof(unsigned long long)});
+  if (c.surr_cnt) v.push_back({c.surr_cnt, kSurrBytes});
   if (c.cap_cnt) v.push_back({c.cap_cnt, sizeof(unsigned long long)});
   return v;
 }
@@ -1640,7 +1681,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     // FP32 form: the neighbour sums' look-ahead (neighbours loaded before any is summed),
     // at the chosen block sizes; the two groups are timed in the same profiled steps
     if (c.precision == SPS_PREC_FP32_FAST && c.d.sp_sph) {
-      const int la[3][2] = {{2, 1}, {4, 2}, {8, 4}};
+      const int la[5][2] = {{0, 0}, {2, 1}, {2, 2}, {4, 2}, {8, 4}};
       int best_la[2] = {c.ahead[0], c.ahead[1]};
       double best_la_ms[2] = {1e300, 1e300};
       const char* names[2] = {"interp", "derivs"};
@@ -1787,7 +1828,7 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
         c.mlp_frag = static_cast<uint2*>(p);
         SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(float) * sps::MLP_BIAS));
         c.mlp_bias = static_cast<float*>(p);
-        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(unsigned long long) * 4));
+        SPS_CUDA_CHECK(cudaMalloc(&p, kSurrBytes));
         c.surr_cnt = static_cast<unsigned long long*>(p);
       }
       cudaStream_t ms = sps::mlp_stream(m);
@@ -1800,6 +1841,8 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
       c.d.mlp_frag = c.mlp_frag;
       c.d.mlp_bias = c.mlp_bias;
       c.d.surr_cnt = c.surr_cnt;
+      c.d.surr_gate = reinterpret_cast<sps::SurrGate*>(c.surr_cnt + 4);
+      reset_gate(c);
       c.d.surr_tol = o->tol;
       for (int k = 0; k < SPS_MLP_NIN; k++) {
         c.d.env_lo[k] = o->env_lo[k];
@@ -1811,6 +1854,38 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
     }
     drop_graphs(c);
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_surrogate_gate(sps_ctx* h, double min_answered, int32_t max_period) {
+  if (!h || !(min_answered <= 1.0) || max_period < 1) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  c.gate_min_frac = min_answered;
+  c.gate_max_period = max_period;
+  if (!c.surr_cnt) return SPS_OK;  // applied at install
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    reset_gate(c);
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
+int sps_surrogate_gate_stats(sps_ctx* h, int64_t* steps) {
+  if (!h || !steps) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  steps[0] = steps[1] = 0;
+  if (!c.surr_cnt) return SPS_OK;
+  try {
+    sps::SurrGate g;
+    SPS_CUDA_CHECK(cudaMemcpyAsync(&g, c.d.surr_gate, sizeof(g), cudaMemcpyDeviceToHost, c.stream));
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    steps[0] = (int64_t)g.steps_on;
+    steps[1] = (int64_t)g.steps_off;
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
   }

@@ -31,6 +31,8 @@ def gpu_lib():
                                               C.POINTER(C.c_int64)]
         lib.sps_selftest_convert.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
                                              C.POINTER(C.c_int64)]
+        lib.sps_selftest_cone.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
+                                          C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         lib.sps_autotune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
         lib.sps_profile_step.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                          C.c_char_p, C.c_int32, C.POINTER(C.c_double),
@@ -244,6 +246,14 @@ def selftest_convert(ctx, n, seed=1):
     m = C.c_int64(0)
     ctx._call("selftest_convert", ctx._h, int(n), int(seed), C.byref(m))
     return m.value
+
+
+def selftest_cone(ctx, n, seed=1):
+    """(mismatches, certified) of the FP32 form's FP32 inside-the-cone certification
+    against the FP64 test of the stress return."""
+    m, k = C.c_int64(0), C.c_int64(0)
+    ctx._call("selftest_cone", ctx._h, int(n), int(seed), C.byref(m), C.byref(k))
+    return m.value, k.value
 
 
 TUNED_KERNELS = ("half", "lists", "interp", "derivs", "adapt_bc", "stage_begin", "rk_final",

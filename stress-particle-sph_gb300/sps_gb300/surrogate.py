@@ -48,6 +48,8 @@ def _lib():
         "sps_mlp_destroy": ([vp], None),
         "sps_surrogate_install": ([vp, vp, P(SurrogateOpts)], C.c_int),
         "sps_surrogate_stats": ([vp, P(C.c_int64), C.c_int32], C.c_int),
+        "sps_surrogate_gate": ([vp, C.c_double, C.c_int32], C.c_int),
+        "sps_surrogate_gate_stats": ([vp, P(C.c_int64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -194,6 +196,23 @@ def stats(ctx, reset=False):
     if rc != _abi.SPS_OK:
         raise SpsError("sps_surrogate_stats", rc, ctx._err())
     return tuple(int(v) for v in c)
+
+
+def set_gate(ctx, min_answered=0.5, max_period=64):
+    """The network runs in a step only while it answers at least min_answered of the
+    step's loading evaluations (<= 0: always); see sps_surrogate_gate."""
+    rc = _lib().sps_surrogate_gate(ctx._h, float(min_answered), int(max_period))
+    if rc != _abi.SPS_OK:
+        raise SpsError("sps_surrogate_gate", rc, ctx._err())
+
+
+def gate_stats(ctx):
+    """(steps run with the network, steps run without it) since install."""
+    c = (C.c_int64 * 2)()
+    rc = _lib().sps_surrogate_gate_stats(ctx._h, c)
+    if rc != _abi.SPS_OK:
+        raise SpsError("sps_surrogate_gate_stats", rc, ctx._err())
+    return int(c[0]), int(c[1])
 
 
 def sample_run(prob, precision, nsteps, every, cap=50000):

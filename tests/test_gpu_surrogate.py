@@ -124,14 +124,18 @@ def test_training_lowers_loss(built_gpu, trained):
     assert err < 0.08
 
 
-def _run(prob, nsteps, precision, net=None, tol=1e-6, env=None):
+def _run(prob, nsteps, precision, net=None, tol=1e-6, env=None, gate=None, gate_steps=None):
     ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps", prob.params_copy(precision=precision))
     ctx.upload_problem(prob)
     if net is not None:
         sg.install(ctx, net, tol=tol, envelope=env)
+        if gate is not None:
+            sg.set_gate(ctx, gate)
     ctx.step(nsteps, 0.0)
     out = ctx.download()
     st = sg.stats(ctx) if net is not None else None
+    if gate_steps is not None:
+        gate_steps.extend(sg.gate_stats(ctx))
     ctx.close()
     return out, st
 
@@ -158,7 +162,8 @@ def test_trained_surrogate_within_error_bar(built_gpu, trained):
     nt = prob.ntotal
     e_fast = rel_l2(fast["stress"][:4 * nt], plain["stress"][:4 * nt])
     for tol in (1e-6, 1e-4, 1e-2):
-        sur, st = _run(prob, nsteps, _abi.SPS_PREC_FP32_FAST, net, tol=tol, env=env)
+        # the gate off: the network runs in every step, so its effect on the error shows
+        sur, st = _run(prob, nsteps, _abi.SPS_PREC_FP32_FAST, net, tol=tol, env=env, gate=0.0)
         e = rel_l2(sur["stress"][:4 * nt], plain["stress"][:4 * nt])
         ev = rel_l2(sur["vel"][:2 * nt], plain["vel"][:2 * nt])
         loading, answered, outside, rejected = st
@@ -169,3 +174,31 @@ def test_trained_surrogate_within_error_bar(built_gpu, trained):
         assert loading > 0
         if tol == 1e-6:
             assert e <= max(3.0 * e_fast, 1e-4), (e, e_fast)
+
+
+def test_gate_skips_steps_where_the_network_does_not_answer(built_gpu, trained):
+    # every prediction rejected (tol < 0): after the first step with loading evaluations the
+    # gate closes, and it reopens for single steps at doubling intervals; the results stay
+    # those of the FP32 form without the network
+    net, train, _, _ = trained
+    prob = cases.column(dx=0.004, **EVAL_MATERIAL)
+    env = sg.Envelope.of(train)
+    n = 60
+    steps = []
+    a, st = _run(prob, n, _abi.SPS_PREC_FP32_FAST, net, tol=-1.0, env=env, gate_steps=steps)
+    b, _ = _run(prob, n, _abi.SPS_PREC_FP32_FAST)
+    for k in ("x", "vel", "stress", "f_drucker", "intvars1"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    on, off = steps
+    assert on + off == n and 3 <= on <= 10, steps
+    assert st[0] > 0 and st[1] == 0
+    # the gate off: the network runs in every step
+    steps = []
+    _run(prob, 20, _abi.SPS_PREC_FP32_FAST, net, tol=-1.0, env=env, gate=0.0, gate_steps=steps)
+    assert steps == [20, 0]
+    # steps that pass keep the network on (every prediction inside the envelope accepted,
+    # a threshold that any answered evaluation meets)
+    steps = []
+    _, st = _run(prob, 20, _abi.SPS_PREC_FP32_FAST, net, tol=1e30, env=env, gate=1e-6,
+                 gate_steps=steps)
+    assert st[1] > 0 and steps == [20, 0], (st, steps)
