@@ -17,8 +17,9 @@ e2e    = the same metric through the C-ABI with host buffers: every step uploads
          state from pinned host memory (sps_upload), advances one step (sps_step) and
          downloads the fields (sps_download).
 --impl reference times the CPU restatement of the reference's step (the oracle; the
-         Fortran reference cannot be compiled on either machine) on a bounded sample, as
-         independent single-threaded replicas on every host core the process may use.
+         Fortran reference cannot be compiled on either machine) on the same workload, on
+         one host thread as the single-threaded reference runs, for a bounded number of
+         steps (min(K, 2) after min(W, 1) warm-up).
 
 The headline runs the FP32 form with the learned Drucker-Prager surrogate installed
 (trained first, on the GPU, on tuples captured from coarse runs of the same slope with
@@ -598,6 +599,69 @@ def rel_errors(a, b):
             float(np.abs(d).max() / max(np.abs(b).max(), 1e-300)))
 
 
+def e2e_through_abi(ctx, prob, nparticles, args, dist, world):
+    """The metric end to end through the C-ABI with host buffers: every step uploads the
+    state from pinned host memory, advances one step and brings the result to the host."""
+    import numpy as np
+    import torch
+    st = prob.state()
+    pinned = {}
+    for k, v in st.items():
+        tt = torch.empty(v.size, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
+                         pin_memory=True)
+        a = tt.numpy()
+        a[:] = v
+        pinned[k] = (tt, a)
+    h2d = sum(a.nbytes for _, a in pinned.values())
+    outs = {}
+    for k, v in ctx.download().items():
+        tt = torch.empty(v.size, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
+                         pin_memory=True)
+        outs[k] = (tt, tt.numpy())
+    out = {k: a for k, (_, a) in outs.items()}
+    d2h = sum(a.nbytes for a in out.values())
+    inputs = {k: a for k, (_, a) in pinned.items()}
+    ctx.upload(**inputs)
+    torch.cuda.synchronize()
+
+    def e2e_sync():
+        te = 0.0
+        for _ in range(args.e2e_steps):
+            ctx.upload(**inputs)
+            te = ctx.step(1, te)
+            ctx.download(out=out)
+
+    def e2e_pipelined():
+        # the result of step k copies out to pinned host memory on the second stream while
+        # step k+1's inputs copy in and step k+1 runs; the host reads it in place
+        te = 0.0
+        for k in range(args.e2e_steps):
+            ctx.upload(**inputs)
+            te = ctx.step(1, te)
+            if k:
+                ctx.snapshot_view()
+            ctx.snapshot()
+        ctx.snapshot_view()
+
+    runs = {}
+    for name, fn in (("sync", e2e_sync), ("pipelined", e2e_pipelined)):
+        fn()  # warm-up (first-touch of the snapshot buffers)
+        barrier(dist)
+        w0 = time.perf_counter()
+        fn()
+        w1 = time.perf_counter()
+        runs[name] = reduce_max(dist, w1 - w0, device="cuda")
+    return {"value": round(nparticles * args.e2e_steps * world / runs["pipelined"], 1),
+            "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+            "path": "every step: sps_upload from pinned host arrays, sps_step(1), "
+                    "sps_snapshot of the result (free surface, device pack in the download "
+                    "layout, copy to pinned host memory on a second stream overlapping the "
+                    "next step's upload and step), sps_snapshot_view of it on the host",
+            "sync": {"value": round(nparticles * args.e2e_steps * world / runs["sync"], 1),
+                     "path": "sps_upload + sps_step(1) + sps_download into pinned arrays"}}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -628,20 +692,36 @@ def run_ours(args):
     kps = sps_gb300.kernels_per_step(ctx)
     if use_surr:
         sg.stats(ctx, reset=True)
+        g0 = sg.gate_stats(ctx)
     t, ms_max, clk = timed_steps(ctx, args.steps, t, dist, local, mark=True)
     value = nparticles * args.steps * world / (ms_max * 1e-3)
     nsteps_done = max(args.warmup, 1) + args.steps
+    f_head = ctx.download()  # the headline run's fields after nsteps_done steps
     if use_surr:
         loading, answered, outside, rejected = sg.stats(ctx)
+        g1 = sg.gate_stats(ctx)
         lf = max(loading, 1)
         surr = {"tol": args.surrogate_tol,
                 "drift_test": "dt |grad f : (D:e + Gs)| / sqrt(J2) <= tol",
                 "training": training,
-                "timed_loading_evaluations": loading,
+                "gate": {"min_answered": 0.5, "max_period": 64,
+                         "timed_steps_with_network": g1[0] - g0[0],
+                         "timed_steps_without": g1[1] - g0[1]},
+                "timed_loading_evaluations_with_network": loading,
                 "answered_frac": round(answered / lf, 6),
                 "outside_envelope_frac": round(outside / lf, 6),
                 "drift_rejected_frac": round(rejected / lf, 6),
                 "fallback_rate": round(1.0 - answered / lf, 6)}
+        # the same context without the network (same launch shapes, state and size), then
+        # the network installed again for the rest of the run
+        sg.install(ctx, None)
+        t = ctx.step(2, t)
+        t, ms_n, _ = timed_steps(ctx, args.steps, t, dist, local)
+        surr["same_context_without_network"] = {
+            "value": round(nparticles * args.steps * world / (ms_n * 1e-3), 1),
+            "ms_per_step": round(ms_n / args.steps, 4)}
+        surr["speed_with_over_without"] = round(ms_n / ms_max, 4)
+        sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
 
     plain = None
     errors = None
@@ -654,7 +734,7 @@ def run_ours(args):
         tp, ms_p, _ = timed_steps(cp, args.steps, tp, dist, local)
         plain = {"value": round(nparticles * args.steps * world / (ms_p * 1e-3), 1),
                  "ms_per_step": round(ms_p / args.steps, 4), "dtype": "f64"}
-        ff, fp = ctx.download(), cp.download()
+        ff, fp = f_head, cp.download()
         nt = prob.ntotal
 
         def errs(a, b):
@@ -671,19 +751,12 @@ def run_ours(args):
             cn = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
                                        prob.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
             cn.upload_problem(prob)
-            sps_gb300.autotune(cn, 2)
-            tn = cn.step(max(args.warmup, 1), 0.0)
-            tn, ms_n, _ = timed_steps(cn, args.steps, tn, dist, local)
-            v_n = nparticles * args.steps * world / (ms_n * 1e-3)
-            surr["fp32_without_surrogate"] = {
-                "value": round(v_n, 1), "ms_per_step": round(ms_n / args.steps, 4),
-                "error_vs_plain": errs(cn.download(), fp)}
-            surr["speed_with_over_without"] = round(value / v_n, 4)
+            cn.step(nsteps_done, 0.0)
+            surr["fp32_without_surrogate"] = {"error_vs_plain": errs(cn.download(), fp)}
             cn.close()
         _, prof_p = sps_gb300.profile_steps(cp, 1, tp)
         plain["kernel_ms_per_step"] = {k: round(v[0], 4) for k, v in sorted(
             prof_p.items(), key=lambda kv: -kv[1][0])[:6]}
-        cp.close()
 
     # per-kernel profile of two steps (events around every kernel, no graph)
     t, prof = sps_gb300.profile_steps(ctx, 2, t)
@@ -724,62 +797,11 @@ def run_ours(args):
         f64 = None
 
     # end to end through the C-ABI with pinned host buffers
-    st = prob.state()
-    pinned = {}
-    for k, v in st.items():
-        tt = torch.empty(v.size, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
-                         pin_memory=True)
-        a = tt.numpy()
-        a[:] = v
-        pinned[k] = (tt, a)
-    h2d = sum(a.nbytes for _, a in pinned.values())
-    outs = {}
-    for k, v in ctx.download().items():
-        tt = torch.empty(v.size, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
-                         pin_memory=True)
-        outs[k] = (tt, tt.numpy())
-    out = {k: a for k, (_, a) in outs.items()}
-    d2h = sum(a.nbytes for a in out.values())
-    inputs = {k: a for k, (_, a) in pinned.items()}
-    ctx.upload(**inputs)
-    torch.cuda.synchronize()
-
-    def e2e_sync():
-        te = 0.0
-        for _ in range(args.e2e_steps):
-            ctx.upload(**inputs)
-            te = ctx.step(1, te)
-            ctx.download(out=out)
-
-    def e2e_pipelined():
-        # the result of step k copies out to pinned host memory on the second stream while
-        # step k+1's inputs copy in and step k+1 runs; the host reads it in place
-        te = 0.0
-        for k in range(args.e2e_steps):
-            ctx.upload(**inputs)
-            te = ctx.step(1, te)
-            if k:
-                ctx.snapshot_view()
-            ctx.snapshot()
-        ctx.snapshot_view()
-
-    e2e_runs = {}
-    for name, fn in (("sync", e2e_sync), ("pipelined", e2e_pipelined)):
-        fn()  # warm-up (first-touch of the snapshot buffers)
-        barrier(dist)
-        w0 = time.perf_counter()
-        fn()
-        w1 = time.perf_counter()
-        e2e_runs[name] = reduce_max(dist, w1 - w0, device="cuda")
-    e2e = {"value": round(nparticles * args.e2e_steps * world / e2e_runs["pipelined"], 1),
-           "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-           "path": "every step: sps_upload from pinned host arrays, sps_step(1), "
-                   "sps_snapshot of the result (free surface, device pack in the download "
-                   "layout, copy to pinned host memory on a second stream overlapping the "
-                   "next step's upload and step), sps_snapshot_view of it on the host",
-           "sync": {"value": round(nparticles * args.e2e_steps * world / e2e_runs["sync"], 1),
-                    "path": "sps_upload + sps_step(1) + sps_download into pinned arrays"}}
+    e2e = e2e_through_abi(ctx, prob, nparticles, args, dist, world)
+    if fast:
+        cp.upload_problem(prob)
+        plain["e2e"] = e2e_through_abi(cp, prob, nparticles, args, dist, world)
+        cp.close()
 
     batch = None
     if fast and not args.no_batch:
@@ -804,7 +826,10 @@ def run_ours(args):
                            (prob.ntotal2 * (3 * 48 * 16 + 400)) / 1e9),
                        "surrogate": ("learned Drucker-Prager flow rule, exact fallback "
                                      "(tol %g)" % args.surrogate_tol if use_surr else "off"),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "free_surface": "the timed steps skip get_nodes_on_free_surface, which "
+                                       "nothing in this workload's step reads; e2e detects it "
+                                       "for every step's output (in FP32 in the FP32 form)"},
             "plain": plain, "error_vs_plain": errors, "surrogate": surr, "batch": batch,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
             "autotuned_blocks": tuned, "algorithmic_bytes_per_launch": alg_bytes,
@@ -844,42 +869,43 @@ def cpu_baseline(args):
             "sample": sample}
 
 
-def _replica(seconds):
-    for p in (os.path.join(ROOT, "stress-particle-sph_gb300"), os.path.join(ROOT, "oracle")):
-        if p not in sys.path:
-            sys.path.insert(0, p)
-    v, sample, steps = cpu_sample(seconds_target=seconds)
-    return v, sample, steps
-
-
 def run_reference(args):
+    """The reference's CPU implementation of the step on the same workload as the GPU arm:
+    the oracle (the C restatement of the reference's single-threaded Fortran step; no
+    Fortran compiler exists on either machine) on the full slope, one host thread, as the
+    reference runs.  A step takes about a minute there, so the timed steps are bounded:
+    min(warmup, 1) untimed and min(steps, 2) timed."""
     rank, world, dist = dist_init("gloo")
     if rank != 0:
         return
-    import multiprocessing as mp
     import orc
     orc.build()
     import sps_gb300
     sps_gb300.build_host()
-    try:
-        cores = len(os.sched_getaffinity(0))
-    except AttributeError:
-        cores = os.cpu_count() or 1
-    seconds = min(60.0, max(10.0, 3.0 * args.steps))
-    # the reference step is single-threaded: one independent replica per host core
-    with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(_replica, [seconds] * cores)
-    v = sum(r[0] for r in res)
-    sample = "%d concurrent replicas (one per core) of: %s" % (cores, res[0][1])
-    steps = min(r[2] for r in res)
+    prob = workload(args.dx)
+    ctx = orc.context(prob.params_copy())
+    ctx.upload_problem(prob)
+    warm, steps = min(args.warmup, 1), max(1, min(args.steps, 2))
+    t = ctx.step(warm, 0.0) if warm else 0.0
+    w0 = time.perf_counter()
+    t = ctx.step(steps, t)
+    el = time.perf_counter() - w0
+    n = prob.nnode + prob.nstress
+    v = n * steps / el
+    sample = ("oracle (C restatement of the reference step, 1 thread, as the single-threaded "
+              "reference runs) on the full workload: %d untimed + %d timed steps in %.1f s"
+              % (warm, steps, el))
     line = {
         "metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world,
-        "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "impl": "reference",
-        "config": {"workload": "vertical slope (same geometry and material), coarser sample",
-                   "precision": "fp64 (reference mixed precision)"},
-        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": cores,
+        "steps": steps, "warmup": warm, "ms_per_step": round(1e3 * el / steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (generated slope geometry, no dataset)", "impl": "reference",
+        "config": {"workload": workload_name(prob, args.dx),
+                   "precision": "fp64 (reference mixed precision)",
+                   "particles": n, "same_as_gpu_arm": True,
+                   "bounded": "steps limited to min(K, 2) after min(W, 1) warm-up (about a "
+                              "minute per step on one core)"},
+        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": 1,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},

@@ -221,17 +221,14 @@ int sps_selftest_cone(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatche
    order depends on it. */
 int sps_autotune(sps_ctx* ctx, int32_t nsteps, int32_t* blocks);
 
-/* How the FP32 form's neighbour sums walk their lists, as sps_autotune chose it after the
-   block sizes (no reference counterpart): ahead[0] for the interpolation, ahead[1] for
-   the derivative sums.  0: the staged walk -- every thread copies its list entries into
-   shared memory with asynchronous copies (cp.async) eight entries ahead of its sum, and
-   loads the records of two neighbours at a time; 2, 4 or 8 (interpolation), 1, 2 or 4
-   (derivatives): that many neighbours' entries and records are loaded before any of them
-   is summed.  Every choice sums the neighbours in the same order, so the results do not
-   depend on it.  Defaults before tuning: 4 and 2. */
+/* The look-ahead of the FP32 form's neighbour sums that sps_autotune chose after the
+   block sizes (no reference counterpart): ahead[0] neighbours a pass in the interpolation
+   (2, 4 or 8), ahead[1] in the node derivative sums (1, 2 or 4); a pass loads its
+   neighbours' list entries and records before it sums any of them, in the same order, so
+   the results do not depend on these.  Defaults before tuning: 4 and 2. */
 int sps_tuned_lookahead(sps_ctx* ctx, int32_t* ahead);
 
-/* Sets that choice directly (interp 0, 2, 4 or 8; derivs 0, 1, 2 or 4), e.g. to reuse the
+/* Sets that look-ahead directly (interp 2, 4 or 8; derivs 1, 2 or 4), e.g. to reuse the
    values tuned on one context in another of the same workload. */
 int sps_set_lookahead(sps_ctx* ctx, int32_t interp, int32_t derivs);
 

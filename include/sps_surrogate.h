@@ -114,7 +114,8 @@ int sps_surrogate_install(sps_ctx* ctx, sps_mlp* m, const sps_surrogate_opts* op
 
 /* The gate that keeps the network from costing time where it does not pay (no reference
    counterpart): a step runs the network only while it answers at least min_answered of
-   that step's loading evaluations; after a step below that, the exact rule alone runs for
+   that step's loading evaluations (a step without loading evaluations counts as below:
+   the network had nothing to answer); after a step below that, the exact rule alone runs for
    a period of steps and then the network is tried for one step again, the period
    doubling up to max_period steps while these tries keep failing and returning to 1 after
    one that passes.  The decision is taken on the device at the end of every step.

@@ -83,6 +83,7 @@ struct Real {
   int ntype_eco, ncrit, ntype_solid, ic_grav;
   double dt, dx, alpha, beta, damping;
   double D11, D12, D22, D33, D41, D42;
+  float D11f, D12f, D22f, D33f, D41f, D42f;  // the same rounded to FP32 (FP32 form's rates)
   double tanfi, coh, young, poiss;
   double alpha2, kc;  // adapt_stress2 constants (FP64)
   float alpha2f, kcf; // the same rounded to FP32 (the FP32 form's inside-the-cone test)
@@ -109,7 +110,8 @@ enum ErrBits : int {
 };
 
 // The surrogate's gate (sps_surrogate_gate): the network runs in a step only while it
-// answers at least min_frac of the step's loading evaluations.  After a step below that it
+// answers at least min_frac of the step's loading evaluations (a step without any counts as
+// below).  After a step below that it
 // is off for `period` steps and then runs one step again (a probe); the period doubles, up
 // to max_period, while probes keep failing, and returns to 1 after a step that passes.
 // Updated on the device at the end of every step, so no host synchronisation is needed.
@@ -749,7 +751,6 @@ void launch_vol(Ctx& c, int lo, int hi);
 void launch_finterp(Ctx& c);
 void launch_fderivs(Ctx& c, int stage);
 void launch_fsp_tail(Ctx& c, int stage);
-int set_staged_limits();  // cudaError_t of raising the staged walk's shared-memory limits
 void launch_surface(Ctx& c);
 void launch_surface_f32(Ctx& c);
 void launch_lists_keys(Ctx& c);

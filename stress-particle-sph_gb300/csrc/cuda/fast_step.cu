@@ -55,66 +55,6 @@ __device__ __forceinline__ float dfdiff(float ah, float al, float bh, float bl) 
   return (ah - bh) + (al - bl);
 }
 
-// ---- the staged neighbour walk ------------------------------------------------------------
-// A neighbour sum waits on two dependent loads per neighbour: its list entry, streamed from
-// DRAM, and then the neighbour's records, gathered mostly from L1/L2.  In the staged walk
-// every thread copies its own list entries into shared memory with cp.async, kDE entries
-// ahead of the one it sums, so that the DRAM stream runs in the background; the records of
-// kSP entries at a time are then loaded together from the staged entries.  A thread reads
-// only its own slots, so no barrier between threads is needed, and the neighbours are
-// summed in list order, so every result bit is that of the direct walk.
-constexpr int kDE = 8, kSP = 2;
-static_assert(kDE % kSP == 0, "entries are staged in groups of kSP");
-constexpr int kStagedSlots = kDE;  // 16-byte shared-memory slots per thread
-
-__device__ __forceinline__ void cp_async16_cg(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-// Walks the deg entries of list column col in order.  load(e, r0, r1) loads the records of
-// entry e's neighbour (issued for kSP entries before any is summed); sum(e, r0, r1) adds
-// it.  smem: kDE x blockDim.x 16-byte slots.  Group g of the cp.async groups holds entries
-// g kSP .. g kSP + kSP - 1: the prologue commits groups 0 .. kDE/kSP - 1, pass m commits
-// group m + kDE/kSP, and pass m waits for group m.
-template <class Load, class Sum>
-__device__ __forceinline__ void staged_walk(const int4* __restrict__ list, int col, int N2,
-                                            int deg, int4* smem, Load load, Sum sum) {
-  const int B = blockDim.x, tid = threadIdx.x;
-  for (int g = 0; g < kDE / kSP; g++) {
-    for (int q = 0; q < kSP; q++) {
-      const int k = g * kSP + q;
-      if (k < deg) cp_async16_cg(&smem[k * B + tid], &list[ell(k, col, N2)]);
-    }
-    cp_async_commit();
-  }
-  for (int k = 0; k < deg; k += kSP) {
-    cp_async_wait<kDE / kSP - 1>();
-    float4 r0[kSP], r1[kSP];
-#pragma unroll
-    for (int q = 0; q < kSP; q++)
-      if (k + q < deg) load(smem[((k + q) % kDE) * B + tid], r0[q], r1[q]);
-    // the entries are read again for the sums rather than kept in registers
-    asm volatile("" ::: "memory");
-#pragma unroll
-    for (int q = 0; q < kSP; q++)
-      if (k + q < deg) sum(smem[((k + q) % kDE) * B + tid], r0[q], r1[q]);
-#pragma unroll
-    for (int q = 0; q < kSP; q++)
-      if (k + q + kDE < deg)
-        cp_async16_cg(&smem[((k + q) % kDE) * B + tid], &list[ell(k + q + kDE, col, N2)]);
-    cp_async_commit();
-  }
-  cp_async_wait<0>();
-}
-
 // stress_point_update (2_SPH_main_2018.f90:403-482), FP32 sums.  A stress-point's velocity
 // is the weighted mean of its nodes' velocities; it is formed as the first node's velocity
 // plus the weighted mean of the deviations, which are small and exact in double-float.
@@ -168,24 +108,9 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
       nm.add(h2);
     };
-    if (KP == 0) {  // the staged walk: records {recV, recI} of the non-wall partners
-      extern __shared__ int4 staged_smem[];
-      staged_walk(
-          D.cross, col, D.N2, deg, staged_smem,
-          [&](const int4& e, float4& r, float4& ri) {
-            if (e.y >= 0) {
-              r = D.recV[e.x];
-              ri = D.recI[e.x];
-            }
-          },
-          [&](const int4& e, const float4& r, const float4& ri) {
-            if (e.y >= 0) term(__int_as_float(e.y), r, ri.y);
-          });
-      deg = 0;  // walked
-    }
     // kP neighbours a pass: their entries and records are loaded before any is summed, so
     // that the loads overlap (the sum order is unchanged)
-    constexpr int kP = KP > 0 ? KP : 1;
+    constexpr int kP = KP;
     int k = 0;
     for (; k + kP - 1 < deg; k += kP) {
       int4 e[kP];
@@ -228,22 +153,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
     };
-    if (KP == 0) {  // the staged walk: records {recS, recI} of the non-wall partners
-      extern __shared__ int4 staged_smem[];
-      staged_walk(
-          D.cross, col, D.N2, deg, staged_smem,
-          [&](const int4& e, float4& rs, float4& ri) {
-            if (e.y >= 0) {
-              rs = D.recS[e.x];
-              ri = D.recI[e.x];
-            }
-          },
-          [&](const int4& e, const float4& rs, const float4& ri) {
-            if (e.y >= 0) term(__int_as_float(e.y), rs, ri);
-          });
-      deg = 0;  // walked
-    }
-    constexpr int kP = KP > 0 ? KP : 1;  // neighbours a pass, as above
+    constexpr int kP = KP;  // neighbours a pass, as above
     int k = 0;
     for (; k + kP - 1 < deg; k += kP) {
       int4 e[kP];
@@ -289,7 +199,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets
 // KP: neighbours a pass, loaded before any is summed (as in k_finterp)
 template <int KIND, int KP>
-__global__ void __launch_bounds__(256, KIND == 1 ? 4 : (KP == 0 ? 2 : 3)) k_fderivs(Dev D, int stage,
+__global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int stage,
                                                     const int32_t* __restrict__ tgt, int ntgt) {
   const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (k0 >= ntgt) return;
@@ -346,32 +256,20 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : (KP == 0 ? 2 : 3)) k_fder
       }
     };
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (KP == 0) {  // the staged walk: records {recV, recI}; a wall partner reads its volume
-      extern __shared__ int4 staged_smem[];
-      staged_walk(
-          D.cross, col, D.N2, deg, staged_smem,
-          [&](const int4& e, float4& r, float4& ri) {
-            ri = D.recI[e.x];
-            r = e.y >= 0 ? D.recV[e.x] : z;
-          },
-          [&](const int4& e, const float4& r, const float4& ri) { term(e, ri.y, r); });
-      deg = 0;  // walked
-    }
-    constexpr int kP = KP > 0 ? KP : 1;
     int k = 0;
-    for (; k + kP - 1 < deg; k += kP) {
-      int4 e[kP];
-      float vol[kP];
-      float4 r[kP];
+    for (; k + KP - 1 < deg; k += KP) {
+      int4 e[KP];
+      float vol[KP];
+      float4 r[KP];
 #pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
+      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
 #pragma unroll
-      for (int q = 0; q < kP; q++) {
+      for (int q = 0; q < KP; q++) {
         vol[q] = D.recI[e[q].x].y;
         r[q] = e[q].y >= 0 ? D.recV[e[q].x] : z;
       }
 #pragma unroll
-      for (int q = 0; q < kP; q++) term(e[q], vol[q], r[q]);
+      for (int q = 0; q < KP; q++) term(e[q], vol[q], r[q]);
     }
     for (; k < deg; k++) {
       const int4 e = D.cross[ell(k, col, D.N2)];
@@ -425,32 +323,16 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : (KP == 0 ? 2 : 3)) k_fder
       sx.add(m, dwx);
       sy.add(m, dwy);
     };
-    if (KP == 0) {  // the staged walk: records {recA, recAl} of the non-wall partners
-      extern __shared__ int4 staged_smem[];
-      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      staged_walk(
-          D.cross, col, D.N2, deg, staged_smem,
-          [&](const int4& e, float4& a, float4& l) {
-            a = l = z;
-            if (e.y >= 0) {
-              a = D.recA[e.x];
-              l = D.recAl[e.x];
-            }
-          },
-          [&](const int4& e, const float4& a, const float4& l) { term(e, a, l); });
-      deg = 0;  // walked
-    }
     // KP neighbours a pass: entries and records loaded before any is summed
-    constexpr int kP = KP > 0 ? KP : 1;
     int k = 0;
-    for (; k + kP - 1 < deg; k += kP) {
+    for (; k + KP - 1 < deg; k += KP) {
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      int4 e[kP];
-      float4 a[kP], l[kP];
+      int4 e[KP];
+      float4 a[KP], l[KP];
 #pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
+      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
 #pragma unroll
-      for (int q = 0; q < kP; q++) {
+      for (int q = 0; q < KP; q++) {
         a[q] = l[q] = z;
         if (e[q].y >= 0) {
           a[q] = D.recA[e[q].x];
@@ -458,7 +340,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : (KP == 0 ? 2 : 3)) k_fder
         }
       }
 #pragma unroll
-      for (int q = 0; q < kP; q++) term(e[q], a[q], l[q]);
+      for (int q = 0; q < KP; q++) term(e[q], a[q], l[q]);
     }
     for (; k < deg; k++) {
       const int4 e = D.cross[ell(k, col, D.N2)];
@@ -664,34 +546,14 @@ __global__ void k_fxsph(Dev D) {
 
 }  // namespace
 
-// dynamic shared memory of a staged-walk launch of b threads
-inline size_t staged_bytes(int b) { return (size_t)kStagedSlots * sizeof(int4) * b; }
-
-// raises the staged kernels' dynamic shared-memory limit to what their largest block needs
-// (512 threads; 256 for the derivative sums, whose launch bounds cap the block there);
-// called once per context, on its device, before any launch or capture
-int set_staged_limits() {
-  const int lim = (int)staged_bytes(512), lim256 = (int)staged_bytes(256);
-  const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t e = cudaSuccess;
-  for (cudaError_t r : {cudaFuncSetAttribute(k_finterp<1, 0>, attr, lim),
-                        cudaFuncSetAttribute(k_finterp<2, 0>, attr, lim),
-                        cudaFuncSetAttribute(k_fderivs<1, 0>, attr, lim256),
-                        cudaFuncSetAttribute(k_fderivs<2, 0>, attr, lim256)})
-    if (r != cudaSuccess && e == cudaSuccess) e = r;
-  return (int)e;
-}
-
-// the targets split by kind (k_split_targets) after the pair build; one launch per kind.
-// KP 0: the staged walk; otherwise KP neighbours loaded ahead of their sums
+// the targets split by kind (k_split_targets) after the pair build; one launch per kind
 template <int KP>
 void launch_finterp_kp(Ctx& c) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_INTERP];
-  const size_t sm = KP == 0 ? staged_bytes(b) : 0;
   c.kernels_launched += 1;
-  if (ns > 0) k_finterp<1, KP><<<(ns + b - 1) / b, b, sm, c.stream>>>(D, D.tgtS, ns);
-  k_finterp<2, KP><<<(D.NN + b - 1) / b, b, sm, c.stream>>>(D, D.tgtN, D.NN);
+  if (ns > 0) k_finterp<1, KP><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, D.tgtS, ns);
+  k_finterp<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, D.tgtN, D.NN);
 }
 void launch_finterp(Ctx& c) {
   const Dev& D = c.d;
@@ -700,7 +562,6 @@ void launch_finterp(Ctx& c) {
     return;
   }
   switch (c.ahead[0]) {
-    case 0: launch_finterp_kp<0>(c); break;
     case 2: launch_finterp_kp<2>(c); break;
     case 8: launch_finterp_kp<8>(c); break;
     default: launch_finterp_kp<4>(c);
@@ -711,19 +572,12 @@ void launch_fderivs_kp(Ctx& c, int stage) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_DERIVS];
   c.kernels_launched += 1;
-  if (KP == 0) {
-    const size_t sm = staged_bytes(b);
-    if (ns > 0) k_fderivs<1, 0><<<(ns + b - 1) / b, b, sm, c.stream>>>(D, stage, D.tgtS, ns);
-    k_fderivs<2, 0><<<(D.NN + b - 1) / b, b, sm, c.stream>>>(D, stage, D.tgtN, D.NN);
-    return;
-  }
   // the stress-point sums (64 registers) load one neighbour ahead; more spill
   if (ns > 0) k_fderivs<1, 1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
   k_fderivs<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
 }
 void launch_fderivs(Ctx& c, int stage) {
   switch (c.ahead[1]) {
-    case 0: launch_fderivs_kp<0>(c, stage); break;
     case 1: launch_fderivs_kp<1>(c, stage); break;
     case 4: launch_fderivs_kp<4>(c, stage); break;
     default: launch_fderivs_kp<2>(c, stage);

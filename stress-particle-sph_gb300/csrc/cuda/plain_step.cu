@@ -78,11 +78,13 @@ __global__ void k_next_step(Dev D) {
     // deltas of this step (the counters restart from 0 when the host resets them)
     const unsigned long long dl = l >= g.load0 ? l - g.load0 : l;
     const unsigned long long da = a >= g.ans0 ? a - g.ans0 : a;
-    if (g.min_frac > 0.0 && dl > 0 && (double)da < g.min_frac * (double)dl) {
+    // a step without loading evaluations gave the network nothing to answer: it counts as
+    // a step that did not pay
+    if (g.min_frac > 0.0 && (dl == 0 || (double)da < g.min_frac * (double)dl)) {
       g.on = 0;
       g.wait = g.period;
       g.period = g.period * 2 < g.max_period ? g.period * 2 : g.max_period;
-    } else if (dl > 0) {
+    } else {
       g.period = 1;
     }
   } else {

@@ -504,7 +504,6 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
     c.device = dev;
-    SPS_CUDA_CHECK((cudaError_t)sps::set_staged_limits());
     SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     SPS_CUDA_CHECK(cudaStreamCreateWithFlags(&c.up_stream, cudaStreamNonBlocking));
     SPS_CUDA_CHECK(cudaEventCreateWithFlags(&c.up_ready, cudaEventDisableTiming));
@@ -559,6 +558,12 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
       M.D33 = q.D33;
       M.D41 = q.D41;
       M.D42 = q.D42;
+      M.D11f = (float)q.D11;
+      M.D12f = (float)q.D12;
+      M.D22f = (float)q.D22;
+      M.D33f = (float)q.D33;
+      M.D41f = (float)q.D41;
+      M.D42f = (float)q.D42;
       M.tanfi = q.props[12];
       M.coh = q.props[13];
       M.young = q.props[2];
@@ -1473,9 +1478,8 @@ int sps_tuned_lookahead(sps_ctx* h, int32_t* ahead) {
 int sps_set_lookahead(sps_ctx* h, int32_t interp, int32_t derivs) {
   if (!h) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
-  if ((interp != 0 && interp != 2 && interp != 4 && interp != 8) ||
-      (derivs != 0 && derivs != 1 && derivs != 2 && derivs != 4))
-    return fail(&c, SPS_ERR_ARG, "sps_set_lookahead: interp 0, 2, 4 or 8; derivs 0, 1, 2 or 4");
+  if ((interp != 2 && interp != 4 && interp != 8) || (derivs != 1 && derivs != 2 && derivs != 4))
+    return fail(&c, SPS_ERR_ARG, "sps_set_lookahead: interp 2, 4 or 8; derivs 1, 2 or 4");
   try {
     SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     c.ahead[0] = interp;
@@ -1681,7 +1685,7 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
     // FP32 form: the neighbour sums' look-ahead (neighbours loaded before any is summed),
     // at the chosen block sizes; the two groups are timed in the same profiled steps
     if (c.precision == SPS_PREC_FP32_FAST && c.d.sp_sph) {
-      const int la[5][2] = {{0, 0}, {2, 1}, {2, 2}, {4, 2}, {8, 4}};
+      const int la[4][2] = {{2, 1}, {2, 2}, {4, 2}, {8, 4}};
       int best_la[2] = {c.ahead[0], c.ahead[1]};
       double best_la_ms[2] = {1e300, 1e300};
       const char* names[2] = {"interp", "derivs"};

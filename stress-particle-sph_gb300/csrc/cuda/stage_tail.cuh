@@ -104,10 +104,12 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
     const Real& M = real_of(D, t);
     const double g11 = g[0], g21 = g[1], g12 = g[2], g22 = g[3];
     double div1[4];
-    div1[0] = -(M.D11 * g11 + M.D12 * g22);
-    div1[1] = -(M.D12 * g11 + M.D22 * g22);
-    div1[2] = -(M.D33 * g21 + M.D33 * g12);
-    div1[3] = -(M.D41 * g11 + M.D42 * g22);
+    if (!FAST) {
+      div1[0] = -(M.D11 * g11 + M.D12 * g22);
+      div1[1] = -(M.D12 * g11 + M.D22 * g22);
+      div1[2] = -(M.D33 * g21 + M.D33 * g12);
+      div1[3] = -(M.D41 * g11 + M.D42 * g22);
+    }
     // plastic_terms (3_SPH_material_2018.f90:1884-1954)
     double st[4] = {D.s0[t], D.s1[t], D.s2[t], D.s3[t]};
     double Gs[4] = {0.0, 0.0, 0.0, 0.0}, der = 0.0;
@@ -150,18 +152,42 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
       for (int k = 0; k < 4; k++) Gs[k] = Gs_net[k];
       der = der_net;
     }
-    double spin[4] = {0.0, 0.0, 0.0, 0.0};
-    if (D.update_x) {
-      double om1 = 0.5 * (g12 - g21);
-      double om2 = -0.5 * (g12 - g21);
-      spin[0] = 2.0 * om1 * st[2];
-      spin[1] = 2.0 * om2 * st[2];
-      spin[2] = om2 * st[0] + om1 * st[1];
-    }
-    for (int k = 0; k < 4; k++) {
-      double rhs = (-div1[k] + spin[k]) + Gs[k];
-      D.RHS1[k][t] = rhs;
-      D.RKs[k][t] = D.RKs[k][t] + f2 * rhs;
+    if (FAST) {
+      // the FP32 form: the elastic rate, the spin and the right-hand side in FP32 (the
+      // gradient comes from FP32 neighbour sums and carries their accuracy), conversions on
+      // the integer pipe; only the RK accumulation stays FP64
+      const float h11 = f32_rn(g11), h21 = f32_rn(g21), h12 = f32_rn(g12), h22 = f32_rn(g22);
+      float r[4];
+      r[0] = fmaf(M.D11f, h11, M.D12f * h22);
+      r[1] = fmaf(M.D12f, h11, M.D22f * h22);
+      r[2] = M.D33f * (h21 + h12);
+      r[3] = fmaf(M.D41f, h11, M.D42f * h22);
+      if (D.update_x) {
+        const float om1 = 0.5f * (h12 - h21);
+        const float t0 = f32_rn(st[0]), t1 = f32_rn(st[1]), t2 = f32_rn(st[2]);
+        r[0] = fmaf(2.0f * om1, t2, r[0]);
+        r[1] = fmaf(-2.0f * om1, t2, r[1]);
+        r[2] = fmaf(om1, t1 - t0, r[2]);
+      }
+      for (int k = 0; k < 4; k++) {
+        const double rhs = f64_of(r[k] + f32_rn(Gs[k]));
+        D.RHS1[k][t] = rhs;
+        D.RKs[k][t] = fma(f2, rhs, D.RKs[k][t]);
+      }
+    } else {
+      double spin[4] = {0.0, 0.0, 0.0, 0.0};
+      if (D.update_x) {
+        double om1 = 0.5 * (g12 - g21);
+        double om2 = -0.5 * (g12 - g21);
+        spin[0] = 2.0 * om1 * st[2];
+        spin[1] = 2.0 * om2 * st[2];
+        spin[2] = om2 * st[0] + om1 * st[1];
+      }
+      for (int k = 0; k < 4; k++) {
+        double rhs = (-div1[k] + spin[k]) + Gs[k];
+        D.RHS1[k][t] = rhs;
+        D.RKs[k][t] = D.RKs[k][t] + f2 * rhs;
+      }
     }
     D.RKd[t] = D.RKd[t] + der * f2;
     if (D.cont_density) {

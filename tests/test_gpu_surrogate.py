@@ -190,15 +190,16 @@ def test_gate_skips_steps_where_the_network_does_not_answer(built_gpu, trained):
     for k in ("x", "vel", "stress", "f_drucker", "intvars1"):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
     on, off = steps
-    assert on + off == n and 3 <= on <= 10, steps
+    assert on + off == n and 3 <= on <= 8, steps
     assert st[0] > 0 and st[1] == 0
     # the gate off: the network runs in every step
     steps = []
     _run(prob, 20, _abi.SPS_PREC_FP32_FAST, net, tol=-1.0, env=env, gate=0.0, gate_steps=steps)
     assert steps == [20, 0]
     # steps that pass keep the network on (every prediction inside the envelope accepted,
-    # a threshold that any answered evaluation meets)
+    # a threshold that any answered evaluation meets); the first step has no loading
+    # evaluation (no plasticity at time 0), so the gate is off in the second
     steps = []
     _, st = _run(prob, 20, _abi.SPS_PREC_FP32_FAST, net, tol=1e30, env=env, gate=1e-6,
                  gate_steps=steps)
-    assert st[1] > 0 and steps == [20, 0], (st, steps)
+    assert st[1] > 0 and steps == [19, 1], (st, steps)
