@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--error-steps", type=int, default=0,
                     help="instead of timing: advance the FP64 plain and the FP32 forms this "
                          "many steps side by side and report their relative errors")
+    ap.add_argument("--error-times", default="",
+                    help="with --error-steps: comma-separated simulated times (s) at which the "
+                         "errors are also reported (the step whose time first reaches each)")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
     ap.add_argument("--workload", default="slope", choices=["slope", "column-batch", "biaxial"],
                     help="slope: the headline (one 2M-particle slope); column-batch: the "
@@ -921,11 +924,18 @@ def run_errors(args):
     from sps_gb300 import _abi
     sps_gb300.build_all()
     prob = workload(args.dx)
+    use_surr = not args.no_surrogate
+    if use_surr:
+        from sps_gb300 import surrogate as sg
+        net, env, training = train_surrogate()
     ctxs = {}
     # "floor": the FP64 plain form again, from initial stresses perturbed by a relative
     # 2^-52 (one FP64 rounding): how far two runs that differ by rounding drift apart
-    for name, prec in (("plain", _abi.SPS_PREC_FP64_PLAIN), ("fp32", _abi.SPS_PREC_FP32_FAST),
-                       ("floor", _abi.SPS_PREC_FP64_PLAIN)):
+    arms = [("plain", _abi.SPS_PREC_FP64_PLAIN), ("fp32", _abi.SPS_PREC_FP32_FAST),
+            ("floor", _abi.SPS_PREC_FP64_PLAIN)]
+    if use_surr:
+        arms.append(("fp32_surrogate", _abi.SPS_PREC_FP32_FAST))
+    for name, prec in arms:
         ctxs[name] = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
                                            prob.params_copy(precision=prec))
         st = prob.state()
@@ -934,8 +944,18 @@ def run_errors(args):
             st["stress"] = st["stress"] * (1.0 + 2.0 ** -52 * rng.uniform(-1, 1, st["stress"].shape))
         ctxs[name].upload(**st)
         ctxs[name].upload_bcs(prob.bc_or_not, prob.bc_info)
+        if name == "fp32_surrogate":
+            sg.install(ctxs[name], net, tol=args.surrogate_tol, envelope=env)
     n = args.error_steps
-    marks = sorted({max(1, n * k // 20) for k in range(1, 21)})
+    marks = {max(1, n * k // 20) for k in range(1, 21)}
+    dt = prob.params.dt_sph
+    for ts in [float(v) for v in args.error_times.split(",") if v.strip()]:
+        tt, k = 0.0, 0
+        while tt < ts and k < n:  # the step whose FP64 time first reaches ts
+            tt += dt
+            k += 1
+        marks.add(k)
+    marks = sorted(marks)
     nt = prob.ntotal
     out, done, t = [], 0, {k: 0.0 for k in ctxs}
     w0 = time.perf_counter()
@@ -945,7 +965,7 @@ def run_errors(args):
         done = m
         b = ctxs["plain"].download()
         row = {"steps": m, "time_s": t["plain"]}
-        for arm in ("fp32", "floor"):
+        for arm in [a for a, _ in arms if a != "plain"]:
             a = ctxs[arm].download()
             for k, sl in (("stress", slice(0, 4 * nt)), ("vel", slice(0, 2 * nt)),
                           ("displ", slice(None))):
@@ -953,10 +973,18 @@ def run_errors(args):
                 row[arm + "_" + k + "_rel_l2"] = l2
                 row[arm + "_" + k + "_rel_linf"] = li
         out.append(row)
-    print(json.dumps({"error_run": {"workload": workload_name(prob, args.dx),
-                                    "reference": "FP64 plain GPU path (bit-identical to the CPU oracle)",
-                                    "checkpoints": out,
-                                    "wall_s": round(time.perf_counter() - w0, 1)}}))
+    extra = {}
+    if use_surr:
+        loading, answered, outside, rejected = sg.stats(ctxs["fp32_surrogate"])
+        extra["surrogate"] = {"tol": args.surrogate_tol, "training": training,
+                              "steps_with_and_without_network": sg.gate_stats(ctxs["fp32_surrogate"]),
+                              "loading_evaluations_with_network": loading,
+                              "answered": answered}
+    print(json.dumps({"error_run": dict({"workload": workload_name(prob, args.dx),
+                                         "reference": "FP64 plain GPU path (bit-identical to "
+                                                      "the CPU oracle)",
+                                         "checkpoints": out,
+                                         "wall_s": round(time.perf_counter() - w0, 1)}, **extra)}))
 
 
 def main():
