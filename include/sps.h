@@ -202,12 +202,12 @@ int sps_selftest_division(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* misma
    bit. */
 int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
 
-/* Self-test (no reference counterpart): the FP32 form's stress return first certifies in
-   FP32 that a stress lies inside the Drucker-Prager cone with a margin covering its
-   roundings, and then skips the FP64 test of adapt_stress2.  On n pseudo-random materials
-   and stresses (a quarter of them within a relative 1e-3 .. 1e-9 of the cone), *mismatches
-   counts stresses certified inside that the FP64 test would return (must be 0) and
-   *certified the stresses certified. */
+/* Self-test (no reference counterpart): the stress return of both forms first certifies
+   in FP32 that a stress lies inside the Drucker-Prager cone with a margin covering its
+   roundings, and then skips the FP64 adapt_stress2.  On n pseudo-random materials and
+   stresses (a quarter of them within a relative 1e-3 .. 1e-9 of the cone), *mismatches
+   counts certified stresses that the FP64 return of either form would change in any bit
+   (must be 0) and *certified the stresses certified. */
 int sps_selftest_cone(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches,
                       int64_t* certified);
 

@@ -30,16 +30,14 @@ namespace {
 constexpr int kBlock = 256;
 
 // adapt_stress2: the reference's FP64 arithmetic in the plain form, the division-free
-// variant in the FP32 form, which first certifies in FP32 the stresses clearly inside the
-// cone (most of them) and leaves those unchanged without any FP64 arithmetic
+// variant in the FP32 form.  Both first certify in FP32 the stresses clearly inside the cone
+// (most of them), which either routine would leave unchanged, and skip every FP64
+// operation for those: the results are bit-identical.
 __device__ __forceinline__ void stress_return(const Dev& D, const Real& M, double& a,
                                               double& b, double& c, double& d) {
-  if (D.fast) {
-    if (!inside_cone_f32(M.alpha2f, M.kcf, a, b, c, d))
-      adapt_stress_fast(M.alpha2, M.kc, M.kc_shift, a, b, c, d);
-  } else {
-    adapt_stress(M.alpha2, M.kc, a, b, c, d);
-  }
+  if (inside_cone_f32(M.alpha2f, M.kcf, a, b, c, d)) return;
+  if (D.fast) adapt_stress_fast(M.alpha2, M.kc, M.kc_shift, a, b, c, d);
+  else adapt_stress(M.alpha2, M.kc, a, b, c, d);
 }
 
 // FP32-form neighbour records of particle i (velocity, volume, stress, internal variable)
@@ -810,11 +808,12 @@ __global__ void k_selftest_conv(int64_t n, uint64_t seed, unsigned long long* ba
   if (nb) atomicAdd(bad, nb);
 }
 
-// the FP32 inside-the-cone certification of the FP32 form's stress return against the FP64
-// test it stands in for, on n pseudo-random Drucker-Prager materials and stresses, a
-// quarter of them placed within a relative 1e-3 .. 1e-9 of the cone and a quarter nearly
-// hydrostatic: bad counts stresses certified inside that the FP64 test (yield >= 0 and
-// yield^2 >= J2, adapt_stress_fast) would return; certified counts the certified ones
+// the FP32 inside-the-cone certification of the stress return against the FP64 returns it
+// lets the step skip, on n pseudo-random Drucker-Prager materials and stresses, a quarter
+// of them placed within a relative 1e-3 .. 1e-9 of the cone and a quarter nearly
+// hydrostatic: bad counts certified stresses that the plain form's adapt_stress (the
+// reference's arithmetic) or the FP32 form's adapt_stress_fast would change in any bit;
+// certified counts the certified ones
 __global__ void k_selftest_cone(int64_t n, uint64_t seed, unsigned long long* bad,
                                 unsigned long long* certified) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -856,12 +855,14 @@ __global__ void k_selftest_cone(int64_t n, uint64_t seed, unsigned long long* ba
     }
     if (inside_cone_f32((float)alpha2, (float)kc, a, b, c, d)) {
       nc++;
-      const double third = 1.0 / 3.0;
-      const double smean = ((a + b) + d) * third;
-      const double d0 = a - smean, d1 = b - smean, d3 = d - smean;
-      const double varj2 = fma(c, c, 0.5 * fma(d0, d0, fma(d1, d1, d3 * d3)));
-      const double yield = fma(-3.0 * alpha2, smean, kc);
-      if (yield < 0 || yield * yield < varj2) nb++;
+      // both returns must leave a certified stress exactly as it is
+      double p0 = a, p1 = b, p2 = c, p3 = d, f0 = a, f1 = b, f2 = c, f3 = d;
+      adapt_stress(alpha2, kc, p0, p1, p2, p3);
+      adapt_stress_fast(alpha2, kc, alpha2 > 0.0 ? kc / (3.0 * alpha2) : 0.0, f0, f1, f2, f3);
+      auto same = [](double x, double y) { return __double_as_longlong(x) == __double_as_longlong(y); };
+      if (!(same(p0, a) && same(p1, b) && same(p2, c) && same(p3, d) && same(f0, a) &&
+            same(f1, b) && same(f2, c) && same(f3, d)))
+        nb++;
     }
   }
   if (nb) atomicAdd(bad, nb);

@@ -310,9 +310,9 @@ def test_integer_pipe_conversions_match_hardware(built_gpu):
 
 
 def test_fp32_cone_certification_is_sound(built_gpu):
-    # the FP32 form skips the FP64 test of the stress return for stresses that an FP32
-    # evaluation with error bounds certifies inside the cone; no certified stress may be one
-    # that the FP64 test would return, including stresses within 1e-9 of the cone
+    # both forms skip the FP64 stress return for stresses that an FP32 evaluation with
+    # error bounds certifies inside the cone; no certified stress may be one that either
+    # FP64 return would change, including stresses within 1e-9 of the cone
     p = cases.bui_like(width=1.0, height=0.5, dx=0.05)
     g = _gpu_ctx(p)
     bad, certified = sps_gb300.selftest_cone(g, 100_000_000, seed=4242)
