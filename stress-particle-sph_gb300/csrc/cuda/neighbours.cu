@@ -440,22 +440,111 @@ __device__ __forceinline__ void cubic_mixed(const Grid& g, dfl dx, dfl dy, float
 // FAST = false: W and dW from the reference's FP64 kernel, stored in FP32 (the plain
 // form); FAST = true: the FP32 form's evaluation (cubic_mixed, or FP32 for a varying h).
 // The pair set is the same.
+// Kernel values of one accepted pair (creator a at sorted position s, partner at sorted
+// position bs in stencil cell q), packed as the finished half-list entry.
 template <bool FAST>
-__global__ void k_half(Dev D) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.N2) return;
-  if (s >= D.gtot->nactive) {
-    D.half_cnt[s] = 0;
-    return;
+__device__ __forceinline__ int4 half_entry(const Dev& D, const Grid& g, int a, int ta, float xa,
+                                           float ya, float ha, float xal, float yal, int bs,
+                                           int q) {
+  const int b = D.sorted[bs];
+  const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
+  // the stencil cell's offset (cells[q]) without indexing a local array
+  const int qx = (q == 1 || q == 4) ? 1 : (q == 2 ? -1 : 0), qy = q >= 2 ? 1 : 0;
+  const float cx = (float)qx * cw, cy = (float)qy * ch;
+  const float4 rb = D.srec[bs];
+  const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
+  double r, dx, dy, mh;
+  if (!FAST) exact_test(D, a, b, r, dx, dy, mh);
+  float wf, d0f, d1f;
+  if (!FAST) {
+    double w, dw0, dw1;
+    if (g.uniform_h) cubic_uniform(g, r, dx, dy, &w, &dw0, &dw1);
+    else sph_kernel(D.skf, D.pi, r, dx, dy, mh, &w, &dw0, &dw1);
+    wf = (float)w;
+    d0f = (float)dw0;
+    d1f = (float)dw1;
+  } else if (g.uniform_h) {
+    // separation as double-float from the cell-relative hi/lo offsets
+    // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float
+    const float2 rl = D.srecl[bs];
+    dfl ddx = df_add(df_add({xa, xal}, {-rb.x, -rl.x}),
+                     {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
+    dfl ddy = df_add(df_add({ya, yal}, {-rb.y, -rl.y}),
+                     {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
+    cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
+  } else {
+    float hm = (ha + rb.z) * 0.5f;
+    float rf = sqrtf(fx * fx + fy * fy);
+    sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
   }
-  int a = D.sorted[s];
-  const Grid g = D.grid[D.rid[a]];
+  const int pt = pint_type(ta, D.itype[b]);
+  return make_int4((int)((unsigned)b | ((unsigned)pt << kHalfTypeShift)), __float_as_int(wf),
+                   __float_as_int(d0f), __float_as_int(d1f));
+}
+
+// Phase 2 of the plain form, warp-cooperative.  The FP64 kernel values are the plain form's
+// cost (FP64 pipe), and a warp whose lanes each evaluate their own creator's pairs runs as
+// many iterations as its longest list with the other lanes idle (17.8 of 32 lanes active
+// per instruction in the per-lane loop).  Here the warp's accepted pairs are numbered
+// creator by creator (a warp scan of the counts) and evaluated 32 at a time, one per lane:
+// lane l takes pair base + l, finds its creator among the warp's lanes by a binary search
+// over the scanned counts, and writes the finished entry into that creator's list at the
+// same place.  Every entry is computed by the same arithmetic as before.  All 32 lanes call
+// this (inactive ones with kk = 0).
+__device__ __forceinline__ void half_phase2_coop(const Dev& D, int s, int kk, int a, int ta,
+                                                 float xa, float ya, float ha) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int incl = kk;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int excl = incl - kk;
+  const int total = __shfl_sync(full, incl, 31);
+  __syncwarp();  // the phase-1 entries of every lane are visible to the others
+  for (int base = 0; base < total; base += 32) {
+    const int p = base + lane;
+    // the last lane whose first pair is at or before p (it owns p: p < its excl + kk)
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int e = __shfl_sync(full, excl, lo + step);
+      if (e <= p) lo += step;
+    }
+    const int so = __shfl_sync(full, s, lo), ao = __shfl_sync(full, a, lo);
+    const int tao = __shfl_sync(full, ta, lo), eo = __shfl_sync(full, excl, lo);
+    const float xo = __shfl_sync(full, xa, lo), yo = __shfl_sync(full, ya, lo);
+    const float ho = __shfl_sync(full, ha, lo);
+    if (p < total) {
+      int4* out = D.half + (size_t)so * D.capH;
+      const int m = p - eo;
+      const int4 e0 = out[m];
+      const Grid& g = D.grid[D.rid[ao]];
+      out[m] = half_entry<false>(D, g, ao, tao, xo, yo, ho, 0.0f, 0.0f, e0.x, e0.y);
+    }
+  }
+  __syncwarp();
+}
+
+// Phase 1 for the creator at sorted position s: the accepted partners in creation order
+// (sorted position, stencil cell) into its half list, its pair count and its list-build
+// record.  Returns the number of entries held (at most capH) and the creator's id, type and
+// FP32 cell-relative offsets.
+template <bool FAST>
+__device__ __forceinline__ int half_phase1(const Dev& D, int s, int& a, int& ta, float& xa,
+                                           float& ya, float& ha) {
+  a = D.sorted[s];
+  const Grid& g = D.grid[D.rid[a]];
   const float tau = g.tau;
   int c = D.cell_of[a] - g.cell0;  // local cell in the realisation's grid
   int nx = g.ndiv[0], ny = g.ndiv[1];
   int ix = c % nx, iy = c / nx;
-  float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
-  float xal = FAST ? D.xrl[a] : 0.0f, yal = FAST ? D.yrl[a] : 0.0f;
+  xa = D.xr[a];
+  ya = D.yr[a];
+  ha = D.hr[a];
+  ta = D.itype[a];
   const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
   int k = 0;
   int4* out = D.half + (size_t)s * D.capH;
@@ -470,7 +559,6 @@ __global__ void k_half(Dev D) {
     int lo = (q == 0) ? s + 1 : D.cell_start[cc];
     int hi = D.cell_start[cc] + D.cell_cnt[cc];
     float cx = (float)cells[q][0] * cw, cy = (float)cells[q][1] * ch;
-    // phase 1: the accepted partners in creation order (sorted position, stencil cell);
     // the kernel values follow in phase 2, so that the lanes of a warp evaluate them
     // together instead of each time one lane accepts a candidate
     for (int bs = lo; bs < hi; bs++) {
@@ -485,51 +573,6 @@ __global__ void k_half(Dev D) {
       k++;
     }
   }
-  // phase 2: kernel values of the accepted pairs.  The finished entry holds the partner's
-  // id with the pair type in its top bits (kHalfIdMask), so that the list build needs
-  // neither the partner's id nor its type from memory; within one stencil cell the
-  // entries ascend in id (a cell is sorted by id) as they do in sorted position.
-  const int kk = min(k, D.capH);
-  const int ta = D.itype[a];
-  for (int m = 0; m < kk; m++) {
-    const int4 e0 = out[m];
-    const int bs = e0.x, q = e0.y;
-    const int b = D.sorted[bs];
-    // the stencil cell's offset (cells[q]) without indexing a local array
-    const int qx = (q == 1 || q == 4) ? 1 : (q == 2 ? -1 : 0), qy = q >= 2 ? 1 : 0;
-    {
-      const float cx = (float)qx * cw, cy = (float)qy * ch;
-      const float4 rb = D.srec[bs];
-      const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
-      double r, dx, dy, mh;
-      if (!FAST) exact_test(D, a, b, r, dx, dy, mh);
-      float wf, d0f, d1f;
-      if (!FAST) {
-        double w, dw0, dw1;
-        if (g.uniform_h) cubic_uniform(g, r, dx, dy, &w, &dw0, &dw1);
-        else sph_kernel(D.skf, D.pi, r, dx, dy, mh, &w, &dw0, &dw1);
-        wf = (float)w;
-        d0f = (float)dw0;
-        d1f = (float)dw1;
-      } else if (g.uniform_h) {
-        // separation as double-float from the cell-relative hi/lo offsets
-        // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float
-        const float2 rl = D.srecl[bs];
-        dfl ddx = df_add(df_add({xa, xal}, {-rb.x, -rl.x}),
-                         {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
-        dfl ddy = df_add(df_add({ya, yal}, {-rb.y, -rl.y}),
-                         {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
-        cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
-      } else {
-        float hm = (ha + rb.z) * 0.5f;
-        float rf = sqrtf(fx * fx + fy * fy);
-        sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
-      }
-      const int pt = pint_type(ta, D.itype[b]);
-      out[m] = make_int4((int)((unsigned)b | ((unsigned)pt << kHalfTypeShift)), __float_as_int(wf),
-                         __float_as_int(d0f), __float_as_int(d1f));
-    }
-  }
   if (k > D.capH) {
     atomicOr(D.err, ERR_HALF_CAP);
     k = D.capH;
@@ -539,6 +582,38 @@ __global__ void k_half(Dev D) {
   // stencil cells 1-4 start, its pair count and its id
   D.half_meta[s] = make_int4((int)((unsigned)gstart[1] | ((unsigned)gstart[2] << 16)),
                              (int)((unsigned)gstart[3] | ((unsigned)gstart[4] << 16)), k, a);
+  return k;
+}
+
+// Phase 2 turns each accepted (partner, stencil cell) into the finished entry: the
+// partner's id with the pair type in its top bits (kHalfIdMask), so that the list build
+// needs neither the partner's id nor its type from memory, and W, dW/dx, dW/dy; within one
+// stencil cell the entries ascend in id (a cell is sorted by id) as they do in sorted
+// position.  The FP32 form's lanes each finish their own list; the plain form's warps
+// share the work (half_phase2_coop), so all of a warp's lanes stay to the end.
+template <bool FAST>
+__global__ void k_half(Dev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = s < D.N2 && s < D.gtot->nactive;
+  if (!active && s < D.N2) D.half_cnt[s] = 0;
+  if (FAST) {
+    if (!active) return;
+    int a, ta;
+    float xa, ya, ha;
+    const int kk = half_phase1<true>(D, s, a, ta, xa, ya, ha);
+    const Grid& g = D.grid[D.rid[a]];
+    const float xal = D.xrl[a], yal = D.yrl[a];
+    int4* out = D.half + (size_t)s * D.capH;
+    for (int m = 0; m < kk; m++) {
+      const int4 e0 = out[m];
+      out[m] = half_entry<true>(D, g, a, ta, xa, ya, ha, xal, yal, e0.x, e0.y);
+    }
+  } else {
+    int a = 0, ta = 0, kk = 0;
+    float xa = 0.0f, ya = 0.0f, ha = 0.0f;
+    if (active) kk = half_phase1<false>(D, s, a, ta, xa, ya, ha);
+    half_phase2_coop(D, s, kk, a, ta, xa, ya, ha);
+  }
 }
 
 // pair counts of every realisation (its pairs are the half lists of its sorted range)
