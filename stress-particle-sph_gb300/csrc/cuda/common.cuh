@@ -493,8 +493,11 @@ __device__ __forceinline__ float f32_trunc(double x) {
 // return below leaves the stress unchanged and may be skipped (the result is bit-identical).
 // Error bounds, u = 2^-24, M = max |component|: the truncated inputs carry 2u M; the mean
 // 16u M; each deviator component 24u M (|d| <= 2.1 M); J2 = d2^2 + (d0^2 + d1^2 + d3^2)/2
-// therefore 256u M^2; yield = kc - 3 alpha smean 4u kc + 64u alpha M.  Anything outside
-// the FP32 range fails the test and takes the FP64 path.
+// therefore 256u M^2; yield = kc - 3 alpha smean 4u kc + 64u alpha M.  These bounds are
+// relative to M and hold while no FP32 square underflows or overflows, so the test also
+// requires 1e-15 <= M <= 1e15 (then 256u M^2 stays far above the FP32 subnormal range and
+// every absolute error that an underflowing term carries is far below it).  Anything
+// outside these ranges fails the test and takes the FP64 path.
 __device__ __forceinline__ bool inside_cone_f32(float alpha2, float kc, double a, double b,
                                                 double c, double d) {
   const float af = f32_trunc(a), bf = f32_trunc(b), cf = f32_trunc(c), df = f32_trunc(d);
@@ -505,7 +508,7 @@ __device__ __forceinline__ bool inside_cone_f32(float alpha2, float kc, double a
   const float j2 = fmaf(cf, cf, 0.5f * fmaf(d0, d0, fmaf(d1, d1, d3 * d3)));
   const float yl = (kc - (3.0f * alpha2) * smean) - (4.0f * u * kc + 64.0f * u * alpha2 * m);
   const float ej = 256.0f * u * (m * m);
-  return yl > 0.0f && yl * yl > (j2 + ej) * (1.0f + 16.0f * u);
+  return m >= 1e-15f && m <= 1e15f && yl > 0.0f && yl * yl > (j2 + ej) * (1.0f + 16.0f * u);
 }
 
 // The same return for the FP32 form, without FP64 divisions or square roots in the common

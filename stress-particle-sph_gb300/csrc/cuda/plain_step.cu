@@ -826,7 +826,8 @@ __global__ void k_selftest_cone(int64_t n, uint64_t seed, unsigned long long* ba
     const double coh = (r1 & 3) == 0 ? 0.0 : 1e5 * uni(mix64(r1 ^ 7));
     const double den = sqrt(9.0 + 12.0 * (tanfi * tanfi));
     const double alpha2 = tanfi / den, kc = (3.0 * coh) / den;
-    const double scale = exp2(-10.0 + 40.0 * uni(r2));  // stress magnitudes 1e-3 .. 1e9
+    // stress magnitudes 1e-30 .. 1e30 (the test's range guard), mostly 1e-3 .. 1e9
+    const double scale = (r2 & 7) == 0 ? exp2(-100.0 + 200.0 * uni(r2)) : exp2(-10.0 + 40.0 * uni(r2));
     const double p = -scale * (uni(r3) - 0.1);         // mostly compressive mean stress
     double s0 = scale * (2.0 * uni(mix64(r3 ^ 1)) - 1.0), s1 = scale * (2.0 * uni(mix64(r3 ^ 2)) - 1.0);
     double s2 = scale * (2.0 * uni(mix64(r3 ^ 3)) - 1.0);
