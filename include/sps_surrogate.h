@@ -93,6 +93,11 @@ int sps_mlp_grad(sps_mlp* m, const float* tuples, int32_t n, float* grad, float*
    of the step (BF16 mma with FP32 accumulation): y is n x 4. */
 int sps_mlp_predict(sps_mlp* m, const float* x, int32_t n, float* y);
 
+/* Which inference code sps_mlp_predict runs: 1 (the default) the 5th-generation tensor-core
+   path the step uses (128-row tiles, tcgen05.mma with tensor-memory accumulators), 0 the
+   warp-level mma.sync path. */
+int sps_mlp_set_inference(sps_mlp* m, int32_t tensor_memory);
+
 int sps_mlp_last_error(sps_mlp* m, char* buf, int32_t len);
 void sps_mlp_destroy(sps_mlp* m);
 

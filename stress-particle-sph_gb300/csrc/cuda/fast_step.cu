@@ -402,15 +402,12 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
 //   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
 // is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
 // Every other stress-point takes the exact flow rule.
-// With the surrogate installed both variants are launched: the one the gate selects for
-// this step runs, the other returns at once (whole blocks).
+// One stress-point (index i among the stress-points) of k_fsp_tail; the warp's 32 lanes
+// call it together.  xs, ys: the warp's tile rows.
 template <bool SURR>
-__global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
-  __shared__ float xs[4][32][16];
-  __shared__ float ys[4][32][8];
-  if (D.surr && (D.surr_gate->on != 0) != SURR) return;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i, float (*xs)[16],
+                                             float (*ys)[8]) {
+  const int lane = threadIdx.x & 31;
   const bool act = i < D.NT - D.NN;
   const int t = D.NN + (act ? i : 0);
   const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
@@ -456,17 +453,17 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     const int row = __popc(mask & ((1u << lane) - 1u));
     const int ntile = (nrows + 15) >> 4;
     if (cand)
-      for (int k = 0; k < 16; k++) xs[w][row][k] = x[k];
+      for (int k = 0; k < 16; k++) xs[row][k] = x[k];
     for (int r = nrows + lane; r < ntile * 16; r += 32)
-      for (int k = 0; k < 16; k++) xs[w][r][k] = 0.0f;
+      for (int k = 0; k < 16; k++) xs[r][k] = 0.0f;
     __syncwarp();
-    mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[w][0][0], &ys[w][0][0], lane);
-    if (ntile > 1) mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[w][16][0], &ys[w][16][0], lane);
+    mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[0][0], &ys[0][0], lane);
+    if (ntile > 1) mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[16][0], &ys[16][0], lane);
     __syncwarp();
     if (cand) {
       bool inside = true;
       for (int k = 0; k < MLP_NOUT; k++) {
-        float yk = ys[w][row][k];
+        float yk = ys[row][k];
         inside = inside && fabsf(yk) <= 1.5f * D.out_max;
         Gnet[k] = (double)yk * scale;
       }
@@ -510,6 +507,21 @@ __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
     tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, nullptr, 0.0,
                         have_dp ? dp : nullptr);
   }
+}
+
+// The stress-point tail over a grid of at most kTailBlocks blocks, each striding over
+// block-sized chunks of the stress-points.  With the surrogate installed both variants are
+// launched: the one the gate selects for this step runs, the other's blocks return at once
+// (a grid of a few SM-fulls, so that the launch that does nothing costs little).
+constexpr int kTailBlocks = 152 * 8;
+template <bool SURR>
+__global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
+  __shared__ float xs[4][32][16];
+  __shared__ float ys[4][32][8];
+  if (D.surr && (D.surr_gate->on != 0) != SURR) return;
+  const int w = threadIdx.x >> 5, ns = D.NT - D.NN;
+  for (int base = blockIdx.x * blockDim.x; base < ns; base += gridDim.x * blockDim.x)
+    fsp_tail_one<SURR>(D, stage, base + threadIdx.x, xs[w], ys[w]);
 }
 
 // XSPH_update (2_SPH_main_2018.f90:189-239), FP32 sums of double-float velocity differences
@@ -586,11 +598,12 @@ void launch_fderivs(Ctx& c, int stage) {
 void launch_fsp_tail(Ctx& c, int stage) {
   int ns = c.d.NT - c.d.NN;
   if (ns <= 0) return;
+  const int nb = std::min((ns + 127) / 128, kTailBlocks);
   if (c.d.surr) {
     c.kernels_launched += 1;
-    k_fsp_tail<true><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+    k_fsp_tail<true><<<nb, 128, 0, c.stream>>>(c.d, stage);
   }
-  k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  k_fsp_tail<false><<<nb, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
   k_fxsph<<<c.grid_of(TK_XSPH, c.d.N2), c.blk[TK_XSPH], 0, c.stream>>>(c.d);

@@ -154,4 +154,17 @@ typedef struct sps_mlp sps_mlp;
 namespace sps {
 void mlp_pack(sps_mlp* m, uint2* frag, float* bias, cudaStream_t st);
 cudaStream_t mlp_stream(sps_mlp* m);
+const float* mlp_params(sps_mlp* m);
+
+// the tensor-core (tcgen05) forward pass of mlp_tc.cu: the network as a shared-memory
+// image (mlp_tc_image_bytes) and padded biases (mlp_tc_bias_count floats) packed from the
+// trainer's FP32 parameters P, then y[r * out_stride + 0..3] = network(x[r * in_stride +
+// 0 .. nin)) for r < *count (count on the device; n_max when count is null, and the bound
+// of *count); err (device) gets bit 0 when a wait ran out
+size_t mlp_tc_image_bytes();
+int mlp_tc_bias_count();
+void mlp_tc_pack(const float* P, void* img, float* bias, cudaStream_t st);
+cudaError_t mlp_tc_forward(const void* img, const float* bias, const float* x, int in_stride,
+                           int nin, const int* count, int n_max, float* y, int out_stride,
+                           int* err, cudaStream_t st);
 }  // namespace sps

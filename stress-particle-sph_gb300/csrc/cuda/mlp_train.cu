@@ -300,8 +300,12 @@ struct sps_mlp {
   float* gtuples = nullptr;
   uint2* frag = nullptr;
   float* bias = nullptr;
+  void* tc_img = nullptr;   // the network as the tensor-core kernel's shared-memory image
+  float* tc_bias = nullptr;
+  int* tc_err = nullptr;
   float *px = nullptr, *py = nullptr;
   int64_t pred_cap = 0;
+  bool tensor_memory_path = true;  // sps_mlp_predict: tcgen05 (else the warp-level mma.sync)
   int64_t adam_t = 0;
   uint64_t rng = 0;
   std::string err;
@@ -405,6 +409,7 @@ void mlp_pack(sps_mlp* m, uint2* frag, float* bias, cudaStream_t st) {
   k_pack<<<(MLP_FRAG_U2 + 255) / 256, 256, 0, st>>>(m->P, frag, bias);
 }
 cudaStream_t mlp_stream(sps_mlp* m) { return m->stream; }
+const float* mlp_params(sps_mlp* m) { return m->P; }
 }  // namespace sps
 
 extern "C" {
@@ -439,6 +444,9 @@ int sps_mlp_create(const sps_mlp_config* cfg, sps_mlp** out) {
     m->ident = m->alloc<int>(B);
     m->gtuples = m->alloc<float>((size_t)B * MLP_TUPLE);
     m->frag = m->alloc<uint2>(MLP_FRAG_U2);
+    m->tc_img = m->alloc<uint8_t>(sps::mlp_tc_image_bytes());
+    m->tc_bias = m->alloc<float>(sps::mlp_tc_bias_count());
+    m->tc_err = m->alloc<int>(1);
     m->bias = m->alloc<float>(MLP_BIAS);
     m->ensure_lossp((B + 255) / 256);
     // Glorot-uniform weights, zero biases and padding
@@ -594,14 +602,32 @@ int sps_mlp_predict(sps_mlp* m, const float* x, int32_t n, float* y) {
       m->pred_cap = n;
     }
     MLP_CHECK(cudaMemcpyAsync(m->px, x, sizeof(float) * MLP_NIN * n, cudaMemcpyHostToDevice, m->stream));
-    sps::mlp_pack(m, m->frag, m->bias, m->stream);
-    k_predict<<<(n + 127) / 128, 128, 0, m->stream>>>(m->frag, m->bias, m->px, n, m->py);
+    int herr = 0;
+    if (m->tensor_memory_path) {
+      // the step's inference: 128-row tiles on tcgen05 with tensor-memory accumulators
+      sps::mlp_tc_pack(m->P, m->tc_img, m->tc_bias, m->stream);
+      MLP_CHECK(cudaMemsetAsync(m->tc_err, 0, sizeof(int), m->stream));
+      MLP_CHECK(sps::mlp_tc_forward(m->tc_img, m->tc_bias, m->px, MLP_NIN, MLP_NIN, nullptr, n,
+                                    m->py, MLP_NOUT, m->tc_err, m->stream));
+      MLP_CHECK(cudaMemcpyAsync(&herr, m->tc_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    } else {
+      // the warp-level mma.sync inference
+      sps::mlp_pack(m, m->frag, m->bias, m->stream);
+      k_predict<<<(n + 127) / 128, 128, 0, m->stream>>>(m->frag, m->bias, m->px, n, m->py);
+    }
     MLP_CHECK(cudaGetLastError());
     MLP_CHECK(cudaMemcpyAsync(y, m->py, sizeof(float) * MLP_NOUT * n, cudaMemcpyDeviceToHost, m->stream));
     MLP_CHECK(cudaStreamSynchronize(m->stream));
+    if (herr) return mfail(m, SPS_ERR_CUDA, "tensor-core inference: a wait ran out");
   } catch (const std::exception& e) {
     return mfail(m, SPS_ERR_CUDA, "%s", e.what());
   }
+  return SPS_OK;
+}
+
+int sps_mlp_set_inference(sps_mlp* m, int32_t tensor_memory) {
+  if (!m || (tensor_memory != 0 && tensor_memory != 1)) return SPS_ERR_ARG;
+  m->tensor_memory_path = tensor_memory == 1;
   return SPS_OK;
 }
 

@@ -29,6 +29,7 @@ CUDA_UNITS = [
     ("cuda/fast_step.cu", []),
     ("cuda/surface.cu", ["-fmad=false"]),
     ("cuda/mlp_train.cu", []),
+    ("cuda/mlp_tc.cu", []),
     ("cuda/neighbour_stats_static.cu", ["-fmad=false"]),
 ]
 

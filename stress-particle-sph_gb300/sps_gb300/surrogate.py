@@ -45,6 +45,7 @@ def _lib():
         "sps_mlp_grad": ([vp, fp, C.c_int32, fp, fp], C.c_int),
         "sps_mlp_predict": ([vp, fp, C.c_int32, fp], C.c_int),
         "sps_mlp_last_error": ([vp, C.c_char_p, C.c_int32], C.c_int),
+        "sps_mlp_set_inference": ([vp, C.c_int32], C.c_int),
         "sps_mlp_destroy": ([vp], None),
         "sps_surrogate_install": ([vp, vp, P(SurrogateOpts)], C.c_int),
         "sps_surrogate_stats": ([vp, P(C.c_int64), C.c_int32], C.c_int),
@@ -116,6 +117,11 @@ class Mlp:
         self._call("sps_mlp_grad", ptr, len(a), g.ctypes.data_as(C.POINTER(C.c_float)),
                    C.byref(loss))
         return loss.value, g
+
+    def set_inference(self, tensor_memory):
+        """predict() through the tcgen05 tensor-memory path (True, the step's) or the
+        warp-level mma.sync path (False)."""
+        self._call("sps_mlp_set_inference", int(bool(tensor_memory)))
 
     def predict(self, x):
         a, ptr = _f32(x)

@@ -51,14 +51,24 @@ def test_gradients_match_oracle(built_gpu, quantize, tol):
     net.close()
 
 
-def test_tensor_core_inference_matches_oracle(built_gpu):
+@pytest.mark.parametrize("tensor_memory", [True, False], ids=["tcgen05", "mma_sync"])
+def test_tensor_core_inference_matches_oracle(built_gpu, tensor_memory):
+    # the tcgen05 path (128-row tiles, tensor-memory accumulators; 1000 rows: a ragged last
+    # tile) and the warp-level mma.sync path against the oracle's BF16 forward pass
     rng = np.random.default_rng(4)
     net = sg.Mlp(batch=256, seed=11)
+    net.set_inference(tensor_memory)
     p = net.params().astype(np.float64)
-    x = rng.uniform(-1.0, 1.0, (1000, mo.NIN)).astype(np.float32)  # 1000: ragged last warp
+    x = rng.uniform(-1.0, 1.0, (1000, mo.NIN)).astype(np.float32)
     y = net.predict(x)
     y_ref, _ = mo.forward(p, x.astype(np.float64), quantize=True)
     assert rel_l2(y, y_ref) <= 5e-3, rel_l2(y, y_ref)
+    # many tiles over every SM, and a second call on the same network
+    x2 = rng.uniform(-1.0, 1.0, (200_000, mo.NIN)).astype(np.float32)
+    y2_ref, _ = mo.forward(p, x2.astype(np.float64), quantize=True)
+    for _ in range(2):
+        y2 = net.predict(x2)
+        assert rel_l2(y2, y2_ref) <= 5e-3, rel_l2(y2, y2_ref)
     net.close()
 
 
