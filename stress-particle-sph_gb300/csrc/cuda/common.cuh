@@ -101,6 +101,9 @@ struct Real {
   double r_x, r_y, disp_tol;
 };
 
+// device error bit of a tensor-core inference whose wait ran out
+constexpr int kErrTensorCore = 1 << 21;
+
 enum ErrBits : int {
   ERR_HALF_CAP = 1,
   ERR_LIST_CAP = 2,
@@ -187,6 +190,13 @@ struct Dev {
   double surr_tol;
   unsigned long long* surr_cnt;  // loading, answered, outside envelope, drift-rejected
   struct SurrGate* surr_gate;    // whether this step runs the network (sps_surrogate_gate)
+  // the network's rows of a stage (tensor-core inference): per stress-point its row or -1,
+  // the rows' inputs (16 floats) and outputs (4 floats), and the row count of each stage
+  int* cand_row;
+  float *xcand, *ycand;
+  int* cand_count;
+  const void* tc_img;   // the network as the tensor-core kernel's shared-memory image
+  const float* tc_bias;
   // cells
   int32_t *cell_of, *cell_cnt, *cell_start, *cell_cursor, *sorted, *spos;
   float *xr, *yr, *hr;

@@ -99,6 +99,9 @@ struct Ctx {
   uint2* mlp_frag = nullptr;
   float* mlp_bias = nullptr;
   unsigned long long* surr_cnt = nullptr;  // the 4 counters, then the gate (SurrGate)
+  void* surr_rows = nullptr;                // cand_row, xcand, ycand, cand_count (one block)
+  void* tc_img = nullptr;                   // tensor-core image of the network and biases
+  int tc_grid = 0;                          // CTAs of the tensor-core forward pass
   double gate_min_frac = 0.5;               // sps_surrogate_gate
   int gate_max_period = 64;
   // output snapshot (sps_snapshot): device copy of the output fields, pinned host copy,

@@ -17,6 +17,10 @@
 // FP32 (k_half<true>).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <stdexcept>
+#include <string>
+
 #include "ctx.cuh"
 #include "stage_tail.cuh"
 
@@ -404,9 +408,43 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
 // Every other stress-point takes the exact flow rule.
 // One stress-point (index i among the stress-points) of k_fsp_tail; the warp's 32 lanes
 // call it together.  xs, ys: the warp's tile rows.
+// The surrogate's view of stress-point t: the exact rule (drucker_prager, whose results dp
+// = {G, vivel, f} the tail reuses), whether it is loading, and for a loading point the
+// network's inputs x, their output scale and whether they lie in the training envelope.
+// Deterministic, so k_fsp_cand and k_fsp_tail<true> reach the same decisions.
+__device__ __forceinline__ void surr_front(const Dev& D, const Real& M, const StepScalars& sc,
+                                           int t, double* g, double* s2v, float* x,
+                                           double& scale, bool& loading, bool& cand,
+                                           double* dp) {
+  const double* gu = D.grad_u + 4 * (size_t)t;
+  for (int k = 0; k < 4; k++) g[k] = gu[k];
+  s2v[0] = D.s0[t];
+  s2v[1] = D.s1[t];
+  s2v[2] = D.s2[t];
+  s2v[3] = D.s3[t];
+  if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
+  double f = D.fdp[t], G2[4], vivel[4];
+  drucker_prager<true>(M, sc.time_sph, s2v, g, &f, G2, vivel);  // the exact rule
+  loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
+  for (int k = 0; k < 4; k++) {
+    dp[k] = G2[k];
+    dp[4 + k] = vivel[k];
+  }
+  dp[8] = f;
+  scale = 0.0;
+  cand = false;
+  if (loading) {
+    scale = mlp_features(s2v, g, M.tanfi, M.coh, M.young, M.poiss, D.rho[t], x);
+    cand = scale > 0.0;
+    for (int k = 0; k < MLP_NIN && cand; k++) cand = x[k] >= D.env_lo[k] && x[k] <= D.env_hi[k];
+  }
+}
+
+// One stress-point (index i among the stress-points) of k_fsp_tail; the warp's 32 lanes
+// call it together.  SURR: the network's prediction for a candidate is the row that
+// k_fsp_cand appended for it this stage, computed by the tensor-core kernel in between.
 template <bool SURR>
-__device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i, float (*xs)[16],
-                                             float (*ys)[8]) {
+__device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
   const int lane = threadIdx.x & 31;
   const bool act = i < D.NT - D.NN;
   const int t = D.NN + (act ? i : 0);
@@ -422,66 +460,33 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i, flo
   double dp[9];
   bool have_dp = false;
   if (SURR && act && M.ntype_eco > 1 && M.ncrit == 12) {
-    const double* gu = D.grad_u + 4 * (size_t)t;
-    for (int k = 0; k < 4; k++) g[k] = gu[k];
-    s2v[0] = D.s0[t];
-    s2v[1] = D.s1[t];
-    s2v[2] = D.s2[t];
-    s2v[3] = D.s3[t];
-    if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
-    double f = D.fdp[t], G2[4], vivel[4];
-    drucker_prager<true>(M, sc.time_sph, s2v, g, &f, G2, vivel);  // the exact rule
-    loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
-    for (int k = 0; k < 4; k++) {
-      dp[k] = G2[k];
-      dp[4 + k] = vivel[k];
-    }
-    dp[8] = f;
+    surr_front(D, M, sc, t, g, s2v, x, scale, loading, cand, dp);
     have_dp = true;
-    if (loading) {
-      scale = mlp_features(s2v, g, M.tanfi, M.coh, M.young, M.poiss, D.rho[t], x);
-      cand = scale > 0.0;
-      for (int k = 0; k < MLP_NIN && cand; k++)
-        cand = x[k] >= D.env_lo[k] && x[k] <= D.env_hi[k];
-    }
   }
-  const unsigned mask = __ballot_sync(0xffffffffu, cand);
-  const int nrows = __popc(mask);
   double Gnet[4];
   bool accept = false;
-  if (SURR && nrows) {  // warp-uniform
-    const int row = __popc(mask & ((1u << lane) - 1u));
-    const int ntile = (nrows + 15) >> 4;
-    if (cand)
-      for (int k = 0; k < 16; k++) xs[row][k] = x[k];
-    for (int r = nrows + lane; r < ntile * 16; r += 32)
-      for (int k = 0; k < 16; k++) xs[r][k] = 0.0f;
-    __syncwarp();
-    mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[0][0], &ys[0][0], lane);
-    if (ntile > 1) mlp_tile16(D.mlp_frag, D.mlp_bias, &xs[16][0], &ys[16][0], lane);
-    __syncwarp();
-    if (cand) {
-      bool inside = true;
-      for (int k = 0; k < MLP_NOUT; k++) {
-        float yk = ys[row][k];
-        inside = inside && fabsf(yk) <= 1.5f * D.out_max;
-        Gnet[k] = (double)yk * scale;
-      }
-      if (inside) {
-        // drift test in FP64
-        double sm = ((s2v[0] + s2v[1]) + s2v[3]) / 3.0;
-        double d0 = s2v[0] - sm, d1 = s2v[1] - sm, d2 = s2v[2], d3 = s2v[3] - sm;
-        double sj = sqrt(d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3));
-        double e0 = M.D11 * g[0] + M.D12 * g[3] + Gnet[0];
-        double e1 = M.D12 * g[0] + M.D22 * g[3] + Gnet[1];
-        double e2 = M.D33 * g[1] + M.D33 * g[2] + Gnet[2];
-        double e3 = M.D41 * g[0] + M.D42 * g[3] + Gnet[3];
-        double df = (d0 * e0 + d1 * e1 + d3 * e3 + 2.0 * d2 * e2) / (2.0 * sj) +
-                    M.alpha2 * (e0 + e1 + e3);
-        accept = sj > 0.0 && M.dt * fabs(df) <= D.surr_tol * sj;
-      } else {
-        cand = false;  // counted as outside the envelope
-      }
+  if (SURR && cand) {
+    const float* y = D.ycand + 4 * (size_t)D.cand_row[i];
+    bool inside = true;
+    for (int k = 0; k < MLP_NOUT; k++) {
+      const float yk = y[k];
+      inside = inside && fabsf(yk) <= 1.5f * D.out_max;
+      Gnet[k] = (double)yk * scale;
+    }
+    if (inside) {
+      // drift test in FP64
+      double sm = ((s2v[0] + s2v[1]) + s2v[3]) / 3.0;
+      double d0 = s2v[0] - sm, d1 = s2v[1] - sm, d2 = s2v[2], d3 = s2v[3] - sm;
+      double sj = sqrt(d2 * d2 + 0.5 * ((d0 * d0 + d1 * d1) + d3 * d3));
+      double e0 = M.D11 * g[0] + M.D12 * g[3] + Gnet[0];
+      double e1 = M.D12 * g[0] + M.D22 * g[3] + Gnet[1];
+      double e2 = M.D33 * g[1] + M.D33 * g[2] + Gnet[2];
+      double e3 = M.D41 * g[0] + M.D42 * g[3] + Gnet[3];
+      double df = (d0 * e0 + d1 * e1 + d3 * e3 + 2.0 * d2 * e2) / (2.0 * sj) +
+                  M.alpha2 * (e0 + e1 + e3);
+      accept = sj > 0.0 && M.dt * fabs(df) <= D.surr_tol * sj;
+    } else {
+      cand = false;  // counted as outside the envelope
     }
   }
   // counters: loading, answered, outside the envelope, drift-rejected
@@ -516,12 +521,42 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i, flo
 constexpr int kTailBlocks = 152 * 8;
 template <bool SURR>
 __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
-  __shared__ float xs[4][32][16];
-  __shared__ float ys[4][32][8];
   if (D.surr && (D.surr_gate->on != 0) != SURR) return;
-  const int w = threadIdx.x >> 5, ns = D.NT - D.NN;
+  const int ns = D.NT - D.NN;
   for (int base = blockIdx.x * blockDim.x; base < ns; base += gridDim.x * blockDim.x)
-    fsp_tail_one<SURR>(D, stage, base + threadIdx.x, xs[w], ys[w]);
+    fsp_tail_one<SURR>(D, stage, base + threadIdx.x);
+}
+
+// The surrogate's candidates of this stage (while the gate runs the network): every loading
+// stress-point whose inputs lie in the training envelope appends its inputs (16 floats) as
+// one row of xcand; cand_row[i] holds the row of stress-point i, or -1.  The rows of a warp
+// are reserved with one atomic on the stage's count (reset at the start of every step).
+__global__ void __launch_bounds__(128) k_fsp_cand(Dev D, int stage) {
+  if (!D.surr || D.surr_gate->on == 0) return;
+  const int ns = D.NT - D.NN, lane = threadIdx.x & 31;
+  for (int base = blockIdx.x * blockDim.x; base < ns; base += gridDim.x * blockDim.x) {
+    const int i = base + threadIdx.x;
+    const bool act = i < ns;
+    const int t = D.NN + (act ? i : 0);
+    const Real& M = real_of(D, t);
+    const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
+    double g[4], s2v[4], scale, dp[9];
+    float x[16];
+    bool loading = false, cand = false;
+    if (act && M.ntype_eco > 1 && M.ncrit == 12)
+      surr_front(D, M, sc, t, g, s2v, x, scale, loading, cand, dp);
+    const unsigned m = __ballot_sync(0xffffffffu, cand);
+    int row0 = 0;
+    if (lane == 0 && m) row0 = atomicAdd(&D.cand_count[stage], __popc(m));
+    row0 = __shfl_sync(0xffffffffu, row0, 0);
+    int row = -1;
+    if (cand) {
+      row = row0 + __popc(m & ((1u << lane) - 1u));
+      float4* o = reinterpret_cast<float4*>(D.xcand + 16 * (size_t)row);
+      for (int q = 0; q < 4; q++) o[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+    }
+    if (act) D.cand_row[i] = row;
+  }
 }
 
 // XSPH_update (2_SPH_main_2018.f90:189-239), FP32 sums of double-float velocity differences
@@ -600,7 +635,13 @@ void launch_fsp_tail(Ctx& c, int stage) {
   if (ns <= 0) return;
   const int nb = std::min((ns + 127) / 128, kTailBlocks);
   if (c.d.surr) {
-    c.kernels_launched += 1;
+    // the network's rows of this stage: candidates, then the tensor-core forward pass over
+    // as many 128-row tiles as there are candidates (a grid of at most one CTA per SM)
+    c.kernels_launched += 3;
+    k_fsp_cand<<<nb, 128, 0, c.stream>>>(c.d, stage);
+    SPS_CUDA_CHECK(mlp_tc_forward(c.d.tc_img, c.d.tc_bias, c.d.xcand, 16, MLP_NIN,
+                                  c.d.cand_count + stage, ns, c.d.ycand, MLP_NOUT, c.d.err,
+                                  kErrTensorCore, c.tc_grid, c.stream));
     k_fsp_tail<true><<<nb, 128, 0, c.stream>>>(c.d, stage);
   }
   k_fsp_tail<false><<<nb, 128, 0, c.stream>>>(c.d, stage);

@@ -160,11 +160,15 @@ const float* mlp_params(sps_mlp* m);
 // image (mlp_tc_image_bytes) and padded biases (mlp_tc_bias_count floats) packed from the
 // trainer's FP32 parameters P, then y[r * out_stride + 0..3] = network(x[r * in_stride +
 // 0 .. nin)) for r < *count (count on the device; n_max when count is null, and the bound
-// of *count); err (device) gets bit 0 when a wait ran out
+// of *count), on grid CTAs (mlp_tc_grid: at most one per SM); err (device) gets err_bit
+// when a wait ran out.  mlp_tc_prepare raises the kernel's shared-memory limit (once per
+// device, before any launch or capture).
 size_t mlp_tc_image_bytes();
 int mlp_tc_bias_count();
 void mlp_tc_pack(const float* P, void* img, float* bias, cudaStream_t st);
+cudaError_t mlp_tc_prepare();
+int mlp_tc_grid(int n_max, int num_sms);
 cudaError_t mlp_tc_forward(const void* img, const float* bias, const float* x, int in_stride,
                            int nin, const int* count, int n_max, float* y, int out_stride,
-                           int* err, cudaStream_t st);
+                           int* err, int err_bit, int grid, cudaStream_t st);
 }  // namespace sps

@@ -145,7 +145,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img
                                                    const float* __restrict__ x, int in_stride,
                                                    int nin, const int* __restrict__ count,
                                                    int n_fixed, float* __restrict__ y,
-                                                   int out_stride, int* __restrict__ err) {
+                                                   int out_stride, int* __restrict__ err,
+                                                   int err_bit) {
   extern __shared__ __align__(128) uint8_t tc_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img
   }
   __syncthreads();
   if (S.abort) {
-    if (tid == 0) atomicOr(err, 1);
+    if (tid == 0) atomicOr(err, err_bit);
     // the tensor core may still be running the timed-out group: wait once more (bounded)
     // before the tensor memory is released
     mbar_wait(mbar, (phase - 1) & 1);
@@ -314,24 +315,23 @@ void mlp_tc_pack(const float* P, void* img, float* bias, cudaStream_t st) {
   k_pack_tc<<<(n + 255) / 256, 256, 0, st>>>(P, static_cast<uint8_t*>(img), bias);
 }
 
+cudaError_t mlp_tc_prepare() {
+  return cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(TcSmem));
+}
+
+int mlp_tc_grid(int n_max, int num_sms) {
+  const int ntiles = (n_max + kTcRows - 1) / kTcRows;
+  return ntiles < num_sms ? ntiles : num_sms;
+}
+
 cudaError_t mlp_tc_forward(const void* img, const float* bias, const float* x, int in_stride,
                            int nin, const int* count, int n_max, float* y, int out_stride,
-                           int* err, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TcSmem));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  if (n_max <= 0) return cudaSuccess;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int ntiles = (n_max + kTcRows - 1) / kTcRows;
-  const int grid = ntiles < nsm ? ntiles : nsm;
-  k_mlp_tc<<<grid, 128, sizeof(TcSmem), st>>>(static_cast<const uint4*>(img), bias, x, in_stride,
-                                              nin, count, n_max, y, out_stride, err);
+                           int* err, int err_bit, int grid, cudaStream_t st) {
+  if (n_max <= 0 || grid <= 0) return cudaSuccess;
+  k_mlp_tc<<<grid, 128, sizeof(TcSmem), st>>>(static_cast<const uint4*>(img), bias, x,
+                                              in_stride, nin, count, n_max, y, out_stride, err,
+                                              err_bit);
   return cudaGetLastError();
 }
 

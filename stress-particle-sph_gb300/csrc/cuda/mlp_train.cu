@@ -605,10 +605,15 @@ int sps_mlp_predict(sps_mlp* m, const float* x, int32_t n, float* y) {
     int herr = 0;
     if (m->tensor_memory_path) {
       // the step's inference: 128-row tiles on tcgen05 with tensor-memory accumulators
+      int dev = 0, nsm = 0;
+      MLP_CHECK(cudaGetDevice(&dev));
+      MLP_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      MLP_CHECK(sps::mlp_tc_prepare());
       sps::mlp_tc_pack(m->P, m->tc_img, m->tc_bias, m->stream);
       MLP_CHECK(cudaMemsetAsync(m->tc_err, 0, sizeof(int), m->stream));
       MLP_CHECK(sps::mlp_tc_forward(m->tc_img, m->tc_bias, m->px, MLP_NIN, MLP_NIN, nullptr, n,
-                                    m->py, MLP_NOUT, m->tc_err, m->stream));
+                                    m->py, MLP_NOUT, m->tc_err, 1, sps::mlp_tc_grid(n, nsm),
+                                    m->stream));
       MLP_CHECK(cudaMemcpyAsync(&herr, m->tc_err, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
     } else {
       // the warp-level mma.sync inference

@@ -62,6 +62,7 @@ __device__ __forceinline__ void write_records(const Dev& D, int i, bool rec_i, d
 
 __global__ void k_load_scalars(Dev D) {
   int k = *D.step_idx;
+  if (D.surr && threadIdx.x < 4) D.cand_count[threadIdx.x] = 0;  // the network's rows
   for (int r = threadIdx.x; r < D.R; r += blockDim.x) D.cur[r] = D.scal_table[(size_t)k * D.R + r];
 }
 

@@ -366,6 +366,7 @@ std::string err_text(int e) {
   if (e & sps::ERR_NPAIRS) m += "more than 2^30 pairs; ";
   if (e & sps::ERR_BOUND) m += "more than 8 wall particles within 0.75 dx of a node; ";
   if (e & (1 << 20)) m += "non-finite value in the particle state; ";
+  if (e & sps::kErrTensorCore) m += "the surrogate's tensor-core inference timed out; ";
   return m;
 }
 
@@ -1058,6 +1059,7 @@ int sps_step(sps_ctx* h, int32_t nsteps, double* time_sph) {
       SPS_CUDA_CHECK(cudaMemsetAsync(c.d.err, 0, sizeof(int), c.stream));
       SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
       if (e & (1 << 20)) return fail(&c, SPS_ERR_NONFINITE, err_text(e));
+      if (e & sps::kErrTensorCore) return fail(&c, SPS_ERR_CUDA, err_text(e));
       return fail(&c, SPS_ERR_CAPACITY, err_text(e));
     }
   } catch (const std::exception& e) {
@@ -1744,7 +1746,7 @@ void sps_destroy(sps_ctx* h) {
   sps::drop_graphs(c);
   if (c.stream) cudaStreamSynchronize(c.stream);
   for (void* p : {(void*)c.cap_buf, (void*)c.cap_cnt, (void*)c.mlp_frag, (void*)c.mlp_bias,
-                  (void*)c.surr_cnt})
+                  (void*)c.surr_cnt, c.surr_rows, c.tc_img})
     if (p) cudaFree(p);
   for (void* p : c.allocs) cudaFree(p);
   if (c.h_err) cudaFreeHost(c.h_err);
@@ -1835,9 +1837,34 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
         SPS_CUDA_CHECK(cudaMalloc(&p, kSurrBytes));
         c.surr_cnt = static_cast<unsigned long long*>(p);
       }
+      const size_t ns = (size_t)(c.d.NT - c.d.NN);
+      if (!c.surr_rows) {
+        // cand_row (ns ints), xcand (16 ns floats), ycand (4 ns floats), cand_count (4 ints)
+        void* p = nullptr;
+        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(int) * ns + sizeof(float) * 20 * ns + 64));
+        c.surr_rows = p;
+        SPS_CUDA_CHECK(cudaMalloc(&p, sps::mlp_tc_image_bytes() +
+                                          sizeof(float) * sps::mlp_tc_bias_count()));
+        c.tc_img = p;
+        SPS_CUDA_CHECK(sps::mlp_tc_prepare());
+        int nsm = 0;
+        SPS_CUDA_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+        c.tc_grid = sps::mlp_tc_grid((int)ns, nsm);
+      }
+      {
+        char* b = static_cast<char*>(c.surr_rows);
+        c.d.cand_row = reinterpret_cast<int*>(b);
+        c.d.xcand = reinterpret_cast<float*>(b + sizeof(int) * ns);
+        c.d.ycand = c.d.xcand + 16 * ns;
+        c.d.cand_count = reinterpret_cast<int*>(c.d.ycand + 4 * ns);
+        c.d.tc_img = c.tc_img;
+        c.d.tc_bias = reinterpret_cast<const float*>(static_cast<char*>(c.tc_img) +
+                                                     sps::mlp_tc_image_bytes());
+      }
       cudaStream_t ms = sps::mlp_stream(m);
       SPS_CUDA_CHECK(cudaStreamSynchronize(ms));
       sps::mlp_pack(m, c.mlp_frag, c.mlp_bias, ms);
+      sps::mlp_tc_pack(sps::mlp_params(m), c.tc_img, const_cast<float*>(c.d.tc_bias), ms);
       SPS_CUDA_CHECK(cudaGetLastError());
       SPS_CUDA_CHECK(cudaStreamSynchronize(ms));
       SPS_CUDA_CHECK(cudaMemsetAsync(c.surr_cnt, 0, sizeof(unsigned long long) * 4, c.stream));
