@@ -1839,9 +1839,10 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
       }
       const size_t ns = (size_t)(c.d.NT - c.d.NN);
       if (!c.surr_rows) {
-        // cand_row (ns ints), xcand (16 ns floats), ycand (4 ns floats), cand_count (4 ints)
+        // xcand (16 ns floats; its rows are written as float4, so it comes first, at the
+        // allocation's alignment), ycand (4 ns floats), cand_row (ns ints), cand_count (4 ints)
         void* p = nullptr;
-        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(int) * ns + sizeof(float) * 20 * ns + 64));
+        SPS_CUDA_CHECK(cudaMalloc(&p, sizeof(float) * 20 * ns + sizeof(int) * ns + 64));
         c.surr_rows = p;
         SPS_CUDA_CHECK(cudaMalloc(&p, sps::mlp_tc_image_bytes() +
                                           sizeof(float) * sps::mlp_tc_bias_count()));
@@ -1853,10 +1854,10 @@ int sps_surrogate_install(sps_ctx* h, sps_mlp* m, const sps_surrogate_opts* o) {
       }
       {
         char* b = static_cast<char*>(c.surr_rows);
-        c.d.cand_row = reinterpret_cast<int*>(b);
-        c.d.xcand = reinterpret_cast<float*>(b + sizeof(int) * ns);
+        c.d.xcand = reinterpret_cast<float*>(b);
         c.d.ycand = c.d.xcand + 16 * ns;
-        c.d.cand_count = reinterpret_cast<int*>(c.d.ycand + 4 * ns);
+        c.d.cand_row = reinterpret_cast<int*>(c.d.ycand + 4 * ns);
+        c.d.cand_count = c.d.cand_row + ns;
         c.d.tc_img = c.tc_img;
         c.d.tc_bias = reinterpret_cast<const float*>(static_cast<char*>(c.tc_img) +
                                                      sps::mlp_tc_image_bytes());
