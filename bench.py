@@ -67,6 +67,9 @@ def parse():
                     help="with --error-steps: comma-separated simulated times (s) at which the "
                          "errors are also reported (the step whose time first reaches each)")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
+    ap.add_argument("--surrogate-gate", type=float, default=0.5,
+                    help="answered fraction below which a step runs without the network "
+                         "(sps_surrogate_gate; 0 keeps the network on in every step)")
     ap.add_argument("--workload", default="slope", choices=["slope", "column-batch", "biaxial"],
                     help="slope: the headline (one 2M-particle slope); column-batch: the "
                          "combined form (batched columns, FP32 + surrogate vs FP64 plain); "
@@ -342,6 +345,7 @@ def three_arms(args, make, n, net, env, training, dist, local):
         b = make(prec)
         if use:
             sg.install(b, net, tol=args.surrogate_tol, envelope=env)
+            sg.set_gate(b, args.surrogate_gate)
         sps_gb300.autotune(b, 2)
         single = not isinstance(b, sps_gb300.Batch)
         t = b.step(max(args.warmup, 1), 0.0) if single else b.step(max(args.warmup, 1))
@@ -688,6 +692,7 @@ def run_ours(args):
     ctx.upload_problem(prob)
     if use_surr:
         sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
+        sg.set_gate(ctx, args.surrogate_gate)
     tuned = sps_gb300.autotune(ctx, 2)  # launch shapes; the state is restored
     if fast:
         tuned = dict(tuned, lookahead=sps_gb300.lookahead(ctx))
@@ -707,7 +712,7 @@ def run_ours(args):
         surr = {"tol": args.surrogate_tol,
                 "drift_test": "dt |grad f : (D:e + Gs)| / sqrt(J2) <= tol",
                 "training": training,
-                "gate": {"min_answered": 0.5, "max_period": 64,
+                "gate": {"min_answered": args.surrogate_gate, "max_period": 64,
                          "timed_steps_with_network": g1[0] - g0[0],
                          "timed_steps_without": g1[1] - g0[1]},
                 "timed_loading_evaluations_with_network": loading,
@@ -725,6 +730,7 @@ def run_ours(args):
             "ms_per_step": round(ms_n / args.steps, 4)}
         surr["speed_with_over_without"] = round(ms_n / ms_max, 4)
         sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
+        sg.set_gate(ctx, args.surrogate_gate)
 
     plain = None
     errors = None
@@ -946,6 +952,7 @@ def run_errors(args):
         ctxs[name].upload_bcs(prob.bc_or_not, prob.bc_info)
         if name == "fp32_surrogate":
             sg.install(ctxs[name], net, tol=args.surrogate_tol, envelope=env)
+            sg.set_gate(ctxs[name], args.surrogate_gate)
     n = args.error_steps
     marks = {max(1, n * k // 20) for k in range(1, 21)}
     dt = prob.params.dt_sph
