@@ -66,6 +66,10 @@ def parse():
     ap.add_argument("--error-times", default="",
                     help="with --error-steps: comma-separated simulated times (s) at which the "
                          "errors are also reported (the step whose time first reaches each)")
+    ap.add_argument("--error-at", type=float, default=0.01,
+                    help="simulated time (s) at which the run also reports the errors of the "
+                         "FP32 form, with and without the surrogate, and of the 2^-52 floor "
+                         "against the FP64 plain form, from fresh contexts (0: skip)")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
     ap.add_argument("--surrogate-gate", type=float, default=0.5,
                     help="answered fraction below which a step runs without the network "
@@ -816,6 +820,18 @@ def run_ours(args):
     if fast and not args.no_batch:
         batch = run_batch(args, dist, local)
 
+    fixed = None
+    if fast and rank == 0 and args.error_at > 0:
+        m = steps_to_time(prob, args.error_at)
+        w0 = time.perf_counter()
+        rows, counters = error_rows(args, prob, [m], net if use_surr else None,
+                                    env if use_surr else None)
+        fixed = dict(rows[0], wall_s=round(time.perf_counter() - w0, 1),
+                     reference="FP64 plain GPU path (bit-identical to the CPU oracle)",
+                     floor="FP64 plain from initial stresses perturbed by 2^-52 relative")
+        if counters is not None:
+            fixed["surrogate"] = counters
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args)
@@ -839,7 +855,8 @@ def run_ours(args):
                        "free_surface": "the timed steps skip get_nodes_on_free_surface, which "
                                        "nothing in this workload's step reads; e2e detects it "
                                        "for every step's output (in FP32 in the FP32 form)"},
-            "plain": plain, "error_vs_plain": errors, "surrogate": surr, "batch": batch,
+            "plain": plain, "error_vs_plain": errors, "error_at_fixed_time": fixed,
+            "surrogate": surr, "batch": batch,
             "e2e": e2e, "gpu_launches": int(kps * args.steps), "roofline": roof,
             "autotuned_blocks": tuned, "algorithmic_bytes_per_launch": alg_bytes,
             "fp64": None if f64 is None else {"dgemm_peak_tflops": round(f64, 2)},
@@ -922,25 +939,30 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def run_errors(args):
-    """FP32 form (optionally with the surrogate) against the FP64 plain form over a long
-    run of the slope workload, with relative L2 / Linf errors at checkpoints."""
+def steps_to_time(prob, ts):
+    """The step whose FP64 time (a sum of dt, as the step loop adds it) first reaches ts."""
+    tt, k = 0.0, 0
+    while tt < ts:
+        tt += prob.params.dt_sph
+        k += 1
+    return k
+
+
+def error_rows(args, prob, marks, net=None, env=None):
+    """Relative L2 / Linf errors against the FP64 plain form at the given step counts, for
+    the FP32 form, the FP32 form with the surrogate (when a network is given) and the
+    "floor": the FP64 plain form again, from initial stresses perturbed by a relative 2^-52
+    (one FP64 rounding), i.e. how far two runs that differ by rounding drift apart.  Returns
+    (rows, surrogate counters or None)."""
     import numpy as np
     import sps_gb300
     from sps_gb300 import _abi
-    sps_gb300.build_all()
-    prob = workload(args.dx)
-    use_surr = not args.no_surrogate
-    if use_surr:
-        from sps_gb300 import surrogate as sg
-        net, env, training = train_surrogate()
-    ctxs = {}
-    # "floor": the FP64 plain form again, from initial stresses perturbed by a relative
-    # 2^-52 (one FP64 rounding): how far two runs that differ by rounding drift apart
     arms = [("plain", _abi.SPS_PREC_FP64_PLAIN), ("fp32", _abi.SPS_PREC_FP32_FAST),
             ("floor", _abi.SPS_PREC_FP64_PLAIN)]
-    if use_surr:
+    if net is not None:
+        from sps_gb300 import surrogate as sg
         arms.append(("fp32_surrogate", _abi.SPS_PREC_FP32_FAST))
+    ctxs = {}
     for name, prec in arms:
         ctxs[name] = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
                                            prob.params_copy(precision=prec))
@@ -953,20 +975,9 @@ def run_errors(args):
         if name == "fp32_surrogate":
             sg.install(ctxs[name], net, tol=args.surrogate_tol, envelope=env)
             sg.set_gate(ctxs[name], args.surrogate_gate)
-    n = args.error_steps
-    marks = {max(1, n * k // 20) for k in range(1, 21)}
-    dt = prob.params.dt_sph
-    for ts in [float(v) for v in args.error_times.split(",") if v.strip()]:
-        tt, k = 0.0, 0
-        while tt < ts and k < n:  # the step whose FP64 time first reaches ts
-            tt += dt
-            k += 1
-        marks.add(k)
-    marks = sorted(marks)
     nt = prob.ntotal
     out, done, t = [], 0, {k: 0.0 for k in ctxs}
-    w0 = time.perf_counter()
-    for m in marks:
+    for m in sorted(marks):
         for name, c in ctxs.items():
             t[name] = c.step(m - done, t[name])
         done = m
@@ -980,13 +991,35 @@ def run_errors(args):
                 row[arm + "_" + k + "_rel_l2"] = l2
                 row[arm + "_" + k + "_rel_linf"] = li
         out.append(row)
+    counters = None
+    if net is not None:
+        c = ctxs["fp32_surrogate"]
+        loading, answered, outside, rejected = sg.stats(c)
+        counters = {"steps_with_and_without_network": sg.gate_stats(c),
+                    "loading_evaluations_with_network": loading, "answered": answered}
+    for c in ctxs.values():
+        c.close()
+    return out, counters
+
+
+def run_errors(args):
+    """FP32 form (optionally with the surrogate) against the FP64 plain form over a long
+    run of the slope workload, with relative L2 / Linf errors at checkpoints."""
+    import sps_gb300
+    sps_gb300.build_all()
+    prob = workload(args.dx)
+    net = env = None
+    if not args.no_surrogate:
+        net, env, training = train_surrogate()
+    n = args.error_steps
+    marks = {max(1, n * k // 20) for k in range(1, 21)}
+    for ts in [float(v) for v in args.error_times.split(",") if v.strip()]:
+        marks.add(min(n, steps_to_time(prob, ts)))
+    w0 = time.perf_counter()
+    out, counters = error_rows(args, prob, marks, net, env)
     extra = {}
-    if use_surr:
-        loading, answered, outside, rejected = sg.stats(ctxs["fp32_surrogate"])
-        extra["surrogate"] = {"tol": args.surrogate_tol, "training": training,
-                              "steps_with_and_without_network": sg.gate_stats(ctxs["fp32_surrogate"]),
-                              "loading_evaluations_with_network": loading,
-                              "answered": answered}
+    if counters is not None:
+        extra["surrogate"] = dict({"tol": args.surrogate_tol, "training": training}, **counters)
     print(json.dumps({"error_run": dict({"workload": workload_name(prob, args.dx),
                                          "reference": "FP64 plain GPU path (bit-identical to "
                                                       "the CPU oracle)",

@@ -160,7 +160,7 @@ const float* mlp_params(sps_mlp* m);
 // image (mlp_tc_image_bytes) and padded biases (mlp_tc_bias_count floats) packed from the
 // trainer's FP32 parameters P, then y[r * out_stride + 0..3] = network(x[r * in_stride +
 // 0 .. nin)) for r < *count (count on the device; n_max when count is null, and the bound
-// of *count), on grid CTAs (mlp_tc_grid: at most one per SM); err (device) gets err_bit
+// of *count), on grid CTAs (mlp_tc_grid: at most two per SM); err (device) gets err_bit
 // when a wait ran out.  mlp_tc_prepare raises the kernel's shared-memory limit (once per
 // device, before any launch or capture).
 size_t mlp_tc_image_bytes();

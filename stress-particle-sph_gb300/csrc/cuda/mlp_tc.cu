@@ -5,16 +5,17 @@
 // activations, FP32 accumulation and biases (the same numbers as the trainer's quantized
 // forward pass and the warp-level inference of mlp.cuh).
 //
-// One CTA of 128 threads (4 warps) holds the whole network in shared memory (73,728 B of
+// One CTA of 256 threads (8 warps) holds the whole network in shared memory (73,728 B of
 // BF16 weights, 1,600 B of biases) and loops over 128-row tiles of its inputs.  Per tile:
 //   - the 128 x 16 input tile is rounded to BF16 into shared memory;
 //   - layer by layer, one elected thread issues tcgen05.mma (kind::f16, M = 128, K = 16 per
 //     instruction, N = 128 for the hidden layers, 16 for the output layer) with the
 //     activation tile as A and the layer's weights as B, accumulating in 128 columns of
 //     tensor memory, and commits the group to an mbarrier;
-//   - every thread waits for the mbarrier, reads its row of the accumulator with
-//     tcgen05.ld (warp w owns tensor-memory lanes 32w .. 32w + 31), adds the bias, applies
-//     SiLU and writes the BF16 activation back into shared memory as the next layer's A.
+//   - every thread waits for the mbarrier, reads half of its row of the accumulator with
+//     tcgen05.ld (warp w reads tensor-memory lanes 32 (w % 4) .. + 31, the sub-partition
+//     it may access, and columns 64 (w / 4) .. + 63), adds the bias, applies SiLU and writes
+//     the BF16 activation back into shared memory as the next layer's A.
 // Shared-memory operands use the no-swizzle K-major layout of 8 x 16-byte core matrices:
 // element (r, k) of an R x K operand sits at byte ((r / 8) (K / 8) + k / 8) 128 + (r % 8) 16
 // + (k % 8) 2, so the leading (K) byte offset between core matrices is 128 and the stride
@@ -139,8 +140,20 @@ __device__ __forceinline__ void put16(uint8_t* tile, int r, int k0, const float*
   *reinterpret_cast<uint4*>(tile + core_off(r, k0 + 8, 128)) = hi;
 }
 
+// SiLU as z sigmoid(z) = h + h tanh(h), h = z / 2, with one hardware tanh (tanh.approx.f32,
+// relative error about 2^-11): one multi-function-unit operation per element instead of an
+// exponential and a reciprocal; the activation is rounded to BF16 (2^-9) right after
+__device__ __forceinline__ float silu_fast(float z) {
+  const float h = 0.5f * z;
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
+}
+
+constexpr int kTcThreads = 256;  // 8 warps: warp w reads lanes 32 (w % 4) .., columns 64 (w / 4) ..
+
 // y[row, 0..3] = network(x[row, 0..nin)) for rows [0, n), n = *count when count is given
-__global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img,
+__global__ void __launch_bounds__(kTcThreads, 2) k_mlp_tc(const uint4* __restrict__ img,
                                                    const float* __restrict__ bias,
                                                    const float* __restrict__ x, int in_stride,
                                                    int nin, const int* __restrict__ count,
@@ -176,7 +189,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = S.tmem;
-  const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's lanes
+  // this warp's tensor-memory lanes (its sub-partition) and its half of the columns
+  const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+  const int r = 32 * (warp & 3) + (tid & 31), chalf = 64 * (warp >> 2);
   const uint32_t a0 = smem_u32(S.a0), ah = smem_u32(S.ah), w = smem_u32(S.w);
   const uint32_t id_h = instr_desc(128, 128), id_o = instr_desc(128, 16);
   uint32_t phase = 0;
@@ -207,13 +222,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img
   };
   // the accumulator of a hidden layer: bias, SiLU, BF16 into the activation tile
   auto hidden_epilogue = [&](const float* b) {
-    const int r = tid;  // tensor-memory lane = row
 #pragma unroll 1
-    for (int c0 = 0; c0 < 128; c0 += 16) {
+    for (int c0 = chalf; c0 < chalf + 64; c0 += 16) {
       float v[16];
       tc_ld16(trow + c0, v);
 #pragma unroll
-      for (int i = 0; i < 16; i++) v[i] = silu(v[i] + b[c0 + i]);
+      for (int i = 0; i < 16; i++) v[i] = silu_fast(v[i] + b[c0 + i]);
       put16(S.ah, r, c0, v);
     }
   };
@@ -226,18 +240,17 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img
   };
 
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // input rows, rounded to BF16 into the K = 16 tile
-    const long row = (long)tile * kTcRows + tid;
-    float v[16];
-#pragma unroll
-    for (int k = 0; k < 16; k++) v[k] = (row < n && k < nin) ? x[row * in_stride + k] : 0.0f;
+    // input rows, rounded to BF16 into the K = 16 tile: thread r, column half chalf / 64
+    const long row = (long)tile * kTcRows + r;
     {
-      uint4 lo = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
-                            pack_bf16(v[6], v[7]));
-      uint4 hi = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
-                            pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
-      *reinterpret_cast<uint4*>(S.a0 + core_off(tid, 0, 16)) = lo;
-      *reinterpret_cast<uint4*>(S.a0 + core_off(tid, 8, 16)) = hi;
+      const int k0 = chalf / 8;  // columns 0-7 (warps 0-3) or 8-15 (warps 4-7)
+      float v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        v[k] = (row < n && k0 + k < nin) ? x[row * in_stride + k0 + k] : 0.0f;
+      *reinterpret_cast<uint4*>(S.a0 + core_off(r, k0, 16)) =
+          make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                     pack_bf16(v[6], v[7]));
     }
     sync_for_mma();
     if (!layer(1)) break;
@@ -250,10 +263,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_tc(const uint4* __restrict__ img
     hidden_epilogue(S.bias + 2 * MLP_H);
     sync_for_mma();
     if (!layer(4)) break;
-    float o[16];
-    tc_ld16(trow, o);
-    if (row < n)
-      for (int k = 0; k < MLP_NOUT; k++) y[row * out_stride + k] = o[k] + S.bias[3 * MLP_H + k];
+    if (warp < 4) {  // the output columns 0-15, by the first four warps
+      float o[16];
+      tc_ld16(trow, o);
+      if (row < n)
+        for (int k = 0; k < MLP_NOUT; k++) y[row * out_stride + k] = o[k] + S.bias[3 * MLP_H + k];
+    }
     tc_fence_before();
     __syncthreads();
     if (S.abort) break;
@@ -320,16 +335,18 @@ cudaError_t mlp_tc_prepare() {
                               (int)sizeof(TcSmem));
 }
 
+// two CTAs per SM (2 x 112 KB of shared memory, 2 x 128 tensor-memory columns): one CTA's
+// epilogue runs while the other's MMAs do
 int mlp_tc_grid(int n_max, int num_sms) {
   const int ntiles = (n_max + kTcRows - 1) / kTcRows;
-  return ntiles < num_sms ? ntiles : num_sms;
+  return ntiles < 2 * num_sms ? ntiles : 2 * num_sms;
 }
 
 cudaError_t mlp_tc_forward(const void* img, const float* bias, const float* x, int in_stride,
                            int nin, const int* count, int n_max, float* y, int out_stride,
                            int* err, int err_bit, int grid, cudaStream_t st) {
   if (n_max <= 0 || grid <= 0) return cudaSuccess;
-  k_mlp_tc<<<grid, 128, sizeof(TcSmem), st>>>(static_cast<const uint4*>(img), bias, x,
+  k_mlp_tc<<<grid, kTcThreads, sizeof(TcSmem), st>>>(static_cast<const uint4*>(img), bias, x,
                                               in_stride, nin, count, n_max, y, out_stride, err,
                                               err_bit);
   return cudaGetLastError();
