@@ -699,7 +699,8 @@ def run_ours(args):
         sg.set_gate(ctx, args.surrogate_gate)
     tuned = sps_gb300.autotune(ctx, 2)  # launch shapes; the state is restored
     if fast:
-        tuned = dict(tuned, lookahead=sps_gb300.lookahead(ctx))
+        tuned = dict(tuned, lookahead=sps_gb300.lookahead(ctx),
+                     l2_prefetch=sps_gb300.prefetch(ctx))
     t = ctx.step(max(args.warmup, 1), 0.0)  # warm-up (also instantiates the step graph)
     kps = sps_gb300.kernels_per_step(ctx)
     if use_surr:

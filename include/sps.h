@@ -217,7 +217,7 @@ int sps_selftest_cone(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatche
    uploaded state, keep the fastest size per kernel, and restore the state, so the results
    of later steps are the same as without tuning.  blocks (may be NULL) receives the 8
    chosen sizes in that order.  The FP32 form then tunes its neighbour sums' look-ahead
-   the same way (sps_tuned_lookahead).  The cell size is not tuned: the reference's pair
+   the same way (sps_tuned_lookahead), then their L2 prefetch (sps_tuned_prefetch).  The cell size is not tuned: the reference's pair
    order depends on it. */
 int sps_autotune(sps_ctx* ctx, int32_t nsteps, int32_t* blocks);
 
@@ -227,6 +227,16 @@ int sps_autotune(sps_ctx* ctx, int32_t nsteps, int32_t* blocks);
    neighbours' list entries and records before it sums any of them, in the same order, so
    the results do not depend on these.  Defaults before tuning: 4 and 2. */
 int sps_tuned_lookahead(sps_ctx* ctx, int32_t* ahead);
+
+/* Whether the FP32 form's neighbour sums request their list entries into L2 ahead of use
+   (no reference counterpart): *flags bit 0 for the interpolation, bit 1 for the
+   derivative sums.  One lane of each warp issues a bulk L2 prefetch of the warp's entries;
+   a hint that changes no result.  sps_autotune times both settings after the look-ahead
+   and keeps the faster per group; the default before tuning is 0 (off). */
+int sps_tuned_prefetch(sps_ctx* ctx, int32_t* flags);
+
+/* Sets those flags directly (0 .. 3). */
+int sps_set_prefetch(sps_ctx* ctx, int32_t flags);
 
 /* Sets that look-ahead directly (interp 2, 4 or 8; derivs 1, 2 or 4), e.g. to reuse the
    values tuned on one context in another of the same workload. */

@@ -217,6 +217,7 @@ struct Dev {
   // at (j * N2 + c) * 2 (ell()), one 32-byte sector; keys flat at k * N2 + c
   int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)
   int32_t *degC, *degS;  // by list column
+  int l2_prefetch;  // FP32 form: bulk L2 prefetch of list entries (bit 0 interp, bit 1 derivs)
   // sorted positions of the stress-point and of the node targets (each in sorted order), so
   // that the gathers run one kind per warp
   int32_t *tgtS, *tgtN, *tflag, *toff;
@@ -247,6 +248,25 @@ struct Dev {
 // stay adjacent, so a warp reading entry k of its targets still reads one contiguous run.
 __device__ __forceinline__ size_t ell(int k, int col, int N2) {
   return (((size_t)(k >> 1) * (size_t)N2 + (size_t)col) << 1) | (size_t)(k & 1);
+}
+
+// Bulk L2 prefetch of the list entries of a warp's targets (one-kind launches, whose active
+// lanes hold consecutive list columns).  For each entry pair j from 1 to the warp's largest
+// degree, the 32-byte sectors of the warp's columns are one contiguous run (ell()), which
+// the warp's first active lane requests with one cp.async.bulk.prefetch.L2: the entries
+// stream from DRAM ahead of the dependent record gathers.  A hint: no result depends on it.
+__device__ __forceinline__ void prefetch_list_l2(const int4* list, int col, int deg, int N2) {
+  const unsigned act = __activemask();
+  const int maxdeg = (int)__reduce_max_sync(act, (unsigned)deg);
+  const int col0 = (int)__reduce_min_sync(act, (unsigned)col);
+  const int col1 = (int)__reduce_max_sync(act, (unsigned)col);
+  if ((int)(threadIdx.x & 31) == __ffs(act) - 1) {
+    const uint32_t bytes = (uint32_t)(col1 - col0 + 1) * 32u;
+    for (int j = 1; 2 * j < maxdeg; j++) {
+      const int4* p = list + ell(2 * j, col0, N2);
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+    }
+  }
 }
 
 // Correctly rounded a / b given y = RN(1/b), by Markstein's theorem (P. Markstein, "Computation

@@ -37,6 +37,8 @@ struct Kahan {
     s = t;
   }
   __device__ __forceinline__ double val() const { return (double)s - (double)c; }
+  // the compensated sum rounded to FP32
+  __device__ __forceinline__ float fval() const { return s - c; }
 };
 
 // sum of exact FP32 products: p = RN(a b) and e = a b - p (exact, by one FMA: the
@@ -57,6 +59,40 @@ struct ProdSum {
 // difference of two double-float values (hi + lo) in FP32
 __device__ __forceinline__ float dfdiff(float ah, float al, float bh, float bl) {
   return (ah - bh) + (al - bl);
+}
+
+// The node tail of get_derivatives / RK4 (tail_node without CSPM) in FP32: the divergence,
+// gravity with damping and the right-hand side carry the FP32 accuracy of the sums they
+// come from; only the RK4 accumulation of the FP64 state is FP64 (one fused multiply-add
+// per component, exact in its product since f2 is 1 or 2).
+__device__ __forceinline__ void tail_node_f32(const Dev& D, const StepScalars& sc, const Real& M,
+                                              int t, const float* g2, int bc_int, float avx,
+                                              float avy, double f2, double afx, double afy) {
+  D.bc_int[t] = bc_int;
+  const float div2x = -(g2[0] + g2[5]);
+  const float div2y = -(g2[2] + g2[4]);
+  float gx = 0.0f, gy = 0.0f;
+  if (M.ic_grav == 1) {
+    const float fg = f32_rn(sc.factg);
+    gx = fg * f32_rn(M.cgrav[0]);
+    gy = fg * f32_rn(M.cgrav[1]);
+  }
+  if (M.damping != 0.0) {
+    const float dmp = f32_rn(M.damping);
+    gx = fmaf(-dmp, f32_rn(D.vx[t]), gx);
+    gy = fmaf(-dmp, f32_rn(D.vy[t]), gy);
+  }
+  float rhsx = ((-div2x + gx) + avx) + f32_rn(D.fbx[t]);
+  float rhsy = ((-div2y + gy) + avy) + f32_rn(D.fby[t]);
+  if (afx != 0.0 || afy != 0.0) {
+    rhsx += f32_rn(afx);
+    rhsy += f32_rn(afy);
+  }
+  const double rx = f64_of(rhsx), ry = f64_of(rhsy);
+  D.RHS2[0][t] = rx;
+  D.RHS2[1][t] = ry;
+  D.RKv[0][t] = fma(f2, rx, D.RKv[0][t]);
+  D.RKv[1][t] = fma(f2, ry, D.RKv[1][t]);
 }
 
 // stress_point_update (2_SPH_main_2018.f90:403-482), FP32 sums.  A stress-point's velocity
@@ -98,6 +134,7 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
   }
   const int col = list_col<KIND>(D, k, s);
   int deg = D.degC[col];
+  if (KIND != 0 && (D.l2_prefetch & 1)) prefetch_list_l2(D.cross, col, deg, D.N2);
   if (KIND == 1 || (KIND == 0 && is_sp(tt))) {
     Kahan v0, v1, nm;
     bool have = false;
@@ -139,11 +176,13 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       const int4 e = D.cross[ell(k, col, D.N2)];
       if (e.y >= 0) term(__int_as_float(e.y), D.recV[e.x], D.recI[e.x].y);
     }
-    double norm = nm.val();
-    if (norm != 0) {
-      double rn = 1.0 / norm;
-      D.vx[t] = ((double)ref.x + (double)ref.z) + v0.val() * rn;
-      D.vy[t] = ((double)ref.y + (double)ref.w) + v1.val() * rn;
+    // the mean deviation in FP32 (its sums carry FP32 accuracy), added to the first
+    // node's velocity (hi + lo, exact in FP64): two FP64 additions per target
+    const float norm = nm.fval();
+    if (norm != 0.0f) {
+      const float rn = __frcp_rn(norm);
+      D.vx[t] = (f64_of(ref.x) + f64_of(ref.z)) + f64_of(v0.fval() * rn);
+      D.vy[t] = (f64_of(ref.y) + f64_of(ref.w)) + f64_of(v1.fval() * rn);
     }
   } else {
     Kahan a, b, c, d, iv, rt, nm;
@@ -180,19 +219,21 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       const int4 e = D.cross[ell(k, col, D.N2)];
       if (e.y >= 0) term(__int_as_float(e.y), D.recS[e.x], D.recI[e.x]);
     }
-    double norm = nm.val();
-    double rn = 1.0 / norm;
-    if (norm != 0) {
-      D.s0[t] = a.val() * rn;
-      D.s1[t] = b.val() * rn;
-      D.s2[t] = c.val() * rn;
-      D.s3[t] = d.val() * rn;
-      D.iv1[t] = iv.val() * rn;
+    // the weighted means in FP32 (no FP64 arithmetic): the sums carry FP32 accuracy
+    const float norm = nm.fval();
+    if (norm != 0.0f) {
+      const float rn = __frcp_rn(norm);
+      D.s0[t] = f64_of(a.fval() * rn);
+      D.s1[t] = f64_of(b.fval() * rn);
+      D.s2[t] = f64_of(c.fval() * rn);
+      D.s3[t] = f64_of(d.fval() * rn);
+      D.iv1[t] = f64_of(iv.fval() * rn);
+      if (D.cont_density) D.rho0[t] = f64_of(rt.fval() * rn);
     } else {
       D.vx[t] = 0.0;
       D.vy[t] = 0.0;
+      if (D.cont_density) D.rho0[t] = rt.val() / nm.val();
     }
-    if (D.cont_density) D.rho0[t] = rt.val() * rn;
   }
 }
 
@@ -209,18 +250,19 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
   if (k0 >= ntgt) return;
   const int s = tgt[k0];
   int t = D.sorted[s];
-  const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
-  const double f2 = f2rk[stage];
+  const double f2 = (stage == 1 || stage == 2) ? 2.0 : 1.0;  // RK4 weights 1, 2, 2, 1
   const Real& Mt = real_of(D, t);
   const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   const int col = list_col<KIND>(D, k0, s);
   int deg = D.degC[col];
+  if (D.l2_prefetch & 2) prefetch_list_l2(D.cross, col, deg, D.N2);
   const double xt = D.px[t], yt = D.py[t];
   if (KIND == 1) {
     Kahan g0, g1, g2, g3, e0, e1, e2, e3;
     const double vtx = D.vx[t], vty = D.vy[t];
-    const float vh0 = (float)vtx, vh1 = (float)vty;
-    const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
+    float vh0, vh1, vl0, vl1;
+    f32_split(vtx, vh0, vl0);
+    f32_split(vty, vh1, vl1);
     auto term = [&](const int4& e, float vol, float4 r) {
       const int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
@@ -279,14 +321,22 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       const int4 e = D.cross[ell(k, col, D.N2)];
       term(e, D.recI[e.x].y, e.y >= 0 ? D.recV[e.x] : z);
     }
-    double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
-    double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
-    tail_sp_grad(D, t, g, AE);  // the rates follow in k_fsp_tail
+    // the rates follow in k_fsp_tail
+    if (D.cspm) {
+      double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
+      double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
+      tail_sp_grad(D, t, g, AE);
+    } else {  // grad_u rounded to FP32 (its sums' accuracy), no FP64 arithmetic
+      double* gu = D.grad_u + 4 * (size_t)t;
+      gu[0] = f64_of(g0.fval());
+      gu[1] = f64_of(g1.fval());
+      gu[2] = f64_of(g2.fval());
+      gu[3] = f64_of(g3.fval());
+    }
   } else {
     Kahan q0, q1, q2, q3, q4, q5, e0, e1, e2, e3;
     ProdSum sx, sy;
     const float4 ah = D.recA[t], al = D.recAl[t];
-    const double At[3] = {D.A[0][t], D.A[1][t], D.A[2][t]};
     int bc_int = 0;
     auto term = [&](int4 e, float4 ra, float4 rl) {
       const int u = e.x;
@@ -313,9 +363,9 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         double ri = D.rinv[u];
         double ri2 = ri * ri;
         m = (float)D.mass[u];
-        d0 = (float)fma(D.s0[t], ri2, -At[0]);
-        d1 = (float)fma(D.s1[t], ri2, -At[1]);
-        d2 = (float)fma(D.s2[t], ri2, -At[2]);
+        d0 = (float)fma(D.s0[t], ri2, -D.A[0][t]);
+        d1 = (float)fma(D.s1[t], ri2, -D.A[1][t]);
+        d2 = (float)fma(D.s2[t], ri2, -D.A[2][t]);
       }
       float mx = m * dwx, my = m * dwy;
       q0.add(mx * d0);
@@ -351,15 +401,15 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
       term(e, e.y >= 0 ? D.recA[e.x] : z, e.y >= 0 ? D.recAl[e.x] : z);
     }
-    double avx = 0.0, avy = 0.0;
+    float avx = 0.0f, avy = 0.0f;
     if (Mt.alpha > 0 || Mt.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904) in FP32
       Kahan ax, ay;
       int degs = D.degS[col];
-      const double vtx = D.vx[t], vty = D.vy[t];
-      const float vh0 = (float)vtx, vh1 = (float)vty;
-      const float vl0 = (float)(vtx - (double)vh0), vl1 = (float)(vty - (double)vh1);
-      const float ht = (float)D.hsml[t], rt = (float)D.rho[t];
+      float vh0, vh1, vl0, vl1;
+      f32_split(D.vx[t], vh0, vl0);
+      f32_split(D.vy[t], vh1, vl1);
+      const float ht = f32_rn(D.hsml[t]), rt = f32_rn(D.rho[t]);
       for (int k = 0; k < degs; k++) {
         int4 e = D.same[ell(k, col, D.N2)];
         int u = e.x;
@@ -378,21 +428,35 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         ax.add(visc * __int_as_float(e.z) * ri.w);
         ay.add(visc * __int_as_float(e.w) * ri.w);
       }
-      avx = -ax.val();
-      avy = -ay.val();
+      avx = -ax.fval();
+      avy = -ay.fval();
     }
-    const double Sx = sx.val(), Sy = sy.val();
-    double g2v[6];
-    g2v[0] = -(q0.val() + 2.0 * At[0] * Sx);
-    g2v[1] = -(q1.val() + 2.0 * At[1] * Sx);
-    g2v[2] = -(q2.val() + 2.0 * At[2] * Sx);
-    g2v[3] = -(q3.val() + 2.0 * At[0] * Sy);
-    g2v[4] = -(q4.val() + 2.0 * At[1] * Sy);
-    g2v[5] = -(q5.val() + 2.0 * At[2] * Sy);
-    double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
+    // g2 = -(q + 2 A_t S) in FP32: A_t (hi + lo) times S (hi + lo) as a double-float
+    // product, so that the large, nearly cancelling part 2 A_t S keeps FP32 accuracy
+    // relative to the result
+    const float sxh = sx.hi.s, sxl = sx.lo - sx.hi.c, syh = sy.hi.s, syl = sy.lo - sy.hi.c;
+    auto g2of = [](float q, float ah_, float al_, float sh, float sl) {
+      const float p = ah_ * sh;
+      const float e = fmaf(ah_, sl, fmaf(al_, sh, fmaf(ah_, sh, -p)));
+      return -(fmaf(2.0f, p, q) + 2.0f * e);
+    };
+    float g2v[6];
+    g2v[0] = g2of(q0.fval(), ah.x, al.x, sxh, sxl);
+    g2v[1] = g2of(q1.fval(), ah.y, al.y, sxh, sxl);
+    g2v[2] = g2of(q2.fval(), ah.z, al.z, sxh, sxl);
+    g2v[3] = g2of(q3.fval(), ah.x, al.x, syh, syl);
+    g2v[4] = g2of(q4.fval(), ah.y, al.y, syh, syl);
+    g2v[5] = g2of(q5.fval(), ah.z, al.z, syh, syl);
     double afx = 0.0, afy = 0.0;
     if (D.art_stress) art_force_node(D, col, t, &afx, &afy);
-    tail_node(D, sc, t, g2v, AE, bc_int, avx, avy, f2, afx, afy);
+    if (D.cspm) {  // the CSPM correction in FP64 (the reference's form)
+      double g2d[6];
+      for (int q = 0; q < 6; q++) g2d[q] = f64_of(g2v[q]);
+      double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
+      tail_node(D, sc, t, g2d, AE, bc_int, f64_of(avx), f64_of(avy), f2, afx, afy);
+    } else {
+      tail_node_f32(D, sc, Mt, t, g2v, bc_int, avx, avy, f2, afx, afy);
+    }
   }
 }
 
@@ -448,8 +512,7 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
   const int lane = threadIdx.x & 31;
   const bool act = i < D.NT - D.NN;
   const int t = D.NN + (act ? i : 0);
-  const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
-  const double f2 = f2rk[stage];
+  const double f2 = (stage == 1 || stage == 2) ? 2.0 : 1.0;  // RK4 weights 1, 2, 2, 1
   const Real& M = real_of(D, t);
   const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   double g[4] = {0.0, 0.0, 0.0, 0.0}, s2v[4] = {0.0, 0.0, 0.0, 0.0};

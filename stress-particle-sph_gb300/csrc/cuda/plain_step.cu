@@ -517,8 +517,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
   }
   int t = D.sorted[s];
   if (t >= D.NT) return;
-  const double f2rk[4] = {1.0, 2.0, 2.0, 1.0};
-  const double f2 = f2rk[stage];
+  const double f2 = (stage == 1 || stage == 2) ? 2.0 : 1.0;  // RK4 weights 1, 2, 2, 1
   const Real& Mt = real_of(D, t);
   const StepScalars& sc = D.cur[D.R == 1 ? 0 : D.rid[t]];
   int tt = D.itype[t];

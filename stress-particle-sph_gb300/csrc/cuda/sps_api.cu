@@ -699,6 +699,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.rinv = dalloc<double>(c, N2);
     for (int k = 0; k < 3; k++) D.A[k] = dalloc<double>(c, NT);
     D.fast = (p->precision == SPS_PREC_FP32_FAST) ? 1 : 0;
+    D.l2_prefetch = 0;  // off until the autotuner finds it faster
     // stress-point and node targets in sorted order (both forms)
     D.tgtS = dalloc<int32_t>(c, NT - NN_ + 1);
     D.tgtN = dalloc<int32_t>(c, NN_ + 1);
@@ -1477,6 +1478,26 @@ int sps_tuned_lookahead(sps_ctx* h, int32_t* ahead) {
   return SPS_OK;
 }
 
+int sps_tuned_prefetch(sps_ctx* h, int32_t* flags) {
+  if (!h || !flags) return SPS_ERR_ARG;
+  *flags = h->c.d.l2_prefetch;
+  return SPS_OK;
+}
+
+int sps_set_prefetch(sps_ctx* h, int32_t flags) {
+  if (!h) return SPS_ERR_ARG;
+  sps::Ctx& c = h->c;
+  if (flags < 0 || flags > 3) return fail(&c, SPS_ERR_ARG, "sps_set_prefetch: flags 0 .. 3");
+  try {
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
+    c.d.l2_prefetch = flags;
+    drop_graphs(c);
+  } catch (const std::exception& e) {
+    return fail(&c, SPS_ERR_CUDA, e.what());
+  }
+  return SPS_OK;
+}
+
 int sps_set_lookahead(sps_ctx* h, int32_t interp, int32_t derivs) {
   if (!h) return SPS_ERR_ARG;
   sps::Ctx& c = h->c;
@@ -1710,6 +1731,26 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       }
       c.ahead[0] = best_la[0];
       c.ahead[1] = best_la[1];
+      // then the bulk L2 prefetch of the list entries, off and on for both groups
+      double best_pf_ms[2] = {1e300, 1e300};
+      int best_pf = 0;
+      for (int pf : {0, 3}) {
+        c.d.l2_prefetch = pf;
+        std::vector<std::string> kn;
+        std::vector<double> kms;
+        std::vector<int> kl;
+        std::fill(t.begin(), t.end(), 0.0);
+        c.itimestep = it0;
+        profile_run(c, nsteps, t.data(), kn, kms, kl);
+        copy(false);
+        for (int g = 0; g < 2; g++)
+          for (size_t q = 0; q < kn.size(); q++)
+            if (kn[q] == names[g] && kms[q] < best_pf_ms[g]) {
+              best_pf_ms[g] = kms[q];
+              best_pf = (best_pf & ~(1 << g)) | (pf & (1 << g));
+            }
+      }
+      c.d.l2_prefetch = best_pf;
     }
     c.surf_stale = stale;
     c.itimestep = it0;

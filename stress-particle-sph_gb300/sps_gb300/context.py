@@ -25,6 +25,8 @@ def gpu_lib():
         lib.sps_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         lib.sps_set_surface_detection.argtypes = [C.c_void_p, C.c_int32]
         lib.sps_tuned_lookahead.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        lib.sps_tuned_prefetch.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        lib.sps_set_prefetch.argtypes = [C.c_void_p, C.c_int32]
         lib.sps_set_lookahead.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         lib.sps_kernels_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         lib.sps_selftest_division.argtypes = [C.c_void_p, C.c_int64, C.c_uint64,
@@ -272,6 +274,19 @@ def lookahead(ctx):
     a = (C.c_int32 * 2)()
     ctx._call("tuned_lookahead", ctx._h, a)
     return {"interp": a[0], "derivs": a[1]}
+
+
+def prefetch(ctx):
+    """The FP32 neighbour sums' bulk L2 prefetch of list entries: {"interp": bool,
+    "derivs": bool} (sps_tuned_prefetch)."""
+    a = C.c_int32()
+    ctx._call("tuned_prefetch", ctx._h, C.byref(a))
+    return {"interp": bool(a.value & 1), "derivs": bool(a.value & 2)}
+
+
+def set_prefetch(ctx, interp, derivs):
+    """sps_set_prefetch: bulk L2 prefetch of list entries in the two neighbour-sum groups."""
+    ctx._call("set_prefetch", ctx._h, int(bool(interp)) | (2 * int(bool(derivs))))
 
 
 def set_lookahead(ctx, interp, derivs):

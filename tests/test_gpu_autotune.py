@@ -66,11 +66,14 @@ def test_lookahead_changes_nothing(built_gpu, make):
     # every look-ahead gives the same bits, so the autotuner may choose any
     p = make()
     res = []
-    for interp, derivs in ((4, 2), (2, 2), (2, 1), (8, 4)):
+    # and the bulk L2 prefetch of list entries is a hint: on or off, the same bits
+    for interp, derivs, pf in ((4, 2, 0), (2, 2, 3), (2, 1, 1), (8, 4, 2)):
         ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
                                     p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
         sps_gb300.set_lookahead(ctx, interp, derivs)
+        sps_gb300.set_prefetch(ctx, pf & 1, pf & 2)
         assert sps_gb300.lookahead(ctx) == {"interp": interp, "derivs": derivs}
+        assert sps_gb300.prefetch(ctx) == {"interp": bool(pf & 1), "derivs": bool(pf & 2)}
         ctx.upload_problem(p)
         ctx.step(10, 0.0)
         res.append(ctx.download())
