@@ -553,6 +553,13 @@ def kernel_bytes(name, prob, deg, fast=False):
         return ent * deg["cross"] + ns * (16 + 16) + nn * (40 + 16 + 16)
     if name == "half":
         return n2 * (4 * 8 + 8) + ent * deg["pairs"]
+    if fast and name == "gather":
+        # the FP32 form's direct lists: entries written (the same-kind lists' only when a
+        # step kernel reads them), and per particle its sorted record (16 + 8 B), its own
+        # offsets (20 B), ids, type, realisation and cell (16 B), counts (12 B), target (4 B)
+        p = prob.params
+        same_written = p.xsph or p.art_stress or p.alpha > 0 or p.beta > 0
+        return ent * (deg["cross"] + (deg["same"] if same_written else 0)) + n2 * 76
     if name == "lists":
         # entries written (the same-kind lists' only when a step kernel reads them: XSPH,
         # artificial viscosity or stress), and the creators' half-list entries read,

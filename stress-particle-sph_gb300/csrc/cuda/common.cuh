@@ -87,6 +87,9 @@ struct Real {
   double tanfi, coh, young, poiss;
   double alpha2, kc;  // adapt_stress2 constants (FP64)
   float alpha2f, kcf; // the same rounded to FP32 (the FP32 form's inside-the-cone test)
+  // drucker_prager's FP32 material constants (tan phi, alpha, k_c, G, K), evaluated once on
+  // the host in IEEE FP32 with the routine's expressions (the FP32 form's body reads them)
+  float dpf_alpha2, dpf_kc, dpf_G, dpf_K;
   double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
   double xmin_dom[2], xmax_dom[2];
   double cgrav[2];
@@ -298,9 +301,9 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
 // result is then discarded.  Zeros, which are common, are handled on the integer pipe.
 static __device__ __noinline__ float f32_rn_hw(double x) { return (float)x; }
 static __device__ __noinline__ double f64_of_hw(float f) { return (double)f; }
-static __device__ __noinline__ void f32_split_hw(double x, float& hi, float& lo) {
-  hi = (float)x;
-  lo = (float)(x - (double)hi);
+static __device__ __noinline__ float2 f32_split_hw(double x) {
+  const float hi = (float)x;
+  return make_float2(hi, (float)(x - (double)hi));
 }
 
 // RN-even double -> float, identical to (float)x
@@ -330,7 +333,9 @@ __device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
       lo = 0.0f;
       return;
     }
-    f32_split_hw(x, hi, lo);
+    const float2 v = f32_split_hw(x);  // returned by value: no local escapes to memory
+    hi = v.x;
+    lo = v.y;
     return;
   }
   const unsigned f23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
@@ -691,19 +696,16 @@ __device__ __forceinline__ void viscoplastic(const Real& M, const double* s, dou
 }
 
 // drucker_prager (3_SPH_material_2018.f90:1958-2083): FP32 body.  s: stress (plane-stress
-// szz already substituted), gu: grad_u(2,2).  Updates *fdp, returns G and vivel.
-// FAST (the FP32 form): the FP64 mean by a product with 1/3 instead of a division.
-template <bool FAST = false>
+// szz already substituted), gu: grad_u(2,2).  Updates *fdp, returns G and vivel.  (The FP32
+// form uses drucker_prager_f32.)
 __device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, const double* s,
                                                const double* gu, double* fdp, double* G,
                                                double* vivel) {
   double f0 = *fdp;
-  // FP32 form: the conversions on the integer pipe (bit-identical to the hardware ones)
-  auto tof = [](double v) { return FAST ? f32_rn(v) : (float)v; };
-  auto tod = [](float v) { return FAST ? f64_of(v) : (double)v; };
+  auto tof = [](double v) { return (float)v; };
+  auto tod = [](float v) { return (double)v; };
   float tanfi = tof(M.tanfi), coh = tof(M.coh), young = tof(M.young), poiss = tof(M.poiss);
-  float smean = FAST ? (float)(((s[0] + s[1]) + s[3]) * (1.0 / 3.0))
-                     : (float)(((s[0] + s[1]) + s[3]) / 3.0);
+  float smean = (float)(((s[0] + s[1]) + s[3]) / 3.0);
   const double smd = tod(smean);
   float dv0 = tof(s[0] - smd);
   float dv1 = tof(s[1] - smd);
@@ -742,6 +744,83 @@ __device__ __forceinline__ void drucker_prager(const Real& M, double time_sph, c
     vivel[1] = tod((sixth * rs) * ((2.0f * dv1 - dv0) - dv3)) * g2;
     vivel[2] = tod(rs * dv2) * g2;
     vivel[3] = tod((sixth * rs) * ((2.0f * dv3 - dv0) - dv1)) * g2;
+  } else {
+    G[0] = G[1] = G[2] = G[3] = 0.0;
+    vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0;
+  }
+}
+
+// exact a + b = s + e (Knuth's TwoSum: additions only, so nothing is contracted)
+__device__ __forceinline__ float two_sum_f(float a, float b, float& e) {
+  const float s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+  return s;
+}
+
+// a >= b for non-NaN doubles on the integer pipe: the bit patterns as ordered keys (the
+// magnitude bits of a negative value flipped, -0 taken as +0)
+__device__ __forceinline__ bool f64_ge(double a, double b) {
+  long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  if ((ia << 1) == 0) ia = 0;
+  if ((ib << 1) == 0) ib = 0;
+  ia ^= (ia >> 63) & 0x7FFFFFFFFFFFFFFFll;
+  ib ^= (ib >> 63) & 0x7FFFFFFFFFFFFFFFll;
+  return ia >= ib;
+}
+
+// drucker_prager for the FP32 form, without FP64 arithmetic (GB300 issues FP64 at 1/64 of
+// its FP32 rate): the stresses enter as hi + lo splits, the mean is formed in double-float
+// and the deviator from it, so each deviatoric component keeps FP32 accuracy relative to
+// itself; the loading test df >= 0 compares the FP64 values exactly on the integer pipe; the
+// material constants are the host's FP32 evaluation (dpf_*).  Same outputs as
+// drucker_prager: the updated f, the plastic source G and vivel.
+__device__ __forceinline__ void drucker_prager_f32(const Real& M, double time_sph,
+                                                   const double* s, const double* gu,
+                                                   double* fdp, double* G, double* vivel) {
+  const double f0 = *fdp;
+  float s0h, s0l, s1h, s1l, s3h, s3l;
+  f32_split(s[0], s0h, s0l);
+  f32_split(s[1], s1h, s1l);
+  f32_split(s[3], s3h, s3l);
+  float e1, e2;
+  const float t1 = two_sum_f(s0h, s1h, e1);
+  const float th = two_sum_f(t1, s3h, e2);
+  const float tl = ((e1 + e2) + (s0l + s1l)) + s3l;
+  const float mh = __fdiv_rn(th, 3.0f);
+  const float ml = __fmul_rn(__fadd_rn(fmaf(-3.0f, mh, th), tl), 1.0f / 3.0f);
+  const float smean = mh + ml;
+  const float dv0 = (s0h - mh) + (s0l - ml);
+  const float dv1 = (s1h - mh) + (s1l - ml);
+  const float dv3 = (s3h - mh) + (s3l - ml);
+  const float dv2 = f32_rn(s[2]);
+  const float varj2 = fmaf(dv2, dv2, 0.5f * fmaf(dv0, dv0, fmaf(dv1, dv1, dv3 * dv3)));
+  const float vari1 = 3.0f * smean;
+  const float eps11 = f32_rn(gu[0]);
+  const float eps12 = 0.5f * (f32_rn(gu[2]) + f32_rn(gu[1]));
+  const float eps22 = f32_rn(gu[3]);
+  const float emean = eps11 + eps22;
+  const float alpha2 = M.dpf_alpha2, kc = M.dpf_kc;
+  const float yield = kc - alpha2 * vari1;
+  const float sj = sqrtf(varj2);
+  const float f1 = sj - yield;
+  *fdp = f64_of(f1);
+  const float s_eps = fmaf(dv0, eps11, fmaf(2.0f * dv2, eps12, dv1 * eps22));
+  if (__double_as_longlong(time_sph) > 0 && f1 >= 0.0f && f64_ge(f64_of(f1), f0) &&
+      sj >= 1e-5f) {
+    const float G_mod = M.dpf_G, K_mod = M.dpf_K;
+    const float gs = __fdiv_rn(G_mod, sj);
+    const float lambda_1 = ((3.0f * alpha2) * K_mod) * emean;
+    const float G2 = __fdiv_rn(fmaf(gs, s_eps, lambda_1), G_mod);
+    G[0] = f64_of((gs * dv0) * G2);
+    G[1] = f64_of((gs * dv1) * G2);
+    G[2] = f64_of((gs * dv2) * G2);
+    G[3] = f64_of((gs * dv3) * G2);
+    const float rs = __frcp_rn(sj), r6 = rs * (1.0f / 6.0f);
+    vivel[0] = f64_of((r6 * ((2.0f * dv0 - dv1) - dv3)) * G2);
+    vivel[1] = f64_of((r6 * ((2.0f * dv1 - dv0) - dv3)) * G2);
+    vivel[2] = f64_of((rs * dv2) * G2);
+    vivel[3] = f64_of((r6 * ((2.0f * dv3 - dv0) - dv1)) * G2);
   } else {
     G[0] = G[1] = G[2] = G[3] = 0.0;
     vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0;
@@ -788,6 +867,7 @@ void launch_surface(Ctx& c);
 void launch_surface_f32(Ctx& c);
 void launch_lists_keys(Ctx& c);
 void launch_lists_same(Ctx& c);
+void ensure_half_lists(Ctx& c);
 void launch_fxsph(Ctx& c);
 void launch_selftest_div(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);
 void launch_selftest_conv(Ctx& c, int64_t n, uint64_t seed, unsigned long long* d_bad);

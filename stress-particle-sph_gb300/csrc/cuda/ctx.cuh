@@ -81,6 +81,19 @@ struct Ctx {
   bool surface_exact = false;
   bool surface_f32() const { return precision == SPS_PREC_FP32_FAST && !surface_exact; }
   int64_t last_refresh = -1;   // steps_done at the last on-demand detection
+  // FP32 form: the steps build their lists straight from the cell stencil (k_fgather) unless
+  // every step runs the exact free-surface detection (its keyed lists come from the half
+  // lists), the smoothing lengths evolve (sle 2: a rebuild after the step could not repeat
+  // the build's band test) or the list capacity leaves no room for the gather's shared
+  // memory (two lists of capC ints for each of 32 threads within 48 KB)
+  bool lists_direct() const {
+    return precision == SPS_PREC_FP32_FAST && !surf_every && d.sle != 2 &&
+           2 * d.capC * 32 * 4 <= 49152;
+  }
+  // the last pair build left the half lists unwritten (k_fgather): sps_dump_pairs and the
+  // keyed lists of the exact detection build them first (set by enqueue_step for every
+  // step, since a replayed graph runs no host code)
+  bool half_stale = false;
   int step_variant = 0;    // the variant launch_*_step enqueues
   int64_t itimestep = 0;   // itimestep_sph of the last step (0 after an upload)
   bool use_graph = true;

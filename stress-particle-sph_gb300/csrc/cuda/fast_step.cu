@@ -362,10 +362,13 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         bc_int = 1;
         double ri = D.rinv[u];
         double ri2 = ri * ri;
+        const double rt = D.rinv[t];
+        const double rt2 = rt * rt;  // A_t = sigma_t (1/rho_t)^2, as k_adapt_bc forms it
+        const double st0 = D.s0[t], st1 = D.s1[t], st2 = D.s2[t];
         m = (float)D.mass[u];
-        d0 = (float)fma(D.s0[t], ri2, -D.A[0][t]);
-        d1 = (float)fma(D.s1[t], ri2, -D.A[1][t]);
-        d2 = (float)fma(D.s2[t], ri2, -D.A[2][t]);
+        d0 = (float)fma(st0, ri2, -(st0 * rt2));
+        d1 = (float)fma(st1, ri2, -(st1 * rt2));
+        d2 = (float)fma(st2, ri2, -(st2 * rt2));
       }
       float mx = m * dwx, my = m * dwy;
       q0.add(mx * d0);
@@ -463,15 +466,13 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
 // Stress-point rates of the FP32 form (after k_fderivs has stored grad_u): one thread per
 // stress-point, one warp per 32 consecutive stress-points, so that the FP64 tail runs in
 // its own kernel on contiguous stress-points instead of diverging against the node branch
-// of k_fderivs.  With the learned surrogate installed, loading stress-points whose inputs
-// lie in the training envelope are packed into 16-row tiles of the warp and sent through
-// the network together on the tensor cores (mma.m16n8k16, BF16 in, FP32 accumulate); a
+// of k_fderivs.  With the learned surrogate installed (and its gate open for the step),
+// loading stress-points whose inputs lie in the training envelope have been appended as
+// rows by k_fsp_cand and run through the network by the tensor-core kernel (mlp_tc.cu); a
 // prediction is kept when the yield-function drift it causes over one step,
 //   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
 // is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
 // Every other stress-point takes the exact flow rule.
-// One stress-point (index i among the stress-points) of k_fsp_tail; the warp's 32 lanes
-// call it together.  xs, ys: the warp's tile rows.
 // The surrogate's view of stress-point t: the exact rule (drucker_prager, whose results dp
 // = {G, vivel, f} the tail reuses), whether it is loading, and for a loading point the
 // network's inputs x, their output scale and whether they lie in the training envelope.
@@ -488,7 +489,7 @@ __device__ __forceinline__ void surr_front(const Dev& D, const Real& M, const St
   s2v[3] = D.s3[t];
   if (M.ntype_solid == 1) s2v[3] = M.poiss * (s2v[0] + s2v[1]);
   double f = D.fdp[t], G2[4], vivel[4];
-  drucker_prager<true>(M, sc.time_sph, s2v, g, &f, G2, vivel);  // the exact rule
+  drucker_prager_f32(M, sc.time_sph, s2v, g, &f, G2, vivel);  // the exact rule
   loading = G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0;
   for (int k = 0; k < 4; k++) {
     dp[k] = G2[k];

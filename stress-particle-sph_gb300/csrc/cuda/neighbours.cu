@@ -321,7 +321,7 @@ __global__ void k_spos(Dev D) {
   if (s >= D.N2) return;
   const int t = D.sorted[s];
   D.spos[t] = s;
-  D.srec[s] = make_float4(D.xr[t], D.yr[t], D.hr[t], 0.0f);
+  D.srec[s] = make_float4(D.xr[t], D.yr[t], D.hr[t], __int_as_float(D.itype[t]));
   if (D.fast) D.srecl[s] = make_float2(D.xrl[t], D.yrl[t]);
 }
 
@@ -616,6 +616,193 @@ __global__ void k_half(Dev D) {
   }
 }
 
+// entries 2j and 2j+1 of a list column in one 32-byte store (ell(): one sector, 32-byte
+// aligned), so that no sector of the lists is ever written in halves
+__device__ __forceinline__ void store_pair(int4* dst, int4 a, int4 b) {
+  asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst), "r"(a.x),
+               "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+               : "memory");
+}
+
+// ---------------------------------------------------------------- FP32 form: direct lists
+// The FP32 form builds each target's lists straight from its 3 x 3 cell stencil, without
+// the half lists and the search through them.  Scanning the stencil's cells in ascending
+// sorted position visits a target's partners in the reference's creation order of their
+// pairs: first the creators before it (the row below, the cell to its left, its own cell
+// up to it), one pair each, then its own half list (the rest of its cell, the cell to its
+// right, the row above).  The lists hold that order; the FP32 form's sums use it in every
+// step (the plain form's walk order reverses the newest pairs in steps where the pair
+// count reaches a new maximum).
+// The pair test is the same symmetric test (prefilter and exact FP64 band test), and the
+// kernel values are evaluated with the target in the creator's role: the separation is
+// negated exactly (double-float additions and the cell shift are sign-symmetric), so W is
+// the same bits as the creator's evaluation and the gradient its exact negation.  Every
+// target also counts the partners after it, which is its half-list length (half_cnt), for
+// the pair count bookkeeping; dummies and inactive positions are counted by k_fgather_rest.
+
+// the list entry of partner bs (cell offset qx, qy) of a target of type ta with FP32
+// cell-relative offsets (xa, xal), (ya, yal) and smoothing length ha: {partner id, W (sign
+// bit set for a dummy partner), dW/dx, dW/dy} with the gradient with respect to the target
+__device__ __forceinline__ int4 gather_entry(const Dev& D, const Grid& g, int ta, float xa,
+                                             float ya, float ha, float xal, float yal, int bs,
+                                             int qx, int qy) {
+  const int b = D.sorted[bs];
+  const float4 rb = D.srec[bs];
+  float wf, d0f, d1f;
+  if (g.uniform_h) {
+    const float2 rl = D.srecl[bs];
+    dfl ddx = df_add(df_add({xa, xal}, {-rb.x, -rl.x}),
+                     {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
+    dfl ddy = df_add(df_add({ya, yal}, {-rb.y, -rl.y}),
+                     {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
+    cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
+  } else {
+    const float cx = (float)qx * (float)g.deltx[0], cy = (float)qy * (float)g.deltx[1];
+    const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
+    const float hm = (ha + rb.z) * 0.5f;
+    const float rf = sqrtf(fx * fx + fy * fy);
+    sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
+  }
+  const int pt = pint_type(ta, __float_as_int(rb.w));
+  const int w = __float_as_int(wf);
+  return make_int4(b, (pt == 6 || pt == 9) ? (int)((unsigned)w | 0x80000000u) : w,
+                   __float_as_int(d0f), __float_as_int(d1f));
+}
+
+// the accepted-partner test of the pair search, from either side of the pair
+__device__ __forceinline__ bool gather_accept(const Dev& D, int a, float xa, float ya, float ha,
+                                              float4 rb, int bs, float cx, float cy, float tau) {
+  float fx, fy;
+  const int pf = prefilter(D, xa, ya, ha, rb, cx, cy, tau, fx, fy);
+  if (pf == 0) return false;
+  if (pf == 2) {
+    double r, dx, dy, mh;
+    return exact_test(D, a, D.sorted[bs], r, dx, dy, mh);
+  }
+  return true;
+}
+
+// KIND 1: the stress-point targets tgt[0..n), 2: the node targets.  SAME: the same-kind
+// entries are written too (the steps that read them: XSPH, artificial viscosity or stress,
+// the FP32 free-surface detection).  Phase 1 tests the stencil's candidates and keeps the
+// accepted ones (sorted position and cell offset) in shared memory; phase 2 evaluates the
+// kernel values, so that a warp's lanes evaluate together.  Dynamic shared memory:
+// (capC + SAME capS) ints per thread, entry k of thread j at k * blockDim + j.
+template <int KIND, bool SAME>
+__global__ void k_fgather(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
+  extern __shared__ int gbuf[];
+  const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k0 >= ntgt) return;
+  const int bd = blockDim.x, tid = threadIdx.x;
+  int* bufC = gbuf;
+  int* bufS = gbuf + (size_t)D.capC * bd;
+  const int s = tgt[k0];
+  const int col = list_col<KIND>(D, k0, s);
+  int nC = 0, nS = 0, nHalf = 0;
+  if (s < D.gtot->nactive) {
+    const int a = D.sorted[s];
+    const int ta = D.itype[a];
+    const Grid& g = D.grid[D.rid[a]];
+    const float tau = g.tau;
+    const int c = D.cell_of[a] - g.cell0;
+    const int nx = g.ndiv[0], ny = g.ndiv[1];
+    const int ix = c % nx, iy = c / nx;
+    const float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
+    const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
+    for (int qy = -1; qy <= 1; qy++) {
+      const int jy = iy + qy;
+      if (jy < 0 || jy >= ny) continue;
+      for (int qx = -1; qx <= 1; qx++) {
+        const int jx = ix + qx;
+        if (jx < 0 || jx >= nx) continue;
+        const int cc = g.cell0 + jy * nx + jx;
+        const int lo = D.cell_start[cc], hi = lo + D.cell_cnt[cc];
+        const float cx = (float)qx * cw, cy = (float)qy * ch;
+        const int code = (qy + 1) * 3 + (qx + 1);  // cell offset, kept in the top 4 bits
+        for (int bs = lo; bs < hi; bs++) {
+          if (bs == s) continue;
+          const float4 rb = D.srec[bs];
+          if (!gather_accept(D, a, xa, ya, ha, rb, bs, cx, cy, tau)) continue;
+          nHalf += bs > s;
+          if (__float_as_int(rb.w) == ta) {
+            if (SAME && nS < D.capS) bufS[(size_t)nS * bd + tid] = bs | (code << kHalfTypeShift);
+            nS++;
+          } else {
+            if (nC < D.capC) bufC[(size_t)nC * bd + tid] = bs | (code << kHalfTypeShift);
+            nC++;
+          }
+        }
+      }
+    }
+    if (nHalf > D.capH) {
+      atomicOr(D.err, ERR_HALF_CAP);
+      nHalf = D.capH;
+    }
+    if (nC > D.capC || nS > D.capS) {
+      atomicOr(D.err, ERR_LIST_CAP);
+      nC = min(nC, D.capC);
+      nS = min(nS, D.capS);
+    }
+    const float xal = D.xrl[a], yal = D.yrl[a];
+    // phase 2: the entries, stored in pairs (whole 32-byte sectors)
+    auto finish = [&](const int* buf, int n, int4* list) {
+      int4 pend = make_int4(0, 0, 0, 0);
+      for (int k = 0; k < n; k++) {
+        const unsigned v = (unsigned)buf[(size_t)k * bd + tid];
+        const int code = (int)(v >> kHalfTypeShift);
+        const int4 e = gather_entry(D, g, ta, xa, ya, ha, xal, yal, (int)(v & kHalfIdMask),
+                                    code % 3 - 1, code / 3 - 1);
+        if (k & 1) store_pair(list + ell(k - 1, col, D.N2), pend, e);
+        else pend = e;
+      }
+      if (n & 1) list[ell(n - 1, col, D.N2)] = pend;
+    };
+    finish(bufC, nC, D.cross);
+    if (SAME) finish(bufS, nS, D.same);
+  }
+  D.degC[col] = nC;
+  D.degS[col] = nS;
+  D.half_cnt[s] = nHalf;
+}
+
+// every sorted position that is not a stress-point or node target: the half-list length
+// of an active dummy (its pairs with the particles after it in its half stencil), zero
+// counts for inactive positions and dummies' list columns
+__global__ void k_fgather_rest(Dev D) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.N2) return;
+  const int a = D.sorted[s];
+  if (a < D.NT) return;  // a stress-point or node target: k_fgather
+  const int col = D.lcol[s];
+  D.degC[col] = 0;
+  D.degS[col] = 0;
+  int k = 0;
+  if (s < D.gtot->nactive) {
+    const Grid& g = D.grid[D.rid[a]];
+    const int c = D.cell_of[a] - g.cell0;
+    const int nx = g.ndiv[0], ny = g.ndiv[1];
+    const int ix = c % nx, iy = c / nx;
+    const float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
+    const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
+    const int cells[5][2] = {{0, 0}, {1, 0}, {-1, 1}, {0, 1}, {1, 1}};
+    for (int q = 0; q < 5; q++) {
+      const int jx = ix + cells[q][0], jy = iy + cells[q][1];
+      if (jx < 0 || jx >= nx || jy >= ny) continue;
+      const int cc = g.cell0 + jy * nx + jx;
+      const int lo = q == 0 ? s + 1 : D.cell_start[cc];
+      const int hi = D.cell_start[cc] + D.cell_cnt[cc];
+      const float cx = (float)cells[q][0] * cw, cy = (float)cells[q][1] * ch;
+      for (int bs = lo; bs < hi; bs++)
+        k += gather_accept(D, a, xa, ya, ha, D.srec[bs], bs, cx, cy, g.tau);
+    }
+    if (k > D.capH) {
+      atomicOr(D.err, ERR_HALF_CAP);
+      k = D.capH;
+    }
+  }
+  D.half_cnt[s] = k;
+}
+
 // pair counts of every realisation (its pairs are the half lists of its sorted range)
 __global__ void k_pair_meta(Dev D) {
   const GridTotal gt = *D.gtot;
@@ -635,14 +822,6 @@ __global__ void k_pair_meta(Dev D) {
   }
   // walk-order keys hold 2 x position in 32 bits
   if (threadIdx.x == 0 && D.half_off[D.N2] > 1073741823LL) atomicOr(D.err, ERR_NPAIRS);
-}
-
-// entries 2j and 2j+1 of a list column in one 32-byte store (ell(): one sector, 32-byte
-// aligned), so that no sector of the lists is ever written in halves
-__device__ __forceinline__ void store_pair(int4* dst, int4 a, int4 b) {
-  asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst), "r"(a.x),
-               "r"(a.y), "r"(a.z), "r"(a.w), "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
-               : "memory");
 }
 
 template <bool KEYS>
@@ -960,6 +1139,37 @@ void launch_lists(Ctx& c, bool keys, bool same = false) {
   else k_lists<false><<<c.grid_of(TK_LISTS, D.N2), c.blk[TK_LISTS], pend, c.stream>>>(D);
 }
 
+// the targets split by kind: their sorted positions (tgtS, tgtN) and every position's list
+// column (lcol)
+void split_targets(Ctx& c) {
+  const Dev& D = c.d;
+  const int nb = (D.N2 + kBlock - 1) / kBlock;
+  k_target_flags<<<nb, kBlock, 0, c.stream>>>(D);
+  scan_i32_to_i32(c, D.tflag, D.toff, D.N2);
+  scan_i32_to_i32(c, D.tflag + D.N2, D.toff + D.N2 + 1, D.N2);
+  k_target_scatter<<<nb, kBlock, 0, c.stream>>>(D);
+}
+
+// FP32 form: the lists straight from the cell stencil (k_fgather, one launch per target
+// kind) and the remaining positions' counts; the block size is the tuned pair-search size,
+// lowered until each thread's candidate lists fit 48 KB of shared memory
+void launch_gather(Ctx& c, bool same, const Dev& D) {
+  const size_t per_thread = sizeof(int) * (size_t)(D.capC + (same ? D.capS : 0));
+  int b = c.blk[TK_HALF];
+  while (b > 32 && per_thread * (size_t)b > 49152) b >>= 1;
+  const size_t sm = per_thread * (size_t)b;
+  const int ns = D.NT - D.NN;
+  c.kernels_launched += 2;
+  if (same) {
+    if (ns > 0) k_fgather<1, true><<<(ns + b - 1) / b, b, sm, c.stream>>>(D, D.tgtS, ns);
+    if (D.NN > 0) k_fgather<2, true><<<(D.NN + b - 1) / b, b, sm, c.stream>>>(D, D.tgtN, D.NN);
+  } else {
+    if (ns > 0) k_fgather<1, false><<<(ns + b - 1) / b, b, sm, c.stream>>>(D, D.tgtS, ns);
+    if (D.NN > 0) k_fgather<2, false><<<(D.NN + b - 1) / b, b, sm, c.stream>>>(D, D.tgtN, D.NN);
+  }
+  k_fgather_rest<<<(D.N2 + kBlock - 1) / kBlock, kBlock, 0, c.stream>>>(D);
+}
+
 int launch_pair_build(Ctx& c) {
   Dev& D = c.d;
   cudaStream_t st = c.stream;
@@ -980,6 +1190,21 @@ int launch_pair_build(Ctx& c) {
   k_cell_sort<<<(D.cell_cap + 1 + kBlock - 1) / kBlock, kBlock, 0, st>>>(D);
   c.mark("spos");
   k_spos<<<nb, kBlock, 0, st>>>(D);
+  // variant bit 2: a download follows most steps; the exact detection wants the keys, the
+  // FP32 detection only the same-kind entries
+  const bool want = (c.step_variant & 4) != 0;
+  if (c.lists_direct()) {
+    c.mark("split_targets", 8);
+    split_targets(c);
+    c.mark("gather");
+    launch_gather(c, D.same_entries || want, D);
+    c.mark("scan_half", 3);
+    scan_i32_to_i64(c, D.half_cnt, D.half_off, D.N2);
+    c.mark("pair_meta");
+    k_pair_meta<<<1, 128, 0, st>>>(D);
+    c.half_stale = true;
+    return 0;
+  }
   c.mark("half");
   if (c.precision == SPS_PREC_FP32_FAST)
     k_half<true><<<c.grid_of(TK_HALF, D.N2), c.blk[TK_HALF], 0, st>>>(D);
@@ -989,23 +1214,44 @@ int launch_pair_build(Ctx& c) {
   c.mark("pair_meta");
   k_pair_meta<<<1, 128, 0, st>>>(D);
   c.mark("split_targets", 8);
-  k_target_flags<<<nb, kBlock, 0, st>>>(D);
-  scan_i32_to_i32(c, D.tflag, D.toff, D.N2);
-  scan_i32_to_i32(c, D.tflag + D.N2, D.toff + D.N2 + 1, D.N2);
-  k_target_scatter<<<nb, kBlock, 0, st>>>(D);
+  split_targets(c);
   c.mark("lists");
-  // variant bit 2: a download follows most steps; the exact detection wants the keys, the
-  // FP32 detection only the same-kind entries
-  const bool want = (c.step_variant & 4) != 0;
   launch_lists(c, c.surf_every || (want && !c.surface_f32()), want);
+  c.half_stale = false;
   return 0;
+}
+
+// The device view of the last pair build for a rebuild after the step: the FP64 positions
+// the build's exact band test read (x0x, x0y hold them from the step's start, before
+// anything moved; the smoothing lengths are constant when the lists are gathered), so the
+// rebuild decides every pair as the build did.  The cell-frame offsets and sorted records
+// are the build's own.
+Dev build_view(const Ctx& c) {
+  Dev D = c.d;
+  D.px = D.x0x;
+  D.py = D.x0y;
+  return D;
+}
+
+// the half lists of the last pair build, when it gathered the lists directly (the FP32
+// form): the same pairs, counts and creation order
+void ensure_half_lists(Ctx& c) {
+  if (!c.half_stale) return;
+  k_half<true><<<c.grid_of(TK_HALF, c.d.N2), c.blk[TK_HALF], 0, c.stream>>>(build_view(c));
+  c.half_stale = false;
 }
 
 // the lists of the last step again, now with their walk-order keys (the on-demand
 // free-surface detection; the lists are rebuilt identically)
-void launch_lists_keys(Ctx& c) { launch_lists(c, true); }
+void launch_lists_keys(Ctx& c) {
+  ensure_half_lists(c);
+  launch_lists(c, true);
+}
 
 // the lists of the last step again with the same-kind entries (the FP32 detection)
-void launch_lists_same(Ctx& c) { launch_lists(c, false, true); }
+void launch_lists_same(Ctx& c) {
+  if (c.lists_direct() && c.half_stale) launch_gather(c, true, build_view(c));
+  else launch_lists(c, false, true);
+}
 
 }  // namespace sps

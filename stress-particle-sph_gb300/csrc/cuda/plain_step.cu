@@ -94,11 +94,15 @@ __global__ void k_next_step(Dev D) {
   g.ans0 = a;
 }
 
+// over every particle (N2): the dummies' positions are kept too, so that x0x, x0y hold the
+// positions of the step's pair build for every particle (a rebuild of the lists after the
+// step decides its band pairs from them)
 __global__ void k_step_init(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= D.NT) return;
+  if (i >= D.N2) return;
   D.x0x[i] = D.px[i];
   D.x0y[i] = D.py[i];
+  if (i >= D.NT) return;
   D.vx0[i] = D.vx[i];
   D.vy0[i] = D.vy[i];
   if (i >= D.NN) {
@@ -214,10 +218,10 @@ __global__ void k_bound(Dev D) {
 __global__ void k_stage_begin(Dev D, int stage) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
-  const double f1rk[4] = {0.0, 0.5, 0.5, 1.0};
+  const double f1 = stage == 0 ? 0.0 : stage == 3 ? 1.0 : 0.5;  // RK4 nodes 0, 1/2, 1/2, 1
   const int r = D.R == 1 ? 0 : D.rid[i];
   const Real& M = real_of(D, i);
-  const double f1dt = f1rk[stage] * M.dt;
+  const double f1dt = f1 * M.dt;
   const StepScalars& sc = D.cur[r];
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
@@ -375,13 +379,11 @@ __global__ void k_adapt_bc(Dev D, int with_A, int bcs = 1) {
   }
   if (with_A) {
     if (D.fast) {
-      // sigma / rho^2 as sigma (1/rho)^2: no FP64 division (the records carry ~48 bits)
+      // sigma / rho^2 as sigma (1/rho)^2: no FP64 division (the records carry ~48 bits);
+      // only the records are stored (k_fderivs forms the FP64 value again where it needs it)
       double ri = D.rinv[i];
       double ri2 = ri * ri;
       double A0 = a * ri2, A1 = b * ri2, A2 = c * ri2;
-      D.A[0][i] = A0;
-      D.A[1][i] = A1;
-      D.A[2][i] = A2;
       float h0, h1, h2, l0, l1, l2;
       f32_split(A0, h0, l0);
       f32_split(A1, h1, l1);
@@ -932,7 +934,7 @@ int launch_plain_step(Ctx& c) {
     k_adapt_bc<<<c.grid_of(TK_ADAPT, D.NT), c.blk[TK_ADAPT], 0, st>>>(D, 0, 0);
   }
   c.mark("step_init");
-  k_step_init<<<nbT, kBlock, 0, st>>>(D);
+  k_step_init<<<(D.N2 + kBlock - 1) / kBlock, kBlock, 0, st>>>(D);
   if (D.inside) {
     c.mark("bound");
     k_bound<<<nbN, kBlock, 0, st>>>(D);

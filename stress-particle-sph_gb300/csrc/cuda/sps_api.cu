@@ -322,8 +322,10 @@ int variant_of(const sps::Ctx& c, int64_t it) {
 void enqueue_step(sps::Ctx& c) {
   c.itimestep += 1;
   c.step_variant = variant_of(c, c.itimestep) | (c.keys_in_step ? 4 : 0);
-  c.keys_written = (c.keys_in_step && !c.surface_f32()) || c.surf_every;
+  c.keys_written = (c.keys_in_step && !c.surface_f32() && !c.lists_direct()) || c.surf_every;
   c.same_written = c.keys_in_step || c.surf_every || c.d.same_entries;
+  // set here, on the host, for every step: a replayed graph runs no host code
+  c.half_stale = c.lists_direct();
   if (c.use_graph && !c.profiling) {
     if (!c.graphs[c.step_variant]) build_graph(c);
     SPS_CUDA_CHECK(cudaGraphLaunch(c.graphs[c.step_variant], c.stream));
@@ -575,6 +577,15 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
       M.kc_shift = M.alpha2 > 0.0 ? M.kc / (3.0 * M.alpha2) : 0.0;
       M.alpha2f = (float)M.alpha2;
       M.kcf = (float)M.kc;
+      {  // drucker_prager's FP32 constants (host FP32, no contraction: -ffp-contract=off)
+        const float tf = (float)M.tanfi, cf = (float)M.coh, yf = (float)M.young,
+                    pf = (float)M.poiss;
+        const float denf = std::sqrt(9.0f + 12.0f * (tf * tf));
+        M.dpf_alpha2 = tf / denf;
+        M.dpf_kc = (3.0f * cf) / denf;
+        M.dpf_G = yf / (2.0f * (1.0f + pf));
+        M.dpf_K = yf / (3.0f * (1.0f - 2.0f * pf));
+      }
       for (int d = 0; d < 2; d++) {
         M.xmin_dom[d] = q.xmin_domain[d];
         M.xmax_dom[d] = q.xmax_domain[d];
@@ -655,8 +666,8 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
     D.subset = dalloc<int8_t>(c, NT);
     D.fint = dalloc<float>(c, NT);
     D.vol32 = p->precision == SPS_PREC_FP32_FAST ? dalloc<float>(c, NT) : nullptr;
-    D.x0x = dalloc<double>(c, NT);
-    D.x0y = dalloc<double>(c, NT);
+    D.x0x = dalloc<double>(c, N2);  // every particle: the positions of the step's pair build
+    D.x0y = dalloc<double>(c, N2);
     D.vx0 = dalloc<double>(c, NT);
     D.vy0 = dalloc<double>(c, NT);
     for (int k = 0; k < 4; k++) {
@@ -1313,6 +1324,9 @@ int sps_dump_pairs_real(sps_ctx* h, int32_t r, int32_t* pair_i, int32_t* pair_j,
       return SPS_OK;
     }
     if (*npairs < meta.n) return fail(&c, SPS_ERR_CAPACITY, "sps_dump_pairs: buffer too small");
+    sps::ensure_half_lists(c);  // after a step that gathered its lists directly
+    SPS_CUDA_CHECK(cudaGetLastError());
+    SPS_CUDA_CHECK(cudaStreamSynchronize(c.stream));
     SPS_CUDA_CHECK(cudaMemcpy(&g, D.grid + r, sizeof(g), cudaMemcpyDeviceToHost));
     SPS_CUDA_CHECK(cudaMemcpy(&gt, D.gtot, sizeof(gt), cudaMemcpyDeviceToHost));
     int32_t lohi[2] = {0, 0};
@@ -1696,7 +1710,9 @@ int sps_autotune(sps_ctx* h, int32_t nsteps, int32_t* blocks) {
       copy(false);
       for (int k = 0; k < sps::TK_N; k++)
         for (size_t q = 0; q < kn.size(); q++)
-          if (kn[q] == sps::kTunedNames[k] && kms[q] < best_ms[k]) {
+          // the FP32 form's direct list gather takes the pair search's block size
+          if ((kn[q] == sps::kTunedNames[k] || (k == sps::TK_HALF && kn[q] == "gather")) &&
+              kms[q] < best_ms[k]) {
             best_ms[k] = kms[q];
             best[k] = c.blk[k];
           }

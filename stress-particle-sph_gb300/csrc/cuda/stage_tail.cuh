@@ -129,7 +129,8 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
           f = dp[8];
         } else {
           f = D.fdp[t];
-          drucker_prager<FAST>(M, sc.time_sph, s2v, g, &f, G2, vivel);
+          if (FAST) drucker_prager_f32(M, sc.time_sph, s2v, g, &f, G2, vivel);
+          else drucker_prager(M, sc.time_sph, s2v, g, &f, G2, vivel);
         }
         D.fdp[t] = f;
         for (int k = 0; k < 4; k++) Gs[k] = -G2[k];

@@ -311,30 +311,49 @@ __global__ void k_fs_normal_f32(Dev D) {
   const bool t_sp = is_sp(D.itype[t]);
   const float ft = D.fint[t];
   const double xt = D.px[t], yt = D.py[t];
-  float nx = 0.0f, ny = 0.0f, nb = 0.0f, g0 = 0.0f, g1 = 0.0f;
+  // compensated sums (Kahan, with the exact FMA residual of each product): the normal's
+  // direction and its orientation test p below are sums that can nearly cancel, and their
+  // result must not depend on the order in which a list holds its neighbours
+  struct Sum {
+    float s = 0.0f, c = 0.0f, e = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+      const float y = x - c;
+      const float t = s + y;
+      c = (t - s) - y;
+      s = t;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+      const float p = __fmul_rn(a, b);
+      e += fmaf(a, b, -p);
+      add(p);
+    }
+    __device__ __forceinline__ double val() const { return ((double)s - (double)c) + (double)e; }
+  };
+  Sum nx, ny, g0, g1;
+  float nb = 0.0f;
   walk_123_f32(D, D.lcol[s], [&](int u, float gx, float gy, bool same) {
     if (surf && D.subset[u] == 1) {
       // the reference adds the same vector x_j - x_i to both particles of the pair
       const bool pair_i = same ? s < D.spos[u] : t_sp;
       const float xv = f32_rn(pair_i ? D.px[u] - xt : xt - D.px[u]);
       const float yv = f32_rn(pair_i ? D.py[u] - yt : yt - D.py[u]);
-      nx -= yv;
-      ny += xv;
+      nx.add(-yv);
+      ny.add(xv);
       nb += 1.0f;
     }
     const float v = D.vol32[u];
     const float df = D.fint[u] - ft;
-    g0 = fmaf(df, v * gx, g0);
-    g1 = fmaf(df, v * gy, g1);
+    g0.add_prod(df, v * gx);
+    g1.add_prod(df, v * gy);
   });
   double dnx = 0.0, dny = 0.0;
   if (surf) {
-    dnx = (double)nx / (double)nb;
-    dny = (double)ny / (double)nb;
+    dnx = nx.val() / (double)nb;
+    dny = ny.val() / (double)nb;
     const float nv = (float)sqrt(dnx * dnx + dny * dny);
     dnx = dnx / (double)nv;
     dny = dny / (double)nv;
-    const float p = (float)((double)g0 * dnx + (double)g1 * dny);
+    const float p = (float)(g0.val() * dnx + g1.val() * dny);
     if (p < 0) {
       dnx = -dnx;
       dny = -dny;

@@ -150,3 +150,26 @@ def test_fast_surface_detection_fp32(built_gpu, make, nsteps):
     ne2, nf2 = ne.reshape(-1, 2)[both], nf.reshape(-1, 2)[both]
     cosang = (ne2 * nf2).sum(axis=1)
     assert np.all(cosang > 1.0 - 1e-6), cosang.min()
+
+
+def test_fast_pair_dump_after_replayed_steps(built_gpu):
+    # the FP32 form gathers its lists straight from the cell stencil and builds the half
+    # lists only when they are asked for (sps_dump_pairs, the exact detection's keyed
+    # lists): after steps replayed from a graph, with or without a detection after each,
+    # the dump is the last step's pair list, the same as a context that never downloaded
+    p = cases.column(dx=0.004)
+    dumps = []
+    for every_step in (True, False):
+        ctx = sps_gb300.StepContext(sps_gb300.gpu_lib(), "sps",
+                                    p.params_copy(precision=_abi.SPS_PREC_FP32_FAST))
+        sps_gb300.set_surface_detection(ctx, True)
+        ctx.upload_problem(p)
+        t = 0.0
+        for _ in range(12):
+            t = ctx.step(1, t)
+            if every_step:
+                ctx.download()
+        dumps.append(ctx.dump_pairs())
+        ctx.close()
+    for k in ("pair_i", "pair_j", "pint_type", "w", "dwdx", "dwdy"):
+        np.testing.assert_array_equal(dumps[0][k], dumps[1][k], err_msg=k)
