@@ -95,6 +95,48 @@ __device__ __forceinline__ void tail_node_f32(const Dev& D, const StepScalars& s
   D.RKv[1][t] = fma(f2, ry, D.RKv[1][t]);
 }
 
+// Walks entries 0 .. deg of list column col, KP entries a pass, software-pipelined: the
+// next pass's entries are loaded while the current pass's records are gathered and summed,
+// so that the entry loads (streamed from DRAM) overlap the record gathers (mostly L2 hits)
+// instead of adding their latency to them.  load(e) returns the records of entry e (called
+// only for entries below deg), sum(e, rec) adds one term; terms are added in list order,
+// so the result does not depend on KP.
+template <int KP, typename Rec, typename Load, typename Sum>
+__device__ __forceinline__ void walk_list(const int4* __restrict__ list, int col, int N2,
+                                          int deg, Load&& load, Sum&& sum) {
+  int4 nxt[KP];
+#pragma unroll
+  for (int q = 0; q < KP; q++)
+    nxt[q] = q < deg ? list[ell(q, col, N2)] : make_int4(0, 0, 0, 0);
+  for (int k = 0; k < deg; k += KP) {
+    int4 cur[KP];
+    Rec rec[KP] = {};
+#pragma unroll
+    for (int q = 0; q < KP; q++) {
+      cur[q] = nxt[q];
+      if (k + q < deg) rec[q] = load(cur[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < KP; q++)
+      nxt[q] = k + KP + q < deg ? list[ell(k + KP + q, col, N2)] : make_int4(0, 0, 0, 0);
+#pragma unroll
+    for (int q = 0; q < KP; q++)
+      if (k + q < deg) sum(cur[q], rec[q]);
+  }
+}
+
+// records of one neighbour, as the four sums read them
+struct RecVI {  // velocity (hi, lo) and m / rho
+  float4 v;
+  float vol;
+};
+struct RecSI {  // stress and {intvar1, m / rho, rho, m}
+  float4 s, i;
+};
+struct RecA {  // sigma / rho^2 (hi with m, lo)
+  float4 a, l;
+};
+
 // stress_point_update (2_SPH_main_2018.f90:403-482), FP32 sums.  A stress-point's velocity
 // is the weighted mean of its nodes' velocities; it is formed as the first node's velocity
 // plus the weighted mean of the deviations, which are small and exact in double-float.
@@ -149,33 +191,19 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
       nm.add(h2);
     };
-    // kP neighbours a pass: their entries and records are loaded before any is summed, so
-    // that the loads overlap (the sum order is unchanged)
-    constexpr int kP = KP;
-    int k = 0;
-    for (; k + kP - 1 < deg; k += kP) {
-      int4 e[kP];
-      float4 r[kP];
-      float vol[kP];
-#pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
-#pragma unroll
-      for (int q = 0; q < kP; q++) {
-        r[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        vol[q] = 0.f;
-        if (e[q].y >= 0) {  // not a dummy partner
-          r[q] = D.recV[e[q].x];
-          vol[q] = D.recI[e[q].x].y;
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < kP; q++)
-        if (e[q].y >= 0) term(__int_as_float(e[q].y), r[q], vol[q]);
-    }
-    for (; k < deg; k++) {
-      const int4 e = D.cross[ell(k, col, D.N2)];
-      if (e.y >= 0) term(__int_as_float(e.y), D.recV[e.x], D.recI[e.x].y);
-    }
+    walk_list<KP, RecVI>(
+        D.cross, col, D.N2, deg,
+        [&](const int4& e) {
+          RecVI r = {make_float4(0.f, 0.f, 0.f, 0.f), 0.f};
+          if (e.y >= 0) {  // not a dummy partner
+            r.v = D.recV[e.x];
+            r.vol = D.recI[e.x].y;
+          }
+          return r;
+        },
+        [&](const int4& e, const RecVI& r) {
+          if (e.y >= 0) term(__int_as_float(e.y), r.v, r.vol);
+        });
     // the mean deviation in FP32 (its sums carry FP32 accuracy), added to the first
     // node's velocity (hi + lo, exact in FP64): two FP64 additions per target
     const float norm = nm.fval();
@@ -196,29 +224,19 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
     };
-    constexpr int kP = KP;  // neighbours a pass, as above
-    int k = 0;
-    for (; k + kP - 1 < deg; k += kP) {
-      int4 e[kP];
-      float4 rs[kP], ri[kP];
-#pragma unroll
-      for (int q = 0; q < kP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
-#pragma unroll
-      for (int q = 0; q < kP; q++) {
-        rs[q] = ri[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (e[q].y >= 0) {
-          rs[q] = D.recS[e[q].x];
-          ri[q] = D.recI[e[q].x];
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < kP; q++)
-        if (e[q].y >= 0) term(__int_as_float(e[q].y), rs[q], ri[q]);
-    }
-    for (; k < deg; k++) {
-      const int4 e = D.cross[ell(k, col, D.N2)];
-      if (e.y >= 0) term(__int_as_float(e.y), D.recS[e.x], D.recI[e.x]);
-    }
+    walk_list<KP, RecSI>(
+        D.cross, col, D.N2, deg,
+        [&](const int4& e) {
+          RecSI r = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+          if (e.y >= 0) {
+            r.s = D.recS[e.x];
+            r.i = D.recI[e.x];
+          }
+          return r;
+        },
+        [&](const int4& e, const RecSI& r) {
+          if (e.y >= 0) term(__int_as_float(e.y), r.s, r.i);
+        });
     // the weighted means in FP32 (no FP64 arithmetic): the sums carry FP32 accuracy
     const float norm = nm.fval();
     if (norm != 0.0f) {
@@ -243,7 +261,9 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
 // is a sum of exact products.  This keeps the near-cancelling stress divergence accurate.
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets
 // KP: neighbours a pass, loaded before any is summed (as in k_finterp)
-template <int KIND, int KP>
+// CSPM: the CSPM correction's moments (D.cspm), a template parameter so that the
+// accumulators of the moments take no registers when it is off
+template <int KIND, int KP, bool CSPM>
 __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int stage,
                                                     const int32_t* __restrict__ tgt, int ntgt) {
   const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -274,7 +294,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         g2.add(du0 * h2);
         g1.add(du1 * h1);
         g3.add(du1 * h2);
-        if (D.cspm) {
+        if (CSPM) {
           float xu = (float)(D.px[u] - xt), yu = (float)(D.py[u] - yt);
           e0.add(xu * h1);
           e1.add(yu * h1);
@@ -302,27 +322,17 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       }
     };
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    int k = 0;
-    for (; k + KP - 1 < deg; k += KP) {
-      int4 e[KP];
-      float vol[KP];
-      float4 r[KP];
-#pragma unroll
-      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
-#pragma unroll
-      for (int q = 0; q < KP; q++) {
-        vol[q] = D.recI[e[q].x].y;
-        r[q] = e[q].y >= 0 ? D.recV[e[q].x] : z;
-      }
-#pragma unroll
-      for (int q = 0; q < KP; q++) term(e[q], vol[q], r[q]);
-    }
-    for (; k < deg; k++) {
-      const int4 e = D.cross[ell(k, col, D.N2)];
-      term(e, D.recI[e.x].y, e.y >= 0 ? D.recV[e.x] : z);
-    }
+    walk_list<KP, RecVI>(
+        D.cross, col, D.N2, deg,
+        [&](const int4& e) {
+          RecVI r;
+          r.vol = D.recI[e.x].y;
+          r.v = e.y >= 0 ? D.recV[e.x] : z;
+          return r;
+        },
+        [&](const int4& e, const RecVI& r) { term(e, r.vol, r.v); });
     // the rates follow in k_fsp_tail
-    if (D.cspm) {
+    if (CSPM) {
       double g[4] = {g0.val(), g1.val(), g2.val(), g3.val()};
       double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
       tail_sp_grad(D, t, g, AE);
@@ -348,7 +358,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         d0 = dfdiff(ra.x, rl.x, ah.x, al.x);
         d1 = dfdiff(ra.y, rl.y, ah.y, al.y);
         d2 = dfdiff(ra.z, rl.z, ah.z, al.z);
-        if (D.cspm) {
+        if (CSPM) {
           float vol = D.recI[u].y;
           float h1b = -(dwx * vol), h2b = -(dwy * vol);
           float xu = (float)(D.px[u] - xt), yu = (float)(D.py[u] - yt);
@@ -380,30 +390,18 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
       sx.add(m, dwx);
       sy.add(m, dwy);
     };
-    // KP neighbours a pass: entries and records loaded before any is summed
-    int k = 0;
-    for (; k + KP - 1 < deg; k += KP) {
-      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      int4 e[KP];
-      float4 a[KP], l[KP];
-#pragma unroll
-      for (int q = 0; q < KP; q++) e[q] = D.cross[ell(k + q, col, D.N2)];
-#pragma unroll
-      for (int q = 0; q < KP; q++) {
-        a[q] = l[q] = z;
-        if (e[q].y >= 0) {
-          a[q] = D.recA[e[q].x];
-          l[q] = D.recAl[e[q].x];
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < KP; q++) term(e[q], a[q], l[q]);
-    }
-    for (; k < deg; k++) {
-      const int4 e = D.cross[ell(k, col, D.N2)];
-      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      term(e, e.y >= 0 ? D.recA[e.x] : z, e.y >= 0 ? D.recAl[e.x] : z);
-    }
+    // KP neighbours a pass, pipelined (walk_list)
+    walk_list<KP, RecA>(
+        D.cross, col, D.N2, deg,
+        [&](const int4& e) {
+          RecA r = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+          if (e.y >= 0) {
+            r.a = D.recA[e.x];
+            r.l = D.recAl[e.x];
+          }
+          return r;
+        },
+        [&](const int4& e, const RecA& r) { term(e, r.a, r.l); });
     float avx = 0.0f, avy = 0.0f;
     if (Mt.alpha > 0 || Mt.beta > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904) in FP32
@@ -452,7 +450,7 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
     g2v[5] = g2of(q5.fval(), ah.z, al.z, syh, syl);
     double afx = 0.0, afy = 0.0;
     if (D.art_stress) art_force_node(D, col, t, &afx, &afy);
-    if (D.cspm) {  // the CSPM correction in FP64 (the reference's form)
+    if (CSPM) {  // the CSPM correction in FP64 (the reference's form)
       double g2d[6];
       for (int q = 0; q < 6; q++) g2d[q] = f64_of(g2v[q]);
       double AE[4] = {e0.val(), e1.val(), e2.val(), e3.val()};
@@ -578,10 +576,11 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
   }
 }
 
-// The stress-point tail over a grid of at most kTailBlocks blocks, each striding over
-// block-sized chunks of the stress-points.  With the surrogate installed both variants are
-// launched: the one the gate selects for this step runs, the other's blocks return at once
-// (a grid of a few SM-fulls, so that the launch that does nothing costs little).
+// The stress-point tail, each block striding over block-sized chunks of the stress-points.
+// With the surrogate installed both variants are launched: the one the gate selects for
+// this step runs, the other's blocks return at once.  The variant with the network runs
+// over at most kTailBlocks blocks (a few SM-fulls, so that the launch costs little when the
+// gate skips it); the one without over a block per 128 stress-points.
 constexpr int kTailBlocks = 152 * 8;
 template <bool SURR>
 __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
@@ -678,14 +677,19 @@ void launch_finterp(Ctx& c) {
     default: launch_finterp_kp<4>(c);
   }
 }
-template <int KP>
+template <int KP, bool CSPM>
 void launch_fderivs_kp(Ctx& c, int stage) {
   const Dev& D = c.d;
   const int ns = D.NT - D.NN, b = c.blk[TK_DERIVS];
   c.kernels_launched += 1;
   // the stress-point sums (64 registers) load one neighbour ahead; more spill
-  if (ns > 0) k_fderivs<1, 1><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
-  k_fderivs<2, KP><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
+  if (ns > 0) k_fderivs<1, 1, CSPM><<<(ns + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtS, ns);
+  k_fderivs<2, KP, CSPM><<<(D.NN + b - 1) / b, b, 0, c.stream>>>(D, stage, D.tgtN, D.NN);
+}
+template <int KP>
+void launch_fderivs_kp(Ctx& c, int stage) {
+  if (c.d.cspm) launch_fderivs_kp<KP, true>(c, stage);
+  else launch_fderivs_kp<KP, false>(c, stage);
 }
 void launch_fderivs(Ctx& c, int stage) {
   switch (c.ahead[1]) {
@@ -700,7 +704,7 @@ void launch_fsp_tail(Ctx& c, int stage) {
   const int nb = std::min((ns + 127) / 128, kTailBlocks);
   if (c.d.surr) {
     // the network's rows of this stage: candidates, then the tensor-core forward pass over
-    // as many 128-row tiles as there are candidates (a grid of at most one CTA per SM)
+    // as many 128-row tiles as there are candidates (a grid of at most two CTAs per SM)
     c.kernels_launched += 3;
     k_fsp_cand<<<nb, 128, 0, c.stream>>>(c.d, stage);
     SPS_CUDA_CHECK(mlp_tc_forward(c.d.tc_img, c.d.tc_bias, c.d.xcand, 16, MLP_NIN,
@@ -708,7 +712,9 @@ void launch_fsp_tail(Ctx& c, int stage) {
                                   kErrTensorCore, c.tc_grid, c.stream));
     k_fsp_tail<true><<<nb, 128, 0, c.stream>>>(c.d, stage);
   }
-  k_fsp_tail<false><<<nb, 128, 0, c.stream>>>(c.d, stage);
+  // the variant without the network over one block per 128 stress-points: when it runs
+  // it does the work, and the scheduler refills SMs with fresh blocks as others wait
+  k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
   k_fxsph<<<c.grid_of(TK_XSPH, c.d.N2), c.blk[TK_XSPH], 0, c.stream>>>(c.d);

@@ -14,6 +14,7 @@
 // expression, so the pair set equals the reference's.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <stdexcept>
 
 #include "ctx.cuh"
@@ -274,14 +275,18 @@ __global__ void k_cell_count(Dev D) {
     int ix = cl % g.ndiv[0], iy = cl / g.ndiv[0];
     double ox = x - (g.xmin[0] + (double)ix * g.deltx[0]);
     double oy = y - (g.xmin[1] + (double)iy * g.deltx[1]);
-    float oxh = (float)ox, oyh = (float)oy;
+    // the conversions on the integer pipe (f32_split: hi = (float)ox and lo = (float)(ox -
+    // hi), the same bits as the hardware conversions, which GB300 issues at its FP64 rate)
+    float oxh, oxl, oyh, oyl;
+    f32_split(ox, oxh, oxl);
+    f32_split(oy, oyh, oyl);
     D.xr[i] = oxh;
     D.yr[i] = oyh;
     if (D.fast) {
-      D.xrl[i] = (float)(ox - (double)oxh);
-      D.yrl[i] = (float)(oy - (double)oyh);
+      D.xrl[i] = oxl;
+      D.yrl[i] = oyl;
     }
-    D.hr[i] = (float)D.hsml[i];
+    D.hr[i] = f32_rn(D.hsml[i]);
     c = g.cell0 + cl;
   }
   D.cell_of[i] = c;
@@ -684,12 +689,14 @@ __device__ __forceinline__ bool gather_accept(const Dev& D, int a, float xa, flo
 
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets.  SAME: the same-kind
 // entries are written too (the steps that read them: XSPH, artificial viscosity or stress,
-// the FP32 free-surface detection).  Phase 1 tests the stencil's candidates and keeps the
+// the FP32 free-surface detection); without them degS holds 0 unless the outside approach
+// reads the counts.  Phase 1 tests the stencil's candidates and keeps the
 // accepted ones (sorted position and cell offset) in shared memory; phase 2 evaluates the
 // kernel values, so that a warp's lanes evaluate together.  Dynamic shared memory:
 // (capC + SAME capS) ints per thread, entry k of thread j at k * blockDim + j.
 template <int KIND, bool SAME>
-__global__ void k_fgather(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
+__global__ void __launch_bounds__(512, 2) k_fgather(Dev D, const int32_t* __restrict__ tgt,
+                                                    int ntgt) {
   extern __shared__ int gbuf[];
   const int k0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (k0 >= ntgt) return;
@@ -709,31 +716,64 @@ __global__ void k_fgather(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
     const int ix = c % nx, iy = c / nx;
     const float xa = D.xr[a], ya = D.yr[a], ha = D.hr[a];
     const float cw = (float)g.deltx[0], ch = (float)g.deltx[1];
+    // same-kind partners before the target matter only for the full same-kind count
+    // (the same lists, or the outside approach's isolated-node test); otherwise only the
+    // ones after it are tested, for the half-list count
+    const bool all_same = SAME || D.outside;
+    // a uniform smoothing length makes the prefilter's bounds constant (the same FP32
+    // expressions as prefilter(), so the same decisions)
+    float s2lo = 0.0f, s2hi = 0.0f;
+    if (g.uniform_h) {
+      const float sv = (float)D.scale_k * ((ha + ha) * 0.5f);
+      const float s2 = sv * sv;
+      s2lo = s2 * (1.0f - tau);
+      s2hi = s2 * (1.0f + tau);
+    }
+    // the stencil row by row: a row's three cells are one contiguous run of sorted
+    // positions; a candidate's cell follows from the run's cell boundaries
     for (int qy = -1; qy <= 1; qy++) {
       const int jy = iy + qy;
       if (jy < 0 || jy >= ny) continue;
-      for (int qx = -1; qx <= 1; qx++) {
-        const int jx = ix + qx;
-        if (jx < 0 || jx >= nx) continue;
-        const int cc = g.cell0 + jy * nx + jx;
-        const int lo = D.cell_start[cc], hi = lo + D.cell_cnt[cc];
-        const float cx = (float)qx * cw, cy = (float)qy * ch;
-        const int code = (qy + 1) * 3 + (qx + 1);  // cell offset, kept in the top 4 bits
-        for (int bs = lo; bs < hi; bs++) {
-          if (bs == s) continue;
-          const float4 rb = D.srec[bs];
-          if (!gather_accept(D, a, xa, ya, ha, rb, bs, cx, cy, tau)) continue;
-          nHalf += bs > s;
-          if (__float_as_int(rb.w) == ta) {
-            if (SAME && nS < D.capS) bufS[(size_t)nS * bd + tid] = bs | (code << kHalfTypeShift);
-            nS++;
-          } else {
-            if (nC < D.capC) bufC[(size_t)nC * bd + tid] = bs | (code << kHalfTypeShift);
-            nC++;
+      const int row0 = g.cell0 + jy * nx;
+      const int cr = row0 + (ix + 1 < nx ? ix + 1 : ix);
+      const int lo = D.cell_start[row0 + (ix > 0 ? ix - 1 : 0)];
+      const int hi = D.cell_start[cr] + D.cell_cnt[cr];
+      const int b0 = D.cell_start[row0 + ix];                         // the centre cell
+      const int b1 = ix + 1 < nx ? D.cell_start[row0 + ix + 1] : hi;  // the right cell
+      const float cy = (float)qy * ch;
+      for (int bs = lo; bs < hi; bs++) {
+        if (bs == s) continue;
+        const float4 rb = D.srec[bs];
+        const bool same = __float_as_int(rb.w) == ta;
+        if (same && !all_same && bs < s) continue;
+        const int qx = bs < b0 ? -1 : (bs < b1 ? 0 : 1);
+        const float cx = qx < 0 ? -cw : (qx > 0 ? cw : 0.0f);  // (float)qx * cw
+        bool acc;
+        if (g.uniform_h) {
+          const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
+          const float d2 = fx * fx + fy * fy;
+          if (d2 > s2hi) continue;
+          acc = d2 < s2lo;
+          if (!acc) {
+            double r, dx, dy, mh;
+            acc = exact_test(D, a, D.sorted[bs], r, dx, dy, mh);
           }
+        } else {
+          acc = gather_accept(D, a, xa, ya, ha, rb, bs, cx, cy, tau);
+        }
+        if (!acc) continue;
+        nHalf += bs > s;
+        const int code = (qy + 1) * 3 + (qx + 1);  // cell offset, kept in the top 4 bits
+        if (same) {
+          if (SAME && nS < D.capS) bufS[(size_t)nS * bd + tid] = bs | (code << kHalfTypeShift);
+          nS++;
+        } else {
+          if (nC < D.capC) bufC[(size_t)nC * bd + tid] = bs | (code << kHalfTypeShift);
+          nC++;
         }
       }
     }
+    if (!all_same) nS = 0;  // not counted: no step kernel reads the same-kind lists or counts
     if (nHalf > D.capH) {
       atomicOr(D.err, ERR_HALF_CAP);
       nHalf = D.capH;
@@ -1155,7 +1195,7 @@ void split_targets(Ctx& c) {
 // lowered until each thread's candidate lists fit 48 KB of shared memory
 void launch_gather(Ctx& c, bool same, const Dev& D) {
   const size_t per_thread = sizeof(int) * (size_t)(D.capC + (same ? D.capS : 0));
-  int b = c.blk[TK_HALF];
+  int b = std::min(c.blk[TK_HALF], 512);  // k_fgather's launch bounds
   while (b > 32 && per_thread * (size_t)b > 49152) b >>= 1;
   const size_t sm = per_thread * (size_t)b;
   const int ns = D.NT - D.NN;

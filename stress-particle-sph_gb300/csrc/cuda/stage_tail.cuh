@@ -133,9 +133,20 @@ __device__ __forceinline__ void tail_sp_rates(const Dev& D, const StepScalars& s
           else drucker_prager(M, sc.time_sph, s2v, g, &f, G2, vivel);
         }
         D.fdp[t] = f;
-        for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
-        if (D.cap_buf && (G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0))
-          capture_tuple(D, t, s2v, g, Gs);
+        if (FAST) {
+          // negation and the non-zero test on the integer pipe (sign bit; magnitude bits)
+          bool nz = false;
+          for (int k = 0; k < 4; k++) {
+            const long long b = __double_as_longlong(G2[k]);
+            Gs[k] = __longlong_as_double(b ^ (long long)0x8000000000000000ull);
+            nz = nz || (b << 1) != 0;
+          }
+          if (D.cap_buf && nz) capture_tuple(D, t, s2v, g, Gs);
+        } else {
+          for (int k = 0; k < 4; k++) Gs[k] = -G2[k];
+          if (D.cap_buf && (G2[0] != 0.0 || G2[1] != 0.0 || G2[2] != 0.0 || G2[3] != 0.0))
+            capture_tuple(D, t, s2v, g, Gs);
+        }
       }
       if (FAST) {
         float v0 = f32_rn(vivel[0]), v1 = f32_rn(vivel[1]), v2 = f32_rn(vivel[2]),
