@@ -544,7 +544,8 @@ def kernel_bytes(name, prob, deg, fast=False):
         return ent * deg["cross"] + (ent * deg["same_nodes"] if visc else 0) + \
             16 * (nn + ns) + ns * (16 + 32 + 32 + 32 + 64 + 16 + 16) + nn * (16 + 16 + 32 + 16)
     if fast and name == "interp":
-        return ent * deg["cross"] + 16 * nn + 32 * ns + ns * 16 + nn * 40
+        # the compact {id, W} entries (8 B) of the gathered lists
+        return 8.0 * deg["cross"] + 16 * nn + 32 * ns + ns * 16 + nn * 40
     if name == "derivs":
         # entries + SP (v,s,m,rho,grad_u w, RHS1 w, RKs rw, fdp rw, RKd rw) + node terms
         return ent * deg["cross"] + ns * (16 + 32 + 16 + 32 + 32 + 64 + 16 + 16) + \
@@ -555,11 +556,13 @@ def kernel_bytes(name, prob, deg, fast=False):
         return n2 * (4 * 8 + 8) + ent * deg["pairs"]
     if fast and name == "gather":
         # the FP32 form's direct lists: entries written (the same-kind lists' only when a
-        # step kernel reads them), and per particle its sorted record (16 + 8 B), its own
-        # offsets (20 B), ids, type, realisation and cell (16 B), counts (12 B), target (4 B)
+        # step kernel reads them) and the compact {id, W} copy of the cross entries (8 B),
+        # and per particle its sorted record (16 + 8 B), its own offsets (20 B), ids, type,
+        # realisation and cell (16 B), counts (12 B), target (4 B)
         p = prob.params
         same_written = p.xsph or p.art_stress or p.alpha > 0 or p.beta > 0
-        return ent * (deg["cross"] + (deg["same"] if same_written else 0)) + n2 * 76
+        return ent * (deg["cross"] + (deg["same"] if same_written else 0)) + \
+            8.0 * deg["cross"] + n2 * 76
     if name == "lists":
         # entries written (the same-kind lists' only when a step kernel reads them: XSPH,
         # artificial viscosity or stress), and the creators' half-list entries read,

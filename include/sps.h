@@ -197,7 +197,8 @@ int sps_selftest_division(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* misma
 
 /* Self-test (no reference counterpart): compare, on the device, the FP64 <-> FP32
    conversions the FP32 form does on the integer pipe (round-to-nearest double -> float,
-   the hi/lo split of a double into two floats, float -> double) with the hardware
+   the hi/lo split of a double into two floats, float -> double, and int -> float for
+   the remainders below 2^29 that the split converts) with the hardware
    conversions, on n pseudo-random values; *mismatches counts results that differ in any
    bit. */
 int sps_selftest_convert(sps_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);

@@ -90,6 +90,7 @@ struct Real {
   // drucker_prager's FP32 material constants (tan phi, alpha, k_c, G, K), evaluated once on
   // the host in IEEE FP32 with the routine's expressions (the FP32 form's body reads them)
   float dpf_alpha2, dpf_kc, dpf_G, dpf_K;
+  double dt6;  // dt / 6 (RK4's final weight), formed on the host
   double kc_shift;    // kc / (3 alpha2): the apex mean stress of the tension cut
   double xmin_dom[2], xmax_dom[2];
   double cgrav[2];
@@ -216,6 +217,11 @@ struct Dev {
                       // pair count, id
   int64_t* half_off;  // exclusive scan of half_cnt over sorted positions (size N2+1)
   int4 *cross, *same;
+  // FP32 form with gathered lists: the cross lists' {neighbour id, W} again, 8 bytes an
+  // entry at k * N2 + col (a warp reads entry k of its columns as one contiguous run): the
+  // interpolation reads only these, half the bytes of the full entries
+  int2* crossW;
+  int use_crossW;
   // per-target lists, entries in pairs: entries 2j and 2j+1 of list column c side by side
   // at (j * N2 + c) * 2 (ell()), one 32-byte sector; keys flat at k * N2 + c
   int32_t *keyC, *keyS;  // per entry: 2 x (position in the reference's walk order) + (target is pair_i)
@@ -321,6 +327,27 @@ __device__ __forceinline__ float f32_rn(double x) {
   return __uint_as_float(((h32 & 0x80000000u) | ((unsigned)(E - 896) << 23) | f23) + up);
 }
 
+// (float)r for |r| < 2^30, round to nearest even, on the integer pipe (GB300 issues the
+// hardware int -> float conversion on its FP64 pipe): the leading bit found with clz, the
+// bits below the 24 kept rounded by their remainder
+__device__ __forceinline__ float i2f_rn(int r) {
+  if (r == 0) return 0.0f;
+  const unsigned sgn = r < 0 ? 0x80000000u : 0u;
+  const unsigned a = r < 0 ? 0u - (unsigned)r : (unsigned)r;
+  const int e = 31 - __clz((int)a);  // the leading bit, 0 .. 29
+  unsigned m;
+  if (e <= 23) {
+    m = a << (23 - e);
+  } else {
+    const int sh = e - 23;
+    m = a >> sh;
+    const unsigned rem = a & ((1u << sh) - 1u), half = 1u << (sh - 1);
+    m += (rem > half || (rem == half && (m & 1u))) ? 1u : 0u;  // may carry into bit 24
+  }
+  // a carry to 2^24 moves into the exponent field by the addition
+  return __uint_as_float(sgn | ((unsigned)(e + 127) << 23) + (m - 0x800000u));
+}
+
 // hi = (float)x, lo = (float)(x - (double)hi): the exact remainder x - hi is the dropped
 // significand bits (minus one float ulp when hi was rounded up), scaled by 2^(E-1075)
 __device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
@@ -344,7 +371,7 @@ __device__ __forceinline__ void f32_split(double x, float& hi, float& lo) {
   hi = __uint_as_float(((h32 & 0x80000000u) | ((unsigned)(E - 896) << 23) | f23) + up);
   int r = (int)rem - (up ? 0x20000000 : 0);
   if (h32 & 0x80000000u) r = -r;
-  lo = __int2float_rn(r) * __uint_as_float((unsigned)(E - 948) << 23);
+  lo = i2f_rn(r) * __uint_as_float((unsigned)(E - 948) << 23);
 }
 
 // exact float -> double, identical to (double)f
@@ -758,16 +785,19 @@ __device__ __forceinline__ float two_sum_f(float a, float b, float& e) {
   return s;
 }
 
-// a >= b for non-NaN doubles on the integer pipe: the bit patterns as ordered keys (the
-// magnitude bits of a negative value flipped, -0 taken as +0)
-__device__ __forceinline__ bool f64_ge(double a, double b) {
-  long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+// an ordered key of a non-NaN double on the integer pipe: the bit pattern with the
+// magnitude bits of a negative value flipped, -0 taken as +0 (a < b exactly when
+// f64_key(a) < f64_key(b))
+__device__ __forceinline__ long long f64_key(double a) {
+  long long ia = __double_as_longlong(a);
   if ((ia << 1) == 0) ia = 0;
-  if ((ib << 1) == 0) ib = 0;
-  ia ^= (ia >> 63) & 0x7FFFFFFFFFFFFFFFll;
-  ib ^= (ib >> 63) & 0x7FFFFFFFFFFFFFFFll;
-  return ia >= ib;
+  return ia ^ ((ia >> 63) & 0x7FFFFFFFFFFFFFFFll);
 }
+__device__ __forceinline__ bool f64_isnan(double a) {
+  return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll;
+}
+// a >= b for non-NaN doubles, on the integer pipe
+__device__ __forceinline__ bool f64_ge(double a, double b) { return f64_key(a) >= f64_key(b); }
 
 // drucker_prager for the FP32 form, without FP64 arithmetic (GB300 issues FP64 at 1/64 of
 // its FP32 rate): the stresses enter as hi + lo splits, the mean is formed in double-float

@@ -77,14 +77,14 @@ __device__ __forceinline__ void tail_node_f32(const Dev& D, const StepScalars& s
     gx = fg * f32_rn(M.cgrav[0]);
     gy = fg * f32_rn(M.cgrav[1]);
   }
-  if (M.damping != 0.0) {
+  if ((__double_as_longlong(M.damping) << 1) != 0) {  // non-zero, on the integer pipe
     const float dmp = f32_rn(M.damping);
     gx = fmaf(-dmp, f32_rn(D.vx[t]), gx);
     gy = fmaf(-dmp, f32_rn(D.vy[t]), gy);
   }
   float rhsx = ((-div2x + gx) + avx) + f32_rn(D.fbx[t]);
   float rhsy = ((-div2y + gy) + avy) + f32_rn(D.fby[t]);
-  if (afx != 0.0 || afy != 0.0) {
+  if (D.art_stress) {
     rhsx += f32_rn(afx);
     rhsy += f32_rn(afy);
   }
@@ -119,6 +119,31 @@ __device__ __forceinline__ void walk_list(const int4* __restrict__ list, int col
 #pragma unroll
     for (int q = 0; q < KP; q++)
       nxt[q] = k + KP + q < deg ? list[ell(k + KP + q, col, N2)] : make_int4(0, 0, 0, 0);
+#pragma unroll
+    for (int q = 0; q < KP; q++)
+      if (k + q < deg) sum(cur[q], rec[q]);
+  }
+}
+
+// the same walk over the compact {id, W} entries (crossW: entry k of column col at
+// k * N2 + col)
+template <int KP, typename Rec, typename Load, typename Sum>
+__device__ __forceinline__ void walk_compact(const int2* __restrict__ list, int col, int N2,
+                                             int deg, Load&& load, Sum&& sum) {
+  int2 nxt[KP];
+#pragma unroll
+  for (int q = 0; q < KP; q++) nxt[q] = q < deg ? list[(size_t)q * N2 + col] : make_int2(0, 0);
+  for (int k = 0; k < deg; k += KP) {
+    int2 cur[KP];
+    Rec rec[KP] = {};
+#pragma unroll
+    for (int q = 0; q < KP; q++) {
+      cur[q] = nxt[q];
+      if (k + q < deg) rec[q] = load(cur[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < KP; q++)
+      nxt[q] = k + KP + q < deg ? list[(size_t)(k + KP + q) * N2 + col] : make_int2(0, 0);
 #pragma unroll
     for (int q = 0; q < KP; q++)
       if (k + q < deg) sum(cur[q], rec[q]);
@@ -191,19 +216,20 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       v1.add(dfdiff(r.y, r.w, ref.y, ref.w) * h2);
       nm.add(h2);
     };
-    walk_list<KP, RecVI>(
-        D.cross, col, D.N2, deg,
-        [&](const int4& e) {
-          RecVI r = {make_float4(0.f, 0.f, 0.f, 0.f), 0.f};
-          if (e.y >= 0) {  // not a dummy partner
-            r.v = D.recV[e.x];
-            r.vol = D.recI[e.x].y;
-          }
-          return r;
-        },
-        [&](const int4& e, const RecVI& r) {
-          if (e.y >= 0) term(__int_as_float(e.y), r.v, r.vol);
-        });
+    auto load = [&](const auto& e) {
+      RecVI r = {make_float4(0.f, 0.f, 0.f, 0.f), 0.f};
+      if (e.y >= 0) {  // not a dummy partner
+        r.v = D.recV[e.x];
+        r.vol = D.recI[e.x].y;
+      }
+      return r;
+    };
+    auto sum = [&](const auto& e, const RecVI& r) {
+      if (e.y >= 0) term(__int_as_float(e.y), r.v, r.vol);
+    };
+    // the compact {id, W} entries when the lists were gathered (half the bytes)
+    if (KIND != 0 && D.use_crossW) walk_compact<KP, RecVI>(D.crossW, col, D.N2, deg, load, sum);
+    else walk_list<KP, RecVI>(D.cross, col, D.N2, deg, load, sum);
     // the mean deviation in FP32 (its sums carry FP32 accuracy), added to the first
     // node's velocity (hi + lo, exact in FP64): two FP64 additions per target
     const float norm = nm.fval();
@@ -224,19 +250,19 @@ __global__ void k_finterp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       if (D.cont_density) rt.add(ri.z * h1);
       nm.add(h1);
     };
-    walk_list<KP, RecSI>(
-        D.cross, col, D.N2, deg,
-        [&](const int4& e) {
-          RecSI r = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
-          if (e.y >= 0) {
-            r.s = D.recS[e.x];
-            r.i = D.recI[e.x];
-          }
-          return r;
-        },
-        [&](const int4& e, const RecSI& r) {
-          if (e.y >= 0) term(__int_as_float(e.y), r.s, r.i);
-        });
+    auto load = [&](const auto& e) {
+      RecSI r = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+      if (e.y >= 0) {
+        r.s = D.recS[e.x];
+        r.i = D.recI[e.x];
+      }
+      return r;
+    };
+    auto sum = [&](const auto& e, const RecSI& r) {
+      if (e.y >= 0) term(__int_as_float(e.y), r.s, r.i);
+    };
+    if (KIND != 0 && D.use_crossW) walk_compact<KP, RecSI>(D.crossW, col, D.N2, deg, load, sum);
+    else walk_list<KP, RecSI>(D.cross, col, D.N2, deg, load, sum);
     // the weighted means in FP32 (no FP64 arithmetic): the sums carry FP32 accuracy
     const float norm = nm.fval();
     if (norm != 0.0f) {
@@ -403,7 +429,8 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
         },
         [&](const int4& e, const RecA& r) { term(e, r.a, r.l); });
     float avx = 0.0f, avy = 0.0f;
-    if (Mt.alpha > 0 || Mt.beta > 0) {
+    // alpha > 0 or beta > 0 (non-negative doubles: a positive one has a positive bit pattern)
+    if (__double_as_longlong(Mt.alpha) > 0 || __double_as_longlong(Mt.beta) > 0) {
       // artificial_viscosity (2_SPH_main_2018.f90:826-904) in FP32
       Kahan ax, ay;
       int degs = D.degS[col];

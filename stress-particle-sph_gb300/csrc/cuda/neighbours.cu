@@ -41,14 +41,6 @@ __device__ __forceinline__ dfl df_2sum(float a, float b) {
   float bb = s - a;
   return {s, (a - (s - bb)) + (b - bb)};
 }
-__device__ __forceinline__ dfl df_add(dfl x, dfl y) {
-  dfl s = df_2sum(x.hi, y.hi);
-  dfl t = df_2sum(x.lo, y.lo);
-  s.lo += t.hi;
-  s = df_fast2sum(s.hi, s.lo);
-  s.lo += t.lo;
-  return df_fast2sum(s.hi, s.lo);
-}
 __device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
   float p = x.hi * y.hi;
   float e = fmaf(x.hi, y.hi, -p);
@@ -62,6 +54,26 @@ __device__ __forceinline__ dfl df_sqrt(dfl x) {
   float e = fmaf(s, s, -p);
   float r = ((x.hi - p) - e) + x.lo;
   return df_fast2sum(s, r * (0.5f * __frcp_rn(s)));
+}
+// x^2 + y^2 of two double-float values, accurate to a few units of 2^-44: the exact
+// squares of the high parts (FMA residuals) summed exactly, the cross terms and residuals
+// added once; sign-symmetric in x and y
+__device__ __forceinline__ dfl df_sumsq(dfl x, dfl y) {
+  const float px = x.hi * x.hi, ex = fmaf(x.hi, x.hi, -px);
+  const float py = y.hi * y.hi, ey = fmaf(y.hi, y.hi, -py);
+  dfl s = df_2sum(px, py);
+  s.lo += (ex + ey) + 2.0f * fmaf(x.hi, x.lo, y.hi * y.lo);
+  return df_fast2sum(s.hi, s.lo);
+}
+// the separation (xa + xal) - (xb + xbl) - q (c.hi + c.lo), q in {-1, 0, 1}, as a
+// double-float: the two exact sums of the high parts, the low parts added once (the cell
+// shift q c.hi is exact); negating every input negates the result exactly
+__device__ __forceinline__ dfl df_sep(float xa, float xal, float xb, float xbl, int q, dfl c) {
+  const float ch = q < 0 ? -c.hi : (q > 0 ? c.hi : 0.0f);
+  const float cl = q < 0 ? -c.lo : (q > 0 ? c.lo : 0.0f);
+  const dfl a = df_2sum(xa, -xb);
+  const dfl b = df_2sum(a.hi, -ch);
+  return df_fast2sum(b.hi, ((a.lo + b.lo) + (xal - xbl)) - cl);
 }
 __device__ __forceinline__ dfl df_from(double v) {
   float h = (float)v;
@@ -93,10 +105,18 @@ __global__ void k_bbox(Dev D) {
     r = D.rid[i];
     const Real& M = D.real[r];
     double x = D.px[i], y = D.py[i];
-    double dxx = (x - M.xmin_dom[0]) * (x - M.xmax_dom[0]);
-    double dyy = (y - M.xmin_dom[1]) * (y - M.xmax_dom[1]);
+    // (x - xmin)(x - xmax) > 0 of the reference: both differences non-zero and of one sign,
+    // i.e. x outside [xmin, xmax] (the product of two such differences cannot underflow to
+    // zero for a domain of non-zero width; a NaN coordinate gives false), decided on the
+    // integer pipe with ordered keys
+    auto outside = [](double v, double lo, double hi) {
+      if (f64_isnan(v)) return false;
+      const long long kv = f64_key(v), kl = f64_key(lo), kh = f64_key(hi);
+      return kv < min(kl, kh) || kv > max(kl, kh);
+    };
     uint8_t o = D.out[i];
-    if (dxx > 0.0 || dyy > 0.0) o = 1;
+    if (outside(x, M.xmin_dom[0], M.xmax_dom[0]) || outside(y, M.xmin_dom[1], M.xmax_dom[1]))
+      o = 1;
     D.out[i] = o;
     if (!o) {
       double h = D.hsml[i];
@@ -419,7 +439,7 @@ __device__ __forceinline__ void sph_kernel_f32(int skf, float pi, float r, float
 // of the FP64 evaluation
 __device__ __forceinline__ void cubic_mixed(const Grid& g, dfl dx, dfl dy, float* w, float* dw0,
                                             float* dw1) {
-  const dfl r = df_sqrt(df_add(df_mul(dx, dx), df_mul(dy, dy)));
+  const dfl r = df_sqrt(df_sumsq(dx, dy));
   const dfl q = df_mul(r, g.df_yh);
   *w = 0.0f;
   *dw0 = 0.0f;
@@ -472,11 +492,8 @@ __device__ __forceinline__ int4 half_entry(const Dev& D, const Grid& g, int a, i
     // separation as double-float from the cell-relative hi/lo offsets
     // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float
     const float2 rl = D.srecl[bs];
-    dfl ddx = df_add(df_add({xa, xal}, {-rb.x, -rl.x}),
-                     {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
-    dfl ddy = df_add(df_add({ya, yal}, {-rb.y, -rl.y}),
-                     {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
-    cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
+    cubic_mixed(g, df_sep(xa, xal, rb.x, rl.x, qx, g.df_cell[0]),
+                df_sep(ya, yal, rb.y, rl.y, qy, g.df_cell[1]), &wf, &d0f, &d1f);
   } else {
     float hm = (ha + rb.z) * 0.5f;
     float rf = sqrtf(fx * fx + fy * fy);
@@ -656,11 +673,8 @@ __device__ __forceinline__ int4 gather_entry(const Dev& D, const Grid& g, int ta
   float wf, d0f, d1f;
   if (g.uniform_h) {
     const float2 rl = D.srecl[bs];
-    dfl ddx = df_add(df_add({xa, xal}, {-rb.x, -rl.x}),
-                     {-(float)qx * g.df_cell[0].hi, -(float)qx * g.df_cell[0].lo});
-    dfl ddy = df_add(df_add({ya, yal}, {-rb.y, -rl.y}),
-                     {-(float)qy * g.df_cell[1].hi, -(float)qy * g.df_cell[1].lo});
-    cubic_mixed(g, ddx, ddy, &wf, &d0f, &d1f);
+    cubic_mixed(g, df_sep(xa, xal, rb.x, rl.x, qx, g.df_cell[0]),
+                df_sep(ya, yal, rb.y, rl.y, qy, g.df_cell[1]), &wf, &d0f, &d1f);
   } else {
     const float cx = (float)qx * (float)g.deltx[0], cy = (float)qy * (float)g.deltx[1];
     const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
@@ -740,7 +754,7 @@ __global__ void __launch_bounds__(512, 2) k_fgather(Dev D, const int32_t* __rest
       const int hi = D.cell_start[cr] + D.cell_cnt[cr];
       const int b0 = D.cell_start[row0 + ix];                         // the centre cell
       const int b1 = ix + 1 < nx ? D.cell_start[row0 + ix + 1] : hi;  // the right cell
-      const float cy = (float)qy * ch;
+      const float cy = qy < 0 ? -ch : (qy > 0 ? ch : 0.0f);  // (float)qy * ch
       for (int bs = lo; bs < hi; bs++) {
         if (bs == s) continue;
         const float4 rb = D.srec[bs];
@@ -785,7 +799,7 @@ __global__ void __launch_bounds__(512, 2) k_fgather(Dev D, const int32_t* __rest
     }
     const float xal = D.xrl[a], yal = D.yrl[a];
     // phase 2: the entries, stored in pairs (whole 32-byte sectors)
-    auto finish = [&](const int* buf, int n, int4* list) {
+    auto finish = [&](const int* buf, int n, int4* list, int2* compact) {
       int4 pend = make_int4(0, 0, 0, 0);
       for (int k = 0; k < n; k++) {
         const unsigned v = (unsigned)buf[(size_t)k * bd + tid];
@@ -794,11 +808,13 @@ __global__ void __launch_bounds__(512, 2) k_fgather(Dev D, const int32_t* __rest
                                     code % 3 - 1, code / 3 - 1);
         if (k & 1) store_pair(list + ell(k - 1, col, D.N2), pend, e);
         else pend = e;
+        // the lanes of a warp write entry k of adjacent columns together: whole sectors
+        if (compact) compact[(size_t)k * D.N2 + col] = make_int2(e.x, e.y);
       }
       if (n & 1) list[ell(n - 1, col, D.N2)] = pend;
     };
-    finish(bufC, nC, D.cross);
-    if (SAME) finish(bufS, nS, D.same);
+    finish(bufC, nC, D.cross, D.use_crossW ? D.crossW : nullptr);
+    if (SAME) finish(bufS, nS, D.same, nullptr);
   }
   D.degC[col] = nC;
   D.degS[col] = nS;

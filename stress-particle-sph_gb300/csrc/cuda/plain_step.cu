@@ -655,7 +655,7 @@ __global__ void k_rk_final(Dev D) {
   const int r = D.R == 1 ? 0 : D.rid[i];
   const Real& M = real_of(D, i);
   const StepScalars& sc = D.cur[r];
-  const double dt6 = M.dt / 6.0;
+  const double dt6 = M.dt6;  // dt / 6, the host's IEEE quotient
   double vx = D.vx[i], vy = D.vy[i];
   double a = D.s0[i], b = D.s1[i], c = D.s2[i], d = D.s3[i];
   if (i < D.NN) {
@@ -684,7 +684,11 @@ __global__ void k_rk_final(Dev D) {
       D.rinv[i] = 1.0 / r;
       if (D.sle == 2) D.hsml[i] = D.hsml0[i] + dt6 * D.RKh[i];
     }
-    double dd = D.RKd[i] / 6.0;
+    // RKd / 6 correctly rounded: the Markstein-corrected product with RN(1/6) for normal
+    // operands (div_rcp), the IEEE division for zero and extreme exponents
+    const double rkd = D.RKd[i];
+    const int ex = (int)((__double_as_longlong(rkd) >> 52) & 0x7FF);
+    double dd = (ex > 64 && ex < 1980) ? div_rcp(rkd, 6.0, 1.0 / 6.0) : rkd / 6.0;
     D.Ddev[i] = dd;
     D.iv1[i] = D.iv1[i] + M.dt * dd;  // update_strain (3_SPH_material_2018.f90:1864)
   }
@@ -695,11 +699,12 @@ __global__ void k_trapezoid(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
   if (D.update_x) {
-    float hx = (float)(0.5 * (D.vx0[i] + D.vx[i]));
-    float hy = (float)(0.5 * (D.vy0[i] + D.vy[i]));
+    // the conversions on the integer pipe (the same bits as the hardware's)
+    float hx = f32_rn(0.5 * (D.vx0[i] + D.vx[i]));
+    float hy = f32_rn(0.5 * (D.vy0[i] + D.vy[i]));
     const double dt = real_of(D, i).dt;
-    double x = D.x0x[i] + (double)hx * dt;
-    double y = D.x0y[i] + (double)hy * dt;
+    double x = D.x0x[i] + f64_of(hx) * dt;
+    double y = D.x0y[i] + f64_of(hy) * dt;
     D.px[i] = x;
     D.py[i] = y;
   }
@@ -802,6 +807,11 @@ __global__ void k_selftest_conv(int64_t n, uint64_t seed, unsigned long long* ba
     f32_split(x, hs, ls);
     float hr = (float)x, lr = (float)(x - (double)hr);
     double b = f64_of(hr);
+    // the integer-pipe int -> float conversion over |r| < 2^29 (f32_split's remainders),
+    // ties included (low bits cleared to land on halfway cases)
+    int ri = (int)(r2 >> 34) - (1 << 29);
+    if ((r2 & 0x30000) == 0) ri &= ~0x3F;
+    if (__float_as_uint(i2f_rn(ri)) != __float_as_uint(__int2float_rn(ri))) nb++;
     if (__float_as_uint(h) != __float_as_uint(hr) || __float_as_uint(hs) != __float_as_uint(hr) ||
         __float_as_uint(ls) != __float_as_uint(lr) ||
         __double_as_longlong(b) != __double_as_longlong((double)hr))

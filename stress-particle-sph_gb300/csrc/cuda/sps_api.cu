@@ -551,6 +551,7 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
       M.ntype_solid = q.ntype_solid;
       M.ic_grav = q.ic_grav;
       M.dt = q.dt_sph;
+      M.dt6 = q.dt_sph / 6.0;
       M.dx = q.dx;
       M.alpha = q.alpha;
       M.beta = q.beta;
@@ -989,6 +990,8 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
         const size_t rows = (size_t)capn + (capn & 1);
         D.cross = dalloc<int4>(c, (size_t)D.N2 * rows);
         D.same = dalloc<int4>(c, (size_t)D.N2 * rows);
+        D.crossW = c.precision == SPS_PREC_FP32_FAST ? dalloc<int2>(c, (size_t)D.N2 * rows)
+                                                     : nullptr;
         D.keyC = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.keyS = dalloc<int32_t>(c, (size_t)D.N2 * (size_t)capn);
         D.capH = D.capC = D.capS = capn;
@@ -1002,6 +1005,11 @@ int sps_upload_real(sps_ctx* h, int32_t r, const double* x, const double* vel,
       if (q.uploaded && !((double)D.scale_k * q.hmin_nd > 0.76 * q.p.dx)) bfl = 0;
     if (bfl != D.bound_from_lists) drop_graphs(c);
     D.bound_from_lists = bfl;
+    // the FP32 form's interpolation reads the compact {id, W} entries that the gathered
+    // lists also write
+    const int uw = c.lists_direct() && D.crossW ? 1 : 0;
+    if (uw != D.use_crossW) drop_graphs(c);
+    D.use_crossW = uw;
   } catch (const std::exception& e) {
     return fail(&c, SPS_ERR_CUDA, e.what());
   }
