@@ -805,9 +805,11 @@ __device__ __forceinline__ bool f64_ge(double a, double b) { return f64_key(a) >
 // itself; the loading test df >= 0 compares the FP64 values exactly on the integer pipe; the
 // material constants are the host's FP32 evaluation (dpf_*).  Same outputs as
 // drucker_prager: the updated f, the plastic source G and vivel.
-__device__ __forceinline__ void drucker_prager_f32(const Real& M, double time_sph,
-                                                   const double* s, const double* gu,
-                                                   double* fdp, double* G, double* vivel) {
+// the body, with its outputs as the FP32 values they are (G, vivel); returns whether the
+// point is loading (G non-zero)
+__device__ __forceinline__ bool drucker_prager_f32v(const Real& M, double time_sph,
+                                                    const double* s, const double* gu,
+                                                    double* fdp, float* G, float* vivel) {
   const double f0 = *fdp;
   float s0h, s0l, s1h, s1l, s3h, s3l;
   f32_split(s[0], s0h, s0l);
@@ -842,18 +844,31 @@ __device__ __forceinline__ void drucker_prager_f32(const Real& M, double time_sp
     const float gs = __fdiv_rn(G_mod, sj);
     const float lambda_1 = ((3.0f * alpha2) * K_mod) * emean;
     const float G2 = __fdiv_rn(fmaf(gs, s_eps, lambda_1), G_mod);
-    G[0] = f64_of((gs * dv0) * G2);
-    G[1] = f64_of((gs * dv1) * G2);
-    G[2] = f64_of((gs * dv2) * G2);
-    G[3] = f64_of((gs * dv3) * G2);
+    G[0] = (gs * dv0) * G2;
+    G[1] = (gs * dv1) * G2;
+    G[2] = (gs * dv2) * G2;
+    G[3] = (gs * dv3) * G2;
     const float rs = __frcp_rn(sj), r6 = rs * (1.0f / 6.0f);
-    vivel[0] = f64_of((r6 * ((2.0f * dv0 - dv1) - dv3)) * G2);
-    vivel[1] = f64_of((r6 * ((2.0f * dv1 - dv0) - dv3)) * G2);
-    vivel[2] = f64_of((rs * dv2) * G2);
-    vivel[3] = f64_of((r6 * ((2.0f * dv3 - dv0) - dv1)) * G2);
-  } else {
-    G[0] = G[1] = G[2] = G[3] = 0.0;
-    vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0;
+    vivel[0] = (r6 * ((2.0f * dv0 - dv1) - dv3)) * G2;
+    vivel[1] = (r6 * ((2.0f * dv1 - dv0) - dv3)) * G2;
+    vivel[2] = (rs * dv2) * G2;
+    vivel[3] = (r6 * ((2.0f * dv3 - dv0) - dv1)) * G2;
+    return G[0] != 0.0f || G[1] != 0.0f || G[2] != 0.0f || G[3] != 0.0f;
+  }
+  G[0] = G[1] = G[2] = G[3] = 0.0f;
+  vivel[0] = vivel[1] = vivel[2] = vivel[3] = 0.0f;
+  return false;
+}
+
+// the same with FP64 outputs (exact conversions of the FP32 values)
+__device__ __forceinline__ void drucker_prager_f32(const Real& M, double time_sph,
+                                                   const double* s, const double* gu,
+                                                   double* fdp, double* G, double* vivel) {
+  float Gf[4], vf[4];
+  drucker_prager_f32v(M, time_sph, s, gu, fdp, Gf, vf);
+  for (int k = 0; k < 4; k++) {
+    G[k] = f64_of(Gf[k]);
+    vivel[k] = f64_of(vf[k]);
   }
 }
 

@@ -101,6 +101,9 @@ struct Ctx {
   // sums (1, 2, 4), whose entries and records are loaded before any is summed; chosen by
   // sps_autotune (results do not depend on them)
   int ahead[2] = {4, 2};
+  // FP32 form: every realisation is Drucker-Prager (ncrit 12, ntype_eco > 1) in plane strain
+  // without continuity density, so the stress-point tail takes its lean kernel
+  bool lean_tail = false;
   // scratch for scans
   int scan_blocks = 0;
   // per-kernel event timing (sps_profile_step)

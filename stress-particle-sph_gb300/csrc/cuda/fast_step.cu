@@ -498,6 +498,48 @@ __global__ void __launch_bounds__(256, KIND == 1 ? 4 : 3) k_fderivs(Dev D, int s
 //   r = dt |grad f : (D:e + Gs)| / sqrt(J2),  f = sqrt(J2) + alpha I1 - k_c,
 // is at most surr_tol (the exact flow rule makes grad f : (D:e + Gs) = 0 up to rounding).
 // Every other stress-point takes the exact flow rule.
+// The stress-point tail of the FP32 form without the network, for the Drucker-Prager plane
+// strain case (every realisation: ntype_eco > 1, ncrit 12, ntype_solid != 1, no
+// continuity density, no training capture; the host checks): the arithmetic of
+// tail_sp_rates<true>
+// with the flow rule's outputs kept as the FP32 values they are (fewer registers, no FP64
+// copies); FP64 only for the state's RK accumulation.
+__device__ __forceinline__ void tail_sp_f32(const Dev& D, const StepScalars& sc, int t,
+                                            double f2) {
+  const Real& M = real_of(D, t);
+  const double* gu = D.grad_u + 4 * (size_t)t;
+  const double g[4] = {gu[0], gu[1], gu[2], gu[3]};
+  const double st[4] = {D.s0[t], D.s1[t], D.s2[t], D.s3[t]};
+  double f = D.fdp[t];
+  float G[4], vv[4];
+  drucker_prager_f32v(M, sc.time_sph, st, g, &f, G, vv);  // (no capture: see lean_tail)
+  D.fdp[t] = f;
+  // explicit fmaf: the same rounding as tail_sp_rates<true>
+  const float q = fmaf(2.0f, fmaf(vv[0], vv[0], fmaf(vv[1], vv[1], __fmul_rn(vv[3], vv[3]))),
+                       __fmul_rn(vv[2], vv[2]));
+  const double der = f64_of(sqrtf(__fmul_rn(q, 1.0f / 3.0f)));
+  const float h11 = f32_rn(g[0]), h21 = f32_rn(g[1]), h12 = f32_rn(g[2]), h22 = f32_rn(g[3]);
+  float r[4];
+  r[0] = fmaf(M.D11f, h11, M.D12f * h22);
+  r[1] = fmaf(M.D12f, h11, M.D22f * h22);
+  r[2] = M.D33f * (h21 + h12);
+  r[3] = fmaf(M.D41f, h11, M.D42f * h22);
+  if (D.update_x) {
+    const float om1 = 0.5f * (h12 - h21);
+    const float t0 = f32_rn(st[0]), t1 = f32_rn(st[1]), t2 = f32_rn(st[2]);
+    r[0] = fmaf(2.0f * om1, t2, r[0]);
+    r[1] = fmaf(-2.0f * om1, t2, r[1]);
+    r[2] = fmaf(om1, t1 - t0, r[2]);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const double rhs = f64_of(r[k] + -G[k]);
+    D.RHS1[k][t] = rhs;
+    D.RKs[k][t] = fma(f2, rhs, D.RKs[k][t]);
+  }
+  D.RKd[t] = D.RKd[t] + der * f2;
+}
+
 // The surrogate's view of stress-point t: the exact rule (drucker_prager, whose results dp
 // = {G, vivel, f} the tail reuses), whether it is loading, and for a loading point the
 // network's inputs x, their output scale and whether they lie in the training envelope.
@@ -533,7 +575,7 @@ __device__ __forceinline__ void surr_front(const Dev& D, const Real& M, const St
 // One stress-point (index i among the stress-points) of k_fsp_tail; the warp's 32 lanes
 // call it together.  SURR: the network's prediction for a candidate is the row that
 // k_fsp_cand appended for it this stage, computed by the tensor-core kernel in between.
-template <bool SURR>
+template <bool SURR, bool LEAN = false>
 __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
   const int lane = threadIdx.x & 31;
   const bool act = i < D.NT - D.NN;
@@ -597,6 +639,8 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
            v3 = -Gnet[3] / (2.0 * gm);
     double der = sqrt((2.0 * ((v0 * v0 + v1 * v1) + v3 * v3) + v2 * v2) / 3.0);
     tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, Gnet, der, have_dp ? dp : nullptr);
+  } else if (LEAN) {
+    tail_sp_f32(D, sc, t, f2);
   } else {
     tail_sp_rates<true>(D, sc, t, D.grad_u + 4 * (size_t)t, f2, nullptr, 0.0,
                         have_dp ? dp : nullptr);
@@ -609,12 +653,13 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
 // over at most kTailBlocks blocks (a few SM-fulls, so that the launch costs little when the
 // gate skips it); the one without over a block per 128 stress-points.
 constexpr int kTailBlocks = 152 * 8;
-template <bool SURR>
+// LEAN (without the network only): tail_sp_f32 for the Drucker-Prager plane strain case
+template <bool SURR, bool LEAN = false>
 __global__ void __launch_bounds__(128) k_fsp_tail(Dev D, int stage) {
   if (D.surr && (D.surr_gate->on != 0) != SURR) return;
   const int ns = D.NT - D.NN;
   for (int base = blockIdx.x * blockDim.x; base < ns; base += gridDim.x * blockDim.x)
-    fsp_tail_one<SURR>(D, stage, base + threadIdx.x);
+    fsp_tail_one<SURR, LEAN>(D, stage, base + threadIdx.x);
 }
 
 // The surrogate's candidates of this stage (while the gate runs the network): every loading
@@ -741,7 +786,9 @@ void launch_fsp_tail(Ctx& c, int stage) {
   }
   // the variant without the network over one block per 128 stress-points: when it runs
   // it does the work, and the scheduler refills SMs with fresh blocks as others wait
-  k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  if (c.lean_tail && !c.d.cap_buf)
+    k_fsp_tail<false, true><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
+  else k_fsp_tail<false><<<(ns + 127) / 128, 128, 0, c.stream>>>(c.d, stage);
 }
 void launch_fxsph(Ctx& c) {
   k_fxsph<<<c.grid_of(TK_XSPH, c.d.N2), c.blk[TK_XSPH], 0, c.stream>>>(c.d);

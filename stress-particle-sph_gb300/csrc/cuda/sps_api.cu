@@ -624,6 +624,9 @@ int sps_create_batch(int32_t nreal, const sps_params* ps, sps_ctx** out) {
                                      cudaMemcpyHostToDevice, c.stream));
       D.real = rd;
       D.real0 = c.real[0];
+      c.lean_tail = p->precision == SPS_PREC_FP32_FAST && !p->cont_density;
+      for (const sps::Real& M : c.real)
+        c.lean_tail = c.lean_tail && M.ntype_eco > 1 && M.ncrit == 12 && M.ntype_solid != 1;
       std::vector<uint16_t> rid(N2);
       for (int r = 0; r < nreal; r++) {
         const sps::Real& M = c.real[r];
