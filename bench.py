@@ -727,7 +727,7 @@ def run_ours(args):
         surr = {"tol": args.surrogate_tol,
                 "drift_test": "dt |grad f : (D:e + Gs)| / sqrt(J2) <= tol",
                 "training": training,
-                "gate": {"min_answered": args.surrogate_gate, "max_period": 64,
+                "gate": {"min_answered": args.surrogate_gate, "max_period": 1024,
                          "timed_steps_with_network": g1[0] - g0[0],
                          "timed_steps_without": g1[1] - g0[1]},
                 "timed_loading_evaluations_with_network": loading,

@@ -124,7 +124,8 @@ int sps_surrogate_install(sps_ctx* ctx, sps_mlp* m, const sps_surrogate_opts* op
    a period of steps and then the network is tried for one step again, the period
    doubling up to max_period steps while these tries keep failing and returning to 1 after
    one that passes.  The decision is taken on the device at the end of every step.
-   min_answered <= 0 keeps the network on in every step.  Defaults at install: 0.5 and 64.
+   min_answered <= 0 keeps the network on in every step.  Defaults at install: 0.5 and 1024
+   (a network that keeps failing is then tried about once in a thousand steps).
    Setting it restarts the gate (on, period 1). */
 int sps_surrogate_gate(sps_ctx* ctx, double min_answered, int32_t max_period);
 

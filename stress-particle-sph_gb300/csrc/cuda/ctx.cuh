@@ -119,7 +119,7 @@ struct Ctx {
   void* tc_img = nullptr;                   // tensor-core image of the network and biases
   int tc_grid = 0;                          // CTAs of the tensor-core forward pass
   double gate_min_frac = 0.5;               // sps_surrogate_gate
-  int gate_max_period = 64;
+  int gate_max_period = 1024;
   // output snapshot (sps_snapshot): device copy of the output fields, pinned host copy,
   // the stream that moves one to the other, and the events that order them
   char* snap_dev = nullptr;

@@ -204,7 +204,7 @@ def stats(ctx, reset=False):
     return tuple(int(v) for v in c)
 
 
-def set_gate(ctx, min_answered=0.5, max_period=64):
+def set_gate(ctx, min_answered=0.5, max_period=1024):
     """The network runs in a step only while it answers at least min_answered of the
     step's loading evaluations (<= 0: always); see sps_surrogate_gate."""
     rc = _lib().sps_surrogate_gate(ctx._h, float(min_answered), int(max_period))
