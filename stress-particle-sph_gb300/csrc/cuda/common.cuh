@@ -288,7 +288,7 @@ __device__ __forceinline__ void prefetch_list_l2(const int4* list, int col, int 
 // values here); a zero numerator returns a signed zero.  Bit-for-bit agreement with the
 // IEEE division is checked on the GPU by sps_selftest.
 __device__ __forceinline__ double div_rcp(double a, double b, double y) {
-  if (a == 0.0) return a * y;
+  if ((__double_as_longlong(a) << 1) == 0) return a * y;  // a zero, tested on the integer pipe
   double q = a * y;
   double r = fma(-b, q, a);
   q = fma(r, y, q);

@@ -485,9 +485,9 @@ __device__ __forceinline__ int4 half_entry(const Dev& D, const Grid& g, int a, i
     double w, dw0, dw1;
     if (g.uniform_h) cubic_uniform(g, r, dx, dy, &w, &dw0, &dw1);
     else sph_kernel(D.skf, D.pi, r, dx, dy, mh, &w, &dw0, &dw1);
-    wf = (float)w;
-    d0f = (float)dw0;
-    d1f = (float)dw1;
+    wf = f32_rn(w);  // the same bits as (float), on the integer pipe
+    d0f = f32_rn(dw0);
+    d1f = f32_rn(dw1);
   } else if (g.uniform_h) {
     // separation as double-float from the cell-relative hi/lo offsets
     // x_a - x_b = (offset_a - offset_b) - (cell shift) with every term in double-float

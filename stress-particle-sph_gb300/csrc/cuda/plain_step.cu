@@ -176,7 +176,8 @@ __global__ void k_bound(Dev D) {
     const int col = D.lcol[D.spos[i]];
     int deg = D.degC[col];
     for (int k = 0; k < deg; k++) {
-      int u = D.cross[ell(k, col, D.N2)].x;
+      // the partner ids only: the compact entries when the lists were gathered
+      int u = D.use_crossW ? D.crossW[(size_t)k * D.N2 + col].x : D.cross[ell(k, col, D.N2)].x;
       if (u < j0 || u >= j1) continue;
       float fx, fy;
       if (!bound_term(D, M, i, u, fx, fy)) continue;
@@ -304,7 +305,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       if (e.y < 0) continue;  // a dummy partner (sign bit of W)
-      double w = (double)__int_as_float(e.y);
+      double w = f64_of(__int_as_float(e.y));  // exact, on the integer pipe
       double h2 = D.vol[u] * w;  // (mass/rho)*w with mass/rho formed once per particle
       v0 = v0 + D.vx[u] * h2;
       v1 = v1 + D.vy[u] * h2;
@@ -320,7 +321,7 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
       int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       if (e.y < 0) continue;  // a dummy partner (sign bit of W)
-      double w = (double)__int_as_float(e.y);
+      double w = f64_of(__int_as_float(e.y));  // exact, on the integer pipe
       double ru = D.rho[u];
       double h1 = D.vol[u] * w;
       a = a + D.s0[u] * h1;
@@ -534,7 +535,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
       int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
-      double Gx = (double)__int_as_float(e.z), Gy = (double)__int_as_float(e.w);
+      double Gx = f64_of(__int_as_float(e.z)), Gy = f64_of(__int_as_float(e.w));
       double mu = D.mass[u], ru = D.rho[u], iu = D.rinv[u];
       if (!wall) {  // node -- stress-point (target is pair_i)
         double h1 = div_rcp(Gx * mu, ru, iu);
@@ -584,7 +585,7 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
       int4 e = D.cross[ell(k, col, D.N2)];
       int u = e.x;
       const bool wall = e.y < 0;  // a dummy partner (sign bit of W)
-      double dwx = -(double)__int_as_float(e.z), dwy = -(double)__int_as_float(e.w);
+      double dwx = -f64_of(__int_as_float(e.z)), dwy = -f64_of(__int_as_float(e.w));
       double mu = D.mass[u];
       if (!wall) {  // node -- stress-point (stress-point is pair_i)
         const double au[3] = {D.A[0][u], D.A[1][u], D.A[2][u]};
@@ -725,7 +726,7 @@ __global__ void k_xsph(Dev D) {
   for (int k = 0; k < deg; k++) {
     int4 e = D.same[ell(k, col, D.N2)];
     int u = e.x;
-    double w = (double)__int_as_float(e.y);
+    double w = f64_of(__int_as_float(e.y));  // exact, on the integer pipe
     double vol = D.vol[u];
     s0 = s0 + (vol * (D.vx[u] - vt0)) * w;
     s1 = s1 + (vol * (D.vy[u] - vt1)) * w;
