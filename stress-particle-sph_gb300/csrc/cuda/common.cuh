@@ -278,6 +278,20 @@ __device__ __forceinline__ void prefetch_list_l2(const int4* list, int col, int 
   }
 }
 
+// an ordered key of a non-NaN double on the integer pipe: the bit pattern with the
+// magnitude bits of a negative value flipped, -0 taken as +0 (a < b exactly when
+// f64_key(a) < f64_key(b))
+__device__ __forceinline__ long long f64_key(double a) {
+  long long ia = __double_as_longlong(a);
+  if ((ia << 1) == 0) ia = 0;
+  return ia ^ ((ia >> 63) & 0x7FFFFFFFFFFFFFFFll);
+}
+__device__ __forceinline__ bool f64_isnan(double a) {
+  return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll;
+}
+// a >= b for non-NaN doubles, on the integer pipe
+__device__ __forceinline__ bool f64_ge(double a, double b) { return f64_key(a) >= f64_key(b); }
+
 // Correctly rounded a / b given y = RN(1/b), by Markstein's theorem (P. Markstein, "Computation
 // of elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
 // 1990; see also Muller et al., Handbook of Floating-Point Arithmetic, the theorem on
@@ -474,17 +488,21 @@ __device__ __forceinline__ void cubic_uniform(const Grid& g, double r, double dx
   *w = 0.0;
   *dw0 = 0.0;
   *dw1 = 0.0;
-  if (q >= 0 && q <= 1.0) {
+  // the branch tests on the integer pipe (ordered keys; q is a non-negative quotient or NaN,
+  // which takes neither branch)
+  const long long kq = f64_key(q);
+  const bool qnan = f64_isnan(q);
+  if (!qnan && kq >= 0 && kq <= f64_key(1.0)) {
     const double two_thirds = (double)(2.0f / 3.0f);
-    *w = g.factor * ((two_thirds - q * q) + (q * q * q) / 2.0);
+    *w = g.factor * ((two_thirds - q * q) + (q * q * q) * 0.5);  // / 2.0, exactly
     double a = div_rcp(g.factor * (-2.0 + 1.5 * q), g.hh, g.yhh);
     *dw0 = a * dx0;
     *dw1 = a * dx1;
-  } else if (q > 1.0 && q <= 2.0) {
+  } else if (!qnan && kq > f64_key(1.0) && kq <= f64_key(2.0)) {
     double t = 2.0 - q;
     *w = g.factor6 * ((t * t) * t);
     double a = div_rcp(g.c3 * (t * t), g.h, g.yh);
-    double yr = 1.0 / r;
+    double yr = __drcp_rn(r);  // RN(1 / r), the correctly rounded reciprocal
     *dw0 = -(a * div_rcp(dx0, r, yr));
     *dw1 = -(a * div_rcp(dx1, r, yr));
   }
@@ -785,19 +803,6 @@ __device__ __forceinline__ float two_sum_f(float a, float b, float& e) {
   return s;
 }
 
-// an ordered key of a non-NaN double on the integer pipe: the bit pattern with the
-// magnitude bits of a negative value flipped, -0 taken as +0 (a < b exactly when
-// f64_key(a) < f64_key(b))
-__device__ __forceinline__ long long f64_key(double a) {
-  long long ia = __double_as_longlong(a);
-  if ((ia << 1) == 0) ia = 0;
-  return ia ^ ((ia >> 63) & 0x7FFFFFFFFFFFFFFFll);
-}
-__device__ __forceinline__ bool f64_isnan(double a) {
-  return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll;
-}
-// a >= b for non-NaN doubles, on the integer pipe
-__device__ __forceinline__ bool f64_ge(double a, double b) { return f64_key(a) >= f64_key(b); }
 
 // drucker_prager for the FP32 form, without FP64 arithmetic (GB300 issues FP64 at 1/64 of
 // its FP32 rate): the stresses enter as hi + lo splits, the mean is formed in double-float

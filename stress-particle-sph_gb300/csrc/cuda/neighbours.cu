@@ -266,17 +266,42 @@ __global__ void k_grid(Dev D) {
 // rounded by div_rcp from the cell size's reciprocal (an IEEE division costs GB300's FP64
 // pipe about ten times as much); non-finite offsets take the IEEE division
 __device__ __forceinline__ double cell_quot(double a, double b, double y) {
-  return isfinite(a) ? div_rcp(a, b, y) : a / b;
+  const bool finite = (__double_as_longlong(a) & 0x7FF0000000000000ll) != 0x7FF0000000000000ll;
+  return finite ? div_rcp(a, b, y) : a / b;
 }
 
-// local cell of a position in a realisation's grid
+// (int)q for 1 <= q < 2^31, truncating, on the integer pipe (the significand shifted by
+// the exponent)
+__device__ __forceinline__ int trunc_pos(double q) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;  // 0 .. 30
+  const unsigned long long m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  return (int)(m >> (52 - e));
+}
+
+// (double)n for 0 <= n < 2^31, exact, on the integer pipe
+__device__ __forceinline__ double i2d_pos(int n) {
+  if (n == 0) return 0.0;
+  const int e = 31 - __clz(n);  // the leading bit
+  const unsigned long long m = ((unsigned long long)(unsigned)n << (52 - e)) & 0x000FFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)(((unsigned long long)(e + 1023) << 52) | m));
+}
+
+// local cell of a position in a realisation's grid: q = (x - xmin) / delta + 1 with the
+// reference's rounding, then its integer part clamped to [1, ndiv]; the comparisons and
+// conversions on the integer pipe (ordered keys; q >= 1 is positive, below 2^31)
 __device__ __forceinline__ int cell_index(const Grid& g, double x, double y) {
-  double qx = cell_quot(x - g.xmin[0], g.deltx[0], g.rdeltx[0]) + 1.0;
-  double qy = cell_quot(y - g.xmin[1], g.deltx[1], g.rdeltx[1]) + 1.0;
+  const double qx = cell_quot(x - g.xmin[0], g.deltx[0], g.rdeltx[0]) + 1.0;
+  const double qy = cell_quot(y - g.xmin[1], g.deltx[1], g.rdeltx[1]) + 1.0;
   // particles inside the bounding box give 1 <= q < ndiv + 1; the clamps only guard
-  // against non-finite coordinates
-  int ix = (qx >= 1.0) ? (qx < (double)g.ndiv[0] ? (int)qx : g.ndiv[0]) : 1;
-  int iy = (qy >= 1.0) ? (qy < (double)g.ndiv[1] ? (int)qy : g.ndiv[1]) : 1;
+  // against non-finite coordinates (a NaN q takes cell 1, as the FP64 comparisons did)
+  auto idx = [](double q, int nd) {
+    if (f64_isnan(q)) return 1;
+    const long long k = f64_key(q);
+    if (!(k >= f64_key(1.0))) return 1;
+    return k < f64_key(i2d_pos(nd)) ? trunc_pos(q) : nd;
+  };
+  const int ix = idx(qx, g.ndiv[0]), iy = idx(qy, g.ndiv[1]);
   return g.ndiv[0] * (iy - 1) + (ix - 1);
 }
 
@@ -293,8 +318,8 @@ __global__ void k_cell_count(Dev D) {
     int cl = cell_index(g, x, y);
     // FP32 offsets from the particle's own cell corner (|offset| <= one cell)
     int ix = cl % g.ndiv[0], iy = cl / g.ndiv[0];
-    double ox = x - (g.xmin[0] + (double)ix * g.deltx[0]);
-    double oy = y - (g.xmin[1] + (double)iy * g.deltx[1]);
+    double ox = x - (g.xmin[0] + i2d_pos(ix) * g.deltx[0]);
+    double oy = y - (g.xmin[1] + i2d_pos(iy) * g.deltx[1]);
     // the conversions on the integer pipe (f32_split: hi = (float)ox and lo = (float)(ox -
     // hi), the same bits as the hardware conversions, which GB300 issues at its FP64 rate)
     float oxh, oxl, oyh, oyl;
@@ -358,9 +383,10 @@ __device__ __forceinline__ bool exact_test(const Dev& D, int a, int b, double& r
   double driac = dx * dx;
   dy = D.py[a] - D.py[b];
   driac = driac + dy * dy;
-  mh = (D.hsml[a] + D.hsml[b]) / 2.0;
+  mh = (D.hsml[a] + D.hsml[b]) * 0.5;  // / 2.0, exactly
   r = sqrt(driac);
-  return r < (double)D.scale_k * mh;
+  // r < scale_k mh with the conversion and the comparison on the integer pipe (r >= 0)
+  return !f64_isnan(r) && f64_key(r) < f64_key(i2d_pos(D.scale_k) * mh);
 }
 
 // 0 = reject, 1 = accept, 2 = undecided (inside the guard band).  (cx, cy) is the corner

@@ -175,31 +175,41 @@ __global__ void k_bound(Dev D) {
   if (D.bound_from_lists) {
     const int col = D.lcol[D.spos[i]];
     int deg = D.degC[col];
-    for (int k = 0; k < deg; k++) {
-      // the partner ids only: the compact entries when the lists were gathered
-      int u = D.use_crossW ? D.crossW[(size_t)k * D.N2 + col].x : D.cross[ell(k, col, D.N2)].x;
-      if (u < j0 || u >= j1) continue;
-      float fx, fy;
-      if (!bound_term(D, M, i, u, fx, fy)) continue;
-      if (n < K) {
-        int p = n++;
-        while (p > 0 && ids[p - 1] > u) {
-          ids[p] = ids[p - 1];
-          tx[p] = tx[p - 1];
-          ty[p] = ty[p - 1];
-          p--;
+    // the partner ids four at a time (independent loads in flight together; the compact
+    // entries when the lists were gathered), then the innermost dummies among them
+    for (int k0 = 0; k0 < deg; k0 += 4) {
+      int uu[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        uu[q] = k0 + q >= deg ? -1
+                : D.use_crossW ? D.crossW[(size_t)(k0 + q) * D.N2 + col].x
+                               : D.cross[ell(k0 + q, col, D.N2)].x;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int u = uu[q];
+        if (u < j0 || u >= j1) continue;
+        float fx, fy;
+        if (!bound_term(D, M, i, u, fx, fy)) continue;
+        if (n < K) {
+          int p = n++;
+          while (p > 0 && ids[p - 1] > u) {
+            ids[p] = ids[p - 1];
+            tx[p] = tx[p - 1];
+            ty[p] = ty[p - 1];
+            p--;
+          }
+          ids[p] = u;
+          tx[p] = fx;
+          ty[p] = fy;
+        } else {
+          atomicOr(D.err, ERR_BOUND);
         }
-        ids[p] = u;
-        tx[p] = fx;
-        ty[p] = fy;
-      } else {
-        atomicOr(D.err, ERR_BOUND);
       }
     }
     double bx = 0.0, by = 0.0;
     for (int k = 0; k < n; k++) {
-      bx = bx + (double)tx[k];
-      by = by + (double)ty[k];
+      bx = bx + f64_of(tx[k]);
+      by = by + f64_of(ty[k]);
     }
     D.fbx[i] = bx;
     D.fby[i] = by;
