@@ -70,6 +70,9 @@ def parse():
                     help="simulated time (s) at which the run also reports the errors of the "
                          "FP32 form, with and without the surrogate, and of the 2^-52 floor "
                          "against the FP64 plain form, from fresh contexts (0: skip)")
+    ap.add_argument("--steady-steps", type=int, default=500,
+                    help="steps with the network before the settled with/without comparison "
+                         "(0: skip)")
     ap.add_argument("--surrogate-tol", type=float, default=1e-6)
     ap.add_argument("--surrogate-gate", type=float, default=0.5,
                     help="answered fraction below which a step runs without the network "
@@ -577,10 +580,11 @@ def kernel_bytes(name, prob, deg, fast=False):
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch group of the FP32
 # form on the full-size slope (dx 0.012 m), from one ncu pass over the first timed stage
 # (profiles/dram_traffic_fp32_slope_2M.md); the neighbour sums' group is the stress-point
-# and the node launch of one stage.  Valid for that workload and this code state only.
-NCU_TRAFFIC_FULL = {"derivs": 337758000 + 22606080 + 429369000 + 40654848,
-                    "interp": 304817000 + 10200320 + 306133000 + 27445248,
-                    "lists": 1009711000 + 493658624, "half": 230960000 + 686468352}
+# and the node launch of one stage, the gather's the two target kinds and the remaining
+# positions.  Valid for that workload and this code state only.
+NCU_TRAFFIC_FULL = {"derivs": 337793792 + 22539776 + 388249856 + 26990592,
+                    "interp": 176712704 + 8054784 + 178151168 + 22437632,
+                    "gather": 100680704 + 339088640 + 101198848 + 336080384 + 8663552}
 NCU_TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum (1 pass), "
                       "FP32 form, this slope at dx 0.012 m, first timed stage")
 
@@ -746,6 +750,24 @@ def run_ours(args):
         surr["speed_with_over_without"] = round(ms_n / ms_max, 4)
         sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
         sg.set_gate(ctx, args.surrogate_gate)
+        # the same comparison once the gate has settled: 500 steps with the network first
+        # (its tries are then hundreds of steps apart), then the timed steps with and
+        # without it from the same state
+        if args.steady_steps > 0:
+            t = ctx.step(args.steady_steps, t)
+            g2 = sg.gate_stats(ctx)
+            t, ms_s, _ = timed_steps(ctx, args.steps, t, dist, local)
+            g3 = sg.gate_stats(ctx)
+            sg.install(ctx, None)
+            t = ctx.step(2, t)
+            t, ms_s0, _ = timed_steps(ctx, args.steps, t, dist, local)
+            surr["settled"] = {
+                "after_steps": args.steady_steps, "ms_per_step_with": round(ms_s / args.steps, 4),
+                "ms_per_step_without": round(ms_s0 / args.steps, 4),
+                "timed_steps_with_network": g3[0] - g2[0],
+                "speed_with_over_without": round(ms_s0 / ms_s, 4)}
+            sg.install(ctx, net, tol=args.surrogate_tol, envelope=env)
+            sg.set_gate(ctx, args.surrogate_gate)
 
     plain = None
     errors = None

@@ -53,7 +53,6 @@ struct ProdSum {
     hi.add(p);
     lo += e;
   }
-  __device__ __forceinline__ double val() const { return hi.val() + (double)lo; }
 };
 
 // difference of two double-float values (hi + lo) in FP32
