@@ -690,23 +690,28 @@ __device__ __forceinline__ void store_pair(int4* dst, int4 a, int4 b) {
 
 // the list entry of partner bs (cell offset qx, qy) of a target of type ta with FP32
 // cell-relative offsets (xa, xal), (ya, yal) and smoothing length ha: {partner id, W (sign
-// bit set for a dummy partner), dW/dx, dW/dy} with the gradient with respect to the target
+// bit set for a dummy partner), dW/dx, dW/dy} with the gradient with respect to the target.
+// f32: the kernel values in FP32 from the FP32 separation (same-kind entries that only the
+// FP32 free-surface detection reads), otherwise r and r/h in double-float (cubic_mixed)
 __device__ __forceinline__ int4 gather_entry(const Dev& D, const Grid& g, int ta, float xa,
                                              float ya, float ha, float xal, float yal, int bs,
-                                             int qx, int qy) {
+                                             int qx, int qy, bool f32 = false) {
   const int b = D.sorted[bs];
   const float4 rb = D.srec[bs];
   float wf, d0f, d1f;
-  if (g.uniform_h) {
+  if (g.uniform_h && !f32) {
     const float2 rl = D.srecl[bs];
     cubic_mixed(g, df_sep(xa, xal, rb.x, rl.x, qx, g.df_cell[0]),
                 df_sep(ya, yal, rb.y, rl.y, qy, g.df_cell[1]), &wf, &d0f, &d1f);
   } else {
-    const float cx = (float)qx * (float)g.deltx[0], cy = (float)qy * (float)g.deltx[1];
+    // the cell shift qx * (float)deltx without conversions on the FP64 pipe
+    const float cw = f32_rn(g.deltx[0]), ch = f32_rn(g.deltx[1]);
+    const float cx = qx < 0 ? -cw : (qx > 0 ? cw : 0.0f);
+    const float cy = qy < 0 ? -ch : (qy > 0 ? ch : 0.0f);
     const float fx = (xa - rb.x) - cx, fy = (ya - rb.y) - cy;
     const float hm = (ha + rb.z) * 0.5f;
     const float rf = sqrtf(fx * fx + fy * fy);
-    sph_kernel_f32(D.skf, (float)D.pi, rf, fx, fy, hm, &wf, &d0f, &d1f);
+    sph_kernel_f32(D.skf, f32_rn(D.pi), rf, fx, fy, hm, &wf, &d0f, &d1f);
   }
   const int pt = pint_type(ta, __float_as_int(rb.w));
   const int w = __float_as_int(wf);
@@ -825,13 +830,13 @@ __global__ void __launch_bounds__(512, 2) k_fgather(Dev D, const int32_t* __rest
     }
     const float xal = D.xrl[a], yal = D.yrl[a];
     // phase 2: the entries, stored in pairs (whole 32-byte sectors)
-    auto finish = [&](const int* buf, int n, int4* list, int2* compact) {
+    auto finish = [&](const int* buf, int n, int4* list, int2* compact, bool f32) {
       int4 pend = make_int4(0, 0, 0, 0);
       for (int k = 0; k < n; k++) {
         const unsigned v = (unsigned)buf[(size_t)k * bd + tid];
         const int code = (int)(v >> kHalfTypeShift);
         const int4 e = gather_entry(D, g, ta, xa, ya, ha, xal, yal, (int)(v & kHalfIdMask),
-                                    code % 3 - 1, code / 3 - 1);
+                                    code % 3 - 1, code / 3 - 1, f32);
         if (k & 1) store_pair(list + ell(k - 1, col, D.N2), pend, e);
         else pend = e;
         // the lanes of a warp write entry k of adjacent columns together: whole sectors
@@ -839,8 +844,10 @@ __global__ void __launch_bounds__(512, 2) k_fgather(Dev D, const int32_t* __rest
       }
       if (n & 1) list[ell(n - 1, col, D.N2)] = pend;
     };
-    finish(bufC, nC, D.cross, D.use_crossW ? D.crossW : nullptr);
-    if (SAME) finish(bufS, nS, D.same, nullptr);
+    finish(bufC, nC, D.cross, D.use_crossW ? D.crossW : nullptr, false);
+    // same-kind entries that no step kernel reads serve the FP32 free-surface detection
+    // only: FP32 kernel values
+    if (SAME) finish(bufS, nS, D.same, nullptr, !D.same_entries);
   }
   D.degC[col] = nC;
   D.degS[col] = nS;
