@@ -253,19 +253,21 @@ __global__ void k_snap_pack(sps::Dev D, char* out, const int64_t* roff) {
   char* base = out + roff[r];
   double2* x = reinterpret_cast<double2*>(base + b.x);
   double2* v = reinterpret_cast<double2*>(base + b.vel);
-  double4* s = reinterpret_cast<double4*>(base + b.stress);
+  double2* s = reinterpret_cast<double2*>(base + b.stress);  // 4 doubles per particle
   x[l] = make_double2(D.px[g], D.py[g]);
   v[l] = make_double2(D.vx[g], D.vy[g]);
   reinterpret_cast<double*>(base + b.rho)[l] = D.rho[g];
   if (g < D.NT) {
-    s[l] = make_double4(D.s0[g], D.s1[g], D.s2[g], D.s3[g]);
+    s[2 * l] = make_double2(D.s0[g], D.s1[g]);
+    s[2 * l + 1] = make_double2(D.s2[g], D.s3[g]);
     reinterpret_cast<double*>(base + b.iv1)[l] = D.iv1[g];
     reinterpret_cast<double*>(base + b.fdp)[l] = D.fdp[g];
     reinterpret_cast<int32_t*>(base + b.bc)[l] = D.bc_or_not[g];
     if (g < D.NN)
       reinterpret_cast<double2*>(base + b.displ)[l] = make_double2(D.dispx[g], D.dispy[g]);
   } else {
-    s[l] = make_double4(0.0, 0.0, 0.0, 0.0);
+    s[2 * l] = make_double2(0.0, 0.0);
+    s[2 * l + 1] = make_double2(0.0, 0.0);
   }
 }
 __global__ void k_aos_to_soa4(const double* in, double* a, double* b, double* c, double* d, int n) {
