@@ -17,9 +17,11 @@ e2e    = the same metric through the C-ABI with host buffers: every step uploads
          state from pinned host memory (sps_upload), advances one step (sps_step) and
          downloads the fields (sps_download).
 --impl reference times the CPU restatement of the reference's step (the oracle; the
-         Fortran reference cannot be compiled on either machine) on the same workload, on
-         one host thread as the single-threaded reference runs, for a bounded number of
-         steps (min(K, 2) after min(W, 1) warm-up).
+         Fortran reference cannot be compiled on either machine) on the same workload, as
+         independent single-threaded replicas (the reference's step is single-threaded),
+         one per host core as far as the host memory allows, for a bounded number of steps
+         (min(K, 2) after min(W, 1) warm-up); value = all replicas' particle-steps over
+         the slowest replica's time.
 
 The headline runs the FP32 form with the learned Drucker-Prager surrogate installed
 (trained first, on the GPU, on tuples captured from coarse runs of the same slope with
@@ -30,6 +32,7 @@ reported after the same number of steps.
 import argparse
 import json
 import os
+import queue
 import statistics
 import subprocess
 import sys
@@ -53,6 +56,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ref-replicas", type=int, default=0,
+                    help="reference arm: single-threaded replicas of the workload run side "
+                         "by side (0: one per core, bounded by the host memory)")
     ap.add_argument("--precision", default="fast", choices=["plain", "fast"])
     ap.add_argument("--dx", type=float, default=0.012)
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -941,43 +947,135 @@ def cpu_baseline(args):
             "sample": sample}
 
 
+# peak resident memory of one oracle replica per particle slot (ntotal2): 2.46 GB measured
+# for the 2.01M-slot slope, interpreter included; rounded up
+REF_BYTES_PER_PARTICLE = 1500
+REF_BYTES_FIXED = 200 << 20
+
+
+def host_memory_available():
+    """Bytes this process may still allocate: MemAvailable from /proc/meminfo, lowered to
+    the cgroup's remaining limit (v2 memory.max - memory.current, or v1
+    memory.limit_in_bytes - memory.usage_in_bytes) where one is set.  None if unknown."""
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    for lim_f, cur_f in (("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory.current"),
+                         ("/sys/fs/cgroup/memory/memory.limit_in_bytes",
+                          "/sys/fs/cgroup/memory/memory.usage_in_bytes")):
+        try:
+            lim = open(lim_f).read().strip()
+            cur = int(open(cur_f).read().strip())
+        except (OSError, ValueError):
+            continue
+        if lim.isdigit() and int(lim) < (1 << 60):
+            left = max(0, int(lim) - cur)
+            avail = left if avail is None else min(avail, left)
+        break
+    return avail
+
+
+def reference_replicas(ntotal2, cores, avail):
+    """How many single-threaded replicas of the reference step run side by side: one per
+    core, as many as fit in 60% of the available memory at the measured footprint per
+    particle slot, at least one."""
+    n = max(1, cores)
+    if avail is not None:
+        per = REF_BYTES_FIXED + REF_BYTES_PER_PARTICLE * ntotal2
+        n = min(n, int(0.6 * avail) // per)
+    return max(1, n)
+
+
+def _ref_replica(dx, warm, steps, barrier, q):
+    """One realisation of the workload on one core (a spawned process): warm-up steps,
+    then the timed steps, started together with the other replicas at the barrier."""
+    try:
+        import orc
+        prob = workload(dx)
+        ctx = orc.context(prob.params_copy())
+        ctx.upload_problem(prob)
+        t = ctx.step(warm, 0.0) if warm else 0.0
+        barrier.wait(timeout=1800)
+        w0 = time.perf_counter()
+        ctx.step(steps, t)
+        q.put(("ok", time.perf_counter() - w0, prob.nnode + prob.nstress))
+    except BaseException as e:  # reported to the parent, which fails the run
+        barrier.abort()
+        q.put(("error", repr(e), 0))
+
+
 def run_reference(args):
     """The reference's CPU implementation of the step on the same workload as the GPU arm:
     the oracle (the C restatement of the reference's single-threaded Fortran step; no
-    Fortran compiler exists on either machine) on the full slope, one host thread, as the
-    reference runs.  A step takes about a minute there, so the timed steps are bounded:
-    min(warmup, 1) untimed and min(steps, 2) timed."""
+    Fortran compiler exists on either machine) on the full slope.  The step is single-
+    threaded, so the host's cores are used as independent replicas of the workload, one
+    per core (bounded by the host memory), which start their timed steps together; the
+    value is all replicas' particle-steps over the slowest replica's time.  A step takes
+    about a minute, so the timed steps are bounded: min(warmup, 1) untimed and
+    min(steps, 2) timed."""
     rank, world, dist = dist_init("gloo")
     if rank != 0:
         return
+    import multiprocessing as mp
     import orc
     orc.build()
     import sps_gb300
     sps_gb300.build_host()
     prob = workload(args.dx)
-    ctx = orc.context(prob.params_copy())
-    ctx.upload_problem(prob)
-    warm, steps = min(args.warmup, 1), max(1, min(args.steps, 2))
-    t = ctx.step(warm, 0.0) if warm else 0.0
-    w0 = time.perf_counter()
-    t = ctx.step(steps, t)
-    el = time.perf_counter() - w0
     n = prob.nnode + prob.nstress
-    v = n * steps / el
-    sample = ("oracle (C restatement of the reference step, 1 thread, as the single-threaded "
-              "reference runs) on the full workload: %d untimed + %d timed steps in %.1f s"
-              % (warm, steps, el))
+    name = workload_name(prob, args.dx)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    reps = args.ref_replicas or reference_replicas(prob.ntotal2, cores or 1, host_memory_available())
+    del prob
+    warm, steps = min(args.warmup, 1), max(1, min(args.steps, 2))
+    ctx = mp.get_context("spawn")
+    barrier, q = ctx.Barrier(reps), ctx.Queue()
+    procs = [ctx.Process(target=_ref_replica, args=(args.dx, warm, steps, barrier, q))
+             for _ in range(reps)]
+    for p in procs:
+        p.start()
+    res, deadline = [], time.time() + 3600
+    try:
+        while len(res) < reps:
+            try:
+                res.append(q.get(timeout=5))
+            except queue.Empty:
+                # a replica that ended without reporting (killed, crashed) fails the run
+                dead = [p.exitcode for p in procs if p.exitcode not in (None, 0)]
+                if dead or time.time() > deadline:
+                    barrier.abort()
+                    raise RuntimeError("reference replica ended without a result (exit codes "
+                                       "%s)" % dead if dead else "reference replicas timed out")
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.terminate()
+    bad = [r[1] for r in res if r[0] != "ok"]
+    if bad:
+        raise RuntimeError("reference replica failed: " + bad[0])
+    el = max(r[1] for r in res)
+    v = reps * n * steps / el
+    sample = ("oracle (C restatement of the reference step; single-threaded, as the reference "
+              "runs) on the same workload, %d replica(s) on %d host core(s), one each: %d untimed "
+              "+ %d timed steps per replica, slowest replica %.3g s"
+              % (reps, cores, warm, steps, el))
     line = {
         "metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": round(1e3 * el / steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (generated slope geometry, no dataset)", "impl": "reference",
-        "config": {"workload": workload_name(prob, args.dx),
+        "config": {"workload": name,
                    "precision": "fp64 (reference mixed precision)",
-                   "particles": n, "same_as_gpu_arm": True,
+                   "particles": n, "same_as_gpu_arm": True, "replicas": reps,
                    "bounded": "steps limited to min(K, 2) after min(W, 1) warm-up (about a "
                               "minute per step on one core)"},
-        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": 1,
+        "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": reps,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
