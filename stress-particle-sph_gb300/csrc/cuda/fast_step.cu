@@ -646,7 +646,10 @@ __device__ __forceinline__ void fsp_tail_one(const Dev& D, int stage, int i) {
   }
 }
 
-// The stress-point tail, each block striding over block-sized chunks of the stress-points.
+// The stress-point tail of an RK4 stage (2_SPH_main_2018.f90:727-777): plastic_terms and
+// drucker_prager (3_SPH_material_2018.f90:1884-2062), the Jaumann spin
+// (2_SPH_main_2018.f90:1021-1034), the rates and their RK accumulation.  Each block strides
+// over block-sized chunks of the stress-points.
 // With the surrogate installed both variants are launched: the one the gate selects for
 // this step runs, the other's blocks return at once.  The variant with the network runs
 // over at most kTailBlocks blocks (a few SM-fulls, so that the launch costs little when the

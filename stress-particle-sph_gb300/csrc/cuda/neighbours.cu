@@ -305,6 +305,8 @@ __device__ __forceinline__ int cell_index(const Grid& g, double x, double y) {
   return g.ndiv[0] * (iy - 1) + (ix - 1);
 }
 
+// Task 2 of grid_find_NEW (2_SPH_main_2018.f90:1275-1286): the cell of every particle
+// inside the domain, and the cells' counts
 __global__ void k_cell_count(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N2) return;
@@ -338,6 +340,8 @@ __global__ void k_cell_count(Dev D) {
   atomicAdd(&D.cell_cnt[c], 1);
 }
 
+// the cells' particle lists (list_picell, 2_SPH_main_2018.f90:1288-1305), filled in any
+// order here and put in ascending id order by k_cell_sort
 __global__ void k_cell_fill(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N2) return;
@@ -346,7 +350,8 @@ __global__ void k_cell_fill(Dev D) {
   D.spos[D.cell_start[c] + slot] = i;  // spos used as scratch here
 }
 
-// per cell: sort the ids ascending (list_picell order), write sorted[] and spos[]
+// per cell: sort the ids ascending (list_picell order, 2_SPH_main_2018.f90:1299-1305),
+// write sorted[] and spos[]
 __global__ void k_cell_sort(Dev D) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   const GridTotal g = *D.gtot;
@@ -633,6 +638,9 @@ __device__ __forceinline__ int half_phase1(const Dev& D, int s, int& a, int& ta,
   return k;
 }
 
+// Task 3 of grid_find_NEW (2_SPH_main_2018.f90:1307-1403): the half-stencil search
+// (:1322-1341), the exact test (:1345-1353), kernel (:1371, :1440-1538) and the pair types
+// of Pint_Update (3_SPH_material_2018.f90:1574-1634).
 // Phase 2 turns each accepted (partner, stencil cell) into the finished entry: the
 // partner's id with the pair type in its top bits (kHalfIdMask), so that the list build
 // needs neither the partner's id nor its type from memory, and W, dW/dx, dW/dy; within one
@@ -732,6 +740,9 @@ __device__ __forceinline__ bool gather_accept(const Dev& D, int a, float xa, flo
   return true;
 }
 
+// FP32 form: Task 3 of grid_find_NEW (2_SPH_main_2018.f90:1307-1403), kernel (:1440-1538)
+// and Pint_Update (3_SPH_material_2018.f90:1574-1634) per target, gathering its entries
+// from the 3 x 3 cell stencil directly in creation order.
 // KIND 1: the stress-point targets tgt[0..n), 2: the node targets.  SAME: the same-kind
 // entries are written too (the steps that read them: XSPH, artificial viscosity or stress,
 // the FP32 free-surface detection); without them degS holds 0 unless the outside approach
@@ -1102,6 +1113,9 @@ __device__ __forceinline__ void lists_target(const Dev& D, int s, int4& pendC, i
   D.degS[col] = nS;
 }
 
+// every target's cross and same lists, built from the creators' half lists in the walk
+// order of the reference's pair linked list (its reuse and relinking,
+// 2_SPH_main_2018.f90:1309-1401).
 // dynamic shared memory: 2 x blockDim int4, the waiting even entries of each thread's two
 // lists (in registers they cost the list build, which waits on its gathers, an eighth of
 // its resident warps)

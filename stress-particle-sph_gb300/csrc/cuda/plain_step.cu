@@ -163,6 +163,8 @@ __device__ __forceinline__ bool bound_term(const Dev& D, const Real& M, int i, i
   return true;
 }
 
+// boundary_forces (2_SPH_main_2018.f90:1039-1165), test 2: the wall force on every node
+// from the innermost dummy row, once per step (positions are frozen within a step)
 __global__ void k_bound(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NN) return;
@@ -226,6 +228,8 @@ __global__ void k_bound(Dev D) {
   }
 }
 
+// start of RK4 stage i (2_SPH_main_2018.f90:700-716): stage velocity and stress,
+// density_update (:807-821) and h with sle 2, adapt_stress2 and the fixed BCs
 __global__ void k_stage_begin(Dev D, int stage) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
@@ -356,6 +360,8 @@ __global__ void k_interp(Dev D, const int32_t* __restrict__ tgt, int ntgt) {
   }
 }
 
+// node density of stress_point_update with cont_density (2_SPH_main_2018.f90:403-482),
+// applied after every node has read the stress-points
 __global__ void k_node_rho(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < D.NN) {
@@ -660,6 +666,9 @@ __global__ void k_derivs(Dev D, int stage, const int32_t* __restrict__ tgt, int 
   }
 }
 
+// end of RK4 (2_SPH_main_2018.f90:784-799): velocity and stress from the accumulated
+// rates, adapt_stress2, BCs, density and h, Ddev_strn; update_strain
+// (3_SPH_material_2018.f90:1864-1880)
 __global__ void k_rk_final(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
@@ -706,6 +715,8 @@ __global__ void k_rk_final(Dev D) {
   if (D.fast) write_records(D, i, i >= D.NN || D.cont_density, vx, vy, a, b, c, d);
 }
 
+// position update of time_integration without XSPH (2_SPH_main_2018.f90:145-146):
+// x = x0 + vel_half dt with vel_half = 0.5 (v0 + v) rounded to FP32
 __global__ void k_trapezoid(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NT) return;
@@ -749,6 +760,8 @@ __global__ void k_xsph(Dev D) {
   if (mark) D.bc_or_not[t] = 3;
 }
 
+// displ = x - x00 (2_SPH_main_2018.f90:166-171; stress-points follow the nodes in
+// standard SPH), or accumulated from the velocities when positions are frozen (:180)
 __global__ void k_displ(Dev D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.NN) return;

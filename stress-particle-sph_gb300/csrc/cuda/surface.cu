@@ -7,9 +7,12 @@
 // linked list: a particle merges its two neighbour lists by their walk-order keys (written
 // by k_lists), which restores that order.  Step 3 (is a neighbour inside the particle's scan
 // region?) does not depend on the order.
-//   k_fs_normal0  steps 1-2: renormalisation matrix, kernel-gradient sums, first normal
-//   k_fs_scan     step 3 + the bc_or_not update: subset (1 surface, 2 inside), f_int
-//   k_fs_normal   step 4: normals of surface particles from their surface neighbours
+//   k_fs_normal0  steps 1-2 (:1180-1253): renormalisation matrix, kernel-gradient sums,
+//                 first normal
+//   k_fs_scan     step 3 (:1254-1369) + the bc_or_not update: subset (1 surface,
+//                 2 inside), f_int
+//   k_fs_normal   step 4 (:1370-1430): normals of surface particles from their surface
+//                 neighbours
 #include <cuda_runtime.h>
 
 #include "ctx.cuh"
@@ -241,9 +244,9 @@ __device__ __forceinline__ void walk_123_f32(const Dev& D, int col, F&& f) {
   }
 }
 
-// steps 1-3 for one particle: its first normal from the kernel-gradient sums, then, with
-// that normal (the scan region needs the particle's own normal only), whether a neighbour
-// lies in its scan region
+// steps 1-3 (3_SPH_material_2018.f90:1180-1369) for one particle: its first normal from
+// the kernel-gradient sums, then, with that normal (the scan region needs the particle's
+// own normal only), whether a neighbour lies in its scan region
 __global__ void k_fs_normal_scan_f32(Dev D) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
@@ -302,6 +305,8 @@ __global__ void k_fs_normal_scan_f32(Dev D) {
   D.subset[t] = (int8_t)sub;
 }
 
+// step 4 (3_SPH_material_2018.f90:1370-1430) of the FP32 detection: the normals of the
+// surface particles from their surface neighbours
 __global__ void k_fs_normal_f32(Dev D) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.N2) return;
