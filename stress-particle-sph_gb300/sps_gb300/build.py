@@ -2,6 +2,7 @@
 
 libsps_gb300.so  -- CUDA kernels for sm_103a + the C-ABI of include/sps.h
 libsph_host.so   -- host-side set-up library of include/sph_host.h
+sps_run          -- the reference's main program over the C-ABI (a driver executable)
 
 The FP64 plain kernels are compiled with -fmad=false and all host code with
 -ffp-contract=off: the reference (gfortran -O3 on x86-64) never fuses a multiply with an
@@ -97,5 +98,19 @@ def build_cuda(force=False, verbose=False):
     return out
 
 
+def build_driver(force=False):
+    """sps_run: the reference's main program over the C-ABI (csrc/host/sps_run.cpp), linked
+    against the two libraries beside it."""
+    src = os.path.join(CSRC, "host", "sps_run.cpp")
+    out = lib_path("sps_run")
+    libs = [lib_path("libsps_gb300.so"), lib_path("libsph_host.so")]
+    if not force and _newer(out, [src] + libs + _headers()):
+        return out
+    _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I" + INCLUDE, "-o", out,
+          src, "-L" + LIB_DIR, "-lsps_gb300", "-lsph_host", "-Wl,-rpath,$ORIGIN"])
+    return out
+
+
 def build_all(force=False, verbose=False):
-    return build_host(force), build_cuda(force, verbose)
+    host, cuda = build_host(force), build_cuda(force, verbose)
+    return host, cuda, build_driver(force)
