@@ -106,11 +106,24 @@ def build_driver(force=False):
     libs = [lib_path("libsps_gb300.so"), lib_path("libsph_host.so")]
     if not force and _newer(out, [src] + libs + _headers()):
         return out
+    # the linker resolves libsps_gb300.so's own dependency (the CUDA runtime) in the
+    # toolkit's library directory
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(NVCC)), "lib64")
     _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I" + INCLUDE, "-o", out,
-          src, "-L" + LIB_DIR, "-lsps_gb300", "-lsph_host", "-Wl,-rpath,$ORIGIN"])
+          src, "-L" + LIB_DIR, "-lsps_gb300", "-lsph_host", "-Wl,-rpath,$ORIGIN",
+          "-Wl,-rpath-link," + cuda_lib])
     return out
 
 
 def build_all(force=False, verbose=False):
+    """The two libraries, then the driver.  The libraries are the product: a driver that
+    fails to link is reported on stderr and does not stop their build (build_driver itself
+    raises, and its test calls it directly)."""
     host, cuda = build_host(force), build_cuda(force, verbose)
-    return host, cuda, build_driver(force)
+    try:
+        driver = build_driver(force)
+    except RuntimeError as e:
+        import sys
+        print("sps_gb300: the sps_run driver was not built: %s" % e, file=sys.stderr)
+        driver = None
+    return host, cuda, driver
